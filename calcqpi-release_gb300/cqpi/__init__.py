@@ -1,0 +1,227 @@
+"""Python binding of libcqpi.so (the engine's C ABI, include/cqpi.h) via ctypes.
+
+This is a thin wrapper for tests, the benchmark and the fitting harness; the drop-in
+product is the C ABI itself and the calcqpi CLI.  Every call goes to the CUDA library;
+there is no CPU fallback: if the library is missing or no GPU is visible, the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "_build", "libcqpi.so")
+
+OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_DOMAIN, ERR_SINGULAR, ERR_STATE, ERR_NOT_SUPPORTED, ERR_NO_DEVICE = range(9)
+PREC_FP64, PREC_MIXED = 0, 1
+
+EXPORTED = [
+    "cqpi_create", "cqpi_destroy", "cqpi_last_error", "cqpi_status_string", "cqpi_version",
+    "cqpi_set_orbitals", "cqpi_set_scattering", "cqpi_set_impurities", "cqpi_solve_bands", "cqpi_run",
+    "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
+    "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times",
+]
+
+
+class CqpiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cqpi status {code}: {msg}")
+        self.code = code
+
+
+class _Model(ctypes.Structure):
+    _fields_ = [("bands", ctypes.c_int32), ("scmaxbands", ctypes.c_int32), ("efermi", ctypes.c_double),
+                ("nhops", ctypes.c_int64), ("R", ctypes.c_void_p), ("orb", ctypes.c_void_p),
+                ("t", ctypes.c_void_p), ("anti", ctypes.c_void_p)]
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("lattice", ctypes.c_int32), ("kpoints", ctypes.c_int32), ("oversamp", ctypes.c_int32),
+                ("window", ctypes.c_int32), ("maxband", ctypes.c_int32), ("spin", ctypes.c_int32),
+                ("eta", ctypes.c_double), ("precision", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load():
+    """Load libcqpi.so (build it first with cqpi_build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libcqpi.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    P, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    L.cqpi_create.argtypes = [ctypes.POINTER(_Model), ctypes.POINTER(_Params), ctypes.POINTER(P)]
+    L.cqpi_destroy.argtypes = [P]
+    L.cqpi_last_error.argtypes = [P]
+    L.cqpi_last_error.restype = ctypes.c_char_p
+    L.cqpi_status_string.argtypes = [ctypes.c_int]
+    L.cqpi_status_string.restype = ctypes.c_char_p
+    L.cqpi_version.restype = ctypes.c_char_p
+    L.cqpi_set_orbitals.argtypes = [P, P, i32, i32, P]
+    L.cqpi_set_scattering.argtypes = [P, P]
+    L.cqpi_set_impurities.argtypes = [P, P, i32]
+    L.cqpi_solve_bands.argtypes = [P]
+    L.cqpi_run.argtypes = [P, P, i32, P, P, i32]
+    L.cqpi_wannierldos.argtypes = [P, P, P]
+    L.cqpi_retrieve_result.argtypes = [P, P]
+    L.cqpi_get_bands.argtypes = [P, P, P]
+    L.cqpi_get_greens_box.argtypes = [P, dbl, P, ctypes.POINTER(i32)]
+    L.cqpi_get_tmatrix.argtypes = [P, dbl, P]
+    L.cqpi_get_stream.argtypes = [P, ctypes.POINTER(P)]
+    L.cqpi_synchronize.argtypes = [P]
+    L.cqpi_kernel_launches.argtypes = [P, ctypes.POINTER(i64)]
+    L.cqpi_stage_times.argtypes = [P, P]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Engine:
+    """One engine handle: a model, the run parameters, the eigen cache and device buffers."""
+
+    def __init__(self, model, lattice, kpoints, oversamp, window, eta, maxband=None, spin=False,
+                 precision=PREC_FP64):
+        L = load()
+        self.bands = int(model.bands)
+        self.lattice, self.kpoints, self.oversamp, self.window = int(lattice), int(kpoints), int(oversamp), int(window)
+        self.maxband = self.bands if maxband is None else int(maxband)
+        self.spin = bool(spin)
+        self.wn = self.lattice * self.oversamp
+        self.side = (2 * self.window + 1) * self.oversamp
+        self.nimp = 1
+        self._R = np.ascontiguousarray(model.R, np.int32)
+        self._orb = np.ascontiguousarray(model.orb, np.int32)
+        self._t = np.ascontiguousarray(np.asarray(model.t, np.complex128).view(np.float64))
+        self._anti = np.ascontiguousarray(model.anti, np.uint8)
+        m = _Model(self.bands, int(getattr(model, "scmaxbands", self.bands)), float(getattr(model, "efermi", 0.0)),
+                   len(model.t), _ptr(self._R), _ptr(self._orb), _ptr(self._t), _ptr(self._anti))
+        p = _Params(self.lattice, self.kpoints, self.oversamp, self.window, self.maxband, int(self.spin), float(eta),
+                    int(precision))
+        h = ctypes.c_void_p()
+        rc = L.cqpi_create(ctypes.byref(m), ctypes.byref(p), ctypes.byref(h))
+        if rc != OK:
+            raise CqpiError(rc, L.cqpi_status_string(rc).decode())
+        self._h = h
+        self._L = L
+
+    def _check(self, rc):
+        if rc != OK:
+            raise CqpiError(rc, self._L.cqpi_last_error(self._h).decode() or self._L.cqpi_status_string(rc).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.cqpi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- inputs
+    def set_orbitals(self, wf, is_zero=None):
+        wf = np.ascontiguousarray(wf, np.float64)
+        z = None if is_zero is None else np.ascontiguousarray(is_zero, np.uint8)
+        self._check(self._L.cqpi_set_orbitals(self._h, _ptr(wf), wf.shape[0], wf.shape[1], _ptr(z)))
+
+    def set_scattering(self, vscat):
+        v = np.ascontiguousarray(np.asarray(vscat, np.complex128).view(np.float64))
+        self._check(self._L.cqpi_set_scattering(self._h, _ptr(v)))
+        self.nimp = 1
+
+    def set_impurities(self, V):
+        V = np.ascontiguousarray(np.asarray(V, np.complex128).reshape(-1, self.bands, self.bands))
+        self._check(self._L.cqpi_set_impurities(self._h, _ptr(V.view(np.float64)), V.shape[0]))
+        self.nimp = V.shape[0]
+
+    # -- compute
+    def solve_bands(self):
+        self._check(self._L.cqpi_solve_bands(self._h))
+
+    def run(self, energies, f32=True, f64=False):
+        """Host maps [nE][nimp][wn][wn] (float32 and/or float64)."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        shape = (len(e), self.nimp, self.wn, self.wn)
+        o32 = np.empty(shape, np.float32) if f32 else None
+        o64 = np.empty(shape, np.float64) if f64 else None
+        self._check(self._L.cqpi_run(self._h, _ptr(e), len(e), _ptr(o32), _ptr(o64), 0))
+        if f32 and f64:
+            return o32, o64
+        return o32 if f32 else o64
+
+    def run_device(self, energies, ptr32=None, ptr64=None):
+        """Asynchronous run into device buffers (raw pointers, e.g. torch tensor.data_ptr())."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        self._check(self._L.cqpi_run(self._h, _ptr(e), len(e), ptr32, ptr64, 1))
+
+    # -- narrow seam
+    def wannierldos(self, T, g0r):
+        T = np.ascontiguousarray(np.asarray(T, np.complex128))
+        g = np.ascontiguousarray(np.asarray(g0r, np.complex128))
+        self._check(self._L.cqpi_wannierldos(self._h, _ptr(T.view(np.float64)), _ptr(g.view(np.float64))))
+
+    def retrieve_result(self):
+        out = np.empty((self.wn, self.wn), np.float64)
+        self._check(self._L.cqpi_retrieve_result(self._h, _ptr(out)))
+        return out
+
+    # -- stage access
+    def get_bands(self):
+        nk = self.kpoints ** 2
+        ev = np.empty((nk, self.bands), np.float64)
+        U = np.empty((nk, self.bands, self.bands), np.complex128)
+        self._check(self._L.cqpi_get_bands(self._h, _ptr(ev), _ptr(U.view(np.float64))))
+        return ev, U
+
+    def greens_box(self, energy):
+        rb = ctypes.c_int32()
+        self._check(self._L.cqpi_get_greens_box(self._h, float(energy), None, ctypes.byref(rb)))
+        nb = 2 * rb.value + 1
+        box = np.empty((nb, nb, self.bands, self.bands), np.complex128)
+        self._check(self._L.cqpi_get_greens_box(self._h, float(energy), _ptr(box.view(np.float64)), ctypes.byref(rb)))
+        return box, rb.value
+
+    def tmatrix(self, energy):
+        T = np.empty((self.bands, self.bands), np.complex128)
+        self._check(self._L.cqpi_get_tmatrix(self._h, float(energy), _ptr(T.view(np.float64))))
+        return T
+
+    # -- runtime
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(self._L.cqpi_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def synchronize(self):
+        self._check(self._L.cqpi_synchronize(self._h))
+
+    def kernel_launches(self) -> int:
+        c = ctypes.c_int64()
+        self._check(self._L.cqpi_kernel_launches(self._h, ctypes.byref(c)))
+        return c.value
+
+    def stage_times(self):
+        t = np.zeros(5, np.float32)
+        self._check(self._L.cqpi_stage_times(self._h, _ptr(t)))
+        return dict(zip(["bands", "greens", "tmatrix", "ldos", "total"], t.tolist()))

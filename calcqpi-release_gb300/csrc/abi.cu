@@ -1,0 +1,601 @@
+// abi.cu -- the extern "C" boundary of libcqpi.so (declared in include/cqpi.h).
+//
+// Owns every device buffer of a handle, validates sizes against the reference's
+// index domain, converts the reference's inputs (hopping list, orbital cache,
+// scattering vector) into the engine's HBM layout and drives the per-energy
+// stages in batches of energies on the handle's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <utility>
+
+#include "cqpi_internal.h"
+
+using namespace cqpi;
+
+namespace {
+
+struct CudaError {
+    cudaError_t code;
+    const char *what;
+};
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) throw CudaError{e_, #call};         \
+    } while (0)
+
+int fail(cqpi_handle *h, int code, const std::string &msg)
+{
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_fail(cqpi_handle *h, const CudaError &e)
+{
+    char buf[512];
+    snprintf(buf, sizeof buf, "CUDA error %d (%s) in %s", (int)e.code, cudaGetErrorString(e.code), e.what);
+    if (h) h->err = buf;
+    return (e.code == cudaErrorMemoryAllocation) ? CQPI_ERR_ALLOC : CQPI_ERR_CUDA;
+}
+
+template <class T>
+void dalloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc((void **)p, sizeof(T) * count));
+}
+
+template <class T>
+void dfree(T *&p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void free_workspace(cqpi_handle *h)
+{
+    dfree(h->ws.g0k);
+    dfree(h->ws.half);
+    dfree(h->ws.box);
+    dfree(h->ws.T);
+    dfree(h->ws.term1);
+    dfree(h->ws.energies);
+    dfree(h->ws.g0k32);
+    dfree(h->ws.half32);
+    h->ws.ebatch = 0;
+}
+
+size_t bytes_per_energy(const cqpi_handle *h)
+{
+    const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
+    return 16 * (bb * nk + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
+}
+
+void ensure_workspace(cqpi_handle *h, int ebatch)
+{
+    if (h->ws.ebatch >= ebatch) return;
+    free_workspace(h);
+    const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
+    dalloc(&h->ws.g0k, ebatch * bb * nk);
+    dalloc(&h->ws.half, ebatch * bb * (size_t)h->kp * h->NB);
+    dalloc(&h->ws.box, ebatch * (size_t)h->NB * h->NB * bb);
+    dalloc(&h->ws.T, ebatch * (size_t)std::max(h->nimp, 1) * bb);
+    dalloc(&h->ws.term1, ebatch * (size_t)h->Q);
+    dalloc(&h->ws.energies, ebatch);
+    h->ws.ebatch = ebatch;
+}
+
+int choose_batch(const cqpi_handle *h, int nE)
+{
+    const size_t budget = (size_t)16 << 30;   // workspace ceiling: 16 GiB of the 288 GB HBM
+    size_t per = bytes_per_energy(h) + (size_t)h->nimp * h->wn * h->wn * 12;
+    int eb = (int)std::max<size_t>(1, budget / std::max<size_t>(per, 1));
+    eb = std::min(eb, 32);
+    return std::max(1, std::min(eb, nE));
+}
+
+void check_launch()
+{
+    CK(cudaGetLastError());
+}
+
+int read_status(cqpi_handle *h)
+{
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (st) {
+        int zero = 0;
+        CK(cudaMemcpyAsync(h->d_status, &zero, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    return st;
+}
+
+void do_bands(cqpi_handle *h)
+{
+    launch_bands(h);
+    check_launch();
+    h->bands_ready = true;
+}
+
+// G0(k) -> G0(R) box -> T -> term1 for ne energies already in ws.energies.
+void do_greens(cqpi_handle *h, int ne)
+{
+    launch_greens_k(h, ne, h->ws.energies);
+    check_launch();
+    launch_fft(h, ne);
+    check_launch();
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cqpi_version(void) { return "cqpi-gb300 0.1 (sm_103a)"; }
+
+const char *cqpi_status_string(int s)
+{
+    switch (s) {
+    case CQPI_OK: return "ok";
+    case CQPI_ERR_ARG: return "invalid argument";
+    case CQPI_ERR_CUDA: return "CUDA error";
+    case CQPI_ERR_ALLOC: return "allocation failed";
+    case CQPI_ERR_DOMAIN: return "sizes outside the reference's index domain";
+    case CQPI_ERR_SINGULAR: return "1 - V G0(0) is singular";
+    case CQPI_ERR_STATE: return "call order violated";
+    case CQPI_ERR_NOT_SUPPORTED: return "not supported";
+    case CQPI_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char *cqpi_last_error(const cqpi_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out)
+{
+    if (!out) return CQPI_ERR_ARG;
+    *out = nullptr;
+    if (!model || !p) return CQPI_ERR_ARG;
+    const int b = model->bands;
+    if (b < 1 || b > CQPI_MAX_BANDS) return CQPI_ERR_ARG;
+    if (model->nhops < 0 || (model->nhops > 0 && (!model->R || !model->orb || !model->t))) return CQPI_ERR_ARG;
+    if (p->lattice < 1 || p->kpoints < 1 || p->oversamp < 1 || p->window < 0) return CQPI_ERR_ARG;
+    if (p->kpoints > 8192) return CQPI_ERR_NOT_SUPPORTED;
+    if (p->maxband < 1 || p->maxband > b) return CQPI_ERR_ARG;
+    if (!(p->eta == p->eta)) return CQPI_ERR_ARG;   // NaN
+    if (p->precision != CQPI_PREC_FP64 && p->precision != CQPI_PREC_MIXED) return CQPI_ERR_ARG;
+    for (int64_t i = 0; i < model->nhops; i++) {
+        if (model->orb[2 * i] < 0 || model->orb[2 * i] >= b || model->orb[2 * i + 1] < 0 || model->orb[2 * i + 1] >= b)
+            return CQPI_ERR_ARG;
+    }
+    // The reference forms G0 indices with unsigned arithmetic, e.g.
+    // (kpoints + ipos + nni2) % kpoints (src/qpi.cc:901,907,921).  They equal the
+    // mathematical R mod kp when lattice/2 + window <= kp and 2*window <= kp, and
+    // always when kp is a power of two (2^64 is then a multiple of kp).
+    const int n2 = p->lattice >> 1;
+    const bool pow2 = (p->kpoints & (p->kpoints - 1)) == 0;
+    if (!pow2 && (n2 + p->window > p->kpoints || 2 * p->window > p->kpoints)) return CQPI_ERR_DOMAIN;
+    // Wide output indices are 32-bit inside kernels.
+    const long long wn = (long long)p->lattice * p->oversamp;
+    if (wn > 46340 || (long long)p->kpoints * p->kpoints > (1LL << 31)) return CQPI_ERR_NOT_SUPPORTED;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return CQPI_ERR_NO_DEVICE;
+    }
+
+    cqpi_handle *h = new (std::nothrow) cqpi_handle();
+    if (!h) return CQPI_ERR_ALLOC;
+    try {
+        CK(cudaGetDevice(&h->device));
+        CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        for (auto &e : h->ev) CK(cudaEventCreate(&e));
+        h->b = b;
+        h->scmax = model->scmaxbands;
+        h->efermi = model->efermi;
+        h->n = p->lattice;
+        h->kp = p->kpoints;
+        h->os = p->oversamp;
+        h->w = p->window;
+        h->m = p->maxband;
+        h->spin = p->spin ? 1 : 0;
+        h->eta = p->eta;
+        h->precision = p->precision;
+        h->Rb = std::max(n2 + h->w, 2 * h->w);
+        h->NB = 2 * h->Rb + 1;
+        h->W = (2 * h->w + 1) * (2 * h->w + 1);
+        h->Q = h->os * h->os;
+        h->wn = (int)wn;
+        if (h->spin) {
+            // spin mode pairs orbitals inside [0, m/2) and [m/2, 2*(m/2)) (src/qpi.cc:924-940)
+            h->nblk = 2;
+            h->mb = h->m >> 1;
+            h->blk_start[0] = 0;
+            h->blk_start[1] = h->mb;
+        } else {
+            h->nblk = 1;
+            h->mb = h->m;
+        }
+
+        // unique in-plane R with summed normal / conjugated (anti) hopping matrices; kz = 0
+        std::map<std::pair<int, int>, int> idx;
+        std::vector<int32_t> Rv;
+        std::vector<double> tn, ta;
+        const size_t bb = (size_t)b * b;
+        for (int64_t i = 0; i < model->nhops; i++) {
+            auto key = std::make_pair(model->R[3 * i], model->R[3 * i + 1]);
+            auto it = idx.find(key);
+            int r;
+            if (it == idx.end()) {
+                r = (int)idx.size();
+                idx[key] = r;
+                Rv.push_back(key.first);
+                Rv.push_back(key.second);
+                tn.resize(tn.size() + 2 * bb, 0.0);
+                ta.resize(ta.size() + 2 * bb, 0.0);
+            } else {
+                r = it->second;
+            }
+            const size_t e = (size_t)r * bb + (size_t)model->orb[2 * i] * b + model->orb[2 * i + 1];
+            std::vector<double> &dst = (model->anti && model->anti[i]) ? ta : tn;
+            dst[2 * e] += model->t[2 * i];
+            dst[2 * e + 1] += model->t[2 * i + 1];
+        }
+        h->nR = (int)idx.size();
+        dalloc(&h->d_R, Rv.size());
+        dalloc(&h->d_tn, tn.size());
+        dalloc(&h->d_ta, ta.size());
+        if (h->nR) {
+            CK(cudaMemcpy(h->d_R, Rv.data(), sizeof(int32_t) * Rv.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(h->d_tn, tn.data(), sizeof(double) * tn.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(h->d_ta, ta.data(), sizeof(double) * ta.size(), cudaMemcpyHostToDevice));
+        }
+        // twiddles e^{+2 pi i t / kp}
+        std::vector<double2> tw(h->kp);
+        for (int t = 0; t < h->kp; t++) {
+            double s, c;
+            sincospi(2.0 * t / h->kp, &s, &c);
+            tw[t] = make_double2(c, s);
+        }
+        dalloc(&h->d_tw, h->kp);
+        CK(cudaMemcpy(h->d_tw, tw.data(), sizeof(double2) * h->kp, cudaMemcpyHostToDevice));
+        const size_t nk = (size_t)h->kp * h->kp;
+        dalloc(&h->d_eval, nk * b);
+        dalloc(&h->d_evec, nk * bb);
+        dalloc(&h->d_status, 1);
+        CK(cudaMemset(h->d_status, 0, sizeof(int)));
+        // default scattering: phase (1,0) on every band (src/qpi.h:99)
+        h->nimp = 1;
+        std::vector<double2> V(bb, make_double2(0.0, 0.0));
+        for (int i = 0; i < b; i++) V[(size_t)i * b + i] = make_double2(1.0, 0.0);
+        dalloc(&h->d_V, bb);
+        CK(cudaMemcpy(h->d_V, V.data(), sizeof(double2) * bb, cudaMemcpyHostToDevice));
+        // the transform kernels keep whole rows / column tiles in shared memory
+        CK(configure_fft(h));
+    } catch (const CudaError &e) {
+        int rc = cuda_fail(h, e);
+        cqpi_destroy(h);
+        return rc;
+    } catch (const std::bad_alloc &) {
+        cqpi_destroy(h);
+        return CQPI_ERR_ALLOC;
+    }
+    *out = h;
+    return CQPI_OK;
+}
+
+int cqpi_destroy(cqpi_handle *h)
+{
+    if (!h) return CQPI_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_workspace(h);
+    dfree(h->d_R);
+    dfree(h->d_tn);
+    dfree(h->d_ta);
+    dfree(h->d_tw);
+    dfree(h->d_tw32);
+    dfree(h->d_eval);
+    dfree(h->d_evec);
+    dfree(h->d_phi);
+    dfree(h->d_V);
+    dfree(h->d_status);
+    dfree(h->d_seam_ldos);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    cudaGetLastError();
+    delete h;
+    return CQPI_OK;
+}
+
+int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t side, const uint8_t *is_zero)
+{
+    if (!h || !wf) return fail(h, CQPI_ERR_ARG, "null argument");
+    if (side != (2 * h->w + 1) * h->os) return fail(h, CQPI_ERR_ARG, "orbital side must be (2*window+1)*oversamp");
+    const int need = h->spin ? 2 * h->mb : h->m;
+    if (norb < need) return fail(h, CQPI_ERR_ARG, "fewer orbitals than maxband");
+    // phi[blk][q][d][ol] = wf[o](w*os + qx - dx*os, w*os + qy - dy*os)  (src/qpi.cc:912-918)
+    const int side1 = 2 * h->w + 1;
+    std::vector<double> phi((size_t)h->nblk * h->Q * h->W * h->mb, 0.0);
+    for (int blk = 0; blk < h->nblk; blk++)
+        for (int qx = 0; qx < h->os; qx++)
+            for (int qy = 0; qy < h->os; qy++)
+                for (int d = 0; d < h->W; d++) {
+                    const int dx = d / side1 - h->w, dy = d % side1 - h->w;
+                    const int ix = h->w * h->os + qx - dx * h->os, iy = h->w * h->os + qy - dy * h->os;
+                    for (int ol = 0; ol < h->mb; ol++) {
+                        const int o = h->blk_start[blk] + ol;
+                        double v = 0.0;
+                        if (!(is_zero && is_zero[o])) v = wf[((size_t)o * side + ix) * side + iy];
+                        phi[((((size_t)blk * h->Q) + qx * h->os + qy) * h->W + d) * h->mb + ol] = v;
+                    }
+                }
+    try {
+        dfree(h->d_phi);
+        dalloc(&h->d_phi, phi.size());
+        CK(cudaMemcpy(h->d_phi, phi.data(), sizeof(double) * phi.size(), cudaMemcpyHostToDevice));
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    h->orbitals_ready = true;
+    return CQPI_OK;
+}
+
+int cqpi_set_impurities(cqpi_handle *h, const double *V, int32_t nimp)
+{
+    if (!h || !V || nimp < 1) return fail(h, CQPI_ERR_ARG, "invalid impurity list");
+    const size_t bb = (size_t)h->b * h->b;
+    try {
+        dfree(h->d_V);
+        dalloc(&h->d_V, bb * nimp);
+        CK(cudaMemcpy(h->d_V, V, sizeof(double2) * bb * nimp, cudaMemcpyHostToDevice));
+        if (nimp > h->nimp) free_workspace(h);
+        h->nimp = nimp;
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_set_scattering(cqpi_handle *h, const double *vscat)
+{
+    if (!h || !vscat) return fail(h, CQPI_ERR_ARG, "null argument");
+    const int b = h->b;
+    std::vector<double> V((size_t)2 * b * b, 0.0);
+    for (int i = 0; i < b; i++) {
+        V[2 * ((size_t)i * b + i)] = vscat[2 * i];
+        V[2 * ((size_t)i * b + i) + 1] = vscat[2 * i + 1];
+    }
+    return cqpi_set_impurities(h, V.data(), 1);
+}
+
+int cqpi_solve_bands(cqpi_handle *h)
+{
+    if (!h) return CQPI_ERR_ARG;
+    try {
+        do_bands(h);
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, double *maps64, int32_t on_device)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (nE < 0 || (nE > 0 && !energies)) return fail(h, CQPI_ERR_ARG, "invalid energy list");
+    if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    if (nE == 0) return CQPI_OK;
+    const size_t mapn = (size_t)h->wn * h->wn;
+    const size_t per_e = (size_t)h->nimp * mapn;
+    float *stage32 = nullptr;
+    double *stage64 = nullptr;
+    try {
+        const int eb = choose_batch(h, nE);
+        ensure_workspace(h, eb);
+        if (!on_device) {
+            if (maps32) dalloc(&stage32, eb * per_e);
+            if (maps64) dalloc(&stage64, eb * per_e);
+        }
+        float tb = 0, tg = 0, tt = 0, tl = 0;
+        CK(cudaEventRecord(h->ev[0], h->stream));
+        if (!h->bands_ready) do_bands(h);
+        CK(cudaEventRecord(h->ev[1], h->stream));
+        CK(cudaEventSynchronize(h->ev[1]));
+        CK(cudaEventElapsedTime(&tb, h->ev[0], h->ev[1]));
+        for (int e0 = 0; e0 < nE; e0 += eb) {
+            const int ne = std::min(eb, nE - e0);
+            CK(cudaMemcpyAsync(h->ws.energies, energies + e0, sizeof(double) * ne, cudaMemcpyHostToDevice, h->stream));
+            CK(cudaEventRecord(h->ev[2], h->stream));
+            do_greens(h, ne);
+            CK(cudaEventRecord(h->ev[3], h->stream));
+            launch_tmatrix(h, ne);
+            check_launch();
+            launch_term1(h, ne);
+            check_launch();
+            CK(cudaEventRecord(h->ev[4], h->stream));
+            float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : stage32) : nullptr;
+            double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : stage64) : nullptr;
+            launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
+            check_launch();
+            CK(cudaEventRecord(h->ev[5], h->stream));
+            if (!on_device) {
+                if (maps32)
+                    CK(cudaMemcpyAsync(maps32 + (size_t)e0 * per_e, stage32, sizeof(float) * ne * per_e,
+                                       cudaMemcpyDeviceToHost, h->stream));
+                if (maps64)
+                    CK(cudaMemcpyAsync(maps64 + (size_t)e0 * per_e, stage64, sizeof(double) * ne * per_e,
+                                       cudaMemcpyDeviceToHost, h->stream));
+            }
+            CK(cudaEventSynchronize(h->ev[5]));
+            float a, c, d;
+            CK(cudaEventElapsedTime(&a, h->ev[2], h->ev[3]));
+            CK(cudaEventElapsedTime(&c, h->ev[3], h->ev[4]));
+            CK(cudaEventElapsedTime(&d, h->ev[4], h->ev[5]));
+            tg += a; tt += c; tl += d;
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        h->stage_ms[0] = tb; h->stage_ms[1] = tg; h->stage_ms[2] = tt; h->stage_ms[3] = tl;
+        h->stage_ms[4] = tb + tg + tt + tl;
+        dfree(stage32);
+        dfree(stage64);
+        if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
+    } catch (const CudaError &e) {
+        dfree(stage32);
+        dfree(stage64);
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_get_bands(cqpi_handle *h, double *eval, double *evec)
+{
+    if (!h) return CQPI_ERR_ARG;
+    const size_t nk = (size_t)h->kp * h->kp, b = h->b, bb = b * b;
+    try {
+        if (!h->bands_ready) do_bands(h);
+        CK(cudaStreamSynchronize(h->stream));
+        if (eval) {
+            std::vector<double> t(nk * b);
+            CK(cudaMemcpy(t.data(), h->d_eval, sizeof(double) * t.size(), cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < nk; k++)
+                for (size_t n = 0; n < b; n++) eval[k * b + n] = t[n * nk + k];
+        }
+        if (evec) {
+            std::vector<double2> t(nk * bb);
+            CK(cudaMemcpy(t.data(), h->d_evec, sizeof(double2) * t.size(), cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < nk; k++)
+                for (size_t e = 0; e < bb; e++) {
+                    evec[2 * (k * bb + e)] = t[e * nk + k].x;
+                    evec[2 * (k * bb + e) + 1] = t[e * nk + k].y;
+                }
+        }
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_get_greens_box(cqpi_handle *h, double energy, double *box, int32_t *rb)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (rb) *rb = h->Rb;
+    if (!box) return CQPI_OK;
+    try {
+        ensure_workspace(h, 1);
+        if (!h->bands_ready) do_bands(h);
+        CK(cudaMemcpyAsync(h->ws.energies, &energy, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        do_greens(h, 1);
+        CK(cudaMemcpyAsync(box, h->ws.box, sizeof(double2) * (size_t)h->NB * h->NB * h->b * h->b, cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_get_tmatrix(cqpi_handle *h, double energy, double *T)
+{
+    if (!h || !T) return CQPI_ERR_ARG;
+    try {
+        ensure_workspace(h, 1);
+        if (!h->bands_ready) do_bands(h);
+        CK(cudaMemcpyAsync(h->ws.energies, &energy, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        do_greens(h, 1);
+        launch_tmatrix(h, 1);
+        check_launch();
+        CK(cudaMemcpyAsync(T, h->ws.T, sizeof(double2) * h->b * h->b, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular");
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r)
+{
+    if (!h || !T || !g0r) return fail(h, CQPI_ERR_ARG, "null argument");
+    if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    const size_t bb = (size_t)h->b * h->b, kp = h->kp;
+    // pick the pruned box out of the full grid: box[R+Rb] = g0r[R mod kp]
+    std::vector<double2> box((size_t)h->NB * h->NB * bb);
+    for (int xb = 0; xb < h->NB; xb++) {
+        const size_t X = (size_t)(((xb - h->Rb) % h->kp + h->kp) % h->kp);
+        for (int yb = 0; yb < h->NB; yb++) {
+            const size_t Y = (size_t)(((yb - h->Rb) % h->kp + h->kp) % h->kp);
+            memcpy(&box[((size_t)xb * h->NB + yb) * bb], g0r + 2 * ((X * kp + Y) * bb), sizeof(double2) * bb);
+        }
+    }
+    try {
+        ensure_workspace(h, 1);
+        if (!h->d_seam_ldos) dalloc(&h->d_seam_ldos, (size_t)h->wn * h->wn);
+        CK(cudaMemcpyAsync(h->ws.box, box.data(), sizeof(double2) * box.size(), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->ws.T, T, sizeof(double2) * bb, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));   // 'box' is a pageable temporary
+        const int saved = h->nimp;
+        h->nimp = 1;
+        launch_term1(h, 1);
+        check_launch();
+        launch_ldos_fp64(h, 1, h->ws.box, h->ws.T, h->ws.term1, nullptr, h->d_seam_ldos);
+        h->nimp = saved;
+        check_launch();
+        h->seam_pending = true;
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_retrieve_result(cqpi_handle *h, double *ldos)
+{
+    if (!h || !ldos) return fail(h, CQPI_ERR_ARG, "null argument");
+    if (!h->seam_pending) return fail(h, CQPI_ERR_STATE, "cqpi_wannierldos has not been called");
+    try {
+        CK(cudaMemcpyAsync(ldos, h->d_seam_ldos, sizeof(double) * h->wn * h->wn, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_get_stream(cqpi_handle *h, void **stream)
+{
+    if (!h || !stream) return CQPI_ERR_ARG;
+    *stream = (void *)h->stream;
+    return CQPI_OK;
+}
+
+int cqpi_synchronize(cqpi_handle *h)
+{
+    if (!h) return CQPI_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, CudaError{e, "cudaStreamSynchronize"});
+    return CQPI_OK;
+}
+
+int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count)
+{
+    if (!h || !count) return CQPI_ERR_ARG;
+    *count = h->launches;
+    return CQPI_OK;
+}
+
+int cqpi_stage_times(const cqpi_handle *h, float *ms5)
+{
+    if (!h || !ms5) return CQPI_ERR_ARG;
+    for (int i = 0; i < 5; i++) ms5[i] = h->stage_ms[i];
+    return CQPI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+// cqpi_internal.h -- shared declarations of the GB300 continuum-LDOS engine.
+//
+// Data layout in HBM (one handle):
+//   bands     eval [b][nk] f64, evec [b*b][nk] f64x2 (o*b+n), nk = kp*kp, k = i*kp + j
+//   greens    g0k  [E][b*b][nk] complex (SoA planes, plane = o*b+a)
+//             half [E][b*b][kp][NB] complex: transform along j done, pruned to Y in box
+//             box  [E][NB][NB][b*b] complex: G0(R) for R in [-Rb, Rb]^2 (box index R+Rb)
+//   T         [E][nimp][b*b] f64x2
+//   term1     [E][os*os] f64 (site-independent part of the LDOS)
+//   phi       [nblk][os*os][W][mb] f64: phi_o(q,d) = wf[o](w*os+qx-dx*os, w*os+qy-dy*os)
+//   maps      [E][nimp][wn][wn] f32 and/or f64, x fastest
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/cqpi.h"
+
+#define CQPI_MAX_BANDS 16
+
+namespace cqpi {
+
+// Unique in-plane lattice vectors with their summed hopping matrices: H(k) adds
+// tn[R] e^{+i theta} + ta[R] e^{-i theta}, theta = 2 pi k.R (anti terms conjugated).
+struct RTerms {
+    std::vector<int32_t> R;     // [nR][2]
+    std::vector<double> tn, ta; // [nR][b*b][2]
+};
+
+struct Workspace {
+    int ebatch = 0;
+    double2 *g0k = nullptr;
+    double2 *half = nullptr;
+    double2 *box = nullptr;
+    double2 *T = nullptr;
+    double *term1 = nullptr;
+    double *energies = nullptr;
+    float2 *g0k32 = nullptr;
+    float2 *half32 = nullptr;
+};
+
+}  // namespace cqpi
+
+struct cqpi_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // model
+    int b = 0, scmax = 0;
+    double efermi = 0.0;
+    int nR = 0;
+    int32_t *d_R = nullptr;
+    double *d_tn = nullptr, *d_ta = nullptr;
+    // parameters
+    int n = 0, kp = 0, os = 0, w = 0, m = 0, spin = 0, precision = 0;
+    double eta = 0.0;
+    int Rb = 0, NB = 0, W = 0, Q = 0, wn = 0, nblk = 1, mb = 0;
+    int blk_start[2] = {0, 0};
+    // eigen cache
+    double *d_eval = nullptr;
+    double2 *d_evec = nullptr;
+    bool bands_ready = false;
+    // twiddles e^{+2 pi i t / kp}
+    double2 *d_tw = nullptr;
+    float2 *d_tw32 = nullptr;
+    // orbitals
+    double *d_phi = nullptr;
+    bool orbitals_ready = false;
+    // impurities
+    int nimp = 0;
+    double2 *d_V = nullptr;   // [nimp][b*b]
+    // workspace
+    cqpi::Workspace ws;
+    int *d_status = nullptr;
+    // narrow seam
+    double *d_seam_ldos = nullptr;
+    bool seam_pending = false;
+    // accounting
+    int64_t launches = 0;
+    float stage_ms[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev[8] = {};
+    std::string err;
+};
+
+namespace cqpi {
+
+// bands.cu
+void launch_bands(cqpi_handle *h);
+// greens.cu
+void launch_greens_k(cqpi_handle *h, int ne, const double *d_energies);
+void launch_fft(cqpi_handle *h, int ne);
+cudaError_t configure_fft(cqpi_handle *h);
+void launch_tmatrix(cqpi_handle *h, int ne);
+void launch_term1(cqpi_handle *h, int ne);
+// ldos.cu
+void launch_ldos_fp64(cqpi_handle *h, int ne, const double2 *box, const double2 *T, const double *term1,
+                      float *out32, double *out64);
+
+inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace cqpi

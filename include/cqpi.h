@@ -1,0 +1,142 @@
+/*
+ * cqpi.h -- C ABI of the GB300 continuum-LDOS engine (libcqpi.so).
+ *
+ * The engine computes CalcQPI's "Wannier mode" quasiparticle-interference maps
+ * (output=wannier, green=normal) on one NVIDIA GB300 (sm_103a):
+ *   H(k) -> Hermitian eigen-solve -> G0(k,w) -> G0(R,w) -> T-matrix -> LDOS map.
+ * Reference path: gpwahl/calcqpi-release, src/qpi.cc:454-950 driven by
+ * src/calcqpi.cc:655-783.
+ *
+ * Conventions (identical to the reference's):
+ *  - hoppings: R[h][3] int32 (lattice units), orb[h][2] int32 0-based (o1,o2),
+ *    t[h][2] double (re,im) already divided by the _hr.dat degeneracy, anti[h]
+ *    (conjugated phase, BdG hole block; src/tightbinding.h:128-135).
+ *  - H(k)_{o1 o2} = -efermi*d (o<scmaxbands) / +efermi*d (otherwise)
+ *                   + sum_h t_h exp(+-2 pi i k.R_h)     (src/tightbinding.cc:210-219)
+ *  - k-grid x_i = i/kp (i <= kp/2) else (i-kp)/kp       (src/qpi.cc:465-466)
+ *  - G0(k) = sum_n U_n U_n^H / (w - e_n + i eta)        (src/tightbinding.cc:282-289)
+ *  - G0(R) = kp^-2 sum_k G0(k) exp(+2 pi i k.R)         (src/qpi.cc:557-578)
+ *  - T = (1 - V G0(R=0))^-1 V                           (src/qpi.cc:833-854)
+ *  - orbitals wf[o][ix][iy], side (2*window+1)*oversamp (src/wannierfunctions.cc:433-442)
+ *  - maps are float32 (or float64) [layer][y][x], x = site_i*oversamp + sub_x,
+ *    the IDL file order of src/idl.cc:78-97.
+ * Complex numbers are interleaved (re, im) doubles.  All entry points return a
+ * status code (CQPI_OK == 0); none exits or aborts.  Calls on one handle are not
+ * thread-safe; distinct handles may be used from distinct threads.
+ */
+#ifndef CQPI_H
+#define CQPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CQPI_OK 0
+#define CQPI_ERR_ARG 1          /* invalid argument / size */
+#define CQPI_ERR_CUDA 2         /* CUDA runtime error (message in cqpi_last_error) */
+#define CQPI_ERR_ALLOC 3        /* device or host allocation failed */
+#define CQPI_ERR_DOMAIN 4       /* sizes outside the reference's index domain */
+#define CQPI_ERR_SINGULAR 5     /* 1 - V G0(0) singular at some energy */
+#define CQPI_ERR_STATE 6        /* call order violated (e.g. no orbitals set) */
+#define CQPI_ERR_NOT_SUPPORTED 7
+#define CQPI_ERR_NO_DEVICE 8    /* no CUDA device visible */
+
+#define CQPI_PREC_FP64 0        /* every stage in FP64 */
+#define CQPI_PREC_MIXED 1       /* FP64 eigen/T/k-sum fold, FP32/tensor-core contraction */
+
+typedef struct cqpi_handle cqpi_handle;
+
+typedef struct {
+    int32_t bands;        /* b = num_wann */
+    int32_t scmaxbands;   /* diagonal sign switch (b, or b/2 for scmodel) */
+    double efermi;        /* 'fermi' keyword */
+    int64_t nhops;
+    const int32_t *R;     /* [nhops][3] */
+    const int32_t *orb;   /* [nhops][2], 0-based */
+    const double *t;      /* [nhops][2] */
+    const uint8_t *anti;  /* [nhops], may be NULL (all 0) */
+} cqpi_model;
+
+typedef struct {
+    int32_t lattice;      /* n: sites per side ('lattice') */
+    int32_t kpoints;      /* kp ('kpoints', defaults to lattice in the CLI) */
+    int32_t oversamp;     /* os ('oversamp') */
+    int32_t window;       /* w ('window') */
+    int32_t maxband;      /* m: orbitals carrying a Wannier function (b, or b/2 for scmodel) */
+    int32_t spin;         /* 'spin': pair orbitals only inside spin half-blocks */
+    double eta;           /* 'eta' */
+    int32_t precision;    /* CQPI_PREC_FP64 or CQPI_PREC_MIXED */
+} cqpi_params;
+
+/* ---- lifetime ------------------------------------------------------------
+ * Replaces tmatrix::tmatrix (src/qpi.h:96-106) + CudaQPI::CudaQPI
+ * (src/qpicudakernel.cu:395-429): validates sizes, uploads the model, creates
+ * the handle's CUDA stream and owns all device memory. */
+int cqpi_create(const cqpi_model *model, const cqpi_params *params, cqpi_handle **out);
+/* Replaces tmatrix::~tmatrix / CudaQPI::~CudaQPI.  NULL is accepted. */
+int cqpi_destroy(cqpi_handle *h);
+/* Human-readable message of the last failing call on this handle. */
+const char *cqpi_last_error(const cqpi_handle *h);
+const char *cqpi_status_string(int status);
+const char *cqpi_version(void);
+
+/* ---- inputs ----------------------------------------------------------------
+ * Orbital cache, replaces the wf upload of CudaQPI::CudaQPI
+ * (src/qpicudakernel.cu:412-416) and the iszero() skips of src/qpi.cc:915-940.
+ * wf: [norb][side][side] doubles, norb >= maxband, side == (2w+1)*oversamp;
+ * is_zero: [norb] flags (NULL = none) for padded 'z' orbitals. */
+int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t side, const uint8_t *is_zero);
+/* Diagonal scattering potential, replaces tmatrix::setscatteringphase
+ * (src/qpi.h:107-130): vscat [bands][2].  Sets one impurity. */
+int cqpi_set_scattering(cqpi_handle *h, const double *vscat);
+/* Extension (C4 workloads): nimp full b x b potentials V[imp][b][b][2]; each
+ * impurity gives its own map.  Diagonal V reproduces cqpi_set_scattering. */
+int cqpi_set_impurities(cqpi_handle *h, const double *V, int32_t nimp);
+
+/* ---- compute ---------------------------------------------------------------
+ * H(k) build + FP64 Hermitian eigen-solve of every k-point, cached on the device.
+ * Replaces tmatrix::calchamiltonian (src/qpi.cc:454-475).  Asynchronous on the
+ * handle's stream; cqpi_run calls it lazily when the cache is empty, as
+ * tmatrix::setgreensfunction does (src/qpi.cc:479-480). */
+int cqpi_solve_bands(cqpi_handle *h);
+/* All energies -> maps.  Replaces, per energy, setgreensfunction +
+ * calcrealspacegreensfunction + calcwannierldos + ldos2idl
+ * (src/calcqpi.cc:690-756).  maps32 / maps64: [nE][nimp][wn][wn] (either may be
+ * NULL), wn = lattice*oversamp.  on_device != 0: the pointers are device memory
+ * and the call returns after enqueueing (cqpi_synchronize to wait); otherwise
+ * they are host memory and the call returns when they are filled. */
+int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, double *maps64, int32_t on_device);
+
+/* ---- narrow seam (GPUQPI, include/gpuqpi.h:18-32) ------------------------
+ * GPUQPI::wannierldos(scat, g0): host T-matrix T[b][b][2] and host real-space
+ * Green's function g0r[kp][kp][b][b][2] (the reference's g0 after
+ * calcrealspacegreensfunction); asynchronous like src/qpicudakernel.cu:577-598. */
+int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r);
+/* GPUQPI::retrieveResult(double*) (src/qpicudakernel.cu:690-704): waits and
+ * copies the last map, ldos[y][x] float64 (= the reference's ldos[x][y]). */
+int cqpi_retrieve_result(cqpi_handle *h, double *ldos);
+
+/* ---- stage access (parity tests, debugging) ----------------------------- */
+/* Eigen cache: eval[kp*kp][b], evec[kp*kp][b][b][2] (component o of vector n at [o][n]). */
+int cqpi_get_bands(cqpi_handle *h, double *eval, double *evec);
+/* G0(R) on the pruned box R in [-Rb, Rb]^2 at one energy: box[(X+Rb)][(Y+Rb)][b][b][2];
+ * *rb receives Rb (pass box = NULL to query it). */
+int cqpi_get_greens_box(cqpi_handle *h, double energy, double *box, int32_t *rb);
+/* T-matrix of impurity 0 at one energy: T[b][b][2]. */
+int cqpi_get_tmatrix(cqpi_handle *h, double energy, double *T);
+
+/* ---- runtime -------------------------------------------------------------- */
+int cqpi_get_stream(cqpi_handle *h, void **stream);   /* cudaStream_t of the handle */
+int cqpi_synchronize(cqpi_handle *h);
+/* Kernels this handle has launched since creation (all of them are the engine's own). */
+int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count);
+/* Device time (ms) of the stages of the last cqpi_run, measured with CUDA events on
+ * the handle's stream: [0] bands, [1] G0(k)+FFT, [2] T-matrix, [3] contraction, [4] total. */
+int cqpi_stage_times(const cqpi_handle *h, float *ms5);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,2 @@
+/* Project-written GSL API subset (test infrastructure only), see ../compat_gsl.h */
+#include "../compat_gsl.h"

@@ -1,0 +1,417 @@
+/*
+ * cqpi_oracle.c -- CPU restatement of the CalcQPI continuum-LDOS path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests/, the smoke
+ * check in __graft_entry__.py and the cpu_baseline / reference arm of
+ * bench.py may load it, as the checker or as the timed CPU baseline.  No
+ * product code links it or calls it.
+ *
+ * Parity pin: the functions below are checked against golden outputs of the
+ * reference's own sources (oracle/build_ref.sh builds them against a
+ * project-written GSL/FFTW API subset, tests/golden/make_golden.py records
+ * the outputs as fixtures).
+ *
+ * Every function restates one step of the reference, cited by file:line
+ * (paths within gpwahl/calcqpi-release).  Complex numbers are interleaved
+ * (re, im) doubles.  Array conventions shared with the engine:
+ *   hoppings   R[h][3] int32, orb[h][2] int32 (0-based), t[h][2], anti[h]
+ *   k index    ik = i*kp + j, i = x index, j = y index   (qpi.cc:457-468)
+ *   eigen      eval[ik][b], evec[ik][o][n] = component o of eigenvector n
+ *   G0 grids   g0[X][Y][o][a] (b x b row-major per point)
+ *   orbitals   wf[o][ix][iy], side = (2w+1)*os           (wannierfunctions.cc:433-442)
+ *   LDOS       ldos[x][y], x = i*os+ii  (the reference's tmatrix::ldos)
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define RE(p, i) ((p)[2 * (i)])
+#define IM(p, i) ((p)[2 * (i) + 1])
+
+/* ---- H(k):  tightbinding.cc:210-219, hoppingterm::addhop tightbinding.h:128-135 ---- */
+void orc_hk(int b, int64_t nhops, const int32_t *R, const int32_t *orb,
+            const double *t, const uint8_t *anti, double efermi, int scmax,
+            double kx, double ky, double *H)
+{
+    memset(H, 0, sizeof(double) * 2 * b * b);
+    for (int i = 0; i < b; i++) RE(H, i * b + i) = (i < scmax) ? -efermi : efermi;
+    for (int64_t h = 0; h < nhops; h++) {
+        /* kz = 0 in the 2D k-grid (qpi.cc:465-468: kvector[2] stays 0) */
+        double ph = 2.0 * M_PI * (R[3 * h] * kx + R[3 * h + 1] * ky + R[3 * h + 2] * 0.0);
+        if (anti[h]) ph = -ph;
+        double c = cos(ph), s = sin(ph);
+        double tr = t[2 * h], ti = t[2 * h + 1];
+        int e = orb[2 * h] * b + orb[2 * h + 1];
+        RE(H, e) += tr * c - ti * s;
+        IM(H, e) += tr * s + ti * c;
+    }
+}
+
+/* ---- Hermitian eigen-solve (gsl_eigen_hermv stand-in, qpi.cc:470) ----
+ * Cyclic complex Jacobi.  G0(k) is invariant under eigenvector phase and
+ * ordering, so any correct Hermitian eigensolver gives the same G0 to
+ * rounding.  A is overwritten; V receives eigenvectors as columns. */
+void orc_hermitian_jacobi(int b, double *A, double *V, double *ev)
+{
+    memset(V, 0, sizeof(double) * 2 * b * b);
+    for (int i = 0; i < b; i++) RE(V, i * b + i) = 1.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0, diag = 0.0;
+        for (int p = 0; p < b; p++)
+            for (int q = 0; q < b; q++) {
+                double a2 = RE(A, p * b + q) * RE(A, p * b + q) + IM(A, p * b + q) * IM(A, p * b + q);
+                if (p == q) diag += a2; else off += a2;
+            }
+        if (off <= 1e-32 * diag || off == 0.0) break;
+        for (int p = 0; p < b - 1; p++)
+            for (int q = p + 1; q < b; q++) {
+                double apr = RE(A, p * b + q), api = IM(A, p * b + q);
+                double c_abs = hypot(apr, api);
+                if (c_abs == 0.0) continue;
+                double app = RE(A, p * b + p), aqq = RE(A, q * b + q);
+                /* e^{i alpha} = A_pq / |A_pq| */
+                double er = apr / c_abs, ei = api / c_abs;
+                double tau = (aqq - app) / (2.0 * c_abs);
+                double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                double cs = 1.0 / sqrt(1.0 + tt * tt), sn = tt * cs;
+                /* G = [[cs, sn], [-sn e^{-ia}, cs e^{-ia}]] ; A <- G^H A G ; V <- V G */
+                for (int r = 0; r < b; r++) {       /* columns: X = A G */
+                    double xpr = RE(A, r * b + p), xpi = IM(A, r * b + p);
+                    double xqr = RE(A, r * b + q), xqi = IM(A, r * b + q);
+                    /* xq * e^{-ia} */
+                    double yr = xqr * er + xqi * ei, yi = xqi * er - xqr * ei;
+                    RE(A, r * b + p) = cs * xpr - sn * yr;  IM(A, r * b + p) = cs * xpi - sn * yi;
+                    RE(A, r * b + q) = sn * xpr + cs * yr;  IM(A, r * b + q) = sn * xpi + cs * yi;
+                    double vpr = RE(V, r * b + p), vpi = IM(V, r * b + p);
+                    double vqr = RE(V, r * b + q), vqi = IM(V, r * b + q);
+                    double wr = vqr * er + vqi * ei, wi = vqi * er - vqr * ei;
+                    RE(V, r * b + p) = cs * vpr - sn * wr;  IM(V, r * b + p) = cs * vpi - sn * wi;
+                    RE(V, r * b + q) = sn * vpr + cs * wr;  IM(V, r * b + q) = sn * vpi + cs * wi;
+                }
+                for (int cidx = 0; cidx < b; cidx++) { /* rows: A <- G^H X */
+                    double xpr = RE(A, p * b + cidx), xpi = IM(A, p * b + cidx);
+                    double xqr = RE(A, q * b + cidx), xqi = IM(A, q * b + cidx);
+                    /* xq * e^{+ia} */
+                    double yr = xqr * er - xqi * ei, yi = xqi * er + xqr * ei;
+                    RE(A, p * b + cidx) = cs * xpr - sn * yr;  IM(A, p * b + cidx) = cs * xpi - sn * yi;
+                    RE(A, q * b + cidx) = sn * xpr + cs * yr;  IM(A, q * b + cidx) = sn * xpi + cs * yi;
+                }
+                RE(A, p * b + q) = IM(A, p * b + q) = 0.0;
+                RE(A, q * b + p) = IM(A, q * b + p) = 0.0;
+                IM(A, p * b + p) = 0.0;
+                IM(A, q * b + q) = 0.0;
+            }
+    }
+    for (int i = 0; i < b; i++) ev[i] = RE(A, i * b + i);
+}
+
+/* ---- tmatrix::calchamiltonian, qpi.cc:454-475 (non-MPI form 457-475) ---- */
+void orc_bands(int b, int64_t nhops, const int32_t *R, const int32_t *orb,
+               const double *t, const uint8_t *anti, double efermi, int scmax,
+               int kp, double *eval, double *evec)
+{
+    size_t cut = (size_t)(kp >> 1);
+#pragma omp parallel
+    {
+        double *H = (double *)malloc(sizeof(double) * 2 * b * b);
+#pragma omp for schedule(static)
+        for (int i = 0; i < kp; i++)
+            for (int j = 0; j < kp; j++) {
+                double x = ((size_t)i > cut) ? ((double)i - kp) / kp : ((double)i / kp);
+                double y = ((size_t)j > cut) ? ((double)j - kp) / kp : ((double)j / kp);
+                size_t ik = (size_t)i * kp + j;
+                orc_hk(b, nhops, R, orb, t, anti, efermi, scmax, x, y, H);
+                orc_hermitian_jacobi(b, H, evec + ik * 2 * b * b, eval + ik * b);
+            }
+        free(H);
+    }
+}
+
+/* ---- G0(k) = sum_n U_n U_n^H / (omega - e_n + i eta)
+ *      tightbinding.cc:282-289 (gsl_blas_zgerc), loop qpi.cc:478-486 ---- */
+void orc_greens_k(int b, int kp, const double *eval, const double *evec,
+                  double omega, double eta, double *g0)
+{
+    size_t nk = (size_t)kp * kp;
+#pragma omp parallel for schedule(static)
+    for (long long ik = 0; ik < (long long)nk; ik++) {
+        const double *U = evec + (size_t)ik * 2 * b * b;
+        double *G = g0 + (size_t)ik * 2 * b * b;
+        memset(G, 0, sizeof(double) * 2 * b * b);
+        for (int n = 0; n < b; n++) {
+            /* factor = 1 / (omega - e_n + i eta)  (gsl_complex_inverse) */
+            double dr = omega - eval[(size_t)ik * b + n], di = eta;
+            double den = dr * dr + di * di;
+            double fr = dr / den, fi = -di / den;
+            for (int o = 0; o < b; o++) {
+                double ur = RE(U, o * b + n), ui = IM(U, o * b + n);
+                double xr = fr * ur - fi * ui, xi = fr * ui + fi * ur;
+                for (int a = 0; a < b; a++) {
+                    /* conj(U[a][n]) */
+                    double vr = RE(U, a * b + n), vi = -IM(U, a * b + n);
+                    RE(G, o * b + a) += xr * vr - xi * vi;
+                    IM(G, o * b + a) += xr * vi + xi * vr;
+                }
+            }
+        }
+    }
+}
+
+/* ---- 1D DFT with sign +1 (FFTW_BACKWARD), unnormalised ---- */
+static void dft_backward_1d(int N, double *x, int stride, double *tmp, const double *tw)
+{
+    /* tw[2k] = cos(2 pi k / N), tw[2k+1] = sin(2 pi k / N) */
+    for (int i = 0; i < N; i++) { tmp[2 * i] = x[2 * (size_t)i * stride]; tmp[2 * i + 1] = x[2 * (size_t)i * stride + 1]; }
+    if ((N & (N - 1)) == 0) {
+        /* iterative radix-2, bit-reversed input */
+        for (int i = 1, j = 0; i < N; i++) {
+            int bit = N >> 1;
+            for (; j & bit; bit >>= 1) j ^= bit;
+            j ^= bit;
+            if (i < j) {
+                double a = tmp[2 * i], c = tmp[2 * i + 1];
+                tmp[2 * i] = tmp[2 * j]; tmp[2 * i + 1] = tmp[2 * j + 1];
+                tmp[2 * j] = a; tmp[2 * j + 1] = c;
+            }
+        }
+        for (int len = 2; len <= N; len <<= 1) {
+            int step = N / len;
+            for (int s = 0; s < N; s += len)
+                for (int k = 0; k < len / 2; k++) {
+                    double wr = tw[2 * (k * step)], wi = tw[2 * (k * step) + 1];
+                    double *u = tmp + 2 * (s + k), *v = tmp + 2 * (s + k + len / 2);
+                    double vr = v[0] * wr - v[1] * wi, vi = v[0] * wi + v[1] * wr;
+                    v[0] = u[0] - vr; v[1] = u[1] - vi;
+                    u[0] += vr; u[1] += vi;
+                }
+        }
+        for (int i = 0; i < N; i++) { x[2 * (size_t)i * stride] = tmp[2 * i]; x[2 * (size_t)i * stride + 1] = tmp[2 * i + 1]; }
+    } else {
+        for (int k = 0; k < N; k++) {
+            double sr = 0.0, si = 0.0;
+            for (int i = 0; i < N; i++) {
+                int idx = (int)(((long long)i * k) % N);
+                double wr = tw[2 * idx], wi = tw[2 * idx + 1];
+                sr += tmp[2 * i] * wr - tmp[2 * i + 1] * wi;
+                si += tmp[2 * i] * wi + tmp[2 * i + 1] * wr;
+            }
+            x[2 * (size_t)k * stride] = sr; x[2 * (size_t)k * stride + 1] = si;
+        }
+    }
+}
+
+/* ---- tmatrix::calcrealspacegreensfunction, qpi.cc:557-578 ----
+ * For each orbital pair: divide by kp^2, 2D backward DFT (plan qpi.h:105),
+ * in place.  g0 holds G0(k) on entry and G0(R) on exit, [X][Y][o][a]. */
+void orc_fft_backward_2d(int kp, int b, double *g0)
+{
+    double *tw = (double *)malloc(sizeof(double) * 2 * kp);
+    for (int k = 0; k < kp; k++) { tw[2 * k] = cos(2.0 * M_PI * k / kp); tw[2 * k + 1] = sin(2.0 * M_PI * k / kp); }
+    double norm = (double)kp * kp;
+    size_t nk = (size_t)kp * kp, bb = (size_t)b * b;
+    for (size_t e = 0; e < bb; e++) {
+#pragma omp parallel for schedule(static)
+        for (long long ik = 0; ik < (long long)nk; ik++) {
+            g0[2 * (ik * bb + e)] /= norm;
+            g0[2 * (ik * bb + e) + 1] /= norm;
+        }
+#pragma omp parallel
+        {
+            double *tmp = (double *)malloc(sizeof(double) * 2 * kp);
+#pragma omp for schedule(static)
+            for (int i = 0; i < kp; i++)      /* transform along Y for each X */
+                dft_backward_1d(kp, g0 + 2 * ((size_t)i * kp * bb + e), (int)bb, tmp, tw);
+#pragma omp for schedule(static)
+            for (int j = 0; j < kp; j++)      /* transform along X for each Y */
+                dft_backward_1d(kp, g0 + 2 * ((size_t)j * bb + e), (int)(kp * bb), tmp, tw);
+            free(tmp);
+        }
+    }
+    free(tw);
+}
+
+/* ---- tmatrix::setscatteringmatrix, qpi.cc:833-854 ----
+ * T = (1 - V G0(R=0))^{-1} V with V = diag(vscat).  LU with partial
+ * pivoting on |.| (gsl_linalg_complex_LU_decomp) then invert. */
+int orc_tmatrix(int b, const double *vscat, const double *g00, double *T)
+{
+    double *M = (double *)calloc(2 * b * b, sizeof(double));
+    double *inv = (double *)calloc(2 * b * b, sizeof(double));
+    for (int i = 0; i < b; i++)
+        for (int j = 0; j < b; j++) {
+            /* (V G0)_{ij} = v_i G0_{ij} */
+            double vr = vscat[2 * i], vi = vscat[2 * i + 1];
+            double gr = RE(g00, i * b + j), gi = IM(g00, i * b + j);
+            RE(M, i * b + j) = (i == j ? 1.0 : 0.0) - (vr * gr - vi * gi);
+            IM(M, i * b + j) = -(vr * gi + vi * gr);
+        }
+    for (int i = 0; i < b; i++) RE(inv, i * b + i) = 1.0;
+    int rc = 0;
+    for (int c = 0; c < b; c++) {
+        int piv = c; double best = -1.0;
+        for (int r = c; r < b; r++) {
+            double a = hypot(RE(M, r * b + c), IM(M, r * b + c));
+            if (a > best) { best = a; piv = r; }
+        }
+        if (best == 0.0) { rc = -1; break; }
+        if (piv != c)
+            for (int k = 0; k < b; k++) {
+                double t0 = RE(M, c * b + k), t1 = IM(M, c * b + k);
+                RE(M, c * b + k) = RE(M, piv * b + k); IM(M, c * b + k) = IM(M, piv * b + k);
+                RE(M, piv * b + k) = t0; IM(M, piv * b + k) = t1;
+                t0 = RE(inv, c * b + k); t1 = IM(inv, c * b + k);
+                RE(inv, c * b + k) = RE(inv, piv * b + k); IM(inv, c * b + k) = IM(inv, piv * b + k);
+                RE(inv, piv * b + k) = t0; IM(inv, piv * b + k) = t1;
+            }
+        double pr = RE(M, c * b + c), pi = IM(M, c * b + c), pd = pr * pr + pi * pi;
+        for (int r = 0; r < b; r++) {
+            if (r == c) continue;
+            double mr = RE(M, r * b + c), mi = IM(M, r * b + c);
+            double fr = (mr * pr + mi * pi) / pd, fi = (mi * pr - mr * pi) / pd;
+            for (int k = 0; k < b; k++) {
+                double xr = RE(M, c * b + k), xi = IM(M, c * b + k);
+                RE(M, r * b + k) -= fr * xr - fi * xi; IM(M, r * b + k) -= fr * xi + fi * xr;
+                xr = RE(inv, c * b + k); xi = IM(inv, c * b + k);
+                RE(inv, r * b + k) -= fr * xr - fi * xi; IM(inv, r * b + k) -= fr * xi + fi * xr;
+            }
+        }
+    }
+    if (rc == 0)
+        for (int r = 0; r < b; r++) {
+            double pr = RE(M, r * b + r), pi = IM(M, r * b + r), pd = pr * pr + pi * pi;
+            for (int k = 0; k < b; k++) {
+                double xr = RE(inv, r * b + k), xi = IM(inv, r * b + k);
+                RE(inv, r * b + k) = (xr * pr + xi * pi) / pd;
+                IM(inv, r * b + k) = (xi * pr - xr * pi) / pd;
+            }
+        }
+    /* T = inv * V : column j scaled by v_j */
+    for (int i = 0; i < b; i++)
+        for (int j = 0; j < b; j++) {
+            double xr = RE(inv, i * b + j), xi = IM(inv, i * b + j);
+            double vr = vscat[2 * j], vi = vscat[2 * j + 1];
+            RE(T, i * b + j) = xr * vr - xi * vi;
+            IM(T, i * b + j) = xr * vi + xi * vr;
+        }
+    free(M); free(inv);
+    return rc;
+}
+
+static void zmul(int b, const double *A, const double *B, double *C)
+{
+    for (int i = 0; i < b; i++)
+        for (int j = 0; j < b; j++) {
+            double sr = 0.0, si = 0.0;
+            for (int k = 0; k < b; k++) {
+                double ar = RE(A, i * b + k), ai = IM(A, i * b + k);
+                double br = RE(B, k * b + j), bi = IM(B, k * b + j);
+                sr += ar * br - ai * bi; si += ar * bi + ai * br;
+            }
+            RE(C, i * b + j) = sr; IM(C, i * b + j) = si;
+        }
+}
+
+/* ---- tmatrix::calcwannierldos (CPU), qpi.cc:876-950 ----
+ * Direct form of the reference: per site, W products T*G0(-(p+d1)) and W^2
+ * products G0(p+d2)*buffer, then the sub-pixel / orbital accumulation.
+ * The G0 index formulas keep the reference's unsigned arithmetic
+ * (size_t kpoints + int offsets, qpi.cc:901,907,921).
+ * Rows [row_begin, row_end) of sites i are computed (all when row_end<=0);
+ * ldos[x][y] for those rows is overwritten. */
+void orc_wannier_ldos(int n, int kp, int b, int os, int w, int m, int spin,
+                      const double *T, const double *g0r, const double *wf,
+                      const uint8_t *wf_zero, double *ldos, int row_begin, int row_end)
+{
+    size_t wn = (size_t)os * n, side = (size_t)(2 * w + 1) * os, bb = (size_t)b * b;
+    size_t kpoints = (size_t)kp, n2 = (size_t)(n >> 1), spinbands = (size_t)(m >> 1);
+    if (row_end <= 0 || row_end > n) row_end = n;
+    for (int i = row_begin; i < row_end; i++)
+        for (size_t ii = 0; ii < (size_t)os; ii++)
+            for (size_t y = 0; y < wn; y++) ldos[((size_t)i * os + ii) * wn + y] = 0.0;
+#define G0AT(X, Y) (g0r + 2 * (((size_t)(X) * kpoints + (size_t)(Y)) * bb))
+#define WF(o, X, Y) (wf[((size_t)(o) * side + (size_t)(X)) * side + (size_t)(Y)])
+#pragma omp parallel
+    {
+        double *buffer = (double *)malloc(sizeof(double) * 2 * bb);
+        double *cldos = (double *)malloc(sizeof(double) * 2 * bb);
+#pragma omp for collapse(2) schedule(dynamic, 4)
+        for (int i = row_begin; i < row_end; i++)
+            for (int j = 0; j < n; j++) {
+                int ipos = i - (int)n2, jpos = j - (int)n2;
+                for (int nni1 = -w; nni1 <= w; nni1++)
+                    for (int nnj1 = -w; nnj1 <= w; nnj1++) {
+                        zmul(b, T, G0AT((kpoints + kpoints - (size_t)(ipos + nni1)) % kpoints,
+                                        (kpoints + kpoints - (size_t)(jpos + nnj1)) % kpoints), buffer);
+                        for (int nni2 = -w; nni2 <= w; nni2++)
+                            for (int nnj2 = -w; nnj2 <= w; nnj2++) {
+                                zmul(b, G0AT((kpoints + (size_t)(ipos + nni2)) % kpoints,
+                                             (kpoints + (size_t)(jpos + nnj2)) % kpoints), buffer, cldos);
+                                const double *gd = G0AT((kpoints - (size_t)nni1 + (size_t)nni2) % kpoints,
+                                                        (kpoints - (size_t)nnj1 + (size_t)nnj2) % kpoints);
+                                for (size_t ii = 0; ii < (size_t)os; ii++)
+                                    for (size_t jj = 0; jj < (size_t)os; jj++) {
+                                        size_t x = ii + (size_t)w * os, y = jj + (size_t)w * os;
+                                        size_t x1 = x - (size_t)((long)nni1 * os), y1 = y - (size_t)((long)nnj1 * os);
+                                        size_t x2 = x - (size_t)((long)nni2 * os), y2 = y - (size_t)((long)nnj2 * os);
+                                        double *out = &ldos[((size_t)i * os + ii) % wn * wn + ((size_t)j * os + jj) % wn];
+                                        if (!spin) {
+                                            for (size_t o1 = 0; o1 < (size_t)m; o1++) {
+                                                if (wf_zero[o1]) continue;
+                                                for (size_t o2 = 0; o2 < (size_t)m; o2++) {
+                                                    if (wf_zero[o2]) continue;
+                                                    double f = WF(o1, x1, y1) * WF(o2, x2, y2);
+                                                    *out -= IM(cldos, o2 * b + o1) * f;
+                                                    *out -= IM(gd, o2 * b + o1) * f;
+                                                }
+                                            }
+                                        } else {
+                                            for (size_t o1 = 0; o1 < spinbands; o1++) {
+                                                if (!wf_zero[o1])
+                                                    for (size_t o2 = 0; o2 < spinbands; o2++) {
+                                                        if (wf_zero[o2]) continue;
+                                                        double f = WF(o1, x1, y1) * WF(o2, x2, y2);
+                                                        *out -= IM(cldos, o2 * b + o1) * f;
+                                                        *out -= IM(gd, o2 * b + o1) * f;
+                                                    }
+                                                size_t s1 = spinbands + o1;
+                                                if (!wf_zero[s1])
+                                                    for (size_t o2 = 0; o2 < spinbands; o2++) {
+                                                        size_t s2 = spinbands + o2;
+                                                        if (wf_zero[s2]) continue;
+                                                        double f = WF(s1, x1, y1) * WF(s2, x2, y2);
+                                                        *out -= IM(cldos, s2 * b + s1) * f;
+                                                        *out -= IM(gd, s2 * b + s1) * f;
+                                                    }
+                                            }
+                                        }
+                                    }
+                            }
+                    }
+            }
+        free(buffer); free(cldos);
+    }
+#undef G0AT
+#undef WF
+}
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_threads(int nt)
+{
+#ifdef _OPENMP
+    if (nt > 0) omp_set_num_threads(nt);
+#else
+    (void)nt;
+#endif
+}

@@ -1,0 +1,278 @@
+"""Restatements of the reference's input/output formats (oracle, test infrastructure only).
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg import this module, as
+the checker of the engine's C++ host code.  Nothing in the product imports it.
+
+* ``read_hr``      -- tightbind::readfile, src/tightbinding.cc:70-149
+* ``read_idl`` / ``write_idl`` -- idl::read / idl::write, src/idl.cc:50-97
+* ``LoadConfig``   -- loadconfig, include/parser.h:24-197
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+_DIGITS = "0123456789"
+
+
+def _find_first_of(s: str, chars: str, pos: int = 0) -> int:
+    for i in range(max(pos, 0), len(s)):
+        if s[i] in chars:
+            return i
+    return -1
+
+
+def read_hr(text: str, scmodel: bool = False):
+    """Parse a Wannier90 ``_hr.dat`` the way tightbinding.cc:70-149 does.
+
+    Returns dict(name, bands, R[h,3], orb[h,2] (0-based), t[h] complex (divided by the
+    degeneracy), anti[h] bool).  Raises ValueError where the reference sets its error flag
+    or exits (invalid orbital index, tightbinding.cc:139-141).
+    """
+    lines = text.split("\n")
+    li = 0
+
+    def getline():
+        nonlocal li
+        if li >= len(lines):
+            raise ValueError("unexpected end of file")
+        s = lines[li]
+        li += 1
+        return s
+
+    name = getline()
+    cut = _find_first_of(name, "\n\r")
+    if cut >= 0:
+        name = name[:cut]
+    bands = int(getline().split()[0])
+    nrpts = int(getline().split()[0])
+    scmax = bands >> 1 if scmodel else bands
+    degs = []
+    buf, pos = "", 0
+    while len(degs) < nrpts:
+        if pos == 0:
+            buf = getline()
+            pos = _find_first_of(buf, _DIGITS, 0)
+            if pos < 0:
+                raise ValueError("degeneracy line without digits")
+        npos = _find_first_of(buf, " \t", pos)
+        ln = (npos - pos) if npos >= 0 else len(buf) - pos
+        npos = _find_first_of(buf, _DIGITS, npos) if npos >= 0 else -1
+        tok = buf[pos:pos + ln].split()
+        if not tok:
+            raise ValueError("bad degeneracy entry")
+        degs.append(int(tok[0]))
+        pos = npos if npos >= 0 else 0
+    R, orb, t, anti = [], [], [], []
+    k = 0
+    prev = None
+    while li < len(lines):
+        s = lines[li]
+        li += 1
+        if len(s) == 0:
+            continue
+        f = s.split()
+        if len(f) < 7:
+            raise ValueError(f"bad hopping line: {s!r}")
+        x, y, z, u, v = (int(f[0]), int(f[1]), int(f[2]), int(f[3]), int(f[4]))
+        hr, hc = float(f[5]), float(f[6])
+        if k == 0 or (x, y, z) != prev:
+            k += 1
+            prev = (x, y, z)
+        if k - 1 >= len(degs):
+            raise ValueError("more R vectors than degeneracies")
+        d = float(degs[k - 1])
+        if u <= 0 or v <= 0 or u > bands or v > bands:
+            raise ValueError("invalid orbital index")
+        R.append((x, y, z))
+        orb.append((u - 1, v - 1))
+        t.append(complex(hr / d, hc / d))
+        anti.append((u - 1) >= scmax and (v - 1) >= scmax)
+    return dict(name=name, bands=bands,
+                R=np.array(R, dtype=np.int32).reshape(-1, 3),
+                orb=np.array(orb, dtype=np.int32).reshape(-1, 2),
+                t=np.array(t, dtype=np.complex128),
+                anti=np.array(anti, dtype=bool), scmaxbands=scmax)
+
+
+def write_hr(path, name: str, bands: int, terms: dict):
+    """Write a ``_hr.dat`` (Wannier90 layout) with degeneracy 1 for every R.
+
+    ``terms`` maps (Rx, Ry, Rz) -> complex [bands, bands] hopping matrix."""
+    keys = sorted(terms)
+    out = [name, f"{bands:12d}", f"{len(keys):12d}"]
+    degs = ["    1"] * len(keys)
+    for i in range(0, len(degs), 15):
+        out.append("".join(degs[i:i + 15]))
+    for key in keys:
+        mat = terms[key]
+        for v in range(bands):
+            for u in range(bands):
+                c = mat[u, v]
+                out.append(f"{key[0]:5d}{key[1]:5d}{key[2]:5d}{u + 1:5d}{v + 1:5d}"
+                           f"{c.real:22.15e}{c.imag:22.15e}")
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")
+
+
+def cxx_double(x: float) -> str:
+    """Format a double like ``std::ostream << double`` with default flags (%g, precision 6)."""
+    if math.isnan(x):
+        return "nan" if math.copysign(1.0, x) > 0 else "-nan"
+    if math.isinf(x):
+        return "inf" if x > 0 else "-inf"
+    return "%g" % x
+
+
+def idl_bias(lb: float, hb: float, layers: int, k: int) -> float:
+    """idl::getbias, src/idl.cc:969-973."""
+    if layers == 1:
+        return lb
+    return (hb - lb) * k / (layers - 1.0) + lb
+
+
+def write_idl(path, data_kyx: np.ndarray, name: str, scan_range=(2.0, 2.0), offset=(-1.0, -1.0),
+              bias=(0.0, 0.0), setpoint=0.0, date: str | None = None):
+    """idl::write, src/idl.cc:78-97: 12 text lines, then float32 data layer-major, y, x fastest."""
+    z, y, x = data_kyx.shape
+    if date is None:
+        date = time.ctime()
+    head = [name, date, str(x), str(y), str(z), cxx_double(scan_range[0]), cxx_double(scan_range[1]),
+            cxx_double(offset[0]), cxx_double(offset[1]), cxx_double(bias[0]), cxx_double(bias[1]),
+            cxx_double(setpoint)]
+    with open(path, "wb") as fh:
+        fh.write(("\n".join(head) + "\n").encode())
+        fh.write(np.ascontiguousarray(data_kyx, dtype="<f4").tobytes())
+
+
+def read_idl(path):
+    """idl::read, src/idl.cc:50-76.  Returns (header dict, data[z][y][x] float32)."""
+    with open(path, "rb") as fh:
+        raw = fh.read()
+    pos = 0
+    lines = []
+    for _ in range(2):
+        e = raw.index(b"\n", pos)
+        lines.append(raw[pos:e].decode(errors="replace"))
+        pos = e + 1
+    vals = []
+    while len(vals) < 10:
+        while raw[pos:pos + 1].isspace():
+            pos += 1
+        e = pos
+        while e < len(raw) and not raw[e:e + 1].isspace():
+            e += 1
+        vals.append(raw[pos:e].decode())
+        pos = e
+    pos += 1  # is.ignore(1,'\n')
+    x, y, z = int(vals[0]), int(vals[1]), int(vals[2])
+    hdr = dict(name=lines[0], date=lines[1], size=(x, y, z),
+               scan_range=(float(vals[3]), float(vals[4])), offset=(float(vals[5]), float(vals[6])),
+               bias=(float(vals[7]), float(vals[8])), setpoint=float(vals[9]))
+    data = np.frombuffer(raw, dtype="<f4", count=x * y * z, offset=pos).reshape(z, y, x)
+    return hdr, data
+
+
+class LoadConfig:
+    """loadconfig, include/parser.h:24-197 (non-line mode)."""
+
+    def __init__(self, text: str):
+        self.name, self.field, self.comments = [], [], []
+        self.warnings = []
+        for line in text.split("\n"):
+            if len(line) == 0:
+                continue
+            h = line.find("#")
+            if h >= 0:
+                self.comments.append(line[h + 1:])
+                line = line[:h]
+            eq, sc = line.find("="), line.find(";")
+            if eq >= 0 and sc >= 0:
+                self.name.append(line[:eq])
+                self.field.append(line[eq + 1:sc])
+            elif eq >= 0 or sc >= 0:
+                self.warnings.append(line)
+        self.used = [0] * len(self.name)
+
+    def probefield(self, key):
+        for i, n in enumerate(self.name):
+            if n == key:
+                self.used[i] += 1
+                return True
+        return False
+
+    def getfield(self, key):
+        val = ""
+        for i, n in enumerate(self.name):
+            if n == key:
+                self.used[i] += 1
+                val = self.field[i]
+        if not val:
+            return ""
+        s = len(val) - len(val.lstrip(" \t"))
+        e = len(val.rstrip(" \t"))
+        if e <= s:
+            return val[s:]
+        return val[s:e]
+
+    @staticmethod
+    def _field2string(v):
+        f, l = v.find('"'), v.rfind('"')
+        return v[f + 1:l] if f >= 0 and l >= 0 else ""
+
+    def getstring(self, key):
+        return self._field2string(self.getfield(key))
+
+    def getvalue(self, key):
+        v = self.getfield(key)
+        return _atof(v) if v else float("nan")
+
+    def getintvalue(self, key):
+        v = self.getfield(key)
+        return _atoi(v) if v else 0
+
+    def getlist(self, key):
+        v = self.getfield(key)
+        f, l = v.find("("), v.rfind(")")
+        out = []
+        if f >= 0 and l >= 0:
+            idx = f + 1
+            while True:
+                nidx = _find_first_of(v, ",)", idx)
+                out.append(v[idx:nidx].strip(" \t"))
+                idx = nidx + 1
+                if nidx == l:
+                    break
+        return out
+
+    def getvector(self, key):
+        return [_atof(s) for s in self.getlist(key)]
+
+    def unused(self):
+        return [self.name[i] for i, u in enumerate(self.used) if not u]
+
+
+def _atof(s: str) -> float:
+    s = s.lstrip(" \t\n")
+    best = 0.0
+    for e in range(len(s), 0, -1):
+        try:
+            return float(s[:e])
+        except ValueError:
+            continue
+    return best
+
+
+def _atoi(s: str) -> int:
+    s = s.lstrip(" \t\n")
+    e = 0
+    if e < len(s) and s[e] in "+-":
+        e += 1
+    while e < len(s) and s[e].isdigit():
+        e += 1
+    try:
+        return int(s[:e])
+    except ValueError:
+        return 0
