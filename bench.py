@@ -1,0 +1,327 @@
+#!/usr/bin/env python
+"""Benchmark of the continuum-LDOS path (pixel*energies/s) on the 3-orbital t2g model.
+
+Workload (default --config C2): square-lattice t2g model (dxz, dyz, dxy), hoppings to
+3rd neighbours N(0, 0.25 eV) with C4 symmetry (seed 2), V = diag(0.3, 0.3, 0.5) eV,
+k-grid 1024^2, field of view 256^2 sites, 10x10 pixels per cell, 101 energies in
+[-0.1, 0.1] eV, eta = 2 meV.  Synthetic inputs generated from seeds (no dataset).
+
+One step = one complete job: H(k) + eigen-solve of all 1024^2 k-points, then for each
+of the 101 energies G0(k) -> pruned FFT -> T-matrix -> LDOS map; the maps (101 x
+2560^2 float32 = 2.6 GB) are written to HBM.  Inputs and outputs are far larger than
+the 129 MB L2, so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+  python bench.py --impl reference ...   # the reference's CPU algorithm on host cores
+
+Under torchrun (N > 1) every rank runs the same job on its own GPU (replicas: energies,
+impurities and fields of view are independent units; there is no data-path
+collective); the time is the max over ranks and value is the sum of all ranks' work.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "calcqpi-release_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "LDOS pixel*energies/s"
+UNIT = "pixel*energies/s"
+
+
+def ldos_flops_per_pixel_energy(b, m, W, spin):
+    """Algorithmic FLOPs of the factored contraction per pixel*energy:
+    8*W*m_eff*b (u and s, complex x real MACs) + 8*b^2 (T s) + 4*b (Im u.Ts) per spin block."""
+    nblk = 2 if spin else 1
+    mb = (m >> 1) if spin else m
+    return nblk * (8 * W * mb * b + 8 * b * b + 4 * b)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="clocks", suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax = max(smax, float(f[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            os.remove(self.path)
+        except Exception:
+            pass
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def cpu_sample(cfg_name, target_s=8.0, threads=None):
+    """Time the reference's CPU algorithm (oracle port of src/qpi.cc:478-950) on one
+    energy of the workload: G0(k) + FFT + T on the full k-grid, the direct LDOS loop
+    on the first R site rows, R chosen for ~target_s seconds.  Returns (pixel*E/s
+    extrapolated to the full energy, cores, description)."""
+    from cqpi import workloads as W
+    from oracle import oracle as O
+    if threads:
+        O.set_threads(threads)
+    c, m, wf = W.config(cfg_name)
+    om = O.Model(m.bands, m.R, m.orb, m.t)
+    ev, U = O.bands(om, c.kpoints)     # once per run in the reference; not part of the sample
+    e = float(c.energy_list()[len(c.energy_list()) // 2])
+    t0 = time.perf_counter()
+    g0r = O.realspace(O.greens_k(ev, U, c.kpoints, e, c.eta))
+    T = O.tmatrix(np.array(c.scattering, complex), g0r[0, 0])
+    tg = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.wannier_ldos(c.lattice, c.kpoints, c.oversamp, c.window, m.bands, c.spin, T, g0r, wf, rows=(0, 2))
+    t2 = time.perf_counter() - t0
+    rows = int(max(2, min(c.lattice, round(2 * target_s / max(t2, 1e-3)))))
+    t0 = time.perf_counter()
+    O.wannier_ldos(c.lattice, c.kpoints, c.oversamp, c.window, m.bands, c.spin, T, g0r, wf, rows=(0, rows))
+    tl = time.perf_counter() - t0
+    t_energy = tg + tl * c.lattice / rows
+    value = c.pixels_per_energy / t_energy
+    desc = (f"{cfg_name}, 1 energy: G0(k)+FFT+T on the full {c.kpoints}^2 k-grid ({tg:.2f} s) + direct LDOS "
+            f"loop on {rows}/{c.lattice} site rows ({tl:.2f} s), extrapolated to the full energy "
+            f"({c.pixels_per_energy} pixels); eigen-solve excluded as in the reference's layer-0 timing")
+    return value, O.num_threads(), desc
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    vals = []
+    desc, cores = "", 1
+    for i in range(args.warmup + args.steps):
+        v, cores, desc = cpu_sample(args.config, target_s=args.cpu_seconds / 2)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"{args.config} continuum LDOS (reference CPU algorithm, oracle port)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    world, rank, local = dist_setup()
+    import torch
+    import cqpi_build
+    cqpi_build.build()
+    import cqpi
+    from cqpi import workloads as W
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    prec = cqpi.PREC_MIXED if args.precision == "mixed" else cqpi.PREC_FP64
+    c, m, wf = W.config(args.config)
+    E = c.energy_list()
+    nE = len(E)
+    vscat = np.array(c.scattering, complex)
+    if len(vscat) < m.bands:
+        vscat = np.concatenate([vscat, np.zeros(m.bands - len(vscat), complex)])
+    eng = cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, spin=c.spin, precision=prec)
+    eng.set_orbitals(wf)
+    eng.set_scattering(vscat)
+    wn = c.lattice * c.oversamp
+    out = torch.empty((nE, 1, wn, wn), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(eng.stream)
+
+    stage_acc = {"bands": 0.0, "greens": 0.0, "tmatrix": 0.0, "ldos": 0.0, "total": 0.0}
+
+    def step(acc=None):
+        eng.solve_bands()
+        eng.run_device(E, ptr32=out.data_ptr())
+        if acc is not None:
+            for k, v in eng.stage_times().items():
+                acc[k] += v
+
+    for _ in range(args.warmup):
+        step()
+    eng.synchronize()
+    launches0 = eng.kernel_launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step(stage_acc)
+    ev1.record(stream)
+    ev1.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = eng.kernel_launches() - launches0
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    work_per_rank = c.pixels_per_energy * nE
+    value = world * work_per_rank / (ms / 1e3)
+
+    # e2e through the public API with host buffers: create the handle from host arrays,
+    # upload orbitals and scattering, run all energies, read the maps back into
+    # page-locked host memory.
+    host_out = torch.empty((nE * wn * wn,), dtype=torch.float32, pin_memory=True).numpy()
+    h2d = (m.R.nbytes + m.orb.nbytes + np.asarray(m.t).nbytes + m.anti.nbytes + wf.nbytes + vscat.nbytes + E.nbytes)
+    d2h = host_out.nbytes
+    e2e_steps = max(1, min(args.steps, 3))
+
+    def e2e_step():
+        with cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, spin=c.spin, precision=prec) as e2:
+            e2.set_orbitals(wf)
+            e2.set_scattering(vscat)
+            e2.run(E, out32=host_out)
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * work_per_rank / e2e_s
+
+    # roofline of the dominant kernel (the LDOS contraction)
+    peaks, peak_src = measured_peaks()
+    F = ldos_flops_per_pixel_energy(m.bands, m.bands, (2 * c.window + 1) ** 2, c.spin)
+    ldos_ms = stage_acc["ldos"] / args.steps
+    achieved = F * work_per_rank / (ldos_ms / 1e3) / 1e12
+    if prec == cqpi.PREC_FP64:
+        peak = cqpi.measure_fma_peak("fp64")
+        roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "measured DFMA loop (cqpi_measure_fma_peak), not in MEASURED_PEAKS.json"}
+    else:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": f"bf16 burst, {peak_src}"}
+    roof["kernel"] = "ldos contraction"
+    roof["flop_per_pixel_energy"] = F
+    roof["traffic"] = None
+    roof["stage_ms_per_step"] = {k: v / args.steps for k, v in stage_acc.items()}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == cqpi.PREC_FP64 else "mixed(f64 eigen/T, tf32x3/f32)",
+            "data": "synthetic (seeded model and orbitals)",
+            "config": {"workload": f"{args.config}: t2g 3-orbital square lattice, k-grid {c.kpoints}^2, "
+                                   f"FOV {c.lattice}^2 sites, {c.oversamp}x{c.oversamp} px/cell, {nE} energies, "
+                                   f"eta={c.eta}", "precision": args.precision,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs/outputs larger than L2 (2.6 GB of maps, 168 MB eigen cache per step)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches), "roofline": roof}
+    if clk is not None:
+        line["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, desc = cpu_sample(args.config, target_s=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="C2")
+    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

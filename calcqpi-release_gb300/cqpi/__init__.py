@@ -22,7 +22,7 @@ EXPORTED = [
     "cqpi_create", "cqpi_destroy", "cqpi_last_error", "cqpi_status_string", "cqpi_version",
     "cqpi_set_orbitals", "cqpi_set_scattering", "cqpi_set_impurities", "cqpi_solve_bands", "cqpi_run",
     "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
-    "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times",
+    "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
 ]
 
 
@@ -81,8 +81,19 @@ def load():
     L.cqpi_synchronize.argtypes = [P]
     L.cqpi_kernel_launches.argtypes = [P, ctypes.POINTER(i64)]
     L.cqpi_stage_times.argtypes = [P, P]
+    L.cqpi_measure_fma_peak.argtypes = [i32, ctypes.POINTER(dbl)]
     _lib = L
     return L
+
+
+def measure_fma_peak(kind: str) -> float:
+    """Measured CUDA-core FMA peak in TFLOP/s ('fp64' or 'fp32')."""
+    L = load()
+    v = ctypes.c_double()
+    rc = L.cqpi_measure_fma_peak({"fp64": 0, "fp32": 1}[kind], ctypes.byref(v))
+    if rc != OK:
+        raise CqpiError(rc, L.cqpi_status_string(rc).decode())
+    return v.value
 
 
 def _ptr(a):
@@ -158,11 +169,14 @@ class Engine:
     def solve_bands(self):
         self._check(self._L.cqpi_solve_bands(self._h))
 
-    def run(self, energies, f32=True, f64=False):
-        """Host maps [nE][nimp][wn][wn] (float32 and/or float64)."""
+    def run(self, energies, f32=True, f64=False, out32=None):
+        """Host maps [nE][nimp][wn][wn] (float32 and/or float64).  ``out32`` may be a
+        preallocated (e.g. page-locked) float32 array to receive the maps."""
         e = np.ascontiguousarray(energies, np.float64).reshape(-1)
         shape = (len(e), self.nimp, self.wn, self.wn)
-        o32 = np.empty(shape, np.float32) if f32 else None
+        if out32 is not None:
+            assert out32.dtype == np.float32 and out32.size == int(np.prod(shape)) and out32.flags.c_contiguous
+        o32 = (out32.reshape(shape) if out32 is not None else np.empty(shape, np.float32)) if f32 else None
         o64 = np.empty(shape, np.float64) if f64 else None
         self._check(self._L.cqpi_run(self._h, _ptr(e), len(e), _ptr(o32), _ptr(o64), 0))
         if f32 and f64:

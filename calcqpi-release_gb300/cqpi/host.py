@@ -1,0 +1,105 @@
+"""ctypes wrappers of the host-side (CPU-only) C ABI in include/cqpi_host.h."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import load
+
+
+class _HR(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 512), ("bands", ctypes.c_int32), ("scmaxbands", ctypes.c_int32),
+                ("nrpts", ctypes.c_int32), ("nhops", ctypes.c_int64), ("R", ctypes.POINTER(ctypes.c_int32)),
+                ("orb", ctypes.POINTER(ctypes.c_int32)), ("t", ctypes.POINTER(ctypes.c_double)),
+                ("anti", ctypes.POINTER(ctypes.c_uint8))]
+
+
+class _IDLHeader(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 1024), ("date", ctypes.c_char * 256), ("size", ctypes.c_int32 * 3),
+                ("scan_range", ctypes.c_double * 2), ("offset", ctypes.c_double * 2), ("bias", ctypes.c_double * 2),
+                ("setpoint", ctypes.c_double), ("data_offset", ctypes.c_int64)]
+
+
+def _lib():
+    L = load()
+    if not getattr(L, "_host_ready", False):
+        P = ctypes.c_void_p
+        L.cqpi_read_hr.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.POINTER(_HR))]
+        L.cqpi_hr_free.argtypes = [ctypes.POINTER(_HR)]
+        L.cqpi_orbital_known.argtypes = [ctypes.c_char_p]
+        L.cqpi_orbital_cache.argtypes = [ctypes.c_char_p] + [ctypes.c_double] * 7 + [ctypes.c_int32, ctypes.c_int32, P]
+        L.cqpi_idl_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_int32, P, P, P, ctypes.c_double, P]
+        L.cqpi_idl_read_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(_IDLHeader)]
+        L.cqpi_idl_read.argtypes = [ctypes.c_char_p, P, ctypes.c_int64]
+        L.cqpi_host_last_error.restype = ctypes.c_char_p
+        L._host_ready = True
+    return L
+
+
+class HostError(RuntimeError):
+    pass
+
+
+def _err(L, rc):
+    raise HostError(f"status {rc}: {L.cqpi_host_last_error().decode()}")
+
+
+def read_hr(path: str, scmodel: bool = False) -> dict:
+    L = _lib()
+    p = ctypes.POINTER(_HR)()
+    rc = L.cqpi_read_hr(path.encode(), int(scmodel), ctypes.byref(p))
+    if rc:
+        _err(L, rc)
+    hr = p.contents
+    n = hr.nhops
+    out = dict(name=hr.name.decode(), bands=hr.bands, scmaxbands=hr.scmaxbands, nrpts=hr.nrpts,
+               R=np.ctypeslib.as_array(hr.R, (n, 3)).copy() if n else np.zeros((0, 3), np.int32),
+               orb=np.ctypeslib.as_array(hr.orb, (n, 2)).copy() if n else np.zeros((0, 2), np.int32),
+               t=(np.ctypeslib.as_array(hr.t, (n, 2)).copy().view(np.complex128).reshape(-1)) if n
+               else np.zeros(0, np.complex128),
+               anti=np.ctypeslib.as_array(hr.anti, (n,)).astype(bool) if n else np.zeros(0, bool))
+    L.cqpi_hr_free(p)
+    return out
+
+
+def orbital_cache(name, window, oversamp, width=0.5, height=5.0, xpos=0.0, ypos=0.0, theta=0.0, phi=0.0,
+                  prefact=1.0) -> np.ndarray:
+    L = _lib()
+    side = (2 * window + 1) * oversamp
+    out = np.empty((side, side), np.float64)
+    rc = L.cqpi_orbital_cache(name.encode(), width, height, xpos, ypos, theta, phi, prefact, window, oversamp,
+                              out.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+    return out
+
+
+def idl_write(path, data_kyx, name, scan_range=(2.0, 2.0), offset=(-1.0, -1.0), bias=(0.0, 0.0), setpoint=0.0,
+              date=None):
+    L = _lib()
+    d = np.ascontiguousarray(data_kyx, np.float32)
+    z, y, x = d.shape
+    sr, of, bi = (np.array(v, np.float64) for v in (scan_range, offset, bias))
+    rc = L.cqpi_idl_write(str(path).encode(), name.encode(), None if date is None else date.encode(), x, y, z,
+                          sr.ctypes.data_as(ctypes.c_void_p), of.ctypes.data_as(ctypes.c_void_p),
+                          bi.ctypes.data_as(ctypes.c_void_p), setpoint, d.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+
+
+def idl_read(path):
+    L = _lib()
+    h = _IDLHeader()
+    rc = L.cqpi_idl_read_header(str(path).encode(), ctypes.byref(h))
+    if rc:
+        _err(L, rc)
+    x, y, z = h.size
+    data = np.empty((z, y, x), np.float32)
+    rc = L.cqpi_idl_read(str(path).encode(), data.ctypes.data_as(ctypes.c_void_p), data.size)
+    if rc:
+        _err(L, rc)
+    hdr = dict(name=h.name.decode(), date=h.date.decode(), size=(x, y, z), scan_range=tuple(h.scan_range),
+               offset=tuple(h.offset), bias=tuple(h.bias), setpoint=h.setpoint)
+    return hdr, data

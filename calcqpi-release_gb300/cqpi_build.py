@@ -64,6 +64,11 @@ def build_lib(verbose=False, extra_flags=()) -> str:
         objs.append(o)
         if not _newer(o, [s] + headers):
             cmds.append([NVCC] + NVFLAGS + list(extra_flags) + ["-c", s, "-o", o])
+    for s in sorted(glob.glob(os.path.join(CSRC, "*.cc"))):
+        o = os.path.join(OBJ, os.path.basename(s)[:-3] + ".host.o")
+        objs.append(o)
+        if not _newer(o, [s] + headers):
+            cmds.append([CXX, "-O2", "-std=c++17", "-fPIC", "-I" + INCLUDE, "-I" + CSRC, "-c", s, "-o", o])
     _run_parallel(cmds, verbose)
     if cmds or not _newer(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()

@@ -1,0 +1,271 @@
+// host_io.cc -- host-side input/output of the drop-in, exported through the C ABI:
+//   cqpi_read_hr        Wannier90 _hr.dat reader   (tightbind::readfile, src/tightbinding.cc:70-149)
+//   cqpi_orbital_cache  analytic orbital cache    (wannierfunctions::precalculate + getwave,
+//                                                  src/wannierfunctions.cc:21-221,433-442)
+//   cqpi_idl_write / cqpi_idl_read_header / cqpi_idl_read
+//                       IDL map container          (idl::write / idl::read, src/idl.cc:50-97)
+// These run on the CPU only; none of them touches the GPU.
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "cqpi.h"
+#include "cqpi_host.h"
+
+namespace {
+
+std::string g_host_err;
+
+int host_fail(int code, const std::string &m)
+{
+    g_host_err = m;
+    return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cqpi_host_last_error(void) { return g_host_err.c_str(); }
+
+int cqpi_read_hr(const char *path, int32_t scmodel, cqpi_hr **out)
+{
+    if (!path || !out) return host_fail(CQPI_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::ifstream is(path);
+    if (!is) return host_fail(CQPI_ERR_ARG, std::string("cannot read or open input file ") + path);
+    std::string buf;
+    size_t lineno = 0;
+    std::string name;
+    int bands = 0, nrpts = 0;
+    if (!std::getline(is, buf)) return host_fail(CQPI_ERR_ARG, "empty _hr.dat");
+    lineno++;
+    name = buf.substr(0, buf.find_first_of("\n\r"));
+    if (!std::getline(is, buf)) return host_fail(CQPI_ERR_ARG, "missing num_wann line");
+    lineno++;
+    std::istringstream(buf) >> bands;
+    if (!std::getline(is, buf)) return host_fail(CQPI_ERR_ARG, "missing nrpts line");
+    lineno++;
+    std::istringstream(buf) >> nrpts;
+    if (bands < 1 || nrpts < 0) return host_fail(CQPI_ERR_ARG, "invalid num_wann / nrpts");
+    const int scmax = scmodel ? (bands >> 1) : bands;
+    // degeneracies: integer tokens read across lines until nrpts are found
+    std::vector<long> degs;
+    degs.reserve(nrpts);
+    size_t pos = 0;
+    while ((int)degs.size() < nrpts) {
+        if (!pos) {
+            if (!std::getline(is, buf)) return host_fail(CQPI_ERR_ARG, "unexpected end of file in degeneracies");
+            lineno++;
+            pos = buf.find_first_of("0123456789", 0);
+            if (pos == std::string::npos) return host_fail(CQPI_ERR_ARG, "error in input file in line " + std::to_string(lineno));
+        }
+        size_t npos = buf.find_first_of(" \t", pos);
+        size_t len = (npos != std::string::npos) ? npos - pos : buf.length() - pos;
+        npos = buf.find_first_of("0123456789", npos);
+        std::istringstream iss(buf.substr(pos, len));
+        long d;
+        iss >> d;
+        if (iss.fail()) return host_fail(CQPI_ERR_ARG, "error in input file in line " + std::to_string(lineno) + ": " + buf);
+        degs.push_back(d);
+        pos = (npos != std::string::npos) ? npos : 0;
+    }
+    // hopping lines: x y z u v re im; the degeneracy index advances whenever (x,y,z) changes
+    std::vector<int32_t> R, orb;
+    std::vector<double> t;
+    std::vector<uint8_t> anti;
+    size_t k = 0;
+    int ox = 0, oy = 0, oz = 0;
+    while (std::getline(is, buf)) {
+        lineno++;
+        if (buf.empty()) continue;
+        std::istringstream iss(buf);
+        int x, y, z;
+        long u, v;
+        double hr, hc;
+        iss >> x >> y >> z >> u >> v >> hr >> hc;
+        if (iss.fail()) return host_fail(CQPI_ERR_ARG, "error in input file in line " + std::to_string(lineno) + ": " + buf);
+        if (k == 0 || x != ox || y != oy || z != oz) {
+            k++;
+            ox = x; oy = y; oz = z;
+        }
+        if (k > degs.size()) return host_fail(CQPI_ERR_ARG, "more R vectors than degeneracies (line " + std::to_string(lineno) + ")");
+        if (u <= 0 || v <= 0 || u > bands || v > bands)
+            return host_fail(CQPI_ERR_ARG, "invalid orbital index in line " + std::to_string(lineno));
+        const double dg = (double)degs[k - 1];
+        R.push_back(x); R.push_back(y); R.push_back(z);
+        orb.push_back((int32_t)(u - 1)); orb.push_back((int32_t)(v - 1));
+        t.push_back(hr / dg); t.push_back(hc / dg);
+        anti.push_back(((u - 1) >= scmax) && ((v - 1) >= scmax));
+    }
+    cqpi_hr *hr = (cqpi_hr *)calloc(1, sizeof(cqpi_hr));
+    if (!hr) return host_fail(CQPI_ERR_ALLOC, "out of memory");
+    snprintf(hr->name, sizeof hr->name, "%s", name.c_str());
+    hr->bands = bands;
+    hr->scmaxbands = scmax;
+    hr->nrpts = nrpts;
+    hr->nhops = (int64_t)anti.size();
+    size_t nh = anti.size() ? anti.size() : 1;
+    hr->R = (int32_t *)malloc(sizeof(int32_t) * 3 * nh);
+    hr->orb = (int32_t *)malloc(sizeof(int32_t) * 2 * nh);
+    hr->t = (double *)malloc(sizeof(double) * 2 * nh);
+    hr->anti = (uint8_t *)malloc(nh);
+    if (!hr->R || !hr->orb || !hr->t || !hr->anti) {
+        cqpi_hr_free(hr);
+        return host_fail(CQPI_ERR_ALLOC, "out of memory");
+    }
+    if (!anti.empty()) {
+        memcpy(hr->R, R.data(), sizeof(int32_t) * R.size());
+        memcpy(hr->orb, orb.data(), sizeof(int32_t) * orb.size());
+        memcpy(hr->t, t.data(), sizeof(double) * t.size());
+        memcpy(hr->anti, anti.data(), anti.size());
+    }
+    *out = hr;
+    return CQPI_OK;
+}
+
+void cqpi_hr_free(cqpi_hr *hr)
+{
+    if (!hr) return;
+    free(hr->R);
+    free(hr->orb);
+    free(hr->t);
+    free(hr->anti);
+    free(hr);
+}
+
+// ------------------------------------------------------------------ orbitals
+static int orbital_type(const char *name)
+{
+    static const char *names[] = {"s", "px", "py", "pz", "dx2", "dxy", "dxz", "dyz", "dr2", "fy3x2", "fxyz",
+                                  "fyz2", "fz3", "fxz2", "fzx2", "fxx2", "n", "z"};
+    for (int i = 0; i < 18; i++)
+        if (!strcmp(name, names[i])) return i;
+    return -1;
+}
+
+int cqpi_orbital_known(const char *name) { return name && orbital_type(name) >= 0; }
+
+// Value of orbital 'type' at (x, y): z = 0 shifted by -height (tip plane below the
+// orbital centre, src/wannierfunctions.cc:127-130), optional rotation for non-s types.
+static double orbital_value(int type, double x, double y, double width, double height, double xpos, double ypos,
+                            double theta, double phi, double prefact, double symmetry)
+{
+    double z = 0.0;
+    x -= xpos; y -= ypos; z -= height;
+    if (type == 17) return 0.0;
+    if (type != 0 && (theta != 0.0 || phi != 0.0)) {
+        const double xc = x, yc = y, zc = z;
+        x = xc * cos(theta) + yc * sin(theta) * cos(phi) + zc * sin(theta) * sin(phi);
+        y = -xc * sin(theta) + yc * cos(theta) * cos(phi) + zc * cos(theta) * sin(phi);
+        z = -sin(phi) * yc + cos(phi) * zc;
+    }
+    const double r = sqrt(x * x + y * y + z * z);
+    const double ex = prefact * exp(-r / width);
+    if (type == 0) return ex / sqrt(4.0 * M_PI);
+    if (type == 16) {
+        const double sc = cos(symmetry * atan2(x, y) / 2.0);
+        return ex * sc * sc * r / width;
+    }
+    if (r == 0.0) return 0.0;
+    switch (type) {
+    case 1: return ex * x / r * sqrt(3.0 / 4.0 / M_PI);
+    case 2: return ex * y / r * sqrt(3.0 / 4.0 / M_PI);
+    case 3: return ex * z / r * sqrt(3.0 / 4.0 / M_PI);
+    case 4: return ex * (x * x - y * y) / 2.0 / r / r * sqrt(15.0 / 4.0 / M_PI);
+    case 5: return ex * x * y / r / r * sqrt(15.0 / 4.0 / M_PI);
+    case 6: return ex * x * z / r / r * sqrt(15.0 / 4.0 / M_PI);
+    case 7: return ex * y * z / r / r * sqrt(15.0 / 4.0 / M_PI);
+    case 8: return ex * (3.0 * z * z - r * r) / 4.0 / r / r * sqrt(5.0 / M_PI);
+    case 9: return ex * y * (3.0 * x * x - y * y) / 4.0 / r / r / r * sqrt(35.0 / 2.0 / M_PI);
+    case 10: return ex * x * y * z / r / r / r * sqrt(105.0 / 4.0 / M_PI);
+    case 11: return ex * y * (5.0 * z * z - r * r) / r / r / r / 4.0 * sqrt(21.0 / 2.0 / M_PI);
+    case 12: return ex * (5.0 * z * z * z - 3.0 * z * r * r) / r / r / r / 4.0 * sqrt(7.0 / M_PI);
+    case 13: return ex * x * (5.0 * z * z - r * r) / 4.0 / r / r / r * sqrt(21.0 / 2.0 / M_PI);
+    case 14: return ex * z * (x * x - y * y) / r / r / r / 4.0 * sqrt(105.0 / M_PI);
+    case 15: return ex * x * (x * x - 3.0 * y * y) / 4.0 / r / r / r * sqrt(35.0 / 2.0 / M_PI);
+    }
+    return NAN;
+}
+
+int cqpi_orbital_cache(const char *name, double width, double height, double xpos, double ypos, double theta,
+                       double phi, double prefact, int32_t window, int32_t oversamp, double *out)
+{
+    const int type = name ? orbital_type(name) : -1;
+    if (type < 0) return host_fail(CQPI_ERR_ARG, std::string("unknown orbital type ") + (name ? name : "(null)"));
+    if (!out || window < 0 || oversamp < 1) return host_fail(CQPI_ERR_ARG, "invalid orbital cache arguments");
+    const int n = (2 * window + 1) * oversamp;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+            out[(size_t)i * n + j] = orbital_value(type, (double)i / oversamp - (double)window - 0.5,
+                                                   (double)j / oversamp - (double)window - 0.5, width, height, xpos,
+                                                   ypos, theta, phi, prefact, 4.0);
+    return CQPI_OK;
+}
+
+// ------------------------------------------------------------------ IDL files
+int cqpi_idl_write(const char *path, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
+                   const double *scan_range, const double *offset, const double *bias, double setpoint,
+                   const float *data)
+{
+    if (!path || sx < 0 || sy < 0 || sz < 0 || (!data && (size_t)sx * sy * sz)) return host_fail(CQPI_ERR_ARG, "invalid IDL arguments");
+    std::string d;
+    if (date) d = date;
+    else {
+        time_t tt = time(nullptr);
+        d = ctime(&tt);
+        d.resize(d.length() - 1);
+    }
+    std::ofstream os(path, std::ios::binary);
+    if (!os) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
+    os << (name ? name : "") << std::endl << d << std::endl << (size_t)sx << std::endl << (size_t)sy << std::endl
+       << (size_t)sz << std::endl << scan_range[0] << std::endl << scan_range[1] << std::endl << offset[0] << std::endl
+       << offset[1] << std::endl << bias[0] << std::endl << bias[1] << std::endl << setpoint << std::endl;
+    os.write((const char *)data, (std::streamsize)(sizeof(float) * (size_t)sx * sy * sz));
+    if (!os) return host_fail(CQPI_ERR_ARG, std::string("error writing to ") + path);
+    return CQPI_OK;
+}
+
+int cqpi_idl_read_header(const char *path, cqpi_idl_header *hdr)
+{
+    if (!path || !hdr) return host_fail(CQPI_ERR_ARG, "null argument");
+    std::ifstream is(path, std::ios::binary);
+    if (!is) return host_fail(CQPI_ERR_ARG, std::string("cannot open ") + path);
+    std::string name, date;
+    std::getline(is, name);
+    std::getline(is, date);
+    size_t s0, s1, s2;
+    is >> s0 >> s1 >> s2 >> hdr->scan_range[0] >> hdr->scan_range[1] >> hdr->offset[0] >> hdr->offset[1] >>
+        hdr->bias[0] >> hdr->bias[1] >> hdr->setpoint;
+    if (!is) return host_fail(CQPI_ERR_ARG, std::string("error reading header of ") + path);
+    is.ignore(1, '\n');
+    snprintf(hdr->name, sizeof hdr->name, "%s", name.c_str());
+    snprintf(hdr->date, sizeof hdr->date, "%s", date.c_str());
+    hdr->size[0] = (int32_t)s0;
+    hdr->size[1] = (int32_t)s1;
+    hdr->size[2] = (int32_t)s2;
+    hdr->data_offset = (int64_t)is.tellg();
+    return CQPI_OK;
+}
+
+int cqpi_idl_read(const char *path, float *data, int64_t count)
+{
+    cqpi_idl_header h;
+    int rc = cqpi_idl_read_header(path, &h);
+    if (rc) return rc;
+    const int64_t n = (int64_t)h.size[0] * h.size[1] * h.size[2];
+    if (!data || count < n) return host_fail(CQPI_ERR_ARG, "IDL data buffer too small");
+    std::ifstream is(path, std::ios::binary);
+    is.seekg(h.data_offset);
+    is.read((char *)data, (std::streamsize)(sizeof(float) * n));
+    if (!is) return host_fail(CQPI_ERR_ARG, std::string("error reading data of ") + path);
+    return CQPI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,519 @@
+// calcqpi_main.cc -- `calcqpi <inputfile>`: the drop-in CLI for the continuum-LDOS
+// ("Wannier mode") path, running on the GB300 engine through the C ABI.
+//
+// Mirrors the reference driver src/calcqpi.cc:131-811 for output=wannier,
+// green=normal: the same keywords and defaults (:133-137), model load (:277-292),
+// scattering setup (:254-272, :393-395), orbital setup from idlorbitalfile
+// (:483-518) or analytic orbitals (:519-576), wffile output (:602-618), the map
+// idl(os*n, os*n, layers, 2, 2, lenergy, henergy, 0, -1, -1) with its comment line
+// (:640-656), layer energies idl::getbias (src/idl.cc:969-973) and the final save
+// (:779-783).  Modes and keywords outside that path (josephson, spf, uspf, nomode,
+// green=surface|bulk, threshold lists, XSF orbitalfiles, bsfile, dosfile) stop with
+// an explicit "not supported" error instead of being ignored.
+#include <unistd.h>
+#include <pwd.h>
+
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "config.h"
+#include "cqpi.h"
+#include "cqpi_host.h"
+
+using cplx = std::complex<double>;
+
+namespace {
+
+// Line-buffered log sink that prefixes every line with "YYYY-MM-DD.HH:MM:SS ".
+class Log {
+    std::ostream *os_;
+    std::ofstream file_;
+    bool bol_ = true;
+
+public:
+    Log() : os_(&std::cout) {}
+    bool open_append(const std::string &path)
+    {
+        file_.open(path.c_str(), std::ios::out | std::ios::app);
+        if (file_.is_open()) os_ = &file_;
+        return file_.is_open();
+    }
+    Log &operator<<(const std::string &s)
+    {
+        for (char c : s) {
+            if (bol_) {
+                char buf[64];
+                time_t now = time(nullptr);
+                struct tm t;
+                localtime_r(&now, &t);
+                strftime(buf, sizeof buf, "%Y-%m-%d.%X ", &t);
+                *os_ << buf;
+            }
+            *os_ << c;
+            bol_ = (c == '\n');
+            if (bol_) os_->flush();
+        }
+        return *this;
+    }
+    template <class T>
+    Log &operator<<(const T &v)
+    {
+        std::ostringstream s;
+        s << v;
+        return *this << s.str();
+    }
+};
+
+struct Section {
+    std::string name;
+    double wall = 0.0, cpu = 0.0;
+};
+
+class Timings {
+    std::vector<Section> secs_;
+    std::chrono::steady_clock::time_point last_ = std::chrono::steady_clock::now();
+    double lastcpu_ = cpu_now();
+    static double cpu_now()
+    {
+        timespec ts;
+        clock_gettime(CLOCK_PROCESS_CPUTIME_ID, &ts);
+        return ts.tv_sec + 1e-9 * ts.tv_nsec;
+    }
+
+public:
+    void add(const std::string &name)
+    {
+        auto now = std::chrono::steady_clock::now();
+        double c = cpu_now();
+        double w = std::chrono::duration<double>(now - last_).count(), dc = c - lastcpu_;
+        last_ = now;
+        lastcpu_ = c;
+        for (auto &s : secs_)
+            if (s.name == name) {
+                s.wall += w;
+                s.cpu += dc;
+                return;
+            }
+        secs_.push_back({name, w, dc});
+    }
+    void print(Log &log) const
+    {
+        double tw = 0, tc = 0;
+        for (auto &s : secs_) { tw += s.wall; tc += s.cpu; }
+        log << "Summary of timings: \n";
+        log << "     Section                            CPU time (s)            Real time (s)\n";
+        for (auto &s : secs_) {
+            std::ostringstream l;
+            l << "     " << std::setw(33) << std::left << s.name << " " << std::setw(12) << std::right << std::fixed
+              << std::setprecision(6) << s.cpu << " (" << std::setprecision(1) << std::setw(5)
+              << (tc > 0 ? 100.0 * s.cpu / tc : 0.0) << "%)   " << std::setprecision(6) << std::setw(12) << s.wall
+              << " (" << std::setprecision(1) << std::setw(5) << (tw > 0 ? 100.0 * s.wall / tw : 0.0) << "%)\n";
+            log << l.str();
+        }
+        std::ostringstream l;
+        l << "     Total time elapsed                " << std::fixed << std::setprecision(6) << std::setw(12) << tc
+          << "           " << std::setw(12) << tw << "\n";
+        log << l.str();
+    }
+};
+
+void help()
+{
+    std::cerr << "calcqpi (GB300 continuum-LDOS engine, " << cqpi_version() << ")\n\n"
+              << "Syntax:\ncalcqpi configfile\n\n"
+              << "Keywords of the continuum-LDOS (wannier) path:\n"
+              << " tbfile, qpifile, output (wannier), logfile, wffile,\n"
+              << " lattice (201), oversamp (4), energies (-1,1), layers (21), kpoints (=lattice),\n"
+              << " green (normal), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
+              << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
+              << " pos[i], zheight (5.0), idlorbitalfile\n";
+}
+
+double getbias(double lb, double hb, size_t layers, size_t k)
+{
+    if (layers == 1) return lb;
+    return (hb - lb) * (double)k / ((double)layers - 1.0) + lb;
+}
+
+int not_supported(Log &log, const std::string &what)
+{
+    log << "Error: " << what << " is not supported by the GB300 continuum-LDOS engine - exiting.\n";
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    if (argc < 2) {
+        help();
+        return 0;
+    }
+    size_t n = 201, layers = 21, oversamp = 4, window = 2, kpoints = 0;
+    bool spin = false, scmodel = false;
+    double lenergy = -1.0, henergy = 1.0, eta = 0.005, efermi = 0.0, radius = 0.5, angle = 0.0, zheight = 5.0,
+           magscat = 0.0;
+    cplx scatphase(1.0, 0.0);
+    std::string tbfile, qpifile;
+    std::vector<cplx> scattering;
+    Timings timings;
+    Log log;
+
+    std::ostringstream cfgerr;
+    InputFile lf(argv[1], cfgerr);
+    if (!lf.ok()) {
+        std::cerr << cfgerr.str();
+        return 1;
+    }
+    if (lf.has("logfile")) log.open_append(lf.str("logfile"));
+    log << "calcqpi (" << cqpi_version() << ")\n"
+        << "New calculation started, using configuration from " << argv[1] << "\n";
+    {
+        char host[256] = {0};
+        gethostname(host, sizeof host - 1);
+        struct passwd *pw = getpwuid(geteuid());
+        log << "Running on one GB300 GPU as user " << (pw ? pw->pw_name : "") << " on machine " << host << "\n";
+    }
+    if (!cfgerr.str().empty()) log << "Error while reading configuration file:\n" << cfgerr.str();
+
+    if (lf.has("tbfile")) tbfile = lf.str("tbfile");
+    else {
+        log << "No tightbinding model specified ... exiting.\n";
+        return 1;
+    }
+    if (lf.has("stbfile")) return not_supported(log, "stbfile (surface Green's function)");
+    if (lf.has("fermi")) efermi = lf.value("fermi");
+    if (lf.has("epserr")) lf.value("epserr");
+    if (lf.has("green")) {
+        std::string g = lf.field("green");
+        if (g == "surface" || g == "bulk") return not_supported(log, "green=" + g);
+        if (g != "normal") log << "Invalid value for green: " << g << "\n";
+    }
+    if (lf.has("spin")) {
+        std::string s = lf.field("spin");
+        if (s == "true") spin = true;
+        else if (s == "false") spin = false;
+        else log << "Invalid value for spin: " << s << "\n";
+    }
+    if (lf.has("scmodel")) {
+        std::string s = lf.field("scmodel");
+        if (s == "true") scmodel = true;
+        else if (s == "false") scmodel = false;
+        else log << "Invalid value for scmodel: " << s << "\n";
+    }
+    if (lf.has("output")) {
+        std::string o = lf.field("output");
+        if (o == "josephson" || o == "spf" || o == "uspf" || o == "nomode") return not_supported(log, "output=" + o);
+        if (o != "wannier") {
+            log << "Unrecognized output mode.";
+            return 1;
+        }
+    }
+    if (lf.has("qpifile")) qpifile = lf.str("qpifile");
+    if (lf.has("lattice")) n = lf.ivalue("lattice");
+    if (lf.has("oversamp")) oversamp = lf.ivalue("oversamp");
+    if (lf.has("window")) window = lf.ivalue("window");
+    if (lf.has("threshold")) {
+        double th = lf.value("threshold");
+        if (!std::isnan(th)) return not_supported(log, "threshold (sparse proximity list)");
+    }
+    if (lf.has("layers")) layers = lf.ivalue("layers");
+    if (lf.has("energies")) {
+        std::vector<double> e = lf.vec("energies");
+        if (e.size() >= 2) { lenergy = e[0]; henergy = e[1]; }
+    }
+    if (lf.has("eta")) eta = lf.value("eta");
+    if (lf.has("etat")) lf.value("etat");
+    if (lf.has("deltat")) lf.value("deltat");
+    if (lf.has("kpoints")) kpoints = lf.ivalue("kpoints");
+    if (!kpoints) kpoints = n;
+    if (lf.has("phase")) {
+        std::vector<double> ph = lf.vec("phase");
+        ph.resize(2, 0.0);
+        scatphase = cplx(ph[0], ph[1]);
+        log << "Using scattering phase (" << ph[0] << "," << ph[1] << ")\n";
+    }
+    if (lf.has("scattering")) {
+        std::vector<double> sl = lf.vec("scattering");
+        for (double s : sl) scattering.push_back(s * scatphase);
+        log << "Scattering: \n";
+        std::ostringstream l;
+        for (size_t i = 0; i < scattering.size(); i++)
+            l << (i ? ",(" : "(") << scattering[i].real() << "," << scattering[i].imag() << ")";
+        log << l.str() << "\n";
+    }
+    if (lf.has("magscat")) magscat = lf.value("magscat");
+    if (lf.has("bsfile")) return not_supported(log, "bsfile (band-structure histogram)");
+    if (lf.has("dosfile")) return not_supported(log, "dosfile (density of states output)");
+
+    log << "Loading TB model " << tbfile << "\n";
+    cqpi_hr *hr = nullptr;
+    if (cqpi_read_hr(tbfile.c_str(), scmodel ? 1 : 0, &hr) != CQPI_OK) {
+        log << cqpi_host_last_error() << "\n" << "Error loading TB model from " << tbfile << ", exiting.\n";
+        return 1;
+    }
+    log << "Loading tb model from " << hr->name << " with " << hr->bands << " orbitals and " << hr->nrpts
+        << " hopping terms.\n";
+    const size_t bands = (size_t)hr->bands;
+    size_t maxbands;
+    if (scmodel) {
+        maxbands = bands >> 1;
+        log << "Assuming TB model to be superconducting, only first half of bands used.\n";
+        size_t sl = scattering.size();
+        if (sl == maxbands)
+            for (size_t i = 0; i < sl; i++) scattering.push_back((-1.0 + 2.0 * magscat) * scattering[i]);
+    } else {
+        maxbands = bands;
+    }
+    double maxhop = 0.0;
+    for (int64_t i = 0; i < hr->nhops; i++) maxhop = std::max(maxhop, std::hypot(hr->t[2 * i], hr->t[2 * i + 1]));
+    if (maxhop / n < eta)
+        log << "Note: Broadening eta (" << eta << ") large compared to maximum hopping (" << maxhop
+            << ") at given k-point resolution (hopping/kpoints=" << maxhop / kpoints << ").\n";
+
+    // scattering vector (tmatrix::setscatteringphase, src/qpi.h:107-130)
+    std::vector<double> vscat(2 * bands, 0.0);
+    for (size_t i = 0; i < bands; i++) {
+        cplx v = scattering.empty() ? scatphase : (i < scattering.size() ? scattering[i] : cplx(0.0, 0.0));
+        vscat[2 * i] = v.real();
+        vscat[2 * i + 1] = v.imag();
+    }
+    {
+        std::ostringstream l;
+        l << "Parameters of calculation:\n"
+          << "         Tight-binding model  : " << tbfile << "\n"
+          << "         Output file for QPI  : " << qpifile << "\n"
+          << "         Bands:               : " << maxbands << "\n"
+          << "         Lattice              : " << n << "x" << n << "\n"
+          << "         kpoints              : " << kpoints << "x" << kpoints << "\n"
+          << "         energy range         : (" << lenergy << "," << henergy << ")\n"
+          << "         energy layers        : " << layers << "\n"
+          << "         Fermi energy         : " << efermi << "\n"
+          << "         broadening parameter : " << eta << "\n"
+          << "         window               : " << window << "\n"
+          << "         oversamp             : " << oversamp << "\n"
+          << "         Green's function     : normal\n"
+          << (spin ? "         spin-polarized calculation\n" : "         paramagnetic calculation\n");
+        log << l.str();
+    }
+    log << "QPI calculations in Wannier-mode (cLDOS).\n";
+
+    // ---------------------------------------------------------------- orbitals
+    std::vector<double> prearr;
+    if (lf.has("prearr")) prearr = lf.vec("prearr");
+    prearr.resize(maxbands, 1.0);
+    std::vector<std::vector<double>> wfs;   // each (2w+1)os squared
+    std::vector<uint8_t> zero;
+    size_t side = 0;
+    if (lf.has("idlorbitalfile")) {
+        std::string of = lf.str("idlorbitalfile");
+        log << "Using IDL orbital file for vacuum overlap.\nLoading wave function file " << of << ".\n";
+        cqpi_idl_header hd;
+        if (cqpi_idl_read_header(of.c_str(), &hd) != CQPI_OK) {
+            log << "Error loading orbitals from file " << of << ", exiting.\n";
+            return 1;
+        }
+        const size_t xs = hd.size[0], ys = hd.size[1], orbs = hd.size[2];
+        prearr.resize(orbs, 1.0);
+        if (xs != ys || xs != (2 * window + 1) * oversamp) {
+            log << "Orbital functions in " << of << " have unsuitable dimensions.\n";
+            return 1;
+        }
+        std::vector<float> raw(xs * ys * orbs);
+        if (cqpi_idl_read(of.c_str(), raw.data(), (int64_t)raw.size()) != CQPI_OK) {
+            log << "Error loading orbitals from file " << of << ", exiting.\n";
+            return 1;
+        }
+        side = xs;
+        for (size_t k = 0; k < orbs; k++) {
+            std::vector<double> a(xs * ys);
+            for (size_t i = 0; i < xs; i++)
+                for (size_t j = 0; j < ys; j++) a[i * ys + j] = prearr[k] * (double)raw[(k * ys + j) * xs + i];
+            wfs.push_back(a);
+            zero.push_back(0);
+        }
+        if ((maxbands >> 1) == orbs && spin) {
+            log << "Found half as many orbitals as needed in spin-polarized calculation, duplicating wave function set.\n";
+            for (size_t k = 0; k < orbs; k++) { wfs.push_back(wfs[k]); zero.push_back(0); }
+        } else if (maxbands > orbs) {
+            log << "Warning: Fewer number of orbitals in " << of << " than there are bands, padding with zeros.\n";
+            for (size_t i = orbs; i < maxbands; i++) { wfs.push_back(std::vector<double>(xs * ys, 0.0)); zero.push_back(1); }
+        }
+    } else if (lf.has("orbitals")) {
+        std::vector<std::string> orbitals = lf.list("orbitals");
+        if (lf.has("radius")) radius = lf.value("radius");
+        if (lf.has("angle")) angle = lf.value("angle");
+        if (lf.has("zheight")) zheight = lf.value("zheight");
+        log << "Using gaussian orbitals for vacuum overlap.\n    Parameters:\n"
+            << "             Radius:         " << radius << "\n"
+            << "             Rotation angle: " << angle << "\n"
+            << "             Height:         " << zheight << "\n";
+        std::vector<double> anglearr;
+        if (lf.has("anglearr")) anglearr = lf.vec("anglearr");
+        anglearr.resize(orbitals.size(), 0.0);
+        prearr.resize(orbitals.size(), 1.0);
+        struct Spec { std::string name; double height, x, y, theta, pre; };
+        std::vector<Spec> specs;
+        for (size_t i = 0; i < orbitals.size(); i++) {
+            if (!cqpi_orbital_known(orbitals[i].c_str())) {
+                log << "Unknown orbital type " << orbitals[i] << " - exiting.\n";
+                return 1;
+            }
+            std::ostringstream key;
+            key << "pos[" << i << "]";
+            double th = (angle + anglearr[i]) * M_PI / 180.0;
+            if (lf.has(key.str())) {
+                std::vector<double> pos = lf.vec(key.str());
+                pos.resize(3, 0.0);
+                specs.push_back({orbitals[i], zheight - pos[2], pos[0], pos[1], th, prearr[i]});
+            } else {
+                specs.push_back({orbitals[i], zheight, 0.0, 0.0, th, prearr[i]});
+            }
+        }
+        if ((maxbands >> 1) == orbitals.size() && spin) {
+            log << "Found half as many orbitals as needed in spin-polarized calculation, duplicating wave function set.\n";
+            const size_t k0 = specs.size();
+            for (size_t k = 0; k < k0; k++) specs.push_back(specs[k]);
+        } else if (orbitals.size() < maxbands) {
+            log << "Warning: Fewer number of orbitals specified than there are bands, padding with zeros.\n";
+            for (size_t i = orbitals.size(); i < maxbands; i++) specs.push_back({"z", zheight, 0.0, 0.0, 0.0, 0.0});
+        }
+        log << "Parameters for Wannier functions:\n";
+        for (size_t i = 0; i < specs.size(); i++) {
+            std::string nm = specs[i].name == "z" ? "zero" : specs[i].name;
+            log << "Orbital " << i << ": " << nm << "@(" << specs[i].x << "," << specs[i].y << "), height "
+                << specs[i].height << ", theta " << specs[i].theta * 180.0 / M_PI << "deg \n";
+        }
+        if (window) {
+            double val = radius * std::sqrt(std::log(100.0) + std::abs(zheight));
+            log << "Recommended window size for r=" << radius << ": " << std::ceil(val * val - zheight * zheight)
+                << "\nchosen window size: " << window << "\n";
+        } else {
+            for (auto &s : specs) {
+                (void)s;
+                double nw = std::ceil(radius * std::sqrt(std::log(1.0 / 0.01)));
+                if (nw > window) window = (size_t)nw;
+            }
+            log << "Using recommended window size for r=" << radius << ": " << window << "\n";
+        }
+        log << "Precalculating wave functions.\n";
+        side = (2 * window + 1) * oversamp;
+        for (auto &s : specs) {
+            std::vector<double> a(side * side);
+            cqpi_orbital_cache(s.name.c_str(), radius, s.height, s.x, s.y, s.theta, 0.0, s.pre, (int32_t)window,
+                               (int32_t)oversamp, a.data());
+            wfs.push_back(a);
+            zero.push_back(s.name == "z");
+        }
+        log << "Done.\n";
+        double mx = 0.0;
+        for (size_t o = 0; o < wfs.size(); o++) {
+            if (zero[o]) continue;
+            double m = 0.0, bnd = 0.0;
+            for (size_t i = 0; i < side; i++)
+                for (size_t j = 0; j < side; j++) {
+                    double v = std::abs(wfs[o][i * side + j]);
+                    m = std::max(m, v);
+                    if (i == 0 || j == 0 || i == side - 1 || j == side - 1) bnd = std::max(bnd, v);
+                }
+            if (m > 0) mx = std::max(mx, bnd / m);
+        }
+        log << "Maximum rel. value at boundary: " << mx << "\n";
+        if (mx > 0.05) log << "Warning: boundary too close, use larger window size!\n";
+    } else if (lf.has("orbitalfiles")) {
+        return not_supported(log, "orbitalfiles (XSF Wannier orbitals)");
+    } else {
+        log << "No orbitals specified (orbitals= or idlorbitalfile=) - exiting.\n";
+        return 1;
+    }
+    if (lf.has("wffile")) {
+        std::vector<float> d(side * side * wfs.size());
+        for (size_t l = 0; l < wfs.size(); l++)
+            for (size_t i = 0; i < side; i++)
+                for (size_t j = 0; j < side; j++) d[(l * side + j) * side + i] = (float)wfs[l][i * side + j];
+        std::ostringstream c;
+        c << "Wannier function file for " << tbfile << " with window=" << window << " and oversamp=" << oversamp;
+        const double sr[2] = {1.0, 1.0}, of[2] = {0.0, 0.0}, bi[2] = {0.0, 0.0};
+        log << "Writing wave function file to " << lf.str("wffile") << "\n";
+        cqpi_idl_write(lf.str("wffile").c_str(), c.str().c_str(), nullptr, (int32_t)side, (int32_t)side,
+                       (int32_t)wfs.size(), sr, of, bi, 0.0, d.data());
+    }
+    if (wfs.size() < maxbands) {
+        log << "Fewer orbitals than bands - exiting.\n";
+        return 1;
+    }
+
+    // ---------------------------------------------------------------- engine
+    cqpi_model model = {hr->bands, hr->scmaxbands, efermi, hr->nhops, hr->R, hr->orb, hr->t, hr->anti};
+    cqpi_params par = {(int32_t)n, (int32_t)kpoints, (int32_t)oversamp, (int32_t)window, (int32_t)maxbands,
+                       spin ? 1 : 0, eta, CQPI_PREC_FP64};
+    if (lf.has("precision")) {
+        std::string p = lf.field("precision");
+        if (p == "mixed") par.precision = CQPI_PREC_MIXED;
+        else if (p != "fp64") log << "Invalid value for precision: " << p << "\n";
+    }
+    cqpi_handle *h = nullptr;
+    int rc = cqpi_create(&model, &par, &h);
+    if (rc != CQPI_OK) {
+        log << "Error: engine creation failed: " << cqpi_status_string(rc) << "\n";
+        return 1;
+    }
+    std::vector<double> wflat(wfs.size() * side * side);
+    for (size_t o = 0; o < wfs.size(); o++) std::copy(wfs[o].begin(), wfs[o].end(), wflat.begin() + o * side * side);
+    rc = cqpi_set_orbitals(h, wflat.data(), (int32_t)wfs.size(), (int32_t)side, zero.data());
+    if (rc == CQPI_OK) rc = cqpi_set_scattering(h, vscat.data());
+    if (rc != CQPI_OK) {
+        log << "Error: " << cqpi_last_error(h) << "\n";
+        cqpi_destroy(h);
+        return 1;
+    }
+    const size_t wn = n * oversamp;
+    std::ostringstream comment;
+    comment << "CQPI calculation for " << hr->name << " with window=" << window << " and oversamp=" << oversamp;
+    timings.add("Initialization of calculation");
+
+    std::vector<double> energies(layers);
+    for (size_t k = 0; k < layers; k++) energies[k] = getbias(lenergy, henergy, layers, k);
+    std::vector<float> maps(wn * wn * layers);
+    // energies go through the engine in groups so that progress is reported per group
+    const size_t group = 16;
+    for (size_t k0 = 0; k0 < layers; k0 += group) {
+        const size_t ne = std::min(group, layers - k0);
+        for (size_t k = k0; k < k0 + ne; k++) {
+            std::ostringstream l;
+            l << "Calculating layer " << k << " at energy " << std::fixed << std::setprecision(4) << energies[k] << "\n";
+            log << l.str();
+        }
+        rc = cqpi_run(h, energies.data() + k0, (int32_t)ne, maps.data() + k0 * wn * wn, nullptr, 0);
+        if (rc != CQPI_OK) {
+            log << "Error: " << cqpi_last_error(h) << "\n";
+            cqpi_destroy(h);
+            return 1;
+        }
+        timings.add("Calculation of CLDOS");
+    }
+    log << "Calculation finished.\nSaving to " << qpifile << "\n";
+    const double sr[2] = {2.0, 2.0}, of[2] = {-1.0, -1.0}, bi[2] = {lenergy, henergy};
+    rc = cqpi_idl_write(qpifile.c_str(), comment.str().c_str(), nullptr, (int32_t)wn, (int32_t)wn, (int32_t)layers, sr,
+                        of, bi, 0.0, maps.data());
+    if (rc != CQPI_OK) log << "Error writing to stream.\n" << cqpi_host_last_error() << "\n";
+    log << "Done.\n";
+    timings.add("Saving data");
+    cqpi_destroy(h);
+    cqpi_hr_free(hr);
+    timings.print(log);
+    std::ostringstream un;
+    lf.report_unused(un);
+    if (!un.str().empty()) std::cerr << un.str();
+    return 0;
+}

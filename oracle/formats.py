@@ -10,6 +10,7 @@ the checker of the engine's C++ host code.  Nothing in the product imports it.
 from __future__ import annotations
 
 import math
+import re
 import time
 
 import numpy as np
@@ -22,6 +23,31 @@ def _find_first_of(s: str, chars: str, pos: int = 0) -> int:
         if s[i] in chars:
             return i
     return -1
+
+
+class _Extract:
+    """Formatted extraction like ``std::istringstream >> int/double``: skip blanks, then
+    take the longest prefix that forms a number (so '1-2.0e+00' yields 1, then -2.0)."""
+    _INT = re.compile(r"[+-]?\d+")
+    _REAL = re.compile(r"[+-]?(\d+\.?\d*([eE][+-]?\d+)?|\.\d+([eE][+-]?\d+)?)")
+
+    def __init__(self, s):
+        self.s, self.p = s, 0
+
+    def _take(self, rx):
+        while self.p < len(self.s) and self.s[self.p] in " \t\r\n\v\f":
+            self.p += 1
+        m = rx.match(self.s, self.p)
+        if not m:
+            raise ValueError("no number at %d" % self.p)
+        self.p = m.end()
+        return m.group(0)
+
+    def integer(self):
+        return int(self._take(self._INT))
+
+    def real(self):
+        return float(self._take(self._REAL))
 
 
 def read_hr(text: str, scmodel: bool = False):
@@ -73,11 +99,12 @@ def read_hr(text: str, scmodel: bool = False):
         li += 1
         if len(s) == 0:
             continue
-        f = s.split()
-        if len(f) < 7:
+        sc = _Extract(s)
+        try:
+            x, y, z, u, v = sc.integer(), sc.integer(), sc.integer(), sc.integer(), sc.integer()
+            hr, hc = sc.real(), sc.real()
+        except ValueError:
             raise ValueError(f"bad hopping line: {s!r}")
-        x, y, z, u, v = (int(f[0]), int(f[1]), int(f[2]), int(f[3]), int(f[4]))
-        hr, hc = float(f[5]), float(f[6])
         if k == 0 or (x, y, z) != prev:
             k += 1
             prev = (x, y, z)
@@ -97,17 +124,20 @@ def read_hr(text: str, scmodel: bool = False):
                 anti=np.array(anti, dtype=bool), scmaxbands=scmax)
 
 
-def write_hr(path, name: str, bands: int, terms: dict):
-    """Write a ``_hr.dat`` (Wannier90 layout) with degeneracy 1 for every R.
+def write_hr(path, name: str, bands: int, terms: dict, degeneracy=None):
+    """Write a ``_hr.dat`` (Wannier90 layout).
 
-    ``terms`` maps (Rx, Ry, Rz) -> complex [bands, bands] hopping matrix."""
+    ``terms`` maps (Rx, Ry, Rz) -> complex [bands, bands] hopping matrix; ``degeneracy``
+    maps R -> integer weight (default 1).  Stored values are hopping * weight so the
+    reader's division by the degeneracy returns the hopping."""
     keys = sorted(terms)
+    deg = {k: 1 for k in keys} if degeneracy is None else degeneracy
     out = [name, f"{bands:12d}", f"{len(keys):12d}"]
-    degs = ["    1"] * len(keys)
+    degs = [f"{deg[k]:5d}" for k in keys]
     for i in range(0, len(degs), 15):
         out.append("".join(degs[i:i + 15]))
     for key in keys:
-        mat = terms[key]
+        mat = terms[key] * deg[key]
         for v in range(bands):
             for u in range(bands):
                 c = mat[u, v]

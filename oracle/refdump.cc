@@ -10,7 +10,7 @@
 // idlorbitalfile route, wannierfunctions.cc:489-498) padded with zero orbitals.
 //
 // usage: refdump <hrfile> <wfbin> <out> n kp os w eta efermi spin maxband layers
-//                lenergy henergy nscat [vre vim]...
+//                lenergy henergy scmodel nscat [vre vim]...
 // wfbin: int32 norb, int32 side, float64 [norb][side][side]
 // out:   per layer: float64 dos (tmatrix::calcdos), float64 ldos[y][x]
 #include <cstdio>
@@ -28,8 +28,8 @@ using namespace std;
 
 int main(int argc, char **argv)
 {
-    if (argc < 17) {
-        cerr << "usage: refdump hr wfbin out n kp os w eta efermi spin maxband layers lenergy henergy nscat [vre vim]..." << endl;
+    if (argc < 18) {
+        cerr << "usage: refdump hr wfbin out n kp os w eta efermi spin maxband layers lenergy henergy scmodel nscat [vre vim]..." << endl;
         return 2;
     }
     const char *hr = argv[1], *wfbin = argv[2], *outp = argv[3];
@@ -38,11 +38,12 @@ int main(int argc, char **argv)
     bool spin = atoi(argv[10]) != 0;
     size_t maxband = atoi(argv[11]), layers = atoi(argv[12]);
     double le = atof(argv[13]), he = atof(argv[14]);
-    int nscat = atoi(argv[15]);
+    bool scmodel = atoi(argv[15]) != 0;
+    int nscat = atoi(argv[16]);
     vector<complex<double> > scat;
-    for (int i = 0; i < nscat; i++) scat.push_back(complex<double>(atof(argv[16 + 2 * i]), atof(argv[17 + 2 * i])));
+    for (int i = 0; i < nscat; i++) scat.push_back(complex<double>(atof(argv[17 + 2 * i]), atof(argv[18 + 2 * i])));
 
-    tightbind *model = new tightbind(string(hr), efermi, false);
+    tightbind *model = new tightbind(string(hr), efermi, scmodel);
     if (!*model) { cerr << "model load failed" << endl; return 1; }
     FILE *f = fopen(wfbin, "rb");
     if (!f) return 1;

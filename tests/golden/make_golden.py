@@ -1,0 +1,224 @@
+"""Generate the golden fixtures under tests/golden/<case>/ from the reference itself.
+
+The reference ships no tests or example data, so its known answers are recorded here:
+for each case this script writes seeded inputs (a _hr.dat, an IDL orbital file or
+analytic orbital keywords, a calcqpi input file), runs the reference CLI built from its
+own sources (oracle/_ref/calcqpi, see oracle/build_ref.sh) and the float64 harness
+oracle/_ref/refdump, and stores:
+
+  model_hr.dat, orbitals.idl (when used), input.cfg   the inputs
+  ref_qpi.idl                                         the reference's output map (float32)
+  ref_wf.idl                                          the reference's wffile output (analytic cases)
+  ref_ldos64.npz                                      float64 maps + tmatrix::calcdos per layer
+  meta.json                                           the parameters
+
+Run from the repository root:  python tests/golden/make_golden.py
+(requires the reference sources, i.e. only in the build container).
+"""
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "calcqpi-release_gb300"))
+
+from cqpi import workloads as W  # noqa: E402
+from oracle import formats as F  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+
+def bdg_c1(delta=0.1):
+    """Two-band BdG form of the C1 model: electron block t(R), hole block -t(R),
+    on-site pairing delta (for scmodel=true)."""
+    base = W.square_c1().terms()
+    terms = {}
+    for R, M in base.items():
+        T = np.zeros((2, 2), complex)
+        T[0, 0] = M[0, 0]
+        T[1, 1] = -M[0, 0]
+        terms[R] = T
+    T0 = np.zeros((2, 2), complex)
+    T0[0, 1] = T0[1, 0] = delta
+    terms[(0, 0, 0)] = T0
+    return terms
+
+
+CASES = {
+    "c1_idl": dict(model="c1", deg=2, n=12, kp=32, os=4, w=2, layers=3, energies=(-0.2, 0.2), eta=0.05,
+                   scattering=(0.5,), orbitals=("idl", "gauss")),
+    "c2_analytic": dict(model="c2", n=8, kp=16, os=3, w=2, layers=2, energies=(-0.1, 0.1), eta=0.02,
+                        scattering=(0.3, 0.3, 0.5),
+                        orbitals=("analytic", dict(names=["dxz", "dyz", "dxy"], radius=0.4, zheight=0.6))),
+    "c3_spin": dict(model="c3", n=6, kp=12, os=2, w=1, layers=2, energies=(-0.05, 0.05), eta=0.02, spin=True,
+                    orbitals=("idl", "tri5")),
+    "edge_odd": dict(model="c1", fermi=0.1, phase=(0.5, 0.3), n=7, kp=12, os=3, w=1, layers=1,
+                     energies=(0.05, 0.3), eta=0.03,
+                     orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5, angle=30.0,
+                                                pos={0: (0.1, 0.2, 0.1)}, prearr=(0.8,)))),
+    "c2_pad": dict(model="c2", n=6, kp=16, os=2, w=1, layers=2, energies=(-0.1, 0.1), eta=0.02,
+                   scattering=(0.3, 0.3, 0.5), orbitals=("idl", "t2g2")),
+    "scmodel": dict(model="bdg", scmodel=True, magscat=0.25, n=8, kp=16, os=2, w=1, layers=2,
+                    energies=(-0.1, 0.1), eta=0.03, scattering=(0.5,),
+                    orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "wrap": dict(model="c1", n=20, kp=8, os=2, w=1, layers=1, energies=(0.1, 0.1), eta=0.05, scattering=(0.7,),
+                 orbitals=("analytic", dict(names=["px"], radius=0.35, zheight=0.4, angle=20.0))),
+}
+
+
+def model_terms(c):
+    if c["model"] == "c1":
+        m = W.square_c1()
+        return m.name, m.bands, m.terms()
+    if c["model"] == "c2":
+        m = W.t2g_c2()
+        return m.name, m.bands, m.terms()
+    if c["model"] == "c3":
+        m = W.triangular_c3()
+        return m.name, m.bands, m.terms()
+    if c["model"] == "bdg":
+        return "BdG square lattice (scmodel)", 2, bdg_c1()
+    raise KeyError(c["model"])
+
+
+def orbital_cube(kind, w, os_):
+    if kind == "gauss":
+        return W.gaussian_c1(w, os_)
+    if kind == "tri5":
+        return W.tri_orbitals_c3(w, os_)
+    if kind == "t2g2":
+        return W.t2g_orbitals_c2(w, os_)[:2]
+    raise KeyError(kind)
+
+
+def fmt_list(v):
+    return "(" + ",".join(repr(float(x)) for x in v) + ")"
+
+
+def make_case(name, c):
+    d = os.path.join(HERE, name)
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    mname, bands, terms = model_terms(c)
+    deg = None
+    if c.get("deg"):
+        deg = {k: c["deg"] for k in terms}
+    F.write_hr(os.path.join(d, "model_hr.dat"), mname, bands, terms, deg)
+    w, os_, n, kp = c["w"], c["os"], c["n"], c["kp"]
+    scmodel = c.get("scmodel", False)
+    spin = c.get("spin", False)
+    maxband = bands >> 1 if scmodel else bands
+    lines = ['tbfile="model_hr.dat";', 'qpifile="ref_qpi.idl";', "output=wannier;",
+             f"lattice={n};", f"kpoints={kp};", f"oversamp={os_};", f"window={w};", f"layers={c['layers']};",
+             f"energies={fmt_list(c['energies'])};", f"eta={c['eta']!r};"]
+    if "fermi" in c:
+        lines.append(f"fermi={c['fermi']!r};")
+    if "phase" in c:
+        lines.append(f"phase={fmt_list(c['phase'])};")
+    if "scattering" in c:
+        lines.append(f"scattering={fmt_list(c['scattering'])};")
+    if spin:
+        lines.append("spin=true;")
+    if scmodel:
+        lines.append("scmodel=true;")
+        lines.append(f"magscat={c['magscat']!r};")
+    kind, spec = c["orbitals"]
+    side = (2 * w + 1) * os_
+    if kind == "idl":
+        cube = orbital_cube(spec, w, os_).astype(np.float32)
+        # file layout data[x][y][orbital] written x fastest (idl.cc:78-97): [orb][y][x]
+        F.write_idl(os.path.join(d, "orbitals.idl"), np.ascontiguousarray(np.transpose(cube, (0, 2, 1))),
+                    "orbital cube", scan_range=(1.0, 1.0), offset=(0.0, 0.0), bias=(0.0, 0.0),
+                    date="Thu Jan  1 00:00:00 2026")
+        lines.append('idlorbitalfile="orbitals.idl";')
+        wf64 = cube.astype(np.float64)
+        if spin and (maxband >> 1) == wf64.shape[0]:
+            wf64 = np.concatenate([wf64, wf64])
+        zero = np.zeros(max(maxband, wf64.shape[0]), np.uint8)
+        if wf64.shape[0] < maxband:
+            zero[wf64.shape[0]:] = 1
+            wf64 = np.concatenate([wf64, np.zeros((maxband - wf64.shape[0], side, side))])
+    else:
+        names = spec["names"]
+        lines.append("orbitals=(" + ",".join(names) + ");")
+        lines.append(f"radius={spec['radius']!r};")
+        lines.append(f"zheight={spec['zheight']!r};")
+        if "angle" in spec:
+            lines.append(f"angle={spec['angle']!r};")
+        for i, p in spec.get("pos", {}).items():
+            lines.append(f"pos[{i}]={fmt_list(p)};")
+        if "prearr" in spec:
+            lines.append(f"prearr={fmt_list(spec['prearr'])};")
+        lines.append('wffile="ref_wf.idl";')
+        cubes = []
+        for i, nm in enumerate(names):
+            pos = spec.get("pos", {}).get(i, (0.0, 0.0, 0.0))
+            pre = spec.get("prearr", (1.0,) * len(names))[i] if i < len(spec.get("prearr", ())) else 1.0
+            cubes.append(O.orbital_cache(nm, w, os_, width=spec["radius"], height=spec["zheight"] - pos[2],
+                                         xpos=pos[0], ypos=pos[1],
+                                         theta=spec.get("angle", 0.0) * np.pi / 180.0, prefact=pre))
+        wf64 = np.stack(cubes)
+        zero = np.zeros(max(maxband, wf64.shape[0]), np.uint8)
+        if spin and (maxband >> 1) == len(names):
+            wf64 = np.concatenate([wf64, wf64])
+        elif wf64.shape[0] < maxband:
+            zero[wf64.shape[0]:] = 1
+            wf64 = np.concatenate([wf64, np.zeros((maxband - wf64.shape[0], side, side))])
+    with open(os.path.join(d, "input.cfg"), "w") as fh:
+        fh.write("# golden case %s (generated by tests/golden/make_golden.py)\n" % name)
+        fh.write("\n".join(lines) + "\n")
+    # reference CLI
+    r = subprocess.run([os.path.join(REF, "calcqpi"), "input.cfg"], cwd=d, capture_output=True, text=True,
+                       timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError(f"{name}: reference failed\n{r.stdout}\n{r.stderr}")
+    # float64 harness
+    scat = [complex(v) for v in c.get("scattering", ())]
+    phase = complex(*c.get("phase", (1.0, 0.0)))
+    scat = [s * phase for s in scat]
+    if scmodel and len(scat) == maxband:
+        scat = scat + [(-1.0 + 2.0 * c["magscat"]) * s for s in scat]
+    vscat = [scat[i] if i < len(scat) else 0j for i in range(bands)] if scat else [phase] * bands
+    wfbin = os.path.join(d, "_wf.bin")
+    with open(wfbin, "wb") as fh:
+        fh.write(np.array([wf64.shape[0], side], np.int32).tobytes())
+        fh.write(np.ascontiguousarray(wf64 * (1 - zero[:wf64.shape[0], None, None])).tobytes())
+    outbin = os.path.join(d, "_ldos.bin")
+    args = [os.path.join(REF, "refdump"), os.path.join(d, "model_hr.dat"), wfbin, outbin, str(n), str(kp), str(os_),
+            str(w), repr(c["eta"]), repr(c.get("fermi", 0.0)), str(int(spin)), str(maxband), str(c["layers"]),
+            repr(c["energies"][0]), repr(c["energies"][1]), str(int(scmodel)), str(len(vscat))]
+    for v in vscat:
+        args += [repr(v.real), repr(v.imag)]
+    r2 = subprocess.run(args, capture_output=True, text=True, timeout=600)
+    if r2.returncode != 0:
+        raise RuntimeError(f"{name}: refdump failed\n{r2.stderr}")
+    wn = n * os_
+    raw = np.fromfile(outbin, np.float64).reshape(c["layers"], 1 + wn * wn)
+    np.savez_compressed(os.path.join(d, "ref_ldos64.npz"), dos=raw[:, 0], ldos=raw[:, 1:].reshape(-1, wn, wn),
+                        vscat=np.array(vscat), wf=wf64, zero=zero)
+    os.remove(wfbin)
+    os.remove(outbin)
+    meta = dict(c)
+    meta["bands"] = bands
+    meta["maxband"] = maxband
+    meta["orbitals"] = [kind, spec]
+    with open(os.path.join(d, "meta.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, default=str)
+    with open(os.path.join(d, "ref_stdout.txt"), "w") as fh:
+        fh.write(r.stdout + r.stderr)
+    print(name, "ok", wn, "x", wn, "x", c["layers"])
+
+
+if __name__ == "__main__":
+    if not os.path.exists(os.path.join(REF, "calcqpi")):
+        subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
+    for nm in (sys.argv[1:] or CASES):
+        make_case(nm, CASES[nm])

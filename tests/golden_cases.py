@@ -1,0 +1,24 @@
+"""Loader for the golden fixtures written by tests/golden/make_golden.py."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+NAMES = sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)) and not d.startswith("_"))
+
+
+def load(name):
+    d = os.path.join(GOLDEN, name)
+    with open(os.path.join(d, "meta.json")) as fh:
+        meta = json.load(fh)
+    z = np.load(os.path.join(d, "ref_ldos64.npz"))
+    return d, meta, {k: z[k] for k in z.files}
+
+
+def energies(meta):
+    lo, hi = meta["energies"]
+    L = meta["layers"]
+    if L == 1:
+        return np.array([lo])
+    return np.array([(hi - lo) * k / (L - 1.0) + lo for k in range(L)])

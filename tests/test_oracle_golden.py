@@ -1,0 +1,99 @@
+"""Pin the oracle to the reference: golden outputs of the reference's own sources."""
+import os
+
+import numpy as np
+import pytest
+
+from golden_cases import NAMES, energies, load
+from oracle import formats as F
+from oracle import oracle as O
+
+
+def _model(d, meta):
+    with open(os.path.join(d, "model_hr.dat")) as fh:
+        hr = F.read_hr(fh.read(), scmodel=meta.get("scmodel", False))
+    return O.Model.from_hr(hr, efermi=meta.get("fermi", 0.0))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference_float64(name):
+    d, meta, ref = load(name)
+    m = _model(d, meta)
+    E = energies(meta)
+    maps = O.run(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], E, ref["vscat"], ref["wf"],
+                 ref["zero"], m=meta["maxband"], spin=meta.get("spin", False))
+    err = np.abs(maps - ref["ldos"]).max() / np.abs(ref["ldos"]).max()
+    assert err < 1e-10, err
+    # tmatrix::calcdos = -sum_i<maxband Im G0(R=0)_ii  (src/qpi.cc:856-862)
+    ev, U = O.bands(m, meta["kp"])
+    for k, e in enumerate(E):
+        g00 = O.realspace(O.greens_k(ev, U, meta["kp"], e, meta["eta"]))[0, 0]
+        dos = -np.imag(np.diag(g00))[:meta["maxband"]].sum()
+        assert abs(dos - ref["dos"][k]) < 1e-12 * max(1.0, abs(ref["dos"][k]))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference_cli_float32(name):
+    d, meta, ref = load(name)
+    hdr, data = F.read_idl(os.path.join(d, "ref_qpi.idl"))
+    wn = meta["n"] * meta["os"]
+    assert hdr["size"] == (wn, wn, meta["layers"])
+    # the CLI's float32 map is the float64 map rounded (src/idl.cc:90-92)
+    assert np.array_equal(data, ref["ldos"].astype(np.float32)) or \
+        np.abs(data - ref["ldos"]).max() <= 2e-7 * np.abs(ref["ldos"]).max()
+
+
+def test_numpy_restatement_matches_reference():
+    for name in ["c2_pad", "edge_odd", "scmodel"]:
+        d, meta, ref = load(name)
+        m = _model(d, meta)
+        E = energies(meta)
+        for k, e in enumerate(E):
+            g0r = O.np_greens_r(m, meta["kp"], e, meta["eta"])
+            T = O.tmatrix(ref["vscat"], g0r[0, 0])
+            got = O.np_wannier_ldos(meta["n"], meta["kp"], meta["os"], meta["w"], meta["maxband"],
+                                    meta.get("spin", False), T, g0r, ref["wf"], ref["zero"]).T
+            err = np.abs(got - ref["ldos"][k]).max() / np.abs(ref["ldos"][k]).max()
+            assert err < 1e-10, (name, err)
+
+
+@pytest.mark.parametrize("name", [n for n in NAMES if os.path.exists(os.path.join(
+    os.path.dirname(os.path.abspath(__file__)), "golden", n, "ref_wf.idl"))])
+def test_orbital_cache_matches_reference(name):
+    d, meta, ref = load(name)
+    hdr, data = F.read_idl(os.path.join(d, "ref_wf.idl"))
+    norb = ref["wf"].shape[0]
+    cube = np.transpose(data, (0, 2, 1))[:norb]   # file [orb][y][x] -> [orb][x][y]
+    assert np.abs(cube - ref["wf"].astype(np.float32)).max() <= 1e-7 * max(np.abs(ref["wf"]).max(), 1e-30)
+    assert hdr["name"].startswith("Wannier function file for model_hr.dat with window=")
+
+
+def test_idl_writer_reproduces_reference_bytes():
+    for name in NAMES:
+        d, meta, ref = load(name)
+        path = os.path.join(d, "ref_qpi.idl")
+        hdr, data = F.read_idl(path)
+        tmp = os.path.join(d, "_tmp.idl")
+        try:
+            F.write_idl(tmp, data, hdr["name"], hdr["scan_range"], hdr["offset"], hdr["bias"], hdr["setpoint"],
+                        date=hdr["date"])
+            with open(tmp, "rb") as a, open(path, "rb") as b:
+                assert a.read() == b.read()
+        finally:
+            os.remove(tmp)
+
+
+def test_config_restatement_reads_inputs():
+    d, meta, ref = load("edge_odd")
+    with open(os.path.join(d, "input.cfg")) as fh:
+        lf = F.LoadConfig(fh.read())
+    assert lf.getintvalue("lattice") == meta["n"]
+    assert lf.getvector("phase") == [0.5, 0.3]
+    assert lf.getstring("tbfile") == "model_hr.dat"
+    assert lf.getlist("orbitals") == ["s"]
+    assert lf.getvector("pos[0]") == [0.1, 0.2, 0.1]
+    assert "wffile" in lf.unused()
+    bad = F.LoadConfig("lattice=3\nx = 4;\n# c=1;\nkpoints=8;\nkpoints=16;\n")
+    assert bad.warnings == ["lattice=3"]
+    assert not bad.probefield("x")          # keys are not trimmed (include/parser.h:44)
+    assert bad.getintvalue("kpoints") == 16  # the last value wins (include/parser.h:117-121)
