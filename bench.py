@@ -274,18 +274,41 @@ def run_ours(args):
         peak = cqpi.measure_fma_peak("fp64")
         roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "peak_source": "measured DFMA loop (cqpi_measure_fma_peak), not in MEASURED_PEAKS.json"}
-    else:
+    elif eng.contraction_kind() == "tcgen05":
         peak = peaks.get("bf16_tflops", 1900.0)
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "peak_source": f"bf16 burst, {peak_src}"}
+                "peak_source": f"bf16 dense burst, {peak_src} (fp16 kind::f16 runs at the same rate)"}
+    else:
+        peak = cqpi.measure_fma_peak("fp32")
+        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "measured FFMA loop (cqpi_measure_fma_peak), not in MEASURED_PEAKS.json"}
     roof["kernel"] = "ldos contraction"
     roof["flop_per_pixel_energy"] = F
     roof["traffic"] = None
     roof["stage_ms_per_step"] = {k: v / args.steps for k, v in stage_acc.items()}
 
+    # accuracy and speed of the all-FP64 path on the same workload (the metric's comparison)
+    fp64_info = None
+    if prec != cqpi.PREC_FP64 and not args.no_fp64_check:
+        sub = np.linspace(0, nE - 1, 5).astype(int)
+        with cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, spin=c.spin,
+                         precision=cqpi.PREC_FP64) as e64:
+            e64.set_orbitals(wf)
+            e64.set_scattering(vscat)
+            ref = e64.run(E[sub], f32=False, f64=True)
+            t0 = time.perf_counter()
+            e64.solve_bands()
+            e64.run(E[sub], f32=False, f64=False)
+            t64 = time.perf_counter() - t0
+        got = out[sub].double().cpu().numpy()
+        errs = [float(np.abs(got[i, 0] - ref[i, 0]).max() / np.abs(ref[i, 0]).max()) for i in range(len(sub))]
+        fp64_value = len(sub) * c.pixels_per_energy / t64
+        fp64_info = {"max_rel_err_vs_fp64": max(errs), "energies_checked": [float(x) for x in E[sub]],
+                     "tolerance": 1e-6, "fp64_path_value": fp64_value, "mixed_over_fp64": value / world / fp64_value}
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == cqpi.PREC_FP64 else "mixed(f64 eigen/T, tf32x3/f32)",
+            "vs_baseline": None, "dtype": "f64" if prec == cqpi.PREC_FP64 else f"mixed: f64 eigen/T/term1, f32 G0+FFT, {eng.contraction_kind()} contraction",
             "data": "synthetic (seeded model and orbitals)",
             "config": {"workload": f"{args.config}: t2g 3-orbital square lattice, k-grid {c.kpoints}^2, "
                                    f"FOV {c.lattice}^2 sites, {c.oversamp}x{c.oversamp} px/cell, {nE} energies, "
@@ -294,6 +317,8 @@ def run_ours(args):
                        "l2": "inputs/outputs larger than L2 (2.6 GB of maps, 168 MB eigen cache per step)"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "roofline": roof}
+    if fp64_info is not None:
+        line["accuracy"] = fp64_info
     if clk is not None:
         line["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -314,9 +339,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="C2")
-    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -23,6 +23,7 @@ EXPORTED = [
     "cqpi_set_orbitals", "cqpi_set_scattering", "cqpi_set_impurities", "cqpi_solve_bands", "cqpi_run",
     "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
+    "cqpi_contraction_kind",
 ]
 
 
@@ -82,6 +83,7 @@ def load():
     L.cqpi_kernel_launches.argtypes = [P, ctypes.POINTER(i64)]
     L.cqpi_stage_times.argtypes = [P, P]
     L.cqpi_measure_fma_peak.argtypes = [i32, ctypes.POINTER(dbl)]
+    L.cqpi_contraction_kind.argtypes = [P, ctypes.POINTER(i32)]
     _lib = L
     return L
 
@@ -234,6 +236,12 @@ class Engine:
         c = ctypes.c_int64()
         self._check(self._L.cqpi_kernel_launches(self._h, ctypes.byref(c)))
         return c.value
+
+    def contraction_kind(self) -> str:
+        """Which contraction kernel the handle uses: 'fp64', 'fp32' (CUDA cores) or 'tcgen05'."""
+        k = ctypes.c_int32()
+        self._check(self._L.cqpi_contraction_kind(self._h, ctypes.byref(k)))
+        return {0: "fp64", 1: "fp32", 2: "tcgen05"}[k.value]
 
     def stage_times(self):
         t = np.zeros(5, np.float32)

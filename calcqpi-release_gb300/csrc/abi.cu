@@ -68,13 +68,16 @@ void free_workspace(cqpi_handle *h)
     dfree(h->ws.energies);
     dfree(h->ws.g0k32);
     dfree(h->ws.half32);
+    dfree(h->ws.box32);
+    dfree(h->ws.T32);
     h->ws.ebatch = 0;
 }
 
 size_t bytes_per_energy(const cqpi_handle *h)
 {
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
-    return 16 * (bb * nk + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
+    const size_t cs = (h->precision == CQPI_PREC_FP64) ? 16 : 8;
+    return cs * (bb * nk + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
 }
 
 void ensure_workspace(cqpi_handle *h, int ebatch)
@@ -82,13 +85,26 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
     if (h->ws.ebatch >= ebatch) return;
     free_workspace(h);
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
-    dalloc(&h->ws.g0k, ebatch * bb * nk);
-    dalloc(&h->ws.half, ebatch * bb * (size_t)h->kp * h->NB);
-    dalloc(&h->ws.box, ebatch * (size_t)h->NB * h->NB * bb);
+    if (h->precision == CQPI_PREC_FP64) {
+        dalloc(&h->ws.g0k, ebatch * bb * nk);
+        dalloc(&h->ws.half, ebatch * bb * (size_t)h->kp * h->NB);
+        dalloc(&h->ws.box, ebatch * (size_t)h->NB * h->NB * bb);
+    } else {
+        dalloc(&h->ws.g0k32, ebatch * bb * nk);
+        dalloc(&h->ws.half32, ebatch * bb * (size_t)h->kp * h->NB);
+        dalloc(&h->ws.box32, ebatch * (size_t)h->NB * h->NB * bb);
+    }
     dalloc(&h->ws.T, ebatch * (size_t)std::max(h->nimp, 1) * bb);
+    dalloc(&h->ws.T32, ebatch * (size_t)std::max(h->nimp, 1) * bb);
     dalloc(&h->ws.term1, ebatch * (size_t)h->Q);
     dalloc(&h->ws.energies, ebatch);
     h->ws.ebatch = ebatch;
+}
+
+void launch_contraction(cqpi_handle *h, int ne, float *o32, double *o64)
+{
+    if (h->precision == CQPI_PREC_FP64) launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
+    else launch_ldos_fp32(h, ne, h->ws.box32, h->ws.T32, h->ws.term1, o32, o64);
 }
 
 int choose_batch(const cqpi_handle *h, int nE)
@@ -270,6 +286,13 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         const size_t nk = (size_t)h->kp * h->kp;
         dalloc(&h->d_eval, nk * b);
         dalloc(&h->d_evec, nk * bb);
+        if (h->precision == CQPI_PREC_MIXED) {
+            dalloc(&h->d_evec32, nk * bb);
+            std::vector<float2> tw32(h->kp);
+            for (int t = 0; t < h->kp; t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
+            dalloc(&h->d_tw32, h->kp);
+            CK(cudaMemcpy(h->d_tw32, tw32.data(), sizeof(float2) * h->kp, cudaMemcpyHostToDevice));
+        }
         dalloc(&h->d_status, 1);
         CK(cudaMemset(h->d_status, 0, sizeof(int)));
         // default scattering: phase (1,0) on every band (src/qpi.h:99)
@@ -304,7 +327,12 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_tw32);
     dfree(h->d_eval);
     dfree(h->d_evec);
+    dfree(h->d_evec32);
     dfree(h->d_phi);
+    dfree(h->d_phi32);
+    dfree(h->d_seam_box);
+    dfree(h->d_seam_T);
+    dfree(h->d_seam_term1);
     dfree(h->d_V);
     dfree(h->d_status);
     dfree(h->d_seam_ldos);
@@ -342,6 +370,10 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
         dfree(h->d_phi);
         dalloc(&h->d_phi, phi.size());
         CK(cudaMemcpy(h->d_phi, phi.data(), sizeof(double) * phi.size(), cudaMemcpyHostToDevice));
+        std::vector<float> phi32(phi.begin(), phi.end());
+        dfree(h->d_phi32);
+        dalloc(&h->d_phi32, phi32.size());
+        CK(cudaMemcpy(h->d_phi32, phi32.data(), sizeof(float) * phi32.size(), cudaMemcpyHostToDevice));
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
@@ -424,7 +456,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             CK(cudaEventRecord(h->ev[4], h->stream));
             float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : stage32) : nullptr;
             double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : stage64) : nullptr;
-            launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
+            launch_contraction(h, ne, o32, o64);
             check_launch();
             CK(cudaEventRecord(h->ev[5], h->stream));
             if (!on_device) {
@@ -494,9 +526,16 @@ int cqpi_get_greens_box(cqpi_handle *h, double energy, double *box, int32_t *rb)
         if (!h->bands_ready) do_bands(h);
         CK(cudaMemcpyAsync(h->ws.energies, &energy, sizeof(double), cudaMemcpyHostToDevice, h->stream));
         do_greens(h, 1);
-        CK(cudaMemcpyAsync(box, h->ws.box, sizeof(double2) * (size_t)h->NB * h->NB * h->b * h->b, cudaMemcpyDeviceToHost,
-                           h->stream));
-        CK(cudaStreamSynchronize(h->stream));
+        const size_t cnt = (size_t)h->NB * h->NB * h->b * h->b;
+        if (h->precision == CQPI_PREC_FP64) {
+            CK(cudaMemcpyAsync(box, h->ws.box, sizeof(double2) * cnt, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        } else {
+            std::vector<float2> t(cnt);
+            CK(cudaMemcpyAsync(t.data(), h->ws.box32, sizeof(float2) * cnt, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            for (size_t i = 0; i < cnt; i++) { box[2 * i] = t[i].x; box[2 * i + 1] = t[i].y; }
+        }
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
@@ -537,16 +576,20 @@ int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r)
         }
     }
     try {
-        ensure_workspace(h, 1);
-        if (!h->d_seam_ldos) dalloc(&h->d_seam_ldos, (size_t)h->wn * h->wn);
-        CK(cudaMemcpyAsync(h->ws.box, box.data(), sizeof(double2) * box.size(), cudaMemcpyHostToDevice, h->stream));
-        CK(cudaMemcpyAsync(h->ws.T, T, sizeof(double2) * bb, cudaMemcpyHostToDevice, h->stream));
+        if (!h->d_seam_ldos) {
+            dalloc(&h->d_seam_ldos, (size_t)h->wn * h->wn);
+            dalloc(&h->d_seam_box, box.size());
+            dalloc(&h->d_seam_T, bb);
+            dalloc(&h->d_seam_term1, (size_t)h->Q);
+        }
+        CK(cudaMemcpyAsync(h->d_seam_box, box.data(), sizeof(double2) * box.size(), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_seam_T, T, sizeof(double2) * bb, cudaMemcpyHostToDevice, h->stream));
         CK(cudaStreamSynchronize(h->stream));   // 'box' is a pageable temporary
         const int saved = h->nimp;
         h->nimp = 1;
-        launch_term1(h, 1);
+        launch_term1_ptr(h, 1, h->d_seam_box, h->d_seam_term1);
         check_launch();
-        launch_ldos_fp64(h, 1, h->ws.box, h->ws.T, h->ws.term1, nullptr, h->d_seam_ldos);
+        launch_ldos_fp64(h, 1, h->d_seam_box, h->d_seam_T, h->d_seam_term1, nullptr, h->d_seam_ldos);
         h->nimp = saved;
         check_launch();
         h->seam_pending = true;
@@ -588,6 +631,13 @@ int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count)
 {
     if (!h || !count) return CQPI_ERR_ARG;
     *count = h->launches;
+    return CQPI_OK;
+}
+
+int cqpi_contraction_kind(const cqpi_handle *h, int32_t *kind)
+{
+    if (!h || !kind) return CQPI_ERR_ARG;
+    *kind = (h->precision == CQPI_PREC_FP64) ? 0 : 1;
     return CQPI_OK;
 }
 

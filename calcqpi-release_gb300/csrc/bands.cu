@@ -16,7 +16,7 @@ template <int B>
 __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, double efermi, int nR,
                                                     const int32_t *__restrict__ R, const double2 *__restrict__ tn,
                                                     const double2 *__restrict__ ta, double *__restrict__ eval,
-                                                    double2 *__restrict__ evec)
+                                                    double2 *__restrict__ evec, float2 *__restrict__ evec32)
 {
     const long long nk = (long long)kp * kp;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,7 +109,10 @@ __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, do
     for (int o = 0; o < B; o++)
 #pragma unroll
         for (int n = 0; n < B; n++)
-            if (o < b && n < b) evec[(size_t)(o * b + n) * nk + k] = make_double2(vr[o][n], vi[o][n]);
+            if (o < b && n < b) {
+                evec[(size_t)(o * b + n) * nk + k] = make_double2(vr[o][n], vi[o][n]);
+                if (evec32) evec32[(size_t)(o * b + n) * nk + k] = make_float2((float)vr[o][n], (float)vi[o][n]);
+            }
 }
 
 template <int B>
@@ -118,7 +121,7 @@ static void launch_bands_t(cqpi_handle *h)
     const long long nk = (long long)h->kp * h->kp;
     bands_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, h->kp, h->scmax, h->efermi, h->nR, h->d_R,
                                                           (const double2 *)h->d_tn, (const double2 *)h->d_ta,
-                                                          h->d_eval, h->d_evec);
+                                                          h->d_eval, h->d_evec, h->d_evec32);
     h->launches++;
 }
 

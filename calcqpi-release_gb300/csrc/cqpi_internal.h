@@ -39,6 +39,8 @@ struct Workspace {
     double *energies = nullptr;
     float2 *g0k32 = nullptr;
     float2 *half32 = nullptr;
+    float2 *box32 = nullptr;
+    float2 *T32 = nullptr;
 };
 
 }  // namespace cqpi
@@ -60,12 +62,14 @@ struct cqpi_handle {
     // eigen cache
     double *d_eval = nullptr;
     double2 *d_evec = nullptr;
+    float2 *d_evec32 = nullptr;   // FP32 copy for the mixed path
     bool bands_ready = false;
     // twiddles e^{+2 pi i t / kp}
     double2 *d_tw = nullptr;
     float2 *d_tw32 = nullptr;
     // orbitals
     double *d_phi = nullptr;
+    float *d_phi32 = nullptr;
     bool orbitals_ready = false;
     // impurities
     int nimp = 0;
@@ -73,8 +77,10 @@ struct cqpi_handle {
     // workspace
     cqpi::Workspace ws;
     int *d_status = nullptr;
-    // narrow seam
+    // narrow seam (always FP64)
     double *d_seam_ldos = nullptr;
+    double2 *d_seam_box = nullptr, *d_seam_T = nullptr;
+    double *d_seam_term1 = nullptr;
     bool seam_pending = false;
     // accounting
     int64_t launches = 0;
@@ -93,8 +99,11 @@ void launch_fft(cqpi_handle *h, int ne);
 cudaError_t configure_fft(cqpi_handle *h);
 void launch_tmatrix(cqpi_handle *h, int ne);
 void launch_term1(cqpi_handle *h, int ne);
+void launch_term1_ptr(cqpi_handle *h, int ne, const double2 *box, double *term1);
 // ldos.cu
 void launch_ldos_fp64(cqpi_handle *h, int ne, const double2 *box, const double2 *T, const double *term1,
+                      float *out32, double *out64);
+void launch_ldos_fp32(cqpi_handle *h, int ne, const float2 *box, const float2 *T, const double *term1,
                       float *out32, double *out64);
 
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }

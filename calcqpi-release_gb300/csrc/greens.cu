@@ -1,9 +1,11 @@
-// greens.cu -- per-energy Green's function stages (FP64 path).
+// greens.cu -- per-energy Green's function stages, FP64 (double2) and mixed (float2).
 //
 //  greens_k   G0(k,w) = sum_n U_n U_n^H / (w - e_n + i eta) for every k and every
 //             energy of the batch; replaces tmatrix::setgreensfunction +
 //             tightbind::calcgreensfunction (src/qpi.cc:478-486,
-//             src/tightbinding.cc:282-289).  HBM-bound (reads the eigen cache).
+//             src/tightbinding.cc:282-289).  w - e_n is always formed in FP64 (the
+//             pole distance needs it at small eta); the mixed path then works in FP32.
+//             HBM-bound (reads the eigen cache, writes the G0(k) planes).
 //  fft        G0(R) = kp^-2 sum_k G0(k) e^{+2 pi i k.R} on the pruned box
 //             R in [-Rb, Rb]^2 only (Rb = lattice/2 + window); replaces the b^2
 //             full FFTW transforms of tmatrix::calcrealspacegreensfunction
@@ -12,53 +14,53 @@
 //             shared memory for power-of-two kp, a pruned direct DFT otherwise.
 //  tmatrix    T = (1 - V G0(R=0))^-1 V in FP64 per energy and impurity
 //             (tmatrix::setscatteringmatrix, src/qpi.cc:833-854).
-//  term1      the site-independent part of the LDOS,
+//  term1      the site-independent part of the LDOS in FP64,
 //             sum_{d1,d2,o1,o2} phi_o1(q,d1) phi_o2(q,d2) Im G0(d2-d1)[o2][o1]
 //             (second accumulation of src/qpi.cc:921).
+#include "cplx.h"
 #include "cqpi_internal.h"
 
 namespace cqpi {
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-
 // ------------------------------------------------------------------ G0(k,w)
-template <int B>
+template <int B, class C>
 __global__ void __launch_bounds__(256) greens_k_kernel(int b, long long nk, double eta, const double *__restrict__ energies,
-                                                       const double *__restrict__ eval, const double2 *__restrict__ evec,
-                                                       double2 *__restrict__ g0k)
+                                                       const double *__restrict__ eval, const C *__restrict__ evec,
+                                                       C *__restrict__ g0k)
 {
+    using R = typename real_of<C>::type;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nk) return;
     const int e = blockIdx.y;
     const double omega = energies[e];
     const int bb = b * b;
-    double2 f[B];
+    C f[B];
 #pragma unroll
     for (int n = 0; n < B; n++) {
         if (n < b) {
-            double dr = omega - eval[(size_t)n * nk + k];
-            double den = dr * dr + eta * eta;
-            f[n] = make_double2(dr / den, -eta / den);
+            const R dr = (R)(omega - eval[(size_t)n * nk + k]);   // FP64 difference, then rounded
+            const R et = (R)eta;
+            const R den = dr * dr + et * et;
+            f[n].x = dr / den;
+            f[n].y = -et / den;
         }
     }
-    double2 *out = g0k + (size_t)e * bb * nk + k;
+    C *out = g0k + (size_t)e * bb * nk + k;
 #pragma unroll
     for (int o = 0; o < B; o++) {
         if (o >= b) continue;
-        double2 x[B];
+        C x[B];
 #pragma unroll
         for (int n = 0; n < B; n++)
             if (n < b) x[n] = cmul(evec[(size_t)(o * b + n) * nk + k], f[n]);
 #pragma unroll
         for (int a = 0; a < B; a++) {
             if (a >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
+            C s = cmake<C>(0.0, 0.0);
 #pragma unroll
             for (int n = 0; n < B; n++) {
                 if (n < b) {
-                    double2 u = evec[(size_t)(a * b + n) * nk + k];
+                    const C u = evec[(size_t)(a * b + n) * nk + k];
                     s.x += x[n].x * u.x + x[n].y * u.y;   // x * conj(u)
                     s.y += x[n].y * u.x - x[n].x * u.y;
                 }
@@ -73,7 +75,12 @@ static void launch_greens_k_t(cqpi_handle *h, int ne, const double *d_energies)
 {
     const long long nk = (long long)h->kp * h->kp;
     dim3 grid(cdiv(nk, 256), ne);
-    greens_k_kernel<B><<<grid, 256, 0, h->stream>>>(h->b, nk, h->eta, d_energies, h->d_eval, h->d_evec, h->ws.g0k);
+    if (h->precision == CQPI_PREC_FP64)
+        greens_k_kernel<B, double2><<<grid, 256, 0, h->stream>>>(h->b, nk, h->eta, d_energies, h->d_eval, h->d_evec,
+                                                                  h->ws.g0k);
+    else
+        greens_k_kernel<B, float2><<<grid, 256, 0, h->stream>>>(h->b, nk, h->eta, d_energies, h->d_eval, h->d_evec32,
+                                                                 h->ws.g0k32);
     h->launches++;
 }
 
@@ -96,14 +103,16 @@ __device__ __forceinline__ int bitrev(int x, int bits) { return bits == 0 ? 0 : 
 __device__ __forceinline__ int posmod(int a, int m) { int r = a % m; return r < 0 ? r + m : r; }
 
 // Pass 1: rows (fixed i, plane, energy), transform along j, keep Y = yb - Rb for yb < NB.
+template <class C>
 __global__ void __launch_bounds__(256) fft_rows_kernel(int kp, int logkp, int NB, int Rb, int bb, long long nk,
-                                                       const double2 *__restrict__ g0k, const double2 *__restrict__ tw,
-                                                       double2 *__restrict__ half)
+                                                       const C *__restrict__ g0k, const C *__restrict__ tw,
+                                                       C *__restrict__ half)
 {
-    extern __shared__ double2 sm[];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
     const int i = blockIdx.x, pl = blockIdx.y, e = blockIdx.z;
-    const double2 *src = g0k + ((size_t)e * bb + pl) * nk + (size_t)i * kp;
-    double2 *dst = half + (((size_t)e * bb + pl) * kp + i) * NB;
+    const C *src = g0k + ((size_t)e * bb + pl) * nk + (size_t)i * kp;
+    C *dst = half + (((size_t)e * bb + pl) * kp + i) * NB;
     if (logkp >= 0) {
         for (int j = threadIdx.x; j < kp; j += blockDim.x) sm[bitrev(j, logkp)] = src[j];
         __syncthreads();
@@ -111,8 +120,8 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(int kp, int logkp, int NB
             const int hl = len >> 1, step = kp / len;
             for (int t = threadIdx.x; t < (kp >> 1); t += blockDim.x) {
                 const int idx = (t / hl) * len + (t % hl);
-                const double2 w = __ldg(tw + (t % hl) * step);
-                const double2 u = sm[idx], v = cmul(sm[idx + hl], w);
+                const C w = tw[(t % hl) * step];
+                const C u = sm[idx], v = cmul(sm[idx + hl], w);
                 sm[idx] = cadd(u, v);
                 sm[idx + hl] = csub(u, v);
             }
@@ -124,56 +133,57 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(int kp, int logkp, int NB
         __syncthreads();
         for (int yb = threadIdx.x; yb < NB; yb += blockDim.x) {
             const int ym = posmod(yb - Rb, kp);
-            double2 s = make_double2(0.0, 0.0);
-            for (int j = 0; j < kp; j++) s = cadd(s, cmul(sm[j], __ldg(tw + (int)(((long long)j * ym) % kp))));
+            C s = cmake<C>(0.0, 0.0);
+            for (int j = 0; j < kp; j++) s = cadd(s, cmul(sm[j], tw[(int)(((long long)j * ym) % kp)]));
             dst[yb] = s;
         }
     }
 }
 
-// Pass 2: C adjacent columns yb (fixed plane, energy), transform along i, keep X = xb - Rb.
-__global__ void __launch_bounds__(256) fft_cols_kernel(int kp, int logkp, int NB, int Rb, int bb, int C, double scale,
-                                                       const double2 *__restrict__ half, const double2 *__restrict__ tw,
-                                                       double2 *__restrict__ box)
+// Pass 2: NC adjacent columns yb (fixed plane, energy), transform along i, keep X = xb - Rb.
+template <class C>
+__global__ void __launch_bounds__(256) fft_cols_kernel(int kp, int logkp, int NB, int Rb, int bb, int NC, double scale,
+                                                       const C *__restrict__ half, const C *__restrict__ tw,
+                                                       C *__restrict__ box)
 {
-    extern __shared__ double2 sm[];
-    const int yb0 = blockIdx.x * C, pl = blockIdx.y, e = blockIdx.z;
-    const double2 *src = half + ((size_t)e * bb + pl) * (size_t)kp * NB;
-    double2 *dst = box + (size_t)e * NB * NB * bb;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    const int yb0 = blockIdx.x * NC, pl = blockIdx.y, e = blockIdx.z;
+    const C *src = half + ((size_t)e * bb + pl) * (size_t)kp * NB;
+    C *dst = box + (size_t)e * NB * NB * bb;
     const bool pow2 = logkp >= 0;
-    for (int idx = threadIdx.x; idx < kp * C; idx += blockDim.x) {
-        const int i = idx / C, c = idx % C, yb = yb0 + c;
+    for (int idx = threadIdx.x; idx < kp * NC; idx += blockDim.x) {
+        const int i = idx / NC, c = idx % NC, yb = yb0 + c;
         const int pos = pow2 ? bitrev(i, logkp) : i;
-        sm[pos * C + c] = (yb < NB) ? src[(size_t)i * NB + yb] : make_double2(0.0, 0.0);
+        sm[pos * NC + c] = (yb < NB) ? src[(size_t)i * NB + yb] : cmake<C>(0.0, 0.0);
     }
     __syncthreads();
     if (pow2) {
         for (int len = 2; len <= kp; len <<= 1) {
             const int hl = len >> 1, step = kp / len;
-            for (int t = threadIdx.x; t < (kp >> 1) * C; t += blockDim.x) {
-                const int c = t % C, bt = t / C;
+            for (int t = threadIdx.x; t < (kp >> 1) * NC; t += blockDim.x) {
+                const int c = t % NC, bt = t / NC;
                 const int idx = (bt / hl) * len + (bt % hl);
-                const double2 w = __ldg(tw + (bt % hl) * step);
-                const double2 u = sm[idx * C + c], v = cmul(sm[(idx + hl) * C + c], w);
-                sm[idx * C + c] = cadd(u, v);
-                sm[(idx + hl) * C + c] = csub(u, v);
+                const C w = tw[(bt % hl) * step];
+                const C u = sm[idx * NC + c], v = cmul(sm[(idx + hl) * NC + c], w);
+                sm[idx * NC + c] = cadd(u, v);
+                sm[(idx + hl) * NC + c] = csub(u, v);
             }
             __syncthreads();
         }
-        for (int idx = threadIdx.x; idx < NB * C; idx += blockDim.x) {
-            const int xb = idx / C, c = idx % C, yb = yb0 + c;
+        for (int idx = threadIdx.x; idx < NB * NC; idx += blockDim.x) {
+            const int xb = idx / NC, c = idx % NC, yb = yb0 + c;
             if (yb >= NB) continue;
-            const double2 v = sm[posmod(xb - Rb, kp) * C + c];
-            dst[((size_t)xb * NB + yb) * bb + pl] = make_double2(v.x * scale, v.y * scale);
+            dst[((size_t)xb * NB + yb) * bb + pl] = cscale(sm[posmod(xb - Rb, kp) * NC + c], scale);
         }
     } else {
-        for (int idx = threadIdx.x; idx < NB * C; idx += blockDim.x) {
-            const int xb = idx / C, c = idx % C, yb = yb0 + c;
+        for (int idx = threadIdx.x; idx < NB * NC; idx += blockDim.x) {
+            const int xb = idx / NC, c = idx % NC, yb = yb0 + c;
             if (yb >= NB) continue;
             const int xm = posmod(xb - Rb, kp);
-            double2 s = make_double2(0.0, 0.0);
-            for (int i = 0; i < kp; i++) s = cadd(s, cmul(sm[i * C + c], __ldg(tw + (int)(((long long)i * xm) % kp))));
-            dst[((size_t)xb * NB + yb) * bb + pl] = make_double2(s.x * scale, s.y * scale);
+            C s = cmake<C>(0.0, 0.0);
+            for (int i = 0; i < kp; i++) s = cadd(s, cmul(sm[i * NC + c], tw[(int)(((long long)i * xm) % kp)]));
+            dst[((size_t)xb * NB + yb) * bb + pl] = cscale(s, scale);
         }
     }
 }
@@ -186,23 +196,30 @@ static int ilog2_exact(int v)
     return l;
 }
 
-// Columns per CTA of pass 2: kp * C complex doubles (<= 128 KiB) of shared memory.
-static int fft_cols_per_block(int kp)
+// Columns per CTA of pass 2: kp * NC complex values (<= 128 KiB) of shared memory.
+static int fft_cols_per_block(int kp, size_t elem)
 {
-    int C = 8192 / kp;
-    return C < 1 ? 1 : (C > 16 ? 16 : C);
+    int c = (int)((128 * 1024) / (elem * (size_t)kp));
+    return c < 1 ? 1 : (c > 16 ? 16 : c);
 }
 
 cudaError_t configure_fft(cqpi_handle *h)
 {
-    cudaError_t e = cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(double2) * h->kp));
+    const int kp = h->kp;
+    cudaError_t e;
+    e = cudaFuncSetAttribute(fft_rows_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(16 * kp));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(fft_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(double2) * h->kp * fft_cols_per_block(h->kp)));
+    e = cudaFuncSetAttribute(fft_cols_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(16 * kp * fft_cols_per_block(kp, 16)));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(fft_rows_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * kp));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fft_cols_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(8 * kp * fft_cols_per_block(kp, 8)));
 }
 
-void launch_fft(cqpi_handle *h, int ne)
+template <class C>
+static void launch_fft_t(cqpi_handle *h, int ne, const C *g0k, const C *tw, C *half, C *box)
 {
     const int kp = h->kp, bb = h->b * h->b, NB = h->NB;
     const long long nk = (long long)kp * kp;
@@ -210,35 +227,41 @@ void launch_fft(cqpi_handle *h, int ne)
     const int thr = kp >= 512 ? 256 : (kp >= 64 ? 128 : 64);
     {
         dim3 grid(kp, bb, ne);
-        size_t smem = sizeof(double2) * kp;
-        fft_rows_kernel<<<grid, thr, smem, h->stream>>>(kp, logkp, NB, h->Rb, bb, nk, h->ws.g0k, h->d_tw, h->ws.half);
+        fft_rows_kernel<C><<<grid, thr, sizeof(C) * kp, h->stream>>>(kp, logkp, NB, h->Rb, bb, nk, g0k, tw, half);
         h->launches++;
     }
     {
-        const int C = fft_cols_per_block(kp);
-        dim3 grid(cdiv(NB, C), bb, ne);
-        size_t smem = sizeof(double2) * kp * C;
-        fft_cols_kernel<<<grid, 256, smem, h->stream>>>(kp, logkp, NB, h->Rb, bb, C, 1.0 / ((double)kp * kp), h->ws.half,
-                                                        h->d_tw, h->ws.box);
+        const int NC = fft_cols_per_block(kp, sizeof(C));
+        dim3 grid(cdiv(NB, NC), bb, ne);
+        fft_cols_kernel<C><<<grid, 256, sizeof(C) * kp * NC, h->stream>>>(kp, logkp, NB, h->Rb, bb, NC,
+                                                                         1.0 / ((double)kp * kp), half, tw, box);
         h->launches++;
     }
 }
 
+void launch_fft(cqpi_handle *h, int ne)
+{
+    if (h->precision == CQPI_PREC_FP64) launch_fft_t<double2>(h, ne, h->ws.g0k, h->d_tw, h->ws.half, h->ws.box);
+    else launch_fft_t<float2>(h, ne, h->ws.g0k32, h->d_tw32, h->ws.half32, h->ws.box32);
+}
+
 // ------------------------------------------------------------------ T-matrix
-__global__ void tmatrix_kernel(int b, int NB, int Rb, int nimp, int ne, const double2 *__restrict__ box,
-                               const double2 *__restrict__ V, double2 *__restrict__ T, int *status)
+template <class C>
+__global__ void tmatrix_kernel(int b, int NB, int Rb, int nimp, int ne, const C *__restrict__ box,
+                               const double2 *__restrict__ V, double2 *__restrict__ T, float2 *__restrict__ T32,
+                               int *status)
 {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= ne * nimp) return;
     const int e = id / nimp, imp = id % nimp;
     const int bb = b * b;
-    const double2 *g = box + (((size_t)e * NB + Rb) * NB + Rb) * bb;
+    const C *g = box + (((size_t)e * NB + Rb) * NB + Rb) * bb;
     const double2 *v = V + (size_t)imp * bb;
     double2 M[CQPI_MAX_BANDS * CQPI_MAX_BANDS], inv[CQPI_MAX_BANDS * CQPI_MAX_BANDS];
     for (int r = 0; r < b; r++)
         for (int c = 0; c < b; c++) {
             double2 s = make_double2(0.0, 0.0);
-            for (int k = 0; k < b; k++) s = cadd(s, cmul(v[r * b + k], g[k * b + c]));   // (V G0)_{rc}
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(v[r * b + k], to_d2(g[k * b + c])));   // (V G0)_{rc}
             M[r * b + c] = make_double2((r == c ? 1.0 : 0.0) - s.x, -s.y);
             inv[r * b + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
         }
@@ -269,9 +292,10 @@ __global__ void tmatrix_kernel(int b, int NB, int Rb, int nimp, int ne, const do
         }
     }
     double2 *out = T + (size_t)id * bb;
+    float2 *out32 = T32 + (size_t)id * bb;
     if (singular) {
         atomicOr(status, 1);
-        for (int k = 0; k < bb; k++) out[k] = make_double2(0.0, 0.0);
+        for (int k = 0; k < bb; k++) { out[k] = make_double2(0.0, 0.0); out32[k] = make_float2(0.f, 0.f); }
         return;
     }
     for (int r = 0; r < b; r++) {
@@ -287,38 +311,44 @@ __global__ void tmatrix_kernel(int b, int NB, int Rb, int nimp, int ne, const do
             double2 s = make_double2(0.0, 0.0);
             for (int k = 0; k < b; k++) s = cadd(s, cmul(inv[r * b + k], v[k * b + c]));
             out[r * b + c] = s;
+            out32[r * b + c] = make_float2((float)s.x, (float)s.y);
         }
 }
 
 void launch_tmatrix(cqpi_handle *h, int ne)
 {
     const int n = ne * h->nimp;
-    tmatrix_kernel<<<cdiv(n, 64), 64, 0, h->stream>>>(h->b, h->NB, h->Rb, h->nimp, ne, h->ws.box, h->d_V, h->ws.T,
-                                                      h->d_status);
+    if (h->precision == CQPI_PREC_FP64)
+        tmatrix_kernel<double2><<<cdiv(n, 64), 64, 0, h->stream>>>(h->b, h->NB, h->Rb, h->nimp, ne, h->ws.box, h->d_V,
+                                                                   h->ws.T, h->ws.T32, h->d_status);
+    else
+        tmatrix_kernel<float2><<<cdiv(n, 64), 64, 0, h->stream>>>(h->b, h->NB, h->Rb, h->nimp, ne, h->ws.box32, h->d_V,
+                                                                  h->ws.T, h->ws.T32, h->d_status);
     h->launches++;
 }
 
 // ------------------------------------------------------------------ site-independent term
+template <class C>
 __global__ void __launch_bounds__(256) term1_kernel(int b, int NB, int Rb, int w, int Q, int W, int nblk, int mb, int bs0,
-                                                    int bs1, const double *__restrict__ phi, const double2 *__restrict__ box,
+                                                    int bs1, const double *__restrict__ phi, const C *__restrict__ box,
                                                     double *__restrict__ term1)
 {
     const int q = blockIdx.x, e = blockIdx.y;
     const int bb = b * b, side = 2 * w + 1;
-    const double2 *boxe = box + (size_t)e * NB * NB * bb;
+    const C *boxe = box + (size_t)e * NB * NB * bb;
     double acc = 0.0;
     const int npair = nblk * W * W;
     for (int t = threadIdx.x; t < npair; t += blockDim.x) {
         const int blk = t / (W * W), d1 = (t / W) % W, d2 = t % W;
         const int bs = blk ? bs1 : bs0;
         const int rx = (d2 / side) - (d1 / side), ry = (d2 % side) - (d1 % side);
-        const double2 *g = boxe + ((size_t)(rx + Rb) * NB + (ry + Rb)) * bb;
+        const C *g = boxe + ((size_t)(rx + Rb) * NB + (ry + Rb)) * bb;
         const double *p1 = phi + (((size_t)blk * Q + q) * W + d1) * mb;
         const double *p2 = phi + (((size_t)blk * Q + q) * W + d2) * mb;
         for (int o1 = 0; o1 < mb; o1++) {
             const double f1 = p1[o1];
             if (f1 == 0.0) continue;
-            for (int o2 = 0; o2 < mb; o2++) acc += f1 * p2[o2] * g[(bs + o2) * b + (bs + o1)].y;
+            for (int o2 = 0; o2 < mb; o2++) acc += f1 * p2[o2] * (double)g[(bs + o2) * b + (bs + o1)].y;
         }
     }
     __shared__ double red[256];
@@ -331,12 +361,21 @@ __global__ void __launch_bounds__(256) term1_kernel(int b, int NB, int Rb, int w
     if (threadIdx.x == 0) term1[(size_t)e * Q + q] = red[0];
 }
 
-void launch_term1(cqpi_handle *h, int ne)
+template <class C>
+static void launch_term1_t(cqpi_handle *h, int ne, const C *box, double *term1)
 {
     dim3 grid(h->Q, ne);
-    term1_kernel<<<grid, 256, 0, h->stream>>>(h->b, h->NB, h->Rb, h->w, h->Q, h->W, h->nblk, h->mb, h->blk_start[0],
-                                              h->blk_start[1], h->d_phi, h->ws.box, h->ws.term1);
+    term1_kernel<C><<<grid, 256, 0, h->stream>>>(h->b, h->NB, h->Rb, h->w, h->Q, h->W, h->nblk, h->mb, h->blk_start[0],
+                                                 h->blk_start[1], h->d_phi, box, term1);
     h->launches++;
+}
+
+void launch_term1_ptr(cqpi_handle *h, int ne, const double2 *box, double *term1) { launch_term1_t(h, ne, box, term1); }
+
+void launch_term1(cqpi_handle *h, int ne)
+{
+    if (h->precision == CQPI_PREC_FP64) launch_term1_t(h, ne, h->ws.box, h->ws.term1);
+    else launch_term1_t(h, ne, h->ws.box32, h->ws.term1);
 }
 
 }  // namespace cqpi

@@ -136,6 +136,9 @@ int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count);
  * the handle's stream: [0] bands, [1] G0(k)+FFT, [2] T-matrix, [3] contraction, [4] total. */
 int cqpi_stage_times(const cqpi_handle *h, float *ms5);
 
+/* Contraction kernel the handle runs: 0 = FP64 CUDA cores, 1 = FP32 CUDA cores,
+ * 2 = tcgen05 tensor cores (split-FP16 x3). */
+int cqpi_contraction_kind(const cqpi_handle *h, int32_t *kind);
 /* Diagnostic: measured CUDA-core FMA throughput of the current device in TFLOP/s
  * (kind 0: FP64 DFMA, kind 1: FP32 FFMA), the roofline denominator of the engine's
  * CUDA-core kernels.  No counterpart in the reference. */

@@ -1,0 +1,56 @@
+"""GPU: the mixed-precision path against the FP64 path and the oracle.
+
+Tolerance (the spec bar): max|rho - rho64| / max|rho64| <= 1e-6 per map.
+"""
+import numpy as np
+import pytest
+
+from cases import case
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+def _run(name, precision):
+    import cqpi
+    m, p, wf, z, v, E = case(name)
+    eng = cqpi.Engine(m, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"], spin=p["spin"],
+                      precision=precision)
+    eng.set_orbitals(wf, z)
+    eng.set_scattering(v)
+    return eng.run(E, f32=False, f64=True), (m, p, wf, z, v, E)
+
+
+@pytest.mark.parametrize("name", ["c1", "c1_odd", "c2", "c2_zero", "c3"])
+def test_mixed_matches_fp64_and_oracle(built_lib, name):
+    import cqpi
+    from oracle import oracle as O
+    mixed, (m, p, wf, z, v, E) = _run(name, cqpi.PREC_MIXED)
+    fp64, _ = _run(name, cqpi.PREC_FP64)
+    for e in range(len(E)):
+        ref = fp64[e, 0]
+        err = np.abs(mixed[e, 0] - ref).max() / np.abs(ref).max()
+        assert err <= TOL, (name, e, err)
+    om = O.Model(m.bands, m.R, m.orb, m.t, m.anti, m.efermi, m.scmaxbands)
+    orc = O.run(om, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"], E, v, wf, z, spin=p["spin"])
+    assert np.abs(mixed[:, 0] - orc).max() / np.abs(orc).max() <= TOL
+
+
+def test_mixed_c2_physics(built_lib):
+    """C2 model and orbitals with the C2 k-grid and eta (sharp poles), a 32^2-site field of view."""
+    import cqpi
+    from cqpi import workloads as W
+    c, m, wf = W.config("C2")
+    E = np.array([-0.1, -0.03, 0.0, 0.05, 0.1])
+    out = {}
+    for prec in (cqpi.PREC_FP64, cqpi.PREC_MIXED):
+        eng = cqpi.Engine(m, 32, c.kpoints, c.oversamp, c.window, c.eta, precision=prec)
+        eng.set_orbitals(wf)
+        eng.set_scattering(np.array(c.scattering, complex))
+        out[prec] = eng.run(E, f32=False, f64=True)
+        eng.close()
+    for e in range(len(E)):
+        ref = out[cqpi.PREC_FP64][e, 0]
+        err = np.abs(out[cqpi.PREC_MIXED][e, 0] - ref).max() / np.abs(ref).max()
+        assert err <= TOL, (E[e], err)
