@@ -70,6 +70,7 @@ void free_workspace(cqpi_handle *h)
     dfree(h->ws.half32);
     dfree(h->ws.box32);
     dfree(h->ws.T32);
+    dfree(h->ws.gmax);
     h->ws.ebatch = 0;
 }
 
@@ -93,6 +94,7 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
         dalloc(&h->ws.g0k32, ebatch * bb * nk);
         dalloc(&h->ws.half32, ebatch * bb * (size_t)h->kp * h->NB);
         dalloc(&h->ws.box32, ebatch * (size_t)h->NB * h->NB * bb);
+        dalloc(&h->ws.gmax, ebatch);
     }
     dalloc(&h->ws.T, ebatch * (size_t)std::max(h->nimp, 1) * bb);
     dalloc(&h->ws.T32, ebatch * (size_t)std::max(h->nimp, 1) * bb);
@@ -101,10 +103,19 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
     h->ws.ebatch = ebatch;
 }
 
-void launch_contraction(cqpi_handle *h, int ne, float *o32, double *o64)
+// tmp32: float buffer of ne*nimp maps used when only float64 maps are requested from the
+// tensor-core contraction (which writes float32).
+void launch_contraction(cqpi_handle *h, int ne, float *o32, double *o64, float *tmp32)
 {
-    if (h->precision == CQPI_PREC_FP64) launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
-    else launch_ldos_fp32(h, ne, h->ws.box32, h->ws.T32, h->ws.term1, o32, o64);
+    if (h->precision == CQPI_PREC_FP64) {
+        launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
+    } else if (h->use_tc) {
+        float *dst = o32 ? o32 : tmp32;
+        CK(launch_ldos_tc(h, ne, dst));
+        if (o64) launch_widen(h, dst, o64, (size_t)ne * h->nimp * h->wn * h->wn);
+    } else {
+        launch_ldos_fp32(h, ne, h->ws.box32, h->ws.T32, h->ws.term1, o32, o64);
+    }
 }
 
 int choose_batch(const cqpi_handle *h, int nE)
@@ -212,6 +223,7 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
     if (!h) return CQPI_ERR_ALLOC;
     try {
         CK(cudaGetDevice(&h->device));
+        CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         for (auto &e : h->ev) CK(cudaEventCreate(&e));
         h->b = b;
@@ -303,6 +315,13 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         CK(cudaMemcpy(h->d_V, V.data(), sizeof(double2) * bb, cudaMemcpyHostToDevice));
         // the transform kernels keep whole rows / column tiles in shared memory
         CK(configure_fft(h));
+        // tensor-core contraction for the mixed path (CUDA-core FP32 kernel otherwise);
+        // CQPI_CONTRACTION=fp32 selects the CUDA-core kernel explicitly
+        if (h->precision == CQPI_PREC_MIXED && tc_supported(h)) {
+            tc_plan(h);
+            const char *force = getenv("CQPI_CONTRACTION");
+            h->use_tc = h->tc.ok && !(force && !strcmp(force, "fp32"));
+        }
     } catch (const CudaError &e) {
         int rc = cuda_fail(h, e);
         cqpi_destroy(h);
@@ -330,6 +349,7 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_evec32);
     dfree(h->d_phi);
     dfree(h->d_phi32);
+    dfree(h->d_tc_a);
     dfree(h->d_seam_box);
     dfree(h->d_seam_T);
     dfree(h->d_seam_term1);
@@ -374,6 +394,13 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
         dfree(h->d_phi32);
         dalloc(&h->d_phi32, phi32.size());
         CK(cudaMemcpy(h->d_phi32, phi32.data(), sizeof(float) * phi32.size(), cudaMemcpyHostToDevice));
+        if (h->use_tc) {
+            std::vector<uint16_t> img;
+            tc_build_a(h, phi, img, h->tc_inv_sA);
+            dfree(h->d_tc_a);
+            dalloc(&h->d_tc_a, img.size());
+            CK(cudaMemcpy(h->d_tc_a, img.data(), sizeof(uint16_t) * img.size(), cudaMemcpyHostToDevice));
+        }
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
@@ -437,6 +464,11 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             if (maps32) dalloc(&stage32, eb * per_e);
             if (maps64) dalloc(&stage64, eb * per_e);
         }
+        float *tmp32 = nullptr;
+        if (h->use_tc && !maps32) {
+            if (!stage32) dalloc(&stage32, eb * per_e);
+            tmp32 = stage32;
+        }
         float tb = 0, tg = 0, tt = 0, tl = 0;
         CK(cudaEventRecord(h->ev[0], h->stream));
         if (!h->bands_ready) do_bands(h);
@@ -446,6 +478,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
         for (int e0 = 0; e0 < nE; e0 += eb) {
             const int ne = std::min(eb, nE - e0);
             CK(cudaMemcpyAsync(h->ws.energies, energies + e0, sizeof(double) * ne, cudaMemcpyHostToDevice, h->stream));
+            if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
             CK(cudaEventRecord(h->ev[2], h->stream));
             do_greens(h, ne);
             CK(cudaEventRecord(h->ev[3], h->stream));
@@ -456,7 +489,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             CK(cudaEventRecord(h->ev[4], h->stream));
             float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : stage32) : nullptr;
             double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : stage64) : nullptr;
-            launch_contraction(h, ne, o32, o64);
+            launch_contraction(h, ne, o32, o64, tmp32);
             check_launch();
             CK(cudaEventRecord(h->ev[5], h->stream));
             if (!on_device) {
@@ -525,6 +558,7 @@ int cqpi_get_greens_box(cqpi_handle *h, double energy, double *box, int32_t *rb)
         ensure_workspace(h, 1);
         if (!h->bands_ready) do_bands(h);
         CK(cudaMemcpyAsync(h->ws.energies, &energy, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned), h->stream));
         do_greens(h, 1);
         const size_t cnt = (size_t)h->NB * h->NB * h->b * h->b;
         if (h->precision == CQPI_PREC_FP64) {
@@ -637,7 +671,7 @@ int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count)
 int cqpi_contraction_kind(const cqpi_handle *h, int32_t *kind)
 {
     if (!h || !kind) return CQPI_ERR_ARG;
-    *kind = (h->precision == CQPI_PREC_FP64) ? 0 : 1;
+    *kind = (h->precision == CQPI_PREC_FP64) ? 0 : (h->use_tc ? 2 : 1);
     return CQPI_OK;
 }
 

@@ -29,6 +29,32 @@ struct RTerms {
     std::vector<double> tn, ta; // [nR][b*b][2]
 };
 
+// Launch plan of the tcgen05 contraction (ldos_tc.cu).
+struct TcPlan {
+    bool ok = false;
+    int TS = 0;          // sites per tile (multiple of 4)
+    int N = 0;           // MMA N = 2*bands*TS (multiple of 16, <= 256)
+    int KP = 0;          // K padded to a multiple of 16
+    int tmem_cols = 0;   // power of two >= 2*nblk*N
+    int a_bytes = 0, b_bytes = 0;
+    size_t smem = 0;
+};
+
+struct TcParams {
+    int b, n, os, w, Rb, NB, W, nblk, mb, bs0, bs1;
+    int TS, N, KP, Q, nimp, ne, wn, ntx;
+    int tmem_cols, a_bytes, b_bytes;
+    float inv_sA;
+    long long spin_limit;
+    const float2 *box;
+    const float2 *T32;
+    const double *term1;
+    const unsigned *gmax;
+    const uint4 *Aimg;
+    float *out;
+    int *status;
+};
+
 struct Workspace {
     int ebatch = 0;
     double2 *g0k = nullptr;
@@ -41,6 +67,7 @@ struct Workspace {
     float2 *half32 = nullptr;
     float2 *box32 = nullptr;
     float2 *T32 = nullptr;
+    unsigned *gmax = nullptr;   // per energy: bits of max |Re|,|Im| of the FP32 box
 };
 
 }  // namespace cqpi
@@ -71,6 +98,12 @@ struct cqpi_handle {
     double *d_phi = nullptr;
     float *d_phi32 = nullptr;
     bool orbitals_ready = false;
+    // tcgen05 contraction
+    bool use_tc = false;
+    cqpi::TcPlan tc;
+    uint16_t *d_tc_a = nullptr;   // Phi hi/lo operand images
+    float tc_inv_sA = 1.0f;
+    int num_sms = 0;
     // impurities
     int nimp = 0;
     double2 *d_V = nullptr;   // [nimp][b*b]
@@ -105,6 +138,12 @@ void launch_ldos_fp64(cqpi_handle *h, int ne, const double2 *box, const double2 
                       float *out32, double *out64);
 void launch_ldos_fp32(cqpi_handle *h, int ne, const float2 *box, const float2 *T, const double *term1,
                       float *out32, double *out64);
+// ldos_tc.cu
+bool tc_supported(const cqpi_handle *h);
+void tc_plan(cqpi_handle *h);
+void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img, float &inv_sA);
+cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out);
+void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n);
 
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 

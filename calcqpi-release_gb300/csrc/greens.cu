@@ -141,10 +141,19 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(int kp, int logkp, int NB
 }
 
 // Pass 2: NC adjacent columns yb (fixed plane, energy), transform along i, keep X = xb - Rb.
+// Pass 2 also records max |Re|,|Im| of the box per energy (gmax, float bits; used to
+// scale the tensor-core operands) when gmax is non-null.
+__device__ __forceinline__ void track_max(unsigned *gmax, float v)
+{
+    v = fmaxf(v, 0.0f);
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0.0f) atomicMax(gmax, __float_as_uint(v));
+}
+
 template <class C>
 __global__ void __launch_bounds__(256) fft_cols_kernel(int kp, int logkp, int NB, int Rb, int bb, int NC, double scale,
                                                        const C *__restrict__ half, const C *__restrict__ tw,
-                                                       C *__restrict__ box)
+                                                       C *__restrict__ box, unsigned *__restrict__ gmax)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     C *sm = reinterpret_cast<C *>(smraw);
@@ -171,11 +180,17 @@ __global__ void __launch_bounds__(256) fft_cols_kernel(int kp, int logkp, int NB
             }
             __syncthreads();
         }
-        for (int idx = threadIdx.x; idx < NB * NC; idx += blockDim.x) {
+        float mx = 0.0f;
+        const int lim = ((NB * NC + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
+        for (int idx = threadIdx.x; idx < lim; idx += blockDim.x) {
             const int xb = idx / NC, c = idx % NC, yb = yb0 + c;
-            if (yb >= NB) continue;
-            dst[((size_t)xb * NB + yb) * bb + pl] = cscale(sm[posmod(xb - Rb, kp) * NC + c], scale);
+            if (idx < NB * NC && yb < NB) {
+                const C v = cscale(sm[posmod(xb - Rb, kp) * NC + c], scale);
+                dst[((size_t)xb * NB + yb) * bb + pl] = v;
+                mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+            }
         }
+        if (gmax) track_max(gmax + e, mx);
     } else {
         for (int idx = threadIdx.x; idx < NB * NC; idx += blockDim.x) {
             const int xb = idx / NC, c = idx % NC, yb = yb0 + c;
@@ -184,6 +199,19 @@ __global__ void __launch_bounds__(256) fft_cols_kernel(int kp, int logkp, int NB
             C s = cmake<C>(0.0, 0.0);
             for (int i = 0; i < kp; i++) s = cadd(s, cmul(sm[i * NC + c], tw[(int)(((long long)i * xm) % kp)]));
             dst[((size_t)xb * NB + yb) * bb + pl] = cscale(s, scale);
+        }
+        if (gmax) {
+            __syncthreads();
+            float mx = 0.0f;
+            const int lim = ((NB * NC + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
+            for (int idx = threadIdx.x; idx < lim; idx += blockDim.x) {
+                const int xb = idx / NC, c = idx % NC, yb = yb0 + c;
+                if (idx < NB * NC && yb < NB) {
+                    const C v = dst[((size_t)xb * NB + yb) * bb + pl];
+                    mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+                }
+            }
+            track_max(gmax + e, mx);
         }
     }
 }
@@ -219,7 +247,7 @@ cudaError_t configure_fft(cqpi_handle *h)
 }
 
 template <class C>
-static void launch_fft_t(cqpi_handle *h, int ne, const C *g0k, const C *tw, C *half, C *box)
+static void launch_fft_t(cqpi_handle *h, int ne, const C *g0k, const C *tw, C *half, C *box, unsigned *gmax)
 {
     const int kp = h->kp, bb = h->b * h->b, NB = h->NB;
     const long long nk = (long long)kp * kp;
@@ -234,15 +262,17 @@ static void launch_fft_t(cqpi_handle *h, int ne, const C *g0k, const C *tw, C *h
         const int NC = fft_cols_per_block(kp, sizeof(C));
         dim3 grid(cdiv(NB, NC), bb, ne);
         fft_cols_kernel<C><<<grid, 256, sizeof(C) * kp * NC, h->stream>>>(kp, logkp, NB, h->Rb, bb, NC,
-                                                                         1.0 / ((double)kp * kp), half, tw, box);
+                                                                         1.0 / ((double)kp * kp), half, tw, box, gmax);
         h->launches++;
     }
 }
 
 void launch_fft(cqpi_handle *h, int ne)
 {
-    if (h->precision == CQPI_PREC_FP64) launch_fft_t<double2>(h, ne, h->ws.g0k, h->d_tw, h->ws.half, h->ws.box);
-    else launch_fft_t<float2>(h, ne, h->ws.g0k32, h->d_tw32, h->ws.half32, h->ws.box32);
+    if (h->precision == CQPI_PREC_FP64)
+        launch_fft_t<double2>(h, ne, h->ws.g0k, h->d_tw, h->ws.half, h->ws.box, nullptr);
+    else
+        launch_fft_t<float2>(h, ne, h->ws.g0k32, h->d_tw32, h->ws.half32, h->ws.box32, h->ws.gmax);
 }
 
 // ------------------------------------------------------------------ T-matrix

@@ -1,0 +1,487 @@
+// ldos_tc.cu -- continuum LDOS contraction on the 5th-generation tensor cores (tcgen05).
+//
+// Replaces tmatrix::calcwannierldos (src/qpi.cc:876-950) / gpucalcwannierldos[spin]
+// (src/qpicudakernel.cu:60-158) in the mixed-precision path.  With the factorisation
+//   u_a(p,q) = sum_{d,o} phi_o(q,d) G0(p+d)[o][a],   s_c(p,q) = sum_{d,o} G0(-p-d)[c][o] phi_o(q,d)
+//   rho(p,q) = -term1(q) - Im( sum_a u_a (T s)_a )
+// the two window sums are GEMMs that share the real, constant A operand
+// Phi[q][(d,o)] (M = oversamp^2 <= 128 rows, K = W*orbitals padded to 16):
+//   D_u[q][(a,re/im,site)] = Phi x B_u,   D_s[q][(c,re/im,site)] = Phi x B_s,
+// N = 2*bands*sites per tile.  Precision: split-FP16 x3 -- A and B are scaled by
+// powers of two (A once per handle, B per energy from max|G0(R)|) and split into
+// fp16 hi + lo; hi*hi + hi*lo + lo*hi are accumulated in FP32 in tensor memory
+// (relative representation error ~2^-22; measured rel. error vs FP64 ~1e-7).
+//
+// Kernel organisation (persistent, 128 threads = 4 warps, one CTA owns TMEM
+// columns for its accumulators):
+//   - A (Phi hi/lo for every spin block) is copied once into shared memory in the
+//     K-major, no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix);
+//   - per tile (energy, site row, TS consecutive sites) and spin block: all threads
+//     gather the G0(R) window from the L2-resident FP32 box (im2col), scale, split and
+//     store B_u / B_s hi/lo in the same layout; one thread issues the tcgen05.mma
+//     chain and tcgen05.commit arrives on an mbarrier; every thread waits (bounded);
+//   - epilogue: tcgen05.ld of the accumulators (warp w reads TMEM lanes 32w..32w+31,
+//     lane = q row), T s and Im(u . Ts) in FP32, term1 in FP64, staging through
+//     shared memory into coalesced row stores of the map.
+// Every spin-wait is bounded; on time-out the CTA sets an error bit in *status,
+// waits (bounded) for its in-flight MMAs, frees its tensor memory and returns.
+// Roofline: tensor-pipe bound (see the bench's roofline object).
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "cplx.h"
+#include "cqpi_internal.h"
+
+namespace cqpi {
+
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading-dimension byte
+// offset (K direction between 16-byte core-matrix columns), stride byte offset
+// (between 8-row groups), version 1, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D f32, A f16, B f16, both K-major, N>>3, M>>4.
+__host__ __device__ __forceinline__ uint32_t idesc_f16(int M, int N)
+{
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(dtmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+// Bounded wait for the given phase parity; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit)
+{
+    for (long long it = 0; it < limit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// Four consecutive accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float &a, float &b, float &c, float &d)
+{
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(taddr)
+                 : "memory");
+    a = __uint_as_float(r0); b = __uint_as_float(r1); c = __uint_as_float(r2); d = __uint_as_float(r3);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Power-of-two scale that maps max|x| to [2^13, 2^14].
+__device__ __forceinline__ float pow2_scale(unsigned maxbits)
+{
+    const float mx = __uint_as_float(maxbits);
+    if (!(mx > 0.0f) || !(mx < 3.0e38f)) return 1.0f;
+    int ex;
+    frexpf(mx, &ex);            // mx = f * 2^ex, f in [0.5, 1)
+    return ldexpf(1.0f, 14 - ex);
+}
+
+// byte offset of element (row r, k) in a K-major no-swizzle operand with KP columns
+__device__ __forceinline__ uint32_t core_off(int r, int kc, int sbo) { return (uint32_t)((r >> 3) * sbo + kc * 128 + (r & 7) * 16); }
+
+}  // namespace tc
+
+constexpr int TC_THREADS = 512;   // 16 warps; warps w, w+4, w+8, w+12 share TMEM lane quarter w%4
+
+template <int B>
+__global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_constant__ TcParams p)
+{
+    using namespace tc;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int bb = p.b * p.b, side = 2 * p.w + 1, n2 = p.n >> 1;
+    const int sbo = p.KP * 16;                  // bytes per 8-row group (8 rows x KP halfs)
+    const int kcs = p.KP >> 3;
+    const int wx = p.TS + 2 * p.w;              // window extent in x (sites + halo)
+    const int wfl = wx * side * bb * 2;         // floats per staged window
+    // shared-memory carve-up (offsets in bytes, 16-byte aligned)
+    unsigned char *smA = sm;
+    unsigned char *smB = smA + (size_t)p.nblk * 2 * p.a_bytes;
+    float *winU = reinterpret_cast<float *>(smB + 4 * (size_t)p.b_bytes);
+    float *winS = winU + wfl + 4;               // +4: a zero slot used by padded k columns
+    int *tblU = reinterpret_cast<int *>(winS + wfl + 4);
+    int *tblS = tblU + p.nblk * p.KP;
+    float *stage = reinterpret_cast<float *>(tblS + p.nblk * p.KP);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(stage + ((p.os * p.TS * p.os + 3) & ~3));
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+
+    {   // A operands (Phi hi/lo of every spin block) -> shared memory, once
+        const uint4 *src = p.Aimg;
+        uint4 *dst = reinterpret_cast<uint4 *>(smA);
+        const int nv = p.nblk * 2 * p.a_bytes / 16;
+        for (int i = tid; i < nv; i += TC_THREADS) dst[i] = src[i];
+    }
+    // k -> float offset of G0(p+d)[o][.] in the u window and of G0(-p-d)[.][o] in the s
+    // window, relative to a site's base; padded k point at the zero slot.
+    for (int i = tid; i < p.nblk * p.KP; i += TC_THREADS) {
+        const int blk = i / p.KP, k = i % p.KP;
+        const int bs = blk ? p.bs1 : p.bs0;
+        if (k < p.W * p.mb) {
+            const int d = k / p.mb, o = bs + k % p.mb;
+            const int dxw = d / side, dyw = d % side;   // dx + w, dy + w
+            tblU[i] = 2 * ((dxw * side + dyw) * bb + o * p.b);
+            tblS[i] = 2 * (((2 * p.w - dxw) * side + (2 * p.w - dyw)) * bb + o);
+        } else {
+            tblU[i] = -1;
+            tblS[i] = -1;
+        }
+    }
+    if (tid < 4) { winU[wfl + tid] = 0.f; winS[wfl + tid] = 0.f; }
+    if (tid == 0) {
+        mbar_init(smem_u32(mbar), 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = idesc_f16(128, p.N);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const int ntiles = p.ne * p.n * p.ntx;
+    const int lq = tid & 127;                 // TMEM lane = accumulator row = q = qy*os + qx
+    const int qx = lq % p.os, qy = lq / p.os;
+    const bool qvalid = lq < p.Q;
+    const int sgrp = tid >> 7;                // warp group g takes the 4-site chunks g, g+4, ...
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int e = t / (p.n * p.ntx);
+        const int rr = t % (p.n * p.ntx);
+        const int j = rr / p.ntx, i0 = (rr % p.ntx) * p.TS;
+        const float sB = pow2_scale(p.gmax[e]);
+        const float2 *boxe = p.box + (size_t)e * p.NB * p.NB * bb;
+        const int py = j - n2, px0 = i0 - n2;
+
+        // ---- stage the scaled G0 windows: u: X in [px0-w, px0+TS-1+w], Y in [py-w, py+w];
+        //      s: X in [-px0-TS+1-w, -px0+w], Y in [-py-w, -py+w]  (zero outside the box)
+        {
+            const int rowlen = side * bb;              // complex values per window x-row
+            const int total = 2 * wx * rowlen;
+            for (int idx = tid; idx < total; idx += TC_THREADS) {
+                const int which = idx / (wx * rowlen), r = idx % (wx * rowlen);
+                const int xl = r / rowlen, c = r % rowlen;
+                const int X = which == 0 ? px0 - p.w + xl : -px0 - (p.TS - 1) - p.w + xl;
+                const int Y0 = which == 0 ? py - p.w : -py - p.w;
+                float2 v = make_float2(0.f, 0.f);
+                if (X >= -p.Rb && X <= p.Rb) {
+                    const int yl = c / bb, pl = c % bb;
+                    const int Y = Y0 + yl;
+                    if (Y >= -p.Rb && Y <= p.Rb) v = boxe[((size_t)(X + p.Rb) * p.NB + (Y + p.Rb)) * bb + pl];
+                }
+                float *w = which == 0 ? winU : winS;
+                w[2 * r] = v.x * sB;
+                w[2 * r + 1] = v.y * sB;
+            }
+        }
+        __syncthreads();
+
+        for (int blk = 0; blk < p.nblk && ok; blk++) {
+            // ---- B operands from the windows: rows n = (a, re/im, site), 8 k per item
+            const int *tU = tblU + blk * p.KP, *tS = tblS + blk * p.KP;
+            const int nitems = 2 * p.N * kcs;
+            for (int it = tid; it < nitems; it += TC_THREADS) {
+                const int op = it >= p.N * kcs;
+                const int rem = op ? it - p.N * kcs : it;
+                const int nrow = rem / kcs, kc = rem - (rem / kcs) * kcs;
+                const int ari = nrow / p.TS, sl = nrow - ari * p.TS;
+                const int a = ari >> 1, ri = ari & 1;
+                const float *w = op ? winS : winU;
+                const int *tb = op ? tS : tU;
+                const int base = op ? (2 * (p.TS - 1 - sl) * side * bb + 2 * a * p.b + ri)
+                                    : (2 * sl * side * bb + 2 * a + ri);
+                float v[8];
+#pragma unroll
+                for (int kk = 0; kk < 8; kk++) {
+                    const int o = tb[kc * 8 + kk];
+                    v[kk] = o >= 0 ? w[base + o] : 0.f;
+                }
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const __half2 h = __floats2half2_rn(v[2 * kk], v[2 * kk + 1]);
+                    const float2 hb = __half22float2(h);
+                    const __half2 l = __floats2half2_rn(v[2 * kk] - hb.x, v[2 * kk + 1] - hb.y);
+                    hw[kk] = *reinterpret_cast<const uint32_t *>(&h);
+                    lw[kk] = *reinterpret_cast<const uint32_t *>(&l);
+                }
+                const uint32_t off = core_off(nrow, kc, sbo);
+                *reinterpret_cast<uint4 *>(smB + (size_t)(op * 2 + 0) * p.b_bytes + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(smB + (size_t)(op * 2 + 1) * p.b_bytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+            fence_proxy_async();
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t aH = smem_u32(smA + (size_t)(blk * 2 + 0) * p.a_bytes);
+                const uint32_t aL = smem_u32(smA + (size_t)(blk * 2 + 1) * p.a_bytes);
+                for (int op = 0; op < 2; op++) {
+                    const uint32_t d = tmem + (uint32_t)(blk * 2 * p.N + op * p.N);
+                    const uint32_t bH = smem_u32(smB + (size_t)(op * 2 + 0) * p.b_bytes);
+                    const uint32_t bL = smem_u32(smB + (size_t)(op * 2 + 1) * p.b_bytes);
+                    for (int ks = 0; ks < (p.KP >> 4); ks++) {
+                        const uint32_t off = (uint32_t)ks * 256u;
+                        mma_f16(d, sdesc(aH + off, 128, sbo), sdesc(bH + off, 128, sbo), idesc, ks > 0 ? 1u : 0u);
+                        mma_f16(d, sdesc(aH + off, 128, sbo), sdesc(bL + off, 128, sbo), idesc, 1u);
+                        mma_f16(d, sdesc(aL + off, 128, sbo), sdesc(bH + off, 128, sbo), idesc, 1u);
+                    }
+                }
+                mma_commit(smem_u32(mbar));
+            }
+            const bool done = mbar_wait(smem_u32(mbar), phase, p.spin_limit);
+            if (done) phase ^= 1u;
+            if (__syncthreads_or(!done)) {
+                ok = false;
+                if (tid == 0) atomicOr(p.status, 2);
+            }
+        }
+        if (!ok) break;
+        tc_fence_after();
+
+        // ---- epilogue: each warp group handles TS/4 sites of its lane quarter
+        const float inv = p.inv_sA / sB;
+        const int wt = p.TS * p.os;
+        for (int imp = 0; imp < p.nimp; imp++) {
+            const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
+            const double t1 = qvalid ? p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.0;
+            for (int s0 = sgrp * 4; s0 < p.TS; s0 += 16) {
+                float term2[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int blk = 0; blk < p.nblk; blk++) {
+                    float ur[2 * B][4], sr[2 * B][4];
+#pragma unroll
+                    for (int ari = 0; ari < 2 * B; ari++) {
+                        if (ari < 2 * p.b) {
+                            const uint32_t cu = (uint32_t)(blk * 2 * p.N + ari * p.TS + s0);
+                            tmem_ld4(tmem + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
+                            tmem_ld4(tmem + lane_base + cu + (uint32_t)p.N, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                        }
+                    }
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int a = 0; a < B; a++) {
+                        if (a >= p.b) continue;
+                        float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                        for (int c = 0; c < B; c++) {
+                            if (c >= p.b) continue;
+                            const float2 tv = __ldg(Te + a * p.b + c);
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                tsr[u] += tv.x * sr[2 * c][u] - tv.y * sr[2 * c + 1][u];
+                                tsi[u] += tv.x * sr[2 * c + 1][u] + tv.y * sr[2 * c][u];
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
+                    }
+                }
+                if (qvalid)
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        stage[qy * wt + (s0 + u) * p.os + qx] = (float)(-t1 - (double)(term2[u] * inv * inv));
+            }
+            __syncthreads();
+            const int xbase = i0 * p.os;
+            const size_t rowbase = ((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os;
+            for (int idx = tid; idx < p.os * wt; idx += TC_THREADS) {
+                const int yy = idx / wt, xx = idx - (idx / wt) * wt;
+                const int x = xbase + xx;
+                if (x < p.wn) p.out[(rowbase + yy) * p.wn + x] = stage[yy * wt + xx];
+            }
+            __syncthreads();
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+
+    if (!ok) {
+        // make sure no MMA of this CTA is still writing tensor memory before it is freed
+        mbar_wait(smem_u32(mbar), phase, p.spin_limit);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, p.tmem_cols);
+    }
+}
+
+__global__ void widen_kernel(const float *__restrict__ src, double *__restrict__ dst, size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
+}
+
+void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n)
+{
+    const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)h->num_sms * 8);
+    widen_kernel<<<grid ? grid : 1, 256, 0, h->stream>>>(src, dst, n);
+    h->launches++;
+}
+
+// ------------------------------------------------------------------ host side
+bool tc_supported(const cqpi_handle *h) { return h->Q <= 128 && h->b <= CQPI_MAX_BANDS; }
+
+void tc_plan(cqpi_handle *h)
+{
+    TcPlan &pl = h->tc;
+    const int twob = 2 * h->b;
+    // TS: multiple of 4 (4-site TMEM loads), N = TS*2b a multiple of 16
+    int TS = 0;
+    for (int t = 32; t >= 4; t -= 4)
+        if ((t * twob) % 16 == 0 && t * twob <= 128) { TS = t; break; }
+    if (!TS)
+        for (int t = 32; t >= 4; t -= 4)
+            if ((t * twob) % 16 == 0 && t * twob <= 256) { TS = t; break; }
+    pl.TS = TS;
+    pl.N = TS * twob;
+    pl.KP = ((h->W * h->mb + 15) / 16) * 16;
+    int cols = 2 * h->nblk * pl.N, tc = 32;
+    while (tc < cols) tc <<= 1;
+    pl.tmem_cols = tc;
+    pl.a_bytes = 128 * pl.KP * 2;
+    pl.b_bytes = pl.N * pl.KP * 2;
+    const size_t wfl = (size_t)(TS + 2 * h->w) * (2 * h->w + 1) * h->b * h->b * 2;
+    pl.smem = (size_t)h->nblk * 2 * pl.a_bytes + 4 * (size_t)pl.b_bytes + 4 * (2 * (wfl + 4)) +
+              4 * (size_t)(2 * h->nblk * pl.KP) + 4 * (size_t)((h->os * TS * h->os + 3) & ~3) + 64;
+    pl.ok = TS > 0 && cols <= 512 && pl.smem <= 227 * 1024;
+}
+
+// Phi hi/lo images in the operand layout: rows m = qy*os + qx, columns k = d*mb + ol.
+void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img, float &inv_sA)
+{
+    const TcPlan &pl = h->tc;
+    double mx = 0.0;
+    for (double v : phi) mx = std::max(mx, std::fabs(v));
+    int ex = 0;
+    if (mx > 0) std::frexp(mx, &ex);
+    const double sA = mx > 0 ? std::ldexp(1.0, 14 - ex) : 1.0;
+    inv_sA = (float)(1.0 / sA);
+    const size_t per = pl.a_bytes / 2;
+    img.assign((size_t)h->nblk * 2 * per, 0);
+    const int sbo = pl.KP * 16;
+    for (int blk = 0; blk < h->nblk; blk++)
+        for (int qy = 0; qy < h->os; qy++)
+            for (int qx = 0; qx < h->os; qx++) {
+                const int m = qy * h->os + qx;
+                for (int d = 0; d < h->W; d++)
+                    for (int ol = 0; ol < h->mb; ol++) {
+                        const double v = sA * phi[((((size_t)blk * h->Q) + qx * h->os + qy) * h->W + d) * h->mb + ol];
+                        const __half hi = __float2half_rn((float)v);
+                        const __half lo = __float2half_rn((float)(v - (double)__half2float(hi)));
+                        const int k = d * h->mb + ol;
+                        const size_t off = ((size_t)(m >> 3) * sbo + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2) / 2;
+                        img[(size_t)(blk * 2 + 0) * per + off] = __half_as_ushort(hi);
+                        img[(size_t)(blk * 2 + 1) * per + off] = __half_as_ushort(lo);
+                    }
+            }
+}
+
+template <int B>
+static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
+{
+    const TcPlan &pl = h->tc;
+    TcParams p;
+    p.b = h->b; p.n = h->n; p.os = h->os; p.w = h->w; p.Rb = h->Rb; p.NB = h->NB; p.W = h->W;
+    p.nblk = h->nblk; p.mb = h->mb; p.bs0 = h->blk_start[0]; p.bs1 = h->blk_start[1];
+    p.TS = pl.TS; p.N = pl.N; p.KP = pl.KP; p.Q = h->Q; p.nimp = h->nimp; p.ne = ne; p.wn = h->wn;
+    p.ntx = (h->n + pl.TS - 1) / pl.TS;
+    p.tmem_cols = pl.tmem_cols; p.a_bytes = pl.a_bytes; p.b_bytes = pl.b_bytes;
+    p.inv_sA = h->tc_inv_sA;
+    p.spin_limit = 1LL << 24;
+    p.box = h->ws.box32; p.T32 = h->ws.T32; p.term1 = h->ws.term1; p.gmax = h->ws.gmax;
+    p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
+    p.out = out;
+    p.status = h->d_status;
+    cudaError_t err = cudaFuncSetAttribute(ldos_tc_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
+    if (err != cudaSuccess) return err;
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ldos_tc_kernel<B>, TC_THREADS, pl.smem);
+    if (err != cudaSuccess) return err;
+    per_sm = std::max(1, std::min(per_sm, (int)(512 / pl.tmem_cols)));
+    const long long ntiles = (long long)ne * h->n * p.ntx;
+    const int grid = (int)std::min<long long>(ntiles, (long long)h->num_sms * per_sm);
+    ldos_tc_kernel<B><<<grid, TC_THREADS, pl.smem, h->stream>>>(p);
+    h->launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out)
+{
+    const int b = h->b;
+    if (b <= 1) return launch_tc_t<1>(h, ne, out);
+    if (b <= 2) return launch_tc_t<2>(h, ne, out);
+    if (b <= 3) return launch_tc_t<3>(h, ne, out);
+    if (b <= 4) return launch_tc_t<4>(h, ne, out);
+    if (b <= 6) return launch_tc_t<6>(h, ne, out);
+    if (b <= 8) return launch_tc_t<8>(h, ne, out);
+    if (b <= 10) return launch_tc_t<10>(h, ne, out);
+    if (b <= 12) return launch_tc_t<12>(h, ne, out);
+    return launch_tc_t<16>(h, ne, out);
+}
+
+}  // namespace cqpi

@@ -54,3 +54,45 @@ def test_mixed_c2_physics(built_lib):
         ref = out[cqpi.PREC_FP64][e, 0]
         err = np.abs(out[cqpi.PREC_MIXED][e, 0] - ref).max() / np.abs(ref).max()
         assert err <= TOL, (E[e], err)
+
+
+@pytest.mark.parametrize("name", ["c1", "c1_odd", "c2", "c2_zero", "c3"])
+def test_tensor_core_contraction_matches_cuda_core(built_lib, name, monkeypatch):
+    """The tcgen05 (split-FP16 x3) contraction against the FP32 CUDA-core contraction and FP64."""
+    import cqpi
+    tc, _ = _run(name, cqpi.PREC_MIXED)
+    monkeypatch.setenv("CQPI_CONTRACTION", "fp32")
+    cc, _ = _run(name, cqpi.PREC_MIXED)
+    fp64, _ = _run(name, cqpi.PREC_FP64)
+    for e in range(tc.shape[0]):
+        ref = fp64[e, 0]
+        assert np.abs(tc[e, 0] - ref).max() / np.abs(ref).max() <= TOL
+        assert np.abs(tc[e, 0] - cc[e, 0]).max() / np.abs(ref).max() <= TOL
+
+
+def test_tensor_core_kernel_selected(built_lib):
+    import cqpi
+    from cqpi import workloads as W
+    c, m, wf = W.config("C2")
+    eng = cqpi.Engine(m, 16, 64, c.oversamp, c.window, c.eta, precision=cqpi.PREC_MIXED)
+    assert eng.contraction_kind() == "tcgen05"
+    eng64 = cqpi.Engine(m, 16, 64, c.oversamp, c.window, c.eta, precision=cqpi.PREC_FP64)
+    assert eng64.contraction_kind() == "fp64"
+
+
+def test_tensor_core_multi_impurity(built_lib):
+    """Several impurities share u and s; each map must equal its single-impurity run."""
+    import cqpi
+    m, p, wf, z, v, E = case("c2")
+    eng = cqpi.Engine(m, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"],
+                      precision=cqpi.PREC_MIXED)
+    eng.set_orbitals(wf, z)
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+    Vs = np.stack([np.diag(v), 0.2 * (A + A.conj().T), np.diag([0.7, -0.2, 0.1])])
+    eng.set_impurities(Vs)
+    allm = eng.run(E, f32=False, f64=True)
+    for k in range(len(Vs)):
+        eng.set_impurities(Vs[k:k + 1])
+        one = eng.run(E, f32=False, f64=True)
+        assert np.abs(allm[:, k] - one[:, 0]).max() <= 1e-7 * np.abs(one).max()
