@@ -78,7 +78,8 @@ size_t bytes_per_energy(const cqpi_handle *h)
 {
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
     const size_t cs = (h->precision == CQPI_PREC_FP64) ? 16 : 8;
-    return cs * (bb * nk + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
+    const size_t g0k = h->use_fft32 ? 0 : bb * nk;
+    return cs * (g0k + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
 }
 
 void ensure_workspace(cqpi_handle *h, int ebatch)
@@ -91,7 +92,7 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
         dalloc(&h->ws.half, ebatch * bb * (size_t)h->kp * h->NB);
         dalloc(&h->ws.box, ebatch * (size_t)h->NB * h->NB * bb);
     } else {
-        dalloc(&h->ws.g0k32, ebatch * bb * nk);
+        if (!h->use_fft32) dalloc(&h->ws.g0k32, ebatch * bb * nk);
         dalloc(&h->ws.half32, ebatch * bb * (size_t)h->kp * h->NB);
         dalloc(&h->ws.box32, ebatch * (size_t)h->NB * h->NB * bb);
         dalloc(&h->ws.gmax, ebatch);
@@ -155,6 +156,11 @@ void do_bands(cqpi_handle *h)
 // G0(k) -> G0(R) box -> T -> term1 for ne energies already in ws.energies.
 void do_greens(cqpi_handle *h, int ne)
 {
+    if (h->use_fft32) {
+        launch_greens_fft32(h, ne, h->ws.energies);
+        check_launch();
+        return;
+    }
     launch_greens_k(h, ne, h->ws.energies);
     check_launch();
     launch_fft(h, ne);
@@ -317,6 +323,11 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         CK(configure_fft(h));
         // tensor-core contraction for the mixed path (CUDA-core FP32 kernel otherwise);
         // CQPI_CONTRACTION=fp32 selects the CUDA-core kernel explicitly
+        if (h->precision == CQPI_PREC_MIXED && fft32_supported(h)) {
+            const char *f = getenv("CQPI_GREENS");
+            h->use_fft32 = !(f && !strcmp(f, "unfused"));
+            CK(configure_fft32(h));
+        }
         if (h->precision == CQPI_PREC_MIXED && tc_supported(h)) {
             tc_plan(h);
             const char *force = getenv("CQPI_CONTRACTION");

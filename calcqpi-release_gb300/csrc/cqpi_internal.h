@@ -37,12 +37,13 @@ struct TcPlan {
     int KP = 0;          // K padded to a multiple of 16
     int tmem_cols = 0;   // power of two >= 2*nblk*N
     int a_bytes = 0, b_bytes = 0;
+    int sst = 0;         // staging row stride (floats)
     size_t smem = 0;
 };
 
 struct TcParams {
     int b, n, os, w, Rb, NB, W, nblk, mb, bs0, bs1;
-    int TS, N, KP, Q, nimp, ne, wn, ntx;
+    int TS, N, KP, Q, nimp, ne, wn, ntx, sst;
     int tmem_cols, a_bytes, b_bytes;
     float inv_sA;
     long long spin_limit;
@@ -98,6 +99,8 @@ struct cqpi_handle {
     double *d_phi = nullptr;
     float *d_phi32 = nullptr;
     bool orbitals_ready = false;
+    // fused FP32 G0(k) + pruned FFT (mixed path, power-of-two k-grid)
+    bool use_fft32 = false;
     // tcgen05 contraction
     bool use_tc = false;
     cqpi::TcPlan tc;
@@ -138,6 +141,10 @@ void launch_ldos_fp64(cqpi_handle *h, int ne, const double2 *box, const double2 
                       float *out32, double *out64);
 void launch_ldos_fp32(cqpi_handle *h, int ne, const float2 *box, const float2 *T, const double *term1,
                       float *out32, double *out64);
+// fft32.cu
+bool fft32_supported(const cqpi_handle *h);
+cudaError_t configure_fft32(cqpi_handle *h);
+void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies);
 // ldos_tc.cu
 bool tc_supported(const cqpi_handle *h);
 void tc_plan(cqpi_handle *h);

@@ -1,0 +1,260 @@
+// fft32.cu -- mixed-path Green's function: fused G0(k,w) assembly + pruned 2D FFT in FP32
+// for power-of-two k-grids.
+//
+// Replaces, per energy, tmatrix::setgreensfunction (src/qpi.cc:478-486) and
+// tmatrix::calcrealspacegreensfunction (src/qpi.cc:557-578), which transform all b^2
+// kp x kp planes in FP64 with FFTW and keep every R.  Here only the box
+// R in [-Rb, Rb]^2 that the contraction reads is produced:
+//
+//   pass 1 (g0_rowfft): one CTA per k-row i.  For every energy of the batch it builds
+//     G0(k_i, k_j) = sum_n U_n U_n^H / (w - e_n + i eta) for all j and all b^2 planes
+//     directly in shared memory (w - e_n in FP64, the rest in FP32; the eigen data of the
+//     row is re-read from L1/L2 for each energy), runs radix-2 transforms along j on all
+//     planes with one barrier per stage, and stores the NB pruned outputs Y = yb - Rb.
+//     No G0(k) array ever reaches HBM.
+//   pass 2 (colfft): NC adjacent columns yb per CTA, transforms along i, keeps
+//     X = xb - Rb, scales by kp^-2 and records max|Re|,|Im| per energy (the operand
+//     scale of the tensor-core contraction).
+//
+// Shared-memory rows are padded by one element per 32 (index p + p/32) so that the
+// bit-reversed stores and the short-stride butterflies do not collide on banks.
+// Roofline: pass 1 reads the eigen cache (96 B per k-point for 3 bands) and writes
+// b^2 * kp * NB complex values; both passes are shared-memory / issue bound at
+// kp = 1024 (0.6 GFLOP per energy), see profiles/.
+#include <algorithm>
+
+#include "cplx.h"
+#include "cqpi_internal.h"
+
+namespace cqpi {
+
+__device__ __forceinline__ int pad32(int x) { return x + (x >> 5); }
+__device__ __forceinline__ int brev_bits(int x, int bits) { return bits == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - bits)); }
+__device__ __forceinline__ int pmod(int a, int m) { int r = a % m; return r < 0 ? r + m : r; }
+
+template <int B>
+__global__ void __launch_bounds__(256) g0_rowfft_kernel(int b, int kp, int logkp, int NB, int Rb, int pg, double eta,
+                                                        const double *__restrict__ energies, int ne,
+                                                        const double *__restrict__ eval, const float2 *__restrict__ evec,
+                                                        const float2 *__restrict__ tw, float2 *__restrict__ half)
+{
+    extern __shared__ __align__(16) float2 sm[];
+    const int bb = b * b;
+    const long long nk = (long long)kp * kp;
+    const int i = blockIdx.x;
+    const int plen = pad32(kp) + 1;
+    float2 *tws = sm + (size_t)pg * plen;
+    const int hk = kp >> 1;
+    for (int t = threadIdx.x; t < hk; t += blockDim.x) tws[t] = tw[t];
+    const float et = (float)eta;
+
+    for (int e = 0; e < ne; e++) {
+        const double om = energies[e];
+        for (int pl0 = 0; pl0 < bb; pl0 += pg) {
+            const int npl = min(pg, bb - pl0);
+            __syncthreads();   // previous users of the plane buffers are done
+            // ---- G0(k) of this row for planes [pl0, pl0+npl), bit-reversed positions
+            for (int j = threadIdx.x; j < kp; j += blockDim.x) {
+                const long long k = (long long)i * kp + j;
+                float2 f[B];
+#pragma unroll
+                for (int n = 0; n < B; n++) {
+                    if (n < b) {
+                        const float dr = (float)(om - eval[(size_t)n * nk + k]);
+                        const float den = dr * dr + et * et;
+                        f[n] = make_float2(dr / den, -et / den);
+                    }
+                }
+                const int pos = pad32(brev_bits(j, logkp));
+                if (B <= 6 && npl == bb) {
+                    // all planes at once: eigenvectors of this k-point in registers
+                    float2 U[B][B];
+#pragma unroll
+                    for (int o = 0; o < B; o++)
+#pragma unroll
+                        for (int n = 0; n < B; n++)
+                            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+#pragma unroll
+                    for (int o = 0; o < B; o++) {
+                        if (o >= b) continue;
+                        float2 x[B];
+#pragma unroll
+                        for (int n = 0; n < B; n++)
+                            if (n < b) x[n] = cmul(U[o][n], f[n]);
+#pragma unroll
+                        for (int a = 0; a < B; a++) {
+                            if (a >= b) continue;
+                            float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int n = 0; n < B; n++) {
+                                if (n < b) {
+                                    s.x += x[n].x * U[a][n].x + x[n].y * U[a][n].y;   // x * conj(U[a][n])
+                                    s.y += x[n].y * U[a][n].x - x[n].x * U[a][n].y;
+                                }
+                            }
+                            sm[(size_t)(o * b + a) * plen + pos] = s;
+                        }
+                    }
+                } else {
+                    for (int q = 0; q < npl; q++) {
+                        const int pl = pl0 + q, o = pl / b, a = pl - o * b;
+                        float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int n = 0; n < B; n++) {
+                            if (n < b) {
+                                const float2 uo = evec[(size_t)(o * b + n) * nk + k];
+                                const float2 ua = evec[(size_t)(a * b + n) * nk + k];
+                                const float2 x = cmul(uo, f[n]);
+                                s.x += x.x * ua.x + x.y * ua.y;   // x * conj(ua)
+                                s.y += x.y * ua.x - x.x * ua.y;
+                            }
+                        }
+                        sm[(size_t)q * plen + pos] = s;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- radix-2 decimation in time over all planes of the group
+            const int nbf = npl * hk;
+            for (int s = 0; s < logkp; s++) {
+                const int hl = 1 << s, tsh = logkp - 1 - s;
+                for (int t = threadIdx.x; t < nbf; t += blockDim.x) {
+                    const int q = t >> (logkp - 1), tt = t & (hk - 1);
+                    const int kk = tt & (hl - 1);
+                    const int idx = ((tt >> s) << (s + 1)) | kk;
+                    float2 *a = sm + (size_t)q * plen;
+                    const float2 w = tws[kk << tsh];
+                    const float2 u = a[pad32(idx)], v = cmul(a[pad32(idx + hl)], w);
+                    a[pad32(idx)] = cadd(u, v);
+                    a[pad32(idx + hl)] = csub(u, v);
+                }
+                __syncthreads();
+            }
+            // ---- pruned outputs
+            for (int q = 0; q < npl; q++) {
+                float2 *dst = half + (((size_t)e * bb + pl0 + q) * kp + i) * NB;
+                const float2 *a = sm + (size_t)q * plen;
+                for (int yb = threadIdx.x; yb < NB; yb += blockDim.x) dst[yb] = a[pad32(pmod(yb - Rb, kp))];
+            }
+        }
+    }
+}
+
+// Pass 2: NC = 2^lnc adjacent columns (fixed plane, energy), transform along i.
+__global__ void __launch_bounds__(256) colfft_kernel(int kp, int logkp, int NB, int Rb, int bb, int lnc, float scale,
+                                                     const float2 *__restrict__ half, const float2 *__restrict__ tw,
+                                                     float2 *__restrict__ box, unsigned *__restrict__ gmax)
+{
+    extern __shared__ __align__(16) float2 sm[];
+    const int NC = 1 << lnc;
+    const int yb0 = blockIdx.x * NC, pl = blockIdx.y, e = blockIdx.z;
+    const int hk = kp >> 1;
+    float2 *tws = sm + (size_t)kp * NC;
+    for (int t = threadIdx.x; t < hk; t += blockDim.x) tws[t] = tw[t];
+    const float2 *src = half + ((size_t)e * bb + pl) * (size_t)kp * NB;
+    for (int idx = threadIdx.x; idx < kp * NC; idx += blockDim.x) {
+        const int ii = idx >> lnc, c = idx & (NC - 1), yb = yb0 + c;
+        sm[(brev_bits(ii, logkp) << lnc) + c] = (yb < NB) ? src[(size_t)ii * NB + yb] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int s = 0; s < logkp; s++) {
+        const int hl = 1 << s, tsh = logkp - 1 - s;
+        for (int t = threadIdx.x; t < hk * NC; t += blockDim.x) {
+            const int c = t & (NC - 1), bt = t >> lnc;
+            const int kk = bt & (hl - 1);
+            const int idx = ((bt >> s) << (s + 1)) | kk;
+            const float2 w = tws[kk << tsh];
+            const float2 u = sm[(idx << lnc) + c], v = cmul(sm[((idx + hl) << lnc) + c], w);
+            sm[(idx << lnc) + c] = cadd(u, v);
+            sm[((idx + hl) << lnc) + c] = csub(u, v);
+        }
+        __syncthreads();
+    }
+    float2 *dst = box + (size_t)e * NB * NB * bb;
+    float mx = 0.0f;
+    const int tot = NB * NC;
+    const int lim = ((tot + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
+    for (int idx = threadIdx.x; idx < lim; idx += blockDim.x) {
+        const int xb = idx >> lnc, c = idx & (NC - 1), yb = yb0 + c;
+        if (idx < tot && yb < NB) {
+            const float2 v = cscale(sm[(pmod(xb - Rb, kp) << lnc) + c], scale);
+            dst[((size_t)xb * NB + yb) * bb + pl] = v;
+            mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(gmax + e, __float_as_uint(mx));
+}
+
+static int ilog2i(int v)
+{
+    int l = 0;
+    while ((1 << l) < v) l++;
+    return l;
+}
+
+// planes per pass-1 CTA: shared memory <= 96 KiB
+static int rowfft_plane_group(const cqpi_handle *h)
+{
+    const size_t plen = (size_t)h->kp + (h->kp >> 5) + 1;
+    int pg = (int)((96 * 1024 - 4 * (size_t)h->kp) / (8 * plen));
+    return std::max(1, std::min(pg, h->b * h->b));
+}
+
+static int colfft_lnc(int kp)
+{
+    int lnc = 4;   // 16 columns
+    while (lnc > 0 && (size_t)8 * kp * (1 << lnc) + 4 * (size_t)kp > 120 * 1024) lnc--;
+    return lnc;
+}
+
+bool fft32_supported(const cqpi_handle *h) { return h->kp >= 2 && (h->kp & (h->kp - 1)) == 0 && h->kp <= 8192; }
+
+cudaError_t configure_fft32(cqpi_handle *h)
+{
+    if (!fft32_supported(h)) return cudaSuccess;
+    const int pg = rowfft_plane_group(h);
+    const size_t s1 = 8 * ((size_t)pg * (h->kp + (h->kp >> 5) + 1) + h->kp / 2);
+    const size_t s2 = 8 * ((size_t)h->kp * (1 << colfft_lnc(h->kp)) + h->kp / 2);
+    cudaError_t e;
+#define CQPI_SETSMEM(K) e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1); if (e != cudaSuccess) return e;
+    CQPI_SETSMEM(g0_rowfft_kernel<1>) CQPI_SETSMEM(g0_rowfft_kernel<2>) CQPI_SETSMEM(g0_rowfft_kernel<3>)
+    CQPI_SETSMEM(g0_rowfft_kernel<4>) CQPI_SETSMEM(g0_rowfft_kernel<6>) CQPI_SETSMEM(g0_rowfft_kernel<8>)
+    CQPI_SETSMEM(g0_rowfft_kernel<10>) CQPI_SETSMEM(g0_rowfft_kernel<12>) CQPI_SETSMEM(g0_rowfft_kernel<16>)
+#undef CQPI_SETSMEM
+    return cudaFuncSetAttribute(colfft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+}
+
+template <int B>
+static void launch_rowfft(cqpi_handle *h, int ne, const double *d_energies, int pg, size_t smem)
+{
+    g0_rowfft_kernel<B><<<h->kp, 256, smem, h->stream>>>(h->b, h->kp, ilog2i(h->kp), h->NB, h->Rb, pg, h->eta,
+                                                         d_energies, ne, h->d_eval, h->d_evec32, h->d_tw32,
+                                                         h->ws.half32);
+}
+
+void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies)
+{
+    const int pg = rowfft_plane_group(h);
+    const size_t s1 = 8 * ((size_t)pg * (h->kp + (h->kp >> 5) + 1) + h->kp / 2);
+    const int b = h->b;
+    if (b <= 1) launch_rowfft<1>(h, ne, d_energies, pg, s1);
+    else if (b <= 2) launch_rowfft<2>(h, ne, d_energies, pg, s1);
+    else if (b <= 3) launch_rowfft<3>(h, ne, d_energies, pg, s1);
+    else if (b <= 4) launch_rowfft<4>(h, ne, d_energies, pg, s1);
+    else if (b <= 6) launch_rowfft<6>(h, ne, d_energies, pg, s1);
+    else if (b <= 8) launch_rowfft<8>(h, ne, d_energies, pg, s1);
+    else if (b <= 10) launch_rowfft<10>(h, ne, d_energies, pg, s1);
+    else if (b <= 12) launch_rowfft<12>(h, ne, d_energies, pg, s1);
+    else launch_rowfft<16>(h, ne, d_energies, pg, s1);
+    h->launches++;
+    const int lnc = colfft_lnc(h->kp), NC = 1 << lnc;
+    const size_t s2 = 8 * ((size_t)h->kp * NC + h->kp / 2);
+    dim3 grid(cdiv(h->NB, NC), h->b * h->b, ne);
+    colfft_kernel<<<grid, 256, s2, h->stream>>>(h->kp, ilog2i(h->kp), h->NB, h->Rb, h->b * h->b, lnc,
+                                                (float)(1.0 / ((double)h->kp * h->kp)), h->ws.half32, h->d_tw32,
+                                                h->ws.box32, h->ws.gmax);
+    h->launches++;
+}
+
+}  // namespace cqpi

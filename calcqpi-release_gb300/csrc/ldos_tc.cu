@@ -160,8 +160,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
     float *winS = winU + wfl + 4;               // +4: a zero slot used by padded k columns
     int *tblU = reinterpret_cast<int *>(winS + wfl + 4);
     int *tblS = tblU + p.nblk * p.KP;
-    float *stage = reinterpret_cast<float *>(tblS + p.nblk * p.KP);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(stage + ((p.os * p.TS * p.os + 3) & ~3));
+    int *rowU = tblS + p.nblk * p.KP;           // per operand row n = (a, re/im, site): window base
+    int *rowS = rowU + p.N;
+    float *stage = reinterpret_cast<float *>(rowS + p.N);
+    const int wt = p.TS * p.os;                 // staged tile width (pixels)
+    const int sst = p.sst;                      // staging row stride, skewed against bank conflicts
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(stage + ((p.os * sst + 3) & ~3));
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
 
     {   // A operands (Phi hi/lo of every spin block) -> shared memory, once
@@ -184,6 +188,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
             tblU[i] = -1;
             tblS[i] = -1;
         }
+    }
+    for (int nrow = tid; nrow < p.N; nrow += TC_THREADS) {
+        const int ari = nrow / p.TS, sl = nrow % p.TS, a = ari >> 1, ri = ari & 1;
+        rowU[nrow] = 2 * sl * side * bb + 2 * a + ri;
+        rowS[nrow] = 2 * (p.TS - 1 - sl) * side * bb + 2 * a * p.b + ri;
     }
     if (tid < 4) { winU[wfl + tid] = 0.f; winS[wfl + tid] = 0.f; }
     if (tid == 0) {
@@ -218,22 +227,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
         // ---- stage the scaled G0 windows: u: X in [px0-w, px0+TS-1+w], Y in [py-w, py+w];
         //      s: X in [-px0-TS+1-w, -px0+w], Y in [-py-w, -py+w]  (zero outside the box)
         {
-            const int rowlen = side * bb;              // complex values per window x-row
-            const int total = 2 * wx * rowlen;
-            for (int idx = tid; idx < total; idx += TC_THREADS) {
-                const int which = idx / (wx * rowlen), r = idx % (wx * rowlen);
-                const int xl = r / rowlen, c = r % rowlen;
+            // one warp per window x-row: for fixed X the Y range and all b^2 planes are a
+            // contiguous segment of side*b^2 complex values in the box; Y always lies in
+            // the box, X only leaves it for padded sites past the field of view
+            const int rowlen = side * bb;
+            for (int seg = warp; seg < 2 * wx; seg += TC_THREADS / 32) {
+                const int which = seg >= wx, xl = which ? seg - wx : seg;
                 const int X = which == 0 ? px0 - p.w + xl : -px0 - (p.TS - 1) - p.w + xl;
                 const int Y0 = which == 0 ? py - p.w : -py - p.w;
-                float2 v = make_float2(0.f, 0.f);
-                if (X >= -p.Rb && X <= p.Rb) {
-                    const int yl = c / bb, pl = c % bb;
-                    const int Y = Y0 + yl;
-                    if (Y >= -p.Rb && Y <= p.Rb) v = boxe[((size_t)(X + p.Rb) * p.NB + (Y + p.Rb)) * bb + pl];
+                float *w = (which == 0 ? winU : winS) + 2 * xl * rowlen;
+                const bool in = X >= -p.Rb && X <= p.Rb;
+                const float2 *src = in ? boxe + ((size_t)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb : boxe;
+                for (int c = (tid & 31); c < rowlen; c += 32) {
+                    const float2 v = in ? src[c] : make_float2(0.f, 0.f);
+                    w[2 * c] = v.x * sB;
+                    w[2 * c + 1] = v.y * sB;
                 }
-                float *w = which == 0 ? winU : winS;
-                w[2 * r] = v.x * sB;
-                w[2 * r + 1] = v.y * sB;
             }
         }
         __syncthreads();
@@ -241,17 +250,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
         for (int blk = 0; blk < p.nblk && ok; blk++) {
             // ---- B operands from the windows: rows n = (a, re/im, site), 8 k per item
             const int *tU = tblU + blk * p.KP, *tS = tblS + blk * p.KP;
+            // items (op, kc, nrow) with nrow fastest: a warp writes 32 consecutive 16-byte
+            // operand rows (4 full core matrices), free of bank conflicts
             const int nitems = 2 * p.N * kcs;
+            const float invN = 1.0f / (float)p.N;
             for (int it = tid; it < nitems; it += TC_THREADS) {
-                const int op = it >= p.N * kcs;
-                const int rem = op ? it - p.N * kcs : it;
-                const int nrow = rem / kcs, kc = rem - (rem / kcs) * kcs;
-                const int ari = nrow / p.TS, sl = nrow - ari * p.TS;
-                const int a = ari >> 1, ri = ari & 1;
+                int g = __float2int_rz(((float)it + 0.5f) * invN);   // it / N
+                int nrow = it - g * p.N;
+                if (nrow < 0) { g--; nrow += p.N; }
+                if (nrow >= p.N) { g++; nrow -= p.N; }
+                const int op = g >= kcs, kc = op ? g - kcs : g;
                 const float *w = op ? winS : winU;
                 const int *tb = op ? tS : tU;
-                const int base = op ? (2 * (p.TS - 1 - sl) * side * bb + 2 * a * p.b + ri)
-                                    : (2 * sl * side * bb + 2 * a + ri);
+                const int base = op ? rowS[nrow] : rowU[nrow];
                 float v[8];
 #pragma unroll
                 for (int kk = 0; kk < 8; kk++) {
@@ -303,7 +314,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
 
         // ---- epilogue: each warp group handles TS/4 sites of its lane quarter
         const float inv = p.inv_sA / sB;
-        const int wt = p.TS * p.os;
         for (int imp = 0; imp < p.nimp; imp++) {
             const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
             const double t1 = qvalid ? p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.0;
@@ -341,15 +351,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
                 if (qvalid)
 #pragma unroll
                     for (int u = 0; u < 4; u++)
-                        stage[qy * wt + (s0 + u) * p.os + qx] = (float)(-t1 - (double)(term2[u] * inv * inv));
+                        stage[qy * sst + (s0 + u) * p.os + qx] = (float)(-t1 - (double)(term2[u] * inv * inv));
             }
             __syncthreads();
             const int xbase = i0 * p.os;
+            const int xend = min(wt, p.wn - xbase);
             const size_t rowbase = ((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os;
-            for (int idx = tid; idx < p.os * wt; idx += TC_THREADS) {
-                const int yy = idx / wt, xx = idx - (idx / wt) * wt;
-                const int x = xbase + xx;
-                if (x < p.wn) p.out[(rowbase + yy) * p.wn + x] = stage[yy * wt + xx];
+            for (int yy = warp; yy < p.os; yy += TC_THREADS / 32) {
+                float *dst = p.out + (rowbase + yy) * p.wn + xbase;
+                for (int xx = (tid & 31); xx < xend; xx += 32) dst[xx] = stage[yy * sst + xx];
             }
             __syncthreads();
         }
@@ -406,8 +416,10 @@ void tc_plan(cqpi_handle *h)
     pl.a_bytes = 128 * pl.KP * 2;
     pl.b_bytes = pl.N * pl.KP * 2;
     const size_t wfl = (size_t)(TS + 2 * h->w) * (2 * h->w + 1) * h->b * h->b * 2;
+    const int wt = TS * h->os;
+    pl.sst = wt + ((h->os - wt) % 32 + 32) % 32;   // row r starts on bank r*os: conflict-free q writes
     pl.smem = (size_t)h->nblk * 2 * pl.a_bytes + 4 * (size_t)pl.b_bytes + 4 * (2 * (wfl + 4)) +
-              4 * (size_t)(2 * h->nblk * pl.KP) + 4 * (size_t)((h->os * TS * h->os + 3) & ~3) + 64;
+              4 * (size_t)(2 * h->nblk * pl.KP + 2 * pl.N) + 4 * (size_t)((h->os * pl.sst + 3) & ~3) + 64;
     pl.ok = TS > 0 && cols <= 512 && pl.smem <= 227 * 1024;
 }
 
@@ -448,7 +460,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     TcParams p;
     p.b = h->b; p.n = h->n; p.os = h->os; p.w = h->w; p.Rb = h->Rb; p.NB = h->NB; p.W = h->W;
     p.nblk = h->nblk; p.mb = h->mb; p.bs0 = h->blk_start[0]; p.bs1 = h->blk_start[1];
-    p.TS = pl.TS; p.N = pl.N; p.KP = pl.KP; p.Q = h->Q; p.nimp = h->nimp; p.ne = ne; p.wn = h->wn;
+    p.TS = pl.TS; p.N = pl.N; p.KP = pl.KP; p.sst = pl.sst; p.Q = h->Q; p.nimp = h->nimp; p.ne = ne; p.wn = h->wn;
     p.ntx = (h->n + pl.TS - 1) / pl.TS;
     p.tmem_cols = pl.tmem_cols; p.a_bytes = pl.a_bytes; p.b_bytes = pl.b_bytes;
     p.inv_sA = h->tc_inv_sA;

@@ -96,3 +96,24 @@ def test_tensor_core_multi_impurity(built_lib):
         eng.set_impurities(Vs[k:k + 1])
         one = eng.run(E, f32=False, f64=True)
         assert np.abs(allm[:, k] - one[:, 0]).max() <= 1e-7 * np.abs(one).max()
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "c2_zero"])
+def test_fused_greens_fft_matches_unfused(built_lib, name, monkeypatch):
+    """The fused FP32 G0(k) + pruned FFT gives the same G0(R) box as the two-kernel path."""
+    import cqpi
+    m, p, wf, z, v, E = case(name)
+
+    def box(env):
+        if env:
+            monkeypatch.setenv("CQPI_GREENS", env)
+        else:
+            monkeypatch.delenv("CQPI_GREENS", raising=False)
+        eng = cqpi.Engine(m, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"], spin=p["spin"],
+                          precision=cqpi.PREC_MIXED)
+        eng.set_orbitals(wf, z)
+        return [eng.greens_box(e)[0] for e in E]
+
+    fused, unfused = box(None), box("unfused")
+    for a, b in zip(fused, unfused):
+        assert np.abs(a - b).max() <= 2e-6 * np.abs(b).max()
