@@ -23,7 +23,7 @@ EXPORTED = [
     "cqpi_set_orbitals", "cqpi_set_scattering", "cqpi_set_impurities", "cqpi_solve_bands", "cqpi_run",
     "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
-    "cqpi_contraction_kind",
+    "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc",
 ]
 
 
@@ -84,6 +84,7 @@ def load():
     L.cqpi_stage_times.argtypes = [P, P]
     L.cqpi_measure_fma_peak.argtypes = [i32, ctypes.POINTER(dbl)]
     L.cqpi_contraction_kind.argtypes = [P, ctypes.POINTER(i32)]
+    L.cqpi_realspace_greens_noalloc.argtypes = [P, i32, i32, i32, P, P]
     _lib = L
     return L
 

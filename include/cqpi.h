@@ -27,6 +27,7 @@
 #ifndef CQPI_H
 #define CQPI_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -135,6 +136,27 @@ int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count);
 /* Device time (ms) of the stages of the last cqpi_run, measured with CUDA events on
  * the handle's stream: [0] bands, [1] G0(k)+FFT, [2] T-matrix, [3] contraction, [4] total. */
 int cqpi_stage_times(const cqpi_handle *h, float *ms5);
+
+/* ---- entry point that allocates nothing ------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory:
+ * code running while a CUDA stream capture is active (cudaMalloc is not permitted there)
+ * and hosts that pre-allocate a fixed device-memory budget and must not let a driver
+ * allocation synchronise the device (e.g. a real-time instrument-control loop).
+ * From a caller-owned device array g0k[kpoints][kpoints][bands][bands][2] (G0(k) of one
+ * energy, k-grid order of src/qpi.cc:465-466) it writes the caller-owned device array
+ * box[2rb+1][2rb+1][bands][bands][2] with G0(R) = kp^-2 sum_k G0(k) e^{+2 pi i k.R}
+ * for R in [-rb, rb]^2 (the part of tmatrix::calcrealspacegreensfunction,
+ * src/qpi.cc:557-578, that the LDOS needs), in FP64, asynchronously on 'stream'
+ * (a cudaStream_t; NULL = default stream).
+ * Limits: kpoints <= 4096, bands <= 16, and bands^2 * kpoints * (2rb+1) complex doubles
+ * must fit the fixed scratch array of CQPI_NOALLOC_SCRATCH_BYTES -- larger requests
+ * return CQPI_ERR_NOT_SUPPORTED.  The array is a file-scope __device__ variable held by
+ * every GPU that loads the library until exit; the first call on a device looks up its
+ * address (make it before any stream capture).  Calls share the array, so calls whose
+ * GPU work overlaps race on it.  No call allocates or frees memory. */
+#define CQPI_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
+int cqpi_realspace_greens_noalloc(const double *g0k, int32_t kpoints, int32_t bands, int32_t rb, double *box,
+                                  void *stream);
 
 /* Contraction kernel the handle runs: 0 = FP64 CUDA cores, 1 = FP32 CUDA cores,
  * 2 = tcgen05 tensor cores (split-FP16 x3). */
