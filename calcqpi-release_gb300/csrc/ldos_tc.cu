@@ -287,17 +287,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
             __syncthreads();
             if (tid == 0) {
                 tc_fence_after();
-                const uint32_t aH = smem_u32(smA + (size_t)(blk * 2 + 0) * p.a_bytes);
-                const uint32_t aL = smem_u32(smA + (size_t)(blk * 2 + 1) * p.a_bytes);
+                // descriptors of K-step 0; one K-step (16 halfs = 256 bytes) adds 256 >> 4 = 16
+                const uint64_t aH = sdesc(smem_u32(smA + (size_t)(blk * 2 + 0) * p.a_bytes), 128, sbo);
+                const uint64_t aL = sdesc(smem_u32(smA + (size_t)(blk * 2 + 1) * p.a_bytes), 128, sbo);
+                const int nks = p.KP >> 4;
                 for (int op = 0; op < 2; op++) {
                     const uint32_t d = tmem + (uint32_t)(blk * 2 * p.N + op * p.N);
-                    const uint32_t bH = smem_u32(smB + (size_t)(op * 2 + 0) * p.b_bytes);
-                    const uint32_t bL = smem_u32(smB + (size_t)(op * 2 + 1) * p.b_bytes);
-                    for (int ks = 0; ks < (p.KP >> 4); ks++) {
-                        const uint32_t off = (uint32_t)ks * 256u;
-                        mma_f16(d, sdesc(aH + off, 128, sbo), sdesc(bH + off, 128, sbo), idesc, ks > 0 ? 1u : 0u);
-                        mma_f16(d, sdesc(aH + off, 128, sbo), sdesc(bL + off, 128, sbo), idesc, 1u);
-                        mma_f16(d, sdesc(aL + off, 128, sbo), sdesc(bH + off, 128, sbo), idesc, 1u);
+                    const uint64_t bH = sdesc(smem_u32(smB + (size_t)(op * 2 + 0) * p.b_bytes), 128, sbo);
+                    const uint64_t bL = sdesc(smem_u32(smB + (size_t)(op * 2 + 1) * p.b_bytes), 128, sbo);
+                    for (int ks = 0; ks < nks; ks++) {
+                        const uint64_t o = (uint64_t)(16 * ks);
+                        mma_f16(d, aH + o, bH + o, idesc, ks > 0 ? 1u : 0u);
+                        mma_f16(d, aH + o, bL + o, idesc, 1u);
+                        mma_f16(d, aL + o, bH + o, idesc, 1u);
                     }
                 }
                 mma_commit(smem_u32(mbar));
@@ -316,7 +318,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
         const float inv = p.inv_sA / sB;
         for (int imp = 0; imp < p.nimp; imp++) {
             const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
-            const double t1 = qvalid ? p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.0;
+            const float t1 = qvalid ? (float)p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.f;
+            const float inv2 = inv * inv;
             for (int s0 = sgrp * 4; s0 < p.TS; s0 += 16) {
                 float term2[4] = {0.f, 0.f, 0.f, 0.f};
                 for (int blk = 0; blk < p.nblk; blk++) {
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
                 if (qvalid)
 #pragma unroll
                     for (int u = 0; u < 4; u++)
-                        stage[qy * sst + (s0 + u) * p.os + qx] = (float)(-t1 - (double)(term2[u] * inv * inv));
+                        stage[qy * sst + (s0 + u) * p.os + qx] = -t1 - term2[u] * inv2;
             }
             __syncthreads();
             const int xbase = i0 * p.os;
