@@ -146,6 +146,77 @@ int read_status(cqpi_handle *h)
     return st;
 }
 
+// ---- asynchronous timing: pooled events and pending (stage, start, end) triples
+int record(cqpi_handle *h)
+{
+    int idx;
+    if (!h->ev_free.empty()) {
+        const cudaEvent_t e = h->ev_free.back();
+        h->ev_free.pop_back();
+        h->ev_pool.push_back(e);
+    } else {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        h->ev_pool.push_back(e);
+    }
+    idx = (int)h->ev_pool.size() - 1;
+    CK(cudaEventRecord(h->ev_pool[idx], h->stream));
+    return idx;
+}
+
+void pend(cqpi_handle *h, int stage, int a, int b)
+{
+    h->ev_pending.push_back(stage);
+    h->ev_pending.push_back(a);
+    h->ev_pending.push_back(b);
+}
+
+// Sum the pending stage intervals into stage_ms (totals since the previous query).
+void collect_times(cqpi_handle *h)
+{
+    for (int i = 0; i < 5; i++) h->stage_ms[i] = 0.f;
+    if (!h->ev_pool.empty()) CK(cudaEventSynchronize(h->ev_pool.back()));
+    for (size_t i = 0; i + 2 < h->ev_pending.size(); i += 3) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, h->ev_pool[h->ev_pending[i + 1]], h->ev_pool[h->ev_pending[i + 2]]));
+        h->stage_ms[h->ev_pending[i]] += ms;
+        h->stage_ms[4] += ms;
+    }
+    for (cudaEvent_t e : h->ev_pool) h->ev_free.push_back(e);
+    h->ev_pool.clear();
+    h->ev_pending.clear();
+}
+
+void ensure_energies(cqpi_handle *h, int n)
+{
+    if (h->energies_cap >= n) return;
+    dfree(h->d_energies_all);
+    if (h->h_energies_pinned) cudaFreeHost(h->h_energies_pinned);
+    h->h_energies_pinned = nullptr;
+    h->energies_cap = 0;
+    dalloc(&h->d_energies_all, (size_t)n);
+    CK(cudaMallocHost((void **)&h->h_energies_pinned, sizeof(double) * n));
+    h->energies_cap = n;
+}
+
+void ensure_stage32(cqpi_handle *h, size_t n)
+{
+    if (h->stage_cap32 >= n) return;
+    dfree(h->stage32);
+    h->stage_cap32 = 0;
+    dalloc(&h->stage32, n);
+    h->stage_cap32 = n;
+}
+
+void ensure_stage64(cqpi_handle *h, size_t n)
+{
+    if (h->stage_cap64 >= n) return;
+    dfree(h->stage64);
+    h->stage_cap64 = 0;
+    dalloc(&h->stage64, n);
+    h->stage_cap64 = n;
+}
+
 void do_bands(cqpi_handle *h)
 {
     launch_bands(h);
@@ -154,14 +225,14 @@ void do_bands(cqpi_handle *h)
 }
 
 // G0(k) -> G0(R) box -> T -> term1 for ne energies already in ws.energies.
-void do_greens(cqpi_handle *h, int ne)
+void do_greens(cqpi_handle *h, int ne, const double *d_energies)
 {
     if (h->use_fft32) {
-        launch_greens_fft32(h, ne, h->ws.energies);
+        launch_greens_fft32(h, ne, d_energies);
         check_launch();
         return;
     }
-    launch_greens_k(h, ne, h->ws.energies);
+    launch_greens_k(h, ne, d_energies);
     check_launch();
     launch_fft(h, ne);
     check_launch();
@@ -369,6 +440,12 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_seam_ldos);
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    for (auto e : h->ev_free) cudaEventDestroy(e);
+    dfree(h->d_energies_all);
+    if (h->h_energies_pinned) cudaFreeHost(h->h_energies_pinned);
+    dfree(h->stage32);
+    dfree(h->stage64);
     if (h->stream) cudaStreamDestroy(h->stream);
     cudaGetLastError();
     delete h;
@@ -451,7 +528,9 @@ int cqpi_solve_bands(cqpi_handle *h)
 {
     if (!h) return CQPI_ERR_ARG;
     try {
+        const int a = record(h);
         do_bands(h);
+        pend(h, 0, a, record(h));
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
@@ -466,67 +545,63 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
     if (nE == 0) return CQPI_OK;
     const size_t mapn = (size_t)h->wn * h->wn;
     const size_t per_e = (size_t)h->nimp * mapn;
-    float *stage32 = nullptr;
-    double *stage64 = nullptr;
     try {
         const int eb = choose_batch(h, nE);
         ensure_workspace(h, eb);
-        if (!on_device) {
-            if (maps32) dalloc(&stage32, eb * per_e);
-            if (maps64) dalloc(&stage64, eb * per_e);
-        }
+        ensure_energies(h, nE);
+        if (h->ev_pool.size() > 2048) collect_times(h);   // bounded event pool when nobody queries
+        // host outputs (and float64-only requests on the tensor-core path) go through
+        // device staging buffers kept by the handle
         float *tmp32 = nullptr;
-        if (h->use_tc && !maps32) {
-            if (!stage32) dalloc(&stage32, eb * per_e);
-            tmp32 = stage32;
+        if ((!on_device && maps32) || (h->use_tc && !maps32)) {
+            ensure_stage32(h, (size_t)eb * per_e);
+            tmp32 = h->stage32;
         }
-        float tb = 0, tg = 0, tt = 0, tl = 0;
-        CK(cudaEventRecord(h->ev[0], h->stream));
-        if (!h->bands_ready) do_bands(h);
-        CK(cudaEventRecord(h->ev[1], h->stream));
-        CK(cudaEventSynchronize(h->ev[1]));
-        CK(cudaEventElapsedTime(&tb, h->ev[0], h->ev[1]));
+        if (!on_device && maps64) ensure_stage64(h, (size_t)eb * per_e);
+        memcpy(h->h_energies_pinned, energies, sizeof(double) * nE);
+        CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * nE, cudaMemcpyHostToDevice,
+                           h->stream));
+        if (!h->bands_ready) {
+            const int a = record(h);
+            do_bands(h);
+            pend(h, 0, a, record(h));
+        }
         for (int e0 = 0; e0 < nE; e0 += eb) {
             const int ne = std::min(eb, nE - e0);
-            CK(cudaMemcpyAsync(h->ws.energies, energies + e0, sizeof(double) * ne, cudaMemcpyHostToDevice, h->stream));
+            const double *den = h->d_energies_all + e0;
             if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
-            CK(cudaEventRecord(h->ev[2], h->stream));
-            do_greens(h, ne);
-            CK(cudaEventRecord(h->ev[3], h->stream));
+            const int t0 = record(h);
+            do_greens(h, ne, den);
+            const int t1 = record(h);
             launch_tmatrix(h, ne);
             check_launch();
             launch_term1(h, ne);
             check_launch();
-            CK(cudaEventRecord(h->ev[4], h->stream));
-            float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : stage32) : nullptr;
-            double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : stage64) : nullptr;
+            const int t2 = record(h);
+            float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : h->stage32) : nullptr;
+            double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : h->stage64) : nullptr;
             launch_contraction(h, ne, o32, o64, tmp32);
             check_launch();
-            CK(cudaEventRecord(h->ev[5], h->stream));
+            const int t3 = record(h);
+            pend(h, 1, t0, t1);
+            pend(h, 2, t1, t2);
+            pend(h, 3, t2, t3);
             if (!on_device) {
                 if (maps32)
-                    CK(cudaMemcpyAsync(maps32 + (size_t)e0 * per_e, stage32, sizeof(float) * ne * per_e,
+                    CK(cudaMemcpyAsync(maps32 + (size_t)e0 * per_e, h->stage32, sizeof(float) * ne * per_e,
                                        cudaMemcpyDeviceToHost, h->stream));
                 if (maps64)
-                    CK(cudaMemcpyAsync(maps64 + (size_t)e0 * per_e, stage64, sizeof(double) * ne * per_e,
+                    CK(cudaMemcpyAsync(maps64 + (size_t)e0 * per_e, h->stage64, sizeof(double) * ne * per_e,
                                        cudaMemcpyDeviceToHost, h->stream));
             }
-            CK(cudaEventSynchronize(h->ev[5]));
-            float a, c, d;
-            CK(cudaEventElapsedTime(&a, h->ev[2], h->ev[3]));
-            CK(cudaEventElapsedTime(&c, h->ev[3], h->ev[4]));
-            CK(cudaEventElapsedTime(&d, h->ev[4], h->ev[5]));
-            tg += a; tt += c; tl += d;
         }
-        CK(cudaStreamSynchronize(h->stream));
-        h->stage_ms[0] = tb; h->stage_ms[1] = tg; h->stage_ms[2] = tt; h->stage_ms[3] = tl;
-        h->stage_ms[4] = tb + tg + tt + tl;
-        dfree(stage32);
-        dfree(stage64);
-        if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
+        h->status_pending = true;
+        if (!on_device) {
+            CK(cudaStreamSynchronize(h->stream));
+            h->status_pending = false;
+            if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
+        }
     } catch (const CudaError &e) {
-        dfree(stage32);
-        dfree(stage64);
         return cuda_fail(h, e);
     }
     return CQPI_OK;
@@ -570,7 +645,7 @@ int cqpi_get_greens_box(cqpi_handle *h, double energy, double *box, int32_t *rb)
         if (!h->bands_ready) do_bands(h);
         CK(cudaMemcpyAsync(h->ws.energies, &energy, sizeof(double), cudaMemcpyHostToDevice, h->stream));
         if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned), h->stream));
-        do_greens(h, 1);
+        do_greens(h, 1, h->ws.energies);
         const size_t cnt = (size_t)h->NB * h->NB * h->b * h->b;
         if (h->precision == CQPI_PREC_FP64) {
             CK(cudaMemcpyAsync(box, h->ws.box, sizeof(double2) * cnt, cudaMemcpyDeviceToHost, h->stream));
@@ -594,7 +669,7 @@ int cqpi_get_tmatrix(cqpi_handle *h, double energy, double *T)
         ensure_workspace(h, 1);
         if (!h->bands_ready) do_bands(h);
         CK(cudaMemcpyAsync(h->ws.energies, &energy, sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        do_greens(h, 1);
+        do_greens(h, 1, h->ws.energies);
         launch_tmatrix(h, 1);
         check_launch();
         CK(cudaMemcpyAsync(T, h->ws.T, sizeof(double2) * h->b * h->b, cudaMemcpyDeviceToHost, h->stream));
@@ -669,6 +744,14 @@ int cqpi_synchronize(cqpi_handle *h)
     if (!h) return CQPI_ERR_ARG;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, CudaError{e, "cudaStreamSynchronize"});
+    if (h->status_pending) {
+        h->status_pending = false;
+        try {
+            if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of a run");
+        } catch (const CudaError &ce) {
+            return cuda_fail(h, ce);
+        }
+    }
     return CQPI_OK;
 }
 
@@ -686,9 +769,14 @@ int cqpi_contraction_kind(const cqpi_handle *h, int32_t *kind)
     return CQPI_OK;
 }
 
-int cqpi_stage_times(const cqpi_handle *h, float *ms5)
+int cqpi_stage_times(cqpi_handle *h, float *ms5)
 {
     if (!h || !ms5) return CQPI_ERR_ARG;
+    try {
+        collect_times(h);
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
     for (int i = 0; i < 5; i++) ms5[i] = h->stage_ms[i];
     return CQPI_OK;
 }

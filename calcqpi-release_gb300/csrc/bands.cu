@@ -16,7 +16,8 @@ template <int B>
 __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, double efermi, int nR,
                                                     const int32_t *__restrict__ R, const double2 *__restrict__ tn,
                                                     const double2 *__restrict__ ta, double *__restrict__ eval,
-                                                    double2 *__restrict__ evec, float2 *__restrict__ evec32)
+                                                    double2 *__restrict__ evec, float2 *__restrict__ evec32,
+                                                    const double2 *__restrict__ tw)
 {
     const long long nk = (long long)kp * kp;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -37,12 +38,13 @@ __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, do
         if (p < b) ar[p][p] = (p < scmax) ? -efermi : efermi;
 
     // H(k) = diag + sum_R tn(R) e^{+i th} + ta(R) e^{-i th},  th = 2 pi (Rx x_i + Ry y_j).
-    // The phase is reduced exactly: (Rx i + Ry j) mod kp (x_i and i/kp differ by an integer).
+    // The phase is reduced exactly, (Rx i + Ry j) mod kp (x_i and i/kp differ by an
+    // integer), and read from the FP64 table tw[t] = e^{+2 pi i t / kp}.
     for (int r = 0; r < nR; r++) {
         long long mm = ((long long)R[2 * r] * i + (long long)R[2 * r + 1] * j) % kp;
         if (mm < 0) mm += kp;
-        double s, c;
-        sincospi(2.0 * (double)mm / (double)kp, &s, &c);
+        const double2 ph = __ldg(tw + mm);
+        const double c = ph.x, s = ph.y;
         const double2 *tnr = tn + (size_t)r * bb, *tar = ta + (size_t)r * bb;
 #pragma unroll
         for (int p = 0; p < B; p++)
@@ -71,10 +73,11 @@ __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, do
         for (int p = 0; p < B - 1; p++)
 #pragma unroll
             for (int q = p + 1; q < B; q++) {
-                const double cab = hypot(ar[p][q], ai[p][q]);
-                if (cab == 0.0) continue;
-                const double er = ar[p][q] / cab, ei = ai[p][q] / cab;
-                const double tau = (ar[q][q] - ar[p][p]) / (2.0 * cab);
+                const double c2 = ar[p][q] * ar[p][q] + ai[p][q] * ai[p][q];
+                if (c2 == 0.0) continue;
+                const double rc = rsqrt(c2), cab = c2 * rc;
+                const double er = ar[p][q] * rc, ei = ai[p][q] * rc;
+                const double tau = (ar[q][q] - ar[p][p]) * (0.5 * rc);
                 const double tt = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
                 const double cs = rsqrt(1.0 + tt * tt), sn = tt * cs;
                 // columns: X = A G, V = V G with G = [[cs, sn], [-sn e^{-ia}, cs e^{-ia}]]
@@ -121,7 +124,7 @@ static void launch_bands_t(cqpi_handle *h)
     const long long nk = (long long)h->kp * h->kp;
     bands_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, h->kp, h->scmax, h->efermi, h->nR, h->d_R,
                                                           (const double2 *)h->d_tn, (const double2 *)h->d_ta,
-                                                          h->d_eval, h->d_evec, h->d_evec32);
+                                                          h->d_eval, h->d_evec, h->d_evec32, h->d_tw);
     h->launches++;
 }
 

@@ -39,6 +39,9 @@ struct TcPlan {
     int a_bytes = 0, b_bytes = 0;
     int sst = 0;         // staging row stride (floats)
     size_t smem = 0;
+    bool pipe = false;   // pipelined variant usable (one spin block)
+    int pipe_tmem_cols = 0;
+    size_t pipe_smem = 0;
 };
 
 struct TcParams {
@@ -122,6 +125,16 @@ struct cqpi_handle {
     int64_t launches = 0;
     float stage_ms[5] = {0, 0, 0, 0, 0};
     cudaEvent_t ev[8] = {};
+    // asynchronous runs: pooled timing events, pending (stage, start, end) triples,
+    // all-energies buffer with a page-locked host mirror, host-output staging
+    std::vector<cudaEvent_t> ev_pool, ev_free;
+    std::vector<int> ev_pending;               // triples: stage, start index, end index into ev_pool
+    double *d_energies_all = nullptr, *h_energies_pinned = nullptr;
+    int energies_cap = 0;
+    float *stage32 = nullptr;
+    double *stage64 = nullptr;
+    size_t stage_cap32 = 0, stage_cap64 = 0;
+    bool status_pending = false;
     std::string err;
 };
 

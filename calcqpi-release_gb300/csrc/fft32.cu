@@ -22,6 +22,8 @@
 // b^2 * kp * NB complex values; both passes are shared-memory / issue bound at
 // kp = 1024 (0.6 GFLOP per energy), see profiles/.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "cplx.h"
 #include "cqpi_internal.h"
@@ -140,6 +142,174 @@ __global__ void __launch_bounds__(256) g0_rowfft_kernel(int b, int kp, int logkp
     }
 }
 
+
+// ------------------------------------------------------------------ register four-step row transform
+// e^{+2 pi i k / 64}, k = 0..63 (cos, sin rounded to float): twiddles of the register FFTs
+__constant__ float2 c_w64[64] = {
+    {1.000000000e+00f, 0.000000000e+00f}, {9.951847267e-01f, 9.801714033e-02f}, {9.807852804e-01f, 1.950903220e-01f}, {9.569403357e-01f, 2.902846773e-01f},
+    {9.238795325e-01f, 3.826834324e-01f}, {8.819212643e-01f, 4.713967368e-01f}, {8.314696123e-01f, 5.555702330e-01f}, {7.730104534e-01f, 6.343932842e-01f},
+    {7.071067812e-01f, 7.071067812e-01f}, {6.343932842e-01f, 7.730104534e-01f}, {5.555702330e-01f, 8.314696123e-01f}, {4.713967368e-01f, 8.819212643e-01f},
+    {3.826834324e-01f, 9.238795325e-01f}, {2.902846773e-01f, 9.569403357e-01f}, {1.950903220e-01f, 9.807852804e-01f}, {9.801714033e-02f, 9.951847267e-01f},
+    {6.123233996e-17f, 1.000000000e+00f}, {-9.801714033e-02f, 9.951847267e-01f}, {-1.950903220e-01f, 9.807852804e-01f}, {-2.902846773e-01f, 9.569403357e-01f},
+    {-3.826834324e-01f, 9.238795325e-01f}, {-4.713967368e-01f, 8.819212643e-01f}, {-5.555702330e-01f, 8.314696123e-01f}, {-6.343932842e-01f, 7.730104534e-01f},
+    {-7.071067812e-01f, 7.071067812e-01f}, {-7.730104534e-01f, 6.343932842e-01f}, {-8.314696123e-01f, 5.555702330e-01f}, {-8.819212643e-01f, 4.713967368e-01f},
+    {-9.238795325e-01f, 3.826834324e-01f}, {-9.569403357e-01f, 2.902846773e-01f}, {-9.807852804e-01f, 1.950903220e-01f}, {-9.951847267e-01f, 9.801714033e-02f},
+    {-1.000000000e+00f, 1.224646799e-16f}, {-9.951847267e-01f, -9.801714033e-02f}, {-9.807852804e-01f, -1.950903220e-01f}, {-9.569403357e-01f, -2.902846773e-01f},
+    {-9.238795325e-01f, -3.826834324e-01f}, {-8.819212643e-01f, -4.713967368e-01f}, {-8.314696123e-01f, -5.555702330e-01f}, {-7.730104534e-01f, -6.343932842e-01f},
+    {-7.071067812e-01f, -7.071067812e-01f}, {-6.343932842e-01f, -7.730104534e-01f}, {-5.555702330e-01f, -8.314696123e-01f}, {-4.713967368e-01f, -8.819212643e-01f},
+    {-3.826834324e-01f, -9.238795325e-01f}, {-2.902846773e-01f, -9.569403357e-01f}, {-1.950903220e-01f, -9.807852804e-01f}, {-9.801714033e-02f, -9.951847267e-01f},
+    {-1.836970199e-16f, -1.000000000e+00f}, {9.801714033e-02f, -9.951847267e-01f}, {1.950903220e-01f, -9.807852804e-01f}, {2.902846773e-01f, -9.569403357e-01f},
+    {3.826834324e-01f, -9.238795325e-01f}, {4.713967368e-01f, -8.819212643e-01f}, {5.555702330e-01f, -8.314696123e-01f}, {6.343932842e-01f, -7.730104534e-01f},
+    {7.071067812e-01f, -7.071067812e-01f}, {7.730104534e-01f, -6.343932842e-01f}, {8.314696123e-01f, -5.555702330e-01f}, {8.819212643e-01f, -4.713967368e-01f},
+    {9.238795325e-01f, -3.826834324e-01f}, {9.569403357e-01f, -2.902846773e-01f}, {9.807852804e-01f, -1.950903220e-01f}, {9.951847267e-01f, -9.801714033e-02f},
+};
+
+// In-register radix-2 DFT of length L (sign +1), natural order in and out.
+template <int L>
+__device__ __forceinline__ void fft_reg(float2 (&x)[L])
+{
+    constexpr int LOG = (L == 2) ? 1 : (L == 4) ? 2 : (L == 8) ? 3 : (L == 16) ? 4 : (L == 32) ? 5 : 6;
+#pragma unroll
+    for (int i = 0; i < L; i++) {
+        int j = 0;
+#pragma unroll
+        for (int bt = 0; bt < LOG; bt++) j |= ((i >> bt) & 1) << (LOG - 1 - bt);
+        if (j > i) { const float2 t = x[i]; x[i] = x[j]; x[j] = t; }
+    }
+    // butterflies as one flat loop of constant trip count per stage, so that every index
+    // is a compile-time constant and x stays in registers
+#pragma unroll
+    for (int s = 0; s < LOG; s++) {
+#pragma unroll
+        for (int t = 0; t < L / 2; t++) {
+            const int hl = 1 << s;
+            const int k = t & (hl - 1);
+            const int i0 = ((t >> s) << (s + 1)) | k;
+            const float2 w = c_w64[k * (64 >> (s + 1))];
+            const float2 u = x[i0], v = cmul(x[i0 + hl], w);
+            x[i0] = cadd(u, v);
+            x[i0 + hl] = csub(u, v);
+        }
+    }
+}
+
+// Pass 1 with the transform along j done as kp = N1 x N2: for each n1 a length-N2 FFT over
+// n2 of x[n1 + N1 n2] (registers), twiddle e^{+2 pi i n1 k2 / kp}, then for each k2 a
+// length-N1 FFT over n1 (registers) giving X[k2 + N2 k1].  One shared-memory exchange
+// between the two passes instead of log2(kp) butterfly rounds.  BM: largest band count
+// whose eigenvectors are kept in registers during the G0 build.
+template <int N1, int N2, int BM = 4>
+__global__ void __launch_bounds__(256) g0_rowfft_reg_kernel(int b, int NB, int Rb, int pg, double eta,
+                                                            const double *__restrict__ energies, int ne,
+                                                            const double *__restrict__ eval,
+                                                            const float2 *__restrict__ evec,
+                                                            const float2 *__restrict__ tw, float2 *__restrict__ half)
+{
+    constexpr int KP = N1 * N2;
+    extern __shared__ __align__(16) float2 sm[];
+    const int bb = b * b;
+    const long long nk = (long long)KP * KP;
+    const int i = blockIdx.x;
+    constexpr int PLEN = KP + KP / 32 + 1;
+    float2 *tws = sm + (size_t)pg * PLEN;        // e^{+2 pi i t / kp}, t < kp
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
+    const float et = (float)eta;
+
+    for (int e = 0; e < ne; e++) {
+        const double om = energies[e];
+        for (int pl0 = 0; pl0 < bb; pl0 += pg) {
+            const int npl = min(pg, bb - pl0);
+            __syncthreads();
+            // ---- G0(k) for planes [pl0, pl0+npl), natural order j (padded)
+            for (int j = threadIdx.x; j < KP; j += blockDim.x) {
+                const long long k = (long long)i * KP + j;
+                const int pos = pad32(j);
+                if (b <= BM && npl == bb) {
+                    float2 f[BM], U[BM][BM];
+#pragma unroll
+                    for (int n = 0; n < BM; n++) {
+                        if (n < b) {
+                            const float dr = (float)(om - eval[(size_t)n * nk + k]);
+                            const float den = dr * dr + et * et;
+                            f[n] = make_float2(dr / den, -et / den);
+                        }
+                    }
+#pragma unroll
+                    for (int o = 0; o < BM; o++)
+#pragma unroll
+                        for (int n = 0; n < BM; n++)
+                            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+#pragma unroll
+                    for (int o = 0; o < BM; o++) {
+                        if (o >= b) continue;
+                        float2 x[BM];
+#pragma unroll
+                        for (int n = 0; n < BM; n++)
+                            if (n < b) x[n] = cmul(U[o][n], f[n]);
+#pragma unroll
+                        for (int a = 0; a < BM; a++) {
+                            if (a >= b) continue;
+                            float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int n = 0; n < BM; n++) {
+                                if (n < b) {
+                                    s.x += x[n].x * U[a][n].x + x[n].y * U[a][n].y;
+                                    s.y += x[n].y * U[a][n].x - x[n].x * U[a][n].y;
+                                }
+                            }
+                            sm[(size_t)(o * b + a) * PLEN + pos] = s;
+                        }
+                    }
+                } else {
+                    for (int q = 0; q < npl; q++) {
+                        const int pl = pl0 + q, o = pl / b, a = pl - o * b;
+                        float2 s = make_float2(0.f, 0.f);
+                        for (int n = 0; n < b; n++) {
+                            const float dr = (float)(om - eval[(size_t)n * nk + k]);
+                            const float den = dr * dr + et * et;
+                            const float2 f = make_float2(dr / den, -et / den);
+                            const float2 x = cmul(evec[(size_t)(o * b + n) * nk + k], f);
+                            const float2 ua = evec[(size_t)(a * b + n) * nk + k];
+                            s.x += x.x * ua.x + x.y * ua.y;
+                            s.y += x.y * ua.x - x.x * ua.y;
+                        }
+                        sm[(size_t)q * PLEN + pos] = s;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- pass A: (plane, n1) tasks, length-N2 transforms over n2, twiddle
+            for (int task = threadIdx.x; task < npl * N1; task += blockDim.x) {
+                const int q = task / N1, n1 = task - q * N1;
+                float2 *a = sm + (size_t)q * PLEN;
+                float2 x[N2];
+#pragma unroll
+                for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
+                fft_reg<N2>(x);
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[(n1 * k2) & (KP - 1)]);
+            }
+            __syncthreads();
+            // ---- pass B: (plane, k2) tasks, length-N1 transforms over n1, pruned stores
+            for (int task = threadIdx.x; task < npl * N2; task += blockDim.x) {
+                const int q = task / N2, k2 = task - q * N2;
+                const float2 *a = sm + (size_t)q * PLEN;
+                float2 x[N1];
+#pragma unroll
+                for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
+                fft_reg<N1>(x);
+                float2 *dst = half + (((size_t)e * bb + pl0 + q) * KP + i) * NB;
+#pragma unroll
+                for (int k1 = 0; k1 < N1; k1++) {
+                    // output Y in [0, kp) is R = Y mod kp; with NB <= kp exactly one box slot or none
+                    const int yb = (k2 + N2 * k1 + Rb) & (KP - 1);
+                    if (yb < NB) dst[yb] = x[k1];
+                }
+            }
+        }
+    }
+}
+
 // Pass 2: NC = 2^lnc adjacent columns (fixed plane, energy), transform along i.
 __global__ void __launch_bounds__(256) colfft_kernel(int kp, int logkp, int NB, int Rb, int bb, int lnc, float scale,
                                                      const float2 *__restrict__ half, const float2 *__restrict__ tw,
@@ -208,6 +378,9 @@ static int colfft_lnc(int kp)
     return lnc;
 }
 
+static bool rowfft_reg_ok(const cqpi_handle *h);
+static cudaError_t configure_rowfft_reg(cqpi_handle *h);
+
 bool fft32_supported(const cqpi_handle *h) { return h->kp >= 2 && (h->kp & (h->kp - 1)) == 0 && h->kp <= 8192; }
 
 cudaError_t configure_fft32(cqpi_handle *h)
@@ -222,7 +395,9 @@ cudaError_t configure_fft32(cqpi_handle *h)
     CQPI_SETSMEM(g0_rowfft_kernel<4>) CQPI_SETSMEM(g0_rowfft_kernel<6>) CQPI_SETSMEM(g0_rowfft_kernel<8>)
     CQPI_SETSMEM(g0_rowfft_kernel<10>) CQPI_SETSMEM(g0_rowfft_kernel<12>) CQPI_SETSMEM(g0_rowfft_kernel<16>)
 #undef CQPI_SETSMEM
-    return cudaFuncSetAttribute(colfft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+    e = cudaFuncSetAttribute(colfft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+    if (e != cudaSuccess) return e;
+    return rowfft_reg_ok(h) ? configure_rowfft_reg(h) : cudaSuccess;
 }
 
 template <int B>
@@ -233,12 +408,62 @@ static void launch_rowfft(cqpi_handle *h, int ne, const double *d_energies, int 
                                                          h->ws.half32);
 }
 
+// register four-step variant: kp = N1 x N2 in {64 ... 4096} and a box no wider than kp
+static bool rowfft_reg_ok(const cqpi_handle *h) { return h->kp >= 64 && h->kp <= 4096 && h->NB <= h->kp; }
+
+static int rowfft_reg_plane_group(const cqpi_handle *h)
+{
+    const size_t plen = (size_t)h->kp + (h->kp >> 5) + 1;
+    int pg = (int)((96 * 1024 - 8 * (size_t)h->kp) / (8 * plen));
+    return std::max(1, std::min(pg, h->b * h->b));
+}
+
+template <int N1, int N2>
+static void launch_rowfft_reg_t(cqpi_handle *h, int ne, const double *d_energies)
+{
+    const int pg = rowfft_reg_plane_group(h);
+    const size_t smem = 8 * ((size_t)pg * (N1 * N2 + (N1 * N2) / 32 + 1) + N1 * N2);
+    g0_rowfft_reg_kernel<N1, N2><<<h->kp, 256, smem, h->stream>>>(h->b, h->NB, h->Rb, pg, h->eta, d_energies, ne,
+                                                                  h->d_eval, h->d_evec32, h->d_tw32, h->ws.half32);
+}
+
+static cudaError_t configure_rowfft_reg(cqpi_handle *h)
+{
+    const int pg = rowfft_reg_plane_group(h);
+    const int smem = (int)(8 * ((size_t)pg * (h->kp + h->kp / 32 + 1) + h->kp));
+    switch (h->kp) {
+    case 64: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 128: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 256: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 512: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 1024: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 2048: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 4096: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    }
+    return cudaSuccess;
+}
+
+static void launch_rowfft_reg(cqpi_handle *h, int ne, const double *d_energies)
+{
+    switch (h->kp) {
+    case 64: launch_rowfft_reg_t<8, 8>(h, ne, d_energies); break;
+    case 128: launch_rowfft_reg_t<8, 16>(h, ne, d_energies); break;
+    case 256: launch_rowfft_reg_t<16, 16>(h, ne, d_energies); break;
+    case 512: launch_rowfft_reg_t<16, 32>(h, ne, d_energies); break;
+    case 1024: launch_rowfft_reg_t<32, 32>(h, ne, d_energies); break;
+    case 2048: launch_rowfft_reg_t<32, 64>(h, ne, d_energies); break;
+    case 4096: launch_rowfft_reg_t<64, 64>(h, ne, d_energies); break;
+    }
+}
+
 void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies)
 {
     const int pg = rowfft_plane_group(h);
     const size_t s1 = 8 * ((size_t)pg * (h->kp + (h->kp >> 5) + 1) + h->kp / 2);
     const int b = h->b;
-    if (b <= 1) launch_rowfft<1>(h, ne, d_energies, pg, s1);
+    const char *force = getenv("CQPI_ROWFFT");
+    if (rowfft_reg_ok(h) && !(force && !strcmp(force, "radix2"))) launch_rowfft_reg(h, ne, d_energies);
+    else if (b <= 1) launch_rowfft<1>(h, ne, d_energies, pg, s1);
     else if (b <= 2) launch_rowfft<2>(h, ne, d_energies, pg, s1);
     else if (b <= 3) launch_rowfft<3>(h, ne, d_energies, pg, s1);
     else if (b <= 4) launch_rowfft<4>(h, ne, d_energies, pg, s1);

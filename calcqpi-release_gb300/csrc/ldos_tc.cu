@@ -30,6 +30,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "cplx.h"
 #include "cqpi_internal.h"
@@ -383,6 +385,293 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
     }
 }
 
+
+// ---------------------------------------------------------------------------------
+// Pipelined variant for one spin block (the non-spin case): tile t's MMAs run on the
+// tensor cores while all warps do the epilogue of tile t-1 and build the B operand of
+// tile t+1.  Two B buffers in shared memory, two accumulator sets in tensor memory,
+// one mbarrier per accumulator set; the G0 windows of tile t+1 are fetched with
+// cp.async (zero-fill outside the box) behind the epilogue.
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int B>
+__global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __grid_constant__ TcParams p)
+{
+    using namespace tc;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int bb = p.b * p.b, side = 2 * p.w + 1, n2 = p.n >> 1;
+    const int sbo = p.KP * 16;
+    const int kcs = p.KP >> 3;
+    const int wx = p.TS + 2 * p.w;
+    const int rowlen = side * bb;
+    const int wfl = wx * rowlen * 2;
+    unsigned char *smA = sm;                                    // hi, lo
+    unsigned char *smB = smA + 2 * (size_t)p.a_bytes;           // 2 buffers x (uH, uL, sH, sL)
+    float *winU = reinterpret_cast<float *>(smB + 8 * (size_t)p.b_bytes);
+    float *winS = winU + wfl + 4;
+    int *tblU = reinterpret_cast<int *>(winS + wfl + 4);
+    int *tblS = tblU + p.KP;
+    int *rowU = tblS + p.KP;
+    int *rowS = rowU + p.N;
+    float *stage = reinterpret_cast<float *>(rowS + p.N);
+    const int wt = p.TS * p.os, sst = p.sst;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(stage + ((p.os * sst + 3) & ~3));   // [2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
+
+    {
+        const uint4 *src = p.Aimg;
+        uint4 *dst = reinterpret_cast<uint4 *>(smA);
+        const int nv = 2 * p.a_bytes / 16;
+        for (int i = tid; i < nv; i += TC_THREADS) dst[i] = src[i];
+    }
+    for (int k = tid; k < p.KP; k += TC_THREADS) {
+        if (k < p.W * p.mb) {
+            const int d = k / p.mb, o = p.bs0 + k % p.mb;
+            const int dxw = d / side, dyw = d % side;
+            tblU[k] = 2 * ((dxw * side + dyw) * bb + o * p.b);
+            tblS[k] = 2 * (((2 * p.w - dxw) * side + (2 * p.w - dyw)) * bb + o);
+        } else {
+            tblU[k] = -(1 << 30);   // resolved below: points at the window's zero slot
+            tblS[k] = -(1 << 30);
+        }
+    }
+    for (int nrow = tid; nrow < p.N; nrow += TC_THREADS) {
+        const int ari = nrow / p.TS, sl = nrow % p.TS, a = ari >> 1, ri = ari & 1;
+        rowU[nrow] = 2 * sl * rowlen + 2 * a + ri;
+        rowS[nrow] = 2 * (p.TS - 1 - sl) * rowlen + 2 * a * p.b + ri;
+    }
+    if (tid < 4) { winU[wfl + tid] = 0.f; winS[wfl + tid] = 0.f; }
+    if (tid == 0) {
+        mbar_init(smem_u32(&mbar[0]), 1);
+        mbar_init(smem_u32(&mbar[1]), 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = idesc_f16(128, p.N);
+    const int ntiles = p.ne * p.n * p.ntx;
+    const int lq = tid & 127;
+    const int qx = lq % p.os, qy = lq / p.os;
+    const bool qvalid = lq < p.Q;
+    const int sgrp = tid >> 7;
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    const uint64_t aH = sdesc(smem_u32(smA), 128, sbo), aL = sdesc(smem_u32(smA + p.a_bytes), 128, sbo);
+
+    // tile t -> (energy e, site row j, first site i0), computed once per tile by thread 0
+    // of each warp would still divide; the decomposition is cheap enough done uniformly.
+    const int per_e = p.n * p.ntx;
+    auto tile_of = [&](int it, int &e, int &j, int &i0) {
+        const int t = blockIdx.x + it * gridDim.x;
+        if (t >= ntiles) return false;
+        e = t / per_e;
+        const int rr = t - e * per_e;
+        j = rr / p.ntx;
+        i0 = (rr - j * p.ntx) * p.TS;
+        return true;
+    };
+    // cp.async the two G0 windows of a tile (unscaled; zero outside the box)
+    auto fetch_windows = [&](int e, int j, int i0) {
+        const float2 *boxe = p.box + (size_t)e * p.NB * p.NB * bb;
+        const int py = j - n2, px0 = i0 - n2;
+        for (int seg = warp; seg < 2 * wx; seg += TC_THREADS / 32) {
+            const int which = seg >= wx, xl = which ? seg - wx : seg;
+            const int X = which == 0 ? px0 - p.w + xl : -px0 - (p.TS - 1) - p.w + xl;
+            const int Y0 = which == 0 ? py - p.w : -py - p.w;
+            const bool in = X >= -p.Rb && X <= p.Rb;
+            const float2 *src = in ? boxe + ((size_t)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb : boxe;
+            float *w = (which == 0 ? winU : winS) + 2 * xl * rowlen;
+            for (int c = lane; c < rowlen; c += 32) cp_async8(smem_u32(w + 2 * c), in ? src + c : src, in ? 8u : 0u);
+        }
+        cp_async_commit();
+    };
+    // B operands of one tile from the windows into buffer bufi (scaled by sB, split hi/lo)
+    auto build_b = [&](int bufi, float sB) {
+        unsigned char *Bb = smB + (size_t)bufi * 4 * p.b_bytes;
+        const int nitems = 2 * p.N * kcs;
+        const float invN = 1.0f / (float)p.N;
+        for (int it = tid; it < nitems; it += TC_THREADS) {
+            int g = __float2int_rz(((float)it + 0.5f) * invN);
+            int nrow = it - g * p.N;
+            if (nrow < 0) { g--; nrow += p.N; }
+            if (nrow >= p.N) { g++; nrow -= p.N; }
+            const int op = g >= kcs, kc = op ? g - kcs : g;
+            const float *w = op ? winS : winU;
+            const int4 *tb4 = reinterpret_cast<const int4 *>((op ? tblS : tblU) + kc * 8);
+            const int base = op ? rowS[nrow] : rowU[nrow];
+            const int4 ta = tb4[0], tb = tb4[1];
+            const int offs[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+            float v[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; kk++) {
+                // padded k (negative table entry) reads the zero slot at float offset wfl
+                const int o = offs[kk] < 0 ? wfl : base + offs[kk];
+                v[kk] = w[o] * sB;
+            }
+            uint32_t hw[4], lw[4];
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                const __half2 h = __floats2half2_rn(v[2 * kk], v[2 * kk + 1]);
+                const float2 hb = __half22float2(h);
+                const __half2 l = __floats2half2_rn(v[2 * kk] - hb.x, v[2 * kk + 1] - hb.y);
+                hw[kk] = *reinterpret_cast<const uint32_t *>(&h);
+                lw[kk] = *reinterpret_cast<const uint32_t *>(&l);
+            }
+            const uint32_t off = core_off(nrow, kc, sbo);
+            *reinterpret_cast<uint4 *>(Bb + (size_t)(op * 2 + 0) * p.b_bytes + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4 *>(Bb + (size_t)(op * 2 + 1) * p.b_bytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+    };
+    auto epilogue = [&](int accs, int e, int j, int i0, float sB) {
+        const float inv = p.inv_sA / sB, inv2 = inv * inv;
+        const uint32_t acc = tmem + (uint32_t)(accs * 2 * p.N);
+        for (int imp = 0; imp < p.nimp; imp++) {
+            const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
+            const float t1 = qvalid ? (float)p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.f;
+            for (int s0 = sgrp * 4; s0 < p.TS; s0 += 16) {
+                float ur[2 * B][4], sr[2 * B][4];
+#pragma unroll
+                for (int ari = 0; ari < 2 * B; ari++) {
+                    if (ari < 2 * p.b) {
+                        const uint32_t cu = (uint32_t)(ari * p.TS + s0);
+                        tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
+                        tmem_ld4(acc + lane_base + cu + (uint32_t)p.N, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                    }
+                }
+                tmem_wait_ld();
+                float term2[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int a = 0; a < B; a++) {
+                    if (a >= p.b) continue;
+                    float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int c = 0; c < B; c++) {
+                        if (c >= p.b) continue;
+                        const float2 tv = __ldg(Te + a * p.b + c);
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            tsr[u] += tv.x * sr[2 * c][u] - tv.y * sr[2 * c + 1][u];
+                            tsi[u] += tv.x * sr[2 * c + 1][u] + tv.y * sr[2 * c][u];
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
+                }
+                if (qvalid)
+#pragma unroll
+                    for (int u = 0; u < 4; u++) stage[qy * sst + (s0 + u) * p.os + qx] = -t1 - term2[u] * inv2;
+            }
+            __syncthreads();
+            const int xbase = i0 * p.os;
+            const int xend = min(wt, p.wn - xbase);
+            const size_t rowbase = ((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os;
+            for (int yy = warp; yy < p.os; yy += TC_THREADS / 32) {
+                float *dst = p.out + (rowbase + yy) * p.wn + xbase;
+                for (int xx = lane; xx < xend; xx += 32) dst[xx] = stage[yy * sst + xx];
+            }
+            __syncthreads();
+        }
+    };
+
+    bool ok = true;
+    int e0, j0, i00;
+    int issued = 0, waited = 0;
+    float sB_cur = 1.f, sB_prev = 1.f;
+    if (tile_of(0, e0, j0, i00)) {
+        fetch_windows(e0, j0, i00);
+        sB_cur = pow2_scale(p.gmax[e0]);
+        cp_async_wait_all();
+        __syncthreads();
+        build_b(0, sB_cur);
+        fence_proxy_async();
+        __syncthreads();
+    }
+    int pe = 0, pj = 0, pi0 = 0;   // tile it-1
+    for (int it = 0; ok; it++) {
+        int e, j, i0;
+        if (!tile_of(it, e, j, i0)) break;
+        const int s = it & 1;
+        if (tid == 0) {
+            tc_fence_after();
+            unsigned char *Bb = smB + (size_t)s * 4 * p.b_bytes;
+            const int nks = p.KP >> 4;
+            for (int op = 0; op < 2; op++) {
+                const uint32_t d = tmem + (uint32_t)(s * 2 * p.N + op * p.N);
+                const uint64_t bH = sdesc(smem_u32(Bb + (size_t)(op * 2 + 0) * p.b_bytes), 128, sbo);
+                const uint64_t bL = sdesc(smem_u32(Bb + (size_t)(op * 2 + 1) * p.b_bytes), 128, sbo);
+                for (int ks = 0; ks < nks; ks++) {
+                    const uint64_t o = (uint64_t)(16 * ks);
+                    mma_f16(d, aH + o, bH + o, idesc, ks > 0 ? 1u : 0u);
+                    mma_f16(d, aH + o, bL + o, idesc, 1u);
+                    mma_f16(d, aL + o, bH + o, idesc, 1u);
+                }
+            }
+            mma_commit(smem_u32(&mbar[s]));
+        }
+        issued++;
+        int ne_, nj, ni0;
+        const bool has_next = tile_of(it + 1, ne_, nj, ni0);
+        if (has_next) fetch_windows(ne_, nj, ni0);       // lands behind the epilogue
+        if (it >= 1) {
+            const int ps = (it - 1) & 1;
+            const bool done = mbar_wait(smem_u32(&mbar[ps]), ((it - 1) >> 1) & 1, p.spin_limit);
+            if (__syncthreads_or(!done)) {
+                ok = false;
+                if (tid == 0) atomicOr(p.status, 2);
+                break;
+            }
+            waited++;
+            tc_fence_after();
+            epilogue(ps, pe, pj, pi0, sB_prev);
+        }
+        float sB_next = sB_cur;
+        if (has_next) {
+            sB_next = (ne_ == e) ? sB_cur : pow2_scale(p.gmax[ne_]);
+            cp_async_wait_all();
+            __syncthreads();
+            build_b((it + 1) & 1, sB_next);
+            fence_proxy_async();
+        }
+        pe = e; pj = j; pi0 = i0;
+        sB_prev = sB_cur;
+        sB_cur = sB_next;
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (ok && issued > waited) {
+        const int last = issued - 1, ps = last & 1;
+        const bool done = mbar_wait(smem_u32(&mbar[ps]), (last >> 1) & 1, p.spin_limit);
+        if (__syncthreads_or(!done)) {
+            ok = false;
+            if (tid == 0) atomicOr(p.status, 2);
+        } else {
+            waited++;
+            tc_fence_after();
+            epilogue(ps, pe, pj, pi0, sB_prev);
+        }
+    }
+    if (!ok) {
+        // bounded waits for every commit not yet observed, then free tensor memory
+        for (int k = waited; k < issued; k++) mbar_wait(smem_u32(&mbar[k & 1]), (k >> 1) & 1, p.spin_limit);
+    }
+    cp_async_wait_all();
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, p.tmem_cols);
+    }
+}
+
 __global__ void widen_kernel(const float *__restrict__ src, double *__restrict__ dst, size_t n)
 {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -424,6 +713,13 @@ void tc_plan(cqpi_handle *h)
     pl.smem = (size_t)h->nblk * 2 * pl.a_bytes + 4 * (size_t)pl.b_bytes + 4 * (2 * (wfl + 4)) +
               4 * (size_t)(2 * h->nblk * pl.KP + 2 * pl.N) + 4 * (size_t)((h->os * pl.sst + 3) & ~3) + 64;
     pl.ok = TS > 0 && cols <= 512 && pl.smem <= 227 * 1024;
+    // pipelined variant (one spin block): two B buffers, two accumulator sets
+    int pcols = 32;
+    while (pcols < 4 * pl.N) pcols <<= 1;
+    pl.pipe_tmem_cols = pcols;
+    pl.pipe_smem = 2 * (size_t)pl.a_bytes + 8 * (size_t)pl.b_bytes + 4 * (2 * (wfl + 4)) +
+                   4 * (size_t)(2 * pl.KP + 2 * pl.N) + 4 * (size_t)((h->os * pl.sst + 3) & ~3) + 64;
+    pl.pipe = pl.ok && h->nblk == 1 && 4 * pl.N <= 512 && pl.pipe_smem <= 227 * 1024;
 }
 
 // Phi hi/lo images in the operand layout: rows m = qy*os + qx, columns k = d*mb + ol.
@@ -472,13 +768,25 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
     p.out = out;
     p.status = h->d_status;
-    cudaError_t err = cudaFuncSetAttribute(ldos_tc_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
+    const char *force = getenv("CQPI_TC_PIPE");
+    const bool pipe = pl.pipe && !(force && !strcmp(force, "0"));
+    const long long ntiles = (long long)ne * h->n * p.ntx;
+    cudaError_t err;
+    if (pipe) {
+        p.tmem_cols = pl.pipe_tmem_cols;
+        err = cudaFuncSetAttribute(ldos_tc_pipe_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.pipe_smem);
+        if (err != cudaSuccess) return err;
+        const int grid = (int)std::min<long long>(ntiles, (long long)h->num_sms);   // one CTA per SM (512 TMEM columns)
+        ldos_tc_pipe_kernel<B><<<grid, TC_THREADS, pl.pipe_smem, h->stream>>>(p);
+        h->launches++;
+        return cudaGetLastError();
+    }
+    err = cudaFuncSetAttribute(ldos_tc_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
     if (err != cudaSuccess) return err;
     int per_sm = 0;
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ldos_tc_kernel<B>, TC_THREADS, pl.smem);
     if (err != cudaSuccess) return err;
     per_sm = std::max(1, std::min(per_sm, (int)(512 / pl.tmem_cols)));
-    const long long ntiles = (long long)ne * h->n * p.ntx;
     const int grid = (int)std::min<long long>(ntiles, (long long)h->num_sms * per_sm);
     ldos_tc_kernel<B><<<grid, TC_THREADS, pl.smem, h->stream>>>(p);
     h->launches++;

@@ -106,8 +106,9 @@ int cqpi_solve_bands(cqpi_handle *h);
  * calcrealspacegreensfunction + calcwannierldos + ldos2idl
  * (src/calcqpi.cc:690-756).  maps32 / maps64: [nE][nimp][wn][wn] (either may be
  * NULL), wn = lattice*oversamp.  on_device != 0: the pointers are device memory
- * and the call returns after enqueueing (cqpi_synchronize to wait); otherwise
- * they are host memory and the call returns when they are filled. */
+ * and the call returns after enqueueing (cqpi_synchronize waits and reports a
+ * singular T-matrix); otherwise they are host memory and the call returns when they
+ * are filled. */
 int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, double *maps64, int32_t on_device);
 
 /* ---- narrow seam (GPUQPI, include/gpuqpi.h:18-32) ------------------------
@@ -133,9 +134,10 @@ int cqpi_get_stream(cqpi_handle *h, void **stream);   /* cudaStream_t of the han
 int cqpi_synchronize(cqpi_handle *h);
 /* Kernels this handle has launched since creation (all of them are the engine's own). */
 int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count);
-/* Device time (ms) of the stages of the last cqpi_run, measured with CUDA events on
- * the handle's stream: [0] bands, [1] G0(k)+FFT, [2] T-matrix, [3] contraction, [4] total. */
-int cqpi_stage_times(const cqpi_handle *h, float *ms5);
+/* Device time (ms) per stage, summed over every cqpi_solve_bands / cqpi_run since the
+ * previous query (waits for them), measured with CUDA events on the handle's stream:
+ * [0] bands, [1] G0(k)+FFT, [2] T-matrix + term1, [3] contraction, [4] total. */
+int cqpi_stage_times(cqpi_handle *h, float *ms5);
 
 /* ---- entry point that allocates nothing ------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory:

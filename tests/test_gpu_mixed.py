@@ -117,3 +117,35 @@ def test_fused_greens_fft_matches_unfused(built_lib, name, monkeypatch):
     fused, unfused = box(None), box("unfused")
     for a, b in zip(fused, unfused):
         assert np.abs(a - b).max() <= 2e-6 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("kp,lattice", [(64, 16), (256, 24), (1024, 20), (128, 160)])
+def test_register_row_fft_matches_radix2(built_lib, kp, lattice, monkeypatch):
+    """Four-step register row transform vs the radix-2 shared-memory transform (the last
+    case has a box wider than the k-grid and takes the radix-2 path in both runs)."""
+    import cqpi
+    from cqpi import workloads as W
+    m = W.t2g_c2()
+    wf = W.t2g_orbitals_c2(2, 3)
+
+    def box(force):
+        if force:
+            monkeypatch.setenv("CQPI_ROWFFT", "radix2")
+        else:
+            monkeypatch.delenv("CQPI_ROWFFT", raising=False)
+        eng = cqpi.Engine(m, lattice, kp, 3, 2, 0.01, precision=cqpi.PREC_MIXED)
+        eng.set_orbitals(wf)
+        return eng.greens_box(0.037)[0]
+
+    a, b = box(False), box(True)
+    assert np.abs(a - b).max() <= 2e-6 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "c2_zero"])
+def test_pipelined_contraction_matches_serial(built_lib, name, monkeypatch):
+    """Software-pipelined tcgen05 kernel (double-buffered B and accumulators) vs the serial one."""
+    import cqpi
+    pipe, _ = _run(name, cqpi.PREC_MIXED)
+    monkeypatch.setenv("CQPI_TC_PIPE", "0")
+    serial, _ = _run(name, cqpi.PREC_MIXED)
+    assert np.abs(pipe - serial).max() <= 1e-7 * np.abs(serial).max()
