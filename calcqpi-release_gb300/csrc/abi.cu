@@ -432,6 +432,7 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_phi);
     dfree(h->d_phi32);
     dfree(h->d_tc_a);
+    dfree(h->d_tc_aw);
     dfree(h->d_seam_box);
     dfree(h->d_seam_T);
     dfree(h->d_seam_term1);
@@ -488,6 +489,12 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
             dfree(h->d_tc_a);
             dalloc(&h->d_tc_a, img.size());
             CK(cudaMemcpy(h->d_tc_a, img.data(), sizeof(uint16_t) * img.size(), cudaMemcpyHostToDevice));
+            if (h->tc.win) {
+                tc_build_a_window(h, phi, img);
+                dfree(h->d_tc_aw);
+                dalloc(&h->d_tc_aw, img.size());
+                CK(cudaMemcpy(h->d_tc_aw, img.data(), sizeof(uint16_t) * img.size(), cudaMemcpyHostToDevice));
+            }
         }
     } catch (const CudaError &e) {
         return cuda_fail(h, e);

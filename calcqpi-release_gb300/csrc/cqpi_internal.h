@@ -42,12 +42,21 @@ struct TcPlan {
     bool pipe = false;   // pipelined variant usable (one spin block)
     int pipe_tmem_cols = 0;
     size_t pipe_smem = 0;
+    // direct-window variant (one spin block): the staged fp16 G0 windows are the B operand
+    bool win = false;
+    int wH = 0;          // 8-site groups per tile (sites per tile = 8*wH)
+    int wNX = 0;         // window width in sites (8*wH + 2*window)
+    int wNKC = 0;        // 8-element K chunks per window row (even)
+    int wKP = 0;         // A columns: (2*window+1) * wNKC * 8
+    int w_a_bytes = 0, w_win_bytes = 0, w_sst = 0, w_tmem_cols = 0;
+    size_t w_smem = 0;
 };
 
 struct TcParams {
     int b, n, os, w, Rb, NB, W, nblk, mb, bs0, bs1;
     int TS, N, KP, Q, nimp, ne, wn, ntx, sst;
     int tmem_cols, a_bytes, b_bytes;
+    int H, NX, NKC, win_bytes;   // direct-window variant
     float inv_sA;
     long long spin_limit;
     const float2 *box;
@@ -108,6 +117,7 @@ struct cqpi_handle {
     bool use_tc = false;
     cqpi::TcPlan tc;
     uint16_t *d_tc_a = nullptr;   // Phi hi/lo operand images
+    uint16_t *d_tc_aw = nullptr;  // Phi hi/lo images in the direct-window K order
     float tc_inv_sA = 1.0f;
     int num_sms = 0;
     // impurities
@@ -162,6 +172,7 @@ void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies);
 bool tc_supported(const cqpi_handle *h);
 void tc_plan(cqpi_handle *h);
 void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img, float &inv_sA);
+void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img);
 cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out);
 void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n);
 

@@ -672,6 +672,355 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __gri
     }
 }
 
+// Direct-window variant (one spin block).  The B operands are not gathered per tile:
+// the two G0 windows of a tile (u: X = px0-w .. px0+TS-1+w, Y = py-w .. py+w; s: the
+// point-reflected window, stored in reflected order) are split into fp16 hi/lo once and
+// laid out as [kchunk][band,re/im][x][8 halfs], where a window row (x, band, re/im)
+// holds the (2w+1) x orbitals values of one X in K order r = dy*orbitals + o (zero
+// padded to 8*NKC).  For a k-step at x-offset dx the B operand of 8 consecutive sites is
+// then 8 consecutive 16-byte rows -- a core matrix -- and each MMA only moves its start
+// address: LBO = one kchunk plane, SBO = one (band, re/im) plane.  N = 8 sites x 2*bands
+// per MMA, one MMA chain per 8-site group.  The A operand (Phi) uses the matching K order
+// k = dx * 8*NKC + r.
+//
+// Warp roles: warps 0-15 stage windows and run the epilogue (TMEM lane quarter = warp % 4);
+// warp 16 issues the MMA chains.  They hand off through mbarriers, so MMA issue never
+// stalls the epilogue:
+//   win_full[b]  : window buffer b staged (arrive: one worker after a worker barrier)
+//   acc_full[s]  : tcgen05.commit of the tile in accumulator set s
+//   acc_empty[s] : workers finished reading accumulator set s
+// Tile t uses window buffer and accumulator set t & 1.  Every wait is bounded; a time-out
+// sets bit 1 of *status and all roles leave their loops (worker decisions are made
+// uniform with a barrier reduction), then in-flight MMAs are awaited (bounded) and the
+// tensor memory is freed.
+constexpr int TCW_WORKERS = 512;
+constexpr int TCW_THREADS = TCW_WORKERS + 32;
+
+namespace tc {
+__device__ __forceinline__ void bar_sync_workers() { asm volatile("bar.sync 1, %0;" ::"n"(TCW_WORKERS) : "memory"); }
+__device__ __forceinline__ bool bar_or_workers(bool pred)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred pin, pout;\n\t"
+        "setp.ne.u32 pin, %1, 0;\n\t"
+        "bar.red.or.pred pout, 1, %2, pin;\n\t"
+        "selp.u32 %0, 1, 0, pout;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "n"(TCW_WORKERS)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+}  // namespace tc
+
+template <int B>
+__global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_constant__ TcParams p)
+{
+    using namespace tc;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int bb = p.b * p.b, side = 2 * p.w + 1, n2 = p.n >> 1;
+    const int twob = 2 * p.b;
+    const int NX = p.NX, NKC = p.NKC, TS = p.TS;
+    const int rowlen = side * bb;                 // complex values per raw window column (one X)
+    const int rawfl = NX * rowlen * 2;            // floats per raw window
+    const int nval = side * p.mb;                 // K entries per window row that carry data
+    const int sbo_a = p.KP * 16;
+    const int colsop = 16 * p.b * p.H;            // accumulator columns per operand
+    unsigned char *smA = sm;                                        // A hi, A lo
+    unsigned char *smW = smA + 2 * (size_t)p.a_bytes;               // [buffer][op][hi,lo] windows
+    float *rawU = reinterpret_cast<float *>(smW + 8 * (size_t)p.win_bytes);
+    float *rawS = rawU + rawfl + 4;                                 // +4: a zero slot after each raw window
+    int *offR = reinterpret_cast<int *>(rawS + rawfl + 4);          // [op][8*NKC] offsets within a raw column
+    float *stage = reinterpret_cast<float *>(offR + 2 * NKC * 8);
+    const int wt = TS * p.os, sst = p.sst;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(stage + ((p.os * sst + 3) & ~3));   // [6]
+    uint64_t *win_full = mbar, *acc_full = mbar + 2, *acc_empty = mbar + 4;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 6);
+
+    if (tid < TCW_WORKERS) {
+        const uint4 *src = p.Aimg;
+        uint4 *dst = reinterpret_cast<uint4 *>(smA);
+        const int nv = 2 * p.a_bytes / 16;
+        for (int i = tid; i < nv; i += TCW_WORKERS) dst[i] = src[i];
+        // K entry r = dy*orbitals + o of a window row -> float offset inside a raw column
+        // (u: element [o][a] at Y-offset dy; s: element [a][o] at the reflected Y-offset)
+        for (int i = tid; i < 2 * NKC * 8; i += TCW_WORKERS) {
+            const int op = i >= NKC * 8, r = i - op * NKC * 8;
+            int v = -1;
+            if (r < nval) {
+                const int dyw = r / p.mb, o = p.bs0 + r % p.mb;
+                v = op == 0 ? 2 * (dyw * bb + o * p.b) : 2 * ((2 * p.w - dyw) * bb + o);
+            }
+            offR[i] = v;
+        }
+        if (tid < 4) { rawU[rawfl + tid] = 0.f; rawS[rawfl + tid] = 0.f; }
+    }
+    if (tid == TCW_WORKERS) {
+        for (int i = 0; i < 6; i++) mbar_init(smem_u32(&mbar[i]), 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int ntiles = p.ne * p.n * p.ntx;
+    auto tile_of = [&](int it, int &e, int &j, int &i0) {
+        const int t = blockIdx.x + it * gridDim.x;
+        if (t >= ntiles) return false;
+        const int per_e = p.n * p.ntx;
+        e = t / per_e;
+        const int rr = t - e * per_e;
+        j = rr / p.ntx;
+        i0 = (rr - j * p.ntx) * TS;
+        return true;
+    };
+
+    if (warp == TCW_WORKERS / 32) {
+        // ---------------------------------------------------------------- MMA warp
+        const uint32_t idesc = idesc_f16(128, 16 * p.b);
+        const uint64_t aH = sdesc(smem_u32(smA), 128, sbo_a), aL = sdesc(smem_u32(smA + p.a_bytes), 128, sbo_a);
+        const uint32_t lbo_b = (uint32_t)(twob * NX * 16), sbo_b = (uint32_t)(NX * 16);
+        int issued = 0;
+        bool ok = true;
+        for (int it = 0;; it++) {
+            int e, j, i0;
+            if (!tile_of(it, e, j, i0)) break;
+            const int s = it & 1;
+            if (!mbar_wait(smem_u32(&win_full[s]), (it >> 1) & 1, p.spin_limit) ||
+                (it >= 2 && !mbar_wait(smem_u32(&acc_empty[s]), ((it - 2) >> 1) & 1, p.spin_limit))) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            if (lane == 0) {
+                const unsigned char *Wb = smW + (size_t)s * 4 * p.win_bytes;
+                for (int op = 0; op < 2; op++) {
+                    const uint64_t bH = sdesc(smem_u32(Wb + (size_t)(op * 2 + 0) * p.win_bytes), lbo_b, sbo_b);
+                    const uint64_t bL = sdesc(smem_u32(Wb + (size_t)(op * 2 + 1) * p.win_bytes), lbo_b, sbo_b);
+                    for (int g = 0; g < p.H; g++) {
+                        const uint32_t d = tmem + (uint32_t)(s * 2 * colsop + op * colsop + g * 16 * p.b);
+                        uint32_t acc_flag = 0u;
+                        for (int dxw = 0; dxw < side; dxw++)
+                            for (int cp = 0; cp < (NKC >> 1); cp++) {
+                                // descriptor address fields count 16-byte units
+                                const uint64_t ao = (uint64_t)((dxw * NKC + 2 * cp) * 8);
+                                const uint64_t bo = (uint64_t)((2 * cp * twob) * NX + 8 * g + dxw);
+                                mma_f16(d, aH + ao, bH + bo, idesc, acc_flag);
+                                mma_f16(d, aH + ao, bL + bo, idesc, 1u);
+                                mma_f16(d, aL + ao, bH + bo, idesc, 1u);
+                                acc_flag = 1u;
+                            }
+                    }
+                }
+                mma_commit(smem_u32(&acc_full[s]));
+            }
+            __syncwarp();
+            issued++;
+        }
+        if (!ok && lane == 0) atomicOr(p.status, 2);
+        // the accumulator sets must be idle before the tensor memory is freed
+        for (int k = issued > 2 ? issued - 2 : 0; k < issued; k++)
+            mbar_wait(smem_u32(&acc_full[k & 1]), (k >> 1) & 1, p.spin_limit);
+    } else {
+        // ---------------------------------------------------------------- workers
+        const int lq = tid & 127;
+        const int qx = lq % p.os, qy = lq / p.os;
+        const bool qvalid = lq < p.Q;
+        const int sgrp = tid >> 7;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        // staging items: one (op, kchunk, band/re-im, x) row of 8 halfs each; this thread's
+        // first item is the same in every tile, so it is decomposed once
+        const int per_op = NKC * twob * NX, nitems = 2 * per_op;
+        auto item_of = [&](int it, int &rbase, int &toff, int &dst) {
+            const int op = it >= per_op;
+            int rem = it - op * per_op;
+            const int kc = rem / (twob * NX);
+            rem -= kc * twob * NX;
+            const int ari = rem / NX, xl = rem - ari * NX;
+            const int a = ari >> 1, ri = ari & 1;
+            rbase = op ? (rawfl + 4) + 2 * (NX - 1 - xl) * rowlen + 2 * a * p.b + ri : 2 * xl * rowlen + 2 * a + ri;
+            toff = op * NKC * 8 + kc * 8;
+            dst = op * 2 * p.win_bytes + ((kc * twob + ari) * NX + xl) * 16;
+        };
+        int it0_rbase = 0, it0_toff = 0, it0_dst = 0;
+        if (tid < nitems) item_of(tid, it0_rbase, it0_toff, it0_dst);
+
+        // cp.async the two raw FP32 windows of a tile (zero outside the box)
+        auto fetch_raw = [&](int e, int j, int i0) {
+            const float2 *boxe = p.box + (size_t)e * p.NB * p.NB * bb;
+            const int py = j - n2, px0 = i0 - n2;
+            for (int seg = warp; seg < 2 * NX; seg += TCW_WORKERS / 32) {
+                const int which = seg >= NX, xl = which ? seg - NX : seg;
+                const int X = which == 0 ? px0 - p.w + xl : -px0 - (TS - 1) - p.w + xl;
+                const int Y0 = which == 0 ? py - p.w : -py - p.w;
+                const bool in = X >= -p.Rb && X <= p.Rb;
+                const float2 *src = in ? boxe + ((size_t)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb : boxe;
+                float *w = (which == 0 ? rawU : rawS) + 2 * xl * rowlen;
+                for (int c = lane; c < rowlen; c += 32) cp_async8(smem_u32(w + 2 * c), in ? src + c : src, in ? 8u : 0u);
+            }
+            cp_async_commit();
+        };
+        // raw windows -> scaled, split fp16 windows in buffer bi
+        auto convert_item = [&](unsigned char *Wb, int rbase, int toff, int dst, float sB) {
+            const int4 *t4 = reinterpret_cast<const int4 *>(offR + toff);
+            const int4 ta = t4[0], tb = t4[1];
+            const int offs[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+            float v[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; kk++) v[kk] = rawU[offs[kk] < 0 ? rawfl : rbase + offs[kk]] * sB;
+            uint32_t hw[4], lw[4];
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                const __half2 hh = __floats2half2_rn(v[2 * kk], v[2 * kk + 1]);
+                const float2 hb = __half22float2(hh);
+                const __half2 ll = __floats2half2_rn(v[2 * kk] - hb.x, v[2 * kk + 1] - hb.y);
+                hw[kk] = *reinterpret_cast<const uint32_t *>(&hh);
+                lw[kk] = *reinterpret_cast<const uint32_t *>(&ll);
+            }
+            *reinterpret_cast<uint4 *>(Wb + dst) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4 *>(Wb + dst + p.win_bytes) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        };
+        // stage window buffer bi for the MMA warp
+        auto stage_windows = [&](int bi, float sB) {
+            cp_async_wait_all();
+            bar_sync_workers();
+            unsigned char *Wb = smW + (size_t)bi * 4 * p.win_bytes;
+            if (tid < nitems) convert_item(Wb, it0_rbase, it0_toff, it0_dst, sB);
+            for (int it = tid + TCW_WORKERS; it < nitems; it += TCW_WORKERS) {
+                int rb_, to_, ds_;
+                item_of(it, rb_, to_, ds_);
+                convert_item(Wb, rb_, to_, ds_, sB);
+            }
+            fence_proxy_async();
+            bar_sync_workers();
+            if (tid == 0) mbar_arrive(smem_u32(&win_full[bi]));
+        };
+        auto epilogue = [&](int accs, int e, int j, int i0, float sB) {
+            const float inv = p.inv_sA / sB, inv2 = inv * inv;
+            const uint32_t acc = tmem + (uint32_t)(accs * 2 * colsop);
+            for (int imp = 0; imp < p.nimp; imp++) {
+                const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
+                const float t1 = qvalid ? (float)p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.f;
+                for (int s0 = sgrp * 4; s0 < TS; s0 += 16) {
+                    const uint32_t cb = (uint32_t)((s0 >> 3) * 16 * p.b + (s0 & 7));
+                    float ur[2 * B][4], sr[2 * B][4];
+#pragma unroll
+                    for (int ari = 0; ari < 2 * B; ari++) {
+                        if (ari < 2 * p.b) {
+                            const uint32_t cu = cb + (uint32_t)(ari * 8);
+                            tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
+                            tmem_ld4(acc + lane_base + cu + (uint32_t)colsop, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                        }
+                    }
+                    tmem_wait_ld();
+                    float term2[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int a = 0; a < B; a++) {
+                        if (a >= p.b) continue;
+                        float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                        for (int c = 0; c < B; c++) {
+                            if (c >= p.b) continue;
+                            const float2 tv = __ldg(Te + a * p.b + c);
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                tsr[u] += tv.x * sr[2 * c][u] - tv.y * sr[2 * c + 1][u];
+                                tsi[u] += tv.x * sr[2 * c + 1][u] + tv.y * sr[2 * c][u];
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
+                    }
+                    if (qvalid)
+#pragma unroll
+                        for (int u = 0; u < 4; u++) stage[qy * sst + (s0 + u) * p.os + qx] = -t1 - term2[u] * inv2;
+                }
+                if (imp == p.nimp - 1) {
+                    // last read of this accumulator set: hand it back to the MMA warp
+                    tc_fence_before();
+                    bar_sync_workers();
+                    if (tid == 0) mbar_arrive(smem_u32(&acc_empty[accs]));
+                } else {
+                    bar_sync_workers();
+                }
+                const int xbase = i0 * p.os;
+                const int xend = min(wt, p.wn - xbase);
+                const size_t rowbase = ((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os;
+                for (int yy = warp; yy < p.os; yy += TCW_WORKERS / 32) {
+                    float *dstp = p.out + (rowbase + yy) * p.wn + xbase;
+                    for (int xx = lane; xx < xend; xx += 32) dstp[xx] = stage[yy * sst + xx];
+                }
+                bar_sync_workers();
+            }
+        };
+
+        bool ok = true;
+        int e0, j0, i00;
+        float sB_cur = 1.f, sB_prev = 1.f;
+        if (tile_of(0, e0, j0, i00)) {
+            fetch_raw(e0, j0, i00);
+            sB_cur = pow2_scale(p.gmax[e0]);
+            stage_windows(0, sB_cur);
+        }
+        int pe = 0, pj = 0, pi0 = 0;   // tile it-1
+        int done_tiles = 0;
+        for (int it = 0; ok; it++) {
+            int e, j, i0;
+            if (!tile_of(it, e, j, i0)) break;
+            int ne_, nj, ni0;
+            const bool has_next = tile_of(it + 1, ne_, nj, ni0);
+            if (has_next) fetch_raw(ne_, nj, ni0);       // lands behind the epilogue
+            if (it >= 1) {
+                const int ps = (it - 1) & 1;
+                const bool done = mbar_wait(smem_u32(&acc_full[ps]), ((it - 1) >> 1) & 1, p.spin_limit);
+                if (bar_or_workers(!done)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                epilogue(ps, pe, pj, pi0, sB_prev);
+                done_tiles++;
+            }
+            float sB_next = sB_cur;
+            if (has_next) {
+                sB_next = (ne_ == e) ? sB_cur : pow2_scale(p.gmax[ne_]);
+                stage_windows((it + 1) & 1, sB_next);
+            }
+            pe = e; pj = j; pi0 = i0;
+            sB_prev = sB_cur;
+            sB_cur = sB_next;
+        }
+        if (ok) {
+            int e, j, i0;
+            const int last = done_tiles;   // the one tile whose epilogue is still due
+            if (tile_of(last, e, j, i0)) {
+                const bool done = mbar_wait(smem_u32(&acc_full[last & 1]), (last >> 1) & 1, p.spin_limit);
+                if (bar_or_workers(!done)) {
+                    ok = false;
+                } else {
+                    tc_fence_after();
+                    epilogue(last & 1, pe, pj, pi0, sB_prev);
+                }
+            }
+        }
+        if (!ok && tid == 0) atomicOr(p.status, 2);
+        cp_async_wait_all();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, p.tmem_cols);
+    }
+}
+
 __global__ void widen_kernel(const float *__restrict__ src, double *__restrict__ dst, size_t n)
 {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -720,6 +1069,61 @@ void tc_plan(cqpi_handle *h)
     pl.pipe_smem = 2 * (size_t)pl.a_bytes + 8 * (size_t)pl.b_bytes + 4 * (2 * (wfl + 4)) +
                    4 * (size_t)(2 * pl.KP + 2 * pl.N) + 4 * (size_t)((h->os * pl.sst + 3) & ~3) + 64;
     pl.pipe = pl.ok && h->nblk == 1 && 4 * pl.N <= 512 && pl.pipe_smem <= 227 * 1024;
+
+    // direct-window variant: 8*H sites per tile, two operands x two accumulator sets of
+    // 16*b*H columns each must fit the 512 TMEM columns
+    {
+        const int side = 2 * h->w + 1;
+        int H = std::min(4, 8 / std::max(1, h->b));
+        pl.wH = H;
+        pl.wNKC = 2 * ((side * h->mb + 15) / 16);
+        pl.wKP = side * pl.wNKC * 8;
+        pl.wNX = 8 * H + 2 * h->w;
+        pl.w_a_bytes = 128 * pl.wKP * 2;
+        pl.w_win_bytes = pl.wNKC * twob * pl.wNX * 16;
+        const int colsop = 16 * h->b * H;
+        int wc = 32;
+        while (wc < 4 * colsop) wc <<= 1;
+        pl.w_tmem_cols = wc;
+        const int wwt = 8 * H * h->os;
+        pl.w_sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
+        const size_t rawfl = (size_t)pl.wNX * side * h->b * h->b * 2;
+        pl.w_smem = 2 * (size_t)pl.w_a_bytes + 8 * (size_t)pl.w_win_bytes + 4 * (2 * (rawfl + 4)) +
+                    4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)((h->os * pl.w_sst + 3) & ~3) + 6 * 8 + 16;
+        pl.win = h->nblk == 1 && H >= 1 && h->Q <= 128 && 16 * h->b <= 256 && 4 * colsop <= 512 &&
+                 pl.w_smem <= 227 * 1024;
+    }
+}
+
+// Phi hi/lo images for the direct-window variant: rows m = qy*os + qx, columns
+// k = dx * 8*NKC + dy*orbitals + o (zero elsewhere); same power-of-two scale as tc_build_a.
+void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img)
+{
+    const TcPlan &pl = h->tc;
+    double mx = 0.0;
+    for (double v : phi) mx = std::max(mx, std::fabs(v));
+    int ex = 0;
+    if (mx > 0) std::frexp(mx, &ex);
+    const double sA = mx > 0 ? std::ldexp(1.0, 14 - ex) : 1.0;
+    const size_t per = pl.w_a_bytes / 2;
+    img.assign(2 * per, 0);
+    const int sbo = pl.wKP * 16, side = 2 * h->w + 1;
+    for (int qy = 0; qy < h->os; qy++)
+        for (int qx = 0; qx < h->os; qx++) {
+            const int m = qy * h->os + qx;
+            for (int d = 0; d < h->W; d++) {
+                const int dxw = d / side, dyw = d % side;
+                for (int ol = 0; ol < h->mb; ol++) {
+                    const double v = sA * phi[(((size_t)qx * h->os + qy) * h->W + d) * h->mb + ol];
+                    const __half hi = __float2half_rn((float)v);
+                    const __half lo = __float2half_rn((float)(v - (double)__half2float(hi)));
+                    const int k = dxw * pl.wNKC * 8 + dyw * h->mb + ol;
+                    const size_t off = ((size_t)(m >> 3) * sbo + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2) / 2;
+                    img[off] = __half_as_ushort(hi);
+                    img[per + off] = __half_as_ushort(lo);
+                }
+            }
+        }
 }
 
 // Phi hi/lo images in the operand layout: rows m = qy*os + qx, columns k = d*mb + ol.
@@ -756,7 +1160,7 @@ template <int B>
 static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
 {
     const TcPlan &pl = h->tc;
-    TcParams p;
+    TcParams p = {};
     p.b = h->b; p.n = h->n; p.os = h->os; p.w = h->w; p.Rb = h->Rb; p.NB = h->NB; p.W = h->W;
     p.nblk = h->nblk; p.mb = h->mb; p.bs0 = h->blk_start[0]; p.bs1 = h->blk_start[1];
     p.TS = pl.TS; p.N = pl.N; p.KP = pl.KP; p.sst = pl.sst; p.Q = h->Q; p.nimp = h->nimp; p.ne = ne; p.wn = h->wn;
@@ -770,8 +1174,24 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     p.status = h->d_status;
     const char *force = getenv("CQPI_TC_PIPE");
     const bool pipe = pl.pipe && !(force && !strcmp(force, "0"));
+    const char *fw = getenv("CQPI_TC_WINDOW");
+    const bool win = pl.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0"));
     const long long ntiles = (long long)ne * h->n * p.ntx;
     cudaError_t err;
+    if (win) {
+        p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes;
+        p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
+        p.ntx = (h->n + p.TS - 1) / p.TS;
+        p.tmem_cols = pl.w_tmem_cols;
+        p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_aw);
+        err = cudaFuncSetAttribute(ldos_tcw_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.w_smem);
+        if (err != cudaSuccess) return err;
+        const long long nt = (long long)ne * h->n * p.ntx;
+        const int grid = (int)std::min<long long>(nt, (long long)h->num_sms);
+        ldos_tcw_kernel<B><<<grid, TCW_THREADS, pl.w_smem, h->stream>>>(p);
+        h->launches++;
+        return cudaGetLastError();
+    }
     if (pipe) {
         p.tmem_cols = pl.pipe_tmem_cols;
         err = cudaFuncSetAttribute(ldos_tc_pipe_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.pipe_smem);

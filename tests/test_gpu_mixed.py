@@ -149,3 +149,36 @@ def test_pipelined_contraction_matches_serial(built_lib, name, monkeypatch):
     monkeypatch.setenv("CQPI_TC_PIPE", "0")
     serial, _ = _run(name, cqpi.PREC_MIXED)
     assert np.abs(pipe - serial).max() <= 1e-7 * np.abs(serial).max()
+
+
+@pytest.mark.parametrize("name", ["c1", "c1_odd", "c2", "c2_zero"])
+def test_window_contraction_matches_gathered(built_lib, name, monkeypatch):
+    """Direct-window tcgen05 kernel (fp16 windows addressed by the MMA descriptors) vs the
+    kernel that gathers the B operand per tile."""
+    import cqpi
+    win, _ = _run(name, cqpi.PREC_MIXED)
+    monkeypatch.setenv("CQPI_TC_WINDOW", "0")
+    gathered, _ = _run(name, cqpi.PREC_MIXED)
+    assert np.abs(win - gathered).max() <= 5e-7 * np.abs(gathered).max()
+
+
+@pytest.mark.parametrize("lattice,window,oversamp", [(40, 3, 5), (33, 2, 10), (24, 4, 3)])
+def test_window_contraction_tiles_and_k_steps(built_lib, lattice, window, oversamp, monkeypatch):
+    """Several tiles per site row with a ragged last tile, and windows whose K rows need
+    more than one 16-wide k-step, against the FP64 path."""
+    import cqpi
+    from cqpi import workloads as W
+    m = W.t2g_c2()
+    wf = W.t2g_orbitals_c2(window, oversamp)
+    E = np.array([-0.04, 0.013])
+    out = {}
+    for prec in (cqpi.PREC_FP64, cqpi.PREC_MIXED):
+        eng = cqpi.Engine(m, lattice, 64, oversamp, window, 0.01, precision=prec)
+        eng.set_orbitals(wf)
+        eng.set_scattering(np.array([0.3, 0.3, 0.3], complex))
+        out[prec] = eng.run(E, f32=False, f64=True)
+        eng.close()
+    ref = out[cqpi.PREC_FP64]
+    for e in range(len(E)):
+        err = np.abs(out[cqpi.PREC_MIXED][e, 0] - ref[e, 0]).max() / np.abs(ref[e, 0]).max()
+        assert err <= TOL, (lattice, window, oversamp, E[e], err)
