@@ -45,10 +45,12 @@ struct TcPlan {
     // direct-window variant (one spin block): the staged fp16 G0 windows are the B operand
     bool win = false;
     int wH = 0;          // 8-site groups per tile (sites per tile = 8*wH)
+    int wEB = 0;         // energies per tile
     int wNX = 0;         // window width in sites (8*wH + 2*window)
     int wNKC = 0;        // 8-element K chunks per window row (even)
     int wKP = 0;         // A columns: (2*window+1) * wNKC * 8
     int w_a_bytes = 0, w_win_bytes = 0, w_sst = 0, w_tmem_cols = 0;
+    bool w_a_tmem = false;   // Phi fits in the tensor-memory columns left by the accumulators
     size_t w_smem = 0;
 };
 
@@ -56,7 +58,8 @@ struct TcParams {
     int b, n, os, w, Rb, NB, W, nblk, mb, bs0, bs1;
     int TS, N, KP, Q, nimp, ne, wn, ntx, sst;
     int tmem_cols, a_bytes, b_bytes;
-    int H, NX, NKC, win_bytes;   // direct-window variant
+    int H, NX, NKC, win_bytes, EB;   // direct-window variant
+    int a_tmem;                  // direct-window variant: Phi operand held in tensor memory
     float inv_sA;
     long long spin_limit;
     const float2 *box;

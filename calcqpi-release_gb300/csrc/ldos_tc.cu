@@ -398,6 +398,7 @@ __device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, uint32_
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 template <int B>
 __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __grid_constant__ TcParams p)
@@ -673,41 +674,51 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __gri
 }
 
 // Direct-window variant (one spin block).  The B operands are not gathered per tile:
-// the two G0 windows of a tile (u: X = px0-w .. px0+TS-1+w, Y = py-w .. py+w; s: the
-// point-reflected window, stored in reflected order) are split into fp16 hi/lo once and
-// laid out as [kchunk][band,re/im][x][8 halfs], where a window row (x, band, re/im)
-// holds the (2w+1) x orbitals values of one X in K order r = dy*orbitals + o (zero
-// padded to 8*NKC).  For a k-step at x-offset dx the B operand of 8 consecutive sites is
-// then 8 consecutive 16-byte rows -- a core matrix -- and each MMA only moves its start
-// address: LBO = one kchunk plane, SBO = one (band, re/im) plane.  N = 8 sites x 2*bands
-// per MMA, one MMA chain per 8-site group.  The A operand (Phi) uses the matching K order
-// k = dx * 8*NKC + r.
+// the G0 windows of a tile -- for each of its EB energies the u window (X = px0-w ..
+// px0+TS-1+w, Y = py-w .. py+w) and the s window (the point reflection, stored in reflected
+// order) -- are split into fp16 hi/lo once and laid out as planes
+//   [kchunk][operand u/s][energy][band, re/im][x][8 halfs],
+// where a plane row (x) holds the (2w+1) x orbitals values of one X in K order
+// r = dy*orbitals + o (zero padded to 8*NKC).  For a k-step at x-offset dx the B operand of
+// 8 consecutive sites in every (operand, energy, band, re/im) plane is then 8 consecutive
+// 16-byte rows -- one core matrix per plane -- and an MMA only moves its start address:
+// SBO = one plane, LBO = one kchunk (all planes).  One MMA therefore covers both operands
+// and all EB energies: N = 8 sites x 2 x EB x 2*bands (192 for 3 bands, 2 energies); the
+// issue cost of tcgen05.mma barely depends on N, so wide MMAs are what makes this fast.
+// The A operand (Phi) uses the matching K order k = dx * 8*NKC + r, from shared memory or
+// (a_tmem) from tensor memory.
 //
-// Warp roles: warps 0-15 stage windows and run the epilogue (TMEM lane quarter = warp % 4);
-// warp 16 issues the MMA chains.  They hand off through mbarriers, so MMA issue never
-// stalls the epilogue:
-//   win_full[b]  : window buffer b staged (arrive: one worker after a worker barrier)
-//   acc_full[s]  : tcgen05.commit of the tile in accumulator set s
-//   acc_empty[s] : workers finished reading accumulator set s
-// Tile t uses window buffer and accumulator set t & 1.  Every wait is bounded; a time-out
-// sets bit 1 of *status and all roles leave their loops (worker decisions are made
-// uniform with a barrier reduction), then in-flight MMAs are awaited (bounded) and the
-// tensor memory is freed.
-constexpr int TCW_WORKERS = 512;
-constexpr int TCW_THREADS = TCW_WORKERS + 32;
+// Warp roles (17 warps), handing off through mbarriers only:
+//   warps 0-7    epilogue: TMEM -> rho (two warps per TMEM lane quarter, warp % 4)
+//   warps 8-15   producer: cp.async of the raw FP32 windows, fp16 split into a window buffer
+//   warp 16      MMA issue (one elected lane)
+//   win_full[b]  : window buffer b staged            (producer -> MMA)
+//   win_empty[b] : MMAs reading buffer b completed    (tcgen05.commit -> producer)
+//   acc_full[s]  : accumulator set s complete         (tcgen05.commit -> epilogue)
+//   acc_empty[s] : epilogue finished reading set s    (epilogue -> MMA)
+// Tile t uses window buffer and accumulator set t & 1, so staging of t+1, the MMAs of t and
+// the epilogue of t-1 run concurrently.  Every wait is bounded; a time-out sets bit 1 of
+// *status and every role leaves its loop (decisions inside a role are made uniform with a
+// barrier reduction), then in-flight MMAs are awaited (bounded) and the tensor memory is
+// freed.
+constexpr int TCW_EPI = 256;
+constexpr int TCW_PROD = 256;
+constexpr int TCW_THREADS = TCW_EPI + TCW_PROD + 32;
 
 namespace tc {
-__device__ __forceinline__ void bar_sync_workers() { asm volatile("bar.sync 1, %0;" ::"n"(TCW_WORKERS) : "memory"); }
-__device__ __forceinline__ bool bar_or_workers(bool pred)
+template <int ID, int COUNT>
+__device__ __forceinline__ void bar_sync_group() { asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(COUNT) : "memory"); }
+template <int ID, int COUNT>
+__device__ __forceinline__ bool bar_or_group(bool pred)
 {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred pin, pout;\n\t"
         "setp.ne.u32 pin, %1, 0;\n\t"
-        "bar.red.or.pred pout, 1, %2, pin;\n\t"
+        "bar.red.or.pred pout, %2, %3, pin;\n\t"
         "selp.u32 %0, 1, 0, pout;\n\t}"
         : "=r"(r)
-        : "r"((uint32_t)pred), "n"(TCW_WORKERS)
+        : "r"((uint32_t)pred), "n"(ID), "n"(COUNT)
         : "memory");
     return r != 0;
 }
@@ -715,6 +726,24 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
+// D (+)= A x B with A read from tensor memory (lane m = row m, 16-bit K pairs per column)
+__device__ __forceinline__ void mma_f16_ta(uint32_t dtmem, uint32_t atmem, uint64_t bd, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+        ::"r"(dtmem), "r"(atmem), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+// eight consecutive 32-bit columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                 ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 }  // namespace tc
 
 template <int B>
@@ -725,31 +754,43 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int bb = p.b * p.b, side = 2 * p.w + 1, n2 = p.n >> 1;
     const int twob = 2 * p.b;
-    const int NX = p.NX, NKC = p.NKC, TS = p.TS;
+    const int NX = p.NX, NKC = p.NKC, TS = p.TS, EB = p.EB;
     const int rowlen = side * bb;                 // complex values per raw window column (one X)
     const int rawfl = NX * rowlen * 2;            // floats per raw window
     const int nval = side * p.mb;                 // K entries per window row that carry data
     const int sbo_a = p.KP * 16;
-    const int colsop = 16 * p.b * p.H;            // accumulator columns per operand
-    unsigned char *smA = sm;                                        // A hi, A lo
-    unsigned char *smW = smA + 2 * (size_t)p.a_bytes;               // [buffer][op][hi,lo] windows
-    float *rawU = reinterpret_cast<float *>(smW + 8 * (size_t)p.win_bytes);
-    float *rawS = rawU + rawfl + 4;                                 // +4: a zero slot after each raw window
-    int *offR = reinterpret_cast<int *>(rawS + rawfl + 4);          // [op][8*NKC] offsets within a raw column
-    float *stage = reinterpret_cast<float *>(offR + 2 * NKC * 8);
-    const int wt = TS * p.os, sst = p.sst;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(stage + ((p.os * sst + 3) & ~3));   // [6]
-    uint64_t *win_full = mbar, *acc_full = mbar + 2, *acc_empty = mbar + 4;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 6);
+    const int NMMA = 8 * 2 * EB * twob;           // MMA N: 8 sites x (u, s) x EB energies x (band, re/im)
+    const int setcols = p.H * NMMA;               // accumulator columns per set
+    const int opcols = EB * twob * 8;             // column offset of the s operand inside a group
+    const int nplanes = 2 * EB * twob;            // planes per kchunk
+    unsigned char *smA = sm;                                                   // A hi, A lo (unless a_tmem)
+    unsigned char *smW = smA + (p.a_tmem ? 0 : 2 * (size_t)p.a_bytes);         // [buffer][hi,lo] windows
+    // raw windows: two buffers of [op][energy] windows, then a zero slot
+    float *raw = reinterpret_cast<float *>(smW + 4 * (size_t)p.win_bytes);
+    const int rawbuf = 2 * EB * rawfl;
+    const int zslot = 2 * rawbuf;
+    int *offR = reinterpret_cast<int *>(raw + zslot + 4);                      // [op][8*NKC] offsets in a raw column
+    // epilogue constants of the current energy block: T [energy][impurity][b*b],
+    // 1/(sA sB)^2 [energy], term1 [energy][q]
+    float2 *cT = reinterpret_cast<float2 *>(offR + 2 * NKC * 8);
+    float *cInv2 = reinterpret_cast<float *>(cT + EB * p.nimp * bb);
+    float *cT1 = cInv2 + EB;
+    const size_t mb_off = ((size_t)(reinterpret_cast<unsigned char *>(cT1 + EB * 128) - sm) + 15) & ~(size_t)15;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + mb_off);   // [8]
+    uint64_t *win_full = mbar, *win_empty = mbar + 2, *acc_full = mbar + 4, *acc_empty = mbar + 6;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 8);
+    constexpr int NW = TCW_EPI + TCW_PROD;
 
-    if (tid < TCW_WORKERS) {
-        const uint4 *src = p.Aimg;
-        uint4 *dst = reinterpret_cast<uint4 *>(smA);
-        const int nv = 2 * p.a_bytes / 16;
-        for (int i = tid; i < nv; i += TCW_WORKERS) dst[i] = src[i];
+    if (tid < NW) {
+        if (!p.a_tmem) {
+            const uint4 *src = p.Aimg;
+            uint4 *dst = reinterpret_cast<uint4 *>(smA);
+            const int nv = 2 * p.a_bytes / 16;
+            for (int i = tid; i < nv; i += NW) dst[i] = src[i];
+        }
         // K entry r = dy*orbitals + o of a window row -> float offset inside a raw column
         // (u: element [o][a] at Y-offset dy; s: element [a][o] at the reflected Y-offset)
-        for (int i = tid; i < 2 * NKC * 8; i += TCW_WORKERS) {
+        for (int i = tid; i < 2 * NKC * 8; i += NW) {
             const int op = i >= NKC * 8, r = i - op * NKC * 8;
             int v = -1;
             if (r < nval) {
@@ -758,10 +799,10 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             }
             offR[i] = v;
         }
-        if (tid < 4) { rawU[rawfl + tid] = 0.f; rawS[rawfl + tid] = 0.f; }
+        if (tid < 4) raw[zslot + tid] = 0.f;
     }
-    if (tid == TCW_WORKERS) {
-        for (int i = 0; i < 6; i++) mbar_init(smem_u32(&mbar[i]), 1);
+    if (tid == NW) {
+        for (int i = 0; i < 8; i++) mbar_init(smem_u32(&mbar[i]), 1);
         fence_mbar_init();
     }
     if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
@@ -770,28 +811,53 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int ntiles = p.ne * p.n * p.ntx;
-    auto tile_of = [&](int it, int &e, int &j, int &i0) {
+    // A operand in tensor memory: columns [acol, acol + KP/2) hold Phi hi and the next KP/2
+    // columns Phi lo; warps 0-3 write their lane quarter, row m = lane, from the image
+    const uint32_t acol = (uint32_t)(2 * setcols);
+    if (p.a_tmem && warp < 4) {
+        const int m = warp * 32 + lane;
+        const unsigned char *img = reinterpret_cast<const unsigned char *>(p.Aimg);
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int hl = 0; hl < 2; hl++)
+            for (int ks = 0; ks < (p.KP >> 4); ks++) {
+                uint32_t v[8];
+                for (int c = 0; c < 2; c++) {
+                    const uint4 q = *reinterpret_cast<const uint4 *>(img + (size_t)hl * p.a_bytes + (size_t)(m >> 3) * sbo_a +
+                                                                     (size_t)(2 * ks + c) * 128 + (m & 7) * 16);
+                    v[4 * c + 0] = q.x; v[4 * c + 1] = q.y; v[4 * c + 2] = q.z; v[4 * c + 3] = q.w;
+                }
+                tmem_st8(trow + acol + (uint32_t)(hl * (p.KP >> 1) + ks * 8), v);
+            }
+        tmem_wait_st();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const int neb = (p.ne + EB - 1) / EB;
+    const int ntiles = neb * p.n * p.ntx;
+    // tile t -> (first energy e0, site row j, first site i0)
+    auto tile_of = [&](int it, int &e0, int &j, int &i0) {
         const int t = blockIdx.x + it * gridDim.x;
         if (t >= ntiles) return false;
         const int per_e = p.n * p.ntx;
-        e = t / per_e;
-        const int rr = t - e * per_e;
+        const int eb = t / per_e;
+        const int rr = t - eb * per_e;
+        e0 = eb * EB;
         j = rr / p.ntx;
         i0 = (rr - j * p.ntx) * TS;
         return true;
     };
 
-    if (warp == TCW_WORKERS / 32) {
+    if (warp == NW / 32) {
         // ---------------------------------------------------------------- MMA warp
-        const uint32_t idesc = idesc_f16(128, 16 * p.b);
+        const uint32_t idesc = idesc_f16(128, NMMA);
         const uint64_t aH = sdesc(smem_u32(smA), 128, sbo_a), aL = sdesc(smem_u32(smA + p.a_bytes), 128, sbo_a);
-        const uint32_t lbo_b = (uint32_t)(twob * NX * 16), sbo_b = (uint32_t)(NX * 16);
+        const uint32_t lbo_b = (uint32_t)(nplanes * NX * 16), sbo_b = (uint32_t)(NX * 16);
         int issued = 0;
         bool ok = true;
         for (int it = 0;; it++) {
-            int e, j, i0;
-            if (!tile_of(it, e, j, i0)) break;
+            int e0, j, i0;
+            if (!tile_of(it, e0, j, i0)) break;
             const int s = it & 1;
             if (!mbar_wait(smem_u32(&win_full[s]), (it >> 1) & 1, p.spin_limit) ||
                 (it >= 2 && !mbar_wait(smem_u32(&acc_empty[s]), ((it - 2) >> 1) & 1, p.spin_limit))) {
@@ -800,26 +866,34 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             }
             tc_fence_after();
             if (lane == 0) {
-                const unsigned char *Wb = smW + (size_t)s * 4 * p.win_bytes;
-                for (int op = 0; op < 2; op++) {
-                    const uint64_t bH = sdesc(smem_u32(Wb + (size_t)(op * 2 + 0) * p.win_bytes), lbo_b, sbo_b);
-                    const uint64_t bL = sdesc(smem_u32(Wb + (size_t)(op * 2 + 1) * p.win_bytes), lbo_b, sbo_b);
-                    for (int g = 0; g < p.H; g++) {
-                        const uint32_t d = tmem + (uint32_t)(s * 2 * colsop + op * colsop + g * 16 * p.b);
-                        uint32_t acc_flag = 0u;
-                        for (int dxw = 0; dxw < side; dxw++)
-                            for (int cp = 0; cp < (NKC >> 1); cp++) {
-                                // descriptor address fields count 16-byte units
+                const unsigned char *Wb = smW + (size_t)s * 2 * p.win_bytes;
+                const uint64_t bH = sdesc(smem_u32(Wb), lbo_b, sbo_b);
+                const uint64_t bL = sdesc(smem_u32(Wb + p.win_bytes), lbo_b, sbo_b);
+                for (int g = 0; g < p.H; g++) {
+                    const uint32_t d = tmem + (uint32_t)(s * setcols + g * NMMA);
+                    uint32_t acc_flag = 0u;
+                    for (int dxw = 0; dxw < side; dxw++)
+                        for (int cp = 0; cp < (NKC >> 1); cp++) {
+                            // descriptor address fields count 16-byte units
+                            const uint64_t bo = (uint64_t)((2 * cp * nplanes) * NX + 8 * g + dxw);
+                            if (p.a_tmem) {
+                                // k-step (dxw, cp) = 16 K values = 8 columns of A
+                                const uint32_t ac = tmem + acol + (uint32_t)((dxw * NKC + 2 * cp) * 4);
+                                const uint32_t acl = ac + (uint32_t)(p.KP >> 1);
+                                mma_f16_ta(d, ac, bH + bo, idesc, acc_flag);
+                                mma_f16_ta(d, ac, bL + bo, idesc, 1u);
+                                mma_f16_ta(d, acl, bH + bo, idesc, 1u);
+                            } else {
                                 const uint64_t ao = (uint64_t)((dxw * NKC + 2 * cp) * 8);
-                                const uint64_t bo = (uint64_t)((2 * cp * twob) * NX + 8 * g + dxw);
                                 mma_f16(d, aH + ao, bH + bo, idesc, acc_flag);
                                 mma_f16(d, aH + ao, bL + bo, idesc, 1u);
                                 mma_f16(d, aL + ao, bH + bo, idesc, 1u);
-                                acc_flag = 1u;
                             }
-                    }
+                            acc_flag = 1u;
+                        }
                 }
                 mma_commit(smem_u32(&acc_full[s]));
+                mma_commit(smem_u32(&win_empty[s]));
             }
             __syncwarp();
             issued++;
@@ -828,53 +902,57 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         // the accumulator sets must be idle before the tensor memory is freed
         for (int k = issued > 2 ? issued - 2 : 0; k < issued; k++)
             mbar_wait(smem_u32(&acc_full[k & 1]), (k >> 1) & 1, p.spin_limit);
-    } else {
-        // ---------------------------------------------------------------- workers
-        const int lq = tid & 127;
-        const int qx = lq % p.os, qy = lq / p.os;
-        const bool qvalid = lq < p.Q;
-        const int sgrp = tid >> 7;
-        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        // staging items: one (op, kchunk, band/re-im, x) row of 8 halfs each; this thread's
-        // first item is the same in every tile, so it is decomposed once
-        const int per_op = NKC * twob * NX, nitems = 2 * per_op;
-        auto item_of = [&](int it, int &rbase, int &toff, int &dst) {
-            const int op = it >= per_op;
-            int rem = it - op * per_op;
-            const int kc = rem / (twob * NX);
-            rem -= kc * twob * NX;
-            const int ari = rem / NX, xl = rem - ari * NX;
+    } else if (warp >= TCW_EPI / 32) {
+        // ---------------------------------------------------------------- producer
+        const int ptid = tid - TCW_EPI, pwarp = warp - TCW_EPI / 32;
+        // staging items: one plane row (kchunk, operand, energy, band/re-im, x) of 8 halfs;
+        // the first two items of this thread are the same in every tile, so they are
+        // decomposed once
+        const int nitems = NKC * nplanes * NX;
+        auto item_of = [&](int it, int &rbase, int &toff, int &dst, int &eei) {
+            const int plane = it / NX, xl = it - plane * NX;
+            const int ari = plane % twob;
+            const int rest = plane / twob;
+            const int ee = rest % EB;
+            const int rest2 = rest / EB;
+            const int op = rest2 & 1, kc = rest2 >> 1;
             const int a = ari >> 1, ri = ari & 1;
-            rbase = op ? (rawfl + 4) + 2 * (NX - 1 - xl) * rowlen + 2 * a * p.b + ri : 2 * xl * rowlen + 2 * a + ri;
+            const int wbase = (op * EB + ee) * rawfl;
+            rbase = op ? wbase + 2 * (NX - 1 - xl) * rowlen + 2 * a * p.b + ri : wbase + 2 * xl * rowlen + 2 * a + ri;
             toff = op * NKC * 8 + kc * 8;
-            dst = op * 2 * p.win_bytes + ((kc * twob + ari) * NX + xl) * 16;
+            dst = (plane * NX + xl) * 16;
+            eei = ee;
         };
-        int it0_rbase = 0, it0_toff = 0, it0_dst = 0;
-        if (tid < nitems) item_of(tid, it0_rbase, it0_toff, it0_dst);
-
-        // cp.async the two raw FP32 windows of a tile (zero outside the box)
-        auto fetch_raw = [&](int e, int j, int i0) {
-            const float2 *boxe = p.box + (size_t)e * p.NB * p.NB * bb;
+        int r0 = 0, t0 = 0, d0 = 0, q0 = 0, r1 = 0, t1 = 0, d1 = 0, q1 = 0, r2 = 0, t2 = 0, d2 = 0, q2 = 0;
+        if (ptid < nitems) item_of(ptid, r0, t0, d0, q0);
+        if (ptid + TCW_PROD < nitems) item_of(ptid + TCW_PROD, r1, t1, d1, q1);
+        if (ptid + 2 * TCW_PROD < nitems) item_of(ptid + 2 * TCW_PROD, r2, t2, d2, q2);
+        auto scale_of = [&](int e) { return e < p.ne ? pow2_scale(p.gmax[e]) : 1.f; };
+        // cp.async the raw FP32 windows of a tile (zero outside the box and past the last energy)
+        auto fetch_raw = [&](int rb, int e0, int j, int i0) {
             const int py = j - n2, px0 = i0 - n2;
-            for (int seg = warp; seg < 2 * NX; seg += TCW_WORKERS / 32) {
-                const int which = seg >= NX, xl = which ? seg - NX : seg;
-                const int X = which == 0 ? px0 - p.w + xl : -px0 - (TS - 1) - p.w + xl;
-                const int Y0 = which == 0 ? py - p.w : -py - p.w;
-                const bool in = X >= -p.Rb && X <= p.Rb;
-                const float2 *src = in ? boxe + ((size_t)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb : boxe;
-                float *w = (which == 0 ? rawU : rawS) + 2 * xl * rowlen;
+            for (int seg = pwarp; seg < 2 * EB * NX; seg += TCW_PROD / 32) {
+                const int w_ = seg / NX, xl = seg - w_ * NX;
+                const int op = w_ / EB, ee = w_ - op * EB;
+                const int e = e0 + ee;
+                const int X = op == 0 ? px0 - p.w + xl : -px0 - (TS - 1) - p.w + xl;
+                const int Y0 = op == 0 ? py - p.w : -py - p.w;
+                const bool in = e < p.ne && X >= -p.Rb && X <= p.Rb;
+                const float2 *src = in ? p.box + ((size_t)e * p.NB * p.NB + (size_t)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb
+                                       : p.box;
+                float *w = raw + rb * rawbuf + w_ * rawfl + 2 * xl * rowlen;
                 for (int c = lane; c < rowlen; c += 32) cp_async8(smem_u32(w + 2 * c), in ? src + c : src, in ? 8u : 0u);
             }
             cp_async_commit();
         };
-        // raw windows -> scaled, split fp16 windows in buffer bi
-        auto convert_item = [&](unsigned char *Wb, int rbase, int toff, int dst, float sB) {
+        // raw windows -> scaled, split fp16 rows in window buffer Wb (hi) and Wb + win_bytes (lo)
+        auto convert_item = [&](unsigned char *Wb, int rb, int rbase, int toff, int dst, float sB) {
             const int4 *t4 = reinterpret_cast<const int4 *>(offR + toff);
             const int4 ta = t4[0], tb = t4[1];
             const int offs[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
             float v[8];
 #pragma unroll
-            for (int kk = 0; kk < 8; kk++) v[kk] = rawU[offs[kk] < 0 ? rawfl : rbase + offs[kk]] * sB;
+            for (int kk = 0; kk < 8; kk++) v[kk] = raw[offs[kk] < 0 ? zslot : rb * rawbuf + rbase + offs[kk]] * sB;
             uint32_t hw[4], lw[4];
 #pragma unroll
             for (int kk = 0; kk < 4; kk++) {
@@ -887,48 +965,104 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             *reinterpret_cast<uint4 *>(Wb + dst) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
             *reinterpret_cast<uint4 *>(Wb + dst + p.win_bytes) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         };
-        // stage window buffer bi for the MMA warp
-        auto stage_windows = [&](int bi, float sB) {
-            cp_async_wait_all();
-            bar_sync_workers();
-            unsigned char *Wb = smW + (size_t)bi * 4 * p.win_bytes;
-            if (tid < nitems) convert_item(Wb, it0_rbase, it0_toff, it0_dst, sB);
-            for (int it = tid + TCW_WORKERS; it < nitems; it += TCW_WORKERS) {
-                int rb_, to_, ds_;
-                item_of(it, rb_, to_, ds_);
-                convert_item(Wb, rb_, to_, ds_, sB);
+        bool ok = true;
+        int e0, j, i0;
+        int se = -1;
+        float sB0 = 1.f, sB1 = 1.f, sB2 = 1.f;
+        if (tile_of(0, e0, j, i0)) fetch_raw(0, e0, j, i0);
+        for (int it = 0; ok; it++) {
+            if (!tile_of(it, e0, j, i0)) break;
+            const int s = it & 1;
+            // the next tile's raw windows go to the other raw buffer, whose last reader (the
+            // previous iteration's convert) finished before that iteration's final barrier
+            int ne_, nj, ni0;
+            const bool has_next = tile_of(it + 1, ne_, nj, ni0);
+            if (has_next) fetch_raw((it + 1) & 1, ne_, nj, ni0);
+            const bool good = it < 2 || mbar_wait(smem_u32(&win_empty[s]), ((it - 2) >> 1) & 1, p.spin_limit);
+            if (bar_or_group<2, TCW_PROD>(!good)) {
+                ok = false;
+                break;
+            }
+            if (e0 != se) {
+                sB0 = scale_of(e0 + q0);
+                sB1 = scale_of(e0 + q1);
+                sB2 = scale_of(e0 + q2);
+                se = e0;
+            }
+            if (has_next) cp_async_wait_1(); else cp_async_wait_all();   // this tile's windows landed
+            bar_sync_group<2, TCW_PROD>();
+            unsigned char *Wb = smW + (size_t)s * 2 * p.win_bytes;
+            const int rb = it & 1;
+            if (ptid < nitems) convert_item(Wb, rb, r0, t0, d0, sB0);
+            if (ptid + TCW_PROD < nitems) convert_item(Wb, rb, r1, t1, d1, sB1);
+            if (ptid + 2 * TCW_PROD < nitems) convert_item(Wb, rb, r2, t2, d2, sB2);
+            for (int k = ptid + 3 * TCW_PROD; k < nitems; k += TCW_PROD) {
+                int rb_, to_, ds_, q_;
+                item_of(k, rb_, to_, ds_, q_);
+                convert_item(Wb, rb, rb_, to_, ds_, scale_of(e0 + q_));
             }
             fence_proxy_async();
-            bar_sync_workers();
-            if (tid == 0) mbar_arrive(smem_u32(&win_full[bi]));
+            bar_sync_group<2, TCW_PROD>();           // buffer staged, raw buffer rb free
+            if (ptid == 0) mbar_arrive(smem_u32(&win_full[s]));
+        }
+        if (!ok && ptid == 0) atomicOr(p.status, 2);
+        cp_async_wait_all();
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int lq = tid & 127;
+        const int qx = lq % p.os, qy = lq / p.os;
+        const bool qvalid = lq < p.Q;
+        const int sub = warp >> 2;                                // 0, 1: the two warps of a lane quarter
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        const int nb = B <= 4 ? B : p.b;                          // bands; a constant for B <= 4
+        const int ncombo = EB * (TS >> 2);                        // (energy, 4-site group) pairs per tile
+        // T, the scale and term1 of an energy block, loaded once per block
+        auto load_block = [&](int e0) {
+            for (int i = tid; i < EB * p.nimp * bb; i += TCW_EPI) {
+                const int e = e0 + i / (p.nimp * bb);
+                cT[i] = e < p.ne ? p.T32[(size_t)e0 * p.nimp * bb + i] : make_float2(0.f, 0.f);
+            }
+            for (int i = tid; i < EB * 128; i += TCW_EPI) {
+                const int ee = i >> 7, q = i & 127, e = e0 + ee;
+                cT1[i] = (e < p.ne && q < p.Q) ? (float)p.term1[(size_t)e * p.Q + (q % p.os) * p.os + q / p.os] : 0.f;
+            }
+            if (tid < EB) {
+                const int e = e0 + tid;
+                const float inv = e < p.ne ? p.inv_sA / pow2_scale(p.gmax[e]) : 0.f;
+                cInv2[tid] = inv * inv;
+            }
+            bar_sync_group<1, TCW_EPI>();
         };
-        auto epilogue = [&](int accs, int e, int j, int i0, float sB) {
-            const float inv = p.inv_sA / sB, inv2 = inv * inv;
-            const uint32_t acc = tmem + (uint32_t)(accs * 2 * colsop);
+        auto epilogue = [&](int accs, int e0, int j, int i0) {
+            const uint32_t acc = tmem + (uint32_t)(accs * setcols);
             for (int imp = 0; imp < p.nimp; imp++) {
-                const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
-                const float t1 = qvalid ? (float)p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.f;
-                for (int s0 = sgrp * 4; s0 < TS; s0 += 16) {
-                    const uint32_t cb = (uint32_t)((s0 >> 3) * 16 * p.b + (s0 & 7));
+                for (int cmb = sub; cmb < ncombo; cmb += 2) {
+                    const int ee = cmb / (TS >> 2), s0 = (cmb - ee * (TS >> 2)) * 4;
+                    const int e = e0 + ee;
+                    if (e >= p.ne) continue;
+                    const float inv2 = cInv2[ee];
+                    const float2 *Te = cT + (ee * p.nimp + imp) * bb;
+                    const float t1 = cT1[ee * 128 + lq];
+                    const uint32_t cb = (uint32_t)((s0 >> 3) * NMMA + ee * twob * 8 + (s0 & 7));
                     float ur[2 * B][4], sr[2 * B][4];
 #pragma unroll
                     for (int ari = 0; ari < 2 * B; ari++) {
-                        if (ari < 2 * p.b) {
+                        if (ari < 2 * nb) {
                             const uint32_t cu = cb + (uint32_t)(ari * 8);
                             tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
-                            tmem_ld4(acc + lane_base + cu + (uint32_t)colsop, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                            tmem_ld4(acc + lane_base + cu + (uint32_t)opcols, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
                         }
                     }
                     tmem_wait_ld();
                     float term2[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                     for (int a = 0; a < B; a++) {
-                        if (a >= p.b) continue;
+                        if (a >= nb) continue;
                         float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                         for (int c = 0; c < B; c++) {
-                            if (c >= p.b) continue;
-                            const float2 tv = __ldg(Te + a * p.b + c);
+                            if (c >= nb) continue;
+                            const float2 tv = Te[a * nb + c];
 #pragma unroll
                             for (int u = 0; u < 4; u++) {
                                 tsr[u] += tv.x * sr[2 * c][u] - tv.y * sr[2 * c + 1][u];
@@ -938,80 +1072,41 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
 #pragma unroll
                         for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
                     }
-                    if (qvalid)
+                    // pixel (qx, qy) of sites i0+s0 .. i0+s0+3 of row j, straight to the map
+                    if (qvalid) {
+                        float *dst = p.out + ((((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os + qy) * p.wn +
+                                              (size_t)(i0 + s0) * p.os + qx);
+                        const int xrem = p.wn - (i0 + s0) * p.os - qx;   // columns left in this map row
 #pragma unroll
-                        for (int u = 0; u < 4; u++) stage[qy * sst + (s0 + u) * p.os + qx] = -t1 - term2[u] * inv2;
+                        for (int u = 0; u < 4; u++)
+                            if (u * p.os < xrem) dst[u * p.os] = -t1 - term2[u] * inv2;
+                    }
                 }
-                if (imp == p.nimp - 1) {
-                    // last read of this accumulator set: hand it back to the MMA warp
-                    tc_fence_before();
-                    bar_sync_workers();
-                    if (tid == 0) mbar_arrive(smem_u32(&acc_empty[accs]));
-                } else {
-                    bar_sync_workers();
-                }
-                const int xbase = i0 * p.os;
-                const int xend = min(wt, p.wn - xbase);
-                const size_t rowbase = ((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os;
-                for (int yy = warp; yy < p.os; yy += TCW_WORKERS / 32) {
-                    float *dstp = p.out + (rowbase + yy) * p.wn + xbase;
-                    for (int xx = lane; xx < xend; xx += 32) dstp[xx] = stage[yy * sst + xx];
-                }
-                bar_sync_workers();
             }
+            // every TMEM read of this accumulator set is done: hand it back to the MMA warp
+            tc_fence_before();
+            bar_sync_group<1, TCW_EPI>();
+            if (tid == 0) mbar_arrive(smem_u32(&acc_empty[accs]));
         };
-
         bool ok = true;
-        int e0, j0, i00;
-        float sB_cur = 1.f, sB_prev = 1.f;
-        if (tile_of(0, e0, j0, i00)) {
-            fetch_raw(e0, j0, i00);
-            sB_cur = pow2_scale(p.gmax[e0]);
-            stage_windows(0, sB_cur);
-        }
-        int pe = 0, pj = 0, pi0 = 0;   // tile it-1
-        int done_tiles = 0;
+        int cur_e0 = -1;
         for (int it = 0; ok; it++) {
-            int e, j, i0;
-            if (!tile_of(it, e, j, i0)) break;
-            int ne_, nj, ni0;
-            const bool has_next = tile_of(it + 1, ne_, nj, ni0);
-            if (has_next) fetch_raw(ne_, nj, ni0);       // lands behind the epilogue
-            if (it >= 1) {
-                const int ps = (it - 1) & 1;
-                const bool done = mbar_wait(smem_u32(&acc_full[ps]), ((it - 1) >> 1) & 1, p.spin_limit);
-                if (bar_or_workers(!done)) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                epilogue(ps, pe, pj, pi0, sB_prev);
-                done_tiles++;
+            int e0, j, i0;
+            if (!tile_of(it, e0, j, i0)) break;
+            if (e0 != cur_e0) {
+                load_block(e0);
+                cur_e0 = e0;
             }
-            float sB_next = sB_cur;
-            if (has_next) {
-                sB_next = (ne_ == e) ? sB_cur : pow2_scale(p.gmax[ne_]);
-                stage_windows((it + 1) & 1, sB_next);
+            const int s = it & 1;
+            const bool done = mbar_wait(smem_u32(&acc_full[s]), (it >> 1) & 1, p.spin_limit);
+            if (bar_or_group<1, TCW_EPI>(!done)) {
+                ok = false;
+                break;
             }
-            pe = e; pj = j; pi0 = i0;
-            sB_prev = sB_cur;
-            sB_cur = sB_next;
-        }
-        if (ok) {
-            int e, j, i0;
-            const int last = done_tiles;   // the one tile whose epilogue is still due
-            if (tile_of(last, e, j, i0)) {
-                const bool done = mbar_wait(smem_u32(&acc_full[last & 1]), (last >> 1) & 1, p.spin_limit);
-                if (bar_or_workers(!done)) {
-                    ok = false;
-                } else {
-                    tc_fence_after();
-                    epilogue(last & 1, pe, pj, pi0, sB_prev);
-                }
-            }
+            tc_fence_after();
+            epilogue(s, e0, j, i0);
         }
         if (!ok && tid == 0) atomicOr(p.status, 2);
-        cp_async_wait_all();
     }
     tc_fence_before();
     __syncthreads();
@@ -1070,28 +1165,42 @@ void tc_plan(cqpi_handle *h)
                    4 * (size_t)(2 * pl.KP + 2 * pl.N) + 4 * (size_t)((h->os * pl.sst + 3) & ~3) + 64;
     pl.pipe = pl.ok && h->nblk == 1 && 4 * pl.N <= 512 && pl.pipe_smem <= 227 * 1024;
 
-    // direct-window variant: 8*H sites per tile, two operands x two accumulator sets of
-    // 16*b*H columns each must fit the 512 TMEM columns
+    // direct-window variant: tiles of 8*H sites x EB energies; one MMA covers both operands
+    // and all EB energies of an 8-site group (N = 32*b*EB <= 256).  Two accumulator sets of
+    // H*N columns (+ Phi hi/lo when held in tensor memory) must fit the 512 TMEM columns.
+    // The MMA count per site-energy falls with EB only, so EB is maximised first, then H.
     {
         const int side = 2 * h->w + 1;
-        int H = std::min(4, 8 / std::max(1, h->b));
-        pl.wH = H;
         pl.wNKC = 2 * ((side * h->mb + 15) / 16);
         pl.wKP = side * pl.wNKC * 8;
-        pl.wNX = 8 * H + 2 * h->w;
         pl.w_a_bytes = 128 * pl.wKP * 2;
-        pl.w_win_bytes = pl.wNKC * twob * pl.wNX * 16;
-        const int colsop = 16 * h->b * H;
-        int wc = 32;
-        while (wc < 4 * colsop) wc <<= 1;
-        pl.w_tmem_cols = wc;
-        const int wwt = 8 * H * h->os;
-        pl.w_sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
-        const size_t rawfl = (size_t)pl.wNX * side * h->b * h->b * 2;
-        pl.w_smem = 2 * (size_t)pl.w_a_bytes + 8 * (size_t)pl.w_win_bytes + 4 * (2 * (rawfl + 4)) +
-                    4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)((h->os * pl.w_sst + 3) & ~3) + 6 * 8 + 16;
-        pl.win = h->nblk == 1 && H >= 1 && h->Q <= 128 && 16 * h->b <= 256 && 4 * colsop <= 512 &&
-                 pl.w_smem <= 227 * 1024;
+        const size_t bbz = (size_t)h->b * h->b;
+        pl.win = false;
+        for (int EB = 4; EB >= 1 && !pl.win; EB--) {
+            const int N = 32 * h->b * EB;
+            if (N > 256) continue;
+            for (int H = 2; H >= 1 && !pl.win; H--) {
+                const int setcols = H * N;
+                if (2 * setcols > 512) continue;
+                const int NX = 8 * H + 2 * h->w;
+                const bool a_tmem = 2 * setcols + pl.wKP <= 512;
+                const int need = 2 * setcols + (a_tmem ? pl.wKP : 0);
+                int wc = 32;
+                while (wc < need) wc <<= 1;
+                const int win_bytes = pl.wNKC * 2 * EB * twob * NX * 16;
+                const int wwt = 8 * H * h->os;
+                const int sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
+                const size_t rawfl = (size_t)NX * side * bbz * 2;
+                // shared memory with Phi in shared memory (the larger of the two layouts)
+                // (the per-impurity epilogue constants are added at launch)
+                const size_t smem = 2 * (size_t)pl.w_a_bytes + 4 * (size_t)win_bytes + 4 * (4 * EB * rawfl + 4) +
+                                    4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * 8 + 16;
+                if (smem > 227 * 1024) continue;
+                pl.wEB = EB; pl.wH = H; pl.wNX = NX; pl.w_win_bytes = win_bytes; pl.w_sst = sst;
+                pl.w_a_tmem = a_tmem; pl.w_tmem_cols = wc; pl.w_smem = smem;
+                pl.win = h->nblk == 1 && h->Q <= 128;
+            }
+        }
     }
 }
 
@@ -1175,20 +1284,25 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     const char *force = getenv("CQPI_TC_PIPE");
     const bool pipe = pl.pipe && !(force && !strcmp(force, "0"));
     const char *fw = getenv("CQPI_TC_WINDOW");
-    const bool win = pl.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0"));
+    // the epilogue keeps T of every impurity of an energy block in shared memory
+    const bool win_fits = pl.w_smem + 8 * (size_t)pl.wEB * h->nimp * h->b * h->b <= 227 * 1024;
+    const bool win = pl.win && win_fits && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0"));
     const long long ntiles = (long long)ne * h->n * p.ntx;
     cudaError_t err;
     if (win) {
-        p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes;
+        p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB;
         p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
         p.ntx = (h->n + p.TS - 1) / p.TS;
         p.tmem_cols = pl.w_tmem_cols;
+        const char *fa = getenv("CQPI_TC_ATMEM");
+        p.a_tmem = pl.w_a_tmem && fa && !strcmp(fa, "1") ? 1 : 0;   // Phi in tensor memory: opt-in
         p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_aw);
-        err = cudaFuncSetAttribute(ldos_tcw_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.w_smem);
+        const size_t smem = pl.w_smem + 8 * (size_t)p.EB * h->nimp * h->b * h->b;
+        err = cudaFuncSetAttribute(ldos_tcw_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return err;
-        const long long nt = (long long)ne * h->n * p.ntx;
+        const long long nt = (long long)((ne + p.EB - 1) / p.EB) * h->n * p.ntx;
         const int grid = (int)std::min<long long>(nt, (long long)h->num_sms);
-        ldos_tcw_kernel<B><<<grid, TCW_THREADS, pl.w_smem, h->stream>>>(p);
+        ldos_tcw_kernel<B><<<grid, TCW_THREADS, smem, h->stream>>>(p);
         h->launches++;
         return cudaGetLastError();
     }

@@ -157,8 +157,13 @@ def test_window_contraction_matches_gathered(built_lib, name, monkeypatch):
     kernel that gathers the B operand per tile."""
     import cqpi
     win, _ = _run(name, cqpi.PREC_MIXED)
+    monkeypatch.setenv("CQPI_TC_ATMEM", "1")
+    win_smem_a, _ = _run(name, cqpi.PREC_MIXED)
+    monkeypatch.delenv("CQPI_TC_ATMEM")
     monkeypatch.setenv("CQPI_TC_WINDOW", "0")
     gathered, _ = _run(name, cqpi.PREC_MIXED)
+    # Phi read from tensor memory or from shared memory: the same products in the same order
+    assert np.abs(win - win_smem_a).max() <= 1e-7 * np.abs(gathered).max()
     assert np.abs(win - gathered).max() <= 5e-7 * np.abs(gathered).max()
 
 
