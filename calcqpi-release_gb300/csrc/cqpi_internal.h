@@ -46,6 +46,7 @@ struct TcPlan {
     bool win = false;
     int wH = 0;          // 8-site groups per tile (sites per tile = 8*wH)
     int wEB = 0;         // energies per tile
+    int wNRAW = 0;       // raw-window ring depth (fetches run wNRAW-1 tiles ahead)
     int wNX = 0;         // window width in sites (8*wH + 2*window)
     int wNKC = 0;        // 8-element K chunks per window row (even)
     int wKP = 0;         // A columns: (2*window+1) * wNKC * 8
@@ -58,7 +59,7 @@ struct TcParams {
     int b, n, os, w, Rb, NB, W, nblk, mb, bs0, bs1;
     int TS, N, KP, Q, nimp, ne, wn, ntx, sst;
     int tmem_cols, a_bytes, b_bytes;
-    int H, NX, NKC, win_bytes, EB;   // direct-window variant
+    int H, NX, NKC, win_bytes, EB, nraw;   // direct-window variant
     int a_tmem;                  // direct-window variant: Phi operand held in tensor memory
     float inv_sA;
     long long spin_limit;

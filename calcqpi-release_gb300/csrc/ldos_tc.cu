@@ -81,17 +81,19 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
-// Bounded wait for the given phase parity; false on time-out.
+// Bounded wait for the given phase parity; false on time-out.  Each try_wait may suspend
+// the thread for up to 1 us (it resumes as soon as the phase completes), so waiting warps
+// do not take issue slots from the working ones; limit counts try_wait attempts.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit)
 {
     for (long long it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(mbar), "r"(parity)
+            : "r"(mbar), "r"(parity), "r"(1000u)
             : "memory");
         if (done) return true;
     }
@@ -398,7 +400,8 @@ __device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, uint32_
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_n() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 template <int B>
 __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __grid_constant__ TcParams p)
@@ -765,17 +768,22 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     const int nplanes = 2 * EB * twob;            // planes per kchunk
     unsigned char *smA = sm;                                                   // A hi, A lo (unless a_tmem)
     unsigned char *smW = smA + (p.a_tmem ? 0 : 2 * (size_t)p.a_bytes);         // [buffer][hi,lo] windows
-    // raw windows: two buffers of [op][energy] windows, then a zero slot
+    // raw windows: a ring of nraw buffers of [op][energy] windows, then a zero slot
     float *raw = reinterpret_cast<float *>(smW + 4 * (size_t)p.win_bytes);
     const int rawbuf = 2 * EB * rawfl;
-    const int zslot = 2 * rawbuf;
+    const int nraw = p.nraw;
+    const int zslot = nraw * rawbuf;
     int *offR = reinterpret_cast<int *>(raw + zslot + 4);                      // [op][8*NKC] offsets in a raw column
     // epilogue constants of the current energy block: T [energy][impurity][b*b],
     // 1/(sA sB)^2 [energy], term1 [energy][q]
     float2 *cT = reinterpret_cast<float2 *>(offR + 2 * NKC * 8);
     float *cInv2 = reinterpret_cast<float *>(cT + EB * p.nimp * bb);
     float *cT1 = cInv2 + EB;
-    const size_t mb_off = ((size_t)(reinterpret_cast<unsigned char *>(cT1 + EB * 128) - sm) + 15) & ~(size_t)15;
+    // producer: source offset (float2 units, -1 outside the box) of every raw-window column
+    // of the tile being fetched, [op][energy][x]
+    const size_t ct_off = ((size_t)(reinterpret_cast<unsigned char *>(cT1 + EB * 128) - sm) + 15) & ~(size_t)15;
+    long long *colTab = reinterpret_cast<long long *>(sm + ct_off);
+    const size_t mb_off = ct_off + 8 * (size_t)(2 * EB * NX);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + mb_off);   // [8]
     uint64_t *win_full = mbar, *win_empty = mbar + 2, *acc_full = mbar + 4, *acc_empty = mbar + 6;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 8);
@@ -904,7 +912,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             mbar_wait(smem_u32(&acc_full[k & 1]), (k >> 1) & 1, p.spin_limit);
     } else if (warp >= TCW_EPI / 32) {
         // ---------------------------------------------------------------- producer
-        const int ptid = tid - TCW_EPI, pwarp = warp - TCW_EPI / 32;
+        const int ptid = tid - TCW_EPI;
         // staging items: one plane row (kchunk, operand, energy, band/re-im, x) of 8 halfs;
         // the first two items of this thread are the same in every tile, so they are
         // decomposed once
@@ -929,19 +937,41 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         if (ptid + 2 * TCW_PROD < nitems) item_of(ptid + 2 * TCW_PROD, r2, t2, d2, q2);
         auto scale_of = [&](int e) { return e < p.ne ? pow2_scale(p.gmax[e]) : 1.f; };
         // cp.async the raw FP32 windows of a tile (zero outside the box and past the last energy)
-        auto fetch_raw = [&](int rb, int e0, int j, int i0) {
-            const int py = j - n2, px0 = i0 - n2;
-            for (int seg = pwarp; seg < 2 * EB * NX; seg += TCW_PROD / 32) {
-                const int w_ = seg / NX, xl = seg - w_ * NX;
-                const int op = w_ / EB, ee = w_ - op * EB;
-                const int e = e0 + ee;
-                const int X = op == 0 ? px0 - p.w + xl : -px0 - (TS - 1) - p.w + xl;
-                const int Y0 = op == 0 ? py - p.w : -py - p.w;
+        // raw-window columns: thread ptid < ncol owns column ptid = (op, energy, x) of the
+        // column table; copies: thread ptid issues copies ptid, ptid + 256, ... of the
+        // 8-byte pieces (column, piece) in column-major order, advanced without divisions
+        const int ncol = 2 * EB * NX, ncopy = ncol * rowlen;
+        int my_op = 0, my_ee = 0, my_xl = 0;
+        if (ptid < ncol) {
+            const int w_ = ptid / NX;
+            my_xl = ptid - w_ * NX;
+            my_op = w_ / EB;
+            my_ee = w_ - my_op * EB;
+        }
+        const int col0 = ptid / rowlen, pc0 = ptid - col0 * rowlen;
+        const int dcol = TCW_PROD / rowlen, dpc = TCW_PROD - dcol * rowlen;
+        // column table of a tile (threads < ncol; read after a producer barrier)
+        auto column_table = [&](int e0, int j, int i0) {
+            if (ptid < ncol) {
+                const int py = j - n2, px0 = i0 - n2, e = e0 + my_ee;
+                const int X = my_op == 0 ? px0 - p.w + my_xl : -px0 - (TS - 1) - p.w + my_xl;
+                const int Y0 = my_op == 0 ? py - p.w : -py - p.w;
                 const bool in = e < p.ne && X >= -p.Rb && X <= p.Rb;
-                const float2 *src = in ? p.box + ((size_t)e * p.NB * p.NB + (size_t)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb
-                                       : p.box;
-                float *w = raw + rb * rawbuf + w_ * rawfl + 2 * xl * rowlen;
-                for (int c = lane; c < rowlen; c += 32) cp_async8(smem_u32(w + 2 * c), in ? src + c : src, in ? 8u : 0u);
+                colTab[ptid] = in ? ((long long)e * p.NB * p.NB + (long long)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb : -1LL;
+            }
+        };
+        // cp.async the raw FP32 windows described by the column table into raw buffer rb
+        // (zero-filled outside the box and past the last energy)
+        auto fetch_raw = [&](int rb) {
+            float *rawb = raw + rb * rawbuf;
+            int col = col0, pc = pc0;
+            for (int idx = ptid; idx < ncopy; idx += TCW_PROD) {
+                const long long so = colTab[col];
+                const float2 *src = so >= 0 ? p.box + so + pc : p.box;
+                cp_async8(smem_u32(rawb + 2 * (col * rowlen + pc)), src, so >= 0 ? 8u : 0u);
+                col += dcol;
+                pc += dpc;
+                if (pc >= rowlen) { pc -= rowlen; col++; }
             }
             cp_async_commit();
         };
@@ -969,15 +999,28 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         int e0, j, i0;
         int se = -1;
         float sB0 = 1.f, sB1 = 1.f, sB2 = 1.f;
-        if (tile_of(0, e0, j, i0)) fetch_raw(0, e0, j, i0);
+        // raw windows run nraw-1 tiles ahead; every iteration commits exactly one cp.async
+        // group (possibly empty), so waiting for all but the newest nraw-1 groups means
+        // this tile's windows have landed
+        for (int k = 0; k < nraw; k++) {
+            int ke, kj, ki0;
+            const bool has = tile_of(k, ke, kj, ki0);
+            if (has) column_table(ke, kj, ki0);
+            bar_sync_group<2, TCW_PROD>();
+            if (k == nraw - 1) break;                 // its table is used by the first iteration
+            if (has) fetch_raw(k);
+            else cp_async_commit();
+            bar_sync_group<2, TCW_PROD>();
+        }
         for (int it = 0; ok; it++) {
             if (!tile_of(it, e0, j, i0)) break;
             const int s = it & 1;
-            // the next tile's raw windows go to the other raw buffer, whose last reader (the
-            // previous iteration's convert) finished before that iteration's final barrier
+            // the tile nraw-1 ahead goes to the raw buffer last read by the previous
+            // iteration's convert, which finished before that iteration's final barrier
             int ne_, nj, ni0;
-            const bool has_next = tile_of(it + 1, ne_, nj, ni0);
-            if (has_next) fetch_raw((it + 1) & 1, ne_, nj, ni0);
+            const int ahead = it + nraw - 1;
+            if (tile_of(ahead, ne_, nj, ni0)) fetch_raw(ahead % nraw);   // table computed last iteration
+            else cp_async_commit();
             const bool good = it < 2 || mbar_wait(smem_u32(&win_empty[s]), ((it - 2) >> 1) & 1, p.spin_limit);
             if (bar_or_group<2, TCW_PROD>(!good)) {
                 ok = false;
@@ -989,10 +1032,12 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                 sB2 = scale_of(e0 + q2);
                 se = e0;
             }
-            if (has_next) cp_async_wait_1(); else cp_async_wait_all();   // this tile's windows landed
+            if (nraw == 4) cp_async_wait_n<3>();
+            else if (nraw == 3) cp_async_wait_n<2>();
+            else cp_async_wait_n<1>();
             bar_sync_group<2, TCW_PROD>();
             unsigned char *Wb = smW + (size_t)s * 2 * p.win_bytes;
-            const int rb = it & 1;
+            const int rb = it % nraw;
             if (ptid < nitems) convert_item(Wb, rb, r0, t0, d0, sB0);
             if (ptid + TCW_PROD < nitems) convert_item(Wb, rb, r1, t1, d1, sB1);
             if (ptid + 2 * TCW_PROD < nitems) convert_item(Wb, rb, r2, t2, d2, sB2);
@@ -1001,6 +1046,9 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                 item_of(k, rb_, to_, ds_, q_);
                 convert_item(Wb, rb, rb_, to_, ds_, scale_of(e0 + q_));
             }
+            // every copy of this iteration was issued before the first barrier above, so the
+            // table can now describe the tile fetched next iteration
+            if (tile_of(ahead + 1, ne_, nj, ni0)) column_table(ne_, nj, ni0);
             fence_proxy_async();
             bar_sync_group<2, TCW_PROD>();           // buffer staged, raw buffer rb free
             if (ptid == 0) mbar_arrive(smem_u32(&win_full[s]));
@@ -1191,11 +1239,19 @@ void tc_plan(cqpi_handle *h)
                 const int wwt = 8 * H * h->os;
                 const int sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
                 const size_t rawfl = (size_t)NX * side * bbz * 2;
-                // shared memory with Phi in shared memory (the larger of the two layouts)
-                // (the per-impurity epilogue constants are added at launch)
-                const size_t smem = 2 * (size_t)pl.w_a_bytes + 4 * (size_t)win_bytes + 4 * (4 * EB * rawfl + 4) +
-                                    4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * 8 + 16;
+                // shared memory with Phi in shared memory (the larger of the two layouts); the
+                // per-impurity epilogue constants are added at launch.  The raw-window ring
+                // is as deep as fits (2..4), leaving 16 KiB for those constants.
+                auto smem_of = [&](int nraw) {
+                    return 2 * (size_t)pl.w_a_bytes + 4 * (size_t)win_bytes + 4 * (nraw * 2 * EB * rawfl + 4) +
+                           4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * (size_t)(2 * EB * NX) +
+                           8 * 8 + 16;
+                };
+                int nraw = 4;
+                while (nraw > 2 && smem_of(nraw) > 211 * 1024) nraw--;
+                const size_t smem = smem_of(nraw);
                 if (smem > 227 * 1024) continue;
+                pl.wNRAW = nraw;
                 pl.wEB = EB; pl.wH = H; pl.wNX = NX; pl.w_win_bytes = win_bytes; pl.w_sst = sst;
                 pl.w_a_tmem = a_tmem; pl.w_tmem_cols = wc; pl.w_smem = smem;
                 pl.win = h->nblk == 1 && h->Q <= 128;
@@ -1276,7 +1332,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     p.ntx = (h->n + pl.TS - 1) / pl.TS;
     p.tmem_cols = pl.tmem_cols; p.a_bytes = pl.a_bytes; p.b_bytes = pl.b_bytes;
     p.inv_sA = h->tc_inv_sA;
-    p.spin_limit = 1LL << 24;
+    p.spin_limit = 1LL << 21;   // try_wait attempts (each suspends at most 1 us)
     p.box = h->ws.box32; p.T32 = h->ws.T32; p.term1 = h->ws.term1; p.gmax = h->ws.gmax;
     p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
     p.out = out;
@@ -1290,7 +1346,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     const long long ntiles = (long long)ne * h->n * p.ntx;
     cudaError_t err;
     if (win) {
-        p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB;
+        p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB; p.nraw = pl.wNRAW;
         p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
         p.ntx = (h->n + p.TS - 1) / p.TS;
         p.tmem_cols = pl.w_tmem_cols;
