@@ -355,6 +355,14 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
             dst[2 * e + 1] += model->t[2 * i + 1];
         }
         h->nR = (int)idx.size();
+        // real hoppings: H(-k) = conj(H(k)), the eigen-solve covers half the k-grid
+        // (CQPI_TIME_REVERSAL=0 solves every k-point)
+        {
+            bool real = true;
+            for (size_t q = 1; q < tn.size(); q += 2) real = real && tn[q] == 0.0 && ta[q] == 0.0;
+            const char *f = getenv("CQPI_TIME_REVERSAL");
+            h->time_reversal = real && !(f && !strcmp(f, "0"));
+        }
         dalloc(&h->d_R, Rv.size());
         dalloc(&h->d_tn, tn.size());
         dalloc(&h->d_ta, ta.size());
@@ -377,6 +385,7 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         dalloc(&h->d_evec, nk * bb);
         if (h->precision == CQPI_PREC_MIXED) {
             dalloc(&h->d_evec32, nk * bb);
+            dalloc(&h->d_eval32, nk * b);
             std::vector<float2> tw32(h->kp);
             for (int t = 0; t < h->kp; t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
             dalloc(&h->d_tw32, h->kp);
@@ -429,6 +438,7 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_eval);
     dfree(h->d_evec);
     dfree(h->d_evec32);
+    dfree(h->d_eval32);
     dfree(h->d_phi);
     dfree(h->d_phi32);
     dfree(h->d_tc_a);

@@ -12,17 +12,26 @@
 
 namespace cqpi {
 
+// tr: all hoppings are real, so H(-k) = conj(H(k)): threads cover the k_x rows
+// 0 .. kp/2 only and each writes its k-point and the point reflection -k (same
+// eigenvalues, conjugated eigenvectors); on the self-reflected rows 0 and kp/2 the
+// thread with the larger j' = -j mod kp leaves the pair to its partner.
 template <int B>
-__global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, double efermi, int nR,
+__global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int tr, int scmax, double efermi, int nR,
                                                     const int32_t *__restrict__ R, const double2 *__restrict__ tn,
                                                     const double2 *__restrict__ ta, double *__restrict__ eval,
                                                     double2 *__restrict__ evec, float2 *__restrict__ evec32,
-                                                    const double2 *__restrict__ tw)
+                                                    float2 *__restrict__ eval32, const double2 *__restrict__ tw)
 {
     const long long nk = (long long)kp * kp;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk) return;
+    const long long nthr = tr ? (long long)(kp / 2 + 1) * kp : nk;
+    if (k >= nthr) return;
     const int i = (int)(k / kp), j = (int)(k % kp);
+    const int ir = (kp - i) % kp, jr = (kp - j) % kp;
+    if (tr && ir == i && jr < j) return;
+    const long long kr = (long long)ir * kp + jr;    // -k
+    const bool pair = tr && kr != k;
     const int bb = b * b;
 
     double ar[B][B], ai[B][B], vr[B][B], vi[B][B];
@@ -107,14 +116,28 @@ __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int scmax, do
 
 #pragma unroll
     for (int n = 0; n < B; n++)
-        if (n < b) eval[(size_t)n * nk + k] = ar[n][n];
+        if (n < b) {
+            eval[(size_t)n * nk + k] = ar[n][n];
+            if (pair) eval[(size_t)n * nk + kr] = ar[n][n];
+            if (eval32) {
+                // eigenvalue as an unevaluated float pair hi + lo (for FP32 energy differences)
+                const float hi = (float)ar[n][n];
+                const float2 e2 = make_float2(hi, (float)(ar[n][n] - (double)hi));
+                eval32[(size_t)n * nk + k] = e2;
+                if (pair) eval32[(size_t)n * nk + kr] = e2;
+            }
+        }
 #pragma unroll
     for (int o = 0; o < B; o++)
 #pragma unroll
         for (int n = 0; n < B; n++)
             if (o < b && n < b) {
                 evec[(size_t)(o * b + n) * nk + k] = make_double2(vr[o][n], vi[o][n]);
-                if (evec32) evec32[(size_t)(o * b + n) * nk + k] = make_float2((float)vr[o][n], (float)vi[o][n]);
+                if (pair) evec[(size_t)(o * b + n) * nk + kr] = make_double2(vr[o][n], -vi[o][n]);
+                if (evec32) {
+                    evec32[(size_t)(o * b + n) * nk + k] = make_float2((float)vr[o][n], (float)vi[o][n]);
+                    if (pair) evec32[(size_t)(o * b + n) * nk + kr] = make_float2((float)vr[o][n], -(float)vi[o][n]);
+                }
             }
 }
 
@@ -122,9 +145,11 @@ template <int B>
 static void launch_bands_t(cqpi_handle *h)
 {
     const long long nk = (long long)h->kp * h->kp;
-    bands_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, h->kp, h->scmax, h->efermi, h->nR, h->d_R,
+    const long long nthr = h->time_reversal ? (long long)(h->kp / 2 + 1) * h->kp : nk;
+    bands_kernel<B><<<cdiv(nthr, 128), 128, 0, h->stream>>>(h->b, h->kp, h->time_reversal ? 1 : 0, h->scmax,
+                                                            h->efermi, h->nR, h->d_R,
                                                           (const double2 *)h->d_tn, (const double2 *)h->d_ta,
-                                                          h->d_eval, h->d_evec, h->d_evec32, h->d_tw);
+                                                          h->d_eval, h->d_evec, h->d_evec32, h->d_eval32, h->d_tw);
     h->launches++;
 }
 

@@ -107,6 +107,8 @@ struct cqpi_handle {
     double *d_eval = nullptr;
     double2 *d_evec = nullptr;
     float2 *d_evec32 = nullptr;   // FP32 copy for the mixed path
+    float2 *d_eval32 = nullptr;   // eigenvalues as float pairs (hi, lo) for the mixed path
+    bool time_reversal = false;   // every hopping is real: H(-k) = conj(H(k))
     bool bands_ready = false;
     // twiddles e^{+2 pi i t / kp}
     double2 *d_tw = nullptr;

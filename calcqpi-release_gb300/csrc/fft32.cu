@@ -144,25 +144,33 @@ __global__ void __launch_bounds__(256) g0_rowfft_kernel(int b, int kp, int logkp
 
 
 // ------------------------------------------------------------------ register four-step row transform
-// e^{+2 pi i k / 64}, k = 0..63 (cos, sin rounded to float): twiddles of the register FFTs
-__constant__ float2 c_w64[64] = {
-    {1.000000000e+00f, 0.000000000e+00f}, {9.951847267e-01f, 9.801714033e-02f}, {9.807852804e-01f, 1.950903220e-01f}, {9.569403357e-01f, 2.902846773e-01f},
-    {9.238795325e-01f, 3.826834324e-01f}, {8.819212643e-01f, 4.713967368e-01f}, {8.314696123e-01f, 5.555702330e-01f}, {7.730104534e-01f, 6.343932842e-01f},
-    {7.071067812e-01f, 7.071067812e-01f}, {6.343932842e-01f, 7.730104534e-01f}, {5.555702330e-01f, 8.314696123e-01f}, {4.713967368e-01f, 8.819212643e-01f},
-    {3.826834324e-01f, 9.238795325e-01f}, {2.902846773e-01f, 9.569403357e-01f}, {1.950903220e-01f, 9.807852804e-01f}, {9.801714033e-02f, 9.951847267e-01f},
-    {6.123233996e-17f, 1.000000000e+00f}, {-9.801714033e-02f, 9.951847267e-01f}, {-1.950903220e-01f, 9.807852804e-01f}, {-2.902846773e-01f, 9.569403357e-01f},
-    {-3.826834324e-01f, 9.238795325e-01f}, {-4.713967368e-01f, 8.819212643e-01f}, {-5.555702330e-01f, 8.314696123e-01f}, {-6.343932842e-01f, 7.730104534e-01f},
-    {-7.071067812e-01f, 7.071067812e-01f}, {-7.730104534e-01f, 6.343932842e-01f}, {-8.314696123e-01f, 5.555702330e-01f}, {-8.819212643e-01f, 4.713967368e-01f},
-    {-9.238795325e-01f, 3.826834324e-01f}, {-9.569403357e-01f, 2.902846773e-01f}, {-9.807852804e-01f, 1.950903220e-01f}, {-9.951847267e-01f, 9.801714033e-02f},
-    {-1.000000000e+00f, 1.224646799e-16f}, {-9.951847267e-01f, -9.801714033e-02f}, {-9.807852804e-01f, -1.950903220e-01f}, {-9.569403357e-01f, -2.902846773e-01f},
-    {-9.238795325e-01f, -3.826834324e-01f}, {-8.819212643e-01f, -4.713967368e-01f}, {-8.314696123e-01f, -5.555702330e-01f}, {-7.730104534e-01f, -6.343932842e-01f},
-    {-7.071067812e-01f, -7.071067812e-01f}, {-6.343932842e-01f, -7.730104534e-01f}, {-5.555702330e-01f, -8.314696123e-01f}, {-4.713967368e-01f, -8.819212643e-01f},
-    {-3.826834324e-01f, -9.238795325e-01f}, {-2.902846773e-01f, -9.569403357e-01f}, {-1.950903220e-01f, -9.807852804e-01f}, {-9.801714033e-02f, -9.951847267e-01f},
-    {-1.836970199e-16f, -1.000000000e+00f}, {9.801714033e-02f, -9.951847267e-01f}, {1.950903220e-01f, -9.807852804e-01f}, {2.902846773e-01f, -9.569403357e-01f},
-    {3.826834324e-01f, -9.238795325e-01f}, {4.713967368e-01f, -8.819212643e-01f}, {5.555702330e-01f, -8.314696123e-01f}, {6.343932842e-01f, -7.730104534e-01f},
-    {7.071067812e-01f, -7.071067812e-01f}, {7.730104534e-01f, -6.343932842e-01f}, {8.314696123e-01f, -5.555702330e-01f}, {8.819212643e-01f, -4.713967368e-01f},
-    {9.238795325e-01f, -3.826834324e-01f}, {9.569403357e-01f, -2.902846773e-01f}, {9.807852804e-01f, -1.950903220e-01f}, {9.951847267e-01f, -9.801714033e-02f},
-};
+// e^{+2 pi i k / 64}, k = 0..63 (cos, sin rounded to float): twiddles of the register FFTs.
+// Local constexpr tables: with k a compile-time constant (fully unrolled butterflies) the
+// values become immediates, so no twiddle is loaded and trivial ones are skipped.
+__device__ __forceinline__ float2 w64(int k)
+{
+    constexpr float re[64] = {
+        1.000000000e+00f, 9.951847267e-01f, 9.807852804e-01f, 9.569403357e-01f, 9.238795325e-01f, 8.819212643e-01f, 8.314696123e-01f, 7.730104534e-01f,
+        7.071067812e-01f, 6.343932842e-01f, 5.555702330e-01f, 4.713967368e-01f, 3.826834324e-01f, 2.902846773e-01f, 1.950903220e-01f, 9.801714033e-02f,
+        6.123233996e-17f, -9.801714033e-02f, -1.950903220e-01f, -2.902846773e-01f, -3.826834324e-01f, -4.713967368e-01f, -5.555702330e-01f, -6.343932842e-01f,
+        -7.071067812e-01f, -7.730104534e-01f, -8.314696123e-01f, -8.819212643e-01f, -9.238795325e-01f, -9.569403357e-01f, -9.807852804e-01f, -9.951847267e-01f,
+        -1.000000000e+00f, -9.951847267e-01f, -9.807852804e-01f, -9.569403357e-01f, -9.238795325e-01f, -8.819212643e-01f, -8.314696123e-01f, -7.730104534e-01f,
+        -7.071067812e-01f, -6.343932842e-01f, -5.555702330e-01f, -4.713967368e-01f, -3.826834324e-01f, -2.902846773e-01f, -1.950903220e-01f, -9.801714033e-02f,
+        -1.836970199e-16f, 9.801714033e-02f, 1.950903220e-01f, 2.902846773e-01f, 3.826834324e-01f, 4.713967368e-01f, 5.555702330e-01f, 6.343932842e-01f,
+        7.071067812e-01f, 7.730104534e-01f, 8.314696123e-01f, 8.819212643e-01f, 9.238795325e-01f, 9.569403357e-01f, 9.807852804e-01f, 9.951847267e-01f,
+    };
+    constexpr float im[64] = {
+        0.000000000e+00f, 9.801714033e-02f, 1.950903220e-01f, 2.902846773e-01f, 3.826834324e-01f, 4.713967368e-01f, 5.555702330e-01f, 6.343932842e-01f,
+        7.071067812e-01f, 7.730104534e-01f, 8.314696123e-01f, 8.819212643e-01f, 9.238795325e-01f, 9.569403357e-01f, 9.807852804e-01f, 9.951847267e-01f,
+        1.000000000e+00f, 9.951847267e-01f, 9.807852804e-01f, 9.569403357e-01f, 9.238795325e-01f, 8.819212643e-01f, 8.314696123e-01f, 7.730104534e-01f,
+        7.071067812e-01f, 6.343932842e-01f, 5.555702330e-01f, 4.713967368e-01f, 3.826834324e-01f, 2.902846773e-01f, 1.950903220e-01f, 9.801714033e-02f,
+        1.224646799e-16f, -9.801714033e-02f, -1.950903220e-01f, -2.902846773e-01f, -3.826834324e-01f, -4.713967368e-01f, -5.555702330e-01f, -6.343932842e-01f,
+        -7.071067812e-01f, -7.730104534e-01f, -8.314696123e-01f, -8.819212643e-01f, -9.238795325e-01f, -9.569403357e-01f, -9.807852804e-01f, -9.951847267e-01f,
+        -1.000000000e+00f, -9.951847267e-01f, -9.807852804e-01f, -9.569403357e-01f, -9.238795325e-01f, -8.819212643e-01f, -8.314696123e-01f, -7.730104534e-01f,
+        -7.071067812e-01f, -6.343932842e-01f, -5.555702330e-01f, -4.713967368e-01f, -3.826834324e-01f, -2.902846773e-01f, -1.950903220e-01f, -9.801714033e-02f,
+    };
+    return make_float2(re[k], im[k]);
+}
 
 // In-register radix-2 DFT of length L (sign +1), natural order in and out.
 template <int L>
@@ -185,8 +193,10 @@ __device__ __forceinline__ void fft_reg(float2 (&x)[L])
             const int hl = 1 << s;
             const int k = t & (hl - 1);
             const int i0 = ((t >> s) << (s + 1)) | k;
-            const float2 w = c_w64[k * (64 >> (s + 1))];
-            const float2 u = x[i0], v = cmul(x[i0 + hl], w);
+            const int widx = k * (64 >> (s + 1));   // < 32; 0: w = 1, 16: w = i
+            const float2 y = x[i0 + hl];
+            const float2 v = widx == 0 ? y : (widx == 16 ? make_float2(-y.y, y.x) : cmul(y, w64(widx)));
+            const float2 u = x[i0];
             x[i0] = cadd(u, v);
             x[i0 + hl] = csub(u, v);
         }
@@ -197,12 +207,13 @@ __device__ __forceinline__ void fft_reg(float2 (&x)[L])
 // n2 of x[n1 + N1 n2] (registers), twiddle e^{+2 pi i n1 k2 / kp}, then for each k2 a
 // length-N1 FFT over n1 (registers) giving X[k2 + N2 k1].  One shared-memory exchange
 // between the two passes instead of log2(kp) butterfly rounds.  BM: largest band count
-// whose eigenvectors are kept in registers during the G0 build.
-template <int N1, int N2, int BM = 4>
-__global__ void __launch_bounds__(256) g0_rowfft_reg_kernel(int b, int NB, int Rb, int pg, double eta,
+// whose eigenvectors are kept in registers during the G0 build.  MAXT: largest block size
+// the kernel is launched with (one thread per transform of a plane group where possible).
+template <int N1, int N2, int BM = 4, int MAXT = 256>
+__global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int Rb, int pg, int eig_smem, double eta,
                                                             const double *__restrict__ energies, int ne,
-                                                            const double *__restrict__ eval,
-                                                            const float2 *__restrict__ evec,
+                                                            const float2 *__restrict__ eval_g,
+                                                            const float2 *__restrict__ evec_g,
                                                             const float2 *__restrict__ tw, float2 *__restrict__ half)
 {
     constexpr int KP = N1 * N2;
@@ -214,31 +225,48 @@ __global__ void __launch_bounds__(256) g0_rowfft_reg_kernel(int b, int NB, int R
     float2 *tws = sm + (size_t)pg * PLEN;        // e^{+2 pi i t / kp}, t < kp
     for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
     const float et = (float)eta;
+    // eigen cache of this k_x row: kept in shared memory for all energies when it fits
+    // ([band][j] eigenvalues, [o*b+n][j] eigenvectors), else read from global memory
+    const float2 *eval = eval_g + (size_t)i * KP;
+    const float2 *evec = evec_g + (size_t)i * KP;
+    long long estride = nk;
+    if (eig_smem) {
+        float2 *se = tws + KP;
+        float2 *sv = se + (size_t)b * KP;
+        for (int t = threadIdx.x; t < b * KP; t += blockDim.x) se[t] = eval[(size_t)(t / KP) * nk + (t % KP)];
+        for (int t = threadIdx.x; t < bb * KP; t += blockDim.x) sv[t] = evec[(size_t)(t / KP) * nk + (t % KP)];
+        eval = se;
+        evec = sv;
+        estride = KP;
+    }
 
     for (int e = 0; e < ne; e++) {
         const double om = energies[e];
+        // omega - eps in FP32 from float pairs: (om_hi - e_hi) is exact when the two are
+        // within a factor of two (Sterbenz), so the difference keeps its accuracy near poles
+        const float om_hi = (float)om, om_lo = (float)(om - (double)om_hi);
         for (int pl0 = 0; pl0 < bb; pl0 += pg) {
             const int npl = min(pg, bb - pl0);
             __syncthreads();
             // ---- G0(k) for planes [pl0, pl0+npl), natural order j (padded)
             for (int j = threadIdx.x; j < KP; j += blockDim.x) {
-                const long long k = (long long)i * KP + j;
                 const int pos = pad32(j);
                 if (b <= BM && npl == bb) {
                     float2 f[BM], U[BM][BM];
 #pragma unroll
                     for (int n = 0; n < BM; n++) {
                         if (n < b) {
-                            const float dr = (float)(om - eval[(size_t)n * nk + k]);
-                            const float den = dr * dr + et * et;
-                            f[n] = make_float2(dr / den, -et / den);
+                            const float2 ev = eval[(size_t)n * estride + j];
+                            const float dr = (om_hi - ev.x) + (om_lo - ev.y);
+                            const float inv = __frcp_rn(dr * dr + et * et);
+                            f[n] = make_float2(dr * inv, -et * inv);
                         }
                     }
 #pragma unroll
                     for (int o = 0; o < BM; o++)
 #pragma unroll
                         for (int n = 0; n < BM; n++)
-                            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+                            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * estride + j];
 #pragma unroll
                     for (int o = 0; o < BM; o++) {
                         if (o >= b) continue;
@@ -265,11 +293,12 @@ __global__ void __launch_bounds__(256) g0_rowfft_reg_kernel(int b, int NB, int R
                         const int pl = pl0 + q, o = pl / b, a = pl - o * b;
                         float2 s = make_float2(0.f, 0.f);
                         for (int n = 0; n < b; n++) {
-                            const float dr = (float)(om - eval[(size_t)n * nk + k]);
-                            const float den = dr * dr + et * et;
-                            const float2 f = make_float2(dr / den, -et / den);
-                            const float2 x = cmul(evec[(size_t)(o * b + n) * nk + k], f);
-                            const float2 ua = evec[(size_t)(a * b + n) * nk + k];
+                            const float2 ev = eval[(size_t)n * estride + j];
+                            const float dr = (om_hi - ev.x) + (om_lo - ev.y);
+                            const float inv = __frcp_rn(dr * dr + et * et);
+                            const float2 f = make_float2(dr * inv, -et * inv);
+                            const float2 x = cmul(evec[(size_t)(o * b + n) * estride + j], f);
+                            const float2 ua = evec[(size_t)(a * b + n) * estride + j];
                             s.x += x.x * ua.x + x.y * ua.y;
                             s.y += x.y * ua.x - x.x * ua.y;
                         }
@@ -418,25 +447,51 @@ static int rowfft_reg_plane_group(const cqpi_handle *h)
     return std::max(1, std::min(pg, h->b * h->b));
 }
 
-template <int N1, int N2>
+// bytes of one k_x row of the eigen cache (FP64 eigenvalues, FP32 eigenvectors)
+static size_t rowfft_eig_bytes(const cqpi_handle *h) { return (size_t)h->kp * (8 * h->b + 8 * h->b * h->b); }   // float2 pairs
+
+// shared memory of the register row transform: pg planes, the twiddles and, when it fits
+// in 227 KiB, the row's eigen cache
+static size_t rowfft_reg_smem(const cqpi_handle *h, bool *eig_smem)
+{
+    const int pg = rowfft_reg_plane_group(h);
+    const size_t base = 8 * ((size_t)pg * (h->kp + h->kp / 32 + 1) + h->kp);
+    const bool fits = base + rowfft_eig_bytes(h) <= 227 * 1024;
+    if (eig_smem) *eig_smem = fits;
+    return fits ? base + rowfft_eig_bytes(h) : base;
+}
+
+// block size: one thread per (plane, n1) / (plane, k2) transform of a plane group, so that
+// both passes run in one round (e.g. 9 planes x 32 = 288 for three bands and kp = 1024)
+template <int N1, int N2, int MAXT>
+static int rowfft_reg_threads(const cqpi_handle *h)
+{
+    const int pg = rowfft_reg_plane_group(h);
+    const int t = ((pg * std::max(N1, N2) + 31) / 32) * 32;
+    return std::max(64, std::min(MAXT, t));
+}
+
+template <int N1, int N2, int MAXT = 256>
 static void launch_rowfft_reg_t(cqpi_handle *h, int ne, const double *d_energies)
 {
     const int pg = rowfft_reg_plane_group(h);
-    const size_t smem = 8 * ((size_t)pg * (N1 * N2 + (N1 * N2) / 32 + 1) + N1 * N2);
-    g0_rowfft_reg_kernel<N1, N2><<<h->kp, 256, smem, h->stream>>>(h->b, h->NB, h->Rb, pg, h->eta, d_energies, ne,
-                                                                  h->d_eval, h->d_evec32, h->d_tw32, h->ws.half32);
+    bool eig = false;
+    const size_t smem = rowfft_reg_smem(h, &eig);
+    const char *f = getenv("CQPI_ROWFFT_EIG");
+    if (f && !strcmp(f, "global")) eig = false;
+    g0_rowfft_reg_kernel<N1, N2, 4, MAXT><<<h->kp, rowfft_reg_threads<N1, N2, MAXT>(h), smem, h->stream>>>(
+        h->b, h->NB, h->Rb, pg, eig ? 1 : 0, h->eta, d_energies, ne, h->d_eval32, h->d_evec32, h->d_tw32, h->ws.half32);
 }
 
 static cudaError_t configure_rowfft_reg(cqpi_handle *h)
 {
-    const int pg = rowfft_reg_plane_group(h);
-    const int smem = (int)(8 * ((size_t)pg * (h->kp + h->kp / 32 + 1) + h->kp));
+    const int smem = (int)rowfft_reg_smem(h, nullptr);
     switch (h->kp) {
     case 64: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 128: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 256: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 512: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    case 1024: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 1024: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 32, 4, 288>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 2048: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 4096: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
@@ -450,7 +505,7 @@ static void launch_rowfft_reg(cqpi_handle *h, int ne, const double *d_energies)
     case 128: launch_rowfft_reg_t<8, 16>(h, ne, d_energies); break;
     case 256: launch_rowfft_reg_t<16, 16>(h, ne, d_energies); break;
     case 512: launch_rowfft_reg_t<16, 32>(h, ne, d_energies); break;
-    case 1024: launch_rowfft_reg_t<32, 32>(h, ne, d_energies); break;
+    case 1024: launch_rowfft_reg_t<32, 32, 288>(h, ne, d_energies); break;
     case 2048: launch_rowfft_reg_t<32, 64>(h, ne, d_energies); break;
     case 4096: launch_rowfft_reg_t<64, 64>(h, ne, d_energies); break;
     }

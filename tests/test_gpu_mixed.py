@@ -187,3 +187,17 @@ def test_window_contraction_tiles_and_k_steps(built_lib, lattice, window, oversa
     for e in range(len(E)):
         err = np.abs(out[cqpi.PREC_MIXED][e, 0] - ref[e, 0]).max() / np.abs(ref[e, 0]).max()
         assert err <= TOL, (lattice, window, oversamp, E[e], err)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "c2_zero"])
+def test_time_reversal_matches_full_solve(built_lib, name, monkeypatch):
+    """Real hoppings: the eigen-solve of half the k-grid plus H(-k) = conj(H(k)) gives the
+    maps of the full solve (FP64 path to rounding, mixed path to its tolerance)."""
+    import cqpi
+    half64, _ = _run(name, cqpi.PREC_FP64)
+    halfmx, _ = _run(name, cqpi.PREC_MIXED)
+    monkeypatch.setenv("CQPI_TIME_REVERSAL", "0")
+    full64, _ = _run(name, cqpi.PREC_FP64)
+    fullmx, _ = _run(name, cqpi.PREC_MIXED)
+    assert np.abs(half64 - full64).max() <= 1e-12 * np.abs(full64).max()
+    assert np.abs(halfmx - fullmx).max() <= 1e-6 * np.abs(fullmx).max()
