@@ -85,6 +85,8 @@ def load():
     L.cqpi_measure_fma_peak.argtypes = [i32, ctypes.POINTER(dbl)]
     L.cqpi_contraction_kind.argtypes = [P, ctypes.POINTER(i32)]
     L.cqpi_realspace_greens_noalloc.argtypes = [P, i32, i32, i32, P, P]
+    L.cqpi_set_hoppings.argtypes = [P, P]
+    L.cqpi_adjoint.argtypes = [P, P, i32, P, i32, P, P]
     _lib = L
     return L
 
@@ -116,6 +118,7 @@ class Engine:
         self.wn = self.lattice * self.oversamp
         self.side = (2 * self.window + 1) * self.oversamp
         self.nimp = 1
+        self.nhops = len(model.t)
         self._R = np.ascontiguousarray(model.R, np.int32)
         self._orb = np.ascontiguousarray(model.orb, np.int32)
         self._t = np.ascontiguousarray(np.asarray(model.t, np.complex128).view(np.float64))
@@ -168,6 +171,13 @@ class Engine:
         self._check(self._L.cqpi_set_impurities(self._h, _ptr(V.view(np.float64)), V.shape[0]))
         self.nimp = V.shape[0]
 
+    def set_hoppings(self, t):
+        """New complex amplitudes for the model's hopping terms (same order as model.t)."""
+        t = np.ascontiguousarray(np.asarray(t, np.complex128).reshape(-1))
+        assert len(t) == self.nhops
+        self._t = np.ascontiguousarray(t.view(np.float64))
+        self._check(self._L.cqpi_set_hoppings(self._h, _ptr(self._t)))
+
     # -- compute
     def solve_bands(self):
         self._check(self._L.cqpi_solve_bands(self._h))
@@ -190,6 +200,22 @@ class Engine:
         """Asynchronous run into device buffers (raw pointers, e.g. torch tensor.data_ptr())."""
         e = np.ascontiguousarray(energies, np.float64).reshape(-1)
         self._check(self._L.cqpi_run(self._h, _ptr(e), len(e), ptr32, ptr64, 1))
+
+    def adjoint(self, energies, dL_dmaps=None, dev_ptr=None):
+        """Reverse-mode derivative of run(): dL/drho (host float32 [nE][nimp][wn][wn], or a
+        device pointer to that layout) -> (dL/dt complex [nhops], dL/dV complex
+        [nimp][b][b]) with dL/dz = dL/dRe z + i dL/dIm z."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        gt = np.zeros(2 * self.nhops, np.float64)
+        gv = np.zeros(2 * self.nimp * self.bands * self.bands, np.float64)
+        if dev_ptr is not None:
+            rc = self._L.cqpi_adjoint(self._h, _ptr(e), len(e), dev_ptr, 1, _ptr(gt), _ptr(gv))
+        else:
+            w = np.ascontiguousarray(dL_dmaps, np.float32)
+            assert w.size == len(e) * self.nimp * self.wn * self.wn
+            rc = self._L.cqpi_adjoint(self._h, _ptr(e), len(e), _ptr(w), 0, _ptr(gt), _ptr(gv))
+        self._check(rc)
+        return gt.view(np.complex128), gv.view(np.complex128).reshape(self.nimp, self.bands, self.bands)
 
     # -- narrow seam
     def wannierldos(self, T, g0r):

@@ -74,6 +74,35 @@ void free_workspace(cqpi_handle *h)
     h->ws.ebatch = 0;
 }
 
+void free_adj(cqpi_handle *h)
+{
+    dfree(h->adj.gbox);
+    dfree(h->adj.M);
+    dfree(h->adj.wsum);
+    dfree(h->adj.gV);
+    dfree(h->adj.A);
+    dfree(h->adj.gk);
+    dfree(h->adj.C);
+    dfree(h->adj.gR);
+    h->adj.ebatch = 0;
+}
+
+void ensure_adj(cqpi_handle *h, int ebatch)
+{
+    if (h->adj.ebatch >= ebatch) return;
+    free_adj(h);
+    const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
+    dalloc(&h->adj.gbox, ebatch * (size_t)h->NB * h->NB * bb);
+    dalloc(&h->adj.M, ebatch * (size_t)std::max(h->nimp, 1) * bb);
+    dalloc(&h->adj.wsum, ebatch * (size_t)h->Q);
+    dalloc(&h->adj.gV, (size_t)std::max(h->nimp, 1) * bb);
+    dalloc(&h->adj.A, bb * (size_t)h->NB * h->kp);
+    dalloc(&h->adj.gk, bb * nk);
+    dalloc(&h->adj.C, bb * nk);
+    dalloc(&h->adj.gR, (size_t)std::max(h->nR, 1) * 2 * bb);
+    h->adj.ebatch = ebatch;
+}
+
 size_t bytes_per_energy(const cqpi_handle *h)
 {
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
@@ -86,6 +115,7 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
 {
     if (h->ws.ebatch >= ebatch) return;
     free_workspace(h);
+    free_adj(h);
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
     if (h->precision == CQPI_PREC_FP64) {
         dalloc(&h->ws.g0k, ebatch * bb * nk);
@@ -350,11 +380,18 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
                 r = it->second;
             }
             const size_t e = (size_t)r * bb + (size_t)model->orb[2 * i] * b + model->orb[2 * i + 1];
-            std::vector<double> &dst = (model->anti && model->anti[i]) ? ta : tn;
+            const bool anti = model->anti && model->anti[i];
+            std::vector<double> &dst = anti ? ta : tn;
             dst[2 * e] += model->t[2 * i];
             dst[2 * e + 1] += model->t[2 * i + 1];
+            h->hop_r.push_back(r);
+            h->hop_o1.push_back(model->orb[2 * i]);
+            h->hop_o2.push_back(model->orb[2 * i + 1]);
+            h->hop_anti.push_back(anti ? 1 : 0);
         }
         h->nR = (int)idx.size();
+        h->rt_tn = tn;
+        h->rt_ta = ta;
         // real hoppings: H(-k) = conj(H(k)), the eigen-solve covers half the k-grid
         // (CQPI_TIME_REVERSAL=0 solves every k-point)
         {
@@ -430,6 +467,7 @@ int cqpi_destroy(cqpi_handle *h)
     if (!h) return CQPI_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_workspace(h);
+    free_adj(h);
     dfree(h->d_R);
     dfree(h->d_tn);
     dfree(h->d_ta);
@@ -521,7 +559,10 @@ int cqpi_set_impurities(cqpi_handle *h, const double *V, int32_t nimp)
         dfree(h->d_V);
         dalloc(&h->d_V, bb * nimp);
         CK(cudaMemcpy(h->d_V, V, sizeof(double2) * bb * nimp, cudaMemcpyHostToDevice));
-        if (nimp > h->nimp) free_workspace(h);
+        if (nimp > h->nimp) {
+            free_workspace(h);
+            free_adj(h);
+        }
         h->nimp = nimp;
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
@@ -618,6 +659,110 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             h->status_pending = false;
             if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
         }
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_set_hoppings(cqpi_handle *h, const double *t)
+{
+    if (!h || !t) return CQPI_ERR_ARG;
+    const size_t bb = (size_t)h->b * h->b;
+    std::vector<double> tn(h->rt_tn.size(), 0.0), ta(h->rt_ta.size(), 0.0);
+    for (size_t i = 0; i < h->hop_r.size(); i++) {
+        if (!(t[2 * i] == t[2 * i]) || !(t[2 * i + 1] == t[2 * i + 1])) return fail(h, CQPI_ERR_ARG, "NaN hopping");
+        const size_t e = (size_t)h->hop_r[i] * bb + (size_t)h->hop_o1[i] * h->b + h->hop_o2[i];
+        std::vector<double> &dst = h->hop_anti[i] ? ta : tn;
+        dst[2 * e] += t[2 * i];
+        dst[2 * e + 1] += t[2 * i + 1];
+    }
+    bool real = true;
+    for (size_t q = 1; q < tn.size(); q += 2) real = real && tn[q] == 0.0 && ta[q] == 0.0;
+    const char *f = getenv("CQPI_TIME_REVERSAL");
+    try {
+        if (!tn.empty()) {
+            CK(cudaMemcpyAsync(h->d_tn, tn.data(), sizeof(double) * tn.size(), cudaMemcpyHostToDevice, h->stream));
+            CK(cudaMemcpyAsync(h->d_ta, ta.data(), sizeof(double) * ta.size(), cudaMemcpyHostToDevice, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        }
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    h->rt_tn.swap(tn);
+    h->rt_ta.swap(ta);
+    h->time_reversal = real && !(f && !strcmp(f, "0"));
+    h->bands_ready = false;
+    return CQPI_OK;
+}
+
+int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float *dL_dmaps, int32_t on_device,
+                 double *dL_dt, double *dL_dV)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (nE < 0 || (nE > 0 && (!energies || !dL_dmaps))) return fail(h, CQPI_ERR_ARG, "invalid energies or map gradient");
+    if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    if (h->nblk != 1) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: spin blocks are not supported");
+    if (h->kp & (h->kp - 1)) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: kpoints must be a power of two");
+    if (h->Q > 128) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: oversamp^2 must be <= 128");
+    const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
+    const size_t mapn = (size_t)h->wn * h->wn, per_e = (size_t)h->nimp * mapn;
+    const int nhops = (int)h->hop_r.size();
+    try {
+        const int eb = choose_batch(h, std::max(nE, 1));
+        ensure_workspace(h, eb);
+        ensure_adj(h, eb);
+        ensure_energies(h, std::max(nE, 1));
+        if (!on_device && nE > 0) ensure_stage32(h, (size_t)eb * per_e);
+        CK(cudaMemsetAsync(h->adj.C, 0, sizeof(double2) * bb * nk, h->stream));
+        CK(cudaMemsetAsync(h->adj.gR, 0, sizeof(double2) * (size_t)std::max(h->nR, 1) * 2 * bb, h->stream));
+        CK(cudaMemsetAsync(h->adj.gV, 0, sizeof(double2) * (size_t)std::max(h->nimp, 1) * bb, h->stream));
+        if (nE > 0) {
+            memcpy(h->h_energies_pinned, energies, sizeof(double) * nE);
+            CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * nE, cudaMemcpyHostToDevice,
+                               h->stream));
+        }
+        if (!h->bands_ready) do_bands(h);
+        for (int e0 = 0; e0 < nE; e0 += eb) {
+            const int ne = std::min(eb, nE - e0);
+            const double *den = h->d_energies_all + e0;
+            if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
+            CK(cudaMemsetAsync(h->adj.gbox, 0, sizeof(double2) * ne * (size_t)h->NB * h->NB * bb, h->stream));
+            CK(cudaMemsetAsync(h->adj.M, 0, sizeof(double2) * ne * (size_t)h->nimp * bb, h->stream));
+            CK(cudaMemsetAsync(h->adj.wsum, 0, sizeof(double) * ne * (size_t)h->Q, h->stream));
+            const float *wm = dL_dmaps + (size_t)e0 * per_e;
+            if (!on_device) {
+                CK(cudaMemcpyAsync(h->stage32, wm, sizeof(float) * ne * per_e, cudaMemcpyHostToDevice, h->stream));
+                wm = h->stage32;
+            }
+            do_greens(h, ne, den);
+            launch_tmatrix(h, ne);
+            check_launch();
+            launch_adj_energy_batch(h, ne, wm, h->adj);
+            check_launch();
+            for (int e = 0; e < ne; e++) {
+                launch_adj_kspace(h, e, energies[e0 + e], h->adj);
+                check_launch();
+            }
+        }
+        launch_adj_hoppings(h, h->adj);
+        check_launch();
+        std::vector<double2> gR((size_t)std::max(h->nR, 1) * 2 * bb), gV((size_t)std::max(h->nimp, 1) * bb);
+        CK(cudaMemcpyAsync(gR.data(), h->adj.gR, sizeof(double2) * gR.size(), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(gV.data(), h->adj.gV, sizeof(double2) * gV.size(), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
+        if (dL_dt)
+            for (int i = 0; i < nhops; i++) {
+                const double2 g = gR[((size_t)h->hop_r[i] * 2 + h->hop_anti[i]) * bb + (size_t)h->hop_o1[i] * h->b + h->hop_o2[i]];
+                dL_dt[2 * i] = g.x;
+                dL_dt[2 * i + 1] = g.y;
+            }
+        if (dL_dV)
+            for (size_t k = 0; k < (size_t)h->nimp * bb; k++) {
+                dL_dV[2 * k] = gV[k].x;
+                dL_dV[2 * k + 1] = gV[k].y;
+            }
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }

@@ -1,0 +1,601 @@
+// adjoint.cu -- reverse-mode derivative of the continuum-LDOS pipeline: given
+// W = dL/drho for every map of a run, the gradient of L with respect to the model's
+// hopping amplitudes t and every impurity matrix V.
+//
+// Forward chain (one spin block):
+//   H(k) = D + sum_R tn(R) e^{+i th} + ta(R) e^{-i th}            (bands.cu)
+//   G(k) = (z - H(k))^{-1} = U diag(f) U^H,  f_n = 1/(omega + i eta - eps_n)
+//   G(R) = kp^-2 sum_k e^{+2 pi i k.R / kp} G(k)                    (greens.cu / fft32.cu)
+//   T    = (1 - V g)^{-1} V,  g = G(0)                               (tmatrix_kernel)
+//   u_a  = sum_{d,o} phi_o(q,d) G(p+d)[o][a],  s_c = sum_{d,o} G(-p-d)[c][o] phi_o(q,d)
+//   rho  = -term1(q) - Im(sum_ac u_a T_ac s_c),
+//   term1(q) = sum_{d1,d2,o1,o2} phi_o1(q,d1) phi_o2(q,d2) Im G(d2-d1)[o2][o1]
+// (src/qpi.cc:454-486, 557-578, 833-854, 876-950).  Gradients of real L with respect to a
+// complex z are written zbar = dL/dRe z + i dL/dIm z; for L = -W Im(c z) this is
+// zbar = -i W conj(c), and a holomorphic linear map z -> y = P z Q pulls back as
+// zbar = P^H ybar Q^H.  The adjoint recomputes G(R) and T per energy (nothing of the
+// forward run is stored) and goes back through:
+//   1. adj_contract_kernel: u, s per pixel; ubar = -i W conj(T s), sbar = -i W conj(u T);
+//      M = sum W u s^T (-> Tbar = -i conj M); window scatter of phi^T ubar / phi^T sbar into
+//      the G(R) box gradient; sum_p W per pixel for the term1 part.
+//   2. adj_term1_kernel: term1 part of the box gradient.
+//   3. adj_tv_kernel: gbar(0) += T^H Tbar T^H, Vbar += A^-H Tbar (1 + g T)^H, A = 1 - V g.
+//   4. adj_cols_kernel / adj_rows_kernel: Gbar(k) = kp^-2 sum_R e^{-2 pi i k.R/kp} Gbar(R)
+//      (the forward's pruned transform read backwards: box -> full k-grid, FP64).
+//   5. adj_kacc_kernel: Hbar(k) = G^H Gbar G^H = U [F* (U^H Gbar U) F*] U^H; the bracket
+//      is accumulated over energies per k in FP64, U [..] U^H is applied once at the end
+//      (adj_hbar_kernel).
+//   6. adj_hop_kernel: tbar for every unique R, normal and conjugated terms:
+//      sum_k e^{-/+ i th(k)} Hbar(k)[p][q] (FP64 sums over the k-grid).
+// The contraction adjoint computes in the handle's precision (FP32 with the mixed box,
+// FP64 with the FP64 box) and accumulates in FP64; steps 2-6 are FP64.
+#include "cplx.h"
+#include "cqpi_internal.h"
+
+namespace cqpi {
+
+namespace {
+
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ void atomic_add2(double2 *p, double2 v)
+{
+    atomicAdd(&p->x, v.x);
+    atomicAdd(&p->y, v.y);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ 1. contraction adjoint
+// grid (n*n sites, ne*nimp maps), block: one thread per sub-pixel q (Q <= 128).
+template <int B, class C>
+__global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os, int w, int Rb, int NB, int Q, int W, int nimp,
+                                                           int mb, int bs0, const typename real_of<C>::type *__restrict__ phi,
+                                                           const C *__restrict__ box, const double2 *__restrict__ T,
+                                                           const float *__restrict__ wmap, double2 *__restrict__ gbox,
+                                                           double2 *__restrict__ Mbuf, double *__restrict__ wsum)
+{
+    using Rl = typename real_of<C>::type;
+    extern __shared__ __align__(16) unsigned char adj_sm[];
+    Rl *ubr = reinterpret_cast<Rl *>(adj_sm);               // [128][b] each: ubar, sbar (re, im)
+    Rl *ubi = ubr + 128 * b, *sbr = ubi + 128 * b, *sbi = sbr + 128 * b;
+    const int site = blockIdx.x, ei = blockIdx.y;
+    const int e = ei / nimp;
+    const int i = site / n, j = site % n;
+    const int n2 = n >> 1, px = i - n2, py = j - n2;
+    const int wn = n * os, bb = b * b, side = 2 * w + 1;
+    const int q = threadIdx.x;
+    const bool qv = q < Q;
+    const int qx = qv ? q / os : 0, qy = qv ? q % os : 0;
+    const C *boxe = box + (size_t)e * NB * NB * bb;
+    const double2 *Te = T + (size_t)ei * bb;
+    double2 *gb = gbox + (size_t)e * NB * NB * bb;
+    const Rl *ph = phi + (size_t)q * W * mb;
+
+    Rl W_ = 0;
+    Rl ur[B], ui[B], sr[B], si[B];
+#pragma unroll
+    for (int a = 0; a < B; a++) { ur[a] = 0; ui[a] = 0; sr[a] = 0; si[a] = 0; }
+    if (qv) {
+        W_ = (Rl)wmap[((size_t)ei * wn + (size_t)j * os + qy) * wn + (size_t)i * os + qx];
+        for (int d = 0; d < W; d++) {
+            const int dx = d / side - w, dy = d % side - w;
+            const C *gs = boxe + ((size_t)(-px - dx + Rb) * NB + (-py - dy + Rb)) * bb;
+            const C *gu = boxe + ((size_t)(px + dx + Rb) * NB + (py + dy + Rb)) * bb;
+            for (int ol = 0; ol < mb; ol++) {
+                const Rl f = ph[d * mb + ol];
+                if (f == (Rl)0) continue;
+                const int o = bs0 + ol;
+#pragma unroll
+                for (int a = 0; a < B; a++) {
+                    if (a < b) {
+                        const C vs = gs[a * b + o], vu = gu[o * b + a];
+                        sr[a] += vs.x * f; si[a] += vs.y * f;
+                        ur[a] += vu.x * f; ui[a] += vu.y * f;
+                    }
+                }
+            }
+        }
+    }
+    // ts = T s, ut = u^T T; ubar = -i W conj(ts), sbar = -i W conj(ut)
+#pragma unroll
+    for (int a = 0; a < B; a++) {
+        Rl tsr = 0, tsi = 0, utr = 0, uti = 0;
+        if (a < b) {
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                if (c < b) {
+                    const double2 t = Te[a * b + c];      // T_ac
+                    tsr += (Rl)t.x * sr[c] - (Rl)t.y * si[c];
+                    tsi += (Rl)t.x * si[c] + (Rl)t.y * sr[c];
+                    const double2 t2 = Te[c * b + a];     // T_ca
+                    utr += ur[c] * (Rl)t2.x - ui[c] * (Rl)t2.y;
+                    uti += ur[c] * (Rl)t2.y + ui[c] * (Rl)t2.x;
+                }
+            }
+        }
+        if (a < b) {
+            ubr[q * b + a] = -W_ * tsi; ubi[q * b + a] = -W_ * tsr;
+            sbr[q * b + a] = -W_ * uti; sbi[q * b + a] = -W_ * utr;
+        }
+    }
+    if (qv && W_ != (Rl)0) atomicAdd(wsum + (size_t)e * Q + q, (double)W_);
+    // M_ac = sum_q W u_a s_c: warp sums, then one atomic per warp and element
+#pragma unroll
+    for (int a = 0; a < B; a++)
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            if (a >= b || c >= b) continue;
+            double mr = qv ? (double)W_ * ((double)ur[a] * sr[c] - (double)ui[a] * si[c]) : 0.0;
+            double mi = qv ? (double)W_ * ((double)ur[a] * si[c] + (double)ui[a] * sr[c]) : 0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                mr += __shfl_xor_sync(0xffffffffu, mr, o);
+                mi += __shfl_xor_sync(0xffffffffu, mi, o);
+            }
+            if ((threadIdx.x & 31) == 0 && (mr != 0.0 || mi != 0.0)) atomic_add2(Mbuf + (size_t)ei * bb + a * b + c, make_double2(mr, mi));
+        }
+    __syncthreads();
+    // window gradients: entry (d, o) of phi^T ubar (into G(p+d)[o][a]) and of phi^T sbar
+    // (into G(-p-d)[c][o])
+    for (int t = threadIdx.x; t < W * mb; t += blockDim.x) {
+        const int d = t / mb, ol = t - d * mb, o = bs0 + ol;
+        const int dx = d / side - w, dy = d % side - w;
+        Rl gur[B], gui[B], gsr[B], gsi[B];
+#pragma unroll
+        for (int a = 0; a < B; a++) { gur[a] = 0; gui[a] = 0; gsr[a] = 0; gsi[a] = 0; }
+        bool any = false;
+        for (int qq = 0; qq < Q; qq++) {
+            const Rl f = phi[((size_t)qq * W + d) * mb + ol];
+            if (f == (Rl)0) continue;
+            any = true;
+#pragma unroll
+            for (int a = 0; a < B; a++) {
+                if (a < b) {
+                    gur[a] += f * ubr[qq * b + a]; gui[a] += f * ubi[qq * b + a];
+                    gsr[a] += f * sbr[qq * b + a]; gsi[a] += f * sbi[qq * b + a];
+                }
+            }
+        }
+        if (!any) continue;
+        double2 *du = gb + ((size_t)(px + dx + Rb) * NB + (py + dy + Rb)) * bb;
+        double2 *ds = gb + ((size_t)(-px - dx + Rb) * NB + (-py - dy + Rb)) * bb;
+#pragma unroll
+        for (int a = 0; a < B; a++) {
+            if (a < b) {
+                atomic_add2(du + o * b + a, make_double2((double)gur[a], (double)gui[a]));
+                atomic_add2(ds + a * b + o, make_double2((double)gsr[a], (double)gsi[a]));
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ 2. term1
+// grid ((4w+1)^2 offsets Delta, ne); threads over q.  rho has -term1, so
+// Gbar(Delta)[o2][o1] += -i sum_q wsum(q) sum_{d1} phi_o1(q,d1) phi_o2(q,d1+Delta).
+__global__ void __launch_bounds__(128) adj_term1_kernel(int b, int w, int Rb, int NB, int Q, int W, int mb, int bs0,
+                                                        const double *__restrict__ phi, const double *__restrict__ wsum,
+                                                        double2 *__restrict__ gbox)
+{
+    const int e = blockIdx.y;
+    const int span = 4 * w + 1, side = 2 * w + 1;
+    const int rx = blockIdx.x / span - 2 * w, ry = blockIdx.x % span - 2 * w;
+    const int bb = b * b;
+    __shared__ double acc[CQPI_MAX_BANDS * CQPI_MAX_BANDS];
+    for (int t = threadIdx.x; t < mb * mb; t += blockDim.x) acc[t] = 0.0;
+    __syncthreads();
+    for (int q = threadIdx.x; q < Q; q += blockDim.x) {
+        const double ws = wsum[(size_t)e * Q + q];
+        if (ws == 0.0) continue;
+        for (int d1 = 0; d1 < W; d1++) {
+            const int x2 = d1 / side + rx, y2 = d1 % side + ry;   // window position of d2 = d1 + Delta
+            if (x2 < 0 || x2 >= side || y2 < 0 || y2 >= side) continue;
+            const int d2 = x2 * side + y2;
+            const double *p1 = phi + ((size_t)q * W + d1) * mb;
+            const double *p2 = phi + ((size_t)q * W + d2) * mb;
+            for (int o1 = 0; o1 < mb; o1++) {
+                if (p1[o1] == 0.0) continue;
+                for (int o2 = 0; o2 < mb; o2++) atomicAdd(&acc[o2 * mb + o1], ws * p1[o1] * p2[o2]);
+            }
+        }
+    }
+    __syncthreads();
+    double2 *g = gbox + ((size_t)e * NB * NB + (size_t)(rx + Rb) * NB + (ry + Rb)) * bb;
+    for (int t = threadIdx.x; t < mb * mb; t += blockDim.x) {
+        const int o2 = t / mb, o1 = t % mb;
+        if (acc[t] != 0.0) atomicAdd(&g[(bs0 + o2) * b + (bs0 + o1)].y, -acc[t]);
+    }
+}
+
+// ------------------------------------------------------------------ 3. T-matrix and V
+// one thread per (energy, impurity)
+template <class C>
+__global__ void adj_tv_kernel(int b, int NB, int Rb, int nimp, int ne, const C *__restrict__ box,
+                              const double2 *__restrict__ V, const double2 *__restrict__ T,
+                              const double2 *__restrict__ Mbuf, double2 *__restrict__ gbox, double2 *__restrict__ gV)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= ne * nimp) return;
+    const int e = id / nimp, imp = id % nimp;
+    const int bb = b * b;
+    constexpr int MB = CQPI_MAX_BANDS * CQPI_MAX_BANDS;
+    double2 g[MB], A[MB], Ai[MB], Tb[MB], X[MB];
+    const C *g0 = box + (((size_t)e * NB + Rb) * NB + Rb) * bb;
+    const double2 *v = V + (size_t)imp * bb, *Te = T + (size_t)id * bb, *M = Mbuf + (size_t)id * bb;
+    for (int k = 0; k < bb; k++) {
+        g[k] = to_d2(g0[k]);
+        Tb[k] = make_double2(-M[k].y, -M[k].x);   // Tbar = -i conj(M)
+    }
+    // A = 1 - V g, Ai = A^-1 (Gauss-Jordan with partial pivoting)
+    for (int r = 0; r < b; r++)
+        for (int c = 0; c < b; c++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(v[r * b + k], g[k * b + c]));
+            A[r * b + c] = make_double2((r == c ? 1.0 : 0.0) - s.x, -s.y);
+            Ai[r * b + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+        }
+    for (int c = 0; c < b; c++) {
+        int piv = c;
+        double best = -1.0;
+        for (int r = c; r < b; r++) {
+            const double a = hypot(A[r * b + c].x, A[r * b + c].y);
+            if (a > best) { best = a; piv = r; }
+        }
+        if (!(best > 0.0)) return;   // singular: the forward run reported it
+        if (piv != c)
+            for (int k = 0; k < b; k++) {
+                double2 t0 = A[c * b + k]; A[c * b + k] = A[piv * b + k]; A[piv * b + k] = t0;
+                t0 = Ai[c * b + k]; Ai[c * b + k] = Ai[piv * b + k]; Ai[piv * b + k] = t0;
+            }
+        const double2 p = A[c * b + c];
+        const double pd = p.x * p.x + p.y * p.y;
+        const double2 pinv = make_double2(p.x / pd, -p.y / pd);
+        for (int k = 0; k < b; k++) {
+            A[c * b + k] = cmul(A[c * b + k], pinv);
+            Ai[c * b + k] = cmul(Ai[c * b + k], pinv);
+        }
+        for (int r = 0; r < b; r++) {
+            if (r == c) continue;
+            const double2 f = A[r * b + c];
+            for (int k = 0; k < b; k++) {
+                A[r * b + k] = csub(A[r * b + k], cmul(f, A[c * b + k]));
+                Ai[r * b + k] = csub(Ai[r * b + k], cmul(f, Ai[c * b + k]));
+            }
+        }
+    }
+    // gbar(0) += T^H Tbar T^H
+    for (int r = 0; r < b; r++)
+        for (int c = 0; c < b; c++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(Tb[r * b + k], cconj(Te[c * b + k])));   // (Tbar T^H)_rc
+            X[r * b + c] = s;
+        }
+    double2 *gz = gbox + (((size_t)e * NB + Rb) * NB + Rb) * bb;
+    for (int r = 0; r < b; r++)
+        for (int c = 0; c < b; c++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(cconj(Te[k * b + r]), X[k * b + c]));     // (T^H X)_rc
+            atomic_add2(gz + r * b + c, s);
+        }
+    // Vbar += A^-H Tbar (1 + g T)^H
+    for (int r = 0; r < b; r++)
+        for (int c = 0; c < b; c++) {
+            double2 s = make_double2(r == c ? 1.0 : 0.0, 0.0);
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(g[r * b + k], Te[k * b + c]));        // (1 + g T)_rc
+            A[r * b + c] = s;
+        }
+    for (int r = 0; r < b; r++)
+        for (int c = 0; c < b; c++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(Tb[r * b + k], cconj(A[c * b + k])));    // (Tbar (1+gT)^H)_rc
+            X[r * b + c] = s;
+        }
+    for (int r = 0; r < b; r++)
+        for (int c = 0; c < b; c++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int k = 0; k < b; k++) s = cadd(s, cmul(cconj(Ai[k * b + r]), X[k * b + c]));    // (A^-H X)_rc
+            atomic_add2(gV + (size_t)imp * bb + r * b + c, s);
+        }
+}
+
+// ------------------------------------------------------------------ 4. box -> k-grid
+// In-place radix-2 transform of x[0..kp) (natural order in and out) with e^{-2 pi i t/kp}
+// twiddles from tw (e^{+2 pi i t/kp}).
+__device__ void fft_minus(double2 *x, int kp, int logkp, const double2 *__restrict__ tw)
+{
+    for (int t = threadIdx.x; t < kp; t += blockDim.x) {
+        const int r = logkp ? (int)(__brev((unsigned)t) >> (32 - logkp)) : 0;
+        if (r > t) { const double2 a = x[t]; x[t] = x[r]; x[r] = a; }
+    }
+    __syncthreads();
+    for (int len = 2; len <= kp; len <<= 1) {
+        const int hl = len >> 1, step = kp / len;
+        for (int t = threadIdx.x; t < (kp >> 1); t += blockDim.x) {
+            const int kk = t % hl, idx = (t / hl) * len + kk;
+            const double2 wv = cconj(__ldg(tw + kk * step));
+            const double2 u = x[idx], v = cmul(x[idx + hl], wv);
+            x[idx] = cadd(u, v);
+            x[idx + hl] = csub(u, v);
+        }
+        __syncthreads();
+    }
+}
+
+// A[pl][yb][kx] = sum_{X in box} e^{-2 pi i kx X/kp} Gbar(X, Y=yb-Rb)[pl]; grid (NB, bb)
+__global__ void __launch_bounds__(256) adj_cols_kernel(int kp, int logkp, int NB, int Rb, int bb, const double2 *__restrict__ gbox,
+                                                       const double2 *__restrict__ tw, double2 *__restrict__ A)
+{
+    extern __shared__ double2 xs[];
+    const int yb = blockIdx.x, pl = blockIdx.y;
+    for (int pos = threadIdx.x; pos < kp; pos += blockDim.x) {
+        double2 s = make_double2(0.0, 0.0);
+        // box columns X = xb - Rb with X == pos (mod kp)
+        int xb = ((pos + Rb) % kp);
+        for (; xb < NB; xb += kp) s = cadd(s, gbox[((size_t)xb * NB + yb) * bb + pl]);
+        xs[pos] = s;
+    }
+    __syncthreads();
+    fft_minus(xs, kp, logkp, tw);
+    double2 *dst = A + ((size_t)pl * NB + yb) * kp;
+    for (int t = threadIdx.x; t < kp; t += blockDim.x) dst[t] = xs[t];
+}
+
+// Gbar(kx, ky)[pl] = kp^-2 sum_{Y in box} e^{-2 pi i ky Y/kp} A[pl][Y+Rb][kx]; grid (kp, bb)
+__global__ void __launch_bounds__(256) adj_rows_kernel(int kp, int logkp, int NB, int Rb, int bb, double scale,
+                                                       const double2 *__restrict__ A, const double2 *__restrict__ tw,
+                                                       double2 *__restrict__ gk)
+{
+    extern __shared__ double2 xs[];
+    const int kx = blockIdx.x, pl = blockIdx.y;
+    const double2 *src = A + (size_t)pl * NB * kp + kx;
+    for (int pos = threadIdx.x; pos < kp; pos += blockDim.x) {
+        double2 s = make_double2(0.0, 0.0);
+        int yb = ((pos + Rb) % kp);
+        for (; yb < NB; yb += kp) s = cadd(s, src[(size_t)yb * kp]);
+        xs[pos] = s;
+    }
+    __syncthreads();
+    fft_minus(xs, kp, logkp, tw);
+    const size_t nk = (size_t)kp * kp;
+    double2 *dst = gk + (size_t)pl * nk + (size_t)kx * kp;
+    for (int t = threadIdx.x; t < kp; t += blockDim.x) dst[t] = cscale(xs[t], scale);
+}
+
+// ------------------------------------------------------------------ 5. per-k resolvent
+// C(k) += F* (U^H Gbar(k) U) F*, F = diag(1/(omega + i eta - eps_n)); one thread per k
+template <int B>
+__global__ void __launch_bounds__(128) adj_kacc_kernel(int b, long long nk, double omega, double eta,
+                                                       const double *__restrict__ eval, const double2 *__restrict__ evec,
+                                                       const double2 *__restrict__ gk, double2 *__restrict__ Cacc)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    double2 U[B][B], G[B][B], X[B][B], f[B];
+#pragma unroll
+    for (int n = 0; n < B; n++) {
+        if (n < b) {
+            const double dr = omega - eval[(size_t)n * nk + k];
+            const double den = dr * dr + eta * eta;
+            f[n] = make_double2(dr / den, eta / den);   // conj(1/(dr + i eta))
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < B; o++)
+#pragma unroll
+        for (int n = 0; n < B; n++)
+            if (o < b && n < b) {
+                U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+                G[o][n] = gk[(size_t)(o * b + n) * nk + k];
+            }
+    // X = Gbar U
+#pragma unroll
+    for (int o = 0; o < B; o++)
+#pragma unroll
+        for (int m = 0; m < B; m++) {
+            if (o >= b || m >= b) continue;
+            double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int a = 0; a < B; a++)
+                if (a < b) s = cadd(s, cmul(G[o][a], U[a][m]));
+            X[o][m] = s;
+        }
+    // C += f*_n (U^H X)_nm f*_m
+#pragma unroll
+    for (int n = 0; n < B; n++)
+#pragma unroll
+        for (int m = 0; m < B; m++) {
+            if (n >= b || m >= b) continue;
+            double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int o = 0; o < B; o++)
+                if (o < b) s = cadd(s, cmul(cconj(U[o][n]), X[o][m]));
+            s = cmul(cmul(f[n], s), f[m]);
+            double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
+            *c = cadd(*c, s);
+        }
+}
+
+// Hbar(k) = U C(k) U^H, written over gk
+template <int B>
+__global__ void __launch_bounds__(128) adj_hbar_kernel(int b, long long nk, const double2 *__restrict__ evec,
+                                                       const double2 *__restrict__ Cacc, double2 *__restrict__ hbar)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    double2 U[B][B], X[B][B];
+#pragma unroll
+    for (int o = 0; o < B; o++)
+#pragma unroll
+        for (int n = 0; n < B; n++)
+            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+    // X = U C
+#pragma unroll
+    for (int o = 0; o < B; o++)
+#pragma unroll
+        for (int m = 0; m < B; m++) {
+            if (o >= b || m >= b) continue;
+            double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int n = 0; n < B; n++)
+                if (n < b) s = cadd(s, cmul(U[o][n], Cacc[(size_t)(n * b + m) * nk + k]));
+            X[o][m] = s;
+        }
+#pragma unroll
+    for (int o = 0; o < B; o++)
+#pragma unroll
+        for (int a = 0; a < B; a++) {
+            if (o >= b || a >= b) continue;
+            double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int m = 0; m < B; m++)
+                if (m < b) s = cadd(s, cmul(X[o][m], cconj(U[a][m])));
+            hbar[(size_t)(o * b + a) * nk + k] = s;
+        }
+}
+
+// ------------------------------------------------------------------ 6. hoppings
+// grid (nR, chunks); out[r][0][pq] = sum_k e^{-i th_r(k)} Hbar(k)[pq] (normal terms),
+// out[r][1][pq] = sum_k e^{+i th_r(k)} Hbar(k)[pq] (conjugated terms), th = 2 pi (Rx i + Ry j)/kp
+__global__ void __launch_bounds__(256) adj_hop_kernel(int b, int kp, const int32_t *__restrict__ R,
+                                                      const double2 *__restrict__ tw, const double2 *__restrict__ hbar,
+                                                      double2 *__restrict__ out)
+{
+    const int r = blockIdx.x;
+    const int bb = b * b;
+    const long long nk = (long long)kp * kp;
+    const long long Rx = R[2 * r], Ry = R[2 * r + 1];
+    __shared__ double2 red[2][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int pq = 0; pq < bb; pq++) {
+        double2 sn = make_double2(0.0, 0.0), sa = make_double2(0.0, 0.0);
+        for (long long k = (long long)blockIdx.y * blockDim.x + threadIdx.x; k < nk; k += (long long)gridDim.y * blockDim.x) {
+            const long long i = k / kp, j = k - i * kp;
+            long long mm = (Rx * i + Ry * j) % kp;
+            if (mm < 0) mm += kp;
+            const double2 ph = __ldg(tw + mm);
+            const double2 h = hbar[(size_t)pq * nk + k];
+            sn = cadd(sn, cmul(cconj(ph), h));
+            sa = cadd(sa, cmul(ph, h));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            sn.x += __shfl_xor_sync(0xffffffffu, sn.x, o);
+            sn.y += __shfl_xor_sync(0xffffffffu, sn.y, o);
+            sa.x += __shfl_xor_sync(0xffffffffu, sa.x, o);
+            sa.y += __shfl_xor_sync(0xffffffffu, sa.y, o);
+        }
+        if (lane == 0) { red[0][warp] = sn; red[1][warp] = sa; }
+        __syncthreads();
+        if (threadIdx.x < 2) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) s = cadd(s, red[threadIdx.x][wv]);
+            atomic_add2(out + ((size_t)r * 2 + threadIdx.x) * bb + pq, s);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+template <int B, class C>
+static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>::type *phi, const C *box,
+                              const float *wmap, AdjWorkspace &aw)
+{
+    dim3 grid((unsigned)(h->n * h->n), (unsigned)(ne * h->nimp));
+    const size_t smem = 4 * 128 * (size_t)h->b * sizeof(typename real_of<C>::type);
+    adj_contract_kernel<B, C><<<grid, 128, smem, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp, h->mb,
+                                                           h->blk_start[0], phi, box, h->ws.T, wmap, aw.gbox, aw.M, aw.wsum);
+    h->launches++;
+}
+
+template <class C>
+static void dispatch_contract(cqpi_handle *h, int ne, const typename real_of<C>::type *phi, const C *box,
+                              const float *wmap, AdjWorkspace &aw)
+{
+    const int b = h->b;
+    if (b <= 1) launch_contract_t<1, C>(h, ne, phi, box, wmap, aw);
+    else if (b <= 2) launch_contract_t<2, C>(h, ne, phi, box, wmap, aw);
+    else if (b <= 3) launch_contract_t<3, C>(h, ne, phi, box, wmap, aw);
+    else if (b <= 4) launch_contract_t<4, C>(h, ne, phi, box, wmap, aw);
+    else if (b <= 6) launch_contract_t<6, C>(h, ne, phi, box, wmap, aw);
+    else if (b <= 8) launch_contract_t<8, C>(h, ne, phi, box, wmap, aw);
+    else if (b <= 12) launch_contract_t<12, C>(h, ne, phi, box, wmap, aw);
+    else launch_contract_t<16, C>(h, ne, phi, box, wmap, aw);
+}
+
+void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorkspace &aw)
+{
+    if (h->precision == CQPI_PREC_FP64) dispatch_contract<double2>(h, ne, h->d_phi, h->ws.box, wmap, aw);
+    else dispatch_contract<float2>(h, ne, h->d_phi32, h->ws.box32, wmap, aw);
+    const int span = 4 * h->w + 1;
+    adj_term1_kernel<<<dim3(span * span, ne), 128, 0, h->stream>>>(h->b, h->w, h->Rb, h->NB, h->Q, h->W, h->mb,
+                                                                   h->blk_start[0], h->d_phi, aw.wsum, aw.gbox);
+    h->launches++;
+    const int nt = ne * h->nimp;
+    if (h->precision == CQPI_PREC_FP64)
+        adj_tv_kernel<double2><<<cdiv(nt, 64), 64, 0, h->stream>>>(h->b, h->NB, h->Rb, h->nimp, ne, h->ws.box, h->d_V,
+                                                                   h->ws.T, aw.M, aw.gbox, aw.gV);
+    else
+        adj_tv_kernel<float2><<<cdiv(nt, 64), 64, 0, h->stream>>>(h->b, h->NB, h->Rb, h->nimp, ne, h->ws.box32, h->d_V,
+                                                                  h->ws.T, aw.M, aw.gbox, aw.gV);
+    h->launches++;
+}
+
+static int ilog2_exact(int v)
+{
+    int l = 0;
+    while ((1 << l) < v) l++;
+    return l;
+}
+
+template <int B>
+static void launch_kacc_t(cqpi_handle *h, double omega, AdjWorkspace &aw)
+{
+    const long long nk = (long long)h->kp * h->kp;
+    adj_kacc_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec, aw.gk, aw.C);
+    h->launches++;
+}
+
+void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw)
+{
+    const int kp = h->kp, logkp = ilog2_exact(kp), bb = h->b * h->b;
+    const size_t smem = sizeof(double2) * kp;
+    const double2 *gbe = aw.gbox + (size_t)e * h->NB * h->NB * bb;
+    adj_cols_kernel<<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw, aw.A);
+    adj_rows_kernel<<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, 1.0 / ((double)kp * kp), aw.A,
+                                                           h->d_tw, aw.gk);
+    h->launches += 2;
+    const int b = h->b;
+    if (b <= 1) launch_kacc_t<1>(h, omega, aw);
+    else if (b <= 2) launch_kacc_t<2>(h, omega, aw);
+    else if (b <= 3) launch_kacc_t<3>(h, omega, aw);
+    else if (b <= 4) launch_kacc_t<4>(h, omega, aw);
+    else if (b <= 6) launch_kacc_t<6>(h, omega, aw);
+    else if (b <= 8) launch_kacc_t<8>(h, omega, aw);
+    else if (b <= 12) launch_kacc_t<12>(h, omega, aw);
+    else launch_kacc_t<16>(h, omega, aw);
+}
+
+template <int B>
+static void launch_hbar_t(cqpi_handle *h, AdjWorkspace &aw)
+{
+    const long long nk = (long long)h->kp * h->kp;
+    adj_hbar_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
+    h->launches++;
+}
+
+void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw)
+{
+    const int b = h->b;
+    if (b <= 1) launch_hbar_t<1>(h, aw);
+    else if (b <= 2) launch_hbar_t<2>(h, aw);
+    else if (b <= 3) launch_hbar_t<3>(h, aw);
+    else if (b <= 4) launch_hbar_t<4>(h, aw);
+    else if (b <= 6) launch_hbar_t<6>(h, aw);
+    else if (b <= 8) launch_hbar_t<8>(h, aw);
+    else if (b <= 12) launch_hbar_t<12>(h, aw);
+    else launch_hbar_t<16>(h, aw);
+    if (h->nR > 0) {
+        const int chunks = std::max(1, std::min(64, (int)(((long long)h->kp * h->kp) / (256 * 64))));
+        adj_hop_kernel<<<dim3(h->nR, chunks), 256, 0, h->stream>>>(b, h->kp, h->d_R, h->d_tw, aw.gk, aw.gR);
+        h->launches++;
+    }
+}
+
+}  // namespace cqpi

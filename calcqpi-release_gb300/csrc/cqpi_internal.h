@@ -72,6 +72,19 @@ struct TcParams {
     int *status;
 };
 
+// Buffers of the adjoint (adjoint.cu), kept by the handle between calls.
+struct AdjWorkspace {
+    int ebatch = 0;
+    double2 *gbox = nullptr;   // [E][NB][NB][b*b]  dL/dG0(R) (box)
+    double2 *M = nullptr;      // [E][nimp][b*b]    sum W u s^T
+    double *wsum = nullptr;    // [E][Q]            sum_p W
+    double2 *gV = nullptr;     // [nimp][b*b]       dL/dV
+    double2 *A = nullptr;      // [b*b][NB][kp]     column pass of the box -> k transform
+    double2 *gk = nullptr;     // [b*b][nk]         dL/dG0(k), then dL/dH(k)
+    double2 *C = nullptr;      // [b*b][nk]         eigenbasis accumulator over energies
+    double2 *gR = nullptr;     // [nR][2][b*b]      dL/dtn, dL/dta per unique R
+};
+
 struct Workspace {
     int ebatch = 0;
     double2 *g0k = nullptr;
@@ -131,7 +144,12 @@ struct cqpi_handle {
     double2 *d_V = nullptr;   // [nimp][b*b]
     // workspace
     cqpi::Workspace ws;
+    cqpi::AdjWorkspace adj;
     int *d_status = nullptr;
+    // model hopping terms as given to cqpi_create (for cqpi_set_hoppings / cqpi_adjoint):
+    // unique-R index, orbital pair and conjugation flag of every term
+    std::vector<int> hop_r, hop_o1, hop_o2, hop_anti;
+    std::vector<double> rt_tn, rt_ta;   // host copies of the summed matrices [nR][b*b][2]
     // narrow seam (always FP64)
     double *d_seam_ldos = nullptr;
     double2 *d_seam_box = nullptr, *d_seam_T = nullptr;
@@ -179,6 +197,10 @@ bool tc_supported(const cqpi_handle *h);
 void tc_plan(cqpi_handle *h);
 void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img, float &inv_sA);
 void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img);
+// adjoint.cu
+void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorkspace &aw);
+void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw);
+void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
 cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out);
 void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n);
 

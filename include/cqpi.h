@@ -111,6 +111,21 @@ int cqpi_solve_bands(cqpi_handle *h);
  * are filled. */
 int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, double *maps64, int32_t on_device);
 
+/* ---- differentiation (extension: the reference computes no derivatives) -----
+ * New hopping amplitudes for the terms of the model given to cqpi_create (same order,
+ * same R / orbitals / conjugation flags): t[nhops][2].  The eigen cache is rebuilt by
+ * the next run or adjoint call. */
+int cqpi_set_hoppings(cqpi_handle *h, const double *t);
+/* Reverse-mode derivative of cqpi_run: given dL_dmaps = dL/drho in the maps32 layout
+ * [nE][nimp][wn][wn] (device memory if on_device != 0, else host), writes
+ *   dL_dt[nhops][2] = (dL/dRe t, dL/dIm t) for every hopping term of the model, and
+ *   dL_dV[nimp][b][b][2] = (dL/dRe V, dL/dIm V) for every impurity matrix entry.
+ * G0(k), G0(R) and T are recomputed per energy from the eigen cache; the call returns
+ * when the gradients are filled.  One spin block, kpoints a power of two, oversamp^2
+ * <= 128; otherwise CQPI_ERR_NOT_SUPPORTED.  Either output may be NULL. */
+int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float *dL_dmaps, int32_t on_device,
+                 double *dL_dt, double *dL_dV);
+
 /* ---- narrow seam (GPUQPI, include/gpuqpi.h:18-32) ------------------------
  * GPUQPI::wannierldos(scat, g0): host T-matrix T[b][b][2] and host real-space
  * Green's function g0r[kp][kp][b][b][2] (the reference's g0 after
