@@ -1,0 +1,143 @@
+"""Fitting harness around the engine's adjoint (outside the drop-in path).
+
+Loss (per energy, summed): || |FFT2(rho_w)| - target_w ||^2, the QPI magnitude of every
+LDOS map against target maps.  Parameters: the independent real amplitudes p of a
+symmetric model family (t = B p, see workloads.t2g_c2_parametrisation) and the impurity
+matrix V.  ``LDOSMaps`` is a torch.autograd.Function whose forward runs the engine
+(cqpi_set_hoppings / cqpi_set_impurities / cqpi_run into a CUDA tensor) and whose backward
+calls cqpi_adjoint on the incoming dL/drho; torch does only the loss (FFT, abs, square) and
+the optimiser.
+"""
+import time
+
+import numpy as np
+
+from . import Engine, PREC_FP64, PREC_MIXED
+from . import workloads as W
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class QPIFit:
+    """One engine plus the fixed pieces of a fit: energies, parametrisation, orbitals."""
+
+    def __init__(self, lattice=128, kpoints=1024, oversamp=10, window=2, energies=None, eta=0.002,
+                 seed=2, precision=PREC_MIXED, V=None):
+        self.model, self.B, self.p0 = W.t2g_c2_parametrisation(seed)
+        self.energies = np.linspace(-0.1, 0.1, 41) if energies is None else np.asarray(energies, np.float64)
+        self.eng = Engine(self.model, lattice, kpoints, oversamp, window, eta, precision=precision)
+        self.eng.set_orbitals(W.t2g_orbitals_c2(window, oversamp))
+        b = self.model.bands
+        self.V0 = np.diag([0.3, 0.3, 0.5]).astype(np.complex128) if V is None else np.asarray(V, np.complex128)
+        self.eng.set_impurities(self.V0[None])
+        self.wn = lattice * oversamp
+        self.bands = b
+        self.precision = precision
+        self.timing = {"forward": [], "adjoint": []}
+
+    def hoppings(self, p):
+        return self.B @ np.asarray(p, np.float64)
+
+    def set_params(self, p, V):
+        self.eng.set_hoppings(self.hoppings(p).astype(np.complex128))
+        self.eng.set_impurities(np.asarray(V, np.complex128).reshape(1, self.bands, self.bands))
+
+    def maps(self, p, V):
+        """rho for parameters (p, V) as a CUDA tensor [nE][1][wn][wn] (no autograd): float32
+        from the mixed engine, float64 from the FP64 engine."""
+        torch = _torch()
+        self.set_params(p, V)
+        fp64 = self.precision == PREC_FP64
+        out = torch.empty((len(self.energies), 1, self.wn, self.wn), dtype=torch.float64 if fp64 else torch.float32,
+                          device="cuda")
+        torch.cuda.synchronize()
+        if fp64:
+            self.eng.run_device(self.energies, ptr64=out.data_ptr())
+        else:
+            self.eng.run_device(self.energies, ptr32=out.data_ptr())
+        self.eng.synchronize()
+        return out
+
+    def close(self):
+        self.eng.close()
+
+
+def _ldos_function():
+    torch = _torch()
+
+    class LDOSMaps(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, p, Vr, fit):
+            t0 = time.perf_counter()
+            V = Vr.detach().cpu().numpy()
+            out = fit.maps(p.detach().cpu().numpy(), V)
+            fit.timing["forward"].append(time.perf_counter() - t0)
+            ctx.fit = fit
+            return out
+
+        @staticmethod
+        def backward(ctx, g):
+            fit = ctx.fit
+            t0 = time.perf_counter()
+            g = g.contiguous().to(torch.float32)
+            torch.cuda.synchronize()          # g is complete before the engine's stream reads it
+            gt, gv = fit.eng.adjoint(fit.energies, dev_ptr=g.data_ptr())
+            fit.timing["adjoint"].append(time.perf_counter() - t0)
+            # t = B p with real p: dL/dp = B^T dL/dRe t; V real: dL/dV = dL/dRe V
+            gp = torch.from_numpy(fit.B.T @ gt.real)
+            gV = torch.from_numpy(np.ascontiguousarray(gv[0].real))
+            return gp, gV, None
+
+    return LDOSMaps
+
+
+def qpi_loss(maps, target):
+    """sum over energies of || |FFT2(rho)| - target ||^2 (target: [nE][wn][wn] magnitudes)."""
+    torch = _torch()
+    q = torch.abs(torch.fft.fft2(maps[:, 0].to(torch.float64)))
+    return torch.sum((q - target) ** 2)
+
+
+def target_maps(fit, rel=0.05, seed=7):
+    """Target QPI magnitudes from seed-perturbed amplitudes p* = p0 (1 + rel N(0,1))."""
+    torch = _torch()
+    rng = np.random.default_rng(seed)
+    p_true = fit.p0 * (1.0 + rel * rng.normal(size=fit.p0.shape))
+    with torch.no_grad():
+        m = fit.maps(p_true, fit.V0.real)
+        tgt = torch.abs(torch.fft.fft2(m[:, 0].to(torch.float64)))
+    return p_true, tgt
+
+
+def run_adam(fit, target, steps=200, lr=2e-3, fit_v=False, log=None):
+    """Adam on (p, V) from p0 / V0; returns (p, V, losses)."""
+    torch = _torch()
+    LDOSMaps = _ldos_function()
+    p = torch.tensor(fit.p0.copy(), dtype=torch.float64, requires_grad=True)
+    Vr = torch.tensor(fit.V0.real.copy(), dtype=torch.float64, requires_grad=fit_v)
+    opt = torch.optim.Adam([p, Vr] if fit_v else [p], lr=lr)
+    losses = []
+    for it in range(steps):
+        opt.zero_grad()
+        maps = LDOSMaps.apply(p, Vr, fit)
+        loss = qpi_loss(maps, target)
+        loss.backward()
+        opt.step()
+        losses.append(float(loss.detach()))
+        if log is not None and (it % 20 == 0 or it == steps - 1):
+            log(it, losses[-1])
+    return p.detach().numpy(), Vr.detach().numpy(), losses
+
+
+def gradient(fit, p, V, target):
+    """(loss, dL/dp, dL/dV) at (p, V) through the adjoint."""
+    torch = _torch()
+    LDOSMaps = _ldos_function()
+    pt = torch.tensor(np.asarray(p, np.float64), requires_grad=True)
+    Vt = torch.tensor(np.asarray(V, np.float64), requires_grad=True)
+    loss = qpi_loss(LDOSMaps.apply(pt, Vt, fit), target)
+    loss.backward()
+    return float(loss.detach()), pt.grad.numpy(), Vt.grad.numpy()

@@ -131,6 +131,50 @@ def t2g_c2(seed: int = 2, sigma: float = 0.25) -> TBModel:
     return _from_terms(terms, 3, "t2g square lattice, seed %d (C2)" % seed)
 
 
+def t2g_c2_parametrisation(seed: int = 2, sigma: float = 0.25):
+    """Independent hopping amplitudes of the C2 model family: the symmetrisation of
+    t2g_c2 is linear in the raw shell matrices, so every C4-symmetric Hermitian model with
+    the same terms is t = B p for a real orthonormal basis B of that map's range.
+    Returns (model, B [nterms][P], p0) with model.t == B @ p0."""
+    model = t2g_c2(seed, sigma)
+    shells = [(0, 0), (1, 0), (0, 1), (-1, 0), (0, -1), (1, 1), (1, -1), (-1, 1), (-1, -1),
+              (2, 0), (0, 2), (-2, 0), (0, -2)]
+    D = np.array([[0, -1, 0], [1, 0, 0], [0, 0, -1]], dtype=np.float64)
+    ops = []
+    Dn = np.eye(3)
+    for n in range(4):
+        def op(r, n=n):
+            x, y = r
+            for _ in range(n):
+                x, y = -y, x
+            return (x, y)
+        ops.append((op, Dn.copy()))
+        Dn = D @ Dn
+    index = {(int(model.R[i, 0]), int(model.R[i, 1]), int(model.orb[i, 0]), int(model.orb[i, 1])): i
+             for i in range(len(model.t))}
+    cols = []
+    for s_ in shells:
+        for u in range(3):
+            for v in range(3):
+                raw = {r: np.zeros((3, 3), np.complex128) for r in shells}
+                raw[s_][u, v] = 1.0
+                sym = _symmetrise(raw, ops, 3)
+                col = np.zeros(len(model.t))
+                for k, M in sym.items():
+                    for a_ in range(3):
+                        for c_ in range(3):
+                            i = index.get((k[0], k[1], a_, c_))
+                            if i is not None:
+                                col[i] = M[a_, c_].real
+                cols.append(col)
+    J = np.array(cols).T
+    Uj, S, _ = np.linalg.svd(J, full_matrices=False)
+    rank = int(np.sum(S > 1e-10 * S[0]))
+    B = Uj[:, :rank]
+    p0 = B.T @ model.t.real
+    return model, B, p0
+
+
 def _rot2(th):
     return np.array([[math.cos(th), -math.sin(th)], [math.sin(th), math.cos(th)]])
 
