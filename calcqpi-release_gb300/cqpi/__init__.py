@@ -23,7 +23,8 @@ EXPORTED = [
     "cqpi_set_orbitals", "cqpi_set_scattering", "cqpi_set_impurities", "cqpi_solve_bands", "cqpi_run",
     "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
-    "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc",
+    "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
+    "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch",
 ]
 
 
@@ -86,6 +87,10 @@ def load():
     L.cqpi_contraction_kind.argtypes = [P, ctypes.POINTER(i32)]
     L.cqpi_realspace_greens_noalloc.argtypes = [P, i32, i32, i32, P, P]
     L.cqpi_set_hoppings.argtypes = [P, P]
+    L.cqpi_run_fov.argtypes = [P, P, i32, P, P, i32]
+    L.cqpi_graph_begin.argtypes = [P]
+    L.cqpi_graph_end.argtypes = [P]
+    L.cqpi_graph_launch.argtypes = [P]
     L.cqpi_adjoint.argtypes = [P, P, i32, P, i32, P, P]
     _lib = L
     return L
@@ -216,6 +221,23 @@ class Engine:
             rc = self._L.cqpi_adjoint(self._h, _ptr(e), len(e), _ptr(w), 0, _ptr(gt), _ptr(gv))
         self._check(rc)
         return gt.view(np.complex128), gv.view(np.complex128).reshape(self.nimp, self.bands, self.bands)
+
+    def run_fov(self, energies, fov, ptr32):
+        """Asynchronous batched run with a field of view per (energy, impurity) map into a
+        device buffer (packed maps, see cqpi_run_fov)."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        self._fov = np.ascontiguousarray(fov, np.int32).reshape(-1)
+        assert len(self._fov) == len(e) * self.nimp
+        self._check(self._L.cqpi_run_fov(self._h, _ptr(e), len(e), _ptr(self._fov), ptr32, 1))
+
+    def graph_begin(self):
+        self._check(self._L.cqpi_graph_begin(self._h))
+
+    def graph_end(self):
+        self._check(self._L.cqpi_graph_end(self._h))
+
+    def graph_launch(self):
+        self._check(self._L.cqpi_graph_launch(self._h))
 
     # -- narrow seam
     def wannierldos(self, T, g0r):

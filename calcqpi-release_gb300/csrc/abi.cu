@@ -179,6 +179,7 @@ int read_status(cqpi_handle *h)
 // ---- asynchronous timing: pooled events and pending (stage, start, end) triples
 int record(cqpi_handle *h)
 {
+    if (h->capturing) return -1;   // no timing events inside a captured graph
     int idx;
     if (!h->ev_free.empty()) {
         const cudaEvent_t e = h->ev_free.back();
@@ -196,6 +197,7 @@ int record(cqpi_handle *h)
 
 void pend(cqpi_handle *h, int stage, int a, int b)
 {
+    if (a < 0 || b < 0) return;
     h->ev_pending.push_back(stage);
     h->ev_pending.push_back(a);
     h->ev_pending.push_back(b);
@@ -204,6 +206,7 @@ void pend(cqpi_handle *h, int stage, int a, int b)
 // Sum the pending stage intervals into stage_ms (totals since the previous query).
 void collect_times(cqpi_handle *h)
 {
+    if (h->capturing) return;
     for (int i = 0; i < 5; i++) h->stage_ms[i] = 0.f;
     if (!h->ev_pool.empty()) CK(cudaEventSynchronize(h->ev_pool.back()));
     for (size_t i = 0; i + 2 < h->ev_pending.size(); i += 3) {
@@ -227,6 +230,23 @@ void ensure_energies(cqpi_handle *h, int n)
     dalloc(&h->d_energies_all, (size_t)n);
     CK(cudaMallocHost((void **)&h->h_energies_pinned, sizeof(double) * n));
     h->energies_cap = n;
+}
+
+void ensure_fov(cqpi_handle *h, size_t n)
+{
+    if (h->fov_cap >= n) return;
+    dfree(h->d_fov);
+    dfree(h->d_fov_off);
+    if (h->h_fov_pinned) cudaFreeHost(h->h_fov_pinned);
+    if (h->h_off_pinned) cudaFreeHost(h->h_off_pinned);
+    h->h_fov_pinned = nullptr;
+    h->h_off_pinned = nullptr;
+    h->fov_cap = 0;
+    dalloc(&h->d_fov, n);
+    dalloc(&h->d_fov_off, n);
+    CK(cudaMallocHost((void **)&h->h_fov_pinned, sizeof(int) * n));
+    CK(cudaMallocHost((void **)&h->h_off_pinned, sizeof(long long) * n));
+    h->fov_cap = n;
 }
 
 void ensure_stage32(cqpi_handle *h, size_t n)
@@ -468,6 +488,12 @@ int cqpi_destroy(cqpi_handle *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_workspace(h);
     free_adj(h);
+    dfree(h->d_fov);
+    dfree(h->d_fov_off);
+    if (h->h_fov_pinned) cudaFreeHost(h->h_fov_pinned);
+    if (h->h_off_pinned) cudaFreeHost(h->h_off_pinned);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
     dfree(h->d_R);
     dfree(h->d_tn);
     dfree(h->d_ta);
@@ -605,6 +631,8 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
     const size_t per_e = (size_t)h->nimp * mapn;
     try {
         const int eb = choose_batch(h, nE);
+        if (h->capturing && (h->ws.ebatch < eb || h->energies_cap < nE || !on_device || !h->bands_ready))
+            return fail(h, CQPI_ERR_STATE, "capture needs device outputs, solved bands and buffers of an earlier identical call");
         ensure_workspace(h, eb);
         ensure_energies(h, nE);
         if (h->ev_pool.size() > 2048) collect_times(h);   // bounded event pool when nobody queries
@@ -662,6 +690,117 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
+    return CQPI_OK;
+}
+
+int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32_t *fov, float *maps, int32_t on_device)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (nE < 0 || (nE > 0 && (!energies || !fov || !maps))) return fail(h, CQPI_ERR_ARG, "invalid energies, fields of view or maps");
+    if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    if (!on_device) return fail(h, CQPI_ERR_NOT_SUPPORTED, "cqpi_run_fov writes device memory (on_device = 1)");
+    if (!tc_window_usable(h))
+        return fail(h, CQPI_ERR_NOT_SUPPORTED, "per-map fields of view need the mixed-precision direct-window contraction");
+    if (nE == 0) return CQPI_OK;
+    const size_t nmap = (size_t)nE * h->nimp;
+    for (size_t k = 0; k < nmap; k++)
+        if (fov[k] < 1 || fov[k] > h->n) return fail(h, CQPI_ERR_ARG, "field of view outside 1..lattice");
+    try {
+        const int eb = choose_batch(h, nE);
+        if (h->capturing && (h->ws.ebatch < eb || h->energies_cap < nE || h->fov_cap < nmap))
+            return fail(h, CQPI_ERR_STATE, "buffers must be allocated before capture: run the same call once first");
+        ensure_workspace(h, eb);
+        ensure_energies(h, nE);
+        ensure_fov(h, nmap);
+        long long off = 0;
+        for (size_t k = 0; k < nmap; k++) {
+            h->h_fov_pinned[k] = fov[k];
+            h->h_off_pinned[k] = off;
+            off += (long long)fov[k] * h->os * fov[k] * h->os;
+        }
+        memcpy(h->h_energies_pinned, energies, sizeof(double) * nE);
+        CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * nE, cudaMemcpyHostToDevice,
+                           h->stream));
+        CK(cudaMemcpyAsync(h->d_fov, h->h_fov_pinned, sizeof(int) * nmap, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_fov_off, h->h_off_pinned, sizeof(long long) * nmap, cudaMemcpyHostToDevice, h->stream));
+        if (!h->bands_ready) {
+            if (h->capturing) return fail(h, CQPI_ERR_STATE, "solve the bands before capture");
+            const int a = record(h);
+            do_bands(h);
+            pend(h, 0, a, record(h));
+        }
+        for (int e0 = 0; e0 < nE; e0 += eb) {
+            const int ne = std::min(eb, nE - e0);
+            const double *den = h->d_energies_all + e0;
+            if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
+            const int t0 = record(h);
+            do_greens(h, ne, den);
+            const int t1 = record(h);
+            launch_tmatrix(h, ne);
+            check_launch();
+            launch_term1(h, ne);
+            check_launch();
+            const int t2 = record(h);
+            CK(launch_ldos_tc(h, ne, maps, h->d_fov + (size_t)e0 * h->nimp, h->d_fov_off + (size_t)e0 * h->nimp));
+            const int t3 = record(h);
+            pend(h, 1, t0, t1);
+            pend(h, 2, t1, t2);
+            pend(h, 3, t2, t3);
+        }
+        h->status_pending = true;
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_graph_begin(cqpi_handle *h)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "capture already active");
+    try {
+        collect_times(h);
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    h->capturing = true;
+    h->graph_kernels = h->launches;
+    return CQPI_OK;
+}
+
+int cqpi_graph_end(cqpi_handle *h)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (!h->capturing) return fail(h, CQPI_ERR_STATE, "no capture active");
+    h->capturing = false;
+    h->graph_kernels = h->launches - h->graph_kernels;   // kernels per replay
+    h->launches -= h->graph_kernels;                      // captured, not yet run
+    try {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamEndCapture(h->stream, &g));
+        if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+        if (h->graph) cudaGraphDestroy(h->graph);
+        h->graph = g;
+        h->graph_exec = nullptr;
+        CK(cudaGraphInstantiate(&h->graph_exec, g, 0));
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_graph_launch(cqpi_handle *h)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (!h->graph_exec) return fail(h, CQPI_ERR_STATE, "no captured graph");
+    try {
+        CK(cudaGraphLaunch(h->graph_exec, h->stream));
+        h->launches += h->graph_kernels;
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    h->status_pending = true;
     return CQPI_OK;
 }
 

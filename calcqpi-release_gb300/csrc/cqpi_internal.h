@@ -69,6 +69,8 @@ struct TcParams {
     const unsigned *gmax;
     const uint4 *Aimg;
     float *out;
+    const int *fov;              // direct-window variant: per-map field of view (sites per side) or NULL
+    const long long *fov_off;    // and the float offset of every map in out
     int *status;
 };
 
@@ -146,6 +148,17 @@ struct cqpi_handle {
     cqpi::Workspace ws;
     cqpi::AdjWorkspace adj;
     int *d_status = nullptr;
+    // per-map fields of view (cqpi_run_fov): device copies and page-locked staging
+    int *d_fov = nullptr;
+    long long *d_fov_off = nullptr;
+    int *h_fov_pinned = nullptr;
+    long long *h_off_pinned = nullptr;
+    size_t fov_cap = 0;
+    // CUDA graph capture of the handle's stream (cqpi_graph_begin / end / launch)
+    bool capturing = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int64_t graph_kernels = 0;   // kernels of one replay
     // model hopping terms as given to cqpi_create (for cqpi_set_hoppings / cqpi_adjoint):
     // unique-R index, orbital pair and conjugation flag of every term
     std::vector<int> hop_r, hop_o1, hop_o2, hop_anti;
@@ -201,7 +214,9 @@ void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vect
 void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorkspace &aw);
 void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw);
 void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
-cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out);
+cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out, const int *fov = nullptr,
+                           const long long *fov_off = nullptr);
+bool tc_window_usable(const cqpi_handle *h);   // the direct-window kernel runs (per-map FOV support)
 void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n);
 
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }

@@ -1121,7 +1121,21 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                         for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
                     }
                     // pixel (qx, qy) of sites i0+s0 .. i0+s0+3 of row j, straight to the map
-                    if (qvalid) {
+                    if (qvalid && p.fov) {
+                        // map (e, imp) covers the centred fov x fov sites of the full field
+                        const int mi = e * p.nimp + imp;
+                        const int fv = p.fov[mi], f2 = fv >> 1;
+                        const int jm = j - n2 + f2;
+                        if (jm >= 0 && jm < fv) {
+                            const size_t wm = (size_t)fv * p.os;
+                            float *dst = p.out + p.fov_off[mi] + ((size_t)jm * p.os + qy) * wm + qx;
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                const int im = i0 + s0 + u - n2 + f2;
+                                if (im >= 0 && im < fv) dst[(size_t)im * p.os] = -t1 - term2[u] * inv2;
+                            }
+                        }
+                    } else if (qvalid) {
                         float *dst = p.out + ((((size_t)e * p.nimp + imp) * p.wn + (size_t)j * p.os + qy) * p.wn +
                                               (size_t)(i0 + s0) * p.os + qx);
                         const int xrem = p.wn - (i0 + s0) * p.os - qx;   // columns left in this map row
@@ -1322,7 +1336,7 @@ void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint
 }
 
 template <int B>
-static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
+static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fov, const long long *fov_off)
 {
     const TcPlan &pl = h->tc;
     TcParams p = {};
@@ -1336,6 +1350,8 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     p.box = h->ws.box32; p.T32 = h->ws.T32; p.term1 = h->ws.term1; p.gmax = h->ws.gmax;
     p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
     p.out = out;
+    p.fov = fov;
+    p.fov_off = fov_off;
     p.status = h->d_status;
     const char *force = getenv("CQPI_TC_PIPE");
     const bool pipe = pl.pipe && !(force && !strcmp(force, "0"));
@@ -1345,6 +1361,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     const bool win = pl.win && win_fits && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0"));
     const long long ntiles = (long long)ne * h->n * p.ntx;
     cudaError_t err;
+    if (fov && !win) return cudaErrorInvalidValue;   // per-map fields of view need the window kernel
     if (win) {
         p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB; p.nraw = pl.wNRAW;
         p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
@@ -1383,18 +1400,26 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out)
     return cudaGetLastError();
 }
 
-cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out)
+cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out, const int *fov, const long long *fov_off)
 {
     const int b = h->b;
-    if (b <= 1) return launch_tc_t<1>(h, ne, out);
-    if (b <= 2) return launch_tc_t<2>(h, ne, out);
-    if (b <= 3) return launch_tc_t<3>(h, ne, out);
-    if (b <= 4) return launch_tc_t<4>(h, ne, out);
-    if (b <= 6) return launch_tc_t<6>(h, ne, out);
-    if (b <= 8) return launch_tc_t<8>(h, ne, out);
-    if (b <= 10) return launch_tc_t<10>(h, ne, out);
-    if (b <= 12) return launch_tc_t<12>(h, ne, out);
-    return launch_tc_t<16>(h, ne, out);
+    if (b <= 1) return launch_tc_t<1>(h, ne, out, fov, fov_off);
+    if (b <= 2) return launch_tc_t<2>(h, ne, out, fov, fov_off);
+    if (b <= 3) return launch_tc_t<3>(h, ne, out, fov, fov_off);
+    if (b <= 4) return launch_tc_t<4>(h, ne, out, fov, fov_off);
+    if (b <= 6) return launch_tc_t<6>(h, ne, out, fov, fov_off);
+    if (b <= 8) return launch_tc_t<8>(h, ne, out, fov, fov_off);
+    if (b <= 10) return launch_tc_t<10>(h, ne, out, fov, fov_off);
+    if (b <= 12) return launch_tc_t<12>(h, ne, out, fov, fov_off);
+    return launch_tc_t<16>(h, ne, out, fov, fov_off);
+}
+
+bool tc_window_usable(const cqpi_handle *h)
+{
+    const char *force = getenv("CQPI_TC_PIPE");
+    const char *fw = getenv("CQPI_TC_WINDOW");
+    return h->use_tc && h->tc.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0")) &&
+           h->tc.w_smem + 8 * (size_t)h->tc.wEB * h->nimp * h->b * h->b <= 227 * 1024;
 }
 
 }  // namespace cqpi

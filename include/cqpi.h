@@ -111,6 +111,20 @@ int cqpi_solve_bands(cqpi_handle *h);
  * are filled. */
 int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, double *maps64, int32_t on_device);
 
+/* Batched maps with a field of view per map (extension: the reference has one field of
+ * view per run).  fov[nE][nimp]: sites per side of map (energy, impurity), 1..lattice,
+ * centred like the full field (a crop of cqpi_run's map); maps: device memory, maps
+ * packed in (energy, impurity) order, map k (fov f) is (f*oversamp)^2 floats, rows of
+ * f*oversamp, starting after the maps before it.  Asynchronous (on_device must be 1);
+ * needs the mixed-precision tensor-core contraction, else CQPI_ERR_NOT_SUPPORTED. */
+int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32_t *fov, float *maps, int32_t on_device);
+/* CUDA graph of the handle's stream: begin / end capture around on-device calls
+ * (cqpi_run / cqpi_run_fov with on_device = 1, after one identical un-captured call so
+ * that every buffer exists), then launch the captured batch as one graph. */
+int cqpi_graph_begin(cqpi_handle *h);
+int cqpi_graph_end(cqpi_handle *h);
+int cqpi_graph_launch(cqpi_handle *h);
+
 /* ---- differentiation (extension: the reference computes no derivatives) -----
  * New hopping amplitudes for the terms of the model given to cqpi_create (same order,
  * same R / orbitals / conjugation flags): t[nhops][2].  The eigen cache is rebuilt by

@@ -1,0 +1,88 @@
+"""GPU: batched maps with a field of view per map (cqpi_run_fov) and CUDA-graph replay.
+
+A map of field of view f is the centred f x f-site crop of the full-field map (the LDOS at a
+site does not depend on how many sites are computed), so the batched maps must equal the
+crops of cqpi_run's maps exactly.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(lattice=24, kp=64, os_=5, w=2, nimp=3, seed=4):
+    import cqpi
+    from cqpi import workloads as W
+    m = W.t2g_c2()
+    eng = cqpi.Engine(m, lattice, kp, os_, w, 0.01, precision=cqpi.PREC_MIXED)
+    eng.set_orbitals(W.t2g_orbitals_c2(w, os_))
+    rng = np.random.default_rng(seed)
+    Vs = []
+    for k in range(nimp):
+        if k % 2 == 0:
+            Vs.append(rng.uniform(-1, 1) * np.eye(3))
+        else:
+            A = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+            Vs.append(0.2 * (A + A.conj().T))
+    eng.set_impurities(np.stack(Vs))
+    return eng
+
+
+def _crops(full, fov, os_, lattice):
+    n2 = lattice >> 1
+    out = []
+    nE, nimp = full.shape[:2]
+    for e in range(nE):
+        for i in range(nimp):
+            f = fov[e * nimp + i]
+            s0 = (n2 - (f >> 1)) * os_
+            out.append(full[e, i, s0:s0 + f * os_, s0:s0 + f * os_].ravel())
+    return np.concatenate(out)
+
+
+def test_run_fov_maps_are_crops_of_full_maps(built_lib):
+    torch = pytest.importorskip("torch")
+    eng = _engine()
+    if eng.contraction_kind() != "tcgen05":
+        pytest.skip("tensor-core contraction not selected")
+    E = np.array([-0.05, -0.01, 0.02, 0.06, 0.08])
+    rng = np.random.default_rng(1)
+    fov = rng.choice([5, 8, 12, 17, 24], size=len(E) * eng.nimp).astype(np.int32)
+    full = eng.run(E)
+    total = int(np.sum((fov * eng.oversamp) ** 2))
+    buf = torch.full((total,), float("nan"), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    eng.run_fov(E, fov, buf.data_ptr())
+    eng.synchronize()
+    got = buf.cpu().numpy()
+    ref = _crops(full, fov, eng.oversamp, eng.lattice)
+    assert np.array_equal(got, ref)
+    eng.close()
+
+
+def test_graph_replay_matches_direct_calls(built_lib):
+    torch = pytest.importorskip("torch")
+    eng = _engine()
+    if eng.contraction_kind() != "tcgen05":
+        pytest.skip("tensor-core contraction not selected")
+    E = np.linspace(-0.08, 0.08, 7)
+    fov = np.full(len(E) * eng.nimp, 16, np.int32)
+    fov[::2] = 9
+    total = int(np.sum((fov * eng.oversamp) ** 2))
+    direct = torch.empty((total,), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    eng.solve_bands()
+    eng.run_fov(E, fov, direct.data_ptr())        # allocates every buffer
+    eng.synchronize()
+    graphed = torch.zeros((total,), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    eng.graph_begin()
+    eng.run_fov(E, fov, graphed.data_ptr())
+    eng.graph_end()
+    n0 = eng.kernel_launches()
+    for _ in range(2):
+        eng.graph_launch()
+    eng.synchronize()
+    assert eng.kernel_launches() > n0
+    assert torch.equal(direct, graphed)
+    eng.close()
