@@ -192,7 +192,11 @@ def run_ours(args):
 
     prec = cqpi.PREC_MIXED if args.precision == "mixed" else cqpi.PREC_FP64
     c, m, wf = W.config(args.config)
+    if args.fov:                 # reduced field of view (profiling captures); the headline uses the config's
+        c.lattice = args.fov
     E = c.energy_list()
+    if args.energies:
+        E = np.linspace(E[0], E[-1], args.energies)
     nE = len(E)
     vscat = np.array(c.scattering, complex)
     if len(vscat) < m.bands:
@@ -285,6 +289,13 @@ def run_ours(args):
     roof["kernel"] = "ldos contraction"
     roof["flop_per_pixel_energy"] = F
     roof["traffic"] = None
+    if (args.config == "C2" and not args.fov and not args.energies and prec != cqpi.PREC_FP64
+            and eng.contraction_kind() == "tcgen05"):
+        # dram__bytes_read.sum + dram__bytes_write.sum of one contraction launch (32 energies
+        # of this workload), one ncu capture: profiles/launches_c2_mixed.md
+        roof["traffic"] = 157.8e6 + 781.1e6
+        roof["traffic_note"] = ("bytes per contraction launch of 32 energies (ncu); algorithmic: 32 G0(R) boxes "
+                                "(157 MB) + 32 maps (839 MB)")
     roof["stage_ms_per_step"] = {k: v / args.steps for k, v in stage_acc.items()}
 
     # accuracy and speed of the all-FP64 path on the same workload (the metric's comparison)
@@ -473,6 +484,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--fov", type=int, default=0, help="override the field of view (sites per side) for small captures")
+    ap.add_argument("--energies", type=int, default=0, help="override the number of energies for small captures")
     ap.add_argument("--adjoint-steps", type=int, default=3,
                     help="Adam iterations of the C5 differentiation workload timed for 'adjoint grad s/it' (0: skip)")
     args = ap.parse_args()

@@ -15,7 +15,7 @@ import numpy as np
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "_build", "libcqpi.so")
 
-OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_DOMAIN, ERR_SINGULAR, ERR_STATE, ERR_NOT_SUPPORTED, ERR_NO_DEVICE = range(9)
+OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_DOMAIN, ERR_SINGULAR, ERR_STATE, ERR_NOT_SUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(10)
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [

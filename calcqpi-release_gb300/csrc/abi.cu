@@ -163,6 +163,15 @@ void check_launch()
     CK(cudaGetLastError());
 }
 
+// Device status word: bit 0 (1) a singular 1 - V G0(0), bit 1 (2) a bounded device wait
+// that ran out (the kernel stopped early; its maps are incomplete).
+int status_code(cqpi_handle *h, int st, const char *what)
+{
+    if (st & 2) return fail(h, CQPI_ERR_TIMEOUT, std::string("a device wait timed out in ") + what);
+    if (st & 1) return fail(h, CQPI_ERR_SINGULAR, std::string("1 - V G0(0) is singular at an energy of ") + what);
+    return CQPI_OK;
+}
+
 int read_status(cqpi_handle *h)
 {
     int st = 0;
@@ -306,6 +315,7 @@ const char *cqpi_status_string(int s)
     case CQPI_ERR_STATE: return "call order violated";
     case CQPI_ERR_NOT_SUPPORTED: return "not supported";
     case CQPI_ERR_NO_DEVICE: return "no CUDA device";
+    case CQPI_ERR_TIMEOUT: return "a bounded device wait timed out";
     }
     return "unknown status";
 }
@@ -685,7 +695,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
         if (!on_device) {
             CK(cudaStreamSynchronize(h->stream));
             h->status_pending = false;
-            if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
+            if (const int st = read_status(h)) return status_code(h, st, "the batch");
         }
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
@@ -890,7 +900,7 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
         CK(cudaMemcpyAsync(gR.data(), h->adj.gR, sizeof(double2) * gR.size(), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaMemcpyAsync(gV.data(), h->adj.gV, sizeof(double2) * gV.size(), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
-        if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of the batch");
+        if (const int st = read_status(h)) return status_code(h, st, "the batch");
         if (dL_dt)
             for (int i = 0; i < nhops; i++) {
                 const double2 g = gR[((size_t)h->hop_r[i] * 2 + h->hop_anti[i]) * bb + (size_t)h->hop_o1[i] * h->b + h->hop_o2[i]];
@@ -975,7 +985,7 @@ int cqpi_get_tmatrix(cqpi_handle *h, double energy, double *T)
         check_launch();
         CK(cudaMemcpyAsync(T, h->ws.T, sizeof(double2) * h->b * h->b, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
-        if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular");
+        if (const int st = read_status(h)) return status_code(h, st, "the call");
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
@@ -1048,7 +1058,7 @@ int cqpi_synchronize(cqpi_handle *h)
     if (h->status_pending) {
         h->status_pending = false;
         try {
-            if (read_status(h)) return fail(h, CQPI_ERR_SINGULAR, "1 - V G0(0) is singular at an energy of a run");
+            if (const int st = read_status(h)) return status_code(h, st, "a run");
         } catch (const CudaError &ce) {
             return cuda_fail(h, ce);
         }

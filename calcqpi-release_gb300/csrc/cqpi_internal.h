@@ -61,6 +61,7 @@ struct TcParams {
     int tmem_cols, a_bytes, b_bytes;
     int H, NX, NKC, win_bytes, EB, nraw;   // direct-window variant
     int a_tmem;                  // direct-window variant: Phi operand held in tensor memory
+    int stall;                   // fault injection: wait on a barrier nothing arrives on
     float inv_sA;
     long long spin_limit;
     const float2 *box;

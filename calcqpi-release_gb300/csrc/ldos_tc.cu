@@ -786,7 +786,8 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     const size_t mb_off = ct_off + 8 * (size_t)(2 * EB * NX);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + mb_off);   // [8]
     uint64_t *win_full = mbar, *win_empty = mbar + 2, *acc_full = mbar + 4, *acc_empty = mbar + 6;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 8);
+    uint64_t *never = mbar + 8;    // fault injection: a barrier nothing arrives on
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 9);
     constexpr int NW = TCW_EPI + TCW_PROD;
 
     if (tid < NW) {
@@ -810,7 +811,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         if (tid < 4) raw[zslot + tid] = 0.f;
     }
     if (tid == NW) {
-        for (int i = 0; i < 8; i++) mbar_init(smem_u32(&mbar[i]), 1);
+        for (int i = 0; i < 9; i++) mbar_init(smem_u32(&mbar[i]), 1);
         fence_mbar_init();
     }
     if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
@@ -862,8 +863,10 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         const uint64_t aH = sdesc(smem_u32(smA), 128, sbo_a), aL = sdesc(smem_u32(smA + p.a_bytes), 128, sbo_a);
         const uint32_t lbo_b = (uint32_t)(nplanes * NX * 16), sbo_b = (uint32_t)(NX * 16);
         int issued = 0;
-        bool ok = true;
-        for (int it = 0;; it++) {
+        // fault injection (tests): wait on a barrier nothing arrives on; the bounded wait
+        // runs out and every role takes the time-out path
+        bool ok = !(p.stall && !mbar_wait(smem_u32(never), 0, p.spin_limit));
+        for (int it = 0; ok; it++) {
             int e0, j, i0;
             if (!tile_of(it, e0, j, i0)) break;
             const int s = it & 1;
@@ -1259,7 +1262,7 @@ void tc_plan(cqpi_handle *h)
                 auto smem_of = [&](int nraw) {
                     return 2 * (size_t)pl.w_a_bytes + 4 * (size_t)win_bytes + 4 * (nraw * 2 * EB * rawfl + 4) +
                            4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * (size_t)(2 * EB * NX) +
-                           8 * 8 + 16;
+                           9 * 8 + 16;
                 };
                 int nraw = 4;
                 while (nraw > 2 && smem_of(nraw) > 211 * 1024) nraw--;
@@ -1347,6 +1350,11 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
     p.tmem_cols = pl.tmem_cols; p.a_bytes = pl.a_bytes; p.b_bytes = pl.b_bytes;
     p.inv_sA = h->tc_inv_sA;
     p.spin_limit = 1LL << 21;   // try_wait attempts (each suspends at most 1 us)
+    // CQPI_TEST_STALL=1: the direct-window kernel waits on a barrier nothing arrives on,
+    // with a short limit, to exercise the time-out path (tests only)
+    const char *stall = getenv("CQPI_TEST_STALL");
+    p.stall = (stall && !strcmp(stall, "1")) ? 1 : 0;
+    if (p.stall) p.spin_limit = 256;
     p.box = h->ws.box32; p.T32 = h->ws.T32; p.term1 = h->ws.term1; p.gmax = h->ws.gmax;
     p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
     p.out = out;

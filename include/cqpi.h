@@ -43,6 +43,7 @@ extern "C" {
 #define CQPI_ERR_STATE 6        /* call order violated (e.g. no orbitals set) */
 #define CQPI_ERR_NOT_SUPPORTED 7
 #define CQPI_ERR_NO_DEVICE 8    /* no CUDA device visible */
+#define CQPI_ERR_TIMEOUT 9      /* a bounded device wait ran out; the kernel stopped early */
 
 #define CQPI_PREC_FP64 0        /* every stage in FP64 */
 #define CQPI_PREC_MIXED 1       /* FP64 eigen/T/k-sum fold, FP32/tensor-core contraction */

@@ -86,3 +86,24 @@ def test_graph_replay_matches_direct_calls(built_lib):
     assert eng.kernel_launches() > n0
     assert torch.equal(direct, graphed)
     eng.close()
+
+
+def test_device_wait_timeout_is_reported_and_handle_recovers(built_lib, monkeypatch):
+    """Fault injection without a GPU fault: with CQPI_TEST_STALL=1 the contraction waits
+    (bounded, ~0.3 ms) on a barrier nothing arrives on; every warp role takes the time-out
+    path, frees its tensor memory and returns, the call reports CQPI_ERR_TIMEOUT, and the
+    same handle then runs normally."""
+    import cqpi
+    eng = _engine()
+    if eng.contraction_kind() != "tcgen05":
+        pytest.skip("tensor-core contraction not selected")
+    E = np.array([-0.03, 0.01, 0.05])
+    good = eng.run(E)
+    monkeypatch.setenv("CQPI_TEST_STALL", "1")
+    with pytest.raises(cqpi.CqpiError) as ei:
+        eng.run(E)
+    assert ei.value.code == cqpi.ERR_TIMEOUT
+    monkeypatch.delenv("CQPI_TEST_STALL")
+    again = eng.run(E)
+    assert np.array_equal(again, good)
+    eng.close()
