@@ -276,6 +276,115 @@ void ensure_stage64(cqpi_handle *h, size_t n)
     h->stage_cap64 = n;
 }
 
+// ---- spin-degenerate reduction (see cqpi_handle::sr_*)
+bool spin_model_reducible(const cqpi_handle *h)
+{
+    if (!h->spin || h->nblk != 2 || h->b != 2 * h->mb || h->blk_start[1] != h->mb) return false;
+    const int b = h->b, mb = h->mb;
+    // diagonal: -efermi for p < scmax, +efermi otherwise; the two blocks must agree
+    for (int p = 0; p < mb; p++)
+        if ((p < h->scmax) != (p + mb < h->scmax)) return false;
+    const size_t bb = (size_t)b * b;
+    for (int r = 0; r < h->nR; r++)
+        for (int p = 0; p < b; p++)
+            for (int q = 0; q < b; q++) {
+                const size_t e = ((size_t)r * bb + (size_t)p * b + q) * 2;
+                const bool cross = (p < mb) != (q < mb);
+                for (int c = 0; c < 2; c++) {
+                    const double vn = h->rt_tn[e + c], va = h->rt_ta[e + c];
+                    if (cross) {
+                        if (vn != 0.0 || va != 0.0) return false;
+                    } else if (p < mb) {
+                        const size_t e2 = ((size_t)r * bb + (size_t)(p + mb) * b + (q + mb)) * 2;
+                        if (vn != h->rt_tn[e2 + c] || va != h->rt_ta[e2 + c]) return false;
+                    }
+                }
+            }
+    return true;
+}
+
+void sr_drop(cqpi_handle *h)
+{
+    if (h->sr_sub) cqpi_destroy(h->sr_sub);
+    h->sr_sub = nullptr;
+    h->sr_stale = true;
+}
+
+bool sr_active(const cqpi_handle *h)
+{
+    const char *f = getenv("CQPI_SPIN_REDUCE");
+    return h->sr_model && h->sr_orb && h->sr_v && !(f && !strcmp(f, "0"));
+}
+
+// Create (or re-create) the mb-band handle of the reduction; shares this handle's stream.
+int sr_prepare(cqpi_handle *h)
+{
+    if (h->sr_sub && !h->sr_stale) return CQPI_OK;
+    sr_drop(h);
+    const int b = h->b, mb = h->mb;
+    const size_t bb = (size_t)b * b;
+    std::vector<int32_t> R, orb;
+    std::vector<double> t;
+    std::vector<uint8_t> anti;
+    for (int r = 0; r < h->nR; r++)
+        for (int p = 0; p < mb; p++)
+            for (int q = 0; q < mb; q++)
+                for (int a = 0; a < 2; a++) {
+                    const std::vector<double> &src = a ? h->rt_ta : h->rt_tn;
+                    const size_t e = ((size_t)r * bb + (size_t)p * b + q) * 2;
+                    if (src[e] == 0.0 && src[e + 1] == 0.0) continue;
+                    R.push_back(h->rt_R[2 * r]);
+                    R.push_back(h->rt_R[2 * r + 1]);
+                    R.push_back(0);
+                    orb.push_back(p);
+                    orb.push_back(q);
+                    t.push_back(src[e]);
+                    t.push_back(src[e + 1]);
+                    anti.push_back((uint8_t)a);
+                }
+    cqpi_model m;
+    m.bands = mb;
+    m.scmaxbands = std::min(h->scmax, mb);
+    m.efermi = h->efermi;
+    m.nhops = (int64_t)t.size() / 2;
+    m.R = R.data();
+    m.orb = orb.data();
+    m.t = t.data();
+    m.anti = anti.data();
+    cqpi_params prm;
+    prm.lattice = h->n;
+    prm.kpoints = h->kp;
+    prm.oversamp = h->os;
+    prm.window = h->w;
+    prm.maxband = mb;
+    prm.spin = 0;
+    prm.eta = h->eta;
+    prm.precision = h->precision;
+    cqpi_handle *sub = nullptr;
+    int rc = cqpi_create(&m, &prm, &sub);
+    if (rc != CQPI_OK) return fail(h, rc, "spin-block reduction: internal handle");
+    cudaStreamDestroy(sub->stream);
+    sub->stream = h->stream;
+    sub->owns_stream = false;
+    sub->out_scale = 2.0f;    // two identical spin blocks
+    rc = cqpi_set_orbitals(sub, h->sr_wf.data(), mb, h->sr_side, h->sr_zero.data());
+    if (rc == CQPI_OK) rc = cqpi_set_impurities(sub, h->sr_V.data(), h->sr_nimp);
+    if (rc != CQPI_OK) {
+        h->err = sub->err;
+        cqpi_destroy(sub);
+        return rc;
+    }
+    h->sr_sub = sub;
+    h->sr_stale = false;
+    return CQPI_OK;
+}
+
+int sr_forward(cqpi_handle *h, int rc)
+{
+    if (rc != CQPI_OK && h->sr_sub) h->err = h->sr_sub->err;
+    return rc;
+}
+
 void do_bands(cqpi_handle *h)
 {
     launch_bands(h);
@@ -422,6 +531,7 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         h->nR = (int)idx.size();
         h->rt_tn = tn;
         h->rt_ta = ta;
+        h->rt_R = Rv;
         // real hoppings: H(-k) = conj(H(k)), the eigen-solve covers half the k-grid
         // (CQPI_TIME_REVERSAL=0 solves every k-point)
         {
@@ -470,9 +580,13 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         CK(configure_fft(h));
         // tensor-core contraction for the mixed path (CUDA-core FP32 kernel otherwise);
         // CQPI_CONTRACTION=fp32 selects the CUDA-core kernel explicitly
+        // fused G0(k) + row transform for up to 4 bands (all b^2 planes of a k-point are
+        // built from registers); more bands go through G0(k) planes in HBM and the separate
+        // transforms, which read the eigen cache once per energy instead of once per plane group
         if (h->precision == CQPI_PREC_MIXED && fft32_supported(h)) {
             const char *f = getenv("CQPI_GREENS");
-            h->use_fft32 = !(f && !strcmp(f, "unfused"));
+            h->use_fft32 = b <= 4 && !(f && !strcmp(f, "unfused"));
+            if (f && !strcmp(f, "fused")) h->use_fft32 = true;
             CK(configure_fft32(h));
         }
         if (h->precision == CQPI_PREC_MIXED && tc_supported(h)) {
@@ -480,6 +594,7 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
             const char *force = getenv("CQPI_CONTRACTION");
             h->use_tc = h->tc.ok && !(force && !strcmp(force, "fp32"));
         }
+        h->sr_model = spin_model_reducible(h);
     } catch (const CudaError &e) {
         int rc = cuda_fail(h, e);
         cqpi_destroy(h);
@@ -531,7 +646,8 @@ int cqpi_destroy(cqpi_handle *h)
     if (h->h_energies_pinned) cudaFreeHost(h->h_energies_pinned);
     dfree(h->stage32);
     dfree(h->stage64);
-    if (h->stream) cudaStreamDestroy(h->stream);
+    sr_drop(h);
+    if (h->stream && h->owns_stream) cudaStreamDestroy(h->stream);
     cudaGetLastError();
     delete h;
     return CQPI_OK;
@@ -584,6 +700,27 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
         return cuda_fail(h, e);
     }
     h->orbitals_ready = true;
+    // spin reduction: the two spin blocks carry the same orbitals
+    h->sr_orb = false;
+    if (h->spin && h->nblk == 2 && norb >= 2 * h->mb) {
+        const size_t n2 = (size_t)side * side;
+        bool same = true;
+        for (int o = 0; o < h->mb && same; o++) {
+            const bool z0 = is_zero && is_zero[o], z1 = is_zero && is_zero[o + h->mb];
+            same = z0 == z1 && (z0 || std::equal(wf + o * n2, wf + (o + 1) * n2, wf + (o + h->mb) * n2));
+        }
+        if (same) {
+            h->sr_orb = true;
+            h->sr_side = side;
+            h->sr_wf.assign(wf, wf + (size_t)h->mb * n2);
+            h->sr_zero.assign(h->mb, 0);
+            for (int o = 0; o < h->mb; o++) h->sr_zero[o] = (is_zero && is_zero[o]) ? 1 : 0;
+            if (h->sr_sub) {
+                const int rc = cqpi_set_orbitals(h->sr_sub, h->sr_wf.data(), h->mb, side, h->sr_zero.data());
+                if (rc != CQPI_OK) sr_drop(h);
+            }
+        }
+    }
     return CQPI_OK;
 }
 
@@ -603,6 +740,32 @@ int cqpi_set_impurities(cqpi_handle *h, const double *V, int32_t nimp)
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
+    // spin reduction: every V is block diagonal with two equal blocks
+    h->sr_v = false;
+    if (h->spin && h->nblk == 2 && h->b == 2 * h->mb) {
+        const int b = h->b, mb = h->mb;
+        bool ok = true;
+        std::vector<double> half((size_t)nimp * mb * mb * 2);
+        for (int i = 0; i < nimp && ok; i++)
+            for (int p = 0; p < b && ok; p++)
+                for (int q = 0; q < b && ok; q++) {
+                    const double *v = V + (((size_t)i * b + p) * b + q) * 2;
+                    if ((p < mb) != (q < mb)) {
+                        ok = v[0] == 0.0 && v[1] == 0.0;
+                    } else if (p < mb) {
+                        const double *v2 = V + (((size_t)i * b + p + mb) * b + q + mb) * 2;
+                        ok = v[0] == v2[0] && v[1] == v2[1];
+                        half[(((size_t)i * mb + p) * mb + q) * 2] = v[0];
+                        half[(((size_t)i * mb + p) * mb + q) * 2 + 1] = v[1];
+                    }
+                }
+        if (ok) {
+            h->sr_v = true;
+            h->sr_V.swap(half);
+            h->sr_nimp = nimp;
+            if (h->sr_sub && cqpi_set_impurities(h->sr_sub, h->sr_V.data(), nimp) != CQPI_OK) sr_drop(h);
+        }
+    }
     return CQPI_OK;
 }
 
@@ -621,6 +784,12 @@ int cqpi_set_scattering(cqpi_handle *h, const double *vscat)
 int cqpi_solve_bands(cqpi_handle *h)
 {
     if (!h) return CQPI_ERR_ARG;
+    if (sr_active(h)) {
+        const int rc = sr_prepare(h);
+        if (rc != CQPI_OK) return rc;
+        h->sr_sub->capturing = h->capturing;
+        return sr_forward(h, cqpi_solve_bands(h->sr_sub));
+    }
     try {
         const int a = record(h);
         do_bands(h);
@@ -634,6 +803,12 @@ int cqpi_solve_bands(cqpi_handle *h)
 int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, double *maps64, int32_t on_device)
 {
     if (!h) return CQPI_ERR_ARG;
+    if (sr_active(h) && h->orbitals_ready) {
+        const int rc = sr_prepare(h);
+        if (rc != CQPI_OK) return rc;
+        h->sr_sub->capturing = h->capturing;
+        return sr_forward(h, cqpi_run(h->sr_sub, energies, nE, maps32, maps64, on_device));
+    }
     if (nE < 0 || (nE > 0 && !energies)) return fail(h, CQPI_ERR_ARG, "invalid energy list");
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
     if (nE == 0) return CQPI_OK;
@@ -706,6 +881,12 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
 int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32_t *fov, float *maps, int32_t on_device)
 {
     if (!h) return CQPI_ERR_ARG;
+    if (sr_active(h) && h->orbitals_ready) {
+        const int rc = sr_prepare(h);
+        if (rc != CQPI_OK) return rc;
+        h->sr_sub->capturing = h->capturing;
+        return sr_forward(h, cqpi_run_fov(h->sr_sub, energies, nE, fov, maps, on_device));
+    }
     if (nE < 0 || (nE > 0 && (!energies || !fov || !maps))) return fail(h, CQPI_ERR_ARG, "invalid energies, fields of view or maps");
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
     if (!on_device) return fail(h, CQPI_ERR_NOT_SUPPORTED, "cqpi_run_fov writes device memory (on_device = 1)");
@@ -776,6 +957,7 @@ int cqpi_graph_begin(cqpi_handle *h)
     }
     h->capturing = true;
     h->graph_kernels = h->launches;
+    h->graph_kernels_sub = h->sr_sub ? h->sr_sub->launches : 0;
     return CQPI_OK;
 }
 
@@ -784,8 +966,15 @@ int cqpi_graph_end(cqpi_handle *h)
     if (!h) return CQPI_ERR_ARG;
     if (!h->capturing) return fail(h, CQPI_ERR_STATE, "no capture active");
     h->capturing = false;
+    int64_t sub_delta = 0;
+    if (h->sr_sub) {
+        h->sr_sub->capturing = false;
+        sub_delta = h->sr_sub->launches - h->graph_kernels_sub;
+        h->sr_sub->launches -= sub_delta;                 // captured, not yet run
+    }
     h->graph_kernels = h->launches - h->graph_kernels;   // kernels per replay
     h->launches -= h->graph_kernels;                      // captured, not yet run
+    h->graph_kernels += sub_delta;
     try {
         cudaGraph_t g = nullptr;
         CK(cudaStreamEndCapture(h->stream, &g));
@@ -842,6 +1031,8 @@ int cqpi_set_hoppings(cqpi_handle *h, const double *t)
     h->rt_ta.swap(ta);
     h->time_reversal = real && !(f && !strcmp(f, "0"));
     h->bands_ready = false;
+    h->sr_model = spin_model_reducible(h);
+    sr_drop(h);
     return CQPI_OK;
 }
 
@@ -1063,20 +1254,22 @@ int cqpi_synchronize(cqpi_handle *h)
             return cuda_fail(h, ce);
         }
     }
+    if (h->sr_sub) return sr_forward(h, cqpi_synchronize(h->sr_sub));
     return CQPI_OK;
 }
 
 int cqpi_kernel_launches(const cqpi_handle *h, int64_t *count)
 {
     if (!h || !count) return CQPI_ERR_ARG;
-    *count = h->launches;
+    *count = h->launches + (h->sr_sub ? h->sr_sub->launches : 0);
     return CQPI_OK;
 }
 
 int cqpi_contraction_kind(const cqpi_handle *h, int32_t *kind)
 {
     if (!h || !kind) return CQPI_ERR_ARG;
-    *kind = (h->precision == CQPI_PREC_FP64) ? 0 : (h->use_tc ? 2 : 1);
+    const cqpi_handle *k = (sr_active(h) && h->sr_sub) ? h->sr_sub : h;
+    *kind = (k->precision == CQPI_PREC_FP64) ? 0 : (k->use_tc ? 2 : 1);
     return CQPI_OK;
 }
 
@@ -1089,6 +1282,12 @@ int cqpi_stage_times(cqpi_handle *h, float *ms5)
         return cuda_fail(h, e);
     }
     for (int i = 0; i < 5; i++) ms5[i] = h->stage_ms[i];
+    if (h->sr_sub) {
+        float sub[5];
+        const int rc = cqpi_stage_times(h->sr_sub, sub);
+        if (rc != CQPI_OK) return sr_forward(h, rc);
+        for (int i = 0; i < 5; i++) ms5[i] += sub[i];
+    }
     return CQPI_OK;
 }
 

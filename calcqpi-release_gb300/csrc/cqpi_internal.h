@@ -63,6 +63,7 @@ struct TcParams {
     int a_tmem;                  // direct-window variant: Phi operand held in tensor memory
     int stall;                   // fault injection: wait on a barrier nothing arrives on
     float inv_sA;
+    float scale;                 // factor of every map value
     long long spin_limit;
     const float2 *box;
     const float2 *T32;
@@ -160,10 +161,23 @@ struct cqpi_handle {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int64_t graph_kernels = 0;   // kernels of one replay
+    int64_t graph_kernels_sub = 0;
     // model hopping terms as given to cqpi_create (for cqpi_set_hoppings / cqpi_adjoint):
     // unique-R index, orbital pair and conjugation flag of every term
     std::vector<int> hop_r, hop_o1, hop_o2, hop_anti;
     std::vector<double> rt_tn, rt_ta;   // host copies of the summed matrices [nR][b*b][2]
+    std::vector<int32_t> rt_R;          // [nR][2]
+    // spin-degenerate reduction: with spin blocks [0, mb) and [mb, 2mb) that do not couple
+    // (hoppings and V) and are identical (hoppings, diagonal, orbitals, V), G0 and T are
+    // block diagonal with equal blocks and every map is exactly twice the map of the mb-band
+    // problem, which an internal handle (sharing this stream) computes
+    bool sr_model = false, sr_orb = false, sr_v = false, sr_stale = true;
+    cqpi_handle *sr_sub = nullptr;
+    std::vector<double> sr_wf, sr_V;
+    std::vector<uint8_t> sr_zero;
+    int sr_side = 0, sr_nimp = 0;
+    bool owns_stream = true;
+    float out_scale = 1.0f;             // factor applied to every map value
     // narrow seam (always FP64)
     double *d_seam_ldos = nullptr;
     double2 *d_seam_box = nullptr, *d_seam_T = nullptr;

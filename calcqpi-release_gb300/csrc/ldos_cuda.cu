@@ -24,8 +24,8 @@ __global__ void __launch_bounds__(128) ldos_cuda_kernel(int b, int n, int os, in
                                                         int nblk, int mb, int bs0, int bs1,
                                                         const typename real_of<C>::type *__restrict__ phi,
                                                         const C *__restrict__ box, const C *__restrict__ T,
-                                                        const double *__restrict__ term1, float *__restrict__ out32,
-                                                        double *__restrict__ out64)
+                                                        const double *__restrict__ term1, double scale,
+                                                        float *__restrict__ out32, double *__restrict__ out64)
 {
     using Rl = typename real_of<C>::type;
     const int wn = n * os;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(128) ldos_cuda_kernel(int b, int n, int os, in
             }
         }
     }
-    const double rho = -term1[(size_t)e * Q + q] - (double)term2;
+    const double rho = (-term1[(size_t)e * Q + q] - (double)term2) * scale;
     const size_t oi = ((size_t)ei * wn + y) * wn + x;
     if (out64) out64[oi] = rho;
     if (out32) out32[oi] = (float)rho;
@@ -113,7 +113,7 @@ static void launch_t(cqpi_handle *h, int ne, const typename real_of<C>::type *ph
     dim3 grid(cdiv(h->wn, 32), cdiv(h->wn, 4), ne * h->nimp);
     ldos_cuda_kernel<B, C><<<grid, blk, 0, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp,
                                                         h->nblk, h->mb, h->blk_start[0], h->blk_start[1], phi, box, T,
-                                                        term1, o32, o64);
+                                                        term1, (double)h->out_scale, o32, o64);
     h->launches++;
 }
 

@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_kernel(const __grid_con
                 if (qvalid)
 #pragma unroll
                     for (int u = 0; u < 4; u++)
-                        stage[qy * sst + (s0 + u) * p.os + qx] = -t1 - term2[u] * inv2;
+                        stage[qy * sst + (s0 + u) * p.os + qx] = (-t1 - term2[u] * inv2) * p.scale;
             }
             __syncthreads();
             const int xbase = i0 * p.os;
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __gri
                 }
                 if (qvalid)
 #pragma unroll
-                    for (int u = 0; u < 4; u++) stage[qy * sst + (s0 + u) * p.os + qx] = -t1 - term2[u] * inv2;
+                    for (int u = 0; u < 4; u++) stage[qy * sst + (s0 + u) * p.os + qx] = (-t1 - term2[u] * inv2) * p.scale;
             }
             __syncthreads();
             const int xbase = i0 * p.os;
@@ -1135,7 +1135,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
 #pragma unroll
                             for (int u = 0; u < 4; u++) {
                                 const int im = i0 + s0 + u - n2 + f2;
-                                if (im >= 0 && im < fv) dst[(size_t)im * p.os] = -t1 - term2[u] * inv2;
+                                if (im >= 0 && im < fv) dst[(size_t)im * p.os] = (-t1 - term2[u] * inv2) * p.scale;
                             }
                         }
                     } else if (qvalid) {
@@ -1144,7 +1144,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                         const int xrem = p.wn - (i0 + s0) * p.os - qx;   // columns left in this map row
 #pragma unroll
                         for (int u = 0; u < 4; u++)
-                            if (u * p.os < xrem) dst[u * p.os] = -t1 - term2[u] * inv2;
+                            if (u * p.os < xrem) dst[u * p.os] = (-t1 - term2[u] * inv2) * p.scale;
                     }
                 }
             }
@@ -1358,6 +1358,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
     p.box = h->ws.box32; p.T32 = h->ws.T32; p.term1 = h->ws.term1; p.gmax = h->ws.gmax;
     p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
     p.out = out;
+    p.scale = h->out_scale;
     p.fov = fov;
     p.fov_off = fov_off;
     p.status = h->d_status;

@@ -201,3 +201,36 @@ def test_time_reversal_matches_full_solve(built_lib, name, monkeypatch):
     fullmx, _ = _run(name, cqpi.PREC_MIXED)
     assert np.abs(half64 - full64).max() <= 1e-12 * np.abs(full64).max()
     assert np.abs(halfmx - fullmx).max() <= 1e-6 * np.abs(fullmx).max()
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 1e-6)])
+def test_spin_block_reduction_matches_full_spin_path(built_lib, precision, tol, monkeypatch):
+    """Spin-degenerate model (decoupled, identical spin blocks; same orbitals and V per
+    block): the reduced run (twice the mb-band maps) equals the full 2mb-band spin run."""
+    import cqpi
+    red, _ = _run("c3", precision)
+    monkeypatch.setenv("CQPI_SPIN_REDUCE", "0")
+    full, _ = _run("c3", precision)
+    assert np.abs(red - full).max() <= tol * np.abs(full).max()
+
+
+def test_spin_block_reduction_only_for_identical_blocks(built_lib):
+    """A potential that differs between the spin blocks keeps the full spin path, whose maps
+    match the FP64 path and the oracle."""
+    import cqpi
+    from oracle import oracle as O
+    m, p, wf, z, v, E = case("c3")
+    v = np.asarray(v, complex).copy()
+    v[5:] *= 0.5                      # spin-dependent scattering
+    out = {}
+    for prec in (cqpi.PREC_FP64, cqpi.PREC_MIXED):
+        eng = cqpi.Engine(m, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"], spin=True,
+                          precision=prec)
+        eng.set_orbitals(wf, z)
+        eng.set_scattering(v)
+        out[prec] = eng.run(E, f32=False, f64=True)
+        eng.close()
+    om = O.Model(m.bands, m.R, m.orb, m.t, m.anti, m.efermi, m.scmaxbands)
+    orc = O.run(om, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"], E, v, wf, z, spin=True)
+    assert np.abs(out[cqpi.PREC_FP64][:, 0] - orc).max() <= 1e-10 * np.abs(orc).max()
+    assert np.abs(out[cqpi.PREC_MIXED][:, 0] - orc).max() <= TOL * np.abs(orc).max()
