@@ -258,6 +258,16 @@ void ensure_fov(cqpi_handle *h, size_t n)
     h->fov_cap = n;
 }
 
+void ensure_copy_stream(cqpi_handle *h)
+{
+    if (h->copy_stream) return;
+    CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++) {
+        CK(cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_copy[i], cudaEventDisableTiming));
+    }
+}
+
 void ensure_stage32(cqpi_handle *h, size_t n)
 {
     if (h->stage_cap32 >= n) return;
@@ -647,6 +657,13 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->stage32);
     dfree(h->stage64);
     sr_drop(h);
+    if (h->copy_stream) {
+        cudaStreamDestroy(h->copy_stream);
+        for (int i = 0; i < 2; i++) {
+            cudaEventDestroy(h->ev_comp[i]);
+            cudaEventDestroy(h->ev_copy[i]);
+        }
+    }
     if (h->stream && h->owns_stream) cudaStreamDestroy(h->stream);
     cudaGetLastError();
     delete h;
@@ -822,13 +839,14 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
         ensure_energies(h, nE);
         if (h->ev_pool.size() > 2048) collect_times(h);   // bounded event pool when nobody queries
         // host outputs (and float64-only requests on the tensor-core path) go through
-        // device staging buffers kept by the handle
-        float *tmp32 = nullptr;
-        if ((!on_device && maps32) || (h->use_tc && !maps32)) {
-            ensure_stage32(h, (size_t)eb * per_e);
-            tmp32 = h->stage32;
-        }
-        if (!on_device && maps64) ensure_stage64(h, (size_t)eb * per_e);
+        // device staging buffers kept by the handle; host outputs use two staging slots and
+        // a copy stream, so the copy of batch k overlaps the computation of batch k+1
+        const int nslot = on_device ? 1 : 2;
+        const size_t slot_n = (size_t)eb * per_e;
+        const bool need32 = (!on_device && maps32) || (h->use_tc && !maps32);
+        if (need32) ensure_stage32(h, nslot * slot_n);
+        if (!on_device && maps64) ensure_stage64(h, nslot * slot_n);
+        if (!on_device) ensure_copy_stream(h);
         memcpy(h->h_energies_pinned, energies, sizeof(double) * nE);
         CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * nE, cudaMemcpyHostToDevice,
                            h->stream));
@@ -837,9 +855,15 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             do_bands(h);
             pend(h, 0, a, record(h));
         }
-        for (int e0 = 0; e0 < nE; e0 += eb) {
+        for (int e0 = 0, bi = 0; e0 < nE; e0 += eb, bi++) {
             const int ne = std::min(eb, nE - e0);
+            const int slot = bi % nslot;
             const double *den = h->d_energies_all + e0;
+            float *s32 = need32 ? h->stage32 + slot * slot_n : nullptr;
+            double *s64 = (!on_device && maps64) ? h->stage64 + slot * slot_n : nullptr;
+            float *tmp32 = need32 ? s32 : nullptr;
+            // the slot's previous contents (batch bi - 2) must have reached the host
+            if (!on_device && bi >= 2) CK(cudaStreamWaitEvent(h->stream, h->ev_copy[slot], 0));
             if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
             const int t0 = record(h);
             do_greens(h, ne, den);
@@ -849,8 +873,8 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             launch_term1(h, ne);
             check_launch();
             const int t2 = record(h);
-            float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : h->stage32) : nullptr;
-            double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : h->stage64) : nullptr;
+            float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : s32) : nullptr;
+            double *o64 = maps64 ? (on_device ? maps64 + (size_t)e0 * per_e : s64) : nullptr;
             launch_contraction(h, ne, o32, o64, tmp32);
             check_launch();
             const int t3 = record(h);
@@ -858,16 +882,20 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             pend(h, 2, t1, t2);
             pend(h, 3, t2, t3);
             if (!on_device) {
+                CK(cudaEventRecord(h->ev_comp[slot], h->stream));
+                CK(cudaStreamWaitEvent(h->copy_stream, h->ev_comp[slot], 0));
                 if (maps32)
-                    CK(cudaMemcpyAsync(maps32 + (size_t)e0 * per_e, h->stage32, sizeof(float) * ne * per_e,
-                                       cudaMemcpyDeviceToHost, h->stream));
+                    CK(cudaMemcpyAsync(maps32 + (size_t)e0 * per_e, s32, sizeof(float) * ne * per_e,
+                                       cudaMemcpyDeviceToHost, h->copy_stream));
                 if (maps64)
-                    CK(cudaMemcpyAsync(maps64 + (size_t)e0 * per_e, h->stage64, sizeof(double) * ne * per_e,
-                                       cudaMemcpyDeviceToHost, h->stream));
+                    CK(cudaMemcpyAsync(maps64 + (size_t)e0 * per_e, s64, sizeof(double) * ne * per_e,
+                                       cudaMemcpyDeviceToHost, h->copy_stream));
+                CK(cudaEventRecord(h->ev_copy[slot], h->copy_stream));
             }
         }
         h->status_pending = true;
         if (!on_device) {
+            CK(cudaStreamSynchronize(h->copy_stream));
             CK(cudaStreamSynchronize(h->stream));
             h->status_pending = false;
             if (const int st = read_status(h)) return status_code(h, st, "the batch");

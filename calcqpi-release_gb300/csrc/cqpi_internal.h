@@ -195,6 +195,9 @@ struct cqpi_handle {
     int energies_cap = 0;
     float *stage32 = nullptr;
     double *stage64 = nullptr;
+    // host outputs: copy stream and per-slot events (computation done / copy done)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_comp[2] = {}, ev_copy[2] = {};
     size_t stage_cap32 = 0, stage_cap64 = 0;
     bool status_pending = false;
     std::string err;
