@@ -210,6 +210,14 @@ def run_ours(args):
 
     stage_acc = {"bands": 0.0, "greens": 0.0, "tmatrix": 0.0, "ldos": 0.0, "total": 0.0}
 
+    tune = None
+    if prec != cqpi.PREC_FP64 and eng.contraction_kind() == "tcgen05" and not args.no_autotune:
+        try:
+            ms_t, n_t = eng.autotune(E)
+            tune = {"shapes_timed": n_t, "batch_ms": ms_t}
+        except cqpi.CqpiError:
+            tune = None
+
     def step():
         eng.solve_bands()
         eng.run_device(E, ptr32=out.data_ptr())
@@ -331,6 +339,8 @@ def run_ours(args):
                        "l2": "inputs/outputs larger than L2 (2.6 GB of maps, 168 MB eigen cache per step)"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "roofline": roof}
+    if tune is not None:
+        line["config"]["autotune"] = tune
     if fp64_info is not None:
         line["accuracy"] = fp64_info
     if clk is not None:
@@ -392,6 +402,10 @@ def run_c4(args):
             eng.run_fov(E[e0:e0 + chunk], fov[e0 * nimp:(e0 + chunk) * nimp], buf.data_ptr())
 
     eng.solve_bands()
+    tune = None
+    if not args.no_autotune:
+        ms_t, n_t = eng.autotune(E[:32])
+        tune = {"shapes_timed": n_t, "batch_ms": ms_t}
     job()                                   # allocates every buffer
     eng.synchronize()
     eng.graph_begin()
@@ -436,6 +450,7 @@ def run_c4(args):
                                    "3x3), field of view per map from {64,128,256,384}^2 sites, 10x10 px/cell, one CUDA "
                                    "graph of cqpi_run_fov chunks (32 energies)",
                        "maps": int(len(fov)), "pixel_energies": pix, "mean_pixels_per_map": pix / len(fov),
+                       "autotune": tune,
                        "l2": "outputs far larger than L2"},
             "gpu_launches": int(launches),
             "latency_ms_per_map": {"p50": float(np.percentile(per_map, 50)), "p99": float(np.percentile(per_map, 99)),
@@ -484,6 +499,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the rule-based contraction tile shape")
     ap.add_argument("--fov", type=int, default=0, help="override the field of view (sites per side) for small captures")
     ap.add_argument("--energies", type=int, default=0, help="override the number of energies for small captures")
     ap.add_argument("--adjoint-steps", type=int, default=3,

@@ -24,7 +24,7 @@ EXPORTED = [
     "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
     "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
-    "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch",
+    "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune",
 ]
 
 
@@ -91,6 +91,7 @@ def load():
     L.cqpi_graph_begin.argtypes = [P]
     L.cqpi_graph_end.argtypes = [P]
     L.cqpi_graph_launch.argtypes = [P]
+    L.cqpi_autotune.argtypes = [P, P, i32, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(i32)]
     L.cqpi_adjoint.argtypes = [P, P, i32, P, i32, P, P]
     _lib = L
     return L
@@ -229,6 +230,15 @@ class Engine:
         self._fov = np.ascontiguousarray(fov, np.int32).reshape(-1)
         assert len(self._fov) == len(e) * self.nimp
         self._check(self._L.cqpi_run_fov(self._h, _ptr(e), len(e), _ptr(self._fov), ptr32, 1))
+
+    def autotune(self, energies):
+        """Time every valid contraction tile shape on the first energy batch and keep the
+        fastest; returns (ms per batch with the chosen shape, shapes timed)."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        ms = ctypes.c_float()
+        n = ctypes.c_int32()
+        self._check(self._L.cqpi_autotune(self._h, _ptr(e), len(e), ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
 
     def graph_begin(self):
         self._check(self._L.cqpi_graph_begin(self._h))

@@ -973,6 +973,45 @@ int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32
     return CQPI_OK;
 }
 
+int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *best_ms, int32_t *tried)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (nE < 1 || !energies) return fail(h, CQPI_ERR_ARG, "invalid energy list");
+    if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (sr_active(h)) {
+        const int rc = sr_prepare(h);
+        if (rc != CQPI_OK) return rc;
+        return sr_forward(h, cqpi_autotune(h->sr_sub, energies, nE, best_ms, tried));
+    }
+    if (!tc_window_usable(h)) return fail(h, CQPI_ERR_NOT_SUPPORTED, "autotuning covers the direct-window tensor-core contraction");
+    try {
+        const int ne = choose_batch(h, nE);
+        const size_t per_e = (size_t)h->nimp * h->wn * h->wn;
+        ensure_workspace(h, ne);
+        ensure_energies(h, nE);
+        ensure_stage32(h, (size_t)ne * per_e);
+        memcpy(h->h_energies_pinned, energies, sizeof(double) * ne);
+        CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * ne, cudaMemcpyHostToDevice,
+                           h->stream));
+        if (!h->bands_ready) do_bands(h);
+        if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
+        do_greens(h, ne, h->d_energies_all);
+        launch_tmatrix(h, ne);
+        launch_term1(h, ne);
+        check_launch();
+        float ms = 0.f;
+        int n = 0;
+        CK(tc_autotune(h, ne, h->stage32, &ms, &n));
+        if (best_ms) *best_ms = ms;
+        if (tried) *tried = n;
+        if (const int st = read_status(h)) return status_code(h, st, "autotuning");
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
 int cqpi_graph_begin(cqpi_handle *h)
 {
     if (!h) return CQPI_ERR_ARG;

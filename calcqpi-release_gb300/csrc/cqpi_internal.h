@@ -235,6 +235,8 @@ void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
 cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out, const int *fov = nullptr,
                            const long long *fov_off = nullptr);
 bool tc_window_usable(const cqpi_handle *h);   // the direct-window kernel runs (per-map FOV support)
+bool window_config(const cqpi_handle *h, int EB, int H, int nraw, TcPlan &pl);
+cudaError_t tc_autotune(cqpi_handle *h, int ne, float *out, float *best_ms, int *tried);
 void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n);
 
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }

@@ -1231,50 +1231,88 @@ void tc_plan(cqpi_handle *h)
     pl.pipe = pl.ok && h->nblk == 1 && 4 * pl.N <= 512 && pl.pipe_smem <= 227 * 1024;
 
     // direct-window variant: tiles of 8*H sites x EB energies; one MMA covers both operands
-    // and all EB energies of an 8-site group (N = 32*b*EB <= 256).  Two accumulator sets of
-    // H*N columns (+ Phi hi/lo when held in tensor memory) must fit the 512 TMEM columns.
-    // The MMA count per site-energy falls with EB only, so EB is maximised first, then H.
-    {
-        const int side = 2 * h->w + 1;
-        pl.wNKC = 2 * ((side * h->mb + 15) / 16);
-        pl.wKP = side * pl.wNKC * 8;
-        pl.w_a_bytes = 128 * pl.wKP * 2;
-        const size_t bbz = (size_t)h->b * h->b;
-        pl.win = false;
-        for (int EB = 4; EB >= 1 && !pl.win; EB--) {
-            const int N = 32 * h->b * EB;
-            if (N > 256) continue;
-            for (int H = 2; H >= 1 && !pl.win; H--) {
-                const int setcols = H * N;
-                if (2 * setcols > 512) continue;
-                const int NX = 8 * H + 2 * h->w;
-                const bool a_tmem = 2 * setcols + pl.wKP <= 512;
-                const int need = 2 * setcols + (a_tmem ? pl.wKP : 0);
-                int wc = 32;
-                while (wc < need) wc <<= 1;
-                const int win_bytes = pl.wNKC * 2 * EB * twob * NX * 16;
-                const int wwt = 8 * H * h->os;
-                const int sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
-                const size_t rawfl = (size_t)NX * side * bbz * 2;
-                // shared memory with Phi in shared memory (the larger of the two layouts); the
-                // per-impurity epilogue constants are added at launch.  The raw-window ring
-                // is as deep as fits (2..4), leaving 16 KiB for those constants.
-                auto smem_of = [&](int nraw) {
-                    return 2 * (size_t)pl.w_a_bytes + 4 * (size_t)win_bytes + 4 * (nraw * 2 * EB * rawfl + 4) +
-                           4 * (size_t)(2 * pl.wNKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * (size_t)(2 * EB * NX) +
-                           9 * 8 + 16;
-                };
-                int nraw = 4;
-                while (nraw > 2 && smem_of(nraw) > 211 * 1024) nraw--;
-                const size_t smem = smem_of(nraw);
-                if (smem > 227 * 1024) continue;
-                pl.wNRAW = nraw;
-                pl.wEB = EB; pl.wH = H; pl.wNX = NX; pl.w_win_bytes = win_bytes; pl.w_sst = sst;
-                pl.w_a_tmem = a_tmem; pl.w_tmem_cols = wc; pl.w_smem = smem;
-                pl.win = h->nblk == 1 && h->Q <= 128;
+    // and all EB energies of an 8-site group (N = 32*b*EB <= 256).  The MMA count per
+    // site-energy falls with EB only, so the default maximises EB, then H, with the deepest
+    // raw-window ring that fits; cqpi_autotune times every valid shape instead.
+    pl.win = false;
+    for (int EB = 4; EB >= 1 && !pl.win; EB--)
+        for (int H = 2; H >= 1 && !pl.win; H--)
+            for (int nraw = 4; nraw >= 2 && !pl.win; nraw--) window_config(h, EB, H, nraw, pl);
+}
+
+// Fill the direct-window fields of pl for EB energies x 8*H sites per tile and an nraw-deep
+// raw-window ring; false if the shape does not fit (N <= 256, two accumulator sets in the
+// 512 TMEM columns, shared memory with 16 KiB left for the per-impurity constants).
+bool window_config(const cqpi_handle *h, int EB, int H, int nraw, TcPlan &pl)
+{
+    if (h->nblk != 1 || h->Q > 128) return false;
+    const int twob = 2 * h->b, side = 2 * h->w + 1;
+    const int NKC = 2 * ((side * h->mb + 15) / 16);
+    const int KP = side * NKC * 8;
+    const int N = 32 * h->b * EB;
+    if (N > 256) return false;
+    const int setcols = H * N;
+    if (2 * setcols > 512) return false;
+    const int NX = 8 * H + 2 * h->w;
+    const bool a_tmem = 2 * setcols + KP <= 512;
+    const int need = 2 * setcols + (a_tmem ? KP : 0);
+    int wc = 32;
+    while (wc < need) wc <<= 1;
+    const int a_bytes = 128 * KP * 2;
+    const int win_bytes = NKC * 2 * EB * twob * NX * 16;
+    const int wwt = 8 * H * h->os;
+    const int sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
+    const size_t rawfl = (size_t)NX * side * h->b * h->b * 2;
+    // shared memory with Phi in shared memory (the larger of the two layouts); the
+    // per-impurity epilogue constants are added at launch
+    const size_t smem = 2 * (size_t)a_bytes + 4 * (size_t)win_bytes + 4 * (nraw * 2 * EB * rawfl + 4) +
+                        4 * (size_t)(2 * NKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * (size_t)(2 * EB * NX) + 9 * 8 + 16;
+    if (smem > 211 * 1024) return false;
+    pl.wNKC = NKC; pl.wKP = KP; pl.w_a_bytes = a_bytes;
+    pl.wNRAW = nraw; pl.wEB = EB; pl.wH = H; pl.wNX = NX; pl.w_win_bytes = win_bytes; pl.w_sst = sst;
+    pl.w_a_tmem = a_tmem; pl.w_tmem_cols = wc; pl.w_smem = smem;
+    pl.win = true;
+    return true;
+}
+
+// Time every valid direct-window shape on the current energy batch (workspace already holds
+// G0(R), T and term1 for ne energies) and keep the fastest.  out: ne*nimp maps of scratch.
+cudaError_t tc_autotune(cqpi_handle *h, int ne, float *out, float *best_ms, int *tried)
+{
+    TcPlan best = h->tc;
+    float best_t = -1.f;
+    int n = 0;
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err != cudaSuccess) return err;
+    err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) { cudaEventDestroy(e0); return err; }
+    const TcPlan base = h->tc;
+    for (int EB = 1; EB <= 4 && err == cudaSuccess; EB++)
+        for (int H = 1; H <= 4 && err == cudaSuccess; H *= 2)
+            for (int nraw = 2; nraw <= 4 && err == cudaSuccess; nraw++) {
+                TcPlan pl = base;
+                if (!window_config(h, EB, H, nraw, pl)) continue;
+                h->tc = pl;
+                if (!tc_window_usable(h)) continue;
+                err = launch_ldos_tc(h, ne, out);                 // warm-up
+                if (err != cudaSuccess) break;
+                err = cudaEventRecord(e0, h->stream);
+                for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_ldos_tc(h, ne, out);
+                if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+                if (err != cudaSuccess) break;
+                n++;
+                if (best_t < 0.f || ms < best_t) { best_t = ms; best = pl; }
             }
-        }
-    }
+    h->tc = (best_t >= 0.f) ? best : base;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_ms) *best_ms = best_t / 3.f;
+    if (tried) *tried = n;
+    return err;
 }
 
 // Phi hi/lo images for the direct-window variant: rows m = qy*os + qx, columns

@@ -119,6 +119,12 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
  * f*oversamp, starting after the maps before it.  Asynchronous (on_device must be 1);
  * needs the mixed-precision tensor-core contraction, else CQPI_ERR_NOT_SUPPORTED. */
 int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32_t *fov, float *maps, int32_t on_device);
+/* Tile-shape autotuner of the tensor-core contraction (extension): runs the Green's function
+ * stages for the first batch of the given energies, times every valid tile shape (energies per
+ * tile, sites per tile, raw-window ring depth) of the direct-window kernel on it and keeps the
+ * fastest for this handle.  best_ms / tried (may be NULL): time of one batch with the chosen
+ * shape, number of shapes timed. */
+int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *best_ms, int32_t *tried);
 /* CUDA graph of the handle's stream: begin / end capture around on-device calls
  * (cqpi_run / cqpi_run_fov with on_device = 1, after one identical un-captured call so
  * that every buffer exists), then launch the captured batch as one graph. */

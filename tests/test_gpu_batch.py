@@ -107,3 +107,18 @@ def test_device_wait_timeout_is_reported_and_handle_recovers(built_lib, monkeypa
     again = eng.run(E)
     assert np.array_equal(again, good)
     eng.close()
+
+
+def test_autotune_keeps_the_maps(built_lib):
+    """Tile shapes change the work split, not the arithmetic of a map value: after the
+    autotuner picks a shape the maps are identical to the default shape's."""
+    eng = _engine()
+    if eng.contraction_kind() != "tcgen05":
+        pytest.skip("tensor-core contraction not selected")
+    E = np.linspace(-0.06, 0.06, 9)
+    before = eng.run(E)
+    ms, n = eng.autotune(E)
+    assert n >= 1 and ms > 0
+    after = eng.run(E)
+    assert np.array_equal(before, after)
+    eng.close()
