@@ -339,6 +339,64 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
     }
 }
 
+// Pass 2 as a four-step register transform (kp = N1 x N2, box no wider than kp): a block
+// takes NC = 256/N1 adjacent columns yb of one (plane, energy), transforms along i with the
+// same two register passes as the row transform, scales by kp^-2 and writes the box rows
+// xb = (X + Rb) mod kp < NB, tracking max|G0| of the energy for the split scale.
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int bb, float scale,
+                                                         const float2 *__restrict__ half, const float2 *__restrict__ tw,
+                                                         float2 *__restrict__ box, unsigned *__restrict__ gmax)
+{
+    constexpr int KP = N1 * N2;
+    constexpr int NC = 256 / N1;
+    constexpr int PLEN = KP + KP / 32 + 1;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tws = sm + (size_t)NC * PLEN;
+    const int yb0 = blockIdx.x * NC, pl = blockIdx.y, e = blockIdx.z;
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
+    const float2 *src = half + ((size_t)e * bb + pl) * (size_t)KP * NB;
+    for (int idx = threadIdx.x; idx < KP * NC; idx += blockDim.x) {
+        const int i = idx / NC, c = idx - i * NC, yb = yb0 + c;
+        sm[(size_t)c * PLEN + pad32(i)] = yb < NB ? src[(size_t)i * NB + yb] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < NC * N1; task += blockDim.x) {
+        const int c = task / N1, n1 = task - c * N1;
+        float2 *a = sm + (size_t)c * PLEN;
+        float2 x[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
+        fft_reg<N2>(x);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[(n1 * k2) & (KP - 1)]);
+    }
+    __syncthreads();
+    float mx = 0.0f;
+    float2 *dst = box + (size_t)e * NB * NB * bb;
+    for (int task = threadIdx.x; task < NC * N2; task += blockDim.x) {
+        const int c = task / N2, k2 = task - c * N2, yb = yb0 + c;
+        const float2 *a = sm + (size_t)c * PLEN;
+        float2 x[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
+        fft_reg<N1>(x);
+        if (yb < NB) {
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) {
+                const int xb = (k2 + N2 * k1 + Rb) & (KP - 1);
+                if (xb < NB) {
+                    const float2 v = cscale(x[k1], scale);
+                    dst[((size_t)xb * NB + yb) * bb + pl] = v;
+                    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(gmax + e, __float_as_uint(mx));
+}
+
 // Pass 2: NC = 2^lnc adjacent columns (fixed plane, energy), transform along i.
 __global__ void __launch_bounds__(256) colfft_kernel(int kp, int logkp, int NB, int Rb, int bb, int lnc, float scale,
                                                      const float2 *__restrict__ half, const float2 *__restrict__ tw,
@@ -409,6 +467,8 @@ static int colfft_lnc(int kp)
 
 static bool rowfft_reg_ok(const cqpi_handle *h);
 static cudaError_t configure_rowfft_reg(cqpi_handle *h);
+static cudaError_t configure_colfft_reg(cqpi_handle *h);
+static void launch_colfft_reg(cqpi_handle *h, int ne);
 
 bool fft32_supported(const cqpi_handle *h) { return h->kp >= 2 && (h->kp & (h->kp - 1)) == 0 && h->kp <= 8192; }
 
@@ -426,7 +486,10 @@ cudaError_t configure_fft32(cqpi_handle *h)
 #undef CQPI_SETSMEM
     e = cudaFuncSetAttribute(colfft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
     if (e != cudaSuccess) return e;
-    return rowfft_reg_ok(h) ? configure_rowfft_reg(h) : cudaSuccess;
+    if (!rowfft_reg_ok(h)) return cudaSuccess;
+    e = configure_rowfft_reg(h);
+    if (e != cudaSuccess) return e;
+    return configure_colfft_reg(h);
 }
 
 template <int B>
@@ -498,6 +561,56 @@ static cudaError_t configure_rowfft_reg(cqpi_handle *h)
     return cudaSuccess;
 }
 
+template <int N1, int N2>
+static size_t colfft_reg_smem()
+{
+    return 8 * ((size_t)(256 / N1) * (N1 * N2 + (N1 * N2) / 32 + 1) + N1 * N2);
+}
+
+template <int N1, int N2>
+static cudaError_t configure_colfft_reg_t()
+{
+    return cudaFuncSetAttribute(colfft_reg_kernel<N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)colfft_reg_smem<N1, N2>());
+}
+
+template <int N1, int N2>
+static void launch_colfft_reg_t(cqpi_handle *h, int ne)
+{
+    constexpr int NC = 256 / N1;
+    dim3 grid(cdiv(h->NB, NC), h->b * h->b, ne);
+    colfft_reg_kernel<N1, N2><<<grid, 256, colfft_reg_smem<N1, N2>(), h->stream>>>(
+        h->NB, h->Rb, h->b * h->b, (float)(1.0 / ((double)h->kp * h->kp)), h->ws.half32, h->d_tw32, h->ws.box32,
+        h->ws.gmax);
+}
+
+static cudaError_t configure_colfft_reg(cqpi_handle *h)
+{
+    switch (h->kp) {
+    case 64: return configure_colfft_reg_t<8, 8>();
+    case 128: return configure_colfft_reg_t<8, 16>();
+    case 256: return configure_colfft_reg_t<16, 16>();
+    case 512: return configure_colfft_reg_t<16, 32>();
+    case 1024: return configure_colfft_reg_t<32, 32>();
+    case 2048: return configure_colfft_reg_t<32, 64>();
+    case 4096: return configure_colfft_reg_t<64, 64>();
+    }
+    return cudaSuccess;
+}
+
+static void launch_colfft_reg(cqpi_handle *h, int ne)
+{
+    switch (h->kp) {
+    case 64: launch_colfft_reg_t<8, 8>(h, ne); break;
+    case 128: launch_colfft_reg_t<8, 16>(h, ne); break;
+    case 256: launch_colfft_reg_t<16, 16>(h, ne); break;
+    case 512: launch_colfft_reg_t<16, 32>(h, ne); break;
+    case 1024: launch_colfft_reg_t<32, 32>(h, ne); break;
+    case 2048: launch_colfft_reg_t<32, 64>(h, ne); break;
+    case 4096: launch_colfft_reg_t<64, 64>(h, ne); break;
+    }
+}
+
 static void launch_rowfft_reg(cqpi_handle *h, int ne, const double *d_energies)
 {
     switch (h->kp) {
@@ -528,12 +641,17 @@ void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies)
     else if (b <= 12) launch_rowfft<12>(h, ne, d_energies, pg, s1);
     else launch_rowfft<16>(h, ne, d_energies, pg, s1);
     h->launches++;
-    const int lnc = colfft_lnc(h->kp), NC = 1 << lnc;
-    const size_t s2 = 8 * ((size_t)h->kp * NC + h->kp / 2);
-    dim3 grid(cdiv(h->NB, NC), h->b * h->b, ne);
-    colfft_kernel<<<grid, 256, s2, h->stream>>>(h->kp, ilog2i(h->kp), h->NB, h->Rb, h->b * h->b, lnc,
-                                                (float)(1.0 / ((double)h->kp * h->kp)), h->ws.half32, h->d_tw32,
-                                                h->ws.box32, h->ws.gmax);
+    const char *fc = getenv("CQPI_COLFFT");
+    if (rowfft_reg_ok(h) && !(fc && !strcmp(fc, "radix2"))) {
+        launch_colfft_reg(h, ne);
+    } else {
+        const int lnc = colfft_lnc(h->kp), NC = 1 << lnc;
+        const size_t s2 = 8 * ((size_t)h->kp * NC + h->kp / 2);
+        dim3 grid(cdiv(h->NB, NC), h->b * h->b, ne);
+        colfft_kernel<<<grid, 256, s2, h->stream>>>(h->kp, ilog2i(h->kp), h->NB, h->Rb, h->b * h->b, lnc,
+                                                    (float)(1.0 / ((double)h->kp * h->kp)), h->ws.half32, h->d_tw32,
+                                                    h->ws.box32, h->ws.gmax);
+    }
     h->launches++;
 }
 

@@ -121,8 +121,8 @@ def test_fused_greens_fft_matches_unfused(built_lib, name, monkeypatch):
 
 @pytest.mark.parametrize("kp,lattice", [(64, 16), (256, 24), (1024, 20), (128, 160)])
 def test_register_row_fft_matches_radix2(built_lib, kp, lattice, monkeypatch):
-    """Four-step register row transform vs the radix-2 shared-memory transform (the last
-    case has a box wider than the k-grid and takes the radix-2 path in both runs)."""
+    """Four-step register row and column transforms vs the radix-2 shared-memory transforms
+    (the last case has a box wider than the k-grid and takes the radix-2 path in both runs)."""
     import cqpi
     from cqpi import workloads as W
     m = W.t2g_c2()
@@ -131,8 +131,10 @@ def test_register_row_fft_matches_radix2(built_lib, kp, lattice, monkeypatch):
     def box(force):
         if force:
             monkeypatch.setenv("CQPI_ROWFFT", "radix2")
+            monkeypatch.setenv("CQPI_COLFFT", "radix2")
         else:
             monkeypatch.delenv("CQPI_ROWFFT", raising=False)
+            monkeypatch.delenv("CQPI_COLFFT", raising=False)
         eng = cqpi.Engine(m, lattice, kp, 3, 2, 0.01, precision=cqpi.PREC_MIXED)
         eng.set_orbitals(wf)
         return eng.greens_box(0.037)[0]
