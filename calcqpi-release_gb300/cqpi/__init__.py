@@ -24,7 +24,8 @@ EXPORTED = [
     "cqpi_wannierldos", "cqpi_retrieve_result", "cqpi_get_bands", "cqpi_get_greens_box", "cqpi_get_tmatrix",
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
     "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
-    "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune",
+    "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune", "cqpi_set_josephson",
+    "cqpi_wannierjosephson",
 ]
 
 
@@ -93,6 +94,8 @@ def load():
     L.cqpi_graph_launch.argtypes = [P]
     L.cqpi_autotune.argtypes = [P, P, i32, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(i32)]
     L.cqpi_adjoint.argtypes = [P, P, i32, P, i32, P, P]
+    L.cqpi_set_josephson.argtypes = [P, i32, dbl, dbl]
+    L.cqpi_wannierjosephson.argtypes = [P, P, P, P]
     _lib = L
     return L
 
@@ -121,6 +124,7 @@ class Engine:
         self.lattice, self.kpoints, self.oversamp, self.window = int(lattice), int(kpoints), int(oversamp), int(window)
         self.maxband = self.bands if maxband is None else int(maxband)
         self.spin = bool(spin)
+        self.eta = float(eta)
         self.wn = self.lattice * self.oversamp
         self.side = (2 * self.window + 1) * self.oversamp
         self.nimp = 1
@@ -240,6 +244,12 @@ class Engine:
         self._check(self._L.cqpi_autotune(self._h, _ptr(e), len(e), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def set_josephson(self, deltat=0.001, etat=None, enable=True):
+        """Josephson mode (output=josephson): tip gap deltat, tip broadening etat (default
+        the sample's eta, as the reference's driver)."""
+        et = self.eta if etat is None else etat
+        self._check(self._L.cqpi_set_josephson(self._h, int(bool(enable)), float(deltat), float(et)))
+
     def graph_begin(self):
         self._check(self._L.cqpi_graph_begin(self._h))
 
@@ -254,6 +264,13 @@ class Engine:
         T = np.ascontiguousarray(np.asarray(T, np.complex128))
         g = np.ascontiguousarray(np.asarray(g0r, np.complex128))
         self._check(self._L.cqpi_wannierldos(self._h, _ptr(T.view(np.float64)), _ptr(g.view(np.float64))))
+
+    def wannierjosephson(self, T, g0r, tip):
+        T = np.ascontiguousarray(np.asarray(T, np.complex128))
+        g = np.ascontiguousarray(np.asarray(g0r, np.complex128))
+        tp = np.array([complex(tip).real, complex(tip).imag], np.float64)
+        self._check(self._L.cqpi_wannierjosephson(self._h, _ptr(T.view(np.float64)), _ptr(g.view(np.float64)),
+                                                  _ptr(tp)))
 
     def retrieve_result(self):
         out = np.empty((self.wn, self.wn), np.float64)

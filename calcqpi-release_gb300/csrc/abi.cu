@@ -134,13 +134,17 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
     h->ws.ebatch = ebatch;
 }
 
+// The tensor-core contraction runs (mixed precision, a plan exists, not in Josephson mode:
+// that mode uses the CUDA-core kernel with its hole-block columns and complex tip factor).
+bool tc_active(const cqpi_handle *h) { return h->use_tc && !h->josephson; }
+
 // tmp32: float buffer of ne*nimp maps used when only float64 maps are requested from the
 // tensor-core contraction (which writes float32).
 void launch_contraction(cqpi_handle *h, int ne, float *o32, double *o64, float *tmp32)
 {
     if (h->precision == CQPI_PREC_FP64) {
         launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
-    } else if (h->use_tc) {
+    } else if (tc_active(h)) {
         float *dst = o32 ? o32 : tmp32;
         CK(launch_ldos_tc(h, ne, dst));
         if (o64) launch_widen(h, dst, o64, (size_t)ne * h->nimp * h->wn * h->wn);
@@ -233,12 +237,53 @@ void ensure_energies(cqpi_handle *h, int n)
 {
     if (h->energies_cap >= n) return;
     dfree(h->d_energies_all);
+    dfree(h->d_tip_all);
     if (h->h_energies_pinned) cudaFreeHost(h->h_energies_pinned);
+    if (h->h_tip_pinned) cudaFreeHost(h->h_tip_pinned);
     h->h_energies_pinned = nullptr;
+    h->h_tip_pinned = nullptr;
     h->energies_cap = 0;
     dalloc(&h->d_energies_all, (size_t)n);
+    dalloc(&h->d_tip_all, (size_t)n);
     CK(cudaMallocHost((void **)&h->h_energies_pinned, sizeof(double) * n));
+    CK(cudaMallocHost((void **)&h->h_tip_pinned, sizeof(double2) * n));
     h->energies_cap = n;
+}
+
+// The driver's Josephson tip factor (src/calcqpi.cc:705-708):
+//   tip = (0, -sign(E) pi deltat) / sqrt((E + i etat)^2 - deltat^2)
+// with the principal square root in the textbook careful form (t = sqrt((|x| + |z|)/2),
+// the other part y / (2t)); sign(E) = copysign(1, E).
+double2 josephson_tip(double energy, double deltat, double etat)
+{
+    const double zr = energy * energy - etat * etat - deltat * deltat, zi = 2.0 * energy * etat;
+    double sr = 0.0, si = 0.0;
+    if (zr != 0.0 || zi != 0.0) {
+        const double t = std::sqrt(0.5 * (std::fabs(zr) + std::hypot(zr, zi)));
+        if (zr >= 0.0) {
+            sr = t;
+            si = zi / (2.0 * t);
+        } else {
+            sr = std::fabs(zi) / (2.0 * t);
+            si = std::copysign(t, zi);
+        }
+    }
+    const double num = -std::copysign(1.0, energy) * M_PI * deltat;
+    const double d = sr * sr + si * si;
+    return make_double2(num * si / d, num * sr / d);
+}
+
+// Energies (and, in Josephson mode, their tip factors) of a call to the device, through the
+// page-locked mirrors, on the handle's stream.
+void upload_energies(cqpi_handle *h, const double *energies, int n)
+{
+    memcpy(h->h_energies_pinned, energies, sizeof(double) * n);
+    CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * n, cudaMemcpyHostToDevice,
+                       h->stream));
+    if (h->josephson) {
+        for (int i = 0; i < n; i++) h->h_tip_pinned[i] = josephson_tip(energies[i], h->jos_deltat, h->jos_etat);
+        CK(cudaMemcpyAsync(h->d_tip_all, h->h_tip_pinned, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+    }
 }
 
 void ensure_fov(cqpi_handle *h, size_t n)
@@ -323,7 +368,7 @@ void sr_drop(cqpi_handle *h)
 bool sr_active(const cqpi_handle *h)
 {
     const char *f = getenv("CQPI_SPIN_REDUCE");
-    return h->sr_model && h->sr_orb && h->sr_v && !(f && !strcmp(f, "0"));
+    return h->sr_model && h->sr_orb && h->sr_v && !h->josephson && !(f && !strcmp(f, "0"));
 }
 
 // Create (or re-create) the mb-band handle of the reduction; shares this handle's stream.
@@ -645,6 +690,7 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_seam_box);
     dfree(h->d_seam_T);
     dfree(h->d_seam_term1);
+    dfree(h->d_seam_tip);
     dfree(h->d_V);
     dfree(h->d_status);
     dfree(h->d_seam_ldos);
@@ -653,7 +699,9 @@ int cqpi_destroy(cqpi_handle *h)
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     for (auto e : h->ev_free) cudaEventDestroy(e);
     dfree(h->d_energies_all);
+    dfree(h->d_tip_all);
     if (h->h_energies_pinned) cudaFreeHost(h->h_energies_pinned);
+    if (h->h_tip_pinned) cudaFreeHost(h->h_tip_pinned);
     dfree(h->stage32);
     dfree(h->stage64);
     sr_drop(h);
@@ -843,13 +891,11 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
         // a copy stream, so the copy of batch k overlaps the computation of batch k+1
         const int nslot = on_device ? 1 : 2;
         const size_t slot_n = (size_t)eb * per_e;
-        const bool need32 = (!on_device && maps32) || (h->use_tc && !maps32);
+        const bool need32 = (!on_device && maps32) || (tc_active(h) && !maps32);
         if (need32) ensure_stage32(h, nslot * slot_n);
         if (!on_device && maps64) ensure_stage64(h, nslot * slot_n);
         if (!on_device) ensure_copy_stream(h);
-        memcpy(h->h_energies_pinned, energies, sizeof(double) * nE);
-        CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * nE, cudaMemcpyHostToDevice,
-                           h->stream));
+        upload_energies(h, energies, nE);
         if (!h->bands_ready) {
             const int a = record(h);
             do_bands(h);
@@ -859,6 +905,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             const int ne = std::min(eb, nE - e0);
             const int slot = bi % nslot;
             const double *den = h->d_energies_all + e0;
+            h->jos_tip = h->josephson ? h->d_tip_all + e0 : nullptr;
             float *s32 = need32 ? h->stage32 + slot * slot_n : nullptr;
             double *s64 = (!on_device && maps64) ? h->stage64 + slot * slot_n : nullptr;
             float *tmp32 = need32 ? s32 : nullptr;
@@ -937,9 +984,7 @@ int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32
             h->h_off_pinned[k] = off;
             off += (long long)fov[k] * h->os * fov[k] * h->os;
         }
-        memcpy(h->h_energies_pinned, energies, sizeof(double) * nE);
-        CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * nE, cudaMemcpyHostToDevice,
-                           h->stream));
+        upload_energies(h, energies, nE);
         CK(cudaMemcpyAsync(h->d_fov, h->h_fov_pinned, sizeof(int) * nmap, cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(h->d_fov_off, h->h_off_pinned, sizeof(long long) * nmap, cudaMemcpyHostToDevice, h->stream));
         if (!h->bands_ready) {
@@ -991,9 +1036,7 @@ int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *bes
         ensure_workspace(h, ne);
         ensure_energies(h, nE);
         ensure_stage32(h, (size_t)ne * per_e);
-        memcpy(h->h_energies_pinned, energies, sizeof(double) * ne);
-        CK(cudaMemcpyAsync(h->d_energies_all, h->h_energies_pinned, sizeof(double) * ne, cudaMemcpyHostToDevice,
-                           h->stream));
+        upload_energies(h, energies, ne);
         if (!h->bands_ready) do_bands(h);
         if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
         do_greens(h, ne, h->d_energies_all);
@@ -1109,6 +1152,7 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
     if (!h) return CQPI_ERR_ARG;
     if (nE < 0 || (nE > 0 && (!energies || !dL_dmaps))) return fail(h, CQPI_ERR_ARG, "invalid energies or map gradient");
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    if (h->josephson) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: Josephson mode is not supported");
     if (h->nblk != 1) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: spin blocks are not supported");
     if (h->kp & (h->kp - 1)) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: kpoints must be a power of two");
     if (h->Q > 128) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: oversamp^2 must be <= 128");
@@ -1250,7 +1294,9 @@ int cqpi_get_tmatrix(cqpi_handle *h, double energy, double *T)
     return CQPI_OK;
 }
 
-int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r)
+// One energy through the FP64 contraction with a given T-matrix and full G0(R) grid; tip
+// selects the Josephson form (tmatrix::calcwannierjosephson) when not NULL.
+static int seam_contract(cqpi_handle *h, const double *T, const double *g0r, const double *tip)
 {
     if (!h || !T || !g0r) return fail(h, CQPI_ERR_ARG, "null argument");
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
@@ -1270,21 +1316,58 @@ int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r)
             dalloc(&h->d_seam_box, box.size());
             dalloc(&h->d_seam_T, bb);
             dalloc(&h->d_seam_term1, (size_t)h->Q);
+            dalloc(&h->d_seam_tip, 1);
         }
         CK(cudaMemcpyAsync(h->d_seam_box, box.data(), sizeof(double2) * box.size(), cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(h->d_seam_T, T, sizeof(double2) * bb, cudaMemcpyHostToDevice, h->stream));
+        if (tip) CK(cudaMemcpyAsync(h->d_seam_tip, tip, sizeof(double2), cudaMemcpyHostToDevice, h->stream));
         CK(cudaStreamSynchronize(h->stream));   // 'box' is a pageable temporary
         const int saved = h->nimp;
         h->nimp = 1;
+        h->jos_tip = tip ? h->d_seam_tip : nullptr;
         launch_term1_ptr(h, 1, h->d_seam_box, h->d_seam_term1);
         check_launch();
         launch_ldos_fp64(h, 1, h->d_seam_box, h->d_seam_T, h->d_seam_term1, nullptr, h->d_seam_ldos);
+        h->jos_tip = nullptr;
         h->nimp = saved;
         check_launch();
         h->seam_pending = true;
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
+    return CQPI_OK;
+}
+
+int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r)
+{
+    if (h && h->josephson) return fail(h, CQPI_ERR_STATE, "Josephson mode is on: use cqpi_wannierjosephson");
+    return seam_contract(h, T, g0r, nullptr);
+}
+
+int cqpi_wannierjosephson(cqpi_handle *h, const double *T, const double *g0r, const double *tip)
+{
+    if (!h || !tip) return fail(h, CQPI_ERR_ARG, "null argument");
+    if (!h->josephson) return fail(h, CQPI_ERR_STATE, "cqpi_set_josephson has not been called");
+    return seam_contract(h, T, g0r, tip);
+}
+
+int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (!enable) {
+        h->josephson = false;
+        return CQPI_OK;
+    }
+    if (!(deltat == deltat) || !(etat == etat)) return fail(h, CQPI_ERR_ARG, "deltat and etat must be numbers");
+    // the reference's Josephson sum runs over the particle block, orbitals 0 .. bands/2 - 1,
+    // and reads the hole-block columns o + bands/2 (src/qpi.cc:956,986)
+    if (h->b < 2 || (h->b & 1)) return fail(h, CQPI_ERR_ARG, "Josephson mode needs a Bogoliubov-de Gennes model (even band count)");
+    if (h->m != (h->b >> 1))
+        return fail(h, CQPI_ERR_ARG, "Josephson mode needs maxband = bands/2 (the particle block)");
+    h->josephson = true;
+    h->jos_deltat = deltat;
+    h->jos_etat = etat;
     return CQPI_OK;
 }
 
@@ -1336,7 +1419,7 @@ int cqpi_contraction_kind(const cqpi_handle *h, int32_t *kind)
 {
     if (!h || !kind) return CQPI_ERR_ARG;
     const cqpi_handle *k = (sr_active(h) && h->sr_sub) ? h->sr_sub : h;
-    *kind = (k->precision == CQPI_PREC_FP64) ? 0 : (k->use_tc ? 2 : 1);
+    *kind = (k->precision == CQPI_PREC_FP64) ? 0 : (tc_active(k) ? 2 : 1);
     return CQPI_OK;
 }
 

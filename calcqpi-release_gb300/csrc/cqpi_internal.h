@@ -178,6 +178,14 @@ struct cqpi_handle {
     int sr_side = 0, sr_nimp = 0;
     bool owns_stream = true;
     float out_scale = 1.0f;             // factor applied to every map value
+    // Josephson mode (tmatrix::calcwannierjosephson): tip gap and broadening, per-energy tip
+    // factors on the device and their page-locked mirror, and the tip factors of the energy
+    // batch being launched (read by the term1 and contraction launchers; NULL otherwise)
+    bool josephson = false;
+    double jos_deltat = 0.001, jos_etat = 0.0;
+    double2 *d_tip_all = nullptr, *h_tip_pinned = nullptr;
+    const double2 *jos_tip = nullptr;
+    double2 *d_seam_tip = nullptr;
     // narrow seam (always FP64)
     double *d_seam_ldos = nullptr;
     double2 *d_seam_box = nullptr, *d_seam_T = nullptr;

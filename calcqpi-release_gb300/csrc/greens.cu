@@ -358,14 +358,19 @@ void launch_tmatrix(cqpi_handle *h, int ne)
 }
 
 // ------------------------------------------------------------------ site-independent term
+// term1(q) = sum_{d1,d2,o1,o2} phi_o1(q,d1) phi_o2(q,d2) Im G0(d2-d1)[o2][o1] per energy; in
+// Josephson mode (tip != NULL, src/qpi.cc:986-990) the column is o1 + coff and the value
+// Im(tip_e * G0(d2-d1)[o2][o1+coff]).
 template <class C>
 __global__ void __launch_bounds__(256) term1_kernel(int b, int NB, int Rb, int w, int Q, int W, int nblk, int mb, int bs0,
-                                                    int bs1, const double *__restrict__ phi, const C *__restrict__ box,
+                                                    int bs1, int coff, const double2 *__restrict__ tip,
+                                                    const double *__restrict__ phi, const C *__restrict__ box,
                                                     double *__restrict__ term1)
 {
     const int q = blockIdx.x, e = blockIdx.y;
     const int bb = b * b, side = 2 * w + 1;
     const C *boxe = box + (size_t)e * NB * NB * bb;
+    const double2 tp = tip ? tip[e] : make_double2(1.0, 0.0);
     double acc = 0.0;
     const int npair = nblk * W * W;
     for (int t = threadIdx.x; t < npair; t += blockDim.x) {
@@ -378,7 +383,11 @@ __global__ void __launch_bounds__(256) term1_kernel(int b, int NB, int Rb, int w
         for (int o1 = 0; o1 < mb; o1++) {
             const double f1 = p1[o1];
             if (f1 == 0.0) continue;
-            for (int o2 = 0; o2 < mb; o2++) acc += f1 * p2[o2] * (double)g[(bs + o2) * b + (bs + o1)].y;
+            for (int o2 = 0; o2 < mb; o2++) {
+                const C v = g[(bs + o2) * b + (bs + o1 + coff)];
+                const double im = tip ? tp.x * (double)v.y + tp.y * (double)v.x : (double)v.y;
+                acc += f1 * p2[o2] * im;
+            }
         }
     }
     __shared__ double red[256];
@@ -395,8 +404,9 @@ template <class C>
 static void launch_term1_t(cqpi_handle *h, int ne, const C *box, double *term1)
 {
     dim3 grid(h->Q, ne);
+    const double2 *tip = h->jos_tip;
     term1_kernel<C><<<grid, 256, 0, h->stream>>>(h->b, h->NB, h->Rb, h->w, h->Q, h->W, h->nblk, h->mb, h->blk_start[0],
-                                                 h->blk_start[1], h->d_phi, box, term1);
+                                                 h->blk_start[1], tip ? h->b >> 1 : 0, tip, h->d_phi, box, term1);
     h->launches++;
 }
 

@@ -14,14 +14,20 @@
 // which is the reference's sum over cldos[o2][o1] = (G0(p+d2) T G0(-(p+d1)))[o2][o1]
 // regrouped.  One thread per output pixel; x = site_i*os + q_x is the fastest
 // index so map stores coalesce.  Roofline: FP64- resp. FP32-FLOP bound.
+//
+// Josephson mode (JOS, tmatrix::calcwannierjosephson, src/qpi.cc:953-1033): the s side
+// reads the hole-block column o + coff (coff = bands/2), term2 is kept complex and
+//   rho(p,q) = -term1_J(q) - Im(tip * term2)
+// with the per-energy tip factor (term1_J already holds Im(tip * sum phi phi G0)).
 #include "cplx.h"
 #include "cqpi_internal.h"
 
 namespace cqpi {
 
-template <int B, class C>
+template <int B, class C, bool JOS>
 __global__ void __launch_bounds__(128) ldos_cuda_kernel(int b, int n, int os, int w, int Rb, int NB, int Q, int W, int nimp,
-                                                        int nblk, int mb, int bs0, int bs1,
+                                                        int nblk, int mb, int bs0, int bs1, int coff,
+                                                        const double2 *__restrict__ tip,
                                                         const typename real_of<C>::type *__restrict__ phi,
                                                         const C *__restrict__ box, const C *__restrict__ T,
                                                         const double *__restrict__ term1, double scale,
@@ -41,7 +47,7 @@ __global__ void __launch_bounds__(128) ldos_cuda_kernel(int b, int n, int os, in
     const C *boxe = box + (size_t)e * NB * NB * bb;
     const C *Te = T + (size_t)ei * bb;
 
-    Rl term2 = 0;
+    Rl term2 = 0, term2r = 0;
     for (int blk = 0; blk < nblk; blk++) {
         const int bs = blk ? bs1 : bs0;
         const Rl *ph = phi + ((size_t)blk * Q + q) * W * mb;
@@ -58,7 +64,7 @@ __global__ void __launch_bounds__(128) ldos_cuda_kernel(int b, int n, int os, in
 #pragma unroll
                 for (int c = 0; c < B; c++) {
                     if (c < b) {
-                        const C v = __ldg(g + c * b + o);
+                        const C v = __ldg(g + c * b + o + coff);
                         sr[c] += v.x * f;
                         si[c] += v.y * f;
                     }
@@ -87,19 +93,26 @@ __global__ void __launch_bounds__(128) ldos_cuda_kernel(int b, int n, int os, in
                 const Rl f = __ldg(ph + d * mb + ol);
                 if (f == (Rl)0) continue;
                 const int o = bs + ol;
-                Rl im = 0;
+                Rl im = 0, re = 0;
 #pragma unroll
                 for (int a = 0; a < B; a++) {
                     if (a < b) {
                         const C v = __ldg(g + o * b + a);
                         im += v.x * ti[a] + v.y * tr[a];
+                        if (JOS) re += v.x * tr[a] - v.y * ti[a];
                     }
                 }
                 term2 += f * im;
+                if (JOS) term2r += f * re;
             }
         }
     }
-    const double rho = (-term1[(size_t)e * Q + q] - (double)term2) * scale;
+    double t2 = (double)term2;
+    if (JOS) {
+        const double2 tp = tip[e];
+        t2 = tp.x * (double)term2 + tp.y * (double)term2r;
+    }
+    const double rho = (-term1[(size_t)e * Q + q] - t2) * scale;
     const size_t oi = ((size_t)ei * wn + y) * wn + x;
     if (out64) out64[oi] = rho;
     if (out32) out32[oi] = (float)rho;
@@ -111,9 +124,17 @@ static void launch_t(cqpi_handle *h, int ne, const typename real_of<C>::type *ph
 {
     dim3 blk(32, 4);
     dim3 grid(cdiv(h->wn, 32), cdiv(h->wn, 4), ne * h->nimp);
-    ldos_cuda_kernel<B, C><<<grid, blk, 0, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp,
-                                                        h->nblk, h->mb, h->blk_start[0], h->blk_start[1], phi, box, T,
-                                                        term1, (double)h->out_scale, o32, o64);
+    const double2 *tip = h->jos_tip;
+    if (tip)
+        ldos_cuda_kernel<B, C, true><<<grid, blk, 0, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W,
+                                                                  h->nimp, h->nblk, h->mb, h->blk_start[0],
+                                                                  h->blk_start[1], h->b >> 1, tip, phi, box, T, term1,
+                                                                  (double)h->out_scale, o32, o64);
+    else
+        ldos_cuda_kernel<B, C, false><<<grid, blk, 0, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W,
+                                                                   h->nimp, h->nblk, h->mb, h->blk_start[0],
+                                                                   h->blk_start[1], 0, nullptr, phi, box, T, term1,
+                                                                   (double)h->out_scale, o32, o64);
     h->launches++;
 }
 

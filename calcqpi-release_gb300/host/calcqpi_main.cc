@@ -1,13 +1,14 @@
 // calcqpi_main.cc -- `calcqpi <inputfile>`: the drop-in CLI for the continuum-LDOS
 // ("Wannier mode") path, running on the GB300 engine through the C ABI.
 //
-// Mirrors the reference driver src/calcqpi.cc:131-811 for output=wannier,
+// Mirrors the reference driver src/calcqpi.cc:131-811 for output=wannier and
+// output=josephson (:225, :249-251 deltat/etat, :451-460, :643-646, :705-709),
 // green=normal: the same keywords and defaults (:133-137), model load (:277-292),
 // scattering setup (:254-272, :393-395), orbital setup from idlorbitalfile
 // (:483-518) or analytic orbitals (:519-576), wffile output (:602-618), the map
 // idl(os*n, os*n, layers, 2, 2, lenergy, henergy, 0, -1, -1) with its comment line
 // (:640-656), layer energies idl::getbias (src/idl.cc:969-973) and the final save
-// (:779-783).  Modes and keywords outside that path (josephson, spf, uspf, nomode,
+// (:779-783).  Modes and keywords outside that path (spf, uspf, nomode,
 // green=surface|bulk, threshold lists, XSF orbitalfiles, bsfile, dosfile) stop with
 // an explicit "not supported" error instead of being ignored.
 #include <unistd.h>
@@ -132,11 +133,11 @@ void help()
     std::cerr << "calcqpi (GB300 continuum-LDOS engine, " << cqpi_version() << ")\n\n"
               << "Syntax:\ncalcqpi configfile\n\n"
               << "Keywords of the continuum-LDOS (wannier) path:\n"
-              << " tbfile, qpifile, output (wannier), logfile, wffile,\n"
+              << " tbfile, qpifile, output (wannier, josephson), logfile, wffile,\n"
               << " lattice (201), oversamp (4), energies (-1,1), layers (21), kpoints (=lattice),\n"
               << " green (normal), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
-              << " pos[i], zheight (5.0), idlorbitalfile\n";
+              << " pos[i], zheight (5.0), idlorbitalfile, deltat (0.001), etat (=eta)\n";
 }
 
 double getbias(double lb, double hb, size_t layers, size_t k)
@@ -211,10 +212,12 @@ int main(int argc, char **argv)
         else if (s == "false") scmodel = false;
         else log << "Invalid value for scmodel: " << s << "\n";
     }
+    bool josephson = false;
     if (lf.has("output")) {
         std::string o = lf.field("output");
-        if (o == "josephson" || o == "spf" || o == "uspf" || o == "nomode") return not_supported(log, "output=" + o);
-        if (o != "wannier") {
+        if (o == "spf" || o == "uspf" || o == "nomode") return not_supported(log, "output=" + o);
+        if (o == "josephson") josephson = true;
+        else if (o != "wannier") {
             log << "Unrecognized output mode.";
             return 1;
         }
@@ -233,8 +236,11 @@ int main(int argc, char **argv)
         if (e.size() >= 2) { lenergy = e[0]; henergy = e[1]; }
     }
     if (lf.has("eta")) eta = lf.value("eta");
-    if (lf.has("etat")) lf.value("etat");
-    if (lf.has("deltat")) lf.value("deltat");
+    // tip of the josephson mode: broadening defaults to the sample's (src/calcqpi.cc:249-251)
+    double etat = NAN, deltat = 0.001;
+    if (lf.has("etat")) etat = lf.value("etat");
+    if (std::isnan(etat)) etat = eta;
+    if (lf.has("deltat")) deltat = lf.value("deltat");
     if (lf.has("kpoints")) kpoints = lf.ivalue("kpoints");
     if (!kpoints) kpoints = n;
     if (lf.has("phase")) {
@@ -306,7 +312,17 @@ int main(int argc, char **argv)
           << (spin ? "         spin-polarized calculation\n" : "         paramagnetic calculation\n");
         log << l.str();
     }
-    log << "QPI calculations in Wannier-mode (cLDOS).\n";
+    if (josephson) {
+        std::ostringstream l;
+        l << "QPI calculations in Josephson-mode.\n   using deltat=" << deltat << ", etat=" << etat << ".\n";
+        log << l.str();
+        if (!scmodel) {
+            log << "Error: Calculation in josephson-mode with scmodel=false makes no sense - exiting.\n";
+            return 1;
+        }
+    } else {
+        log << "QPI calculations in Wannier-mode (cLDOS).\n";
+    }
 
     // ---------------------------------------------------------------- orbitals
     std::vector<double> prearr;
@@ -472,6 +488,7 @@ int main(int argc, char **argv)
     for (size_t o = 0; o < wfs.size(); o++) std::copy(wfs[o].begin(), wfs[o].end(), wflat.begin() + o * side * side);
     rc = cqpi_set_orbitals(h, wflat.data(), (int32_t)wfs.size(), (int32_t)side, zero.data());
     if (rc == CQPI_OK) rc = cqpi_set_scattering(h, vscat.data());
+    if (rc == CQPI_OK && josephson) rc = cqpi_set_josephson(h, 1, deltat, etat);
     if (rc != CQPI_OK) {
         log << "Error: " << cqpi_last_error(h) << "\n";
         cqpi_destroy(h);
@@ -479,7 +496,8 @@ int main(int argc, char **argv)
     }
     const size_t wn = n * oversamp;
     std::ostringstream comment;
-    comment << "CQPI calculation for " << hr->name << " with window=" << window << " and oversamp=" << oversamp;
+    comment << (josephson ? "Josephson calculation for " : "CQPI calculation for ") << hr->name << " with window="
+            << window << " and oversamp=" << oversamp;
     timings.add("Initialization of calculation");
 
     std::vector<double> energies(layers);

@@ -132,6 +132,18 @@ int cqpi_graph_begin(cqpi_handle *h);
 int cqpi_graph_end(cqpi_handle *h);
 int cqpi_graph_launch(cqpi_handle *h);
 
+/* ---- Josephson mode (output=josephson, src/calcqpi.cc:225,451-460,705-709) -----------
+ * enable != 0 switches cqpi_run to the Josephson contraction of
+ * tmatrix::calcwannierjosephson (src/qpi.cc:953-1033): the sum runs over the particle-block
+ * orbitals 0 .. bands/2 - 1, reads the hole-block column o + bands/2 of G0 and T G0, and
+ * every map is -Im(tip(E) * ...) with the driver's per-energy tip factor
+ *   tip(E) = (0, -sign(E) pi deltat) / sqrt((E + i etat)^2 - deltat^2).
+ * Needs an even band count and maxband = bands/2 (CQPI_ERR_ARG otherwise); the driver's
+ * defaults are deltat = 0.001 and etat = eta.  In this mode the mixed path contracts on
+ * FP32 CUDA cores; cqpi_run_fov, cqpi_autotune and cqpi_adjoint return
+ * CQPI_ERR_NOT_SUPPORTED.  enable = 0 returns to the LDOS (wannier) mode. */
+int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat);
+
 /* ---- differentiation (extension: the reference computes no derivatives) -----
  * New hopping amplitudes for the terms of the model given to cqpi_create (same order,
  * same R / orbitals / conjugation flags): t[nhops][2].  The eigen cache is rebuilt by
@@ -152,6 +164,12 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
  * Green's function g0r[kp][kp][b][b][2] (the reference's g0 after
  * calcrealspacegreensfunction); asynchronous like src/qpicudakernel.cu:577-598. */
 int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r);
+/* GPUQPI::wannierjosephson(scat, g0, tip) (include/gpuqpi.h:24, src/qpicudakernel.cu:600-620):
+ * the Josephson form of the same contraction
+ * (tmatrix::calcwannierjosephson, src/qpi.cc:953-1033) with the tip factor tip[2] of the
+ * energy; needs cqpi_set_josephson(h, 1, ...) first (CQPI_ERR_STATE otherwise), as
+ * cqpi_wannierldos needs it off. */
+int cqpi_wannierjosephson(cqpi_handle *h, const double *T, const double *g0r, const double *tip);
 /* GPUQPI::retrieveResult(double*) (src/qpicudakernel.cu:690-704): waits and
  * copies the last map, ldos[y][x] float64 (= the reference's ldos[x][y]). */
 int cqpi_retrieve_result(cqpi_handle *h, double *ldos);

@@ -415,3 +415,110 @@ void orc_set_threads(int nt)
     (void)nt;
 #endif
 }
+
+/* ---- tmatrix::calcwannierjosephson (CPU), qpi.cc:953-1033 ----
+ * The same double window sum as orc_wannier_ldos with three differences of the
+ * reference's Josephson mode: the orbital count is the particle block bands>>1
+ * (qpi.cc:956), the column of cldos and G0 is shifted into the hole block
+ * (o1 + maxband, qpi.cc:986-987,1000-1001,1009-1010), and the sum of the two
+ * terms is multiplied by the tip factor before its imaginary part is taken
+ * (qpi.cc:988-989).  tip = (tip_re, tip_im) is the driver's per-energy factor
+ * (orc_josephson_tip, calcqpi.cc:706-708). */
+void orc_wannier_josephson(int n, int kp, int b, int os, int w, int spin,
+                           const double *T, const double *g0r, const double *wf,
+                           const uint8_t *wf_zero, double tip_re, double tip_im, double *ldos,
+                           int row_begin, int row_end)
+{
+    size_t wn = (size_t)os * n, side = (size_t)(2 * w + 1) * os, bb = (size_t)b * b;
+    size_t kpoints = (size_t)kp, n2 = (size_t)(n >> 1);
+    size_t maxband = (size_t)(b >> 1), spinbands = maxband >> 1;
+    if (row_end <= 0 || row_end > n) row_end = n;
+    for (int i = row_begin; i < row_end; i++)
+        for (size_t ii = 0; ii < (size_t)os; ii++)
+            for (size_t y = 0; y < wn; y++) ldos[((size_t)i * os + ii) * wn + y] = 0.0;
+#define G0AT(X, Y) (g0r + 2 * (((size_t)(X) * kpoints + (size_t)(Y)) * bb))
+#define WF(o, X, Y) (wf[((size_t)(o) * side + (size_t)(X)) * side + (size_t)(Y)])
+/* ldos -= Im(tip * (cldos + g0)[r][c]) * f */
+#define JACC(r, c, f)                                                                       \
+    do {                                                                                    \
+        double vr = RE(cldos, (r) * b + (c)) + RE(gd, (r) * b + (c));                       \
+        double vi = IM(cldos, (r) * b + (c)) + IM(gd, (r) * b + (c));                       \
+        *out -= (vr * tip_im + vi * tip_re) * (f);                                          \
+    } while (0)
+#pragma omp parallel
+    {
+        double *buffer = (double *)malloc(sizeof(double) * 2 * bb);
+        double *cldos = (double *)malloc(sizeof(double) * 2 * bb);
+#pragma omp for collapse(2) schedule(dynamic, 4)
+        for (int i = row_begin; i < row_end; i++)
+            for (int j = 0; j < n; j++) {
+                int ipos = i - (int)n2, jpos = j - (int)n2;
+                for (int nni1 = -w; nni1 <= w; nni1++)
+                    for (int nnj1 = -w; nnj1 <= w; nnj1++) {
+                        zmul(b, T, G0AT((kpoints + kpoints - (size_t)(ipos + nni1)) % kpoints,
+                                        (kpoints + kpoints - (size_t)(jpos + nnj1)) % kpoints), buffer);
+                        for (int nni2 = -w; nni2 <= w; nni2++)
+                            for (int nnj2 = -w; nnj2 <= w; nnj2++) {
+                                zmul(b, G0AT((kpoints + (size_t)(ipos + nni2)) % kpoints,
+                                             (kpoints + (size_t)(jpos + nnj2)) % kpoints), buffer, cldos);
+                                const double *gd = G0AT((kpoints - (size_t)nni1 + (size_t)nni2) % kpoints,
+                                                        (kpoints - (size_t)nnj1 + (size_t)nnj2) % kpoints);
+                                for (size_t ii = 0; ii < (size_t)os; ii++)
+                                    for (size_t jj = 0; jj < (size_t)os; jj++) {
+                                        size_t x = ii + (size_t)w * os, y = jj + (size_t)w * os;
+                                        size_t x1 = x - (size_t)((long)nni1 * os), y1 = y - (size_t)((long)nnj1 * os);
+                                        size_t x2 = x - (size_t)((long)nni2 * os), y2 = y - (size_t)((long)nnj2 * os);
+                                        double *out = &ldos[((size_t)i * os + ii) % wn * wn + ((size_t)j * os + jj) % wn];
+                                        if (!spin) {
+                                            for (size_t o1 = 0; o1 < maxband; o1++) {
+                                                if (wf_zero[o1]) continue;
+                                                for (size_t o2 = 0; o2 < maxband; o2++) {
+                                                    if (wf_zero[o2]) continue;
+                                                    JACC(o2, o1 + maxband, WF(o1, x1, y1) * WF(o2, x2, y2));
+                                                }
+                                            }
+                                        } else {
+                                            for (size_t o1 = 0; o1 < spinbands; o1++) {
+                                                if (!wf_zero[o1])
+                                                    for (size_t o2 = 0; o2 < spinbands; o2++) {
+                                                        if (wf_zero[o2]) continue;
+                                                        JACC(o2, o1 + maxband, WF(o1, x1, y1) * WF(o2, x2, y2));
+                                                    }
+                                                size_t s1 = spinbands + o1;
+                                                if (!wf_zero[s1])
+                                                    for (size_t o2 = 0; o2 < spinbands; o2++) {
+                                                        size_t s2 = spinbands + o2;
+                                                        if (wf_zero[s2]) continue;
+                                                        JACC(s2, s1 + maxband, WF(s1, x1, y1) * WF(s2, x2, y2));
+                                                    }
+                                            }
+                                        }
+                                    }
+                            }
+                    }
+            }
+        free(buffer); free(cldos);
+    }
+#undef JACC
+#undef G0AT
+#undef WF
+}
+
+/* ---- the Josephson tip factor of the driver, calcqpi.cc:705-708 ----
+ * tip = (0, -sign(E) pi deltat) / sqrt((E + i etat)^2 - deltat^2), principal root,
+ * sign(E) = copysign(1, E).  The square root is the textbook careful form
+ * (t = sqrt((|x| + |z|)/2), the other part y/(2t)). */
+void orc_josephson_tip(double energy, double deltat, double etat, double *tip)
+{
+    double zr = energy * energy - etat * etat - deltat * deltat, zi = 2.0 * energy * etat;
+    double sr = 0.0, si = 0.0;
+    if (zr != 0.0 || zi != 0.0) {
+        double t = sqrt(0.5 * (fabs(zr) + hypot(zr, zi)));
+        if (zr >= 0.0) { sr = t; si = zi / (2.0 * t); }
+        else { sr = fabs(zi) / (2.0 * t); si = copysign(t, zi); }
+    }
+    double num = -copysign(1.0, energy) * M_PI * deltat;   /* numerator (0, num) */
+    double d = sr * sr + si * si;
+    tip[0] = num * si / d;
+    tip[1] = num * sr / d;
+}

@@ -55,6 +55,8 @@ def lib():
             L.orc_tmatrix.argtypes = [i32, P, P, P]
             L.orc_tmatrix.restype = i32
             L.orc_wannier_ldos.argtypes = [i32, i32, i32, i32, i32, i32, i32, P, P, P, P, P, i32, i32]
+            L.orc_wannier_josephson.argtypes = [i32, i32, i32, i32, i32, i32, P, P, P, P, dbl, dbl, P, i32, i32]
+            L.orc_josephson_tip.argtypes = [dbl, dbl, dbl, P]
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -145,6 +147,29 @@ def wannier_ldos(n, kp, os_, w, m, spin, T, g0r, wf, wf_zero=None, rows=None) ->
     return out
 
 
+def josephson_tip(energy, deltat, etat) -> complex:
+    """The driver's Josephson tip factor, src/calcqpi.cc:705-708."""
+    t = np.zeros(2, np.float64)
+    lib().orc_josephson_tip(float(energy), float(deltat), float(etat), _p(t))
+    return complex(t[0], t[1])
+
+
+def wannier_josephson(n, kp, os_, w, spin, T, g0r, wf, tip, wf_zero=None, rows=None) -> np.ndarray:
+    """tmatrix::calcwannierjosephson (CPU), src/qpi.cc:953-1033.  Returns ldos[x][y] (float64)."""
+    b = g0r.shape[2]
+    wf = np.ascontiguousarray(wf, dtype=np.float64)
+    z = np.ascontiguousarray(np.zeros(wf.shape[0], np.uint8) if wf_zero is None else wf_zero, dtype=np.uint8)
+    if wf.shape[0] < b >> 1:
+        raise ValueError("Josephson mode needs bands/2 orbitals")
+    T = np.ascontiguousarray(T, dtype=np.complex128)
+    g0r = np.ascontiguousarray(g0r, dtype=np.complex128)
+    out = np.zeros((n * os_, n * os_), np.float64)
+    r0, r1 = (0, n) if rows is None else rows
+    lib().orc_wannier_josephson(n, kp, b, os_, w, int(bool(spin)), _p(T), _p(g0r), _p(wf), _p(z),
+                                float(tip.real), float(tip.imag), _p(out), r0, r1)
+    return out
+
+
 def set_threads(nt: int):
     lib().orc_set_threads(int(nt))
 
@@ -153,17 +178,22 @@ def num_threads() -> int:
     return int(lib().orc_num_threads())
 
 
-def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=None, spin=False):
+def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=None, spin=False, josephson=None):
     """The reference's wannier-mode energy loop (src/calcqpi.cc:673-760, normal Green's
     function): eigen once, then per energy G0(k) -> G0(R) -> T -> LDOS.  Returns maps in
-    IDL file order [layer][y][x], float64."""
+    IDL file order [layer][y][x], float64.  josephson=(deltat, etat) runs the driver's
+    josephson mode instead (calcqpi.cc:705-709)."""
     m = model.bands if m is None else m
     ev, U = bands(model, kp)
     maps = []
     for e in energies:
         g0r = realspace(greens_k(ev, U, kp, e, eta))
         T = tmatrix(vscat, g0r[0, 0])
-        maps.append(wannier_ldos(n, kp, os_, w, m, spin, T, g0r, wf, wf_zero).T)
+        if josephson is not None:
+            tip = josephson_tip(e, josephson[0], josephson[1])
+            maps.append(wannier_josephson(n, kp, os_, w, spin, T, g0r, wf, tip, wf_zero).T)
+        else:
+            maps.append(wannier_ldos(n, kp, os_, w, m, spin, T, g0r, wf, wf_zero).T)
     return np.stack(maps)
 
 

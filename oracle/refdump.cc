@@ -9,12 +9,17 @@
 // output=wannier, green=normal, with orbitals given as a float64 cube (the
 // idlorbitalfile route, wannierfunctions.cc:489-498) padded with zero orbitals.
 //
+// With a trailing "J deltat etat" it runs the josephson mode instead
+// (src/calcqpi.cc:705-709: per-energy tip factor, tmatrix::calcwannierjosephson).
+//
 // usage: refdump <hrfile> <wfbin> <out> n kp os w eta efermi spin maxband layers
-//                lenergy henergy scmodel nscat [vre vim]...
+//                lenergy henergy scmodel nscat [vre vim]... [J deltat etat]
 // wfbin: int32 norb, int32 side, float64 [norb][side][side]
 // out:   per layer: float64 dos (tmatrix::calcdos), float64 ldos[y][x]
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
+#include <string>
 #include <vector>
 #include <complex>
 #include <iostream>
@@ -42,6 +47,9 @@ int main(int argc, char **argv)
     int nscat = atoi(argv[16]);
     vector<complex<double> > scat;
     for (int i = 0; i < nscat; i++) scat.push_back(complex<double>(atof(argv[17 + 2 * i]), atof(argv[18 + 2 * i])));
+    const int ja = 17 + 2 * nscat;
+    const bool josephson = argc >= ja + 3 && string(argv[ja]) == "J";
+    const double deltat = josephson ? atof(argv[ja + 1]) : 0.0, etat = josephson ? atof(argv[ja + 2]) : 0.0;
 
     tightbind *model = new tightbind(string(hr), efermi, scmodel);
     if (!*model) { cerr << "model load failed" << endl; return 1; }
@@ -72,7 +80,15 @@ int main(int argc, char **argv)
         tm->setgreensfunction(energy);
         tm->calcrealspacegreensfunction();
         double dos = tm->calcdos(maxband);
-        tm->calcwannierldos(os, w, wfs, maxband);
+        if (josephson) {
+            gsl_complex ocomp = gsl_complex_rect(energy, etat);
+            gsl_complex tip = gsl_complex_div(gsl_complex_rect(0.0, -copysign(1.0, energy) * M_PI * deltat),
+                                              gsl_complex_sqrt(gsl_complex_sub_real(gsl_complex_mul(ocomp, ocomp),
+                                                                                    deltat * deltat)));
+            tm->calcwannierjosephson(os, w, wfs, tip);
+        } else {
+            tm->calcwannierldos(os, w, wfs, maxband);
+        }
         tm->ldos2array(buf.data());
         fwrite(&dos, 8, 1, o);
         fwrite(buf.data(), 8, wn * wn, o);

@@ -51,6 +51,44 @@ def bdg_c1(delta=0.1):
     return terms
 
 
+def bdg(base: dict, D: np.ndarray) -> dict:
+    """BdG form of an electron model: electron block t(R), hole block -conj(t(R)) (the
+    hole Hamiltonian -H(-k)^*), on-site pairing matrix D between the blocks (for
+    scmodel=true).  Hermitian whenever the electron model is."""
+    b = next(iter(base.values())).shape[0]
+    terms = {}
+    for R, M in base.items():
+        T = np.zeros((2 * b, 2 * b), complex)
+        T[:b, :b] = M
+        T[b:, b:] = -np.conj(M)
+        terms[R] = T
+    T0 = terms.get((0, 0, 0), np.zeros((2 * b, 2 * b), complex)).copy()
+    T0[:b, b:] += D
+    T0[b:, :b] += np.conj(D).T
+    terms[(0, 0, 0)] = T0
+    return terms
+
+
+def bdg_t2g():
+    """Six-band BdG form of the C2 t2g model with an orbital-dependent on-site pairing."""
+    D = np.diag([0.04, 0.04, 0.06]).astype(complex)
+    D[0, 1] = D[1, 0] = 0.01
+    return bdg(W.t2g_c2().terms(), D)
+
+
+def bdg_spin():
+    """Four-band BdG form of a spinful one-orbital square lattice (orbitals up, down; a
+    Zeeman splitting of 0.05 on site) with equal-spin pairing 0.08 so that both spin
+    blocks of the Josephson sum are non-zero."""
+    base = {}
+    for R, M in W.square_c1().terms().items():
+        base[R] = M[0, 0] * np.eye(2, dtype=complex)
+    T0 = base.get((0, 0, 0), np.zeros((2, 2), complex)).copy()
+    T0 += np.diag([0.05, -0.05])
+    base[(0, 0, 0)] = T0
+    return bdg(base, 0.08 * np.eye(2, dtype=complex))
+
+
 CASES = {
     "c1_idl": dict(model="c1", deg=2, n=12, kp=32, os=4, w=2, layers=3, energies=(-0.2, 0.2), eta=0.05,
                    scattering=(0.5,), orbitals=("idl", "gauss")),
@@ -68,6 +106,15 @@ CASES = {
     "scmodel": dict(model="bdg", scmodel=True, magscat=0.25, n=8, kp=16, os=2, w=1, layers=2,
                     energies=(-0.1, 0.1), eta=0.03, scattering=(0.5,),
                     orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "josephson": dict(model="bdg", scmodel=True, magscat=0.25, n=8, kp=16, os=2, w=1, layers=3,
+                      energies=(-0.12, 0.09), eta=0.03, scattering=(0.5,), josephson=(0.02, 0.01),
+                      orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "josephson_t2g": dict(model="bdg_t2g", scmodel=True, magscat=0.0, n=6, kp=16, os=2, w=1, layers=2,
+                          energies=(-0.06, 0.05), eta=0.02, scattering=(0.3, 0.3, 0.5), josephson=(None, None),
+                          orbitals=("analytic", dict(names=["dxz", "dyz", "dxy"], radius=0.4, zheight=0.6))),
+    "josephson_spin": dict(model="bdg_spin", scmodel=True, spin=True, magscat=0.1, n=6, kp=12, os=2, w=1,
+                           layers=2, energies=(-0.1, 0.07), eta=0.03, scattering=(0.4,), josephson=(0.05, 0.02),
+                           orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
     "wrap": dict(model="c1", n=20, kp=8, os=2, w=1, layers=1, energies=(0.1, 0.1), eta=0.05, scattering=(0.7,),
                  orbitals=("analytic", dict(names=["px"], radius=0.35, zheight=0.4, angle=20.0))),
 }
@@ -85,6 +132,10 @@ def model_terms(c):
         return m.name, m.bands, m.terms()
     if c["model"] == "bdg":
         return "BdG square lattice (scmodel)", 2, bdg_c1()
+    if c["model"] == "bdg_t2g":
+        return "BdG t2g model (scmodel)", 6, bdg_t2g()
+    if c["model"] == "bdg_spin":
+        return "BdG spinful square lattice (scmodel)", 4, bdg_spin()
     raise KeyError(c["model"])
 
 
@@ -116,7 +167,9 @@ def make_case(name, c):
     scmodel = c.get("scmodel", False)
     spin = c.get("spin", False)
     maxband = bands >> 1 if scmodel else bands
-    lines = ['tbfile="model_hr.dat";', 'qpifile="ref_qpi.idl";', "output=wannier;",
+    jos = c.get("josephson")
+    lines = ['tbfile="model_hr.dat";', 'qpifile="ref_qpi.idl";',
+             "output=josephson;" if jos else "output=wannier;",
              f"lattice={n};", f"kpoints={kp};", f"oversamp={os_};", f"window={w};", f"layers={c['layers']};",
              f"energies={fmt_list(c['energies'])};", f"eta={c['eta']!r};"]
     if "fermi" in c:
@@ -125,6 +178,11 @@ def make_case(name, c):
         lines.append(f"phase={fmt_list(c['phase'])};")
     if "scattering" in c:
         lines.append(f"scattering={fmt_list(c['scattering'])};")
+    if jos:
+        if jos[0] is not None:
+            lines.append(f"deltat={jos[0]!r};")
+        if jos[1] is not None:
+            lines.append(f"etat={jos[1]!r};")
     if spin:
         lines.append("spin=true;")
     if scmodel:
@@ -197,6 +255,9 @@ def make_case(name, c):
             repr(c["energies"][0]), repr(c["energies"][1]), str(int(scmodel)), str(len(vscat))]
     for v in vscat:
         args += [repr(v.real), repr(v.imag)]
+    if jos:
+        # the driver's defaults: deltat 0.001, etat = eta (src/calcqpi.cc:137,249-251)
+        args += ["J", repr(0.001 if jos[0] is None else jos[0]), repr(c["eta"] if jos[1] is None else jos[1])]
     r2 = subprocess.run(args, capture_output=True, text=True, timeout=600)
     if r2.returncode != 0:
         raise RuntimeError(f"{name}: refdump failed\n{r2.stderr}")

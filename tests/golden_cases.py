@@ -22,3 +22,12 @@ def energies(meta):
     if L == 1:
         return np.array([lo])
     return np.array([(hi - lo) * k / (L - 1.0) + lo for k in range(L)])
+
+
+def josephson(meta):
+    """(deltat, etat) of a josephson-mode case with the driver's defaults (deltat 0.001,
+    etat = eta; src/calcqpi.cc:137,249-251), or None for a wannier-mode case."""
+    j = meta.get("josephson")
+    if not j:
+        return None
+    return (0.001 if j[0] is None else j[0], meta["eta"] if j[1] is None else j[1])

@@ -42,6 +42,6 @@ def test_cli_rejects_out_of_scope_modes(built_lib, tmp_path):
     for f in ("model_hr.dat", "orbitals.idl", "input.cfg"):
         shutil.copy(os.path.join(d, f), tmp_path / f)
     with open(tmp_path / "input.cfg", "a") as fh:
-        fh.write("output=josephson;\n")
+        fh.write("output=spf;\n")
     r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "not supported" in r.stdout

@@ -1,0 +1,127 @@
+"""GPU: Josephson mode (output=josephson, tmatrix::calcwannierjosephson, src/qpi.cc:953-1033).
+
+* FP64 engine against the reference's own float64 maps (golden fixtures) to 1e-10 relative;
+* mixed-precision engine (FP32 CUDA-core contraction, FP64 term1) against them to 1e-6;
+* the narrow seam GPUQPI::wannierjosephson against the oracle to 1e-12;
+* the mode's argument and state errors.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from golden_cases import energies, josephson, load
+
+pytestmark = pytest.mark.gpu
+
+JOS = ["josephson", "josephson_t2g", "josephson_spin"]
+
+
+def _model(d, meta):
+    from oracle import formats as F
+    from oracle import oracle as O
+    with open(os.path.join(d, "model_hr.dat")) as fh:
+        hr = F.read_hr(fh.read(), scmodel=True)
+    return O.Model.from_hr(hr, efermi=meta.get("fermi", 0.0))
+
+
+def _engine(name, precision):
+    import cqpi
+    d, meta, ref = load(name)
+    m = _model(d, meta)
+    eng = cqpi.Engine(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], maxband=meta["maxband"],
+                      spin=meta.get("spin", False), precision=precision)
+    eng.set_orbitals(ref["wf"], ref["zero"])
+    eng.set_scattering(ref["vscat"])
+    dt, et = josephson(meta)
+    eng.set_josephson(dt, et)
+    return eng, meta, ref, m
+
+
+@pytest.mark.parametrize("name", JOS)
+def test_josephson_fp64_matches_reference(built_lib, name):
+    import cqpi
+    eng, meta, ref, _ = _engine(name, cqpi.PREC_FP64)
+    got = eng.run(energies(meta), f32=False, f64=True)[:, 0]
+    err = np.abs(got - ref["ldos"]).max() / np.abs(ref["ldos"]).max()
+    assert err < 1e-10, err
+    eng.close()
+
+
+@pytest.mark.parametrize("name", JOS)
+def test_josephson_mixed_matches_reference(built_lib, name):
+    import cqpi
+    eng, meta, ref, _ = _engine(name, cqpi.PREC_MIXED)
+    got = eng.run(energies(meta), f32=False, f64=True)[:, 0]
+    for k in range(len(got)):
+        err = np.abs(got[k] - ref["ldos"][k]).max() / np.abs(ref["ldos"][k]).max()
+        assert err <= 1e-6, (k, err)
+    assert eng.contraction_kind() == "fp32"
+    eng.close()
+
+
+def test_josephson_seam_matches_oracle(built_lib):
+    """GPUQPI::wannierjosephson(scat, g0, tip) + retrieveResult with the oracle's G0(R), T, tip."""
+    from oracle import oracle as O
+    eng, meta, ref, m = _engine("josephson_t2g", 0)
+    kp = meta["kp"]
+    ev, U = O.bands(m, kp)
+    e = energies(meta)[0]
+    g0r = O.realspace(O.greens_k(ev, U, kp, e, meta["eta"]))
+    T = O.tmatrix(ref["vscat"], g0r[0, 0])
+    tip = O.josephson_tip(e, *josephson(meta))
+    eng.wannierjosephson(T, g0r, tip)
+    got = eng.retrieve_result()
+    want = O.wannier_josephson(meta["n"], kp, meta["os"], meta["w"], False, T, g0r, ref["wf"], tip, ref["zero"]).T
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    eng.close()
+
+
+def test_josephson_mode_toggles_back_to_ldos(built_lib):
+    import cqpi
+    eng, meta, ref, m = _engine("josephson", cqpi.PREC_FP64)
+    E = energies(meta)
+    j1 = eng.run(E, f32=False, f64=True)
+    eng.set_josephson(enable=False)
+    ldos = eng.run(E, f32=False, f64=True)
+    eng.set_josephson(*josephson(meta))
+    j2 = eng.run(E, f32=False, f64=True)
+    assert np.array_equal(j1, j2)
+    plain = cqpi.Engine(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], maxband=meta["maxband"],
+                        precision=cqpi.PREC_FP64)
+    plain.set_orbitals(ref["wf"], ref["zero"])
+    plain.set_scattering(ref["vscat"])
+    assert np.array_equal(ldos, plain.run(E, f32=False, f64=True))
+    plain.close()
+    eng.close()
+
+
+def test_josephson_errors(built_lib):
+    import cqpi
+    from cases import case
+    # odd band count (the C2 model: 3 bands)
+    m, p, wf, z, v, E = case("c2")
+    eng = cqpi.Engine(m, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"])
+    with pytest.raises(cqpi.CqpiError) as ex:
+        eng.set_josephson(0.01)
+    assert ex.value.code == cqpi.ERR_ARG
+    eng.close()
+    # maxband other than bands/2
+    d, meta, ref = load("josephson_t2g")
+    mm = _model(d, meta)
+    eng = cqpi.Engine(mm, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], maxband=mm.bands)
+    with pytest.raises(cqpi.CqpiError) as ex:
+        eng.set_josephson(0.01)
+    assert ex.value.code == cqpi.ERR_ARG
+    eng.close()
+    # the adjoint, fields of view and the plain seam are refused in Josephson mode
+    eng, meta, ref, m = _engine("josephson_t2g", cqpi.PREC_MIXED)
+    E = energies(meta)
+    wn = meta["n"] * meta["os"]
+    with pytest.raises(cqpi.CqpiError) as ex:
+        eng.adjoint(E, np.zeros((len(E), 1, wn, wn), np.float32))
+    assert ex.value.code == cqpi.ERR_NOT_SUPPORTED
+    with pytest.raises(cqpi.CqpiError) as ex:
+        eng.wannierldos(np.eye(m.bands), np.zeros((meta["kp"], meta["kp"], m.bands, m.bands)))
+    assert ex.value.code == cqpi.ERR_STATE
+    eng.close()

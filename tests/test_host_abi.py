@@ -98,3 +98,18 @@ def test_idl_roundtrip_and_reference_bytes(built_lib, tmp_path):
         host.idl_write(out, data, hdr["name"], hdr["scan_range"], hdr["offset"], hdr["bias"], hdr["setpoint"],
                        date=hdr["date"])
         assert out.read_bytes() == open(path, "rb").read()
+
+
+def test_cli_josephson_needs_scmodel(built_lib, tmp_path):
+    """output=josephson with scmodel=false stops before any device work, with the
+    reference's message (src/calcqpi.cc:458-461)."""
+    import shutil
+    d, meta, ref = load("c1_idl")
+    for f in ("model_hr.dat", "orbitals.idl", "input.cfg"):
+        shutil.copy(os.path.join(d, f), tmp_path / f)
+    with open(tmp_path / "input.cfg", "a") as fh:
+        fh.write("output=josephson;\ndeltat=0.01;\n")
+    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert "Josephson-mode" in r.stdout and "using deltat=0.01, etat=0.05." in r.stdout
+    assert "josephson-mode with scmodel=false makes no sense" in r.stdout

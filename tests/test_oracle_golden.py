@@ -4,7 +4,7 @@ import os
 import numpy as np
 import pytest
 
-from golden_cases import NAMES, energies, load
+from golden_cases import NAMES, energies, josephson, load
 from oracle import formats as F
 from oracle import oracle as O
 
@@ -21,7 +21,7 @@ def test_oracle_matches_reference_float64(name):
     m = _model(d, meta)
     E = energies(meta)
     maps = O.run(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], E, ref["vscat"], ref["wf"],
-                 ref["zero"], m=meta["maxband"], spin=meta.get("spin", False))
+                 ref["zero"], m=meta["maxband"], spin=meta.get("spin", False), josephson=josephson(meta))
     err = np.abs(maps - ref["ldos"]).max() / np.abs(ref["ldos"]).max()
     assert err < 1e-10, err
     # tmatrix::calcdos = -sum_i<maxband Im G0(R=0)_ii  (src/qpi.cc:856-862)
@@ -97,3 +97,13 @@ def test_config_restatement_reads_inputs():
     assert bad.warnings == ["lattice=3"]
     assert not bad.probefield("x")          # keys are not trimmed (include/parser.h:44)
     assert bad.getintvalue("kpoints") == 16  # the last value wins (include/parser.h:117-121)
+
+
+def test_josephson_tip_matches_complex_arithmetic():
+    """The tip factor of src/calcqpi.cc:705-708 against numpy's principal square root,
+    including energies near zero and below the tip gap."""
+    for e in [-0.3, -0.02, -1e-9, 0.0, 1e-9, 0.004, 0.02, 0.5]:
+        for dt, et in [(0.001, 0.005), (0.02, 0.01), (0.05, 1e-4)]:
+            want = 1j * (-np.copysign(1.0, e) * np.pi * dt) / np.sqrt(complex(e, et) ** 2 - dt * dt)
+            got = O.josephson_tip(e, dt, et)
+            assert abs(got - want) <= 1e-14 * abs(want), (e, dt, et, got, want)
