@@ -25,7 +25,7 @@ EXPORTED = [
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
     "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
     "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune", "cqpi_set_josephson",
-    "cqpi_wannierjosephson",
+    "cqpi_wannierjosephson", "cqpi_set_threshold", "cqpi_wannierldoslist",
 ]
 
 
@@ -96,6 +96,8 @@ def load():
     L.cqpi_adjoint.argtypes = [P, P, i32, P, i32, P, P]
     L.cqpi_set_josephson.argtypes = [P, i32, dbl, dbl]
     L.cqpi_wannierjosephson.argtypes = [P, P, P, P]
+    L.cqpi_set_threshold.argtypes = [P, dbl, P, i32, ctypes.POINTER(i64)]
+    L.cqpi_wannierldoslist.argtypes = [P, P, P]
     _lib = L
     return L
 
@@ -250,6 +252,16 @@ class Engine:
         et = self.eta if etat is None else etat
         self._check(self._L.cqpi_set_josephson(self._h, int(bool(enable)), float(deltat), float(et)))
 
+    def set_threshold(self, threshold, spinarr=None) -> int:
+        """Proximity-list form of the LDOS (threshold keyword); None or NaN: the full sum.
+        Returns the list's entry count."""
+        c = ctypes.c_int64()
+        thr = float("nan") if threshold is None else float(threshold)
+        sa = None if spinarr is None else np.ascontiguousarray(np.asarray(spinarr, np.int32))
+        self._check(self._L.cqpi_set_threshold(self._h, thr, None if sa is None else _ptr(sa),
+                                               0 if sa is None else len(sa), ctypes.byref(c)))
+        return c.value
+
     def graph_begin(self):
         self._check(self._L.cqpi_graph_begin(self._h))
 
@@ -271,6 +283,11 @@ class Engine:
         tp = np.array([complex(tip).real, complex(tip).imag], np.float64)
         self._check(self._L.cqpi_wannierjosephson(self._h, _ptr(T.view(np.float64)), _ptr(g.view(np.float64)),
                                                   _ptr(tp)))
+
+    def wannierldoslist(self, T, g0r):
+        T = np.ascontiguousarray(np.asarray(T, np.complex128))
+        g = np.ascontiguousarray(np.asarray(g0r, np.complex128))
+        self._check(self._L.cqpi_wannierldoslist(self._h, _ptr(T.view(np.float64)), _ptr(g.view(np.float64))))
 
     def retrieve_result(self):
         out = np.empty((self.wn, self.wn), np.float64)

@@ -136,13 +136,30 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
 
 // The tensor-core contraction runs (mixed precision, a plan exists, not in Josephson mode:
 // that mode uses the CUDA-core kernel with its hole-block columns and complex tip factor).
-bool tc_active(const cqpi_handle *h) { return h->use_tc && !h->josephson; }
+bool tc_active(const cqpi_handle *h) { return h->use_tc && !h->josephson && !h->list_mode; }
+
+// The proximity-list contraction runs (threshold set; the Josephson mode ignores the list,
+// as src/calcqpi.cc:705-709 does).
+bool list_active(const cqpi_handle *h) { return h->list_mode && !h->josephson; }
+
+// term1 of an energy batch: the list form or the full window form.
+void do_term1(cqpi_handle *h, int ne)
+{
+    if (list_active(h))
+        launch_term1_list(h, ne, h->precision == CQPI_PREC_FP64 ? (const void *)h->ws.box : (const void *)h->ws.box32,
+                          h->ws.term1);
+    else
+        launch_term1(h, ne);
+}
 
 // tmp32: float buffer of ne*nimp maps used when only float64 maps are requested from the
 // tensor-core contraction (which writes float32).
 void launch_contraction(cqpi_handle *h, int ne, float *o32, double *o64, float *tmp32)
 {
-    if (h->precision == CQPI_PREC_FP64) {
+    if (list_active(h)) {
+        if (h->precision == CQPI_PREC_FP64) launch_ldos_list(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
+        else launch_ldos_list(h, ne, h->ws.box32, h->ws.T32, h->ws.term1, o32, o64);
+    } else if (h->precision == CQPI_PREC_FP64) {
         launch_ldos_fp64(h, ne, h->ws.box, h->ws.T, h->ws.term1, o32, o64);
     } else if (tc_active(h)) {
         float *dst = o32 ? o32 : tmp32;
@@ -368,7 +385,7 @@ void sr_drop(cqpi_handle *h)
 bool sr_active(const cqpi_handle *h)
 {
     const char *f = getenv("CQPI_SPIN_REDUCE");
-    return h->sr_model && h->sr_orb && h->sr_v && !h->josephson && !(f && !strcmp(f, "0"));
+    return h->sr_model && h->sr_orb && h->sr_v && !h->josephson && !h->list_mode && !(f && !strcmp(f, "0"));
 }
 
 // Create (or re-create) the mb-band handle of the reduction; shares this handle's stream.
@@ -459,6 +476,103 @@ void do_greens(cqpi_handle *h, int ne, const double *d_energies)
     check_launch();
     launch_fft(h, ne);
     check_launch();
+}
+
+// mkthresholdlist (src/qpi.cc:139-253) over the handle's orbitals: the entries (d1, d2, q,
+// o1, o2, f) with |f| = |phi_o1 phi_o2| > threshold * max phi^2, in the maxband / spin form
+// (orbitals 0 .. maxband-1, or both spin blocks of maxband/2) or the spinarr form (orbitals
+// of equal non-zero label).  Stored on the device CSR by (d1, q), list order kept.
+int build_list(cqpi_handle *h)
+{
+    const int wins = 2 * h->w + 1, os = h->os, xs = os * wins, norb = h->wf_norb, b = h->b;
+    double maxval = 0.0;
+    for (size_t k = 0; k < h->wf_host.size(); k++) maxval = std::max(maxval, h->wf_host[k] * h->wf_host[k]);
+    const double thr = h->list_threshold * maxval;
+    struct Ent {
+        int d1, q, d2, o1, o2;
+        double f;
+    };
+    std::vector<Ent> ents;
+    auto wfv = [&](int o, int x, int y) { return h->wf_host[((size_t)o * xs + x) * xs + y]; };
+    auto push = [&](int xn1, int yn1, int xn2, int yn2, int i, int j, int o1, int o2) {
+        const int x = i + (wins - 1) * os, y = j + (wins - 1) * os;
+        const double f = wfv(o1, x - xn1 * os, y - yn1 * os) * wfv(o2, x - xn2 * os, y - yn2 * os);
+        if (std::fabs(f) > thr) ents.push_back({xn1 * wins + yn1, i * os + j, xn2 * wins + yn2, o1, o2, f});
+    };
+    const int maxband = h->m, spinbands = maxband >> 1;
+    for (int xn1 = 0; xn1 < wins; xn1++)
+        for (int yn1 = 0; yn1 < wins; yn1++)
+            for (int xn2 = 0; xn2 < wins; xn2++)
+                for (int yn2 = 0; yn2 < wins; yn2++) {
+                    if (h->list_use_spinarr) {
+                        for (int o1 = 0; o1 < norb; o1++) {
+                            if (!h->list_spinarr[o1]) continue;
+                            for (int o2 = 0; o2 < norb; o2++) {
+                                if (h->list_spinarr[o1] != h->list_spinarr[o2]) continue;
+                                for (int i = 0; i < os; i++)
+                                    for (int j = 0; j < os; j++) push(xn1, yn1, xn2, yn2, i, j, o1, o2);
+                            }
+                        }
+                    } else if (h->spin) {
+                        for (int o1 = 0; o1 < spinbands; o1++)
+                            for (int o2 = 0; o2 < spinbands; o2++)
+                                for (int i = 0; i < os; i++)
+                                    for (int j = 0; j < os; j++) {
+                                        push(xn1, yn1, xn2, yn2, i, j, o1, o2);
+                                        push(xn1, yn1, xn2, yn2, i, j, spinbands + o1, spinbands + o2);
+                                    }
+                    } else {
+                        for (int o1 = 0; o1 < maxband; o1++)
+                            for (int o2 = 0; o2 < maxband; o2++)
+                                for (int i = 0; i < os; i++)
+                                    for (int j = 0; j < os; j++) push(xn1, yn1, xn2, yn2, i, j, o1, o2);
+                    }
+                }
+    std::vector<int> pidx((size_t)b * b, -1);
+    std::vector<int2> pairs;
+    for (const Ent &e : ents) {
+        if (e.o1 >= b || e.o2 >= b) return fail(h, CQPI_ERR_ARG, "a proximity-list orbital is beyond the band count");
+        int &p = pidx[(size_t)e.o1 * b + e.o2];
+        if (p < 0) {
+            p = (int)pairs.size();
+            pairs.push_back(make_int2(e.o1, e.o2));
+        }
+    }
+    const int npair = std::max<int>(1, (int)pairs.size());
+    if (pairs.empty()) pairs.push_back(make_int2(0, 0));
+    const size_t nseg = (size_t)h->W * h->Q;
+    std::vector<int> off(nseg + 1, 0), u(std::max<size_t>(ents.size(), 1), 0);
+    std::vector<double> f(std::max<size_t>(ents.size(), 1), 0.0);
+    for (const Ent &e : ents) off[(size_t)e.d1 * h->Q + e.q + 1]++;
+    for (size_t k = 0; k < nseg; k++) off[k + 1] += off[k];
+    std::vector<int> pos(off.begin(), off.end() - 1);
+    for (const Ent &e : ents) {
+        const int s = pos[(size_t)e.d1 * h->Q + e.q]++;
+        u[s] = e.d2 * npair + pidx[(size_t)e.o1 * b + e.o2];
+        f[s] = e.f;
+    }
+    std::vector<float> f32(f.begin(), f.end());
+    h->list_npair = npair;
+    h->list_count = (int64_t)ents.size();
+    if (list_smem_bytes(h, true) > 227 * 1024)   // the FP64 form (also the seam's)
+        return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list: window, bands and pairs exceed the shared memory of a block");
+    dfree(h->d_list_off);
+    dfree(h->d_list_u);
+    dfree(h->d_list_f);
+    dfree(h->d_list_f32);
+    dfree(h->d_list_pair);
+    dalloc(&h->d_list_off, off.size());
+    dalloc(&h->d_list_u, u.size());
+    dalloc(&h->d_list_f, f.size());
+    dalloc(&h->d_list_f32, f32.size());
+    dalloc(&h->d_list_pair, pairs.size());
+    CK(cudaMemcpy(h->d_list_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_u, u.data(), sizeof(int) * u.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_f, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_f32, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_pair, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice));
+    CK(configure_list(h));
+    return CQPI_OK;
 }
 
 }  // namespace
@@ -691,6 +805,11 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_seam_T);
     dfree(h->d_seam_term1);
     dfree(h->d_seam_tip);
+    dfree(h->d_list_off);
+    dfree(h->d_list_u);
+    dfree(h->d_list_f);
+    dfree(h->d_list_f32);
+    dfree(h->d_list_pair);
     dfree(h->d_V);
     dfree(h->d_status);
     dfree(h->d_seam_ldos);
@@ -765,6 +884,23 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
         return cuda_fail(h, e);
     }
     h->orbitals_ready = true;
+    // host copy for the proximity list (zero orbitals as zeros, src/wannierfunctions.cc)
+    {
+        const size_t n2 = (size_t)side * side;
+        h->wf_host.assign(wf, wf + (size_t)norb * n2);
+        h->wf_norb = norb;
+        if (is_zero)
+            for (int o = 0; o < norb; o++)
+                if (is_zero[o]) std::fill(h->wf_host.begin() + o * n2, h->wf_host.begin() + (o + 1) * n2, 0.0);
+    }
+    if (h->list_mode) {
+        try {
+            const int rc = build_list(h);
+            if (rc != CQPI_OK) return rc;
+        } catch (const CudaError &e) {
+            return cuda_fail(h, e);
+        }
+    }
     // spin reduction: the two spin blocks carry the same orbitals
     h->sr_orb = false;
     if (h->spin && h->nblk == 2 && norb >= 2 * h->mb) {
@@ -917,7 +1053,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             const int t1 = record(h);
             launch_tmatrix(h, ne);
             check_launch();
-            launch_term1(h, ne);
+            do_term1(h, ne);
             check_launch();
             const int t2 = record(h);
             float *o32 = maps32 ? (on_device ? maps32 + (size_t)e0 * per_e : s32) : nullptr;
@@ -1002,7 +1138,7 @@ int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32
             const int t1 = record(h);
             launch_tmatrix(h, ne);
             check_launch();
-            launch_term1(h, ne);
+            do_term1(h, ne);
             check_launch();
             const int t2 = record(h);
             CK(launch_ldos_tc(h, ne, maps, h->d_fov + (size_t)e0 * h->nimp, h->d_fov_off + (size_t)e0 * h->nimp));
@@ -1041,7 +1177,7 @@ int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *bes
         if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
         do_greens(h, ne, h->d_energies_all);
         launch_tmatrix(h, ne);
-        launch_term1(h, ne);
+        do_term1(h, ne);
         check_launch();
         float ms = 0.f;
         int n = 0;
@@ -1153,6 +1289,7 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
     if (nE < 0 || (nE > 0 && (!energies || !dL_dmaps))) return fail(h, CQPI_ERR_ARG, "invalid energies or map gradient");
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
     if (h->josephson) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: Josephson mode is not supported");
+    if (h->list_mode) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: the proximity-list form is not supported");
     if (h->nblk != 1) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: spin blocks are not supported");
     if (h->kp & (h->kp - 1)) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: kpoints must be a power of two");
     if (h->Q > 128) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: oversamp^2 must be <= 128");
@@ -1296,7 +1433,7 @@ int cqpi_get_tmatrix(cqpi_handle *h, double energy, double *T)
 
 // One energy through the FP64 contraction with a given T-matrix and full G0(R) grid; tip
 // selects the Josephson form (tmatrix::calcwannierjosephson) when not NULL.
-static int seam_contract(cqpi_handle *h, const double *T, const double *g0r, const double *tip)
+static int seam_contract(cqpi_handle *h, const double *T, const double *g0r, const double *tip, bool list)
 {
     if (!h || !T || !g0r) return fail(h, CQPI_ERR_ARG, "null argument");
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
@@ -1325,9 +1462,18 @@ static int seam_contract(cqpi_handle *h, const double *T, const double *g0r, con
         const int saved = h->nimp;
         h->nimp = 1;
         h->jos_tip = tip ? h->d_seam_tip : nullptr;
-        launch_term1_ptr(h, 1, h->d_seam_box, h->d_seam_term1);
-        check_launch();
-        launch_ldos_fp64(h, 1, h->d_seam_box, h->d_seam_T, h->d_seam_term1, nullptr, h->d_seam_ldos);
+        const int saved_prec = h->precision;
+        h->precision = CQPI_PREC_FP64;   // the seam is FP64 on every handle
+        if (list) {
+            launch_term1_list(h, 1, h->d_seam_box, h->d_seam_term1);
+            check_launch();
+            launch_ldos_list(h, 1, h->d_seam_box, h->d_seam_T, h->d_seam_term1, nullptr, h->d_seam_ldos);
+        } else {
+            launch_term1_ptr(h, 1, h->d_seam_box, h->d_seam_term1);
+            check_launch();
+            launch_ldos_fp64(h, 1, h->d_seam_box, h->d_seam_T, h->d_seam_term1, nullptr, h->d_seam_ldos);
+        }
+        h->precision = saved_prec;
         h->jos_tip = nullptr;
         h->nimp = saved;
         check_launch();
@@ -1341,14 +1487,54 @@ static int seam_contract(cqpi_handle *h, const double *T, const double *g0r, con
 int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r)
 {
     if (h && h->josephson) return fail(h, CQPI_ERR_STATE, "Josephson mode is on: use cqpi_wannierjosephson");
-    return seam_contract(h, T, g0r, nullptr);
+    if (h && h->list_mode) return fail(h, CQPI_ERR_STATE, "a proximity list is set: use cqpi_wannierldoslist");
+    return seam_contract(h, T, g0r, nullptr, false);
+}
+
+int cqpi_wannierldoslist(cqpi_handle *h, const double *T, const double *g0r)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (!h->list_mode) return fail(h, CQPI_ERR_STATE, "cqpi_set_threshold has not been called");
+    return seam_contract(h, T, g0r, nullptr, true);
+}
+
+int cqpi_set_threshold(cqpi_handle *h, double threshold, const int32_t *spinarr, int32_t nspinarr, int64_t *count)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (threshold != threshold) {   // NaN: the full window sum (the reference's default)
+        h->list_mode = false;
+        if (count) *count = 0;
+        return CQPI_OK;
+    }
+    if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
+    if (h->Q > 512) return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list: oversamp^2 must be <= 512");
+    if (nspinarr < 0 || (nspinarr > 0 && !spinarr)) return fail(h, CQPI_ERR_ARG, "invalid spinarr");
+    h->list_threshold = threshold;
+    h->list_use_spinarr = spinarr != nullptr;
+    // spinarr.resize(orbitals, 0) (src/qpi.cc:217)
+    h->list_spinarr.assign(h->wf_norb, 0);
+    for (int i = 0; i < std::min<int>(nspinarr, h->wf_norb); i++) h->list_spinarr[i] = spinarr[i];
+    h->list_mode = true;
+    try {
+        const int rc = build_list(h);
+        if (rc != CQPI_OK) {
+            h->list_mode = false;
+            return rc;
+        }
+    } catch (const CudaError &e) {
+        h->list_mode = false;
+        return cuda_fail(h, e);
+    }
+    if (count) *count = h->list_count;
+    return CQPI_OK;
 }
 
 int cqpi_wannierjosephson(cqpi_handle *h, const double *T, const double *g0r, const double *tip)
 {
     if (!h || !tip) return fail(h, CQPI_ERR_ARG, "null argument");
     if (!h->josephson) return fail(h, CQPI_ERR_STATE, "cqpi_set_josephson has not been called");
-    return seam_contract(h, T, g0r, tip);
+    return seam_contract(h, T, g0r, tip, false);
 }
 
 int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat)

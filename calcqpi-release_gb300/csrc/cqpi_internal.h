@@ -186,6 +186,22 @@ struct cqpi_handle {
     double2 *d_tip_all = nullptr, *h_tip_pinned = nullptr;
     const double2 *jos_tip = nullptr;
     double2 *d_seam_tip = nullptr;
+    // proximity-list form of the wannier mode (threshold keyword, mkthresholdlist +
+    // tmatrix::calcwannierldos(os, w, flaglist)): host copy of the orbitals the list is built
+    // from, the list's parameters, and the list on the device, CSR by (d1, q): entry s holds
+    // u = d2 * npair + pair index and the factor f; pairs are the (o1, o2) the list uses
+    std::vector<double> wf_host;
+    int wf_norb = 0;
+    bool list_mode = false;
+    double list_threshold = 0.0;
+    std::vector<int32_t> list_spinarr;
+    bool list_use_spinarr = false;
+    int list_npair = 0;
+    int64_t list_count = 0;
+    int *d_list_off = nullptr, *d_list_u = nullptr;
+    double *d_list_f = nullptr;
+    float *d_list_f32 = nullptr;
+    int2 *d_list_pair = nullptr;
     // narrow seam (always FP64)
     double *d_seam_ldos = nullptr;
     double2 *d_seam_box = nullptr, *d_seam_T = nullptr;
@@ -240,6 +256,12 @@ void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vect
 void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorkspace &aw);
 void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw);
 void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
+// ldos_list.cu
+size_t list_smem_bytes(const cqpi_handle *h, bool fp64);
+cudaError_t configure_list(cqpi_handle *h);
+void launch_term1_list(cqpi_handle *h, int ne, const void *box, double *term1);
+void launch_ldos_list(cqpi_handle *h, int ne, const void *box, const void *T, const double *term1, float *o32,
+                      double *o64);
 cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out, const int *fov = nullptr,
                            const long long *fov_off = nullptr);
 bool tc_window_usable(const cqpi_handle *h);   // the direct-window kernel runs (per-map FOV support)

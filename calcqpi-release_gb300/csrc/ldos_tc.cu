@@ -1465,7 +1465,7 @@ bool tc_window_usable(const cqpi_handle *h)
 {
     const char *force = getenv("CQPI_TC_PIPE");
     const char *fw = getenv("CQPI_TC_WINDOW");
-    return h->use_tc && !h->josephson && h->tc.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0")) &&
+    return h->use_tc && !h->josephson && !h->list_mode && h->tc.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0")) &&
            h->tc.w_smem + 8 * (size_t)h->tc.wEB * h->nimp * h->b * h->b <= 227 * 1024;
 }
 

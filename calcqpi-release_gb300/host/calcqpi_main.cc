@@ -8,8 +8,9 @@
 // (:483-518) or analytic orbitals (:519-576), wffile output (:602-618), the map
 // idl(os*n, os*n, layers, 2, 2, lenergy, henergy, 0, -1, -1) with its comment line
 // (:640-656), layer energies idl::getbias (src/idl.cc:969-973) and the final save
-// (:779-783).  Modes and keywords outside that path (spf, uspf, nomode,
-// green=surface|bulk, threshold lists, XSF orbitalfiles, bsfile, dosfile) stop with
+// (:779-783), the proximity list of the threshold / spinarr keywords (:238, :619-635,
+// :700-701).  Modes and keywords outside that path (spf, uspf, nomode,
+// green=surface|bulk, XSF orbitalfiles, bsfile, dosfile) stop with
 // an explicit "not supported" error instead of being ignored.
 #include <unistd.h>
 #include <pwd.h>
@@ -137,7 +138,7 @@ void help()
               << " lattice (201), oversamp (4), energies (-1,1), layers (21), kpoints (=lattice),\n"
               << " green (normal), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
-              << " pos[i], zheight (5.0), idlorbitalfile, deltat (0.001), etat (=eta)\n";
+              << " pos[i], zheight (5.0), idlorbitalfile, deltat (0.001), etat (=eta), threshold, spinarr\n";
 }
 
 double getbias(double lb, double hb, size_t layers, size_t k)
@@ -226,10 +227,9 @@ int main(int argc, char **argv)
     if (lf.has("lattice")) n = lf.ivalue("lattice");
     if (lf.has("oversamp")) oversamp = lf.ivalue("oversamp");
     if (lf.has("window")) window = lf.ivalue("window");
-    if (lf.has("threshold")) {
-        double th = lf.value("threshold");
-        if (!std::isnan(th)) return not_supported(log, "threshold (sparse proximity list)");
-    }
+    // proximity list of the wannier mode (src/calcqpi.cc:238, :619-635, :700-701)
+    double threshold = NAN;
+    if (lf.has("threshold")) threshold = lf.value("threshold");
     if (lf.has("layers")) layers = lf.ivalue("layers");
     if (lf.has("energies")) {
         std::vector<double> e = lf.vec("energies");
@@ -307,8 +307,9 @@ int main(int argc, char **argv)
           << "         Fermi energy         : " << efermi << "\n"
           << "         broadening parameter : " << eta << "\n"
           << "         window               : " << window << "\n"
-          << "         oversamp             : " << oversamp << "\n"
-          << "         Green's function     : normal\n"
+          << "         oversamp             : " << oversamp << "\n";
+        if (!std::isnan(threshold)) l << "         threshold            : " << threshold << "\n";
+        l << "         Green's function     : normal\n"
           << (spin ? "         spin-polarized calculation\n" : "         paramagnetic calculation\n");
         log << l.str();
     }
@@ -488,6 +489,24 @@ int main(int argc, char **argv)
     for (size_t o = 0; o < wfs.size(); o++) std::copy(wfs[o].begin(), wfs[o].end(), wflat.begin() + o * side * side);
     rc = cqpi_set_orbitals(h, wflat.data(), (int32_t)wfs.size(), (int32_t)side, zero.data());
     if (rc == CQPI_OK) rc = cqpi_set_scattering(h, vscat.data());
+    if (rc == CQPI_OK && !std::isnan(threshold)) {
+        log << "Creating threshold list ... done\n";
+        std::vector<int32_t> spinarr;
+        const bool use_spinarr = lf.has("spinarr");
+        if (use_spinarr)
+            for (double v : lf.vec("spinarr")) spinarr.push_back((int32_t)v);
+        int64_t count = 0;
+        rc = cqpi_set_threshold(h, threshold, use_spinarr ? spinarr.data() : nullptr, (int32_t)spinarr.size(), &count);
+        if (rc == CQPI_OK) {
+            const double w1 = 2.0 * window + 1.0;
+            const double entries = w1 * w1 * w1 * w1 * oversamp * oversamp * wfs.size() * wfs.size();
+            std::ostringstream l;
+            l << "Threshold list has " << count << "/" << (size_t)entries << " entries (" << count / entries * 100.0
+              << "%), requiring " << std::fixed << std::setprecision(2)
+              << count * 40.0 / 1024.0 / 1024.0 / 1024.0 << "GB of memory.\n";
+            log << l.str();
+        }
+    }
     if (rc == CQPI_OK && josephson) rc = cqpi_set_josephson(h, 1, deltat, etat);
     if (rc != CQPI_OK) {
         log << "Error: " << cqpi_last_error(h) << "\n";

@@ -144,6 +144,19 @@ int cqpi_graph_launch(cqpi_handle *h);
  * CQPI_ERR_NOT_SUPPORTED.  enable = 0 returns to the LDOS (wannier) mode. */
 int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat);
 
+/* ---- proximity list (threshold keyword, src/calcqpi.cc:238,619-635,700-701) -----------
+ * threshold = NaN: the full window sum (default).  Otherwise builds the reference's list
+ * (mkthresholdlist, src/qpi.cc:139-253) from the orbitals of the last cqpi_set_orbitals call
+ * (and rebuilds it on every later one): the (sub-pixel, d1, d2, o1, o2) terms whose factor
+ * |phi_o1 phi_o2| exceeds threshold * max phi^2 -- orbitals 0 .. maxband-1 (spin: both
+ * blocks of maxband/2), or, with spinarr (nspinarr labels, padded with 0 to the orbital
+ * count), the orbital pairs of equal non-zero label -- and cqpi_run then sums only those
+ * (tmatrix::calcwannierldos(os, w, flaglist)).  *count (may be NULL) receives the entry
+ * count.  oversamp^2 <= 512.  The Josephson mode ignores the list (as the reference's
+ * driver); cqpi_run_fov, cqpi_autotune and cqpi_adjoint return CQPI_ERR_NOT_SUPPORTED while
+ * it is set. */
+int cqpi_set_threshold(cqpi_handle *h, double threshold, const int32_t *spinarr, int32_t nspinarr, int64_t *count);
+
 /* ---- differentiation (extension: the reference computes no derivatives) -----
  * New hopping amplitudes for the terms of the model given to cqpi_create (same order,
  * same R / orbitals / conjugation flags): t[nhops][2].  The eigen cache is rebuilt by
@@ -170,6 +183,10 @@ int cqpi_wannierldos(cqpi_handle *h, const double *T, const double *g0r);
  * energy; needs cqpi_set_josephson(h, 1, ...) first (CQPI_ERR_STATE otherwise), as
  * cqpi_wannierldos needs it off. */
 int cqpi_wannierjosephson(cqpi_handle *h, const double *T, const double *g0r, const double *tip);
+/* GPUQPI::wannierldoslist(scat, g0) (include/gpuqpi.h:25, src/qpicudakernel.cu:624-636): the
+ * proximity-list form (tmatrix::calcwannierldos(os, w, flaglist), src/qpi.cc:1085-1134) with
+ * the list of cqpi_set_threshold; CQPI_ERR_STATE without one. */
+int cqpi_wannierldoslist(cqpi_handle *h, const double *T, const double *g0r);
 /* GPUQPI::retrieveResult(double*) (src/qpicudakernel.cu:690-704): waits and
  * copies the last map, ldos[y][x] float64 (= the reference's ldos[x][y]). */
 int cqpi_retrieve_result(cqpi_handle *h, double *ldos);

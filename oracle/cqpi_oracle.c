@@ -522,3 +522,137 @@ void orc_josephson_tip(double energy, double deltat, double etat, double *tip)
     tip[0] = num * si / d;
     tip[1] = num * sr / d;
 }
+
+/* ---- mkthresholdlist, qpi.cc:139-211 (maxband / spin form) and :213-253 (spinarr form) ----
+ * Entries (list, i, j, o1, o2, factor) of the proximity list: factor = wf_o1(x - xn1 os,
+ * y - yn1 os) wf_o2(x - xn2 os, y - yn2 os), x = i + 2w os, kept when |factor| >
+ * threshold * max_l,x,y wf_l^2.  list = ((xn1 wins + yn1) wins + xn2) wins + yn2 with
+ * wins = 2w+1 (the reference's flags[xn1][yn1][xn2][yn2]); entries come in the
+ * reference's push order, so each list is contiguous.  spinarr (NULL for the maxband form)
+ * has norb entries.  Writes at most cap entries (ent[k][5] int32, fac[k]) and returns the
+ * count.  wf[o][ix][iy] of side (2w+1) os, norb orbitals. */
+int64_t orc_threshold_list(int w, int os, int norb, const double *wf, double threshold, int maxband, int spin,
+                           const int32_t *spinarr, int32_t *ent, double *fac, int64_t cap)
+{
+    size_t wins = (size_t)(2 * w + 1), xs = (size_t)os * wins;
+    double maxval = 0.0;
+    int64_t count = 0;
+#define WFC(o, X, Y) (wf[((size_t)(o) * xs + (size_t)(X)) * xs + (size_t)(Y)])
+    for (int l = 0; l < norb; l++)
+        for (size_t i = 0; i < xs; i++)
+            for (size_t j = 0; j < xs; j++) {
+                double v = WFC(l, i, j) * WFC(l, i, j);
+                if (v > maxval) maxval = v;
+            }
+    if (!maxband) maxband = norb;
+    size_t spinbands = (size_t)(maxband >> 1);
+#define PUSH(L, I, J, O1, O2, F)                                                            \
+    do {                                                                                    \
+        if (count < cap) {                                                                  \
+            int32_t *e_ = ent + 5 * count;                                                  \
+            e_[0] = (int32_t)(L); e_[1] = (int32_t)(I); e_[2] = (int32_t)(J);               \
+            e_[3] = (int32_t)(O1); e_[4] = (int32_t)(O2); fac[count] = (F);                  \
+        }                                                                                   \
+        count++;                                                                            \
+    } while (0)
+    for (size_t xn1 = 0; xn1 < wins; xn1++)
+        for (size_t yn1 = 0; yn1 < wins; yn1++)
+            for (size_t xn2 = 0; xn2 < wins; xn2++)
+                for (size_t yn2 = 0; yn2 < wins; yn2++) {
+                    size_t L = ((xn1 * wins + yn1) * wins + xn2) * wins + yn2;
+                    if (spinarr) {
+                        for (int o1 = 0; o1 < norb; o1++) {
+                            if (!spinarr[o1]) continue;
+                            for (int o2 = 0; o2 < norb; o2++) {
+                                if (spinarr[o1] != spinarr[o2]) continue;
+                                for (size_t i = 0; i < (size_t)os; i++)
+                                    for (size_t j = 0; j < (size_t)os; j++) {
+                                        size_t x = i + (wins - 1) * os, y = j + (wins - 1) * os;
+                                        double f = WFC(o1, x - xn1 * os, y - yn1 * os) * WFC(o2, x - xn2 * os, y - yn2 * os);
+                                        if (fabs(f) > threshold * maxval) PUSH(L, i, j, o1, o2, f);
+                                    }
+                            }
+                        }
+                    } else if (spin) {
+                        for (size_t o1 = 0; o1 < spinbands; o1++)
+                            for (size_t o2 = 0; o2 < spinbands; o2++)
+                                for (size_t i = 0; i < (size_t)os; i++)
+                                    for (size_t j = 0; j < (size_t)os; j++) {
+                                        size_t x = i + (wins - 1) * os, y = j + (wins - 1) * os;
+                                        double f = WFC(o1, x - xn1 * os, y - yn1 * os) * WFC(o2, x - xn2 * os, y - yn2 * os);
+                                        if (fabs(f) > threshold * maxval) PUSH(L, i, j, o1, o2, f);
+                                        size_t s1 = spinbands + o1, s2 = spinbands + o2;
+                                        f = WFC(s1, x - xn1 * os, y - yn1 * os) * WFC(s2, x - xn2 * os, y - yn2 * os);
+                                        if (fabs(f) > threshold * maxval) PUSH(L, i, j, s1, s2, f);
+                                    }
+                    } else {
+                        for (size_t o1 = 0; o1 < (size_t)maxband; o1++)
+                            for (size_t o2 = 0; o2 < (size_t)maxband; o2++)
+                                for (size_t i = 0; i < (size_t)os; i++)
+                                    for (size_t j = 0; j < (size_t)os; j++) {
+                                        size_t x = i + (wins - 1) * os, y = j + (wins - 1) * os;
+                                        double f = WFC(o1, x - xn1 * os, y - yn1 * os) * WFC(o2, x - xn2 * os, y - yn2 * os);
+                                        if (fabs(f) > threshold * maxval) PUSH(L, i, j, o1, o2, f);
+                                    }
+                    }
+                }
+#undef PUSH
+#undef WFC
+    return count;
+}
+
+/* ---- tmatrix::calcwannierldos(os, w, flaglist) (CPU), qpi.cc:1085-1134 ----
+ * The double window sum of orc_wannier_ldos with the proximity list in place of the
+ * orbital / sub-pixel loops: per (d1, d2) only the entries of list (d1, d2) are
+ * accumulated.  ent/fac/nent as written by orc_threshold_list (lists contiguous, in list
+ * order). */
+void orc_wannier_ldos_list(int n, int kp, int b, int os, int w, const double *T, const double *g0r,
+                           int64_t nent, const int32_t *ent, const double *fac, double *ldos,
+                           int row_begin, int row_end)
+{
+    size_t wn = (size_t)os * n, bb = (size_t)b * b, wins = (size_t)(2 * w + 1);
+    size_t nlist = wins * wins * wins * wins;
+    size_t kpoints = (size_t)kp, n2 = (size_t)(n >> 1);
+    int64_t *off = (int64_t *)calloc(nlist + 1, sizeof(int64_t));
+    for (int64_t k = 0; k < nent; k++) off[ent[5 * k] + 1]++;
+    for (size_t l = 0; l < nlist; l++) off[l + 1] += off[l];
+    if (row_end <= 0 || row_end > n) row_end = n;
+    for (int i = row_begin; i < row_end; i++)
+        for (size_t ii = 0; ii < (size_t)os; ii++)
+            for (size_t y = 0; y < wn; y++) ldos[((size_t)i * os + ii) * wn + y] = 0.0;
+#define G0AT(X, Y) (g0r + 2 * (((size_t)(X) * kpoints + (size_t)(Y)) * bb))
+#pragma omp parallel
+    {
+        double *buffer = (double *)malloc(sizeof(double) * 2 * bb);
+        double *cldos = (double *)malloc(sizeof(double) * 2 * bb);
+#pragma omp for collapse(2) schedule(dynamic, 4)
+        for (int i = row_begin; i < row_end; i++)
+            for (int j = 0; j < n; j++) {
+                int ipos = i - (int)n2, jpos = j - (int)n2;
+                for (int nni1 = -w; nni1 <= w; nni1++)
+                    for (int nnj1 = -w; nnj1 <= w; nnj1++) {
+                        zmul(b, T, G0AT((kpoints + kpoints - (size_t)(ipos + nni1)) % kpoints,
+                                        (kpoints + kpoints - (size_t)(jpos + nnj1)) % kpoints), buffer);
+                        for (int nni2 = -w; nni2 <= w; nni2++)
+                            for (int nnj2 = -w; nnj2 <= w; nnj2++) {
+                                zmul(b, G0AT((kpoints + (size_t)(ipos + nni2)) % kpoints,
+                                             (kpoints + (size_t)(jpos + nnj2)) % kpoints), buffer, cldos);
+                                const double *gd = G0AT((kpoints - (size_t)nni1 + (size_t)nni2) % kpoints,
+                                                        (kpoints - (size_t)nnj1 + (size_t)nnj2) % kpoints);
+                                size_t L = (((size_t)(nni1 + w) * wins + (size_t)(nnj1 + w)) * wins + (size_t)(nni2 + w)) * wins
+                                           + (size_t)(nnj2 + w);
+                                for (int64_t k = off[L]; k < off[L + 1]; k++) {
+                                    const int32_t *e = ent + 5 * k;
+                                    size_t ii = (size_t)e[1], jj = (size_t)e[2], o1 = (size_t)e[3], o2 = (size_t)e[4];
+                                    double *out = &ldos[((size_t)i * os + ii) % wn * wn + ((size_t)j * os + jj) % wn];
+                                    *out -= IM(cldos, o2 * b + o1) * fac[k];
+                                    *out -= IM(gd, o2 * b + o1) * fac[k];
+                                }
+                            }
+                    }
+            }
+        free(buffer); free(cldos);
+    }
+#undef G0AT
+    free(off);
+}

@@ -57,6 +57,9 @@ def lib():
             L.orc_wannier_ldos.argtypes = [i32, i32, i32, i32, i32, i32, i32, P, P, P, P, P, i32, i32]
             L.orc_wannier_josephson.argtypes = [i32, i32, i32, i32, i32, i32, P, P, P, P, dbl, dbl, P, i32, i32]
             L.orc_josephson_tip.argtypes = [dbl, dbl, dbl, P]
+            L.orc_threshold_list.argtypes = [i32, i32, i32, P, dbl, i32, i32, P, P, P, i64]
+            L.orc_threshold_list.restype = i64
+            L.orc_wannier_ldos_list.argtypes = [i32, i32, i32, i32, i32, P, P, i64, P, P, P, i32, i32]
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -170,6 +173,37 @@ def wannier_josephson(n, kp, os_, w, spin, T, g0r, wf, tip, wf_zero=None, rows=N
     return out
 
 
+def threshold_list(w, os_, wf, threshold, maxband=0, spin=False, spinarr=None):
+    """mkthresholdlist, src/qpi.cc:139-253: (entries [k][5] int32 = (list, i, j, o1, o2),
+    factors [k]), lists contiguous in the reference's order."""
+    wf = np.ascontiguousarray(wf, dtype=np.float64)
+    sa = None
+    if spinarr is not None:   # spinarr.resize(orbitals, 0), qpi.cc:217
+        sa = np.zeros(wf.shape[0], np.int32)
+        k = min(len(spinarr), wf.shape[0])
+        sa[:k] = np.asarray(spinarr, np.int32)[:k]
+    args = (w, os_, wf.shape[0], _p(wf), float(threshold), int(maxband), int(bool(spin)),
+            None if sa is None else _p(sa))
+    n = lib().orc_threshold_list(*args, None, None, 0)
+    ent = np.zeros((max(n, 1), 5), np.int32)
+    fac = np.zeros(max(n, 1), np.float64)
+    lib().orc_threshold_list(*args, _p(ent), _p(fac), n)
+    return ent[:n], fac[:n]
+
+
+def wannier_ldos_list(n, kp, os_, w, T, g0r, ent, fac, rows=None) -> np.ndarray:
+    """tmatrix::calcwannierldos(os, w, flaglist) (CPU), src/qpi.cc:1085-1134; ldos[x][y]."""
+    b = g0r.shape[2]
+    T = np.ascontiguousarray(T, dtype=np.complex128)
+    g0r = np.ascontiguousarray(g0r, dtype=np.complex128)
+    ent = np.ascontiguousarray(ent, dtype=np.int32)
+    fac = np.ascontiguousarray(fac, dtype=np.float64)
+    out = np.zeros((n * os_, n * os_), np.float64)
+    r0, r1 = (0, n) if rows is None else rows
+    lib().orc_wannier_ldos_list(n, kp, b, os_, w, _p(T), _p(g0r), len(fac), _p(ent), _p(fac), _p(out), r0, r1)
+    return out
+
+
 def set_threads(nt: int):
     lib().orc_set_threads(int(nt))
 
@@ -178,18 +212,26 @@ def num_threads() -> int:
     return int(lib().orc_num_threads())
 
 
-def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=None, spin=False, josephson=None):
+def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=None, spin=False, josephson=None,
+        threshold=None, spinarr=None):
     """The reference's wannier-mode energy loop (src/calcqpi.cc:673-760, normal Green's
     function): eigen once, then per energy G0(k) -> G0(R) -> T -> LDOS.  Returns maps in
     IDL file order [layer][y][x], float64.  josephson=(deltat, etat) runs the driver's
-    josephson mode instead (calcqpi.cc:705-709)."""
+    josephson mode instead (calcqpi.cc:705-709); threshold (and spinarr) the proximity-list
+    form of the wannier mode (calcqpi.cc:619-635,700-701)."""
     m = model.bands if m is None else m
     ev, U = bands(model, kp)
     maps = []
+    if threshold is not None and josephson is None:
+        wz = np.asarray(wf, np.float64) if wf_zero is None else \
+            np.asarray(wf, np.float64) * (1 - np.asarray(wf_zero, np.float64)[:len(wf), None, None])
+        ent, fac = threshold_list(w, os_, wz, threshold, m, spin, spinarr)
     for e in energies:
         g0r = realspace(greens_k(ev, U, kp, e, eta))
         T = tmatrix(vscat, g0r[0, 0])
-        if josephson is not None:
+        if threshold is not None and josephson is None:
+            maps.append(wannier_ldos_list(n, kp, os_, w, T, g0r, ent, fac).T)
+        elif josephson is not None:
             tip = josephson_tip(e, josephson[0], josephson[1])
             maps.append(wannier_josephson(n, kp, os_, w, spin, T, g0r, wf, tip, wf_zero).T)
         else:

@@ -10,10 +10,13 @@
 // idlorbitalfile route, wannierfunctions.cc:489-498) padded with zero orbitals.
 //
 // With a trailing "J deltat etat" it runs the josephson mode instead
-// (src/calcqpi.cc:705-709: per-energy tip factor, tmatrix::calcwannierjosephson).
+// (src/calcqpi.cc:705-709: per-energy tip factor, tmatrix::calcwannierjosephson); with
+// "T threshold" the proximity-list form of the wannier mode (mkthresholdlist with maxband
+// and spin, src/calcqpi.cc:619-630,700-701), with "S threshold k s_0 .. s_k-1" the same
+// with a spinarr (mkthresholdlist(..., spinarr)).
 //
 // usage: refdump <hrfile> <wfbin> <out> n kp os w eta efermi spin maxband layers
-//                lenergy henergy scmodel nscat [vre vim]... [J deltat etat]
+//                lenergy henergy scmodel nscat [vre vim]... [J deltat etat | T thr | S thr k s...]
 // wfbin: int32 norb, int32 side, float64 [norb][side][side]
 // out:   per layer: float64 dos (tmatrix::calcdos), float64 ldos[y][x]
 #include <cstdio>
@@ -50,6 +53,13 @@ int main(int argc, char **argv)
     const int ja = 17 + 2 * nscat;
     const bool josephson = argc >= ja + 3 && string(argv[ja]) == "J";
     const double deltat = josephson ? atof(argv[ja + 1]) : 0.0, etat = josephson ? atof(argv[ja + 2]) : 0.0;
+    const bool listmode = argc >= ja + 2 && (string(argv[ja]) == "T" || string(argv[ja]) == "S");
+    const double threshold = listmode ? atof(argv[ja + 1]) : 0.0;
+    vector<int> spinarr;
+    if (listmode && string(argv[ja]) == "S") {
+        int k = atoi(argv[ja + 2]);
+        for (int i = 0; i < k; i++) spinarr.push_back(atoi(argv[ja + 3 + i]));
+    }
 
     tightbind *model = new tightbind(string(hr), efermi, scmodel);
     if (!*model) { cerr << "model load failed" << endl; return 1; }
@@ -71,6 +81,12 @@ int main(int argc, char **argv)
     tmatrix *tm = new tmatrix(model, n, kp, eta, spin);
     if (scat.size() > 0) tm->setscatteringphase(scat);
     else tm->setscatteringphase(complex<double>(1.0, 0.0));
+    flaglist fls;
+    if (listmode) {
+        size_t count = spinarr.empty() ? mkthresholdlist(fls, wfs, w, os, threshold, maxband, spin)
+                                       : mkthresholdlist(fls, wfs, w, os, threshold, spinarr);
+        cerr << "threshold list entries " << count << endl;
+    }
     idl ldosmap(n * os, n * os, layers, 2.0, 2.0, le, he, 0.0, -1.0, -1.0);
     size_t wn = n * os;
     vector<double> buf(wn * wn);
@@ -86,6 +102,8 @@ int main(int argc, char **argv)
                                               gsl_complex_sqrt(gsl_complex_sub_real(gsl_complex_mul(ocomp, ocomp),
                                                                                     deltat * deltat)));
             tm->calcwannierjosephson(os, w, wfs, tip);
+        } else if (listmode) {
+            tm->calcwannierldos(os, w, fls);
         } else {
             tm->calcwannierldos(os, w, wfs, maxband);
         }

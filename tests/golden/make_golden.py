@@ -115,6 +115,14 @@ CASES = {
     "josephson_spin": dict(model="bdg_spin", scmodel=True, spin=True, magscat=0.1, n=6, kp=12, os=2, w=1,
                            layers=2, energies=(-0.1, 0.07), eta=0.03, scattering=(0.4,), josephson=(0.05, 0.02),
                            orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "threshold_c2": dict(model="c2", n=6, kp=16, os=3, w=2, layers=2, energies=(-0.1, 0.1), eta=0.02,
+                         scattering=(0.3, 0.3, 0.5), threshold=0.05,
+                         orbitals=("analytic", dict(names=["dxz", "dyz", "dxy"], radius=0.4, zheight=0.6))),
+    "threshold_spin": dict(model="c3", n=6, kp=12, os=2, w=1, layers=2, energies=(-0.05, 0.05), eta=0.02,
+                           spin=True, threshold=0.02, orbitals=("idl", "tri5")),
+    "threshold_spinarr": dict(model="c2", n=5, kp=16, os=2, w=1, layers=2, energies=(-0.08, 0.06), eta=0.02,
+                              scattering=(0.3, 0.3, 0.5), threshold=0.0, spinarr=(1, 0, 1),
+                              orbitals=("idl", "t2g3")),
     "wrap": dict(model="c1", n=20, kp=8, os=2, w=1, layers=1, energies=(0.1, 0.1), eta=0.05, scattering=(0.7,),
                  orbitals=("analytic", dict(names=["px"], radius=0.35, zheight=0.4, angle=20.0))),
 }
@@ -146,6 +154,8 @@ def orbital_cube(kind, w, os_):
         return W.tri_orbitals_c3(w, os_)
     if kind == "t2g2":
         return W.t2g_orbitals_c2(w, os_)[:2]
+    if kind == "t2g3":
+        return W.t2g_orbitals_c2(w, os_)
     raise KeyError(kind)
 
 
@@ -178,6 +188,10 @@ def make_case(name, c):
         lines.append(f"phase={fmt_list(c['phase'])};")
     if "scattering" in c:
         lines.append(f"scattering={fmt_list(c['scattering'])};")
+    if "threshold" in c:
+        lines.append(f"threshold={c['threshold']!r};")
+    if "spinarr" in c:
+        lines.append("spinarr=(" + ",".join(str(int(v)) for v in c["spinarr"]) + ");")
     if jos:
         if jos[0] is not None:
             lines.append(f"deltat={jos[0]!r};")
@@ -255,6 +269,11 @@ def make_case(name, c):
             repr(c["energies"][0]), repr(c["energies"][1]), str(int(scmodel)), str(len(vscat))]
     for v in vscat:
         args += [repr(v.real), repr(v.imag)]
+    if "threshold" in c and not jos:
+        if "spinarr" in c:
+            args += ["S", repr(c["threshold"]), str(len(c["spinarr"]))] + [str(int(v)) for v in c["spinarr"]]
+        else:
+            args += ["T", repr(c["threshold"])]
     if jos:
         # the driver's defaults: deltat 0.001, etat = eta (src/calcqpi.cc:137,249-251)
         args += ["J", repr(0.001 if jos[0] is None else jos[0]), repr(c["eta"] if jos[1] is None else jos[1])]

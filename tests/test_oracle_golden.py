@@ -21,7 +21,8 @@ def test_oracle_matches_reference_float64(name):
     m = _model(d, meta)
     E = energies(meta)
     maps = O.run(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], E, ref["vscat"], ref["wf"],
-                 ref["zero"], m=meta["maxband"], spin=meta.get("spin", False), josephson=josephson(meta))
+                 ref["zero"], m=meta["maxband"], spin=meta.get("spin", False), josephson=josephson(meta),
+                 threshold=meta.get("threshold"), spinarr=meta.get("spinarr"))
     err = np.abs(maps - ref["ldos"]).max() / np.abs(ref["ldos"]).max()
     assert err < 1e-10, err
     # tmatrix::calcdos = -sum_i<maxband Im G0(R=0)_ii  (src/qpi.cc:856-862)
@@ -107,3 +108,16 @@ def test_josephson_tip_matches_complex_arithmetic():
             want = 1j * (-np.copysign(1.0, e) * np.pi * dt) / np.sqrt(complex(e, et) ** 2 - dt * dt)
             got = O.josephson_tip(e, dt, et)
             assert abs(got - want) <= 1e-14 * abs(want), (e, dt, et, got, want)
+
+
+@pytest.mark.parametrize("name", [n for n in NAMES if n.startswith("threshold")])
+def test_threshold_list_count_matches_reference_log(name):
+    """mkthresholdlist restated: the entry count the reference's CLI logged."""
+    import re
+    d, meta, ref = load(name)
+    with open(os.path.join(d, "ref_stdout.txt")) as fh:
+        want = int(re.search(r"Threshold list has (\d+)/", fh.read()).group(1))
+    wz = ref["wf"] * (1 - ref["zero"][:len(ref["wf"]), None, None])
+    ent, fac = O.threshold_list(meta["w"], meta["os"], wz, meta["threshold"], meta["maxband"],
+                                meta.get("spin", False), meta.get("spinarr"))
+    assert len(fac) == want
