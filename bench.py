@@ -40,12 +40,32 @@ METRIC = "LDOS pixel*energies/s"
 UNIT = "pixel*energies/s"
 
 
-def ldos_flops_per_pixel_energy(b, m, W, spin):
+def ldos_flops_per_pixel_energy(b, m, W, spin, josephson=False):
     """Algorithmic FLOPs of the factored contraction per pixel*energy:
-    8*W*m_eff*b (u and s, complex x real MACs) + 8*b^2 (T s) + 4*b (Im u.Ts) per spin block."""
+    8*W*m_eff*b (u and s, complex x real MACs) + 8*b^2 (T s) + 4*b (Im u.Ts) per spin block;
+    the Josephson form adds Re u.Ts (4*b) and the tip product (3)."""
     nblk = 2 if spin else 1
     mb = (m >> 1) if spin else m
-    return nblk * (8 * W * mb * b + 8 * b * b + 4 * b)
+    return nblk * (8 * W * mb * b + 8 * b * b + 4 * b + (4 * b + 3 if josephson else 0))
+
+
+def workload_desc(name, c, m, nE):
+    kind = {"C1": "square 1-orbital lattice", "C2": "t2g 3-orbital square lattice",
+            "C3": "triangular 5-orbital x spin lattice", "C5": "t2g 3-orbital square lattice",
+            "CJ": "Josephson mode (output=josephson) on the 6-band BdG t2g square lattice"}.get(name, name)
+    return (f"{name}: {kind}, k-grid {c.kpoints}^2, FOV {c.lattice}^2 sites, {c.oversamp}x{c.oversamp} px/cell, "
+            f"{nE} energies, eta={c.eta}")
+
+
+def make_engine(cqpi, c, m, wf, vscat, prec):
+    """Engine of a workload with its orbitals, scattering and (CJ) Josephson tip."""
+    eng = cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, maxband=c.extra.get("maxband"),
+                      spin=c.spin, precision=prec)
+    eng.set_orbitals(wf)
+    eng.set_scattering(vscat)
+    if "josephson" in c.extra:
+        eng.set_josephson(*c.extra["josephson"])
+    return eng
 
 
 class ClockSampler:
@@ -120,19 +140,27 @@ def cpu_sample(cfg_name, target_s=8.0, threads=None):
     if threads:
         O.set_threads(threads)
     c, m, wf = W.config(cfg_name)
-    om = O.Model(m.bands, m.R, m.orb, m.t)
+    om = O.Model(m.bands, m.R, m.orb, m.t, None, m.efermi, m.scmaxbands)
     ev, U = O.bands(om, c.kpoints)     # once per run in the reference; not part of the sample
     e = float(c.energy_list()[len(c.energy_list()) // 2])
     t0 = time.perf_counter()
     g0r = O.realspace(O.greens_k(ev, U, c.kpoints, e, c.eta))
     T = O.tmatrix(np.array(c.scattering, complex), g0r[0, 0])
     tg = time.perf_counter() - t0
+    jos = c.extra.get("josephson")
+    tip = O.josephson_tip(e, *jos) if jos else None
+
+    def contraction(rows):
+        if jos:   # tmatrix::calcwannierjosephson, src/qpi.cc:953-1033
+            return O.wannier_josephson(c.lattice, c.kpoints, c.oversamp, c.window, c.spin, T, g0r, wf, tip, rows=rows)
+        return O.wannier_ldos(c.lattice, c.kpoints, c.oversamp, c.window, m.bands, c.spin, T, g0r, wf, rows=rows)
+
     t0 = time.perf_counter()
-    O.wannier_ldos(c.lattice, c.kpoints, c.oversamp, c.window, m.bands, c.spin, T, g0r, wf, rows=(0, 2))
+    contraction((0, 2))
     t2 = time.perf_counter() - t0
     rows = int(max(2, min(c.lattice, round(2 * target_s / max(t2, 1e-3)))))
     t0 = time.perf_counter()
-    O.wannier_ldos(c.lattice, c.kpoints, c.oversamp, c.window, m.bands, c.spin, T, g0r, wf, rows=(0, rows))
+    contraction((0, rows))
     tl = time.perf_counter() - t0
     t_energy = tg + tl * c.lattice / rows
     value = c.pixels_per_energy / t_energy
@@ -165,7 +193,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"{args.config} continuum LDOS (reference CPU algorithm, oracle port)"},
+            "config": {"workload": f"{args.config} continuum LDOS (reference CPU algorithm, oracle port)"
+                                   if args.config != "CJ" else
+                                   "CJ Josephson-mode maps (reference CPU algorithm, oracle port)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -201,9 +231,7 @@ def run_ours(args):
     vscat = np.array(c.scattering, complex)
     if len(vscat) < m.bands:
         vscat = np.concatenate([vscat, np.zeros(m.bands - len(vscat), complex)])
-    eng = cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, spin=c.spin, precision=prec)
-    eng.set_orbitals(wf)
-    eng.set_scattering(vscat)
+    eng = make_engine(cqpi, c, m, wf, vscat, prec)
     wn = c.lattice * c.oversamp
     out = torch.empty((nE, 1, wn, wn), dtype=torch.float32, device="cuda")
     stream = torch.cuda.ExternalStream(eng.stream)
@@ -259,7 +287,7 @@ def run_ours(args):
     h2d = t_host.nbytes + wf.nbytes + vscat.nbytes + E.nbytes
     d2h = host_out.nbytes
     e2e_steps = max(1, min(args.steps, 3))
-    e2 = cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, spin=c.spin, precision=prec)
+    e2 = make_engine(cqpi, c, m, wf, vscat, prec)
 
     def e2e_step():
         e2.set_hoppings(t_host)
@@ -283,7 +311,8 @@ def run_ours(args):
 
     # roofline of the dominant kernel (the LDOS contraction)
     peaks, peak_src = measured_peaks()
-    F = ldos_flops_per_pixel_energy(m.bands, m.bands, (2 * c.window + 1) ** 2, c.spin)
+    F = ldos_flops_per_pixel_energy(m.bands, c.extra.get("maxband", m.bands), (2 * c.window + 1) ** 2, c.spin,
+                                    "josephson" in c.extra)
     ldos_ms = stage_acc["ldos"] / args.steps
     achieved = F * work_per_rank / (ldos_ms / 1e3) / 1e12
     if prec == cqpi.PREC_FP64:
@@ -314,33 +343,41 @@ def run_ours(args):
     fp64_info = None
     if prec != cqpi.PREC_FP64 and not args.no_fp64_check:
         sub = np.linspace(0, nE - 1, 5).astype(int)
-        with cqpi.Engine(m, c.lattice, c.kpoints, c.oversamp, c.window, c.eta, spin=c.spin,
-                         precision=cqpi.PREC_FP64) as e64:
-            e64.set_orbitals(wf)
-            e64.set_scattering(vscat)
+        with make_engine(cqpi, c, m, wf, vscat, cqpi.PREC_FP64) as e64:
             ref = e64.run(E[sub], f32=False, f64=True)
             t0 = time.perf_counter()
             e64.solve_bands()
             e64.run(E[sub], f32=False, f64=False)
             t64 = time.perf_counter() - t0
         got = out[sub].double().cpu().numpy()
-        errs = [float(np.abs(got[i, 0] - ref[i, 0]).max() / np.abs(ref[i, 0]).max()) for i in range(len(sub))]
-        rms = [float(np.sqrt(np.mean((got[i, 0] - ref[i, 0]) ** 2) / np.mean(ref[i, 0] ** 2))) for i in range(len(sub))]
+        # per-map relative errors; a map that vanishes to rounding in FP64 (the Josephson map
+        # at E = 0: ~1e-17 of the largest) has no relative error of its own and is reported
+        # against the largest checked map instead
+        gmax = max(float(np.abs(ref[i, 0]).max()) for i in range(len(sub)))
+        live = [i for i in range(len(sub)) if np.abs(ref[i, 0]).max() > 1e-9 * gmax]
+        zero = [i for i in range(len(sub)) if i not in live]
+        errs = [float(np.abs(got[i, 0] - ref[i, 0]).max() / np.abs(ref[i, 0]).max()) for i in live]
+        rms = [float(np.sqrt(np.mean((got[i, 0] - ref[i, 0]) ** 2) / np.mean(ref[i, 0] ** 2))) for i in live]
+        zero_info = {"energies": [float(E[sub][i]) for i in zero],
+                     "max_abs_err_over_largest_map": max([float(np.abs(got[i, 0] - ref[i, 0]).max()) / gmax
+                                                          for i in zero], default=0.0)} if zero else None
         fp64_value = len(sub) * c.pixels_per_energy / t64
         fp64_info = {"max_rel_err_vs_fp64": max(errs), "rms_rel_err_vs_fp64": max(rms),
                      "rel_err_definitions": "max|rho-rho64|/max|rho64| and rms(rho-rho64)/rms(rho64) per map, worst map",
+                     "per_map_max_rel_err": errs,
                      "energies_checked": [float(x) for x in E[sub]],
                      "tolerance": 1e-6, "fp64_path_value": fp64_value, "mixed_over_fp64": value / world / fp64_value}
+        if zero_info:
+            fp64_info["vanishing_maps"] = zero_info
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == cqpi.PREC_FP64 else f"mixed: f64 eigen/T/term1, f32 G0+FFT, {eng.contraction_kind()} contraction",
             "data": "synthetic (seeded model and orbitals)",
-            "config": {"workload": f"{args.config}: t2g 3-orbital square lattice, k-grid {c.kpoints}^2, "
-                                   f"FOV {c.lattice}^2 sites, {c.oversamp}x{c.oversamp} px/cell, {nE} energies, "
-                                   f"eta={c.eta}", "precision": args.precision,
+            "config": {"workload": workload_desc(args.config, c, m, nE), "precision": args.precision,
                        "parallelism": f"replicas x{world}",
-                       "l2": "inputs/outputs larger than L2 (2.6 GB of maps, 168 MB eigen cache per step)"},
+                       "l2": (f"inputs/outputs larger than L2 ({nE * wn * wn * 4 / 1e9:.1f} GB of maps, "
+                              f"{c.kpoints ** 2 * (16 * m.bands ** 2 + 8 * m.bands) / 1e6:.0f} MB eigen cache per step)")},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "roofline": roof}
     if tune is not None:

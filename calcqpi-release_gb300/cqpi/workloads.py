@@ -131,6 +131,34 @@ def t2g_c2(seed: int = 2, sigma: float = 0.25) -> TBModel:
     return _from_terms(terms, 3, "t2g square lattice, seed %d (C2)" % seed)
 
 
+def bdg(base: TBModel, D, name: str = None) -> TBModel:
+    """Bogoliubov-de Gennes form of an electron model for scmodel=true: electron block t(R),
+    hole block -conj(t(R)) (the hole Hamiltonian -H(-k)^*), on-site pairing matrix D between
+    the blocks; Hermitian whenever the electron model is.  Bands 2b, the particle block first."""
+    b = base.bands
+    terms = {}
+    for R, M in base.terms().items():
+        T = np.zeros((2 * b, 2 * b), np.complex128)
+        T[:b, :b] = M
+        T[b:, b:] = -np.conj(M)
+        terms[R] = T
+    T0 = terms.get((0, 0, 0), np.zeros((2 * b, 2 * b), np.complex128)).copy()
+    T0[:b, b:] += D
+    T0[b:, :b] += np.conj(np.asarray(D)).T
+    terms[(0, 0, 0)] = T0
+    m = _from_terms(terms, 2 * b, name or ("BdG " + base.name))
+    m.scmaxbands = b
+    return m
+
+
+def bdg_t2g_c2(seed: int = 2) -> TBModel:
+    """Six-band BdG form of the C2 t2g model with an orbital-dependent on-site pairing
+    (0.04, 0.04, 0.06 eV on the diagonal, 0.01 eV between dxz and dyz)."""
+    D = np.diag([0.04, 0.04, 0.06]).astype(np.complex128)
+    D[0, 1] = D[1, 0] = 0.01
+    return bdg(t2g_c2(seed), D, "BdG t2g square lattice, seed %d (CJ)" % seed)
+
+
 def t2g_c2_parametrisation(seed: int = 2, sigma: float = 0.25):
     """Independent hopping amplitudes of the C2 model family: the symmetrisation of
     t2g_c2 is linear in the raw shell matrices, so every C4-symmetric Hermitian model with
@@ -303,7 +331,7 @@ class Config:
 
 
 def config(name: str) -> tuple:
-    """(Config, TBModel, orbital cube [m, side, side]) for C1, C2, C3 or C5."""
+    """(Config, TBModel, orbital cube [m, side, side]) for C1, C2, C3, C5 or CJ (Josephson)."""
     if name == "C1":
         c = Config("C1", 64, 256, 8, 2, 21, (-0.2, 0.2), 0.005, (0.5,))
         return c, square_c1(), gaussian_c1(c.window, c.oversamp)
@@ -314,6 +342,13 @@ def config(name: str) -> tuple:
         c = Config("C3", 512, 2048, 6, 2, 64, (-0.1, 0.1), 0.001, tuple([1.0] * 10), spin=True)
         orbs = tri_orbitals_c3(c.window, c.oversamp)
         return c, triangular_c3(), np.concatenate([orbs, orbs])
+    if name == "CJ":
+        # Josephson mode (output=josephson) on the BdG form of the C2 model: C2 grid and field of
+        # view, tip gap 1 meV (the reference's default deltat), tip broadening = eta; scattering
+        # duplicated into the hole block with magscat = 0 (src/calcqpi.cc:281-286)
+        c = Config("CJ", 256, 1024, 10, 2, 101, (-0.1, 0.1), 0.002, (0.3, 0.3, 0.5, -0.3, -0.3, -0.5),
+                   extra={"josephson": (0.001, 0.002), "maxband": 3})
+        return c, bdg_t2g_c2(), t2g_orbitals_c2(c.window, c.oversamp)
     if name == "C5":
         c = Config("C5", 128, 1024, 10, 2, 41, (-0.1, 0.1), 0.002, (0.3, 0.3, 0.5))
         return c, t2g_c2(), t2g_orbitals_c2(c.window, c.oversamp)

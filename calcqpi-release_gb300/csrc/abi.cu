@@ -134,9 +134,14 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
     h->ws.ebatch = ebatch;
 }
 
-// The tensor-core contraction runs (mixed precision, a plan exists, not in Josephson mode:
-// that mode uses the CUDA-core kernel with its hole-block columns and complex tip factor).
-bool tc_active(const cqpi_handle *h) { return h->use_tc && !h->josephson && !h->list_mode; }
+// The tensor-core contraction runs: mixed precision with a plan, no proximity list, and in the
+// Josephson mode only through the direct-window kernel (one spin block), whose producer reads
+// the hole-block columns and whose epilogue applies the tip factor; otherwise the CUDA-core
+// kernels run.
+bool tc_active(const cqpi_handle *h)
+{
+    return h->use_tc && !h->list_mode && (!h->josephson || tc_window_usable(h));
+}
 
 // The proximity-list contraction runs (threshold set; the Josephson mode ignores the list,
 // as src/calcqpi.cc:705-709 does).
@@ -1076,6 +1081,7 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
                 CK(cudaEventRecord(h->ev_copy[slot], h->copy_stream));
             }
         }
+        h->jos_tip = nullptr;
         h->status_pending = true;
         if (!on_device) {
             CK(cudaStreamSynchronize(h->copy_stream));
@@ -1132,6 +1138,7 @@ int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32
         for (int e0 = 0; e0 < nE; e0 += eb) {
             const int ne = std::min(eb, nE - e0);
             const double *den = h->d_energies_all + e0;
+            h->jos_tip = h->josephson ? h->d_tip_all + e0 : nullptr;
             if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
             const int t0 = record(h);
             do_greens(h, ne, den);
@@ -1147,6 +1154,7 @@ int cqpi_run_fov(cqpi_handle *h, const double *energies, int32_t nE, const int32
             pend(h, 2, t1, t2);
             pend(h, 3, t2, t3);
         }
+        h->jos_tip = nullptr;
         h->status_pending = true;
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
@@ -1173,6 +1181,7 @@ int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *bes
         ensure_energies(h, nE);
         ensure_stage32(h, (size_t)ne * per_e);
         upload_energies(h, energies, ne);
+        h->jos_tip = h->josephson ? h->d_tip_all : nullptr;
         if (!h->bands_ready) do_bands(h);
         if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
         do_greens(h, ne, h->d_energies_all);
@@ -1181,7 +1190,9 @@ int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *bes
         check_launch();
         float ms = 0.f;
         int n = 0;
-        CK(tc_autotune(h, ne, h->stage32, &ms, &n));
+        const cudaError_t te = tc_autotune(h, ne, h->stage32, &ms, &n);
+        h->jos_tip = nullptr;
+        CK(te);
         if (best_ms) *best_ms = ms;
         if (tried) *tried = n;
         if (const int st = read_status(h)) return status_code(h, st, "autotuning");
@@ -1541,6 +1552,7 @@ int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double eta
 {
     if (!h) return CQPI_ERR_ARG;
     if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    h->jos_tip = nullptr;
     if (!enable) {
         h->josephson = false;
         return CQPI_OK;

@@ -62,6 +62,8 @@ struct TcParams {
     int H, NX, NKC, win_bytes, EB, nraw;   // direct-window variant
     int a_tmem;                  // direct-window variant: Phi operand held in tensor memory
     int stall;                   // fault injection: wait on a barrier nothing arrives on
+    int coff;                    // Josephson mode: column offset of the s operand (bands/2), else 0
+    const double2 *tip;          // Josephson mode: tip factor per energy of the batch, else NULL
     float inv_sA;
     float scale;                 // factor of every map value
     long long spin_limit;

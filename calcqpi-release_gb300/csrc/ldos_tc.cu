@@ -749,7 +749,9 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8])
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 }  // namespace tc
 
-template <int B>
+// JOS: the Josephson form (p.coff, p.tip); a template flag so that the LDOS epilogue keeps
+// its register budget.
+template <int B, bool JOS>
 __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_constant__ TcParams p)
 {
     using namespace tc;
@@ -779,9 +781,10 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     float2 *cT = reinterpret_cast<float2 *>(offR + 2 * NKC * 8);
     float *cInv2 = reinterpret_cast<float *>(cT + EB * p.nimp * bb);
     float *cT1 = cInv2 + EB;
+    float *cTip = cT1 + EB * 128;   // Josephson tip factor (re, im) [energy]
     // producer: source offset (float2 units, -1 outside the box) of every raw-window column
     // of the tile being fetched, [op][energy][x]
-    const size_t ct_off = ((size_t)(reinterpret_cast<unsigned char *>(cT1 + EB * 128) - sm) + 15) & ~(size_t)15;
+    const size_t ct_off = ((size_t)(reinterpret_cast<unsigned char *>(cTip + 2 * EB) - sm) + 15) & ~(size_t)15;
     long long *colTab = reinterpret_cast<long long *>(sm + ct_off);
     const size_t mb_off = ct_off + 8 * (size_t)(2 * EB * NX);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + mb_off);   // [8]
@@ -798,13 +801,14 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             for (int i = tid; i < nv; i += NW) dst[i] = src[i];
         }
         // K entry r = dy*orbitals + o of a window row -> float offset inside a raw column
-        // (u: element [o][a] at Y-offset dy; s: element [a][o] at the reflected Y-offset)
+        // (u: element [o][a] at Y-offset dy; s: element [a][o + coff] at the reflected
+        // Y-offset, coff = bands/2 in the Josephson mode: the hole-block column)
         for (int i = tid; i < 2 * NKC * 8; i += NW) {
             const int op = i >= NKC * 8, r = i - op * NKC * 8;
             int v = -1;
             if (r < nval) {
                 const int dyw = r / p.mb, o = p.bs0 + r % p.mb;
-                v = op == 0 ? 2 * (dyw * bb + o * p.b) : 2 * ((2 * p.w - dyw) * bb + o);
+                v = op == 0 ? 2 * (dyw * bb + o * p.b) : 2 * ((2 * p.w - dyw) * bb + o + p.coff);
             }
             offR[i] = v;
         }
@@ -1067,6 +1071,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
         const int nb = B <= 4 ? B : p.b;                          // bands; a constant for B <= 4
         const int ncombo = EB * (TS >> 2);                        // (energy, 4-site group) pairs per tile
+        constexpr bool jos = JOS;                                 // Josephson mode
         // T, the scale and term1 of an energy block, loaded once per block
         auto load_block = [&](int e0) {
             for (int i = tid; i < EB * p.nimp * bb; i += TCW_EPI) {
@@ -1081,6 +1086,9 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                 const int e = e0 + tid;
                 const float inv = e < p.ne ? p.inv_sA / pow2_scale(p.gmax[e]) : 0.f;
                 cInv2[tid] = inv * inv;
+                const double2 tp = (p.tip && e < p.ne) ? p.tip[e] : make_double2(0.0, 0.0);
+                cTip[2 * tid] = (float)tp.x;
+                cTip[2 * tid + 1] = (float)tp.y;
             }
             bar_sync_group<1, TCW_EPI>();
         };
@@ -1105,7 +1113,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                         }
                     }
                     tmem_wait_ld();
-                    float term2[4] = {0.f, 0.f, 0.f, 0.f};
+                    float term2[4] = {0.f, 0.f, 0.f, 0.f}, term2r[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                     for (int a = 0; a < B; a++) {
                         if (a >= nb) continue;
@@ -1122,6 +1130,16 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                         }
 #pragma unroll
                         for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
+                        if (jos) {
+#pragma unroll
+                            for (int u = 0; u < 4; u++) term2r[u] += ur[2 * a][u] * tsr[u] - ur[2 * a + 1][u] * tsi[u];
+                        }
+                    }
+                    if (jos) {
+                        // Im(tip * sum u T s) (tmatrix::calcwannierjosephson, src/qpi.cc:986-990)
+                        const float tx = cTip[2 * ee], ty = cTip[2 * ee + 1];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) term2[u] = tx * term2[u] + ty * term2r[u];
                     }
                     // pixel (qx, qy) of sites i0+s0 .. i0+s0+3 of row j, straight to the map
                     if (qvalid && p.fov) {
@@ -1266,7 +1284,7 @@ bool window_config(const cqpi_handle *h, int EB, int H, int nraw, TcPlan &pl)
     // shared memory with Phi in shared memory (the larger of the two layouts); the
     // per-impurity epilogue constants are added at launch
     const size_t smem = 2 * (size_t)a_bytes + 4 * (size_t)win_bytes + 4 * (nraw * 2 * EB * rawfl + 4) +
-                        4 * (size_t)(2 * NKC * 8) + 4 * (size_t)EB * (1 + 128) + 16 + 8 * (size_t)(2 * EB * NX) + 9 * 8 + 16;
+                        4 * (size_t)(2 * NKC * 8) + 4 * (size_t)EB * (3 + 128) + 16 + 8 * (size_t)(2 * EB * NX) + 9 * 8 + 16;
     if (smem > 211 * 1024) return false;
     pl.wNKC = NKC; pl.wKP = KP; pl.w_a_bytes = a_bytes;
     pl.wNRAW = nraw; pl.wEB = EB; pl.wH = H; pl.wNX = NX; pl.w_win_bytes = win_bytes; pl.w_sst = sst;
@@ -1400,6 +1418,8 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
     p.fov = fov;
     p.fov_off = fov_off;
     p.status = h->d_status;
+    p.coff = h->josephson ? h->b >> 1 : 0;
+    p.tip = h->josephson ? h->jos_tip : nullptr;
     const char *force = getenv("CQPI_TC_PIPE");
     const bool pipe = pl.pipe && !(force && !strcmp(force, "0"));
     const char *fw = getenv("CQPI_TC_WINDOW");
@@ -1409,6 +1429,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
     const long long ntiles = (long long)ne * h->n * p.ntx;
     cudaError_t err;
     if (fov && !win) return cudaErrorInvalidValue;   // per-map fields of view need the window kernel
+    if (h->josephson && (!win || !h->jos_tip)) return cudaErrorInvalidValue;   // so does the Josephson form
     if (win) {
         p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB; p.nraw = pl.wNRAW;
         p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
@@ -1418,11 +1439,24 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
         p.a_tmem = pl.w_a_tmem && fa && !strcmp(fa, "1") ? 1 : 0;   // Phi in tensor memory: opt-in
         p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_aw);
         const size_t smem = pl.w_smem + 8 * (size_t)p.EB * h->nimp * h->b * h->b;
-        err = cudaFuncSetAttribute(ldos_tcw_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (err != cudaSuccess) return err;
         const long long nt = (long long)((ne + p.EB - 1) / p.EB) * h->n * p.ntx;
         const int grid = (int)std::min<long long>(nt, (long long)h->num_sms);
-        ldos_tcw_kernel<B><<<grid, TCW_THREADS, smem, h->stream>>>(p);
+        if (h->josephson) {
+            // Bogoliubov-de Gennes models have an even band count
+            if constexpr (B % 2 == 0) {
+                err = cudaFuncSetAttribute(ldos_tcw_kernel<B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+                if (err != cudaSuccess) return err;
+                ldos_tcw_kernel<B, true><<<grid, TCW_THREADS, smem, h->stream>>>(p);
+            } else {
+                return cudaErrorInvalidValue;
+            }
+        } else {
+            err = cudaFuncSetAttribute(ldos_tcw_kernel<B, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+            if (err != cudaSuccess) return err;
+            ldos_tcw_kernel<B, false><<<grid, TCW_THREADS, smem, h->stream>>>(p);
+        }
         h->launches++;
         return cudaGetLastError();
     }
@@ -1465,7 +1499,7 @@ bool tc_window_usable(const cqpi_handle *h)
 {
     const char *force = getenv("CQPI_TC_PIPE");
     const char *fw = getenv("CQPI_TC_WINDOW");
-    return h->use_tc && !h->josephson && !h->list_mode && h->tc.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0")) &&
+    return h->use_tc && !h->list_mode && h->tc.win && h->d_tc_aw && !(fw && !strcmp(fw, "0")) && !(force && !strcmp(force, "0")) &&
            h->tc.w_smem + 8 * (size_t)h->tc.wEB * h->nimp * h->b * h->b <= 227 * 1024;
 }
 

@@ -139,9 +139,10 @@ int cqpi_graph_launch(cqpi_handle *h);
  * every map is -Im(tip(E) * ...) with the driver's per-energy tip factor
  *   tip(E) = (0, -sign(E) pi deltat) / sqrt((E + i etat)^2 - deltat^2).
  * Needs an even band count and maxband = bands/2 (CQPI_ERR_ARG otherwise); the driver's
- * defaults are deltat = 0.001 and etat = eta.  In this mode the mixed path contracts on
- * FP32 CUDA cores; cqpi_run_fov, cqpi_autotune and cqpi_adjoint return
- * CQPI_ERR_NOT_SUPPORTED.  enable = 0 returns to the LDOS (wannier) mode. */
+ * defaults are deltat = 0.001 and etat = eta.  In this mode the mixed path contracts on the
+ * tensor cores (direct-window kernel, one spin block) or else on FP32 CUDA cores;
+ * cqpi_adjoint returns CQPI_ERR_NOT_SUPPORTED.  enable = 0 returns to the LDOS (wannier)
+ * mode. */
 int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat);
 
 /* ---- proximity list (threshold keyword, src/calcqpi.cc:238,619-635,700-701) -----------

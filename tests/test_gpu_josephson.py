@@ -56,7 +56,8 @@ def test_josephson_mixed_matches_reference(built_lib, name):
     for k in range(len(got)):
         err = np.abs(got[k] - ref["ldos"][k]).max() / np.abs(ref["ldos"][k]).max()
         assert err <= 1e-6, (k, err)
-    assert eng.contraction_kind() == "fp32"
+    # one spin block: the tcgen05 direct-window kernel; two: FP32 CUDA cores
+    assert eng.contraction_kind() == ("fp32" if meta.get("spin") else "tcgen05")
     eng.close()
 
 
@@ -124,4 +125,67 @@ def test_josephson_errors(built_lib):
     with pytest.raises(cqpi.CqpiError) as ex:
         eng.wannierldos(np.eye(m.bands), np.zeros((meta["kp"], meta["kp"], m.bands, m.bands)))
     assert ex.value.code == cqpi.ERR_STATE
+    eng.close()
+
+
+def _bdg_c2_engine(precision, lattice=24, kpoints=256, contraction=None, monkeypatch=None):
+    import cqpi
+    from cqpi import workloads as W
+    if contraction:
+        monkeypatch.setenv("CQPI_CONTRACTION", contraction)
+    c, m, wf = W.config("CJ")
+    eng = cqpi.Engine(m, lattice, kpoints, c.oversamp, c.window, 0.01, maxband=3, precision=precision)
+    eng.set_orbitals(wf)
+    eng.set_scattering(np.array(c.scattering, complex))
+    eng.set_josephson(0.001, 0.01)
+    if contraction:
+        monkeypatch.delenv("CQPI_CONTRACTION")
+    return eng
+
+
+def test_josephson_tensor_cores_on_bdg_t2g(built_lib, monkeypatch):
+    """6-band BdG t2g model, C2 orbitals and window: the tcgen05 Josephson contraction against
+    the FP64 engine (1e-6) and against the FP32 CUDA-core kernel.  (At E = 0 this model's
+    Josephson map vanishes to rounding, ~1e-18, so a relative bar is meaningless there.)"""
+    import cqpi
+    E = np.array([-0.08, -0.02, 0.006, 0.03, 0.09])
+    e64 = _bdg_c2_engine(cqpi.PREC_FP64)
+    ref = e64.run(E, f32=False, f64=True)
+    e64.close()
+    tc = _bdg_c2_engine(cqpi.PREC_MIXED)
+    assert tc.contraction_kind() == "tcgen05"
+    got = tc.run(E, f32=False, f64=True)
+    tc.close()
+    f32 = _bdg_c2_engine(cqpi.PREC_MIXED, contraction="fp32", monkeypatch=monkeypatch)
+    assert f32.contraction_kind() == "fp32"
+    g32 = f32.run(E, f32=False, f64=True)
+    f32.close()
+    for e in range(len(E)):
+        scale = np.abs(ref[e, 0]).max()
+        assert np.abs(got[e, 0] - ref[e, 0]).max() <= 1e-6 * scale, (E[e], np.abs(got[e, 0] - ref[e, 0]).max() / scale)
+        assert np.abs(g32[e, 0] - ref[e, 0]).max() <= 1e-6 * scale
+
+
+def test_josephson_fields_of_view_crop_full_maps(built_lib):
+    """cqpi_run_fov in the Josephson mode: every map equals the centred crop of cqpi_run's."""
+    import cqpi
+    import torch
+    E = np.array([-0.05, 0.04])
+    eng = _bdg_c2_engine(cqpi.PREC_MIXED)
+    full = eng.run(E, f32=True, f64=False)
+    fov = np.array([[8], [16]], np.int32)
+    os_ = 10
+    tot = int(sum((f * os_) ** 2 for f in fov.reshape(-1)))
+    buf = torch.zeros(tot, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    eng.run_fov(E, fov, buf.data_ptr())
+    eng.synchronize()
+    flat = buf.cpu().numpy()
+    off, n = 0, 24
+    for k, f in enumerate(fov.reshape(-1)):
+        w = f * os_
+        got = flat[off:off + w * w].reshape(w, w)
+        lo = (n // 2 - f // 2) * os_
+        assert np.array_equal(got, full[k, 0, lo:lo + w, lo:lo + w])
+        off += w * w
     eng.close()
