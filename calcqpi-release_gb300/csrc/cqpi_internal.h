@@ -249,6 +249,7 @@ void launch_ldos_fp32(cqpi_handle *h, int ne, const float2 *box, const float2 *T
 bool fft32_supported(const cqpi_handle *h);
 cudaError_t configure_fft32(cqpi_handle *h);
 void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies);
+bool launch_fft32_planes(cqpi_handle *h, int ne);
 // ldos_tc.cu
 bool tc_supported(const cqpi_handle *h);
 void tc_plan(cqpi_handle *h);

@@ -339,6 +339,55 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
     }
 }
 
+// Pass 1 of the unfused mixed path (more than 4 bands: G0(k) planes already in HBM, written
+// by greens_k_kernel): RPC rows r = (energy * b^2 + plane) * kp + i per CTA, loaded with
+// coalesced row reads, then the four-step register transform along j and the pruned stores
+// of g0_rowfft_reg_kernel.  HBM-bound: one read of the G0(k) planes, NB / kp of it written.
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) rowfft_reg_g0k_kernel(int NB, int Rb, long long nrows,
+                                                             const float2 *__restrict__ g0k,
+                                                             const float2 *__restrict__ tw, float2 *__restrict__ half)
+{
+    constexpr int KP = N1 * N2;
+    constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
+    constexpr int PLEN = KP + KP / 32 + 1;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tws = sm + (size_t)RPC * PLEN;
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
+    const long long r0 = (long long)blockIdx.x * RPC;
+    for (int idx = threadIdx.x; idx < RPC * KP; idx += blockDim.x) {
+        const int rr = idx / KP, j = idx - rr * KP;
+        if (r0 + rr < nrows) sm[(size_t)rr * PLEN + pad32(j)] = g0k[(size_t)(r0 + rr) * KP + j];
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < RPC * N1; task += blockDim.x) {
+        const int q = task / N1, n1 = task - q * N1;
+        float2 *a = sm + (size_t)q * PLEN;
+        float2 x[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
+        fft_reg<N2>(x);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[(n1 * k2) & (KP - 1)]);
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < RPC * N2; task += blockDim.x) {
+        const int q = task / N2, k2 = task - q * N2;
+        if (r0 + q >= nrows) continue;
+        const float2 *a = sm + (size_t)q * PLEN;
+        float2 x[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
+        fft_reg<N1>(x);
+        float2 *dst = half + (size_t)(r0 + q) * NB;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; k1++) {
+            const int yb = (k2 + N2 * k1 + Rb) & (KP - 1);
+            if (yb < NB) dst[yb] = x[k1];
+        }
+    }
+}
+
 // Pass 2 as a four-step register transform (kp = N1 x N2, box no wider than kp): a block
 // takes NC = 256/N1 adjacent columns yb of one (plane, energy), transforms along i with the
 // same two register passes as the row transform, scales by kp^-2 and writes the box rows
@@ -467,6 +516,7 @@ static int colfft_lnc(int kp)
 
 static bool rowfft_reg_ok(const cqpi_handle *h);
 static cudaError_t configure_rowfft_reg(cqpi_handle *h);
+static cudaError_t configure_rowfft_g0k(cqpi_handle *h);
 static cudaError_t configure_colfft_reg(cqpi_handle *h);
 static void launch_colfft_reg(cqpi_handle *h, int ne);
 
@@ -488,6 +538,8 @@ cudaError_t configure_fft32(cqpi_handle *h)
     if (e != cudaSuccess) return e;
     if (!rowfft_reg_ok(h)) return cudaSuccess;
     e = configure_rowfft_reg(h);
+    if (e != cudaSuccess) return e;
+    e = configure_rowfft_g0k(h);
     if (e != cudaSuccess) return e;
     return configure_colfft_reg(h);
 }
@@ -598,6 +650,43 @@ static cudaError_t configure_colfft_reg(cqpi_handle *h)
     return cudaSuccess;
 }
 
+template <int N1, int N2>
+static size_t rowfft_g0k_smem()
+{
+    constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
+    return 8 * ((size_t)RPC * (N1 * N2 + (N1 * N2) / 32 + 1) + N1 * N2);
+}
+
+template <int N1, int N2>
+static cudaError_t configure_rowfft_g0k_t()
+{
+    return cudaFuncSetAttribute(rowfft_reg_g0k_kernel<N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)rowfft_g0k_smem<N1, N2>());
+}
+
+static cudaError_t configure_rowfft_g0k(cqpi_handle *h)
+{
+    switch (h->kp) {
+    case 64: return configure_rowfft_g0k_t<8, 8>();
+    case 128: return configure_rowfft_g0k_t<8, 16>();
+    case 256: return configure_rowfft_g0k_t<16, 16>();
+    case 512: return configure_rowfft_g0k_t<16, 32>();
+    case 1024: return configure_rowfft_g0k_t<32, 32>();
+    case 2048: return configure_rowfft_g0k_t<32, 64>();
+    case 4096: return configure_rowfft_g0k_t<64, 64>();
+    }
+    return cudaSuccess;
+}
+
+template <int N1, int N2>
+static void launch_rowfft_g0k_t(cqpi_handle *h, int ne)
+{
+    constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
+    const long long nrows = (long long)ne * h->b * h->b * h->kp;
+    rowfft_reg_g0k_kernel<N1, N2><<<(unsigned)((nrows + RPC - 1) / RPC), 256, rowfft_g0k_smem<N1, N2>(), h->stream>>>(
+        h->NB, h->Rb, nrows, h->ws.g0k32, h->d_tw32, h->ws.half32);
+}
+
 static void launch_colfft_reg(cqpi_handle *h, int ne)
 {
     switch (h->kp) {
@@ -653,6 +742,28 @@ void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies)
                                                     h->ws.box32, h->ws.gmax);
     }
     h->launches++;
+}
+
+// Transforms of the unfused mixed path (G0(k) planes in ws.g0k32) with the register
+// four-step kernels; false when the k-grid is outside their range (the radix-2 kernels of
+// greens.cu run instead).
+bool launch_fft32_planes(cqpi_handle *h, int ne)
+{
+    const char *force = getenv("CQPI_ROWFFT");
+    if (!fft32_supported(h) || !rowfft_reg_ok(h) || (force && !strcmp(force, "radix2"))) return false;
+    switch (h->kp) {
+    case 64: launch_rowfft_g0k_t<8, 8>(h, ne); break;
+    case 128: launch_rowfft_g0k_t<8, 16>(h, ne); break;
+    case 256: launch_rowfft_g0k_t<16, 16>(h, ne); break;
+    case 512: launch_rowfft_g0k_t<16, 32>(h, ne); break;
+    case 1024: launch_rowfft_g0k_t<32, 32>(h, ne); break;
+    case 2048: launch_rowfft_g0k_t<32, 64>(h, ne); break;
+    case 4096: launch_rowfft_g0k_t<64, 64>(h, ne); break;
+    }
+    h->launches++;
+    launch_colfft_reg(h, ne);
+    h->launches++;
+    return true;
 }
 
 }  // namespace cqpi

@@ -271,7 +271,7 @@ void launch_fft(cqpi_handle *h, int ne)
 {
     if (h->precision == CQPI_PREC_FP64)
         launch_fft_t<double2>(h, ne, h->ws.g0k, h->d_tw, h->ws.half, h->ws.box, nullptr);
-    else
+    else if (!launch_fft32_planes(h, ne))
         launch_fft_t<float2>(h, ne, h->ws.g0k32, h->d_tw32, h->ws.half32, h->ws.box32, h->ws.gmax);
 }
 
