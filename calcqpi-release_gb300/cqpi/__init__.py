@@ -25,7 +25,7 @@ EXPORTED = [
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
     "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
     "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune", "cqpi_set_josephson",
-    "cqpi_wannierjosephson", "cqpi_set_threshold", "cqpi_wannierldoslist",
+    "cqpi_wannierjosephson", "cqpi_set_threshold", "cqpi_wannierldoslist", "cqpi_set_list",
 ]
 
 
@@ -98,6 +98,7 @@ def load():
     L.cqpi_wannierjosephson.argtypes = [P, P, P, P]
     L.cqpi_set_threshold.argtypes = [P, dbl, P, i32, ctypes.POINTER(i64)]
     L.cqpi_wannierldoslist.argtypes = [P, P, P]
+    L.cqpi_set_list.argtypes = [P, i64, P, P]
     _lib = L
     return L
 
@@ -261,6 +262,13 @@ class Engine:
         self._check(self._L.cqpi_set_threshold(self._h, thr, None if sa is None else _ptr(sa),
                                                0 if sa is None else len(sa), ctypes.byref(c)))
         return c.value
+
+    def set_list(self, ent, factor):
+        """Explicit proximity list: ent[k] = (list, i, j, o1, o2), factor[k]."""
+        ent = np.ascontiguousarray(np.asarray(ent, np.int32).reshape(-1, 5))
+        fac = np.ascontiguousarray(np.asarray(factor, np.float64).reshape(-1))
+        assert len(ent) == len(fac)
+        self._check(self._L.cqpi_set_list(self._h, len(fac), _ptr(ent), _ptr(fac)))
 
     def graph_begin(self):
         self._check(self._L.cqpi_graph_begin(self._h))

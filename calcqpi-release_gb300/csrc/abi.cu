@@ -483,21 +483,75 @@ void do_greens(cqpi_handle *h, int ne, const double *d_energies)
     check_launch();
 }
 
+struct ListEnt {
+    int d1, q, d2, o1, o2;
+    double f;
+};
+
+// A proximity list on the device, CSR by (d1, q) with the list order kept inside every
+// segment; pairs = the (o1, o2) the list uses.
+int upload_list(cqpi_handle *h, const std::vector<ListEnt> &ents)
+{
+    const int b = h->b;
+    std::vector<int> pidx((size_t)b * b, -1);
+    std::vector<int2> pairs;
+    for (const ListEnt &e : ents) {
+        if (e.o1 < 0 || e.o2 < 0 || e.o1 >= b || e.o2 >= b)
+            return fail(h, CQPI_ERR_ARG, "a proximity-list orbital is outside the band count");
+        int &p = pidx[(size_t)e.o1 * b + e.o2];
+        if (p < 0) {
+            p = (int)pairs.size();
+            pairs.push_back(make_int2(e.o1, e.o2));
+        }
+    }
+    const int npair = std::max<int>(1, (int)pairs.size());
+    if (pairs.empty()) pairs.push_back(make_int2(0, 0));
+    const size_t nseg = (size_t)h->W * h->Q;
+    std::vector<int> off(nseg + 1, 0), u(std::max<size_t>(ents.size(), 1), 0);
+    std::vector<double> f(std::max<size_t>(ents.size(), 1), 0.0);
+    for (const ListEnt &e : ents) off[(size_t)e.d1 * h->Q + e.q + 1]++;
+    for (size_t k = 0; k < nseg; k++) off[k + 1] += off[k];
+    std::vector<int> pos(off.begin(), off.end() - 1);
+    for (const ListEnt &e : ents) {
+        const int s = pos[(size_t)e.d1 * h->Q + e.q]++;
+        u[s] = e.d2 * npair + pidx[(size_t)e.o1 * b + e.o2];
+        f[s] = e.f;
+    }
+    std::vector<float> f32(f.begin(), f.end());
+    h->list_npair = npair;
+    h->list_count = (int64_t)ents.size();
+    if (list_smem_bytes(h, true) > 227 * 1024)   // the FP64 form (also the seam's)
+        return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list: window, bands and pairs exceed the shared memory of a block");
+    dfree(h->d_list_off);
+    dfree(h->d_list_u);
+    dfree(h->d_list_f);
+    dfree(h->d_list_f32);
+    dfree(h->d_list_pair);
+    dalloc(&h->d_list_off, off.size());
+    dalloc(&h->d_list_u, u.size());
+    dalloc(&h->d_list_f, f.size());
+    dalloc(&h->d_list_f32, f32.size());
+    dalloc(&h->d_list_pair, pairs.size());
+    CK(cudaMemcpy(h->d_list_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_u, u.data(), sizeof(int) * u.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_f, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_f32, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_list_pair, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice));
+    CK(configure_list(h));
+    return CQPI_OK;
+}
+
 // mkthresholdlist (src/qpi.cc:139-253) over the handle's orbitals: the entries (d1, d2, q,
 // o1, o2, f) with |f| = |phi_o1 phi_o2| > threshold * max phi^2, in the maxband / spin form
 // (orbitals 0 .. maxband-1, or both spin blocks of maxband/2) or the spinarr form (orbitals
-// of equal non-zero label).  Stored on the device CSR by (d1, q), list order kept.
+// of equal non-zero label).
 int build_list(cqpi_handle *h)
 {
     const int wins = 2 * h->w + 1, os = h->os, xs = os * wins, norb = h->wf_norb, b = h->b;
     double maxval = 0.0;
     for (size_t k = 0; k < h->wf_host.size(); k++) maxval = std::max(maxval, h->wf_host[k] * h->wf_host[k]);
     const double thr = h->list_threshold * maxval;
-    struct Ent {
-        int d1, q, d2, o1, o2;
-        double f;
-    };
-    std::vector<Ent> ents;
+    std::vector<ListEnt> ents;
     auto wfv = [&](int o, int x, int y) { return h->wf_host[((size_t)o * xs + x) * xs + y]; };
     auto push = [&](int xn1, int yn1, int xn2, int yn2, int i, int j, int o1, int o2) {
         const int x = i + (wins - 1) * os, y = j + (wins - 1) * os;
@@ -533,51 +587,7 @@ int build_list(cqpi_handle *h)
                                     for (int j = 0; j < os; j++) push(xn1, yn1, xn2, yn2, i, j, o1, o2);
                     }
                 }
-    std::vector<int> pidx((size_t)b * b, -1);
-    std::vector<int2> pairs;
-    for (const Ent &e : ents) {
-        if (e.o1 >= b || e.o2 >= b) return fail(h, CQPI_ERR_ARG, "a proximity-list orbital is beyond the band count");
-        int &p = pidx[(size_t)e.o1 * b + e.o2];
-        if (p < 0) {
-            p = (int)pairs.size();
-            pairs.push_back(make_int2(e.o1, e.o2));
-        }
-    }
-    const int npair = std::max<int>(1, (int)pairs.size());
-    if (pairs.empty()) pairs.push_back(make_int2(0, 0));
-    const size_t nseg = (size_t)h->W * h->Q;
-    std::vector<int> off(nseg + 1, 0), u(std::max<size_t>(ents.size(), 1), 0);
-    std::vector<double> f(std::max<size_t>(ents.size(), 1), 0.0);
-    for (const Ent &e : ents) off[(size_t)e.d1 * h->Q + e.q + 1]++;
-    for (size_t k = 0; k < nseg; k++) off[k + 1] += off[k];
-    std::vector<int> pos(off.begin(), off.end() - 1);
-    for (const Ent &e : ents) {
-        const int s = pos[(size_t)e.d1 * h->Q + e.q]++;
-        u[s] = e.d2 * npair + pidx[(size_t)e.o1 * b + e.o2];
-        f[s] = e.f;
-    }
-    std::vector<float> f32(f.begin(), f.end());
-    h->list_npair = npair;
-    h->list_count = (int64_t)ents.size();
-    if (list_smem_bytes(h, true) > 227 * 1024)   // the FP64 form (also the seam's)
-        return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list: window, bands and pairs exceed the shared memory of a block");
-    dfree(h->d_list_off);
-    dfree(h->d_list_u);
-    dfree(h->d_list_f);
-    dfree(h->d_list_f32);
-    dfree(h->d_list_pair);
-    dalloc(&h->d_list_off, off.size());
-    dalloc(&h->d_list_u, u.size());
-    dalloc(&h->d_list_f, f.size());
-    dalloc(&h->d_list_f32, f32.size());
-    dalloc(&h->d_list_pair, pairs.size());
-    CK(cudaMemcpy(h->d_list_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_u, u.data(), sizeof(int) * u.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_f, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_f32, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_pair, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice));
-    CK(configure_list(h));
-    return CQPI_OK;
+    return upload_list(h, ents);
 }
 
 }  // namespace
@@ -898,7 +908,7 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
             for (int o = 0; o < norb; o++)
                 if (is_zero[o]) std::fill(h->wf_host.begin() + o * n2, h->wf_host.begin() + (o + 1) * n2, 0.0);
     }
-    if (h->list_mode) {
+    if (h->list_mode && h->list_from_orbitals) {
         try {
             const int rc = build_list(h);
             if (rc != CQPI_OK) return rc;
@@ -1509,6 +1519,39 @@ int cqpi_wannierldoslist(cqpi_handle *h, const double *T, const double *g0r)
     return seam_contract(h, T, g0r, nullptr, true);
 }
 
+int cqpi_set_list(cqpi_handle *h, int64_t nent, const int32_t *ent, const double *factor)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (nent < 0 || (nent > 0 && (!ent || !factor))) return fail(h, CQPI_ERR_ARG, "invalid proximity list");
+    if (h->Q > 512) return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list: oversamp^2 must be <= 512");
+    if (nent > (int64_t)1 << 30) return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list longer than 2^30 entries");
+    const int wins = 2 * h->w + 1;
+    const int64_t nlist = (int64_t)wins * wins * wins * wins;
+    std::vector<ListEnt> ents((size_t)nent);
+    for (int64_t k = 0; k < nent; k++) {
+        const int32_t *e = ent + 5 * k;
+        if (e[0] < 0 || e[0] >= nlist || e[1] < 0 || e[1] >= h->os || e[2] < 0 || e[2] >= h->os)
+            return fail(h, CQPI_ERR_ARG, "proximity-list entry outside the window or the sub-pixel grid");
+        const int L = e[0], xn1 = L / (wins * wins * wins), yn1 = (L / (wins * wins)) % wins;
+        const int xn2 = (L / wins) % wins, yn2 = L % wins;
+        ents[(size_t)k] = {xn1 * wins + yn1, e[1] * h->os + e[2], xn2 * wins + yn2, e[3], e[4], factor[k]};
+    }
+    h->list_mode = true;
+    h->list_from_orbitals = false;
+    try {
+        const int rc = upload_list(h, ents);
+        if (rc != CQPI_OK) {
+            h->list_mode = false;
+            return rc;
+        }
+    } catch (const CudaError &e) {
+        h->list_mode = false;
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
 int cqpi_set_threshold(cqpi_handle *h, double threshold, const int32_t *spinarr, int32_t nspinarr, int64_t *count)
 {
     if (!h) return CQPI_ERR_ARG;
@@ -1527,6 +1570,7 @@ int cqpi_set_threshold(cqpi_handle *h, double threshold, const int32_t *spinarr,
     h->list_spinarr.assign(h->wf_norb, 0);
     for (int i = 0; i < std::min<int>(nspinarr, h->wf_norb); i++) h->list_spinarr[i] = spinarr[i];
     h->list_mode = true;
+    h->list_from_orbitals = true;
     try {
         const int rc = build_list(h);
         if (rc != CQPI_OK) {

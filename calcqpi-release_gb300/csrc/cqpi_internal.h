@@ -198,6 +198,7 @@ struct cqpi_handle {
     double list_threshold = 0.0;
     std::vector<int32_t> list_spinarr;
     bool list_use_spinarr = false;
+    bool list_from_orbitals = true;     // built by cqpi_set_threshold (rebuilt with the orbitals)
     int list_npair = 0;
     int64_t list_count = 0;
     int *d_list_off = nullptr, *d_list_u = nullptr;

@@ -157,6 +157,12 @@ int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double eta
  * driver); cqpi_run_fov, cqpi_autotune and cqpi_adjoint return CQPI_ERR_NOT_SUPPORTED while
  * it is set. */
 int cqpi_set_threshold(cqpi_handle *h, double threshold, const int32_t *spinarr, int32_t nspinarr, int64_t *count);
+/* An explicit proximity list, as the reference's list-mode GPU backend receives it
+ * (CudaQPI(..., flaglist&), src/qpicudakernel.cu:431-487): nent entries ent[k][5] =
+ * (list, i, j, o1, o2) with list = ((xn1*wins + yn1)*wins + xn2)*wins + yn2, wins = 2w+1
+ * (flags[xn1][yn1][xn2][yn2]), sub-pixel (i, j) and orbitals o1, o2 < bands, and factor[k].
+ * Replaces any list; kept when the orbitals change.  cqpi_set_threshold(NaN) clears it. */
+int cqpi_set_list(cqpi_handle *h, int64_t nent, const int32_t *ent, const double *factor);
 
 /* ---- differentiation (extension: the reference computes no derivatives) -----
  * New hopping amplitudes for the terms of the model given to cqpi_create (same order,

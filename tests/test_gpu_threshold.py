@@ -125,3 +125,26 @@ def test_threshold_rebuilt_on_new_orbitals_and_refusals(built_lib):
         eng.wannierldos(np.eye(m.bands), np.zeros((meta["kp"], meta["kp"], m.bands, m.bands)))
     assert ex.value.code == cqpi.ERR_STATE
     eng.close()
+
+
+def test_explicit_list_equals_threshold_list(built_lib):
+    """cqpi_set_list with the oracle's mkthresholdlist entries (the form the reference's
+    list-mode GPU backend receives) gives the same maps as cqpi_set_threshold, and survives
+    new orbitals unchanged."""
+    import cqpi
+    from oracle import oracle as O
+    eng, meta, ref, m, d, count = _engine("threshold_spin", cqpi.PREC_FP64)
+    E = energies(meta)
+    a = eng.run(E, f32=False, f64=True)
+    wz = ref["wf"] * (1 - ref["zero"][:len(ref["wf"]), None, None])
+    ent, fac = O.threshold_list(meta["w"], meta["os"], wz, meta["threshold"], meta["maxband"], True)
+    eng.set_list(ent, fac)
+    b = eng.run(E, f32=False, f64=True)
+    assert np.array_equal(a, b)
+    eng.set_orbitals(2.0 * ref["wf"], ref["zero"])      # an explicit list is not rebuilt
+    c = eng.run(E, f32=False, f64=True)
+    assert np.array_equal(a, c)
+    with pytest.raises(cqpi.CqpiError) as ex:
+        eng.set_list(np.array([[0, 0, 0, 0, eng.bands]]), np.array([1.0]))
+    assert ex.value.code == cqpi.ERR_ARG
+    eng.close()
