@@ -31,6 +31,8 @@ def _lib():
         L.cqpi_orbital_cache.argtypes = [ctypes.c_char_p] + [ctypes.c_double] * 7 + [ctypes.c_int32, ctypes.c_int32, P]
         L.cqpi_idl_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32,
                                      ctypes.c_int32, P, P, P, ctypes.c_double, P]
+        L.cqpi_xsf_orbital_cache.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_double, P]
         L.cqpi_idl_read_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(_IDLHeader)]
         L.cqpi_idl_read.argtypes = [ctypes.c_char_p, P, ctypes.c_int64]
         L.cqpi_host_last_error.restype = ctypes.c_char_p
@@ -71,6 +73,18 @@ def orbital_cache(name, window, oversamp, width=0.5, height=5.0, xpos=0.0, ypos=
     out = np.empty((side, side), np.float64)
     rc = L.cqpi_orbital_cache(name.encode(), width, height, xpos, ypos, theta, phi, prefact, window, oversamp,
                               out.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+    return out
+
+
+def xsf_orbital_cache(path, height, window, oversamp, prefact=1.0) -> np.ndarray:
+    """Orbital cache [side][side] from an XSF file (the orbitalfiles keyword)."""
+    L = _lib()
+    side = (2 * window + 1) * oversamp
+    out = np.empty((side, side), np.float64)
+    rc = L.cqpi_xsf_orbital_cache(str(path).encode(), float(height), window, oversamp, float(prefact),
+                                  out.ctypes.data_as(ctypes.c_void_p))
     if rc:
         _err(L, rc)
     return out

@@ -2,9 +2,12 @@
 //   cqpi_read_hr        Wannier90 _hr.dat reader   (tightbind::readfile, src/tightbinding.cc:70-149)
 //   cqpi_orbital_cache  analytic orbital cache    (wannierfunctions::precalculate + getwave,
 //                                                  src/wannierfunctions.cc:21-221,433-442)
+//   cqpi_xsf_orbital_cache  XSF orbital cache   (xcfloader + wannierfunctions(file, ...),
+//                                                  src/loadxcf.cc:37-345, src/wannierfunctions.cc:444-463)
 //   cqpi_idl_write / cqpi_idl_read_header / cqpi_idl_read
 //                       IDL map container          (idl::write / idl::read, src/idl.cc:50-97)
 // These run on the CPU only; none of them touches the GPU.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -265,6 +268,192 @@ int cqpi_idl_read(const char *path, float *data, int64_t count)
     is.seekg(h.data_offset);
     is.read((char *)data, (std::streamsize)(sizeof(float) * n));
     if (!is) return host_fail(CQPI_ERR_ARG, std::string("error reading data of ") + path);
+    return CQPI_OK;
+}
+
+// ------------------------------------------------------------------ XSF orbitals
+// The XSF reader of the orbitalfiles keyword, as xcfloader reads a file (src/loadxcf.cc:
+// 37-185): a line counts only when a newline ends it; '#' anywhere makes the rest of the
+// line a comment; CRYSTAL enables PRIMVEC / CONVVEC / PRIMCOORD; in the data grid a value
+// starts at one of "+-0123456789" and ends at a blank, and a value that runs to the end of
+// its line makes the reader take the next line.  Values are stored cube[i][j][k], x fastest
+// in the file.
+struct XsfGrid {
+    size_t xs = 0, ys = 0, zs = 0;
+    std::vector<double> cube;                  // [i][j][k]
+    double origin[3] = {0, 0, 0};
+    double axis[3][3] = {};                    // spanning vectors
+    double convvec[3][3] = {};
+    bool has_convvec = false, has_grid = false, error = false;
+    std::vector<double> atom_z;
+};
+
+static bool xsf_next(std::istream &is, std::string &line)
+{
+    std::getline(is, line);
+    return !is.eof();
+}
+
+static bool xsf_read(const char *path, XsfGrid &g, std::string &err)
+{
+    std::ifstream is(path);
+    if (!is) {
+        err = std::string("Could not open file ") + path;
+        return false;
+    }
+    std::string line;
+    bool crystal = false;
+    while (xsf_next(is, line)) {
+        if (line.find('#') != std::string::npos) continue;
+        if (line.find("CRYSTAL") != std::string::npos) {
+            crystal = true;
+        } else if (crystal && (line.find("PRIMVEC") != std::string::npos ||
+                               line.find("CONVVEC") != std::string::npos)) {
+            const bool conv = line.find("CONVVEC") != std::string::npos;
+            for (int r = 0; r < 3; r++) {
+                std::string pl;
+                std::getline(is, pl);
+                std::istringstream iss(pl);
+                double v[3] = {0, 0, 0};
+                iss >> v[0] >> v[1] >> v[2];
+                if (conv)
+                    for (int c = 0; c < 3; c++) g.convvec[r][c] = v[c];
+            }
+            if (conv) g.has_convvec = true;
+        } else if (crystal && line.find("PRIMCOORD") != std::string::npos) {
+            std::string pl;
+            std::getline(is, pl);
+            std::istringstream iss(pl);
+            size_t natoms = 0, type = 0;
+            iss >> natoms >> type;
+            for (size_t a = 0; a < natoms; a++) {
+                std::getline(is, pl);
+                std::istringstream ia(pl);
+                std::string name;
+                double x = 0, y = 0, z = 0;
+                ia >> name >> x >> y >> z;
+                g.atom_z.push_back(z);
+            }
+        } else if (line.find("BEGIN_BLOCK_DATAGRID_3D") != std::string::npos) {
+            std::string pl, kw;
+            std::getline(is, pl);
+            { std::istringstream iss(pl); kw.clear(); iss >> kw; }
+            if (kw != "3D_field") g.error = true;
+            std::getline(is, pl);
+            { std::istringstream iss(pl); kw.clear(); iss >> kw; }
+            if (kw != "BEGIN_DATAGRID_3D_UNKNOWN") g.error = true;
+            std::getline(is, pl);
+            { std::istringstream iss(pl); iss >> g.xs >> g.ys >> g.zs; }
+            if (g.xs == 0 || g.ys == 0 || g.zs == 0 || g.xs * g.ys * g.zs > ((size_t)1 << 31)) {
+                err = std::string("invalid data grid size in ") + path;
+                return false;
+            }
+            std::getline(is, pl);
+            { std::istringstream iss(pl); iss >> g.origin[0] >> g.origin[1] >> g.origin[2]; }
+            for (int r = 0; r < 3; r++) {
+                std::getline(is, pl);
+                std::istringstream iss(pl);
+                iss >> g.axis[r][0] >> g.axis[r][1] >> g.axis[r][2];
+            }
+            g.cube.assign(g.xs * g.ys * g.zs, 0.0);
+            std::getline(is, line);
+            size_t npos = 0;
+            for (size_t k = 0; k < g.zs; k++)
+                for (size_t j = 0; j < g.ys; j++)
+                    for (size_t i = 0; i < g.xs; i++) {
+                        const size_t pos = line.find_first_of("+-0123456789", npos);
+                        if (pos == std::string::npos) {
+                            err = std::string("cannot parse data line of ") + path;
+                            return false;
+                        }
+                        npos = line.find_first_of(" \t", pos);
+                        const bool reload = npos == std::string::npos;
+                        std::istringstream niss(line.substr(pos, reload ? std::string::npos : npos - pos));
+                        double v = 0.0;
+                        niss >> v;
+                        g.cube[(i * g.ys + j) * g.zs + k] = v;
+                        if (reload) {
+                            std::getline(is, line);
+                            npos = 0;
+                        }
+                    }
+            if (line.find("END_DATAGRID_3D") == std::string::npos) g.error = true;
+            std::getline(is, line);
+            if (line.find("END_BLOCK_DATAGRID_3D") == std::string::npos) g.error = true;
+            g.has_grid = true;
+        }
+    }
+    if (g.error) err = std::string("malformed data grid block in ") + path;
+    else if (!g.has_grid) err = std::string("no 3D data grid in ") + path;
+    else if (!g.has_convvec) err = std::string("no CONVVEC in ") + path;
+    return !g.error && g.has_grid && g.has_convvec;
+}
+
+// xcfloader::operator() after getvalue (src/loadxcf.cc:187-202,326-328): lattice units ->
+// Cartesian with CONVVEC, fractional grid coordinates by solving [a0 a1 a2] f = r - origin
+// (Gaussian elimination with partial pivoting), nearest grid point round(f * n), zero
+// outside the grid.  A NaN height (getzheight(0)) gives zero.
+static double xsf_value(const XsfGrid &g, double xu, double yu, double z)
+{
+    const double r[3] = {xu * g.convvec[0][0] + yu * g.convvec[1][0] - g.origin[0],
+                         xu * g.convvec[0][1] + yu * g.convvec[1][1] - g.origin[1], z - g.origin[2]};
+    double A[3][4];
+    for (int row = 0; row < 3; row++) {
+        for (int c = 0; c < 3; c++) A[row][c] = g.axis[c][row];
+        A[row][3] = r[row];
+    }
+    for (int c = 0; c < 3; c++) {
+        int piv = c;
+        for (int row = c + 1; row < 3; row++)
+            if (std::fabs(A[row][c]) > std::fabs(A[piv][c])) piv = row;
+        if (piv != c)
+            for (int k = 0; k < 4; k++) std::swap(A[c][k], A[piv][k]);
+        if (A[c][c] == 0.0) return 0.0;
+        for (int row = c + 1; row < 3; row++) {
+            const double m = A[row][c] / A[c][c];
+            for (int k = c; k < 4; k++) A[row][k] -= m * A[c][k];
+        }
+    }
+    double f[3];
+    for (int c = 2; c >= 0; c--) {
+        double v = A[c][3];
+        for (int k = c + 1; k < 3; k++) v -= A[c][k] * f[k];
+        f[c] = v / A[c][c];
+    }
+    const size_t n[3] = {g.xs, g.ys, g.zs};
+    long long idx[3];
+    for (int a = 0; a < 3; a++) {
+        const double v = f[a] * (double)n[a];
+        if (!std::isfinite(v) || std::fabs(v) > 4e18) return 0.0;
+        idx[a] = (long long)std::round(v);
+        if (idx[a] < 0 || (size_t)idx[a] >= n[a]) return 0.0;
+    }
+    return g.cube[((size_t)idx[0] * g.ys + (size_t)idx[1]) * g.zs + (size_t)idx[2]];
+}
+
+int cqpi_xsf_orbital_cache(const char *path, double height, int32_t window, int32_t oversamp, double prefact,
+                           double *out)
+{
+    if (!path || !out || window < 0 || oversamp < 1) return host_fail(CQPI_ERR_ARG, "invalid XSF orbital arguments");
+    XsfGrid g;
+    std::string err;
+    if (!xsf_read(path, g, err)) return host_fail(CQPI_ERR_ARG, err);
+    // xcfloader::getzheight (src/loadxcf.cc:330-345): above the highest / below the lowest atom
+    double z = NAN;
+    if (height > 0.0 && !g.atom_z.empty()) {
+        z = g.atom_z[0];
+        for (double v : g.atom_z) z = std::max(z, v);
+        z += height;
+    } else if (height < 0.0 && !g.atom_z.empty()) {
+        z = g.atom_z[0];
+        for (double v : g.atom_z) z = std::min(z, v);
+        z += height;
+    }
+    const int n = (2 * window + 1) * oversamp;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+            out[(size_t)i * n + j] =
+                prefact * xsf_value(g, (double)i / oversamp - (double)window, (double)j / oversamp - (double)window, z);
     return CQPI_OK;
 }
 

@@ -4,13 +4,14 @@
 // Mirrors the reference driver src/calcqpi.cc:131-811 for output=wannier and
 // output=josephson (:225, :249-251 deltat/etat, :451-460, :643-646, :705-709),
 // green=normal: the same keywords and defaults (:133-137), model load (:277-292),
-// scattering setup (:254-272, :393-395), orbital setup from idlorbitalfile
+// scattering setup (:254-272, :393-395), orbital setup from idlorbitalfile, XSF
+// orbitalfiles (:577-600)
 // (:483-518) or analytic orbitals (:519-576), wffile output (:602-618), the map
 // idl(os*n, os*n, layers, 2, 2, lenergy, henergy, 0, -1, -1) with its comment line
 // (:640-656), layer energies idl::getbias (src/idl.cc:969-973) and the final save
 // (:779-783), the proximity list of the threshold / spinarr keywords (:238, :619-635,
 // :700-701).  Modes and keywords outside that path (spf, uspf, nomode,
-// green=surface|bulk, XSF orbitalfiles, bsfile, dosfile) stop with
+// green=surface|bulk, bsfile, dosfile) stop with
 // an explicit "not supported" error instead of being ignored.
 #include <unistd.h>
 #include <pwd.h>
@@ -138,7 +139,8 @@ void help()
               << " lattice (201), oversamp (4), energies (-1,1), layers (21), kpoints (=lattice),\n"
               << " green (normal), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
-              << " pos[i], zheight (5.0), idlorbitalfile, deltat (0.001), etat (=eta), threshold, spinarr\n";
+              << " pos[i], zheight (5.0), idlorbitalfile, orbitalfiles, deltat (0.001), etat (=eta), threshold,\n"
+              << " spinarr\n";
 }
 
 double getbias(double lb, double hb, size_t layers, size_t k)
@@ -448,9 +450,40 @@ int main(int argc, char **argv)
         log << "Maximum rel. value at boundary: " << mx << "\n";
         if (mx > 0.05) log << "Warning: boundary too close, use larger window size!\n";
     } else if (lf.has("orbitalfiles")) {
-        return not_supported(log, "orbitalfiles (XSF Wannier orbitals)");
+        // DFT / Wannier90 orbitals from XSF files (src/calcqpi.cc:577-600)
+        if (lf.has("zheight")) zheight = lf.value("zheight");
+        {
+            std::ostringstream l;
+            l << "Using Wannier90/XSF-orbitals for vacuum overlap.\n    Parameters:\n"
+              << "             zheight:         " << zheight << "\n";
+            log << l.str();
+        }
+        std::vector<std::string> files = lf.strlist("orbitalfiles");
+        prearr.resize(files.size(), 1.0);
+        side = (2 * window + 1) * oversamp;
+        for (size_t i = 0; i < files.size(); i++) {
+            log << "Loading wave function file " << files[i] << ".\n";
+            std::vector<double> a(side * side);
+            if (cqpi_xsf_orbital_cache(files[i].c_str(), zheight, (int32_t)window, (int32_t)oversamp, prearr[i],
+                                       a.data()) != CQPI_OK) {
+                log << cqpi_host_last_error() << "\nError loading wave function file " << files[i] << "\n";
+                return 1;
+            }
+            wfs.push_back(a);
+            zero.push_back(0);
+        }
+        if ((maxbands >> 1) == files.size() && spin) {
+            log << "Found half as many orbitals as needed in spin-polarized calculation, duplicating wave function set.\n";
+            for (size_t k = 0; k < files.size(); k++) { wfs.push_back(wfs[k]); zero.push_back(0); }
+        } else if (files.size() < maxbands) {
+            log << "Fewer number of orbital files specified than there are bands, padding with zeros.\n";
+            // the reference counts the padding from its (empty) analytic orbital list, so
+            // maxbands zero orbitals follow the files (src/calcqpi.cc:596-599); kept, since
+            // the wffile output shows them
+            for (size_t i = 0; i < maxbands; i++) { wfs.push_back(std::vector<double>(side * side, 0.0)); zero.push_back(1); }
+        }
     } else {
-        log << "No orbitals specified (orbitals= or idlorbitalfile=) - exiting.\n";
+        log << "No orbitals specified (orbitals=, idlorbitalfile= or orbitalfiles=) - exiting.\n";
         return 1;
     }
     if (lf.has("wffile")) {

@@ -43,6 +43,16 @@ int cqpi_orbital_known(const char *name);
 int cqpi_orbital_cache(const char *name, double width, double height, double xpos, double ypos, double theta,
                        double phi, double prefact, int32_t window, int32_t oversamp, double *out);
 
+/* Replaces wannierfunctions(filename, height, window, oversamp, prefact) with its XSF
+ * reader xcfloader (src/wannierfunctions.cc:444-463, src/loadxcf.cc:37-345), the
+ * orbitalfiles keyword: out[i][j] = prefact * value of the XSF 3D data grid at the lattice
+ * point (i/os - w, j/os - w) (CONVVEC to Cartesian, nearest grid point, zero outside) and at
+ * z = height above the highest atom of PRIMCOORD (below the lowest for height < 0; height 0
+ * gives zeros), side (2w+1)*os.  A file that cannot be read (missing, no data grid, no
+ * CONVVEC, malformed block) returns CQPI_ERR_ARG with the reason in cqpi_host_last_error(). */
+int cqpi_xsf_orbital_cache(const char *path, double height, int32_t window, int32_t oversamp, double prefact,
+                           double *out);
+
 /* IDL map header (src/idl.h:41-60). */
 typedef struct {
     char name[1024];

@@ -6,6 +6,9 @@ the checker of the engine's C++ host code.  Nothing in the product imports it.
 * ``read_hr``      -- tightbind::readfile, src/tightbinding.cc:70-149
 * ``read_idl`` / ``write_idl`` -- idl::read / idl::write, src/idl.cc:50-97
 * ``LoadConfig``   -- loadconfig, include/parser.h:24-197
+* ``read_xsf`` / ``xsf_orbital_cache`` -- xcfloader (src/loadxcf.cc:37-345) and the XSF
+  constructor of wannierfunctions (src/wannierfunctions.cc:444-463); ``write_xsf`` writes
+  the fixture files
 """
 from __future__ import annotations
 
@@ -306,3 +309,184 @@ def _atoi(s: str) -> int:
         return int(s[:e])
     except ValueError:
         return 0
+
+
+# --------------------------------------------------------------------------- XSF orbitals
+class Xsf:
+    """XSF file as xcfloader::readfile keeps it (src/loadxcf.cc:37-185): comments, PRIMVEC,
+    CONVVEC, PRIMCOORD atoms, and the first 3D data grid cube[i][j][k] (x fastest in the
+    file) with its origin and spanning vectors.  ``error`` mirrors xcfloader::error."""
+
+    def __init__(self):
+        self.comments, self.primvec, self.convvec, self.atoms, self.coords = [], [], [], [], []
+        self.origin, self.axes = [], []
+        self.shape = (0, 0, 0)
+        self.cube = None
+        self.error = False
+
+
+def read_xsf(path) -> Xsf:
+    """xcfloader::readfile restated: a line counts only when a newline ends it
+    (``while(!eof) { getline; if(!eof) ... }``); '#' anywhere makes the rest a comment;
+    CRYSTAL enables PRIMVEC / CONVVEC / PRIMCOORD; the data grid is tokenised as the
+    reference does (a token starts at one of '+-0123456789' and ends at a blank; a token
+    that runs to the end of its line loads the next line)."""
+    x = Xsf()
+    with open(path, "r", newline="") as fh:
+        text = fh.read()
+    parts = text.split("\n")
+    lines = parts[:-1]          # the last piece has no newline after it
+    it = iter(lines)
+    pos_line = [0]
+
+    def nxt():
+        pos_line[0] += 1
+        try:
+            return next(it)
+        except StopIteration:
+            return ""
+
+    crystal = False
+    while True:
+        try:
+            line = next(it)
+        except StopIteration:
+            break
+        pos_line[0] += 1
+        h = line.find("#")
+        if h >= 0:
+            x.comments.append(line[h + 1:])
+            continue
+        if "CRYSTAL" in line:
+            crystal = True
+        elif crystal and "PRIMVEC" in line:
+            for _ in range(3):
+                e = _Extract(nxt())
+                x.primvec.append([e.real(), e.real(), e.real()])
+        elif crystal and "CONVVEC" in line:
+            for _ in range(3):
+                e = _Extract(nxt())
+                x.convvec.append([e.real(), e.real(), e.real()])
+        elif crystal and "PRIMCOORD" in line:
+            e = _Extract(nxt())
+            natoms = e.integer()
+            for _ in range(natoms):
+                toks = nxt().split()
+                x.atoms.append(toks[0])
+                x.coords.append([float(toks[1]), float(toks[2]), float(toks[3])])
+        elif "BEGIN_BLOCK_DATAGRID_3D" in line:
+            t = nxt().split()
+            if not t or t[0] != "3D_field":
+                x.error = True
+            t = nxt().split()
+            if not t or t[0] != "BEGIN_DATAGRID_3D_UNKNOWN":
+                x.error = True
+            e = _Extract(nxt())
+            xs, ys, zs = e.integer(), e.integer(), e.integer()
+            x.shape = (xs, ys, zs)
+            e = _Extract(nxt())
+            x.origin = [e.real(), e.real(), e.real()]
+            for _ in range(3):
+                e = _Extract(nxt())
+                x.axes.append([e.real(), e.real(), e.real()])
+            cube = np.zeros((xs, ys, zs))
+            line = nxt()
+            npos = 0
+            for k in range(zs):
+                for j in range(ys):
+                    for i in range(xs):
+                        p = _find_first_of(line, "+-0123456789", npos)
+                        if p < 0:
+                            x.error = True
+                            x.cube = cube
+                            return x
+                        npos = _find_first_of(line, " \t", p)
+                        reload = npos < 0
+                        tok = line[p:] if reload else line[p:npos]
+                        try:
+                            cube[i, j, k] = _Extract(tok).real()
+                        except ValueError:
+                            cube[i, j, k] = 0.0
+                        if reload:
+                            line = nxt()
+                            npos = 0
+            x.cube = cube
+            if "END_DATAGRID_3D" not in line:
+                x.error = True
+            if "END_BLOCK_DATAGRID_3D" not in nxt():
+                x.error = True
+    return x
+
+
+def _cround(v: float) -> int:
+    """C's round(): half away from zero (abs(v) - floor(abs(v)) is exact in binary)."""
+    a = abs(v)
+    r = math.floor(a)
+    if a - r >= 0.5:
+        r += 1
+    return int(r) if v >= 0 else -int(r)
+
+
+def xsf_value(x: Xsf, xu: float, yu: float, z: float) -> float:
+    """xcfloader::getvalue + operator() (src/loadxcf.cc:187-202,326-328): lattice units ->
+    Cartesian with CONVVEC, fractional grid coordinates from the spanning vectors, nearest
+    grid point round(f * n), zero outside the grid (and for a NaN height)."""
+    cx = xu * x.convvec[0][0] + yu * x.convvec[1][0]
+    cy = xu * x.convvec[0][1] + yu * x.convvec[1][1]
+    b = np.array([cx, cy, z]) - np.array(x.origin)
+    M = np.array(x.axes, dtype=np.float64).T          # columns: spanning vectors
+    f = np.linalg.solve(M, b)
+    if not np.all(np.isfinite(f)):
+        return 0.0
+    idx = [_cround(v * n) for v, n in zip(f, x.shape)]
+    if all(0 <= idx[a] < x.shape[a] for a in range(3)):
+        return float(x.cube[idx[0], idx[1], idx[2]])
+    return 0.0
+
+
+def xsf_zheight(x: Xsf, height: float) -> float:
+    """xcfloader::getzheight (src/loadxcf.cc:330-345)."""
+    if height > 0.0:
+        return max(c[2] for c in x.coords) + height
+    if height < 0.0:
+        return min(c[2] for c in x.coords) + height
+    return float("nan")
+
+
+def xsf_orbital_cache(path, height, window, oversamp, prefact=1.0) -> np.ndarray:
+    """wannierfunctions(filename, height, window, oversamp, prefact)
+    (src/wannierfunctions.cc:444-463): cache[i][j] = prefact * getvalue(i/os - w, j/os - w,
+    zheight), side (2w+1) os -- no half-cell shift, unlike the analytic orbitals."""
+    x = read_xsf(path)
+    if x.error:
+        raise ValueError("XSF file could not be read: %s" % path)
+    z = xsf_zheight(x, height)
+    n = (2 * window + 1) * oversamp
+    out = np.zeros((n, n))
+    for i in range(n):
+        for j in range(n):
+            out[i, j] = prefact * xsf_value(x, i / oversamp - window, j / oversamp - window, z)
+    return out
+
+
+def write_xsf(path, cube: np.ndarray, origin, axes, convvec, atoms, comment="generated", per_line=6):
+    """An XSF file (CRYSTAL, PRIMVEC = CONVVEC, PRIMCOORD, one 3D data grid) that the
+    reference's reader accepts: values x fastest, a newline after every per_line values and
+    after the last one, no trailing blanks."""
+    xs, ys, zs = cube.shape
+    out = ["# " + comment, "CRYSTAL", "PRIMVEC"]
+    out += ["%.10f %.10f %.10f" % tuple(v) for v in convvec]
+    out.append("CONVVEC")
+    out += ["%.10f %.10f %.10f" % tuple(v) for v in convvec]
+    out.append("PRIMCOORD")
+    out.append("%d 1" % len(atoms))
+    out += ["%s %.10f %.10f %.10f" % (a[0], a[1], a[2], a[3]) for a in atoms]
+    out += ["BEGIN_BLOCK_DATAGRID_3D", "3D_field", "BEGIN_DATAGRID_3D_UNKNOWN", "%d %d %d" % (xs, ys, zs),
+            "%.10f %.10f %.10f" % tuple(origin)]
+    out += ["%.10f %.10f %.10f" % tuple(v) for v in axes]
+    vals = ["%.8e" % v for v in np.transpose(cube, (2, 1, 0)).reshape(-1)]
+    for s in range(0, len(vals), per_line):
+        out.append(" ".join(vals[s:s + per_line]))
+    out += ["END_DATAGRID_3D", "END_BLOCK_DATAGRID_3D"]
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")

@@ -15,8 +15,13 @@
 // and spin, src/calcqpi.cc:619-630,700-701), with "S threshold k s_0 .. s_k-1" the same
 // with a spinarr (mkthresholdlist(..., spinarr)).
 //
+// With "X height k file_0 prefact_0 ..." the orbitals are the XSF files, loaded by the
+// reference's wannierfunctions(file, height, window, oversamp, prefact) (the orbitalfiles
+// keyword); wfbin is then ignored.
+//
 // usage: refdump <hrfile> <wfbin> <out> n kp os w eta efermi spin maxband layers
 //                lenergy henergy scmodel nscat [vre vim]... [J deltat etat | T thr | S thr k s...]
+//                [X height k file prefact ...]
 // wfbin: int32 norb, int32 side, float64 [norb][side][side]
 // out:   per layer: float64 dos (tmatrix::calcdos), float64 ldos[y][x]
 #include <cstdio>
@@ -50,32 +55,68 @@ int main(int argc, char **argv)
     int nscat = atoi(argv[16]);
     vector<complex<double> > scat;
     for (int i = 0; i < nscat; i++) scat.push_back(complex<double>(atof(argv[17 + 2 * i]), atof(argv[18 + 2 * i])));
-    const int ja = 17 + 2 * nscat;
-    const bool josephson = argc >= ja + 3 && string(argv[ja]) == "J";
-    const double deltat = josephson ? atof(argv[ja + 1]) : 0.0, etat = josephson ? atof(argv[ja + 2]) : 0.0;
-    const bool listmode = argc >= ja + 2 && (string(argv[ja]) == "T" || string(argv[ja]) == "S");
-    const double threshold = listmode ? atof(argv[ja + 1]) : 0.0;
+    // trailing options: J deltat etat | T thr | S thr k s_0 .. s_k-1 | X height k file_0 .. file_k-1
+    bool josephson = false, listmode = false;
+    double deltat = 0.0, etat = 0.0, threshold = 0.0, xsfheight = 0.0;
     vector<int> spinarr;
-    if (listmode && string(argv[ja]) == "S") {
-        int k = atoi(argv[ja + 2]);
-        for (int i = 0; i < k; i++) spinarr.push_back(atoi(argv[ja + 3 + i]));
+    vector<string> xsffiles;
+    vector<double> xsfpre;
+    for (int a = 17 + 2 * nscat; a < argc;) {
+        const string opt = argv[a];
+        if (opt == "J" && a + 2 < argc) {
+            josephson = true; deltat = atof(argv[a + 1]); etat = atof(argv[a + 2]); a += 3;
+        } else if (opt == "T" && a + 1 < argc) {
+            listmode = true; threshold = atof(argv[a + 1]); a += 2;
+        } else if (opt == "S" && a + 2 < argc) {
+            listmode = true; threshold = atof(argv[a + 1]);
+            const int k = atoi(argv[a + 2]);
+            for (int i = 0; i < k; i++) spinarr.push_back(atoi(argv[a + 3 + i]));
+            a += 3 + k;
+        } else if (opt == "X" && a + 2 < argc) {
+            xsfheight = atof(argv[a + 1]);
+            const int k = atoi(argv[a + 2]);
+            for (int i = 0; i < k; i++) {
+                xsffiles.push_back(argv[a + 3 + 2 * i]);
+                xsfpre.push_back(atof(argv[a + 4 + 2 * i]));
+            }
+            a += 3 + 2 * k;
+        } else {
+            cerr << "unknown option " << opt << endl;
+            return 2;
+        }
     }
 
     tightbind *model = new tightbind(string(hr), efermi, scmodel);
     if (!*model) { cerr << "model load failed" << endl; return 1; }
-    FILE *f = fopen(wfbin, "rb");
-    if (!f) return 1;
-    int norb = 0, side = 0;
-    if (fread(&norb, 4, 1, f) != 1 || fread(&side, 4, 1, f) != 1) return 1;
     vector<wannierfunctions> wfs;
-    vector<vector<double> > arr(side, vector<double>(side, 0.0));
-    for (int o = 0; o < norb; o++) {
-        for (int i = 0; i < side; i++)
-            for (int j = 0; j < side; j++)
-                if (fread(&arr[i][j], 8, 1, f) != 1) return 1;
-        wfs.push_back(wannierfunctions(arr, 1.0));
+    size_t norb = 0;
+    if (!xsffiles.empty()) {
+        // orbitalfiles: wannierfunctions(file, zheight, window, oversamp, prefact) as the driver
+        // builds them (src/calcqpi.cc:577-590)
+        for (size_t i = 0; i < xsffiles.size(); i++) {
+            wfs.push_back(wannierfunctions(xsffiles[i], xsfheight, w, os, xsfpre[i]));
+            if (!wfs.back()) { cerr << "XSF load failed: " << xsffiles[i] << endl; return 1; }
+        }
+        norb = xsffiles.size();
+    } else {
+        FILE *f = fopen(wfbin, "rb");
+        if (!f) return 1;
+        int nf = 0, side = 0;
+        if (fread(&nf, 4, 1, f) != 1 || fread(&side, 4, 1, f) != 1) return 1;
+        vector<vector<double> > arr(side, vector<double>(side, 0.0));
+        for (int o = 0; o < nf; o++) {
+            for (int i = 0; i < side; i++)
+                for (int j = 0; j < side; j++)
+                    if (fread(&arr[i][j], 8, 1, f) != 1) return 1;
+            wfs.push_back(wannierfunctions(arr, 1.0));
+        }
+        fclose(f);
+        norb = nf;
     }
-    fclose(f);
+    if (spin && (maxband >> 1) == norb) {
+        for (size_t k = 0; k < norb; k++) wfs.push_back(wfs[k]);   // src/calcqpi.cc:592-595
+        norb *= 2;
+    }
     for (size_t i = norb; i < maxband; i++) wfs.push_back(wannierfunctions("z", 0.5, 5.0, 0.0, 0.0, 0.0, 0.0, 0.0));
 
     tmatrix *tm = new tmatrix(model, n, kp, eta, spin);

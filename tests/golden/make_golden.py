@@ -123,6 +123,11 @@ CASES = {
     "threshold_spinarr": dict(model="c2", n=5, kp=16, os=2, w=1, layers=2, energies=(-0.08, 0.06), eta=0.02,
                               scattering=(0.3, 0.3, 0.5), threshold=0.0, spinarr=(1, 0, 1),
                               orbitals=("idl", "t2g3")),
+    "xsf_t2g": dict(model="c2", n=6, kp=16, os=3, w=2, layers=2, energies=(-0.1, 0.1), eta=0.02,
+                    scattering=(0.3, 0.3, 0.5), orbitals=("xsf", dict(names=["dxz", "dyz", "dxy"], zheight=0.5))),
+    "xsf_pad": dict(model="c2", n=5, kp=16, os=2, w=1, layers=2, energies=(-0.08, 0.05), eta=0.02,
+                    scattering=(0.3, 0.3, 0.5),
+                    orbitals=("xsf", dict(names=["dxz", "dxy"], zheight=0.75, prearr=(0.7, 1.3)))),
     "wrap": dict(model="c1", n=20, kp=8, os=2, w=1, layers=1, energies=(0.1, 0.1), eta=0.05, scattering=(0.7,),
                  orbitals=("analytic", dict(names=["px"], radius=0.35, zheight=0.4, angle=20.0))),
 }
@@ -157,6 +162,26 @@ def orbital_cube(kind, w, os_):
     if kind == "t2g3":
         return W.t2g_orbitals_c2(w, os_)
     raise KeyError(kind)
+
+
+XSF_GRID = dict(origin=(-2.5, -2.5, -1.0), axes=((5.0, 0.0, 0.0), (0.0, 5.0, 0.0), (0.0, 0.0, 4.0)),
+                shape=(40, 40, 16), convvec=((1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 8.0)))
+
+
+def xsf_cubes(names, seed=5, sigma=0.6):
+    """Seeded Wannier-like orbitals on the XSF grid: d angular part (centred on the atom at
+    the origin) times a Gaussian, plus 5% seeded noise so that no symmetry hides an index
+    error.  Grid points r = origin + (i/xs, j/ys, k/zs) . axes, as the reference reads them."""
+    g = XSF_GRID
+    xs, ys, zs = g["shape"]
+    i, j, k = np.meshgrid(np.arange(xs), np.arange(ys), np.arange(zs), indexing="ij")
+    X = g["origin"][0] + g["axes"][0][0] * i / xs
+    Y = g["origin"][1] + g["axes"][1][1] * j / ys
+    Z = g["origin"][2] + g["axes"][2][2] * k / zs
+    rad = np.exp(-(X * X + Y * Y + Z * Z) / sigma ** 2)
+    ang = {"dxz": X * Z, "dyz": Y * Z, "dxy": X * Y, "s": np.ones_like(X), "pz": Z}
+    rng = np.random.default_rng(seed)
+    return [ang[nm] * rad * (1.0 + 0.05 * rng.normal(size=X.shape)) for nm in names]
 
 
 def fmt_list(v):
@@ -218,6 +243,37 @@ def make_case(name, c):
         if wf64.shape[0] < maxband:
             zero[wf64.shape[0]:] = 1
             wf64 = np.concatenate([wf64, np.zeros((maxband - wf64.shape[0], side, side))])
+    elif kind == "xsf":
+        names = spec["names"]
+        files = []
+        for q, cube in enumerate(xsf_cubes(names)):
+            fn = "orb%d.xsf" % q
+            F.write_xsf(os.path.join(d, fn), cube, XSF_GRID["origin"], XSF_GRID["axes"], XSF_GRID["convvec"],
+                        [("Fe", 0.0, 0.0, 0.0)], comment="seeded %s-like orbital" % names[q])
+            files.append(fn)
+        lines.append("orbitalfiles=(" + ",".join('"%s"' % fn for fn in files) + ");")
+        lines.append(f"zheight={spec['zheight']!r};")
+        pre = spec.get("prearr", (1.0,) * len(files))
+        if "prearr" in spec:
+            lines.append(f"prearr={fmt_list(pre)};")
+        # with fewer files than bands the reference appends zero orbitals without a cache and
+        # its wffile output then crashes (segmentation fault): ask for wffile only otherwise
+        if len(files) >= maxband or (spin and (maxband >> 1) == len(files)):
+            lines.append('wffile="ref_wf.idl";')
+        wf64 = np.stack([F.xsf_orbital_cache(os.path.join(d, fn), spec["zheight"], w, os_, pre[q])
+                         for q, fn in enumerate(files)])
+        # the driver pads with maxband zero orbitals when fewer files than bands are given
+        # (src/calcqpi.cc:596-599 counts from the empty analytic orbital list)
+        zero = np.zeros(wf64.shape[0], np.uint8)
+        if spin and (maxband >> 1) == len(files):
+            wf64 = np.concatenate([wf64, wf64])
+            zero = np.zeros(wf64.shape[0], np.uint8)
+        elif len(files) < maxband:
+            wf64 = np.concatenate([wf64, np.zeros((maxband, side, side))])
+            zero = np.concatenate([zero, np.ones(maxband, np.uint8)])
+        xsf_args = ["X", repr(spec["zheight"]), str(len(files))]
+        for q, fn in enumerate(files):
+            xsf_args += [os.path.join(d, fn), repr(float(pre[q]))]
     else:
         names = spec["names"]
         lines.append("orbitals=(" + ",".join(names) + ");")
@@ -269,6 +325,8 @@ def make_case(name, c):
             repr(c["energies"][0]), repr(c["energies"][1]), str(int(scmodel)), str(len(vscat))]
     for v in vscat:
         args += [repr(v.real), repr(v.imag)]
+    if kind == "xsf":
+        args += xsf_args
     if "threshold" in c and not jos:
         if "spinarr" in c:
             args += ["S", repr(c["threshold"]), str(len(c["spinarr"]))] + [str(int(v)) for v in c["spinarr"]]

@@ -113,3 +113,51 @@ def test_cli_josephson_needs_scmodel(built_lib, tmp_path):
     assert r.returncode == 1
     assert "Josephson-mode" in r.stdout and "using deltat=0.01, etat=0.05." in r.stdout
     assert "josephson-mode with scmodel=false makes no sense" in r.stdout
+
+
+@pytest.mark.parametrize("name", [n for n in NAMES if n.startswith("xsf")])
+def test_xsf_orbital_cache_matches_restatement(built_lib, name):
+    """cqpi_xsf_orbital_cache (C++) against the restatement of xcfloader + the XSF
+    wannierfunctions constructor, which the golden tests pin to the reference."""
+    from cqpi import host as Hh
+    d, meta, ref = load(name)
+    spec = meta["orbitals"][1]
+    pre = spec.get("prearr", [1.0] * len(spec["names"]))
+    for q in range(len(spec["names"])):
+        path = os.path.join(d, "orb%d.xsf" % q)
+        got = Hh.xsf_orbital_cache(path, spec["zheight"], meta["w"], meta["os"], pre[q])
+        want = F.xsf_orbital_cache(path, spec["zheight"], meta["w"], meta["os"], pre[q])
+        assert np.array_equal(got, want)
+        assert np.array_equal(got, ref["wf"][q])
+
+
+def test_xsf_errors(built_lib, tmp_path):
+    from cqpi import host as Hh
+    with pytest.raises(Hh.HostError):
+        Hh.xsf_orbital_cache(str(tmp_path / "missing.xsf"), 0.5, 1, 2)
+    d, meta, ref = load("xsf_t2g")
+    txt = open(os.path.join(d, "orb0.xsf")).read()
+    bad = tmp_path / "bad.xsf"
+    bad.write_text(txt.replace("3D_field", "2D_field"))
+    with pytest.raises(Hh.HostError):
+        Hh.xsf_orbital_cache(str(bad), 0.5, 1, 2)
+    noconv = tmp_path / "noconv.xsf"
+    lines = txt.split("\n")
+    i = lines.index("CONVVEC")
+    noconv.write_text("\n".join(lines[:i] + lines[i + 4:]))
+    with pytest.raises(Hh.HostError):
+        Hh.xsf_orbital_cache(str(noconv), 0.5, 1, 2)
+    # height 0: the reference's getzheight returns NaN; the cache is zero
+    assert not Hh.xsf_orbital_cache(os.path.join(d, "orb0.xsf"), 0.0, 1, 2).any()
+
+
+def test_cli_orbitalfiles_missing_file(built_lib, tmp_path):
+    """orbitalfiles with a file that cannot be read stops before any device work."""
+    import shutil
+    d, meta, ref = load("xsf_t2g")
+    for f in ("model_hr.dat", "input.cfg", "orb0.xsf", "orb2.xsf"):
+        shutil.copy(os.path.join(d, f), tmp_path / f)
+    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert "Using Wannier90/XSF-orbitals for vacuum overlap." in r.stdout
+    assert "Error loading wave function file orb1.xsf" in r.stdout
