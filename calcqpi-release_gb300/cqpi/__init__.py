@@ -15,7 +15,9 @@ import numpy as np
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "_build", "libcqpi.so")
 
-OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_DOMAIN, ERR_SINGULAR, ERR_STATE, ERR_NOT_SUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(10)
+(OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_DOMAIN, ERR_SINGULAR, ERR_STATE, ERR_NOT_SUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT,
+ ERR_NOT_CONVERGED) = range(11)
+GREEN_NORMAL, GREEN_SURFACE, GREEN_BULK = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [
@@ -25,7 +27,7 @@ EXPORTED = [
     "cqpi_get_stream", "cqpi_synchronize", "cqpi_kernel_launches", "cqpi_stage_times", "cqpi_measure_fma_peak",
     "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
     "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune", "cqpi_set_josephson",
-    "cqpi_wannierjosephson", "cqpi_set_threshold", "cqpi_wannierldoslist", "cqpi_set_list",
+    "cqpi_wannierjosephson", "cqpi_set_threshold", "cqpi_wannierldoslist", "cqpi_set_list", "cqpi_set_greens",
 ]
 
 
@@ -99,6 +101,7 @@ def load():
     L.cqpi_set_threshold.argtypes = [P, dbl, P, i32, ctypes.POINTER(i64)]
     L.cqpi_wannierldoslist.argtypes = [P, P, P]
     L.cqpi_set_list.argtypes = [P, i64, P, P]
+    L.cqpi_set_greens.argtypes = [P, i32, dbl, P]
     _lib = L
     return L
 
@@ -262,6 +265,23 @@ class Engine:
         self._check(self._L.cqpi_set_threshold(self._h, thr, None if sa is None else _ptr(sa),
                                                0 if sa is None else len(sa), ctypes.byref(c)))
         return c.value
+
+    def set_greens(self, mode, epserr=1e-5, surface_model=None):
+        """Green's function: GREEN_NORMAL, GREEN_SURFACE or GREEN_BULK (green keyword), with
+        an optional surface-layer model (stbfile)."""
+        if isinstance(mode, str):
+            mode = {"normal": GREEN_NORMAL, "surface": GREEN_SURFACE, "bulk": GREEN_BULK}[mode]
+        sm = None
+        if surface_model is not None:
+            self._sR = np.ascontiguousarray(surface_model.R, np.int32)
+            self._so = np.ascontiguousarray(surface_model.orb, np.int32)
+            self._st = np.ascontiguousarray(np.asarray(surface_model.t, np.complex128).view(np.float64))
+            self._sa = np.ascontiguousarray(surface_model.anti, np.uint8)
+            self._sm = _Model(int(surface_model.bands), int(getattr(surface_model, "scmaxbands", surface_model.bands)),
+                              float(getattr(surface_model, "efermi", 0.0)), len(surface_model.t), _ptr(self._sR),
+                              _ptr(self._so), _ptr(self._st), _ptr(self._sa))
+            sm = ctypes.byref(self._sm)
+        self._check(self._L.cqpi_set_greens(self._h, int(mode), float(epserr), sm))
 
     def set_list(self, ent, factor):
         """Explicit proximity list: ent[k] = (list, i, j, o1, o2), factor[k]."""

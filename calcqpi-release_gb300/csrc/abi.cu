@@ -107,7 +107,7 @@ size_t bytes_per_energy(const cqpi_handle *h)
 {
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
     const size_t cs = (h->precision == CQPI_PREC_FP64) ? 16 : 8;
-    const size_t g0k = h->use_fft32 ? 0 : bb * nk;
+    const size_t g0k = (h->use_fft32 && h->gmode == CQPI_GREEN_NORMAL) ? 0 : bb * nk;
     return cs * (g0k + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
 }
 
@@ -122,7 +122,7 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
         dalloc(&h->ws.half, ebatch * bb * (size_t)h->kp * h->NB);
         dalloc(&h->ws.box, ebatch * (size_t)h->NB * h->NB * bb);
     } else {
-        if (!h->use_fft32) dalloc(&h->ws.g0k32, ebatch * bb * nk);
+        if (!h->use_fft32 || h->gmode != CQPI_GREEN_NORMAL) dalloc(&h->ws.g0k32, ebatch * bb * nk);
         dalloc(&h->ws.half32, ebatch * bb * (size_t)h->kp * h->NB);
         dalloc(&h->ws.box32, ebatch * (size_t)h->NB * h->NB * bb);
         dalloc(&h->ws.gmax, ebatch);
@@ -194,6 +194,7 @@ void check_launch()
 int status_code(cqpi_handle *h, int st, const char *what)
 {
     if (st & 2) return fail(h, CQPI_ERR_TIMEOUT, std::string("a device wait timed out in ") + what);
+    if (st & 4) return fail(h, CQPI_ERR_NOT_CONVERGED, std::string("the surface / bulk decimation did not converge in ") + what);
     if (st & 1) return fail(h, CQPI_ERR_SINGULAR, std::string("1 - V G0(0) is singular at an energy of ") + what);
     return CQPI_OK;
 }
@@ -390,7 +391,8 @@ void sr_drop(cqpi_handle *h)
 bool sr_active(const cqpi_handle *h)
 {
     const char *f = getenv("CQPI_SPIN_REDUCE");
-    return h->sr_model && h->sr_orb && h->sr_v && !h->josephson && !h->list_mode && !(f && !strcmp(f, "0"));
+    return h->sr_model && h->sr_orb && h->sr_v && !h->josephson && !h->list_mode && h->gmode == CQPI_GREEN_NORMAL &&
+           !(f && !strcmp(f, "0"));
 }
 
 // Create (or re-create) the mb-band handle of the reduction; shares this handle's stream.
@@ -462,9 +464,69 @@ int sr_forward(cqpi_handle *h, int rc)
     return rc;
 }
 
+// Device hopping sets of the surface / bulk Green's function: surface in-plane (the surface
+// model's R_z = 0 terms, or the model's), bulk in-plane (R_z = 0), bulk coupling (R_z < 0)
+// (tightbind::setmatrix with kzdepinplane / kzdepoutofplane, src/tightbinding.cc:184-207).
+void upload_surface_terms(cqpi_handle *h)
+{
+    std::vector<int4> ti;
+    std::vector<double2> tt;
+    std::vector<int> an;
+    SurfaceTerms &S = h->surf;
+    const size_t nm = h->hop_r.size();
+    auto model_set = [&](bool inplane) {
+        for (size_t i = 0; i < nm; i++)
+            if (inplane ? h->hop_rz[i] == 0 : h->hop_rz[i] < 0) {
+                ti.push_back(make_int4(h->hop_rx[i], h->hop_ry[i], h->hop_o1[i], h->hop_o2[i]));
+                tt.push_back(make_double2(h->hop_t[2 * i], h->hop_t[2 * i + 1]));
+                an.push_back(h->hop_anti[i]);
+            }
+    };
+    S.off_s = 0;
+    if (h->surf_own_model) {
+        for (size_t i = 0; i < h->surf_anti.size(); i++)
+            if (h->surf_R[3 * i + 2] == 0) {
+                ti.push_back(make_int4(h->surf_R[3 * i], h->surf_R[3 * i + 1], h->surf_orb[2 * i], h->surf_orb[2 * i + 1]));
+                tt.push_back(make_double2(h->surf_t[2 * i], h->surf_t[2 * i + 1]));
+                an.push_back(h->surf_anti[i]);
+            }
+    } else {
+        model_set(true);
+    }
+    S.ns = (int)ti.size();
+    S.off_b = (int)ti.size();
+    model_set(true);
+    S.nb = (int)ti.size() - S.off_b;
+    S.off_o = (int)ti.size();
+    model_set(false);
+    S.no = (int)ti.size() - S.off_o;
+    if (ti.empty()) {
+        ti.push_back(make_int4(0, 0, 0, 0));
+        tt.push_back(make_double2(0.0, 0.0));
+        an.push_back(0);
+    }
+    dfree(S.d_i);
+    dfree(S.d_t);
+    dfree(S.d_anti);
+    dalloc(&S.d_i, ti.size());
+    dalloc(&S.d_t, tt.size());
+    dalloc(&S.d_anti, an.size());
+    CK(cudaMemcpy(S.d_i, ti.data(), sizeof(int4) * ti.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(S.d_t, tt.data(), sizeof(double2) * tt.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(S.d_anti, an.data(), sizeof(int) * an.size(), cudaMemcpyHostToDevice));
+    if (!S.d_mats) dalloc(&S.d_mats, (size_t)3 * h->kp * h->kp * h->b * h->b);
+}
+
+// The k-space data of the current Green's function: the eigen cache, or in the surface /
+// bulk modes the per-k in-plane and coupling matrices.
 void do_bands(cqpi_handle *h)
 {
-    launch_bands(h);
+    if (h->gmode != CQPI_GREEN_NORMAL) {
+        upload_surface_terms(h);
+        launch_surface_mats(h);
+    } else {
+        launch_bands(h);
+    }
     check_launch();
     h->bands_ready = true;
 }
@@ -472,6 +534,13 @@ void do_bands(cqpi_handle *h)
 // G0(k) -> G0(R) box -> T -> term1 for ne energies already in ws.energies.
 void do_greens(cqpi_handle *h, int ne, const double *d_energies)
 {
+    if (h->gmode != CQPI_GREEN_NORMAL) {
+        launch_greens_surface(h, ne, d_energies);
+        check_launch();
+        launch_fft(h, ne);
+        check_launch();
+        return;
+    }
     if (h->use_fft32) {
         launch_greens_fft32(h, ne, d_energies);
         check_launch();
@@ -522,6 +591,10 @@ int upload_list(cqpi_handle *h, const std::vector<ListEnt> &ents)
     h->list_count = (int64_t)ents.size();
     if (list_smem_bytes(h, true) > 227 * 1024)   // the FP64 form (also the seam's)
         return fail(h, CQPI_ERR_NOT_SUPPORTED, "proximity list: window, bands and pairs exceed the shared memory of a block");
+    dfree(h->surf.d_i);
+    dfree(h->surf.d_t);
+    dfree(h->surf.d_anti);
+    dfree(h->surf.d_mats);
     dfree(h->d_list_off);
     dfree(h->d_list_u);
     dfree(h->d_list_f);
@@ -609,6 +682,7 @@ const char *cqpi_status_string(int s)
     case CQPI_ERR_NOT_SUPPORTED: return "not supported";
     case CQPI_ERR_NO_DEVICE: return "no CUDA device";
     case CQPI_ERR_TIMEOUT: return "a bounded device wait timed out";
+    case CQPI_ERR_NOT_CONVERGED: return "the surface / bulk decimation did not converge";
     }
     return "unknown status";
 }
@@ -708,6 +782,11 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
             dst[2 * e] += model->t[2 * i];
             dst[2 * e + 1] += model->t[2 * i + 1];
             h->hop_r.push_back(r);
+            h->hop_rx.push_back(model->R[3 * i]);
+            h->hop_ry.push_back(model->R[3 * i + 1]);
+            h->hop_rz.push_back(model->R[3 * i + 2]);
+            h->hop_t.push_back(model->t[2 * i]);
+            h->hop_t.push_back(model->t[2 * i + 1]);
             h->hop_o1.push_back(model->orb[2 * i]);
             h->hop_o2.push_back(model->orb[2 * i + 1]);
             h->hop_anti.push_back(anti ? 1 : 0);
@@ -1296,6 +1375,7 @@ int cqpi_set_hoppings(cqpi_handle *h, const double *t)
     }
     h->rt_tn.swap(tn);
     h->rt_ta.swap(ta);
+    h->hop_t.assign(t, t + 2 * h->hop_r.size());
     h->time_reversal = real && !(f && !strcmp(f, "0"));
     h->bands_ready = false;
     h->sr_model = spin_model_reducible(h);
@@ -1311,6 +1391,8 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
     if (!h->orbitals_ready) return fail(h, CQPI_ERR_STATE, "cqpi_set_orbitals has not been called");
     if (h->josephson) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: Josephson mode is not supported");
     if (h->list_mode) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: the proximity-list form is not supported");
+    if (h->gmode != CQPI_GREEN_NORMAL)
+        return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: surface / bulk Green's functions are not supported");
     if (h->nblk != 1) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: spin blocks are not supported");
     if (h->kp & (h->kp - 1)) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: kpoints must be a power of two");
     if (h->Q > 128) return fail(h, CQPI_ERR_NOT_SUPPORTED, "adjoint: oversamp^2 must be <= 128");
@@ -1381,6 +1463,7 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
 int cqpi_get_bands(cqpi_handle *h, double *eval, double *evec)
 {
     if (!h) return CQPI_ERR_ARG;
+    if (h->gmode != CQPI_GREEN_NORMAL) return fail(h, CQPI_ERR_NOT_SUPPORTED, "no eigen cache in the surface / bulk modes");
     const size_t nk = (size_t)h->kp * h->kp, b = h->b, bb = b * b;
     try {
         if (!h->bands_ready) do_bands(h);
@@ -1590,6 +1673,49 @@ int cqpi_wannierjosephson(cqpi_handle *h, const double *T, const double *g0r, co
     if (!h || !tip) return fail(h, CQPI_ERR_ARG, "null argument");
     if (!h->josephson) return fail(h, CQPI_ERR_STATE, "cqpi_set_josephson has not been called");
     return seam_contract(h, T, g0r, tip, false);
+}
+
+int cqpi_set_greens(cqpi_handle *h, int32_t mode, double epserr, const cqpi_model *smodel)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (mode != CQPI_GREEN_NORMAL && mode != CQPI_GREEN_SURFACE && mode != CQPI_GREEN_BULK)
+        return fail(h, CQPI_ERR_ARG, "unknown Green's function mode");
+    if (mode != CQPI_GREEN_NORMAL) {
+        if (!(epserr > 0.0)) return fail(h, CQPI_ERR_ARG, "epserr must be positive");
+        if (h->b > 8) return fail(h, CQPI_ERR_NOT_SUPPORTED, "surface / bulk Green's functions: at most 8 bands");
+        if (smodel) {
+            if (smodel->bands != h->b) return fail(h, CQPI_ERR_ARG, "the surface model must have the model's band count");
+            if (smodel->nhops < 0 || (smodel->nhops > 0 && (!smodel->R || !smodel->orb || !smodel->t)))
+                return fail(h, CQPI_ERR_ARG, "invalid surface model");
+            for (int64_t i = 0; i < smodel->nhops; i++)
+                if (smodel->orb[2 * i] < 0 || smodel->orb[2 * i] >= h->b || smodel->orb[2 * i + 1] < 0 ||
+                    smodel->orb[2 * i + 1] >= h->b)
+                    return fail(h, CQPI_ERR_ARG, "surface model orbital index out of range");
+        }
+    }
+    const int old = h->gmode;
+    h->gmode = mode;
+    h->epserr = epserr;
+    h->surf_own_model = mode != CQPI_GREEN_NORMAL && smodel != nullptr;
+    h->surf_R.clear();
+    h->surf_orb.clear();
+    h->surf_t.clear();
+    h->surf_anti.clear();
+    if (h->surf_own_model) {
+        h->surf_R.assign(smodel->R, smodel->R + 3 * smodel->nhops);
+        h->surf_orb.assign(smodel->orb, smodel->orb + 2 * smodel->nhops);
+        h->surf_t.assign(smodel->t, smodel->t + 2 * smodel->nhops);
+        for (int64_t i = 0; i < smodel->nhops; i++) h->surf_anti.push_back(smodel->anti && smodel->anti[i] ? 1 : 0);
+    }
+    // the k-space data and the G0(k) buffers depend on the mode
+    h->bands_ready = false;
+    if ((old == CQPI_GREEN_NORMAL) != (mode == CQPI_GREEN_NORMAL)) {
+        free_workspace(h);
+        free_adj(h);
+    }
+    sr_drop(h);
+    return CQPI_OK;
 }
 
 int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat)

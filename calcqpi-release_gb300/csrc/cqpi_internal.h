@@ -91,6 +91,17 @@ struct AdjWorkspace {
     double2 *gR = nullptr;     // [nR][2][b*b]      dL/dtn, dL/dta per unique R
 };
 
+// Hopping terms of the surface / bulk Green's function on the device: three sets (surface
+// in-plane, bulk in-plane, bulk R_z < 0) packed one after the other, and the k-dependent
+// matrices eps_s, eps_b, alpha [3][kp*kp][b*b] built from them.
+struct SurfaceTerms {
+    int ns = 0, nb = 0, no = 0, off_s = 0, off_b = 0, off_o = 0;
+    int4 *d_i = nullptr;        // (rx, ry, o1, o2)
+    double2 *d_t = nullptr;     // amplitudes
+    int *d_anti = nullptr;
+    double2 *d_mats = nullptr;
+};
+
 struct Workspace {
     int ebatch = 0;
     double2 *g0k = nullptr;
@@ -188,6 +199,17 @@ struct cqpi_handle {
     double2 *d_tip_all = nullptr, *h_tip_pinned = nullptr;
     const double2 *jos_tip = nullptr;
     double2 *d_seam_tip = nullptr;
+    // surface / bulk Green's function: mode, tolerance, the surface model's in-plane terms
+    // (host; empty = the model itself) and the device terms and matrices
+    int gmode = 0;
+    double epserr = 1e-5;
+    bool surf_own_model = false;
+    std::vector<int32_t> surf_R, surf_orb;
+    std::vector<double> surf_t;
+    std::vector<uint8_t> surf_anti;
+    std::vector<int32_t> hop_rx, hop_ry, hop_rz;   // R of every model term
+    std::vector<double> hop_t;                     // current amplitudes of the model terms
+    cqpi::SurfaceTerms surf;
     // proximity-list form of the wannier mode (threshold keyword, mkthresholdlist +
     // tmatrix::calcwannierldos(os, w, flaglist)): host copy of the orbitals the list is built
     // from, the list's parameters, and the list on the device, CSR by (d1, q): entry s holds
@@ -260,6 +282,9 @@ void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vect
 void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorkspace &aw);
 void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw);
 void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
+// surface.cu
+void launch_surface_mats(cqpi_handle *h);
+void launch_greens_surface(cqpi_handle *h, int ne, const double *d_energies);
 // ldos_list.cu
 size_t list_smem_bytes(const cqpi_handle *h, bool fp64);
 cudaError_t configure_list(cqpi_handle *h);

@@ -3,7 +3,8 @@
 //
 // Mirrors the reference driver src/calcqpi.cc:131-811 for output=wannier and
 // output=josephson (:225, :249-251 deltat/etat, :451-460, :643-646, :705-709),
-// green=normal: the same keywords and defaults (:133-137), model load (:277-292),
+// green=normal|surface|bulk (stbfile, epserr; :203-209, :293-307, :683-688): the same
+// keywords and defaults (:133-137), model load (:277-292),
 // scattering setup (:254-272, :393-395), orbital setup from idlorbitalfile, XSF
 // orbitalfiles (:577-600)
 // (:483-518) or analytic orbitals (:519-576), wffile output (:602-618), the map
@@ -11,7 +12,7 @@
 // (:640-656), layer energies idl::getbias (src/idl.cc:969-973) and the final save
 // (:779-783), the proximity list of the threshold / spinarr keywords (:238, :619-635,
 // :700-701).  Modes and keywords outside that path (spf, uspf, nomode,
-// green=surface|bulk, bsfile, dosfile) stop with
+// bsfile, dosfile) stop with
 // an explicit "not supported" error instead of being ignored.
 #include <unistd.h>
 #include <pwd.h>
@@ -137,7 +138,7 @@ void help()
               << "Keywords of the continuum-LDOS (wannier) path:\n"
               << " tbfile, qpifile, output (wannier, josephson), logfile, wffile,\n"
               << " lattice (201), oversamp (4), energies (-1,1), layers (21), kpoints (=lattice),\n"
-              << " green (normal), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
+              << " green (normal|surface|bulk), stbfile, epserr (1e-5), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
               << " pos[i], zheight (5.0), idlorbitalfile, orbitalfiles, deltat (0.001), etat (=eta), threshold,\n"
               << " spinarr\n";
@@ -195,13 +196,17 @@ int main(int argc, char **argv)
         log << "No tightbinding model specified ... exiting.\n";
         return 1;
     }
-    if (lf.has("stbfile")) return not_supported(log, "stbfile (surface Green's function)");
+    std::string stbfile;
+    if (lf.has("stbfile")) stbfile = lf.str("stbfile");
     if (lf.has("fermi")) efermi = lf.value("fermi");
-    if (lf.has("epserr")) lf.value("epserr");
+    double epserr = 1e-5;
+    if (lf.has("epserr")) epserr = lf.value("epserr");
+    int gmode = CQPI_GREEN_NORMAL;   // green keyword (src/calcqpi.cc:206-209)
     if (lf.has("green")) {
         std::string g = lf.field("green");
-        if (g == "surface" || g == "bulk") return not_supported(log, "green=" + g);
-        if (g != "normal") log << "Invalid value for green: " << g << "\n";
+        if (g == "surface") gmode = CQPI_GREEN_SURFACE;
+        else if (g == "bulk") gmode = CQPI_GREEN_BULK;
+        else if (g != "normal") log << "Invalid value for green: " << g << "\n";
     }
     if (lf.has("spin")) {
         std::string s = lf.field("spin");
@@ -283,6 +288,26 @@ int main(int argc, char **argv)
     } else {
         maxbands = bands;
     }
+    // surface-layer model and the principal-layer check (src/calcqpi.cc:293-307)
+    cqpi_hr *shr = nullptr;
+    if (!stbfile.empty()) {
+        log << "Loading surface TB model " << stbfile << "\n";
+        if (cqpi_read_hr(stbfile.c_str(), scmodel ? 1 : 0, &shr) != CQPI_OK) {
+            log << cqpi_host_last_error() << "\n" << "Error loading surface TB model from " << stbfile << ", exiting.\n";
+            return 1;
+        }
+    }
+    if (gmode != CQPI_GREEN_NORMAL) {
+        auto principal = [](const cqpi_hr *m) {
+            for (int64_t i = 0; i < m->nhops; i++)
+                if (std::abs(m->R[3 * i + 2]) > 1 && (m->t[2 * i] != 0.0 || m->t[2 * i + 1] != 0.0)) return false;
+            return true;
+        };
+        if (!principal(hr))
+            log << "Warning: Tight-binding model in file " << tbfile << " is not in principal layer form.\n";
+        if (shr && !principal(shr))
+            log << "Warning: Surface tight-binding model in file " << stbfile << " is not in principal layer form.\n";
+    }
     double maxhop = 0.0;
     for (int64_t i = 0; i < hr->nhops; i++) maxhop = std::max(maxhop, std::hypot(hr->t[2 * i], hr->t[2 * i + 1]));
     if (maxhop / n < eta)
@@ -300,6 +325,7 @@ int main(int argc, char **argv)
         std::ostringstream l;
         l << "Parameters of calculation:\n"
           << "         Tight-binding model  : " << tbfile << "\n"
+          << "         Surface tight-binding model: " << stbfile << "\n"
           << "         Output file for QPI  : " << qpifile << "\n"
           << "         Bands:               : " << maxbands << "\n"
           << "         Lattice              : " << n << "x" << n << "\n"
@@ -309,9 +335,11 @@ int main(int argc, char **argv)
           << "         Fermi energy         : " << efermi << "\n"
           << "         broadening parameter : " << eta << "\n"
           << "         window               : " << window << "\n"
-          << "         oversamp             : " << oversamp << "\n";
+          << "         oversamp             : " << oversamp << "\n"
+          << "         epserr               : " << epserr << "\n";
         if (!std::isnan(threshold)) l << "         threshold            : " << threshold << "\n";
-        l << "         Green's function     : normal\n"
+        l << "         Green's function     : "
+          << (gmode == CQPI_GREEN_SURFACE ? "surface" : gmode == CQPI_GREEN_BULK ? "bulk" : "normal") << "\n"
           << (spin ? "         spin-polarized calculation\n" : "         paramagnetic calculation\n");
         log << l.str();
     }
@@ -541,6 +569,11 @@ int main(int argc, char **argv)
         }
     }
     if (rc == CQPI_OK && josephson) rc = cqpi_set_josephson(h, 1, deltat, etat);
+    if (rc == CQPI_OK && gmode != CQPI_GREEN_NORMAL) {
+        cqpi_model sm = {};
+        if (shr) sm = {shr->bands, shr->scmaxbands, efermi, shr->nhops, shr->R, shr->orb, shr->t, shr->anti};
+        rc = cqpi_set_greens(h, gmode, epserr, shr ? &sm : nullptr);
+    }
     if (rc != CQPI_OK) {
         log << "Error: " << cqpi_last_error(h) << "\n";
         cqpi_destroy(h);
@@ -581,6 +614,7 @@ int main(int argc, char **argv)
     timings.add("Saving data");
     cqpi_destroy(h);
     cqpi_hr_free(hr);
+    if (shr) cqpi_hr_free(shr);
     timings.print(log);
     std::ostringstream un;
     lf.report_unused(un);

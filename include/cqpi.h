@@ -44,9 +44,15 @@ extern "C" {
 #define CQPI_ERR_NOT_SUPPORTED 7
 #define CQPI_ERR_NO_DEVICE 8    /* no CUDA device visible */
 #define CQPI_ERR_TIMEOUT 9      /* a bounded device wait ran out; the kernel stopped early */
+#define CQPI_ERR_NOT_CONVERGED 10 /* the surface / bulk decimation did not reach epserr */
 
 #define CQPI_PREC_FP64 0        /* every stage in FP64 */
 #define CQPI_PREC_MIXED 1       /* FP64 eigen/T/k-sum fold, FP32/tensor-core contraction */
+
+/* Green's function of cqpi_set_greens (the green keyword, src/calcqpi.cc:129,206-209) */
+#define CQPI_GREEN_NORMAL 0     /* G0(k) from the eigen cache */
+#define CQPI_GREEN_SURFACE 1    /* surface Green's function of a layered model */
+#define CQPI_GREEN_BULK 2       /* bulk Green's function of a layered model */
 
 typedef struct cqpi_handle cqpi_handle;
 
@@ -131,6 +137,18 @@ int cqpi_autotune(cqpi_handle *h, const double *energies, int32_t nE, float *bes
 int cqpi_graph_begin(cqpi_handle *h);
 int cqpi_graph_end(cqpi_handle *h);
 int cqpi_graph_launch(cqpi_handle *h);
+
+/* ---- surface / bulk Green's function (green=surface|bulk, stbfile, epserr;
+ * tmatrix::calcsurfacegreensfunction, src/qpi.cc:488-554) -----------------------------
+ * mode CQPI_GREEN_SURFACE / CQPI_GREEN_BULK replaces G0(k) by the decimation over the
+ * layers of the model: the terms with R_z = 0 are the in-plane Hamiltonian, those with
+ * R_z < 0 the coupling to the next layer (principal-layer form); surface_model (NULL = the
+ * model itself; same band count) supplies the in-plane terms of the surface layer; the
+ * iteration stops when the Frobenius norms of both couplings are <= epserr (at most 200
+ * doublings; else the run returns CQPI_ERR_NOT_CONVERGED).  CQPI_GREEN_NORMAL returns to
+ * the eigen-based G0.  Up to 8 bands; cqpi_adjoint and cqpi_get_bands return
+ * CQPI_ERR_NOT_SUPPORTED in these modes. */
+int cqpi_set_greens(cqpi_handle *h, int32_t mode, double epserr, const cqpi_model *surface_model);
 
 /* ---- Josephson mode (output=josephson, src/calcqpi.cc:225,451-460,705-709) -----------
  * enable != 0 switches cqpi_run to the Josephson contraction of

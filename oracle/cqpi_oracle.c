@@ -656,3 +656,126 @@ void orc_wannier_ldos_list(int n, int kp, int b, int os, int w, const double *T,
 #undef G0AT
     free(off);
 }
+
+/* complex b x b inverse by Gauss-Jordan with partial pivoting (the role of
+ * gsl_linalg_complex_LU_decomp + LU_invert in calcgreensfunctioninv); A is destroyed */
+static void zinv(int b, double *A, double *inv)
+{
+    memset(inv, 0, sizeof(double) * 2 * b * b);
+    for (int i = 0; i < b; i++) RE(inv, i * b + i) = 1.0;
+    for (int c = 0; c < b; c++) {
+        int piv = c; double best = -1.0;
+        for (int r = c; r < b; r++) {
+            double a = hypot(RE(A, r * b + c), IM(A, r * b + c));
+            if (a > best) { best = a; piv = r; }
+        }
+        if (piv != c)
+            for (int k = 0; k < b; k++) {
+                double t0 = RE(A, c * b + k), t1 = IM(A, c * b + k);
+                RE(A, c * b + k) = RE(A, piv * b + k); IM(A, c * b + k) = IM(A, piv * b + k);
+                RE(A, piv * b + k) = t0; IM(A, piv * b + k) = t1;
+                t0 = RE(inv, c * b + k); t1 = IM(inv, c * b + k);
+                RE(inv, c * b + k) = RE(inv, piv * b + k); IM(inv, c * b + k) = IM(inv, piv * b + k);
+                RE(inv, piv * b + k) = t0; IM(inv, piv * b + k) = t1;
+            }
+        double pr = RE(A, c * b + c), pi = IM(A, c * b + c), pd = pr * pr + pi * pi;
+        for (int r = 0; r < b; r++) {
+            if (r == c) continue;
+            double mr = RE(A, r * b + c), mi = IM(A, r * b + c);
+            double fr = (mr * pr + mi * pi) / pd, fi = (mi * pr - mr * pi) / pd;
+            for (int k = 0; k < b; k++) {
+                double xr = RE(A, c * b + k), xi = IM(A, c * b + k);
+                RE(A, r * b + k) -= fr * xr - fi * xi; IM(A, r * b + k) -= fr * xi + fi * xr;
+                xr = RE(inv, c * b + k); xi = IM(inv, c * b + k);
+                RE(inv, r * b + k) -= fr * xr - fi * xi; IM(inv, r * b + k) -= fr * xi + fi * xr;
+            }
+        }
+    }
+    for (int r = 0; r < b; r++) {
+        double pr = RE(A, r * b + r), pi = IM(A, r * b + r), pd = pr * pr + pi * pi;
+        for (int k = 0; k < b; k++) {
+            double xr = RE(inv, r * b + k), xi = IM(inv, r * b + k);
+            RE(inv, r * b + k) = (xr * pr + xi * pi) / pd;
+            IM(inv, r * b + k) = (xi * pr - xr * pi) / pd;
+        }
+    }
+}
+
+/* (omega + i eta - H)^-1: tightbindingcontext::calcgreensfunctioninv, tightbinding.h:75-85 */
+static void resolvent(int b, const double *H, double omega, double eta, double *work, double *g)
+{
+    for (int i = 0; i < b * b; i++) { RE(work, i) = -RE(H, i); IM(work, i) = -IM(H, i); }
+    for (int i = 0; i < b; i++) { RE(work, i * b + i) += omega; IM(work, i * b + i) += eta; }
+    zinv(b, work, g);
+}
+
+static double matnorm(int b, const double *A)   /* qpi.cc:55-61 */
+{
+    double v = 0.0;
+    for (int i = 0; i < b * b; i++) v += RE(A, i) * RE(A, i) + IM(A, i) * IM(A, i);
+    return sqrt(v);
+}
+
+/* ---- tmatrix::calcsurfacegreensfunction, qpi.cc:488-554 ----
+ * Per k-point: eps_s = in-plane H of the surface model (or the bulk model), eps_b = in-plane
+ * H of the bulk model (hoppings with R_z = 0, tightbinding.cc:184-207), alpha = the bulk
+ * hoppings with R_z < 0 (no diagonal), beta = alpha^H; renormalise
+ *   g = (w + i eta - eps_b)^-1,  eps_s += a g b,  eps_b += a g b + b g a,
+ *   a = a g a,  b = b g b
+ * until |a|_F <= epserr and |b|_F <= epserr; then G0(k) = (w + i eta - eps_s|eps_b)^-1.
+ * Hopping sets are passed already split (R_z = 0 and R_z < 0); ns < 0 uses the bulk set
+ * for the surface.  max_iter bounds the loop (the reference has no bound); returns the
+ * number of k-points that did not converge.  g0[kp][kp][b][b] as orc_greens_k. */
+int64_t orc_surface_greens_k(int b, int kp,
+                             int64_t nb_, const int32_t *Rb, const int32_t *ob, const double *tb, const uint8_t *ab,
+                             int64_t no, const int32_t *Ro, const int32_t *oo, const double *to, const uint8_t *ao,
+                             int64_t ns, const int32_t *Rs, const int32_t *os_, const double *ts, const uint8_t *as,
+                             double efermi, int scmax, double omega, double eta, double epserr, int surface,
+                             int max_iter, double *g0)
+{
+    size_t cut = (size_t)(kp >> 1), bb = (size_t)b * b;
+    int64_t bad = 0;
+#pragma omp parallel reduction(+ : bad)
+    {
+        double *es = (double *)malloc(sizeof(double) * 2 * bb), *eb = (double *)malloc(sizeof(double) * 2 * bb);
+        double *al = (double *)malloc(sizeof(double) * 2 * bb), *be = (double *)malloc(sizeof(double) * 2 * bb);
+        double *g = (double *)malloc(sizeof(double) * 2 * bb), *w = (double *)malloc(sizeof(double) * 2 * bb);
+        double *b1 = (double *)malloc(sizeof(double) * 2 * bb), *b2 = (double *)malloc(sizeof(double) * 2 * bb);
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < kp; i++)
+            for (int j = 0; j < kp; j++) {
+                double x = ((size_t)i > cut) ? ((double)i - kp) / kp : (double)i / kp;
+                double y = ((size_t)j > cut) ? ((double)j - kp) / kp : (double)j / kp;
+                if (ns >= 0) orc_hk(b, ns, Rs, os_, ts, as, efermi, scmax, x, y, es);
+                else orc_hk(b, nb_, Rb, ob, tb, ab, efermi, scmax, x, y, es);
+                orc_hk(b, nb_, Rb, ob, tb, ab, efermi, scmax, x, y, eb);
+                orc_hk(b, no, Ro, oo, to, ao, 0.0, scmax, x, y, al);   /* no diagonal */
+                for (int r = 0; r < b; r++)
+                    for (int c = 0; c < b; c++) {
+                        RE(be, r * b + c) = RE(al, c * b + r);
+                        IM(be, r * b + c) = -IM(al, c * b + r);
+                    }
+                int it = 0;
+                do {
+                    resolvent(b, eb, omega, eta, w, g);
+                    zmul(b, g, be, b1);
+                    zmul(b, al, b1, b2);              /* a g b */
+                    for (size_t e = 0; e < 2 * bb; e++) { es[e] += b2[e]; eb[e] += b2[e]; }
+                    zmul(b, g, al, b1);
+                    zmul(b, be, b1, b2);              /* b g a */
+                    for (size_t e = 0; e < 2 * bb; e++) eb[e] += b2[e];
+                    zmul(b, g, al, b1);
+                    zmul(b, al, b1, b2);
+                    memcpy(al, b2, sizeof(double) * 2 * bb);
+                    zmul(b, g, be, b1);
+                    zmul(b, be, b1, b2);
+                    memcpy(be, b2, sizeof(double) * 2 * bb);
+                    it++;
+                } while ((matnorm(b, al) > epserr || matnorm(b, be) > epserr) && it < max_iter);
+                if (matnorm(b, al) > epserr || matnorm(b, be) > epserr) bad++;
+                resolvent(b, surface ? es : eb, omega, eta, w, g0 + 2 * (((size_t)i * kp + j) * bb));
+            }
+        free(es); free(eb); free(al); free(be); free(g); free(w); free(b1); free(b2);
+    }
+    return bad;
+}

@@ -60,6 +60,9 @@ def lib():
             L.orc_threshold_list.argtypes = [i32, i32, i32, P, dbl, i32, i32, P, P, P, i64]
             L.orc_threshold_list.restype = i64
             L.orc_wannier_ldos_list.argtypes = [i32, i32, i32, i32, i32, P, P, i64, P, P, P, i32, i32]
+            L.orc_surface_greens_k.argtypes = [i32, i32, i64, P, P, P, P, i64, P, P, P, P, i64, P, P, P, P,
+                                               dbl, i32, dbl, dbl, dbl, i32, i32, P]
+            L.orc_surface_greens_k.restype = i64
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -204,6 +207,34 @@ def wannier_ldos_list(n, kp, os_, w, T, g0r, ent, fac, rows=None) -> np.ndarray:
     return out
 
 
+def _split(model: Model, sel):
+    R = np.ascontiguousarray(model.R[sel])
+    o = np.ascontiguousarray(model.orb[sel])
+    t = np.ascontiguousarray(model.t[sel])
+    a = np.ascontiguousarray(model.anti[sel])
+    return len(t), R, o, t, a
+
+
+def surface_greens_k(model: Model, kp: int, omega: float, eta: float, epserr: float, surface: bool,
+                     smodel: Model = None, max_iter: int = 1000) -> np.ndarray:
+    """tmatrix::calcsurfacegreensfunction, src/qpi.cc:488-554 (green=surface / bulk):
+    g0[kp, kp, b, b].  Raises if a k-point does not converge within max_iter."""
+    b = model.bands
+    nb_, Rb, ob, tb, ab = _split(model, model.R[:, 2] == 0)
+    no, Ro, oo, to, ao = _split(model, model.R[:, 2] < 0)
+    if smodel is not None:
+        ns, Rs, os_, ts, as_ = _split(smodel, smodel.R[:, 2] == 0)
+    else:
+        ns, Rs, os_, ts, as_ = -1, Rb, ob, tb, ab
+    g = np.zeros((kp, kp, b, b), np.complex128)
+    bad = lib().orc_surface_greens_k(b, kp, nb_, _p(Rb), _p(ob), _p(tb), _p(ab), no, _p(Ro), _p(oo), _p(to),
+                                     _p(ao), ns, _p(Rs), _p(os_), _p(ts), _p(as_), model.efermi,
+                                     model.scmaxbands, omega, eta, epserr, int(bool(surface)), max_iter, _p(g))
+    if bad:
+        raise RuntimeError("%d k-points did not converge" % bad)
+    return g
+
+
 def set_threads(nt: int):
     lib().orc_set_threads(int(nt))
 
@@ -213,21 +244,24 @@ def num_threads() -> int:
 
 
 def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=None, spin=False, josephson=None,
-        threshold=None, spinarr=None):
+        threshold=None, spinarr=None, green=None, epserr=1e-5, smodel=None):
     """The reference's wannier-mode energy loop (src/calcqpi.cc:673-760, normal Green's
     function): eigen once, then per energy G0(k) -> G0(R) -> T -> LDOS.  Returns maps in
     IDL file order [layer][y][x], float64.  josephson=(deltat, etat) runs the driver's
     josephson mode instead (calcqpi.cc:705-709); threshold (and spinarr) the proximity-list
     form of the wannier mode (calcqpi.cc:619-635,700-701)."""
     m = model.bands if m is None else m
-    ev, U = bands(model, kp)
+    ev, U = bands(model, kp) if green not in ("surface", "bulk") else (None, None)
     maps = []
     if threshold is not None and josephson is None:
         wz = np.asarray(wf, np.float64) if wf_zero is None else \
             np.asarray(wf, np.float64) * (1 - np.asarray(wf_zero, np.float64)[:len(wf), None, None])
         ent, fac = threshold_list(w, os_, wz, threshold, m, spin, spinarr)
     for e in energies:
-        g0r = realspace(greens_k(ev, U, kp, e, eta))
+        if green in ("surface", "bulk"):   # src/calcqpi.cc:675-693
+            g0r = realspace(surface_greens_k(model, kp, e, eta, epserr, green == "surface", smodel))
+        else:
+            g0r = realspace(greens_k(ev, U, kp, e, eta))
         T = tmatrix(vscat, g0r[0, 0])
         if threshold is not None and josephson is None:
             maps.append(wannier_ldos_list(n, kp, os_, w, T, g0r, ent, fac).T)

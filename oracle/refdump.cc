@@ -17,11 +17,12 @@
 //
 // With "X height k file_0 prefact_0 ..." the orbitals are the XSF files, loaded by the
 // reference's wannierfunctions(file, height, window, oversamp, prefact) (the orbitalfiles
-// keyword); wfbin is then ignored.
+// keyword); wfbin is then ignored.  With "G surface|bulk epserr stbfile" the Green's function
+// is tmatrix::calcsurfacegreensfunction (green=surface|bulk, "-" = no stbfile).
 //
 // usage: refdump <hrfile> <wfbin> <out> n kp os w eta efermi spin maxband layers
 //                lenergy henergy scmodel nscat [vre vim]... [J deltat etat | T thr | S thr k s...]
-//                [X height k file prefact ...]
+//                [X height k file prefact ...] [G surface|bulk epserr stbfile|-]
 // wfbin: int32 norb, int32 side, float64 [norb][side][side]
 // out:   per layer: float64 dos (tmatrix::calcdos), float64 ldos[y][x]
 #include <cstdio>
@@ -61,6 +62,9 @@ int main(int argc, char **argv)
     vector<int> spinarr;
     vector<string> xsffiles;
     vector<double> xsfpre;
+    int gmode = 0;              // 1 surface, 2 bulk Green's function (src/calcqpi.cc:683-688)
+    double epserr = 1e-5;
+    string stbfile = "-";
     for (int a = 17 + 2 * nscat; a < argc;) {
         const string opt = argv[a];
         if (opt == "J" && a + 2 < argc) {
@@ -72,6 +76,11 @@ int main(int argc, char **argv)
             const int k = atoi(argv[a + 2]);
             for (int i = 0; i < k; i++) spinarr.push_back(atoi(argv[a + 3 + i]));
             a += 3 + k;
+        } else if (opt == "G" && a + 3 < argc) {
+            gmode = string(argv[a + 1]) == "surface" ? 1 : 2;
+            epserr = atof(argv[a + 2]);
+            stbfile = argv[a + 3];
+            a += 4;
         } else if (opt == "X" && a + 2 < argc) {
             xsfheight = atof(argv[a + 1]);
             const int k = atoi(argv[a + 2]);
@@ -88,6 +97,11 @@ int main(int argc, char **argv)
 
     tightbind *model = new tightbind(string(hr), efermi, scmodel);
     if (!*model) { cerr << "model load failed" << endl; return 1; }
+    tightbind *smodel = nullptr;
+    if (gmode && stbfile != "-") {
+        smodel = new tightbind(stbfile, efermi, scmodel);
+        if (!*smodel) { cerr << "surface model load failed" << endl; return 1; }
+    }
     vector<wannierfunctions> wfs;
     size_t norb = 0;
     if (!xsffiles.empty()) {
@@ -134,7 +148,8 @@ int main(int argc, char **argv)
     FILE *o = fopen(outp, "wb");
     for (size_t k = 0; k < layers; k++) {
         double energy = ldosmap.getbias(k);
-        tm->setgreensfunction(energy);
+        if (gmode) tm->calcsurfacegreensfunction(energy, epserr, gmode == 1, smodel);
+        else tm->setgreensfunction(energy);
         tm->calcrealspacegreensfunction();
         double dos = tm->calcdos(maxband);
         if (josephson) {

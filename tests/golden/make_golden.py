@@ -89,6 +89,35 @@ def bdg_spin():
     return bdg(base, 0.08 * np.eye(2, dtype=complex))
 
 
+def stacked(base: dict, tz: dict) -> dict:
+    """A layered model: the in-plane terms of base plus interlayer terms tz[(rx, ry)] at
+    R_z = +1 and their Hermitian partners at R_z = -1 (principal-layer form)."""
+    terms = {k: v.copy() for k, v in base.items()}
+    for (rx, ry), M in tz.items():
+        terms[(rx, ry, 1)] = terms.get((rx, ry, 1), 0) + M
+        terms[(-rx, -ry, -1)] = terms.get((-rx, -ry, -1), 0) + np.conj(M).T
+    return terms
+
+
+def c1_layered():
+    return stacked(W.square_c1().terms(), {(0, 0): np.array([[-0.4 + 0j]]), (1, 0): np.array([[0.1 + 0j]]),
+                                           (-1, 0): np.array([[0.1 + 0j]])})
+
+
+def c1_surface_layer():
+    """The surface layer of c1_layered: in-plane hoppings with a 0.2 eV on-site shift."""
+    terms = {k: v.copy() for k, v in W.square_c1().terms().items()}
+    terms[(0, 0, 0)] = terms.get((0, 0, 0), np.zeros((1, 1), complex)) + 0.2
+    return terms
+
+
+def t2g_layered(seed=9):
+    rng = np.random.default_rng(seed)
+    tz = {(0, 0): 0.15 * (rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))),
+          (1, 0): 0.05 * rng.normal(size=(3, 3)) + 0j}
+    return stacked(W.t2g_c2().terms(), tz)
+
+
 CASES = {
     "c1_idl": dict(model="c1", deg=2, n=12, kp=32, os=4, w=2, layers=3, energies=(-0.2, 0.2), eta=0.05,
                    scattering=(0.5,), orbitals=("idl", "gauss")),
@@ -128,6 +157,13 @@ CASES = {
     "xsf_pad": dict(model="c2", n=5, kp=16, os=2, w=1, layers=2, energies=(-0.08, 0.05), eta=0.02,
                     scattering=(0.3, 0.3, 0.5),
                     orbitals=("xsf", dict(names=["dxz", "dxy"], zheight=0.75, prearr=(0.7, 1.3)))),
+    "surface_c1": dict(model="c1z", green="surface", surface_model=True, n=8, kp=16, os=2, w=1, layers=2,
+                       energies=(-0.3, 0.4), eta=0.05, scattering=(0.5,),
+                       orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "bulk_t2g": dict(model="t2gz", green="bulk", epserr=1e-7, n=6, kp=16, os=2, w=1, layers=2,
+                     energies=(-0.1, 0.15), eta=0.03, scattering=(0.3, 0.3, 0.5), orbitals=("idl", "t2g3")),
+    "surface_t2g": dict(model="t2gz", green="surface", n=6, kp=16, os=2, w=1, layers=1,
+                        energies=(0.05, 0.05), eta=0.03, scattering=(0.3, 0.3, 0.5), orbitals=("idl", "t2g3")),
     "wrap": dict(model="c1", n=20, kp=8, os=2, w=1, layers=1, energies=(0.1, 0.1), eta=0.05, scattering=(0.7,),
                  orbitals=("analytic", dict(names=["px"], radius=0.35, zheight=0.4, angle=20.0))),
 }
@@ -145,6 +181,10 @@ def model_terms(c):
         return m.name, m.bands, m.terms()
     if c["model"] == "bdg":
         return "BdG square lattice (scmodel)", 2, bdg_c1()
+    if c["model"] == "c1z":
+        return "layered square lattice", 1, c1_layered()
+    if c["model"] == "t2gz":
+        return "layered t2g square lattice", 3, t2g_layered()
     if c["model"] == "bdg_t2g":
         return "BdG t2g model (scmodel)", 6, bdg_t2g()
     if c["model"] == "bdg_spin":
@@ -213,6 +253,13 @@ def make_case(name, c):
         lines.append(f"phase={fmt_list(c['phase'])};")
     if "scattering" in c:
         lines.append(f"scattering={fmt_list(c['scattering'])};")
+    if "green" in c:
+        lines.append(f"green={c['green']};")
+        if "epserr" in c:
+            lines.append(f"epserr={c['epserr']!r};")
+        if c.get("surface_model"):
+            F.write_hr(os.path.join(d, "surf_hr.dat"), "surface layer", bands, c1_surface_layer(), None)
+            lines.append('stbfile="surf_hr.dat";')
     if "threshold" in c:
         lines.append(f"threshold={c['threshold']!r};")
     if "spinarr" in c:
@@ -327,6 +374,9 @@ def make_case(name, c):
         args += [repr(v.real), repr(v.imag)]
     if kind == "xsf":
         args += xsf_args
+    if "green" in c:
+        args += ["G", c["green"], repr(c.get("epserr", 1e-5)),
+                 os.path.join(d, "surf_hr.dat") if c.get("surface_model") else "-"]
     if "threshold" in c and not jos:
         if "spinarr" in c:
             args += ["S", repr(c["threshold"]), str(len(c["spinarr"]))] + [str(int(v)) for v in c["spinarr"]]

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 def test_cli_reproduces_reference_output(built_lib, name, tmp_path):
     d, meta, ref = load(name)
     for f in os.listdir(d):
-        if f in ("model_hr.dat", "orbitals.idl", "input.cfg") or f.endswith(".xsf"):
+        if f in ("model_hr.dat", "surf_hr.dat", "orbitals.idl", "input.cfg") or f.endswith(".xsf"):
             shutil.copy(os.path.join(d, f), tmp_path / f)
     r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr

@@ -15,6 +15,24 @@ def _model(d, meta):
     return O.Model.from_hr(hr, efermi=meta.get("fermi", 0.0))
 
 
+def _smodel(d, meta):
+    if not meta.get("surface_model"):
+        return None
+    with open(os.path.join(d, "surf_hr.dat")) as fh:
+        hr = F.read_hr(fh.read(), scmodel=meta.get("scmodel", False))
+    return O.Model.from_hr(hr, efermi=meta.get("fermi", 0.0))
+
+
+def _g0r(m, meta, d, e, cache):
+    if meta.get("green"):
+        return O.realspace(O.surface_greens_k(m, meta["kp"], e, meta["eta"], meta.get("epserr", 1e-5),
+                                              meta["green"] == "surface", _smodel(d, meta)))
+    if "eig" not in cache:
+        cache["eig"] = O.bands(m, meta["kp"])
+    ev, U = cache["eig"]
+    return O.realspace(O.greens_k(ev, U, meta["kp"], e, meta["eta"]))
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_oracle_matches_reference_float64(name):
     d, meta, ref = load(name)
@@ -22,13 +40,14 @@ def test_oracle_matches_reference_float64(name):
     E = energies(meta)
     maps = O.run(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], E, ref["vscat"], ref["wf"],
                  ref["zero"], m=meta["maxband"], spin=meta.get("spin", False), josephson=josephson(meta),
-                 threshold=meta.get("threshold"), spinarr=meta.get("spinarr"))
+                 threshold=meta.get("threshold"), spinarr=meta.get("spinarr"), green=meta.get("green"),
+                 epserr=meta.get("epserr", 1e-5), smodel=_smodel(d, meta))
     err = np.abs(maps - ref["ldos"]).max() / np.abs(ref["ldos"]).max()
     assert err < 1e-10, err
     # tmatrix::calcdos = -sum_i<maxband Im G0(R=0)_ii  (src/qpi.cc:856-862)
-    ev, U = O.bands(m, meta["kp"])
+    cache = {}
     for k, e in enumerate(E):
-        g00 = O.realspace(O.greens_k(ev, U, meta["kp"], e, meta["eta"]))[0, 0]
+        g00 = _g0r(m, meta, d, e, cache)[0, 0]
         dos = -np.imag(np.diag(g00))[:meta["maxband"]].sum()
         assert abs(dos - ref["dos"][k]) < 1e-12 * max(1.0, abs(ref["dos"][k]))
 
