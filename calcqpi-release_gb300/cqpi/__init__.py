@@ -28,6 +28,7 @@ EXPORTED = [
     "cqpi_contraction_kind", "cqpi_realspace_greens_noalloc", "cqpi_set_hoppings", "cqpi_adjoint", "cqpi_run_fov",
     "cqpi_graph_begin", "cqpi_graph_end", "cqpi_graph_launch", "cqpi_autotune", "cqpi_set_josephson",
     "cqpi_wannierjosephson", "cqpi_set_threshold", "cqpi_wannierldoslist", "cqpi_set_list", "cqpi_set_greens",
+    "cqpi_spf", "cqpi_uspf", "cqpi_dos",
 ]
 
 
@@ -102,6 +103,9 @@ def load():
     L.cqpi_wannierldoslist.argtypes = [P, P, P]
     L.cqpi_set_list.argtypes = [P, i64, P, P]
     L.cqpi_set_greens.argtypes = [P, i32, dbl, P]
+    L.cqpi_spf.argtypes = [P, P, i32, i32, P, P]
+    L.cqpi_uspf.argtypes = [P, P, i32, i32, P, P, P, P]
+    L.cqpi_dos.argtypes = [P, P, i32, i32, P]
     _lib = L
     return L
 
@@ -282,6 +286,30 @@ class Engine:
                               _ptr(self._so), _ptr(self._st), _ptr(self._sa))
             sm = ctypes.byref(self._sm)
         self._check(self._L.cqpi_set_greens(self._h, int(mode), float(epserr), sm))
+
+    def spf(self, energies, maxband=None):
+        """Spectral function maps [nE][lattice][lattice] (float64, IDL order)."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        out = np.empty((len(e), self.lattice, self.lattice), np.float64)
+        self._check(self._L.cqpi_spf(self._h, _ptr(e), len(e), int(maxband or self.maxband), None, _ptr(out)))
+        return out
+
+    def uspf(self, energies, pos, prearr, maxband=None):
+        """Unfolded spectral function maps [nE][lattice][lattice] (float64, IDL order)."""
+        m = int(maxband or self.maxband)
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        p = np.ascontiguousarray(np.asarray(pos, np.float64)[:, :2].reshape(m, 2))
+        q = np.ascontiguousarray(np.asarray(prearr, np.float64).reshape(m))
+        out = np.empty((len(e), self.lattice, self.lattice), np.float64)
+        self._check(self._L.cqpi_uspf(self._h, _ptr(e), len(e), m, _ptr(p), _ptr(q), None, _ptr(out)))
+        return out
+
+    def dos(self, energies, maxband=None):
+        """-sum_i<maxband Im G0(R=0)_ii per energy."""
+        e = np.ascontiguousarray(energies, np.float64).reshape(-1)
+        out = np.empty(len(e), np.float64)
+        self._check(self._L.cqpi_dos(self._h, _ptr(e), len(e), int(maxband or self.maxband), _ptr(out)))
+        return out
 
     def set_list(self, ent, factor):
         """Explicit proximity list: ent[k] = (list, i, j, o1, o2), factor[k]."""

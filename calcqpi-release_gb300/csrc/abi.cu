@@ -1718,6 +1718,105 @@ int cqpi_set_greens(cqpi_handle *h, int32_t mode, double epserr, const cqpi_mode
     return CQPI_OK;
 }
 
+// Spectral function / unfolded spectral function of all energies into host maps [nE][n][n].
+static int spectral(cqpi_handle *h, int kind, const double *energies, int32_t nE, int32_t maxband, const double *pos,
+                    const double *pre, float *maps32, double *maps64)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (nE < 0 || (nE > 0 && !energies)) return fail(h, CQPI_ERR_ARG, "invalid energy list");
+    if (maxband < 1 || maxband > h->b) return fail(h, CQPI_ERR_ARG, "maxband outside 1..bands");
+    if (kind == 1 && (!pos || !pre)) return fail(h, CQPI_ERR_ARG, "uspf needs orbital positions and prefactors");
+    // tmatrix::calcspf computes nothing unless the k-grid is the lattice (src/qpi.cc:670)
+    if (kind == 0 && h->kp != h->n) return fail(h, CQPI_ERR_ARG, "output=spf needs kpoints = lattice");
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (nE == 0) return CQPI_OK;
+    const size_t mapn = (size_t)h->n * h->n;
+    double *d_pp = nullptr;
+    try {
+        ensure_energies(h, nE);
+        upload_energies(h, energies, nE);
+        ensure_stage64(h, (size_t)nE * mapn);
+        if (!h->bands_ready) do_bands(h);
+        const int mb = kind == 1 ? maxband : 0;
+        std::vector<double> pp(3 * (size_t)std::max(mb, 1), 0.0);
+        for (int i = 0; i < mb; i++) {
+            pp[2 * i] = pos[2 * i];
+            pp[2 * i + 1] = pos[2 * i + 1];
+            pp[2 * (size_t)mb + i] = pre[i];
+        }
+        dalloc(&d_pp, pp.size());
+        CK(cudaMemcpyAsync(d_pp, pp.data(), sizeof(double) * pp.size(), cudaMemcpyHostToDevice, h->stream));
+        if (h->gmode == CQPI_GREEN_NORMAL) {
+            launch_spectral(h, kind, nE, 0, h->d_energies_all, maxband, d_pp, d_pp + 2 * mb, h->stage64);
+            check_launch();
+        } else {
+            const int eb = choose_batch(h, nE);
+            ensure_workspace(h, eb);
+            for (int e0 = 0; e0 < nE; e0 += eb) {
+                const int ne = std::min(eb, nE - e0);
+                launch_greens_surface(h, ne, h->d_energies_all + e0);
+                check_launch();
+                launch_spectral(h, kind, ne, e0, h->d_energies_all + e0, maxband, d_pp, d_pp + 2 * mb, h->stage64);
+                check_launch();
+            }
+        }
+        std::vector<double> host((size_t)nE * mapn);
+        CK(cudaMemcpyAsync(host.data(), h->stage64, sizeof(double) * host.size(), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        dfree(d_pp);
+        d_pp = nullptr;
+        if (maps64) std::copy(host.begin(), host.end(), maps64);
+        if (maps32)
+            for (size_t i = 0; i < host.size(); i++) maps32[i] = (float)host[i];
+        if (const int st = read_status(h)) return status_code(h, st, "the spectral function");
+    } catch (const CudaError &e) {
+        if (d_pp) cudaFree(d_pp);
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
+int cqpi_spf(cqpi_handle *h, const double *energies, int32_t nE, int32_t maxband, float *maps32, double *maps64)
+{
+    return spectral(h, 0, energies, nE, maxband, nullptr, nullptr, maps32, maps64);
+}
+
+int cqpi_uspf(cqpi_handle *h, const double *energies, int32_t nE, int32_t maxband, const double *pos,
+              const double *prearr, float *maps32, double *maps64)
+{
+    return spectral(h, 1, energies, nE, maxband, pos, prearr, maps32, maps64);
+}
+
+int cqpi_dos(cqpi_handle *h, const double *energies, int32_t nE, int32_t maxband, double *dos)
+{
+    if (!h) return CQPI_ERR_ARG;
+    if (nE < 0 || (nE > 0 && (!energies || !dos))) return fail(h, CQPI_ERR_ARG, "invalid energies or output");
+    if (maxband < 1 || maxband > h->b) return fail(h, CQPI_ERR_ARG, "maxband outside 1..bands");
+    if (h->capturing) return fail(h, CQPI_ERR_STATE, "not during a capture");
+    if (nE == 0) return CQPI_OK;
+    try {
+        const int eb = choose_batch(h, nE);
+        ensure_workspace(h, eb);
+        ensure_energies(h, nE);
+        ensure_stage64(h, (size_t)nE);
+        upload_energies(h, energies, nE);
+        if (!h->bands_ready) do_bands(h);
+        for (int e0 = 0; e0 < nE; e0 += eb) {
+            const int ne = std::min(eb, nE - e0);
+            if (h->ws.gmax) CK(cudaMemsetAsync(h->ws.gmax, 0, sizeof(unsigned) * ne, h->stream));
+            do_greens(h, ne, h->d_energies_all + e0);
+            launch_dos(h, ne, maxband, h->stage64 + e0);
+            check_launch();
+        }
+        CK(cudaMemcpyAsync(dos, h->stage64, sizeof(double) * nE, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (const int st = read_status(h)) return status_code(h, st, "the density of states");
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
+    return CQPI_OK;
+}
+
 int cqpi_set_josephson(cqpi_handle *h, int32_t enable, double deltat, double etat)
 {
     if (!h) return CQPI_ERR_ARG;

@@ -285,6 +285,10 @@ void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
 // surface.cu
 void launch_surface_mats(cqpi_handle *h);
 void launch_greens_surface(cqpi_handle *h, int ne, const double *d_energies);
+// spectral.cu
+void launch_spectral(cqpi_handle *h, int kind, int ne, int e_base, const double *d_energies, int maxband,
+                     const double *d_pos, const double *d_pre, double *out);
+void launch_dos(cqpi_handle *h, int ne, int maxband, double *dos);
 // ldos_list.cu
 size_t list_smem_bytes(const cqpi_handle *h, bool fp64);
 cudaError_t configure_list(cqpi_handle *h);

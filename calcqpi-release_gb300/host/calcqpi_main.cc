@@ -1,19 +1,17 @@
-// calcqpi_main.cc -- `calcqpi <inputfile>`: the drop-in CLI for the continuum-LDOS
-// ("Wannier mode") path, running on the GB300 engine through the C ABI.
+// calcqpi_main.cc -- `calcqpi <inputfile>`: the drop-in CLI of the reference's driver,
+// running on the GB300 engine through the C ABI.
 //
-// Mirrors the reference driver src/calcqpi.cc:131-811 for output=wannier and
-// output=josephson (:225, :249-251 deltat/etat, :451-460, :643-646, :705-709),
-// green=normal|surface|bulk (stbfile, epserr; :203-209, :293-307, :683-688): the same
-// keywords and defaults (:133-137), model load (:277-292),
-// scattering setup (:254-272, :393-395), orbital setup from idlorbitalfile, XSF
-// orbitalfiles (:577-600)
-// (:483-518) or analytic orbitals (:519-576), wffile output (:602-618), the map
-// idl(os*n, os*n, layers, 2, 2, lenergy, henergy, 0, -1, -1) with its comment line
-// (:640-656), layer energies idl::getbias (src/idl.cc:969-973) and the final save
-// (:779-783), the proximity list of the threshold / spinarr keywords (:238, :619-635,
-// :700-701).  Modes and keywords outside that path (spf, uspf, nomode,
-// bsfile, dosfile) stop with
-// an explicit "not supported" error instead of being ignored.
+// Mirrors src/calcqpi.cc:131-811: the keywords and defaults (:133-137), model load
+// (:277-292), surface-layer model and green=normal|surface|bulk with epserr (:203-209,
+// :293-307, :683-688), scattering setup (:254-272, :393-395), the output modes
+// wannier, josephson (:225, :249-251 deltat/etat, :451-460, :643-646, :705-709), spf / uspf
+// (:333-334, :465-482, :647-652, :712-717) and nomode, the dosfile (:336-391), orbital setup
+// from idlorbitalfile (:483-518), analytic orbitals (:519-576) or XSF orbitalfiles
+// (:577-600), wffile output (:602-618), the proximity list of the threshold / spinarr
+// keywords (:238, :619-635, :700-701), the map idl(n, n, layers, 2, 2, lenergy, henergy, 0,
+// -1, -1) with its comment line (:638-656), layer energies idl::getbias (src/idl.cc:969-973)
+// and the final save (:779-783).  The band-structure histogram (bsfile) stops with an
+// explicit "not supported" error instead of being ignored.
 #include <unistd.h>
 #include <pwd.h>
 
@@ -136,7 +134,8 @@ void help()
     std::cerr << "calcqpi (GB300 continuum-LDOS engine, " << cqpi_version() << ")\n\n"
               << "Syntax:\ncalcqpi configfile\n\n"
               << "Keywords of the continuum-LDOS (wannier) path:\n"
-              << " tbfile, qpifile, output (wannier, josephson), logfile, wffile,\n"
+              << " tbfile, qpifile, output (wannier, josephson, spf, uspf, nomode), logfile, wffile, dosfile,\n"
+              << " doslayers (101), dosenergies ((-0.1,0.1)),\n"
               << " lattice (201), oversamp (4), energies (-1,1), layers (21), kpoints (=lattice),\n"
               << " green (normal|surface|bulk), stbfile, epserr (1e-5), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
@@ -220,11 +219,14 @@ int main(int argc, char **argv)
         else if (s == "false") scmodel = false;
         else log << "Invalid value for scmodel: " << s << "\n";
     }
-    bool josephson = false;
+    // output mode (src/calcqpi.cc:127,221-229)
+    enum { OUT_WANNIER, OUT_JOSEPHSON, OUT_SPF, OUT_USPF, OUT_NONE } outmode = OUT_WANNIER;
     if (lf.has("output")) {
         std::string o = lf.field("output");
-        if (o == "spf" || o == "uspf" || o == "nomode") return not_supported(log, "output=" + o);
-        if (o == "josephson") josephson = true;
+        if (o == "josephson") outmode = OUT_JOSEPHSON;
+        else if (o == "spf") outmode = OUT_SPF;
+        else if (o == "uspf") outmode = OUT_USPF;
+        else if (o == "nomode") outmode = OUT_NONE;
         else if (o != "wannier") {
             log << "Unrecognized output mode.";
             return 1;
@@ -250,6 +252,9 @@ int main(int argc, char **argv)
     if (lf.has("deltat")) deltat = lf.value("deltat");
     if (lf.has("kpoints")) kpoints = lf.ivalue("kpoints");
     if (!kpoints) kpoints = n;
+    if (outmode == OUT_SPF) kpoints = n;   // src/calcqpi.cc:333-334
+    const bool josephson = outmode == OUT_JOSEPHSON;
+    const bool kspace = outmode == OUT_SPF || outmode == OUT_USPF || outmode == OUT_NONE;   // no orbitals needed
     if (lf.has("phase")) {
         std::vector<double> ph = lf.vec("phase");
         ph.resize(2, 0.0);
@@ -267,7 +272,20 @@ int main(int argc, char **argv)
     }
     if (lf.has("magscat")) magscat = lf.value("magscat");
     if (lf.has("bsfile")) return not_supported(log, "bsfile (band-structure histogram)");
-    if (lf.has("dosfile")) return not_supported(log, "dosfile (density of states output)");
+    // density of states file (src/calcqpi.cc:336-391)
+    std::string dosfile;
+    size_t doslayers = 101;
+    double doslenergy = -0.1, doshenergy = 0.1;
+    if (lf.has("dosfile")) {
+        dosfile = lf.str("dosfile");
+        if (lf.has("doslayers")) doslayers = lf.ivalue("doslayers");
+        if (lf.has("dosenergies")) {
+            std::vector<double> de = lf.vec("dosenergies");
+            de.resize(2, 0.0);
+            doslenergy = de[0];
+            doshenergy = de[1];
+        }
+    }
 
     log << "Loading TB model " << tbfile << "\n";
     cqpi_hr *hr = nullptr;
@@ -351,14 +369,36 @@ int main(int argc, char **argv)
             log << "Error: Calculation in josephson-mode with scmodel=false makes no sense - exiting.\n";
             return 1;
         }
-    } else {
+    } else if (outmode == OUT_WANNIER) {
         log << "QPI calculations in Wannier-mode (cLDOS).\n";
+    } else if (outmode == OUT_SPF) {
+        log << "Calculations of spectral function.\n";
+    } else if (outmode == OUT_USPF) {
+        log << "Calculations of unfolded spectral function.\n";
     }
+    // band positions of the unfolded spectral function (src/calcqpi.cc:465-478)
+    std::vector<double> uspf_pos;
+    if (outmode == OUT_USPF)
+        for (size_t i = 0; i < maxbands; i++) {
+            std::ostringstream key;
+            key << "pos[" << i << "]";
+            if (lf.has(key.str())) {
+                std::vector<double> pos = lf.vec(key.str());
+                pos.resize(2, 0.0);
+                uspf_pos.push_back(pos[0]);
+                uspf_pos.push_back(pos[1]);
+            } else {
+                uspf_pos.push_back(0.0);
+                uspf_pos.push_back(0.0);
+                log << "No position found for band " << i << ", using (0,0,0).\n";
+            }
+        }
 
     // ---------------------------------------------------------------- orbitals
     std::vector<double> prearr;
     if (lf.has("prearr")) prearr = lf.vec("prearr");
     prearr.resize(maxbands, 1.0);
+    const std::vector<double> uspf_pre = prearr;   // before the orbital setups resize it
     std::vector<std::vector<double>> wfs;   // each (2w+1)os squared
     std::vector<uint8_t> zero;
     size_t side = 0;
@@ -510,7 +550,7 @@ int main(int argc, char **argv)
             // the wffile output shows them
             for (size_t i = 0; i < maxbands; i++) { wfs.push_back(std::vector<double>(side * side, 0.0)); zero.push_back(1); }
         }
-    } else {
+    } else if (!kspace) {
         log << "No orbitals specified (orbitals=, idlorbitalfile= or orbitalfiles=) - exiting.\n";
         return 1;
     }
@@ -526,7 +566,7 @@ int main(int argc, char **argv)
         cqpi_idl_write(lf.str("wffile").c_str(), c.str().c_str(), nullptr, (int32_t)side, (int32_t)side,
                        (int32_t)wfs.size(), sr, of, bi, 0.0, d.data());
     }
-    if (wfs.size() < maxbands) {
+    if (wfs.size() < maxbands && !kspace) {
         log << "Fewer orbitals than bands - exiting.\n";
         return 1;
     }
@@ -548,7 +588,7 @@ int main(int argc, char **argv)
     }
     std::vector<double> wflat(wfs.size() * side * side);
     for (size_t o = 0; o < wfs.size(); o++) std::copy(wfs[o].begin(), wfs[o].end(), wflat.begin() + o * side * side);
-    rc = cqpi_set_orbitals(h, wflat.data(), (int32_t)wfs.size(), (int32_t)side, zero.data());
+    if (wfs.size() >= maxbands) rc = cqpi_set_orbitals(h, wflat.data(), (int32_t)wfs.size(), (int32_t)side, zero.data());
     if (rc == CQPI_OK) rc = cqpi_set_scattering(h, vscat.data());
     if (rc == CQPI_OK && !std::isnan(threshold)) {
         log << "Creating threshold list ... done\n";
@@ -579,10 +619,41 @@ int main(int argc, char **argv)
         cqpi_destroy(h);
         return 1;
     }
-    const size_t wn = n * oversamp;
+    if (!dosfile.empty()) {
+        std::ostringstream l;
+        l << "Calculating density of states in energy range (" << doslenergy << "," << doshenergy << ") with "
+          << doslayers << " layers.\n";
+        log << l.str();
+        const double step = (doshenergy - doslenergy) / doslayers;
+        std::vector<double> de(doslayers), dv(doslayers);
+        for (size_t k = 0; k < doslayers; k++) de[k] = doslenergy + k * step;
+        rc = cqpi_dos(h, de.data(), (int32_t)doslayers, (int32_t)maxbands, dv.data());
+        if (rc != CQPI_OK) {
+            log << "Error: " << cqpi_last_error(h) << "\n";
+            cqpi_destroy(h);
+            return 1;
+        }
+        std::ofstream dosout(dosfile.c_str());
+        for (size_t k = 0; k < doslayers; k++) dosout << doslenergy + k * step << " " << dv[k] << std::endl;
+        log << "... done and saved to " << dosfile << ".\n";
+        timings.add("Calculation of density of states");
+    }
+    if (outmode == OUT_NONE) {
+        cqpi_destroy(h);
+        cqpi_hr_free(hr);
+        if (shr) cqpi_hr_free(shr);
+        timings.print(log);
+        return 0;
+    }
+    // maps: lattice*oversamp pixels per side for the real-space modes, lattice for the
+    // spectral functions (src/calcqpi.cc:638-656)
+    const size_t wn = kspace ? n : n * oversamp;
     std::ostringstream comment;
-    comment << (josephson ? "Josephson calculation for " : "CQPI calculation for ") << hr->name << " with window="
-            << window << " and oversamp=" << oversamp;
+    if (outmode == OUT_SPF) comment << "SPF calculation for " << hr->name;
+    else if (outmode == OUT_USPF) comment << "USPF calculation for " << hr->name << " with kpoints=" << kpoints;
+    else
+        comment << (josephson ? "Josephson calculation for " : "CQPI calculation for ") << hr->name << " with window="
+                << window << " and oversamp=" << oversamp;
     timings.add("Initialization of calculation");
 
     std::vector<double> energies(layers);
@@ -597,7 +668,14 @@ int main(int argc, char **argv)
             l << "Calculating layer " << k << " at energy " << std::fixed << std::setprecision(4) << energies[k] << "\n";
             log << l.str();
         }
-        rc = cqpi_run(h, energies.data() + k0, (int32_t)ne, maps.data() + k0 * wn * wn, nullptr, 0);
+        float *dst = maps.data() + k0 * wn * wn;
+        if (outmode == OUT_SPF)
+            rc = cqpi_spf(h, energies.data() + k0, (int32_t)ne, (int32_t)maxbands, dst, nullptr);
+        else if (outmode == OUT_USPF)
+            rc = cqpi_uspf(h, energies.data() + k0, (int32_t)ne, (int32_t)maxbands, uspf_pos.data(), uspf_pre.data(),
+                           dst, nullptr);
+        else
+            rc = cqpi_run(h, energies.data() + k0, (int32_t)ne, dst, nullptr, 0);
         if (rc != CQPI_OK) {
             log << "Error: " << cqpi_last_error(h) << "\n";
             cqpi_destroy(h);

@@ -138,6 +138,22 @@ int cqpi_graph_begin(cqpi_handle *h);
 int cqpi_graph_end(cqpi_handle *h);
 int cqpi_graph_launch(cqpi_handle *h);
 
+/* ---- k-space outputs (output=spf|uspf, dosfile) ------------------------------------
+ * Host maps [nE][lattice][lattice] in IDL order (either pointer may be NULL); synchronous.
+ * cqpi_spf: tmatrix::calcspf(maxband) (src/qpi.cc:659-683), -sum_{l<maxband} Im G0(k)_ll on
+ * the k-grid shifted by kp/2; needs kpoints = lattice (the driver sets it for output=spf,
+ * src/calcqpi.cc:333-334), else CQPI_ERR_ARG.
+ * cqpi_uspf: tmatrix::calcuspf (src/qpi.cc:735-775), unfolded with the orbital positions
+ * pos[maxband][2] (lattice units) and prefactors prearr[maxband]; spin handles sum the two
+ * blocks of maxband/2 orbitals.
+ * cqpi_dos: tmatrix::calcdos after the real-space transform (src/qpi.cc:856-862, the dosfile
+ * loop src/calcqpi.cc:336-391): dos[e] = -sum_{i<maxband} Im G0(R=0)_ii.
+ * All three follow the handle's Green's function (normal, surface, bulk). */
+int cqpi_spf(cqpi_handle *h, const double *energies, int32_t nE, int32_t maxband, float *maps32, double *maps64);
+int cqpi_uspf(cqpi_handle *h, const double *energies, int32_t nE, int32_t maxband, const double *pos,
+              const double *prearr, float *maps32, double *maps64);
+int cqpi_dos(cqpi_handle *h, const double *energies, int32_t nE, int32_t maxband, double *dos);
+
 /* ---- surface / bulk Green's function (green=surface|bulk, stbfile, epserr;
  * tmatrix::calcsurfacegreensfunction, src/qpi.cc:488-554) -----------------------------
  * mode CQPI_GREEN_SURFACE / CQPI_GREEN_BULK replaces G0(k) by the decimation over the

@@ -235,6 +235,42 @@ def surface_greens_k(model: Model, kp: int, omega: float, eta: float, epserr: fl
     return g
 
 
+def spf(g0k: np.ndarray, maxband: int, shift: bool = True) -> np.ndarray:
+    """tmatrix::calcspf, src/qpi.cc:659-683: ldos[x][y] = -sum_{l<maxband} Im G0(k)_ll with
+    k = (x + kp/2) mod kp (shift)."""
+    kp = g0k.shape[0]
+    tr = -np.imag(np.einsum("ijll->ij", g0k[:, :, :maxband, :maxband]))
+    ks = kp >> 1 if shift else 0
+    idx = (np.arange(kp) + ks) % kp
+    return tr[np.ix_(idx, idx)]
+
+
+def uspf(g0k: np.ndarray, n: int, maxband: int, pos, prearr, spin: bool = False) -> np.ndarray:
+    """tmatrix::calcuspf, src/qpi.cc:735-775: the spectral function unfolded with the orbital
+    positions, ldos[i][j] = -sum_{k,l} pre_k pre_l Im(G0(ki,kj)[l][k] e^{2 pi i (kx dx + ky dy)}),
+    dx = pos_k - pos_l, kx = (i - n/2)/kp, ki = ((i + n/2) mod n) mod kp (spin: two blocks)."""
+    kp = g0k.shape[0]
+    h = n >> 1
+    out = np.zeros((n, n))
+    pos = np.asarray(pos, np.float64)
+    pre = np.asarray(prearr, np.float64)
+    blocks = [range(0, maxband >> 1), range(maxband >> 1, 2 * (maxband >> 1))] if spin else [range(maxband)]
+    for i in range(n):
+        kx = (i - h) / kp
+        ki = ((i + h) % n) % kp
+        for j in range(n):
+            ky = (j - h) / kp
+            kj = ((j + h) % n) % kp
+            tr = 0.0
+            for blk in blocks:
+                for k in blk:
+                    for l in blk:
+                        ph = np.exp(1j * 2.0 * np.pi * (kx * (pos[k][0] - pos[l][0]) + ky * (pos[k][1] - pos[l][1])))
+                        tr -= pre[k] * pre[l] * np.imag(g0k[ki, kj, l, k] * ph)
+            out[i, j] = tr
+    return out
+
+
 def set_threads(nt: int):
     lib().orc_set_threads(int(nt))
 
@@ -244,7 +280,8 @@ def num_threads() -> int:
 
 
 def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=None, spin=False, josephson=None,
-        threshold=None, spinarr=None, green=None, epserr=1e-5, smodel=None):
+        threshold=None, spinarr=None, green=None, epserr=1e-5, smodel=None, output="wannier", pos=None,
+        prearr=None):
     """The reference's wannier-mode energy loop (src/calcqpi.cc:673-760, normal Green's
     function): eigen once, then per energy G0(k) -> G0(R) -> T -> LDOS.  Returns maps in
     IDL file order [layer][y][x], float64.  josephson=(deltat, etat) runs the driver's
@@ -257,6 +294,17 @@ def run(model: Model, n, kp, os_, w, eta, energies, vscat, wf, wf_zero=None, m=N
         wz = np.asarray(wf, np.float64) if wf_zero is None else \
             np.asarray(wf, np.float64) * (1 - np.asarray(wf_zero, np.float64)[:len(wf), None, None])
         ent, fac = threshold_list(w, os_, wz, threshold, m, spin, spinarr)
+    if output in ("spf", "uspf"):   # src/calcqpi.cc:675-717: G0(k) only, no transform
+        for e in energies:
+            if green in ("surface", "bulk"):
+                g0k = surface_greens_k(model, kp, e, eta, epserr, green == "surface", smodel)
+            else:
+                g0k = greens_k(ev, U, kp, e, eta)
+            if output == "spf":
+                maps.append(spf(g0k, m).T)
+            else:
+                maps.append(uspf(g0k, n, m, pos, prearr, spin).T)
+        return np.stack(maps)
     for e in energies:
         if green in ("surface", "bulk"):   # src/calcqpi.cc:675-693
             g0r = realspace(surface_greens_k(model, kp, e, eta, epserr, green == "surface", smodel))

@@ -18,11 +18,15 @@
 // With "X height k file_0 prefact_0 ..." the orbitals are the XSF files, loaded by the
 // reference's wannierfunctions(file, height, window, oversamp, prefact) (the orbitalfiles
 // keyword); wfbin is then ignored.  With "G surface|bulk epserr stbfile" the Green's function
-// is tmatrix::calcsurfacegreensfunction (green=surface|bulk, "-" = no stbfile).
+// is tmatrix::calcsurfacegreensfunction (green=surface|bulk, "-" = no stbfile).  "P" writes
+// the spectral function (tmatrix::calcspf, output=spf; pass os = 1 and kp = n), "U k x y pre
+// ..." the unfolded one (tmatrix::calcuspf with k band positions and prefactors); no G0(R),
+// dos written as 0.
 //
 // usage: refdump <hrfile> <wfbin> <out> n kp os w eta efermi spin maxband layers
 //                lenergy henergy scmodel nscat [vre vim]... [J deltat etat | T thr | S thr k s...]
 //                [X height k file prefact ...] [G surface|bulk epserr stbfile|-]
+//                [P | U k x_0 y_0 pre_0 ...]
 // wfbin: int32 norb, int32 side, float64 [norb][side][side]
 // out:   per layer: float64 dos (tmatrix::calcdos), float64 ldos[y][x]
 #include <cstdio>
@@ -63,6 +67,9 @@ int main(int argc, char **argv)
     vector<string> xsffiles;
     vector<double> xsfpre;
     int gmode = 0;              // 1 surface, 2 bulk Green's function (src/calcqpi.cc:683-688)
+    int spfmode = 0;            // 1 output=spf, 2 output=uspf (src/calcqpi.cc:712-717)
+    vector<vector<double> > uspos;
+    vector<double> uspre;
     double epserr = 1e-5;
     string stbfile = "-";
     for (int a = 17 + 2 * nscat; a < argc;) {
@@ -76,6 +83,17 @@ int main(int argc, char **argv)
             const int k = atoi(argv[a + 2]);
             for (int i = 0; i < k; i++) spinarr.push_back(atoi(argv[a + 3 + i]));
             a += 3 + k;
+        } else if (opt == "P") {
+            spfmode = 1;
+            a += 1;
+        } else if (opt == "U" && a + 1 < argc) {
+            spfmode = 2;
+            const int k = atoi(argv[a + 1]);
+            for (int i = 0; i < k; i++) {
+                uspos.push_back(vector<double>{atof(argv[a + 2 + 3 * i]), atof(argv[a + 3 + 3 * i]), 0.0});
+                uspre.push_back(atof(argv[a + 4 + 3 * i]));
+            }
+            a += 2 + 3 * k;
         } else if (opt == "G" && a + 3 < argc) {
             gmode = string(argv[a + 1]) == "surface" ? 1 : 2;
             epserr = atof(argv[a + 2]);
@@ -150,9 +168,16 @@ int main(int argc, char **argv)
         double energy = ldosmap.getbias(k);
         if (gmode) tm->calcsurfacegreensfunction(energy, epserr, gmode == 1, smodel);
         else tm->setgreensfunction(energy);
-        tm->calcrealspacegreensfunction();
-        double dos = tm->calcdos(maxband);
-        if (josephson) {
+        double dos = 0.0;
+        if (!spfmode) {
+            tm->calcrealspacegreensfunction();
+            dos = tm->calcdos(maxband);
+        }
+        if (spfmode == 1) {
+            tm->calcspf(maxband);
+        } else if (spfmode == 2) {
+            tm->calcuspf(maxband, uspos, uspre);
+        } else if (josephson) {
             gsl_complex ocomp = gsl_complex_rect(energy, etat);
             gsl_complex tip = gsl_complex_div(gsl_complex_rect(0.0, -copysign(1.0, energy) * M_PI * deltat),
                                               gsl_complex_sqrt(gsl_complex_sub_real(gsl_complex_mul(ocomp, ocomp),

@@ -164,6 +164,17 @@ CASES = {
                      energies=(-0.1, 0.15), eta=0.03, scattering=(0.3, 0.3, 0.5), orbitals=("idl", "t2g3")),
     "surface_t2g": dict(model="t2gz", green="surface", n=6, kp=16, os=2, w=1, layers=1,
                         energies=(0.05, 0.05), eta=0.03, scattering=(0.3, 0.3, 0.5), orbitals=("idl", "t2g3")),
+    "spf_t2g": dict(model="c2", output="spf", n=16, kp=16, os=2, w=1, layers=2, energies=(-0.1, 0.1), eta=0.02,
+                    scattering=(0.3, 0.3, 0.5), orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "uspf_t2g": dict(model="c2", output="uspf", n=16, kp=16, os=2, w=1, layers=2, energies=(-0.05, 0.08),
+                     eta=0.02, scattering=(0.3, 0.3, 0.5), pos={0: (0.1, 0.2), 1: (-0.2, 0.1)},
+                     prearr=(1.0, 0.8, 1.2), orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "uspf_rect": dict(model="c1", output="uspf", n=12, kp=16, os=2, w=1, layers=1, energies=(0.2, 0.2), eta=0.05,
+                      scattering=(0.5,), pos={0: (0.25, 0.0)},
+                      orbitals=("analytic", dict(names=["s"], radius=0.3, zheight=0.5))),
+    "dos_c2": dict(model="c2", n=6, kp=16, os=2, w=1, layers=1, energies=(0.02, 0.02), eta=0.02,
+                   scattering=(0.3, 0.3, 0.5), dosfile=dict(layers=7, energies=(-0.2, 0.25)),
+                   orbitals=("idl", "t2g3")),
     "wrap": dict(model="c1", n=20, kp=8, os=2, w=1, layers=1, energies=(0.1, 0.1), eta=0.05, scattering=(0.7,),
                  orbitals=("analytic", dict(names=["px"], radius=0.35, zheight=0.4, angle=20.0))),
 }
@@ -243,8 +254,8 @@ def make_case(name, c):
     spin = c.get("spin", False)
     maxband = bands >> 1 if scmodel else bands
     jos = c.get("josephson")
-    lines = ['tbfile="model_hr.dat";', 'qpifile="ref_qpi.idl";',
-             "output=josephson;" if jos else "output=wannier;",
+    outmode = c.get("output", "josephson" if jos else "wannier")
+    lines = ['tbfile="model_hr.dat";', 'qpifile="ref_qpi.idl";', f"output={outmode};",
              f"lattice={n};", f"kpoints={kp};", f"oversamp={os_};", f"window={w};", f"layers={c['layers']};",
              f"energies={fmt_list(c['energies'])};", f"eta={c['eta']!r};"]
     if "fermi" in c:
@@ -262,6 +273,15 @@ def make_case(name, c):
             lines.append('stbfile="surf_hr.dat";')
     if "threshold" in c:
         lines.append(f"threshold={c['threshold']!r};")
+    if outmode == "uspf":
+        for i, pxy in c.get("pos", {}).items():
+            lines.append(f"pos[{i}]={fmt_list(pxy)};")
+        if "prearr" in c:
+            lines.append(f"prearr={fmt_list(c['prearr'])};")
+    if "dosfile" in c:
+        lines.append('dosfile="ref_dos.txt";')
+        lines.append(f"doslayers={c['dosfile']['layers']};")
+        lines.append(f"dosenergies={fmt_list(c['dosfile']['energies'])};")
     if "spinarr" in c:
         lines.append("spinarr=(" + ",".join(str(int(v)) for v in c["spinarr"]) + ");")
     if jos:
@@ -335,7 +355,9 @@ def make_case(name, c):
         lines.append('wffile="ref_wf.idl";')
         cubes = []
         for i, nm in enumerate(names):
-            pos = spec.get("pos", {}).get(i, (0.0, 0.0, 0.0))
+            # pos[i] lines (orbital spec, or the uspf band positions) also place the orbitals
+            pos = tuple(dict(c.get("pos", {}), **spec.get("pos", {})).get(i, (0.0, 0.0, 0.0)))
+            pos = pos + (0.0,) * (3 - len(pos))
             pre = spec.get("prearr", (1.0,) * len(names))[i] if i < len(spec.get("prearr", ())) else 1.0
             cubes.append(O.orbital_cache(nm, w, os_, width=spec["radius"], height=spec["zheight"] - pos[2],
                                          xpos=pos[0], ypos=pos[1],
@@ -367,7 +389,11 @@ def make_case(name, c):
         fh.write(np.array([wf64.shape[0], side], np.int32).tobytes())
         fh.write(np.ascontiguousarray(wf64 * (1 - zero[:wf64.shape[0], None, None])).tobytes())
     outbin = os.path.join(d, "_ldos.bin")
-    args = [os.path.join(REF, "refdump"), os.path.join(d, "model_hr.dat"), wfbin, outbin, str(n), str(kp), str(os_),
+    spfm = outmode in ("spf", "uspf")
+    os_run = 1 if spfm else os_
+    kp_run = n if outmode == "spf" else kp          # output=spf runs on an n x n k-grid (src/calcqpi.cc:333-334)
+    args = [os.path.join(REF, "refdump"), os.path.join(d, "model_hr.dat"), wfbin, outbin, str(n), str(kp_run),
+            str(os_run),
             str(w), repr(c["eta"]), repr(c.get("fermi", 0.0)), str(int(spin)), str(maxband), str(c["layers"]),
             repr(c["energies"][0]), repr(c["energies"][1]), str(int(scmodel)), str(len(vscat))]
     for v in vscat:
@@ -382,13 +408,21 @@ def make_case(name, c):
             args += ["S", repr(c["threshold"]), str(len(c["spinarr"]))] + [str(int(v)) for v in c["spinarr"]]
         else:
             args += ["T", repr(c["threshold"])]
+    if outmode == "spf":
+        args += ["P"]
+    elif outmode == "uspf":
+        args += ["U", str(maxband)]
+        pre = list(c.get("prearr", ())) + [1.0] * maxband
+        for i in range(maxband):
+            pxy = c.get("pos", {}).get(i, (0.0, 0.0))
+            args += [repr(float(pxy[0])), repr(float(pxy[1])), repr(float(pre[i]))]
     if jos:
         # the driver's defaults: deltat 0.001, etat = eta (src/calcqpi.cc:137,249-251)
         args += ["J", repr(0.001 if jos[0] is None else jos[0]), repr(c["eta"] if jos[1] is None else jos[1])]
     r2 = subprocess.run(args, capture_output=True, text=True, timeout=600)
     if r2.returncode != 0:
         raise RuntimeError(f"{name}: refdump failed\n{r2.stderr}")
-    wn = n * os_
+    wn = n * os_run
     raw = np.fromfile(outbin, np.float64).reshape(c["layers"], 1 + wn * wn)
     np.savez_compressed(os.path.join(d, "ref_ldos64.npz"), dos=raw[:, 0], ldos=raw[:, 1:].reshape(-1, wn, wn),
                         vscat=np.array(vscat), wf=wf64, zero=zero)

@@ -31,3 +31,17 @@ def josephson(meta):
     if not j:
         return None
     return (0.001 if j[0] is None else j[0], meta["eta"] if j[1] is None else j[1])
+
+
+def uspf_pos(meta):
+    """Band positions of an output=uspf case, (0, 0) where pos[i] is not given."""
+    if meta.get("output") != "uspf":
+        return None
+    return [tuple(meta.get("pos", {}).get(str(i), (0.0, 0.0)))[:2] for i in range(meta["maxband"])]
+
+
+def uspf_pre(meta):
+    if meta.get("output") != "uspf":
+        return None
+    pre = list(meta.get("prearr", ()))[:meta["maxband"]]
+    return pre + [1.0] * (meta["maxband"] - len(pre))

@@ -30,6 +30,9 @@ def test_cli_reproduces_reference_output(built_lib, name, tmp_path):
     assert dg.shape == dr.shape
     err = np.abs(dg.astype(np.float64) - dr).max() / np.abs(dr).max()
     assert err <= 2e-7, err
+    if os.path.exists(os.path.join(d, "ref_dos.txt")):
+        with open(tmp_path / "ref_dos.txt") as a, open(os.path.join(d, "ref_dos.txt")) as b:
+            assert a.read() == b.read()
     if os.path.exists(os.path.join(d, "ref_wf.idl")):
         hw, dw = F.read_idl(tmp_path / "ref_wf.idl")
         hw0, dw0 = F.read_idl(os.path.join(d, "ref_wf.idl"))
@@ -42,6 +45,6 @@ def test_cli_rejects_out_of_scope_modes(built_lib, tmp_path):
     for f in ("model_hr.dat", "orbitals.idl", "input.cfg"):
         shutil.copy(os.path.join(d, f), tmp_path / f)
     with open(tmp_path / "input.cfg", "a") as fh:
-        fh.write("output=spf;\n")
+        fh.write('bsfile="bs.idl";\n')
     r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "not supported" in r.stdout

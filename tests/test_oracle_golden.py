@@ -4,7 +4,7 @@ import os
 import numpy as np
 import pytest
 
-from golden_cases import NAMES, energies, josephson, load
+from golden_cases import NAMES, energies, josephson, load, uspf_pos, uspf_pre
 from oracle import formats as F
 from oracle import oracle as O
 
@@ -38,12 +38,17 @@ def test_oracle_matches_reference_float64(name):
     d, meta, ref = load(name)
     m = _model(d, meta)
     E = energies(meta)
-    maps = O.run(m, meta["n"], meta["kp"], meta["os"], meta["w"], meta["eta"], E, ref["vscat"], ref["wf"],
+    out = meta.get("output", "wannier")
+    kp = meta["n"] if out == "spf" else meta["kp"]
+    maps = O.run(m, meta["n"], kp, meta["os"], meta["w"], meta["eta"], E, ref["vscat"], ref["wf"],
                  ref["zero"], m=meta["maxband"], spin=meta.get("spin", False), josephson=josephson(meta),
                  threshold=meta.get("threshold"), spinarr=meta.get("spinarr"), green=meta.get("green"),
-                 epserr=meta.get("epserr", 1e-5), smodel=_smodel(d, meta))
+                 epserr=meta.get("epserr", 1e-5), smodel=_smodel(d, meta), output=out, pos=uspf_pos(meta),
+                 prearr=uspf_pre(meta))
     err = np.abs(maps - ref["ldos"]).max() / np.abs(ref["ldos"]).max()
     assert err < 1e-10, err
+    if out in ("spf", "uspf"):
+        return
     # tmatrix::calcdos = -sum_i<maxband Im G0(R=0)_ii  (src/qpi.cc:856-862)
     cache = {}
     for k, e in enumerate(E):
@@ -56,7 +61,8 @@ def test_oracle_matches_reference_float64(name):
 def test_oracle_matches_reference_cli_float32(name):
     d, meta, ref = load(name)
     hdr, data = F.read_idl(os.path.join(d, "ref_qpi.idl"))
-    wn = meta["n"] * meta["os"]
+    # spectral functions are lattice x lattice maps (src/calcqpi.cc:647-652)
+    wn = meta["n"] * (1 if meta.get("output") in ("spf", "uspf") else meta["os"])
     assert hdr["size"] == (wn, wn, meta["layers"])
     # the CLI's float32 map is the float64 map rounded (src/idl.cc:90-92)
     assert np.array_equal(data, ref["ldos"].astype(np.float32)) or \
@@ -140,3 +146,22 @@ def test_threshold_list_count_matches_reference_log(name):
     ent, fac = O.threshold_list(meta["w"], meta["os"], wz, meta["threshold"], meta["maxband"],
                                 meta.get("spin", False), meta.get("spinarr"))
     assert len(fac) == want
+
+
+def test_dosfile_matches_reference_text():
+    """dosfile (src/calcqpi.cc:336-391): energies dosl + k (dosh - dosl) / doslayers and
+    -sum_i<maxband Im G0(R=0)_ii, written with the stream's default 6 significant digits."""
+    d, meta, ref = load("dos_c2")
+    m = _model(d, meta)
+    dl, dh = meta["dosfile"]["energies"]
+    L = meta["dosfile"]["layers"]
+    step = (dh - dl) / L
+    ev, U = O.bands(m, meta["kp"])
+    lines = []
+    for k in range(L):
+        e = dl + k * step
+        g00 = O.realspace(O.greens_k(ev, U, meta["kp"], e, meta["eta"]))[0, 0]
+        dos = -np.imag(np.diag(g00))[:meta["maxband"]].sum()
+        lines.append("%s %s" % (F.cxx_double(e), F.cxx_double(dos)))
+    with open(os.path.join(d, "ref_dos.txt")) as fh:
+        assert fh.read().splitlines() == lines
