@@ -58,6 +58,18 @@ void dfree(T *&p)
     p = nullptr;
 }
 
+// Keep a device buffer of at least count elements, reallocating only when it must grow
+// (cudaFree synchronises the device; repeated uploads of same-sized data avoid it).
+template <class T>
+void dreserve(T **p, size_t &cap, size_t count)
+{
+    if (*p && cap >= count) return;
+    dfree(*p);
+    cap = 0;
+    dalloc(p, count);
+    cap = count;
+}
+
 void free_workspace(cqpi_handle *h)
 {
     dfree(h->ws.g0k);
@@ -173,6 +185,14 @@ void launch_contraction(cqpi_handle *h, int ne, float *o32, double *o64, float *
     } else {
         launch_ldos_fp32(h, ne, h->ws.box32, h->ws.T32, h->ws.term1, o32, o64);
     }
+}
+
+// energies per batch of a run with host outputs (CQPI_HOST_BATCH overrides)
+int host_batch()
+{
+    const char *f = getenv("CQPI_HOST_BATCH");
+    const int v = f ? atoi(f) : 0;
+    return v > 0 ? v : 16;
 }
 
 int choose_batch(const cqpi_handle *h, int nE)
@@ -954,26 +974,25 @@ int cqpi_set_orbitals(cqpi_handle *h, const double *wf, int32_t norb, int32_t si
                     }
                 }
     try {
-        dfree(h->d_phi);
-        dalloc(&h->d_phi, phi.size());
-        CK(cudaMemcpy(h->d_phi, phi.data(), sizeof(double) * phi.size(), cudaMemcpyHostToDevice));
+        // the stream may still read the previous images: uploads are ordered on it
+        dreserve(&h->d_phi, h->cap_phi, phi.size());
+        CK(cudaMemcpyAsync(h->d_phi, phi.data(), sizeof(double) * phi.size(), cudaMemcpyHostToDevice, h->stream));
         std::vector<float> phi32(phi.begin(), phi.end());
-        dfree(h->d_phi32);
-        dalloc(&h->d_phi32, phi32.size());
-        CK(cudaMemcpy(h->d_phi32, phi32.data(), sizeof(float) * phi32.size(), cudaMemcpyHostToDevice));
+        dreserve(&h->d_phi32, h->cap_phi32, phi32.size());
+        CK(cudaMemcpyAsync(h->d_phi32, phi32.data(), sizeof(float) * phi32.size(), cudaMemcpyHostToDevice, h->stream));
+        std::vector<uint16_t> img, imgw;
         if (h->use_tc) {
-            std::vector<uint16_t> img;
             tc_build_a(h, phi, img, h->tc_inv_sA);
-            dfree(h->d_tc_a);
-            dalloc(&h->d_tc_a, img.size());
-            CK(cudaMemcpy(h->d_tc_a, img.data(), sizeof(uint16_t) * img.size(), cudaMemcpyHostToDevice));
+            dreserve(&h->d_tc_a, h->cap_tc_a, img.size());
+            CK(cudaMemcpyAsync(h->d_tc_a, img.data(), sizeof(uint16_t) * img.size(), cudaMemcpyHostToDevice, h->stream));
             if (h->tc.win) {
-                tc_build_a_window(h, phi, img);
-                dfree(h->d_tc_aw);
-                dalloc(&h->d_tc_aw, img.size());
-                CK(cudaMemcpy(h->d_tc_aw, img.data(), sizeof(uint16_t) * img.size(), cudaMemcpyHostToDevice));
+                tc_build_a_window(h, phi, imgw);
+                dreserve(&h->d_tc_aw, h->cap_tc_aw, imgw.size());
+                CK(cudaMemcpyAsync(h->d_tc_aw, imgw.data(), sizeof(uint16_t) * imgw.size(), cudaMemcpyHostToDevice,
+                                   h->stream));
             }
         }
+        CK(cudaStreamSynchronize(h->stream));   // the host vectors are pageable temporaries
     } catch (const CudaError &e) {
         return cuda_fail(h, e);
     }
@@ -1110,7 +1129,10 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
     const size_t mapn = (size_t)h->wn * h->wn;
     const size_t per_e = (size_t)h->nimp * mapn;
     try {
-        const int eb = choose_batch(h, nE);
+        // host outputs: the device-to-host copy (~0.2 TB/s, against ~7 TB/s of HBM) of a batch can
+        // start only when the batch is complete, so batches of a few energies keep the copy of the
+        // last one short while the copies of the others run behind the computation
+        const int eb = on_device ? choose_batch(h, nE) : std::min(choose_batch(h, nE), host_batch());
         if (h->capturing && (h->ws.ebatch < eb || h->energies_cap < nE || !on_device || !h->bands_ready))
             return fail(h, CQPI_ERR_STATE, "capture needs device outputs, solved bands and buffers of an earlier identical call");
         ensure_workspace(h, eb);
@@ -1131,8 +1153,8 @@ int cqpi_run(cqpi_handle *h, const double *energies, int32_t nE, float *maps32, 
             do_bands(h);
             pend(h, 0, a, record(h));
         }
-        for (int e0 = 0, bi = 0; e0 < nE; e0 += eb, bi++) {
-            const int ne = std::min(eb, nE - e0);
+        for (int e0 = 0, bi = 0, ne = 0; e0 < nE; e0 += ne, bi++) {
+            ne = std::min(eb, nE - e0);
             const int slot = bi % nslot;
             const double *den = h->d_energies_all + e0;
             h->jos_tip = h->josephson ? h->d_tip_all + e0 : nullptr;

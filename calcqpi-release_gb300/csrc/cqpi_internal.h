@@ -155,6 +155,7 @@ struct cqpi_handle {
     uint16_t *d_tc_a = nullptr;   // Phi hi/lo operand images
     uint16_t *d_tc_aw = nullptr;  // Phi hi/lo images in the direct-window K order
     float tc_inv_sA = 1.0f;
+    size_t cap_phi = 0, cap_phi32 = 0, cap_tc_a = 0, cap_tc_aw = 0;   // element capacities of the four images
     int num_sms = 0;
     // impurities
     int nimp = 0;

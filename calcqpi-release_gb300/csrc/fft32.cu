@@ -591,9 +591,12 @@ static void launch_rowfft_reg_t(cqpi_handle *h, int ne, const double *d_energies
 {
     const int pg = rowfft_reg_plane_group(h);
     bool eig = false;
-    const size_t smem = rowfft_reg_smem(h, &eig);
+    size_t smem = rowfft_reg_smem(h, &eig);
     const char *f = getenv("CQPI_ROWFFT_EIG");
-    if (f && !strcmp(f, "global")) eig = false;
+    if (f && !strcmp(f, "global") && eig) {
+        eig = false;
+        smem -= rowfft_eig_bytes(h);
+    }
     g0_rowfft_reg_kernel<N1, N2, 4, MAXT><<<h->kp, rowfft_reg_threads<N1, N2, MAXT>(h), smem, h->stream>>>(
         h->b, h->NB, h->Rb, pg, eig ? 1 : 0, h->eta, d_energies, ne, h->d_eval32, h->d_evec32, h->d_tw32, h->ws.half32);
 }
