@@ -52,7 +52,8 @@ def ldos_flops_per_pixel_energy(b, m, W, spin, josephson=False):
 def workload_desc(name, c, m, nE):
     kind = {"C1": "square 1-orbital lattice", "C2": "t2g 3-orbital square lattice",
             "C3": "triangular 5-orbital x spin lattice", "C5": "t2g 3-orbital square lattice",
-            "CJ": "Josephson mode (output=josephson) on the 6-band BdG t2g square lattice"}.get(name, name)
+            "CJ": "Josephson mode (output=josephson) on the 6-band BdG t2g square lattice",
+            "CS": "surface Green's function (green=surface) of the layered t2g lattice"}.get(name, name)
     return (f"{name}: {kind}, k-grid {c.kpoints}^2, FOV {c.lattice}^2 sites, {c.oversamp}x{c.oversamp} px/cell, "
             f"{nE} energies, eta={c.eta}")
 
@@ -65,6 +66,8 @@ def make_engine(cqpi, c, m, wf, vscat, prec):
     eng.set_scattering(vscat)
     if "josephson" in c.extra:
         eng.set_josephson(*c.extra["josephson"])
+    if "green" in c.extra:
+        eng.set_greens(c.extra["green"], c.extra.get("epserr", 1e-5))
     return eng
 
 
@@ -141,10 +144,15 @@ def cpu_sample(cfg_name, target_s=8.0, threads=None):
         O.set_threads(threads)
     c, m, wf = W.config(cfg_name)
     om = O.Model(m.bands, m.R, m.orb, m.t, None, m.efermi, m.scmaxbands)
-    ev, U = O.bands(om, c.kpoints)     # once per run in the reference; not part of the sample
+    # the eigen-solve is once per run in the reference and not part of the sample
+    ev, U = O.bands(om, c.kpoints) if not c.extra.get("green") else (None, None)
     e = float(c.energy_list()[len(c.energy_list()) // 2])
     t0 = time.perf_counter()
-    g0r = O.realspace(O.greens_k(ev, U, c.kpoints, e, c.eta))
+    if c.extra.get("green"):   # tmatrix::calcsurfacegreensfunction, src/qpi.cc:488-554
+        g0k = O.surface_greens_k(om, c.kpoints, e, c.eta, c.extra.get("epserr", 1e-5), c.extra["green"] == "surface")
+    else:
+        g0k = O.greens_k(ev, U, c.kpoints, e, c.eta)
+    g0r = O.realspace(g0k)
     T = O.tmatrix(np.array(c.scattering, complex), g0r[0, 0])
     tg = time.perf_counter() - t0
     jos = c.extra.get("josephson")

@@ -159,6 +159,20 @@ def bdg_t2g_c2(seed: int = 2) -> TBModel:
     return bdg(t2g_c2(seed), D, "BdG t2g square lattice, seed %d (CJ)" % seed)
 
 
+def t2g_layered_c2(seed: int = 9) -> TBModel:
+    """The C2 model stacked into layers (principal-layer form): in-plane terms at R_z = 0,
+    seeded interlayer couplings at R_z = +1 (on site and along x) and their Hermitian partners
+    at R_z = -1, for the surface / bulk Green's functions."""
+    rng = np.random.default_rng(seed)
+    terms = {k: v.copy() for k, v in t2g_c2().terms().items()}
+    tz = {(0, 0): 0.15 * (rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))),
+          (1, 0): 0.05 * rng.normal(size=(3, 3)) + 0j}
+    for (rx, ry), M in tz.items():
+        terms[(rx, ry, 1)] = terms.get((rx, ry, 1), 0) + M
+        terms[(-rx, -ry, -1)] = terms.get((-rx, -ry, -1), 0) + np.conj(M).T
+    return _from_terms(terms, 3, "layered t2g square lattice, seed %d (CS)" % seed)
+
+
 def t2g_c2_parametrisation(seed: int = 2, sigma: float = 0.25):
     """Independent hopping amplitudes of the C2 model family: the symmetrisation of
     t2g_c2 is linear in the raw shell matrices, so every C4-symmetric Hermitian model with
@@ -331,7 +345,8 @@ class Config:
 
 
 def config(name: str) -> tuple:
-    """(Config, TBModel, orbital cube [m, side, side]) for C1, C2, C3, C5 or CJ (Josephson)."""
+    """(Config, TBModel, orbital cube [m, side, side]) for C1, C2, C3, C5, CJ (Josephson) or CS
+    (surface Green's function)."""
     if name == "C1":
         c = Config("C1", 64, 256, 8, 2, 21, (-0.2, 0.2), 0.005, (0.5,))
         return c, square_c1(), gaussian_c1(c.window, c.oversamp)
@@ -349,6 +364,12 @@ def config(name: str) -> tuple:
         c = Config("CJ", 256, 1024, 10, 2, 101, (-0.1, 0.1), 0.002, (0.3, 0.3, 0.5, -0.3, -0.3, -0.5),
                    extra={"josephson": (0.001, 0.002), "maxband": 3})
         return c, bdg_t2g_c2(), t2g_orbitals_c2(c.window, c.oversamp)
+    if name == "CS":
+        # surface Green's function (green=surface) of the layered C2 model: C2 grid and field of
+        # view, 21 energies
+        c = Config("CS", 256, 1024, 10, 2, 21, (-0.1, 0.1), 0.002, (0.3, 0.3, 0.5),
+                   extra={"green": "surface", "epserr": 1e-5})
+        return c, t2g_layered_c2(), t2g_orbitals_c2(c.window, c.oversamp)
     if name == "C5":
         c = Config("C5", 128, 1024, 10, 2, 41, (-0.1, 0.1), 0.002, (0.3, 0.3, 0.5))
         return c, t2g_c2(), t2g_orbitals_c2(c.window, c.oversamp)

@@ -525,15 +525,13 @@ void upload_surface_terms(cqpi_handle *h)
         tt.push_back(make_double2(0.0, 0.0));
         an.push_back(0);
     }
-    dfree(S.d_i);
-    dfree(S.d_t);
-    dfree(S.d_anti);
-    dalloc(&S.d_i, ti.size());
-    dalloc(&S.d_t, tt.size());
-    dalloc(&S.d_anti, an.size());
-    CK(cudaMemcpy(S.d_i, ti.data(), sizeof(int4) * ti.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(S.d_t, tt.data(), sizeof(double2) * tt.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(S.d_anti, an.data(), sizeof(int) * an.size(), cudaMemcpyHostToDevice));
+    dreserve(&S.d_i, S.cap_i, ti.size());
+    dreserve(&S.d_t, S.cap_t, tt.size());
+    dreserve(&S.d_anti, S.cap_anti, an.size());
+    CK(cudaMemcpyAsync(S.d_i, ti.data(), sizeof(int4) * ti.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(S.d_t, tt.data(), sizeof(double2) * tt.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(S.d_anti, an.data(), sizeof(int) * an.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));   // pageable temporaries
     if (!S.d_mats) dalloc(&S.d_mats, (size_t)3 * h->kp * h->kp * h->b * h->b);
 }
 

@@ -99,6 +99,7 @@ struct SurfaceTerms {
     int4 *d_i = nullptr;        // (rx, ry, o1, o2)
     double2 *d_t = nullptr;     // amplitudes
     int *d_anti = nullptr;
+    size_t cap_i = 0, cap_t = 0, cap_anti = 0;
     double2 *d_mats = nullptr;
 };
 
