@@ -70,6 +70,60 @@ void dreserve(T **p, size_t &cap, size_t count)
     cap = count;
 }
 
+// H(k) = sum_R C(R) e^{i theta_R} with C(R) = tn(R) + ta(-R) (normal terms of R, conjugated
+// terms of -R).  The eigen-solve builds it from pairs {R, -R}: C(R) e^{i th} + C(-R) e^{-i th}
+// = P cos th + Q sin th with P = C(R) + C(-R), Q = i (C(R) - C(-R)) (R = 0: P = C(0), Q = 0).
+void upload_pairs(cqpi_handle *h)
+{
+    const int nR = h->nR;
+    const size_t bb = (size_t)h->b * h->b;
+    std::map<std::pair<int, int>, int> idx;
+    for (int r = 0; r < nR; r++) idx[std::make_pair(h->rt_R[2 * r], h->rt_R[2 * r + 1])] = r;
+    auto C = [&](int r, size_t e, double2 &out) {   // C(R_r)[e]
+        out = make_double2(h->rt_tn[2 * (r * bb + e)], h->rt_tn[2 * (r * bb + e) + 1]);
+        auto it = idx.find(std::make_pair(-h->rt_R[2 * r], -h->rt_R[2 * r + 1]));
+        if (it != idx.end()) {
+            out.x += h->rt_ta[2 * (it->second * bb + e)];
+            out.y += h->rt_ta[2 * (it->second * bb + e) + 1];
+        }
+    };
+    std::vector<int32_t> pR;
+    std::vector<double2> pq;
+    std::vector<char> done(nR, 0);
+    for (int r = 0; r < nR; r++) {
+        if (done[r]) continue;
+        const int rx = h->rt_R[2 * r], ry = h->rt_R[2 * r + 1];
+        auto it = idx.find(std::make_pair(-rx, -ry));
+        const int partner = (it != idx.end() && it->second != r) ? it->second : -1;
+        done[r] = 1;
+        if (partner >= 0) done[partner] = 1;
+        pR.push_back(rx);
+        pR.push_back(ry);
+        const size_t base = pq.size();
+        pq.resize(base + 2 * bb);
+        for (size_t e = 0; e < bb; e++) {
+            double2 c1, c2 = make_double2(0.0, 0.0);
+            C(r, e, c1);
+            if (partner >= 0) C(partner, e, c2);
+            if (rx == 0 && ry == 0) {
+                pq[base + e] = c1;
+                pq[base + bb + e] = make_double2(0.0, 0.0);
+            } else {
+                pq[base + e] = make_double2(c1.x + c2.x, c1.y + c2.y);
+                pq[base + bb + e] = make_double2(-(c1.y - c2.y), c1.x - c2.x);   // i (c1 - c2)
+            }
+        }
+    }
+    h->npair_R = (int)(pR.size() / 2);
+    dreserve(&h->d_pR, h->cap_pR, std::max<size_t>(pR.size(), 2));
+    dreserve(&h->d_pPQ, h->cap_pPQ, std::max<size_t>(pq.size(), 1));
+    if (!pR.empty()) {
+        CK(cudaMemcpyAsync(h->d_pR, pR.data(), sizeof(int32_t) * pR.size(), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_pPQ, pq.data(), sizeof(double2) * pq.size(), cudaMemcpyHostToDevice, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));   // pageable temporaries
+}
+
 void free_workspace(cqpi_handle *h)
 {
     dfree(h->ws.g0k);
@@ -829,6 +883,7 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
             CK(cudaMemcpy(h->d_tn, tn.data(), sizeof(double) * tn.size(), cudaMemcpyHostToDevice));
             CK(cudaMemcpy(h->d_ta, ta.data(), sizeof(double) * ta.size(), cudaMemcpyHostToDevice));
         }
+        upload_pairs(h);
         // twiddles e^{+2 pi i t / kp}
         std::vector<double2> tw(h->kp);
         for (int t = 0; t < h->kp; t++) {
@@ -903,6 +958,8 @@ int cqpi_destroy(cqpi_handle *h)
     dfree(h->d_R);
     dfree(h->d_tn);
     dfree(h->d_ta);
+    dfree(h->d_pR);
+    dfree(h->d_pPQ);
     dfree(h->d_tw);
     dfree(h->d_tw32);
     dfree(h->d_eval);
@@ -1396,6 +1453,11 @@ int cqpi_set_hoppings(cqpi_handle *h, const double *t)
     h->rt_tn.swap(tn);
     h->rt_ta.swap(ta);
     h->hop_t.assign(t, t + 2 * h->hop_r.size());
+    try {
+        upload_pairs(h);
+    } catch (const CudaError &e) {
+        return cuda_fail(h, e);
+    }
     h->time_reversal = real && !(f && !strcmp(f, "0"));
     h->bands_ready = false;
     h->sr_model = spin_model_reducible(h);

@@ -7,7 +7,11 @@
 // cyclic complex Jacobi in FP64: G0(k) is invariant under eigenvector phase and
 // ordering, so it matches any exact Hermitian eigensolver to rounding.
 //
-// Roofline: FP64-FLOP bound (GB300 FP64 is ~1/64 of FP32); once per run.
+// Roofline: FP64-FLOP bound (GB300 FP64 is ~1/64 of FP32); once per run.  The sweeps start
+// from FP32 Jacobi eigenvectors (see below), so most rotations run on the FP32 pipe.
+#include <cstdlib>
+#include <cstring>
+
 #include "cqpi_internal.h"
 
 namespace cqpi {
@@ -17,11 +21,12 @@ namespace cqpi {
 // eigenvalues, conjugated eigenvectors); on the self-reflected rows 0 and kp/2 the
 // thread with the larger j' = -j mod kp leaves the pair to its partner.
 template <int B>
-__global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int tr, int scmax, double efermi, int nR,
-                                                    const int32_t *__restrict__ R, const double2 *__restrict__ tn,
-                                                    const double2 *__restrict__ ta, double *__restrict__ eval,
+__global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int tr, int scmax, double efermi, int npr,
+                                                    const int32_t *__restrict__ pR, const double2 *__restrict__ pPQ,
+                                                    double *__restrict__ eval,
                                                     double2 *__restrict__ evec, float2 *__restrict__ evec32,
-                                                    float2 *__restrict__ eval32, const double2 *__restrict__ tw)
+                                                    float2 *__restrict__ eval32, const double2 *__restrict__ tw,
+                                                    int mixed)
 {
     const long long nk = (long long)kp * kp;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -46,28 +51,157 @@ __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int tr, int s
     for (int p = 0; p < B; p++)
         if (p < b) ar[p][p] = (p < scmax) ? -efermi : efermi;
 
-    // H(k) = diag + sum_R tn(R) e^{+i th} + ta(R) e^{-i th},  th = 2 pi (Rx x_i + Ry y_j).
-    // The phase is reduced exactly, (Rx i + Ry j) mod kp (x_i and i/kp differ by an
-    // integer), and read from the FP64 table tw[t] = e^{+2 pi i t / kp}.
-    for (int r = 0; r < nR; r++) {
-        long long mm = ((long long)R[2 * r] * i + (long long)R[2 * r + 1] * j) % kp;
+    // H(k) = diag + sum over {R, -R} pairs of P cos th + Q sin th, th = 2 pi (Rx x_i + Ry y_j)
+    // (P, Q built on the host from the normal and conjugated terms).  Only the lower triangle
+    // is accumulated and then mirrored: the matrix is taken as Hermitian, from its lower
+    // triangle and real diagonal, as gsl_eigen_hermv takes it (src/qpi.cc:470).  The phase is
+    // reduced exactly, (Rx i + Ry j) mod kp (x_i and i/kp differ by an integer), and read from
+    // the FP64 table tw[t] = e^{+2 pi i t / kp}.
+    for (int r = 0; r < npr; r++) {
+        long long mm = ((long long)pR[2 * r] * i + (long long)pR[2 * r + 1] * j) % kp;
         if (mm < 0) mm += kp;
         const double2 ph = __ldg(tw + mm);
         const double c = ph.x, s = ph.y;
-        const double2 *tnr = tn + (size_t)r * bb, *tar = ta + (size_t)r * bb;
+        const double2 *P = pPQ + (size_t)r * 2 * bb, *Q = P + bb;
+#pragma unroll
+        for (int p = 0; p < B; p++)
+#pragma unroll
+            for (int q = 0; q <= p; q++) {
+                if (p < b) {
+                    const double2 x = __ldg(P + p * b + q), y = __ldg(Q + p * b + q);
+                    ar[p][q] += x.x * c + y.x * s;
+                    ai[p][q] += x.y * c + y.y * s;
+                }
+            }
+    }
+#pragma unroll
+    for (int p = 0; p < B; p++) {
+        ai[p][p] = 0.0;
+#pragma unroll
+        for (int q = p + 1; q < B; q++) { ar[p][q] = ar[q][p]; ai[p][q] = -ai[q][p]; }
+    }
+
+    // Mixed precision: cyclic Jacobi in FP32 on a copy of H gives eigenvectors to ~1e-7; they
+    // are orthonormalised in FP64 (modified Gram-Schmidt), H is rotated into that basis in FP64
+    // (A = V^H H V, off-diagonal ~1e-7 of the diagonal) and the FP64 Jacobi below converges in
+    // one or two sweeps instead of five to eight (FP64 runs at 1/64 of the FP32 rate here).
+    if (mixed) {
+        float fr[B][B], fi[B][B], ur[B][B], ui[B][B];
 #pragma unroll
         for (int p = 0; p < B; p++)
 #pragma unroll
             for (int q = 0; q < B; q++) {
-                if (p < b && q < b) {
-                    double2 x = __ldg(tnr + p * b + q), y = __ldg(tar + p * b + q);
-                    ar[p][q] += (x.x + y.x) * c - (x.y - y.y) * s;
-                    ai[p][q] += (x.y + y.y) * c + (x.x - y.x) * s;
+                fr[p][q] = (float)ar[p][q]; fi[p][q] = (float)ai[p][q];
+                ur[p][q] = (p == q) ? 1.f : 0.f; ui[p][q] = 0.f;
+            }
+        for (int sweep = 0; sweep < 12; sweep++) {
+            float off = 0.f, dg = 0.f;
+#pragma unroll
+            for (int p = 0; p < B; p++)
+#pragma unroll
+                for (int q = 0; q < B; q++) {
+                    const float a2 = fr[p][q] * fr[p][q] + fi[p][q] * fi[p][q];
+                    if (p == q) dg += a2; else off += a2;
+                }
+            if (off == 0.f || off <= 1e-13f * dg) break;
+#pragma unroll
+            for (int p = 0; p < B - 1; p++)
+#pragma unroll
+                for (int q = p + 1; q < B; q++) {
+                    const float c2 = fr[p][q] * fr[p][q] + fi[p][q] * fi[p][q];
+                    if (c2 == 0.f) continue;
+                    const float rc = rsqrtf(c2);
+                    const float er = fr[p][q] * rc, ei = fi[p][q] * rc;
+                    const float tau = (fr[q][q] - fr[p][p]) * (0.5f * rc);
+                    const float tt = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+                    const float cs = rsqrtf(1.f + tt * tt), sn = tt * cs;
+#pragma unroll
+                    for (int r = 0; r < B; r++) {
+                        const float xpr = fr[r][p], xpi = fi[r][p];
+                        const float yr = fr[r][q] * er + fi[r][q] * ei, yi = fi[r][q] * er - fr[r][q] * ei;
+                        fr[r][p] = cs * xpr - sn * yr; fi[r][p] = cs * xpi - sn * yi;
+                        fr[r][q] = sn * xpr + cs * yr; fi[r][q] = sn * xpi + cs * yi;
+                        const float vpr = ur[r][p], vpi = ui[r][p];
+                        const float wr = ur[r][q] * er + ui[r][q] * ei, wi = ui[r][q] * er - ur[r][q] * ei;
+                        ur[r][p] = cs * vpr - sn * wr; ui[r][p] = cs * vpi - sn * wi;
+                        ur[r][q] = sn * vpr + cs * wr; ui[r][q] = sn * vpi + cs * wi;
+                    }
+#pragma unroll
+                    for (int cc = 0; cc < B; cc++) {
+                        const float xpr = fr[p][cc], xpi = fi[p][cc];
+                        const float yr = fr[q][cc] * er - fi[q][cc] * ei, yi = fi[q][cc] * er + fr[q][cc] * ei;
+                        fr[p][cc] = cs * xpr - sn * yr; fi[p][cc] = cs * xpi - sn * yi;
+                        fr[q][cc] = sn * xpr + cs * yr; fi[q][cc] = sn * xpi + cs * yi;
+                    }
+                    fr[p][q] = fi[p][q] = fr[q][p] = fi[q][p] = 0.f;
+                    fi[p][p] = 0.f; fi[q][q] = 0.f;
+                }
+        }
+        // V = orthonormalised U (FP64 modified Gram-Schmidt over the b columns)
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+#pragma unroll
+            for (int r = 0; r < B; r++) { vr[r][c] = (double)ur[r][c]; vi[r][c] = (double)ui[r][c]; }
+#pragma unroll
+            for (int c2 = 0; c2 < B; c2++) {
+                if (c2 >= c || c2 >= b) continue;
+                double pr = 0.0, pi = 0.0;   // v_c2^H v_c
+#pragma unroll
+                for (int r = 0; r < B; r++) {
+                    pr += vr[r][c2] * vr[r][c] + vi[r][c2] * vi[r][c];
+                    pi += vr[r][c2] * vi[r][c] - vi[r][c2] * vr[r][c];
+                }
+#pragma unroll
+                for (int r = 0; r < B; r++) {
+                    vr[r][c] -= pr * vr[r][c2] - pi * vi[r][c2];
+                    vi[r][c] -= pr * vi[r][c2] + pi * vr[r][c2];
                 }
             }
+            if (c < b) {
+                double nn = 0.0;
+#pragma unroll
+                for (int r = 0; r < B; r++) nn += vr[r][c] * vr[r][c] + vi[r][c] * vi[r][c];
+                const double inv = rsqrt(nn);
+#pragma unroll
+                for (int r = 0; r < B; r++) { vr[r][c] *= inv; vi[r][c] *= inv; }
+            }
+        }
+        // A = V^H (H V): rows of H V overwrite the rows of H, then columns of V^H T the columns
+#pragma unroll
+        for (int r = 0; r < B; r++) {
+            double tr_[B], ti_[B];
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                double sr = 0.0, si = 0.0;
+#pragma unroll
+                for (int k2 = 0; k2 < B; k2++) {
+                    sr += ar[r][k2] * vr[k2][c] - ai[r][k2] * vi[k2][c];
+                    si += ar[r][k2] * vi[k2][c] + ai[r][k2] * vr[k2][c];
+                }
+                tr_[c] = sr; ti_[c] = si;
+            }
+#pragma unroll
+            for (int c = 0; c < B; c++) { ar[r][c] = tr_[c]; ai[r][c] = ti_[c]; }
+        }
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            double tr_[B], ti_[B];
+#pragma unroll
+            for (int r = 0; r < B; r++) {
+                double sr = 0.0, si = 0.0;
+#pragma unroll
+                for (int k2 = 0; k2 < B; k2++) {   // conj(V[k2][r]) T[k2][c]
+                    sr += vr[k2][r] * ar[k2][c] + vi[k2][r] * ai[k2][c];
+                    si += vr[k2][r] * ai[k2][c] - vi[k2][r] * ar[k2][c];
+                }
+                tr_[r] = sr; ti_[r] = si;
+            }
+#pragma unroll
+            for (int r = 0; r < B; r++) { ar[r][c] = tr_[r]; ai[r][c] = ti_[r]; }
+        }
     }
 
-    // cyclic Jacobi sweeps
+    // cyclic Jacobi sweeps (FP64), from V = identity or from the FP32 eigenvectors
     for (int sweep = 0; sweep < 40; sweep++) {
         double off = 0.0, dg = 0.0;
 #pragma unroll
@@ -141,15 +275,22 @@ __global__ void __launch_bounds__(128) bands_kernel(int b, int kp, int tr, int s
             }
 }
 
+// FP32 pre-diagonalisation before the FP64 sweeps (CQPI_BANDS_MIXED=0: FP64 throughout)
+static int bands_mixed()
+{
+    const char *f = getenv("CQPI_BANDS_MIXED");
+    return (f && !strcmp(f, "0")) ? 0 : 1;
+}
+
 template <int B>
 static void launch_bands_t(cqpi_handle *h)
 {
     const long long nk = (long long)h->kp * h->kp;
     const long long nthr = h->time_reversal ? (long long)(h->kp / 2 + 1) * h->kp : nk;
     bands_kernel<B><<<cdiv(nthr, 128), 128, 0, h->stream>>>(h->b, h->kp, h->time_reversal ? 1 : 0, h->scmax,
-                                                            h->efermi, h->nR, h->d_R,
-                                                          (const double2 *)h->d_tn, (const double2 *)h->d_ta,
-                                                          h->d_eval, h->d_evec, h->d_evec32, h->d_eval32, h->d_tw);
+                                                            h->efermi, h->npair_R, h->d_pR, h->d_pPQ,
+                                                          h->d_eval, h->d_evec, h->d_evec32, h->d_eval32, h->d_tw,
+                                                          bands_mixed());
     h->launches++;
 }
 

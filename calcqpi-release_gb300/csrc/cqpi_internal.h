@@ -129,6 +129,11 @@ struct cqpi_handle {
     int nR = 0;
     int32_t *d_R = nullptr;
     double *d_tn = nullptr, *d_ta = nullptr;
+    // {R, -R} pairs of the H(k) build: R [np][2], then P and Q [np][2][b*b] (see upload_pairs)
+    int npair_R = 0;
+    int32_t *d_pR = nullptr;
+    double2 *d_pPQ = nullptr;
+    size_t cap_pR = 0, cap_pPQ = 0;
     // parameters
     int n = 0, kp = 0, os = 0, w = 0, m = 0, spin = 0, precision = 0;
     double eta = 0.0;
