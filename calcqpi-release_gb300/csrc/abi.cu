@@ -137,6 +137,8 @@ void free_workspace(cqpi_handle *h)
     dfree(h->ws.box32);
     dfree(h->ws.T32);
     dfree(h->ws.gmax);
+    dfree(h->ws.boxT32);
+    dfree(h->ws.gmaxT);
     h->ws.ebatch = 0;
 }
 
@@ -174,7 +176,8 @@ size_t bytes_per_energy(const cqpi_handle *h)
     const size_t bb = (size_t)h->b * h->b, nk = (size_t)h->kp * h->kp;
     const size_t cs = (h->precision == CQPI_PREC_FP64) ? 16 : 8;
     const size_t g0k = (h->use_fft32 && h->gmode == CQPI_GREEN_NORMAL) ? 0 : bb * nk;
-    return cs * (g0k + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb) + 8 * (size_t)h->Q;
+    const size_t boxT = h->use_tc ? (size_t)h->NB * h->NB * bb : 0;   // T G0 box of the folded s operand
+    return cs * (g0k + bb * (size_t)h->kp * h->NB + (size_t)h->NB * h->NB * bb + boxT) + 8 * (size_t)h->Q;
 }
 
 void ensure_workspace(cqpi_handle *h, int ebatch)
@@ -192,6 +195,10 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
         dalloc(&h->ws.half32, ebatch * bb * (size_t)h->kp * h->NB);
         dalloc(&h->ws.box32, ebatch * (size_t)h->NB * h->NB * bb);
         dalloc(&h->ws.gmax, ebatch);
+        if (h->use_tc) {
+            dalloc(&h->ws.boxT32, ebatch * (size_t)h->NB * h->NB * bb);
+            dalloc(&h->ws.gmaxT, ebatch);
+        }
     }
     dalloc(&h->ws.T, ebatch * (size_t)std::max(h->nimp, 1) * bb);
     dalloc(&h->ws.T32, ebatch * (size_t)std::max(h->nimp, 1) * bb);

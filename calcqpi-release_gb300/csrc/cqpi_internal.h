@@ -71,6 +71,8 @@ struct TcParams {
     const float2 *T32;
     const double *term1;
     const unsigned *gmax;
+    const float2 *boxT;          // direct-window variant, one impurity: (T G0)(R) per energy for the s
+    const unsigned *gmaxT;       // operand (T folded out of the epilogue) and its max |Re|,|Im|; else NULL
     const uint4 *Aimg;
     float *out;
     const int *fov;              // direct-window variant: per-map field of view (sites per side) or NULL
@@ -116,6 +118,8 @@ struct Workspace {
     float2 *box32 = nullptr;
     float2 *T32 = nullptr;
     unsigned *gmax = nullptr;   // per energy: bits of max |Re|,|Im| of the FP32 box
+    float2 *boxT32 = nullptr;   // per energy: T G0(R) on the box (one impurity, tensor-core path)
+    unsigned *gmaxT = nullptr;  // per energy: bits of max |Re|,|Im| of boxT32
 };
 
 }  // namespace cqpi

@@ -751,7 +751,7 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 
 // JOS: the Josephson form (p.coff, p.tip); a template flag so that the LDOS epilogue keeps
 // its register budget.
-template <int B, bool JOS>
+template <int B, bool JOS, bool FOLD>
 __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_constant__ TcParams p)
 {
     using namespace tc;
@@ -936,13 +936,20 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             rbase = op ? wbase + 2 * (NX - 1 - xl) * rowlen + 2 * a * p.b + ri : wbase + 2 * xl * rowlen + 2 * a + ri;
             toff = op * NKC * 8 + kc * 8;
             dst = (plane * NX + xl) * 16;
-            eei = ee;
+            eei = op * EB + ee;   // operand and energy: the s operand may carry its own scale
         };
         int r0 = 0, t0 = 0, d0 = 0, q0 = 0, r1 = 0, t1 = 0, d1 = 0, q1 = 0, r2 = 0, t2 = 0, d2 = 0, q2 = 0;
         if (ptid < nitems) item_of(ptid, r0, t0, d0, q0);
         if (ptid + TCW_PROD < nitems) item_of(ptid + TCW_PROD, r1, t1, d1, q1);
         if (ptid + 2 * TCW_PROD < nitems) item_of(ptid + 2 * TCW_PROD, r2, t2, d2, q2);
-        auto scale_of = [&](int e) { return e < p.ne ? pow2_scale(p.gmax[e]) : 1.f; };
+        // split scale of (operand, energy) qq = op * EB + ee: the s operand of the folded form is
+        // T G0 with its own maximum
+        auto scale_of = [&](int e0, int qq) {
+            const bool sop = qq >= EB;
+            const int e = e0 + (sop ? qq - EB : qq);
+            if (e >= p.ne) return 1.f;
+            return pow2_scale((sop && p.gmaxT) ? p.gmaxT[e] : p.gmax[e]);
+        };
         // cp.async the raw FP32 windows of a tile (zero outside the box and past the last energy)
         // raw-window columns: thread ptid < ncol owns column ptid = (op, energy, x) of the
         // column table; copies: thread ptid issues copies ptid, ptid + 256, ... of the
@@ -957,6 +964,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         }
         const int col0 = ptid / rowlen, pc0 = ptid - col0 * rowlen;
         const int dcol = TCW_PROD / rowlen, dpc = TCW_PROD - dcol * rowlen;
+        const long long sofs = FOLD ? (long long)(((uintptr_t)p.boxT - (uintptr_t)p.box) / sizeof(float2)) : 0LL;
         // column table of a tile (threads < ncol; read after a producer barrier)
         auto column_table = [&](int e0, int j, int i0) {
             if (ptid < ncol) {
@@ -964,7 +972,10 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                 const int X = my_op == 0 ? px0 - p.w + my_xl : -px0 - (TS - 1) - p.w + my_xl;
                 const int Y0 = my_op == 0 ? py - p.w : -py - p.w;
                 const bool in = e < p.ne && X >= -p.Rb && X <= p.Rb;
-                colTab[ptid] = in ? ((long long)e * p.NB * p.NB + (long long)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb : -1LL;
+                // the s columns of the folded form read T G0: offset of boxT from box, float2 units
+                const long long base = (FOLD && my_op == 1) ? sofs : 0LL;
+                colTab[ptid] = in ? base + ((long long)e * p.NB * p.NB + (long long)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb
+                                  : -1LL;
             }
         };
         // cp.async the raw FP32 windows described by the column table into raw buffer rb
@@ -1034,9 +1045,9 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                 break;
             }
             if (e0 != se) {
-                sB0 = scale_of(e0 + q0);
-                sB1 = scale_of(e0 + q1);
-                sB2 = scale_of(e0 + q2);
+                sB0 = scale_of(e0, q0);
+                sB1 = scale_of(e0, q1);
+                sB2 = scale_of(e0, q2);
                 se = e0;
             }
             if (nraw == 4) cp_async_wait_n<3>();
@@ -1051,7 +1062,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             for (int k = ptid + 3 * TCW_PROD; k < nitems; k += TCW_PROD) {
                 int rb_, to_, ds_, q_;
                 item_of(k, rb_, to_, ds_, q_);
-                convert_item(Wb, rb, rb_, to_, ds_, scale_of(e0 + q_));
+                convert_item(Wb, rb, rb_, to_, ds_, scale_of(e0, q_));
             }
             // every copy of this iteration was issued before the first barrier above, so the
             // table can now describe the tile fetched next iteration
@@ -1072,6 +1083,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         const int nb = B <= 4 ? B : p.b;                          // bands; a constant for B <= 4
         const int ncombo = EB * (TS >> 2);                        // (energy, 4-site group) pairs per tile
         constexpr bool jos = JOS;                                 // Josephson mode
+        constexpr bool fold = FOLD;                               // T folded into the s operand
         // T, the scale and term1 of an energy block, loaded once per block
         auto load_block = [&](int e0) {
             for (int i = tid; i < EB * p.nimp * bb; i += TCW_EPI) {
@@ -1085,7 +1097,8 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             if (tid < EB) {
                 const int e = e0 + tid;
                 const float inv = e < p.ne ? p.inv_sA / pow2_scale(p.gmax[e]) : 0.f;
-                cInv2[tid] = inv * inv;
+                const float invs = (e < p.ne && p.gmaxT) ? p.inv_sA / pow2_scale(p.gmaxT[e]) : inv;
+                cInv2[tid] = inv * invs;
                 const double2 tp = (p.tip && e < p.ne) ? p.tip[e] : make_double2(0.0, 0.0);
                 cTip[2 * tid] = (float)tp.x;
                 cTip[2 * tid + 1] = (float)tp.y;
@@ -1114,9 +1127,21 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                     }
                     tmem_wait_ld();
                     float term2[4] = {0.f, 0.f, 0.f, 0.f}, term2r[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (fold) {
+                        // the s accumulators already hold (T s)_a
+#pragma unroll
+                        for (int a = 0; a < B; a++) {
+                            if (a >= nb) continue;
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                term2[u] += ur[2 * a][u] * sr[2 * a + 1][u] + ur[2 * a + 1][u] * sr[2 * a][u];
+                                if (jos) term2r[u] += ur[2 * a][u] * sr[2 * a][u] - ur[2 * a + 1][u] * sr[2 * a + 1][u];
+                            }
+                        }
+                    }
 #pragma unroll
                     for (int a = 0; a < B; a++) {
-                        if (a >= nb) continue;
+                        if (a >= nb || fold) continue;
                         float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                         for (int c = 0; c < B; c++) {
@@ -1394,6 +1419,49 @@ void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint
             }
 }
 
+// (T G0)(R)[a][o] = sum_c T[a][c] G0(R)[c][o] on the box, per energy, for one impurity: the
+// s operand of the direct-window kernel with T folded in (its epilogue then only forms
+// Im(sum_a u_a (T s)_a)).  FP32 (the operand is split from FP32 anyway); per-energy
+// max |Re|,|Im| for the operand's split scale.
+__global__ void __launch_bounds__(256) tfold_kernel(int b, long long npt, const float2 *__restrict__ box,
+                                                    const float2 *__restrict__ T, float2 *__restrict__ boxT,
+                                                    unsigned *__restrict__ gmaxT)
+{
+    const long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = blockIdx.y, bb = b * b;
+    float mx = 0.f;
+    if (pt < npt) {
+        const float2 *g = box + ((size_t)e * npt + pt) * bb;
+        const float2 *Te = T + (size_t)e * bb;
+        float2 *o = boxT + ((size_t)e * npt + pt) * bb;
+        for (int a = 0; a < b; a++)
+            for (int oc = 0; oc < b; oc++) {
+                float sr = 0.f, si = 0.f;
+                for (int c = 0; c < b; c++) {
+                    const float2 t = Te[a * b + c];
+                    const float2 v = g[c * b + oc];
+                    sr += t.x * v.x - t.y * v.y;
+                    si += t.x * v.y + t.y * v.x;
+                }
+                const float2 r = make_float2(sr, si);
+                o[a * b + oc] = r;
+                mx = fmaxf(mx, fmaxf(fabsf(r.x), fabsf(r.y)));
+            }
+    }
+    for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+    if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(gmaxT + e, __float_as_uint(mx));
+}
+
+template <int B, bool JOS, bool FOLD>
+static cudaError_t launch_tcw(const TcParams &p, int grid, size_t smem, cudaStream_t st)
+{
+    cudaError_t err = cudaFuncSetAttribute(ldos_tcw_kernel<B, JOS, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+    if (err != cudaSuccess) return err;
+    ldos_tcw_kernel<B, JOS, FOLD><<<grid, TCW_THREADS, smem, st>>>(p);
+    return cudaSuccess;
+}
+
 template <int B>
 static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fov, const long long *fov_off)
 {
@@ -1431,6 +1499,21 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
     if (fov && !win) return cudaErrorInvalidValue;   // per-map fields of view need the window kernel
     if (h->josephson && (!win || !h->jos_tip)) return cudaErrorInvalidValue;   // so does the Josephson form
     if (win) {
+        // one impurity: T folded into the s operand (CQPI_TC_FOLD=0 keeps T in the epilogue)
+        const char *ff = getenv("CQPI_TC_FOLD");
+        // (not in the Josephson mode: its maps cancel more and keep T in the FP32 epilogue)
+        if (h->nimp == 1 && !h->josephson && h->ws.boxT32 && !(ff && !strcmp(ff, "0"))) {
+            const long long npt = (long long)h->NB * h->NB;
+            err = cudaMemsetAsync(h->ws.gmaxT, 0, sizeof(unsigned) * ne, h->stream);
+            if (err != cudaSuccess) return err;
+            tfold_kernel<<<dim3(cdiv(npt, 256), ne), 256, 0, h->stream>>>(h->b, npt, h->ws.box32, h->ws.T32, h->ws.boxT32,
+                                                                         h->ws.gmaxT);
+            h->launches++;
+            err = cudaGetLastError();
+            if (err != cudaSuccess) return err;
+            p.boxT = h->ws.boxT32;
+            p.gmaxT = h->ws.gmaxT;
+        }
         p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB; p.nraw = pl.wNRAW;
         p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
         p.ntx = (h->n + p.TS - 1) / p.TS;
@@ -1441,22 +1524,20 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
         const size_t smem = pl.w_smem + 8 * (size_t)p.EB * h->nimp * h->b * h->b;
         const long long nt = (long long)((ne + p.EB - 1) / p.EB) * h->n * p.ntx;
         const int grid = (int)std::min<long long>(nt, (long long)h->num_sms);
+        const bool fold = p.boxT != nullptr;
         if (h->josephson) {
             // Bogoliubov-de Gennes models have an even band count
             if constexpr (B % 2 == 0) {
-                err = cudaFuncSetAttribute(ldos_tcw_kernel<B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
-                if (err != cudaSuccess) return err;
-                ldos_tcw_kernel<B, true><<<grid, TCW_THREADS, smem, h->stream>>>(p);
+                if (fold) err = launch_tcw<B, true, true>(p, grid, smem, h->stream);
+                else err = launch_tcw<B, true, false>(p, grid, smem, h->stream);
             } else {
                 return cudaErrorInvalidValue;
             }
         } else {
-            err = cudaFuncSetAttribute(ldos_tcw_kernel<B, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-            if (err != cudaSuccess) return err;
-            ldos_tcw_kernel<B, false><<<grid, TCW_THREADS, smem, h->stream>>>(p);
+            if (fold) err = launch_tcw<B, false, true>(p, grid, smem, h->stream);
+            else err = launch_tcw<B, false, false>(p, grid, smem, h->stream);
         }
+        if (err != cudaSuccess) return err;
         h->launches++;
         return cudaGetLastError();
     }
