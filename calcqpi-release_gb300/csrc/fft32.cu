@@ -34,6 +34,17 @@ __device__ __forceinline__ int pad32(int x) { return x + (x >> 5); }
 __device__ __forceinline__ int brev_bits(int x, int bits) { return bits == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - bits)); }
 __device__ __forceinline__ int pmod(int a, int m) { int r = a % m; return r < 0 ? r + m : r; }
 
+// Planes of the upper triangle o <= a in row-major order (reciprocity: with real hoppings
+// H(-k) = conj H(k), so G0(-k) = G0(k)^T and G0(R)[a][o] = G0(-R)[o][a]: only these planes are
+// transformed and the lower ones are filled by the point reflection of R).
+__device__ __forceinline__ void tri_plane(int b, int idx, int &o, int &a)
+{
+    o = 0;
+    while (idx >= b - o) { idx -= b - o; o++; }
+    a = o + idx;
+}
+__device__ __forceinline__ int tri_index(int b, int o, int a) { return o * b - (o * (o - 1)) / 2 + (a - o); }
+
 template <int B>
 __global__ void __launch_bounds__(256) g0_rowfft_kernel(int b, int kp, int logkp, int NB, int Rb, int pg, double eta,
                                                         const double *__restrict__ energies, int ne,
@@ -210,7 +221,8 @@ __device__ __forceinline__ void fft_reg(float2 (&x)[L])
 // whose eigenvectors are kept in registers during the G0 build.  MAXT: largest block size
 // the kernel is launched with (one thread per transform of a plane group where possible).
 template <int N1, int N2, int BM = 4, int MAXT = 256>
-__global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int Rb, int pg, int eig_smem, double eta,
+__global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int Rb, int pg, int eig_smem, int tr,
+                                                            double eta,
                                                             const double *__restrict__ energies, int ne,
                                                             const float2 *__restrict__ eval_g,
                                                             const float2 *__restrict__ evec_g,
@@ -219,6 +231,7 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
     constexpr int KP = N1 * N2;
     extern __shared__ __align__(16) float2 sm[];
     const int bb = b * b;
+    const int np = tr ? (b * (b + 1)) / 2 : bb;   // planes transformed (tr: upper triangle)
     const long long nk = (long long)KP * KP;
     const int i = blockIdx.x;
     constexpr int PLEN = KP + KP / 32 + 1;
@@ -245,13 +258,13 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
         // omega - eps in FP32 from float pairs: (om_hi - e_hi) is exact when the two are
         // within a factor of two (Sterbenz), so the difference keeps its accuracy near poles
         const float om_hi = (float)om, om_lo = (float)(om - (double)om_hi);
-        for (int pl0 = 0; pl0 < bb; pl0 += pg) {
-            const int npl = min(pg, bb - pl0);
+        for (int pl0 = 0; pl0 < np; pl0 += pg) {
+            const int npl = min(pg, np - pl0);
             __syncthreads();
             // ---- G0(k) for planes [pl0, pl0+npl), natural order j (padded)
             for (int j = threadIdx.x; j < KP; j += blockDim.x) {
                 const int pos = pad32(j);
-                if (b <= BM && npl == bb) {
+                if (b <= BM && npl == np) {
                     float2 f[BM], U[BM][BM];
 #pragma unroll
                     for (int n = 0; n < BM; n++) {
@@ -276,7 +289,7 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
                             if (n < b) x[n] = cmul(U[o][n], f[n]);
 #pragma unroll
                         for (int a = 0; a < BM; a++) {
-                            if (a >= b) continue;
+                            if (a >= b || (tr && a < o)) continue;
                             float2 s = make_float2(0.f, 0.f);
 #pragma unroll
                             for (int n = 0; n < BM; n++) {
@@ -285,12 +298,14 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
                                     s.y += x[n].y * U[a][n].x - x[n].x * U[a][n].y;
                                 }
                             }
-                            sm[(size_t)(o * b + a) * PLEN + pos] = s;
+                            sm[(size_t)(tr ? tri_index(b, o, a) : o * b + a) * PLEN + pos] = s;
                         }
                     }
                 } else {
                     for (int q = 0; q < npl; q++) {
-                        const int pl = pl0 + q, o = pl / b, a = pl - o * b;
+                        const int pl = pl0 + q;
+                        int o = pl / b, a = pl - o * b;
+                        if (tr) tri_plane(b, pl, o, a);
                         float2 s = make_float2(0.f, 0.f);
                         for (int n = 0; n < b; n++) {
                             const float2 ev = eval[(size_t)n * estride + j];
@@ -327,7 +342,7 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
 #pragma unroll
                 for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
                 fft_reg<N1>(x);
-                float2 *dst = half + (((size_t)e * bb + pl0 + q) * KP + i) * NB;
+                float2 *dst = half + (((size_t)e * np + pl0 + q) * KP + i) * NB;
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) {
                     // output Y in [0, kp) is R = Y mod kp; with NB <= kp exactly one box slot or none
@@ -393,7 +408,7 @@ __global__ void __launch_bounds__(256) rowfft_reg_g0k_kernel(int NB, int Rb, lon
 // same two register passes as the row transform, scales by kp^-2 and writes the box rows
 // xb = (X + Rb) mod kp < NB, tracking max|G0| of the energy for the split scale.
 template <int N1, int N2>
-__global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int bb, float scale,
+__global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int b, int np, int tr, float scale,
                                                          const float2 *__restrict__ half, const float2 *__restrict__ tw,
                                                          float2 *__restrict__ box, unsigned *__restrict__ gmax)
 {
@@ -403,8 +418,11 @@ __global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int bb,
     extern __shared__ __align__(16) float2 sm[];
     float2 *tws = sm + (size_t)NC * PLEN;
     const int yb0 = blockIdx.x * NC, pl = blockIdx.y, e = blockIdx.z;
+    const int bb = b * b;
+    int po = pl / b, pa = pl - po * b;          // the plane's orbitals (o, a)
+    if (tr) tri_plane(b, pl, po, pa);
     for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
-    const float2 *src = half + ((size_t)e * bb + pl) * (size_t)KP * NB;
+    const float2 *src = half + ((size_t)e * np + pl) * (size_t)KP * NB;
     for (int idx = threadIdx.x; idx < KP * NC; idx += blockDim.x) {
         const int i = idx / NC, c = idx - i * NC, yb = yb0 + c;
         sm[(size_t)c * PLEN + pad32(i)] = yb < NB ? src[(size_t)i * NB + yb] : make_float2(0.f, 0.f);
@@ -436,7 +454,9 @@ __global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int bb,
                 const int xb = (k2 + N2 * k1 + Rb) & (KP - 1);
                 if (xb < NB) {
                     const float2 v = cscale(x[k1], scale);
-                    dst[((size_t)xb * NB + yb) * bb + pl] = v;
+                    dst[((size_t)xb * NB + yb) * bb + po * b + pa] = v;
+                    // reciprocity: G0(-R)[a][o] = G0(R)[o][a]
+                    if (tr && po != pa) dst[((size_t)(2 * Rb - xb) * NB + (2 * Rb - yb)) * bb + pa * b + po] = v;
                     mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
                 }
             }
@@ -518,7 +538,7 @@ static bool rowfft_reg_ok(const cqpi_handle *h);
 static cudaError_t configure_rowfft_reg(cqpi_handle *h);
 static cudaError_t configure_rowfft_g0k(cqpi_handle *h);
 static cudaError_t configure_colfft_reg(cqpi_handle *h);
-static void launch_colfft_reg(cqpi_handle *h, int ne);
+static void launch_colfft_reg(cqpi_handle *h, int ne, int tr);
 
 bool fft32_supported(const cqpi_handle *h) { return h->kp >= 2 && (h->kp & (h->kp - 1)) == 0 && h->kp <= 8192; }
 
@@ -555,11 +575,25 @@ static void launch_rowfft(cqpi_handle *h, int ne, const double *d_energies, int 
 // register four-step variant: kp = N1 x N2 in {64 ... 4096} and a box no wider than kp
 static bool rowfft_reg_ok(const cqpi_handle *h) { return h->kp >= 64 && h->kp <= 4096 && h->NB <= h->kp; }
 
-static int rowfft_reg_plane_group(const cqpi_handle *h)
+// planes the fused row transform carries: the upper triangle under reciprocity (real hoppings,
+// CQPI_RECIPROCITY=0 disables), else all b^2
+// (both transforms must be the register kernels: the radix-2 ones carry every plane)
+static int rowfft_planes(const cqpi_handle *h)
+{
+    const char *f = getenv("CQPI_RECIPROCITY");
+    const char *fr = getenv("CQPI_ROWFFT");
+    const char *fc = getenv("CQPI_COLFFT");
+    const bool tr = h->time_reversal && !(f && !strcmp(f, "0")) && !(fr && !strcmp(fr, "radix2")) &&
+                    !(fc && !strcmp(fc, "radix2"));
+    return tr ? h->b * (h->b + 1) / 2 : h->b * h->b;
+}
+
+// all = true: the largest group any hopping set can need (for the shared-memory limit)
+static int rowfft_reg_plane_group(const cqpi_handle *h, bool all = false)
 {
     const size_t plen = (size_t)h->kp + (h->kp >> 5) + 1;
     int pg = (int)((96 * 1024 - 8 * (size_t)h->kp) / (8 * plen));
-    return std::max(1, std::min(pg, h->b * h->b));
+    return std::max(1, std::min(pg, all ? h->b * h->b : rowfft_planes(h)));
 }
 
 // bytes of one k_x row of the eigen cache (FP64 eigenvalues, FP32 eigenvectors)
@@ -567,9 +601,9 @@ static size_t rowfft_eig_bytes(const cqpi_handle *h) { return (size_t)h->kp * (8
 
 // shared memory of the register row transform: pg planes, the twiddles and, when it fits
 // in 227 KiB, the row's eigen cache
-static size_t rowfft_reg_smem(const cqpi_handle *h, bool *eig_smem)
+static size_t rowfft_reg_smem(const cqpi_handle *h, bool *eig_smem, bool all = false)
 {
-    const int pg = rowfft_reg_plane_group(h);
+    const int pg = rowfft_reg_plane_group(h, all);
     const size_t base = 8 * ((size_t)pg * (h->kp + h->kp / 32 + 1) + h->kp);
     const bool fits = base + rowfft_eig_bytes(h) <= 227 * 1024;
     if (eig_smem) *eig_smem = fits;
@@ -592,18 +626,27 @@ static void launch_rowfft_reg_t(cqpi_handle *h, int ne, const double *d_energies
     const int pg = rowfft_reg_plane_group(h);
     bool eig = false;
     size_t smem = rowfft_reg_smem(h, &eig);
+    // a small block (up to 6 warps: the 6 reciprocity planes of 3 bands) runs faster as two
+    // blocks per SM reading the row's eigen data through L2 than as one block with it in
+    // shared memory (measured: C2 G0 + transforms 7.1 -> 6.0 ms per job)
+    const int threads = rowfft_reg_threads<N1, N2, MAXT>(h);
+    const size_t base = eig ? smem - rowfft_eig_bytes(h) : smem;
+    const bool two = threads <= 192 && 2 * base <= 227 * 1024;
     const char *f = getenv("CQPI_ROWFFT_EIG");
-    if (f && !strcmp(f, "global") && eig) {
+    if (eig && (two || (f && !strcmp(f, "global"))) && !(f && !strcmp(f, "smem"))) {
         eig = false;
-        smem -= rowfft_eig_bytes(h);
+        smem = base;
     }
-    g0_rowfft_reg_kernel<N1, N2, 4, MAXT><<<h->kp, rowfft_reg_threads<N1, N2, MAXT>(h), smem, h->stream>>>(
-        h->b, h->NB, h->Rb, pg, eig ? 1 : 0, h->eta, d_energies, ne, h->d_eval32, h->d_evec32, h->d_tw32, h->ws.half32);
+    const int tr = rowfft_planes(h) != h->b * h->b ? 1 : 0;
+    g0_rowfft_reg_kernel<N1, N2, 4, MAXT><<<h->kp, threads, smem, h->stream>>>(
+        h->b, h->NB, h->Rb, pg, eig ? 1 : 0, tr, h->eta, d_energies, ne, h->d_eval32, h->d_evec32, h->d_tw32,
+        h->ws.half32);
 }
 
 static cudaError_t configure_rowfft_reg(cqpi_handle *h)
 {
-    const int smem = (int)rowfft_reg_smem(h, nullptr);
+    // the largest launch: every plane, or the reciprocity planes with the eigen cache
+    const int smem = (int)std::max(rowfft_reg_smem(h, nullptr, true), rowfft_reg_smem(h, nullptr, false));
     switch (h->kp) {
     case 64: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 128: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -630,12 +673,13 @@ static cudaError_t configure_colfft_reg_t()
 }
 
 template <int N1, int N2>
-static void launch_colfft_reg_t(cqpi_handle *h, int ne)
+static void launch_colfft_reg_t(cqpi_handle *h, int ne, int tr)
 {
     constexpr int NC = 256 / N1;
-    dim3 grid(cdiv(h->NB, NC), h->b * h->b, ne);
+    const int np = tr ? h->b * (h->b + 1) / 2 : h->b * h->b;
+    dim3 grid(cdiv(h->NB, NC), np, ne);
     colfft_reg_kernel<N1, N2><<<grid, 256, colfft_reg_smem<N1, N2>(), h->stream>>>(
-        h->NB, h->Rb, h->b * h->b, (float)(1.0 / ((double)h->kp * h->kp)), h->ws.half32, h->d_tw32, h->ws.box32,
+        h->NB, h->Rb, h->b, np, tr, (float)(1.0 / ((double)h->kp * h->kp)), h->ws.half32, h->d_tw32, h->ws.box32,
         h->ws.gmax);
 }
 
@@ -690,16 +734,16 @@ static void launch_rowfft_g0k_t(cqpi_handle *h, int ne)
         h->NB, h->Rb, nrows, h->ws.g0k32, h->d_tw32, h->ws.half32);
 }
 
-static void launch_colfft_reg(cqpi_handle *h, int ne)
+static void launch_colfft_reg(cqpi_handle *h, int ne, int tr)
 {
     switch (h->kp) {
-    case 64: launch_colfft_reg_t<8, 8>(h, ne); break;
-    case 128: launch_colfft_reg_t<8, 16>(h, ne); break;
-    case 256: launch_colfft_reg_t<16, 16>(h, ne); break;
-    case 512: launch_colfft_reg_t<16, 32>(h, ne); break;
-    case 1024: launch_colfft_reg_t<32, 32>(h, ne); break;
-    case 2048: launch_colfft_reg_t<32, 64>(h, ne); break;
-    case 4096: launch_colfft_reg_t<64, 64>(h, ne); break;
+    case 64: launch_colfft_reg_t<8, 8>(h, ne, tr); break;
+    case 128: launch_colfft_reg_t<8, 16>(h, ne, tr); break;
+    case 256: launch_colfft_reg_t<16, 16>(h, ne, tr); break;
+    case 512: launch_colfft_reg_t<16, 32>(h, ne, tr); break;
+    case 1024: launch_colfft_reg_t<32, 32>(h, ne, tr); break;
+    case 2048: launch_colfft_reg_t<32, 64>(h, ne, tr); break;
+    case 4096: launch_colfft_reg_t<64, 64>(h, ne, tr); break;
     }
 }
 
@@ -735,7 +779,7 @@ void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies)
     h->launches++;
     const char *fc = getenv("CQPI_COLFFT");
     if (rowfft_reg_ok(h) && !(fc && !strcmp(fc, "radix2"))) {
-        launch_colfft_reg(h, ne);
+        launch_colfft_reg(h, ne, rowfft_planes(h) != b * b ? 1 : 0);
     } else {
         const int lnc = colfft_lnc(h->kp), NC = 1 << lnc;
         const size_t s2 = 8 * ((size_t)h->kp * NC + h->kp / 2);
@@ -764,7 +808,7 @@ bool launch_fft32_planes(cqpi_handle *h, int ne)
     case 4096: launch_rowfft_g0k_t<64, 64>(h, ne); break;
     }
     h->launches++;
-    launch_colfft_reg(h, ne);
+    launch_colfft_reg(h, ne, 0);
     h->launches++;
     return true;
 }
