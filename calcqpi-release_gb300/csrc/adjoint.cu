@@ -28,7 +28,9 @@
 //   6. adj_hop_kernel: tbar for every unique R, normal and conjugated terms:
 //      sum_k e^{-/+ i th(k)} Hbar(k)[p][q] (FP64 sums over the k-grid).
 // The contraction adjoint computes in the handle's precision (FP32 with the mixed box,
-// FP64 with the FP64 box) and accumulates in FP64; steps 2-6 are FP64.
+// FP64 with the FP64 box) and accumulates in FP64; steps 4-5 follow the handle's precision
+// too (FP32 transform and per-k rotation for the mixed handle, the energy sum of C(k) in
+// FP64); steps 2, 3 and 6 are FP64.
 #include "cplx.h"
 #include "cqpi_internal.h"
 
@@ -299,19 +301,21 @@ __global__ void adj_tv_kernel(int b, int NB, int Rb, int nimp, int ne, const C *
 // ------------------------------------------------------------------ 4. box -> k-grid
 // In-place radix-2 transform of x[0..kp) (natural order in and out) with e^{-2 pi i t/kp}
 // twiddles from tw (e^{+2 pi i t/kp}).
-__device__ void fft_minus(double2 *x, int kp, int logkp, const double2 *__restrict__ tw)
+template <class C>
+__device__ void fft_minus(C *x, int kp, int logkp, const C *__restrict__ tw)
 {
     for (int t = threadIdx.x; t < kp; t += blockDim.x) {
         const int r = logkp ? (int)(__brev((unsigned)t) >> (32 - logkp)) : 0;
-        if (r > t) { const double2 a = x[t]; x[t] = x[r]; x[r] = a; }
+        if (r > t) { const C a = x[t]; x[t] = x[r]; x[r] = a; }
     }
     __syncthreads();
     for (int len = 2; len <= kp; len <<= 1) {
         const int hl = len >> 1, step = kp / len;
         for (int t = threadIdx.x; t < (kp >> 1); t += blockDim.x) {
             const int kk = t % hl, idx = (t / hl) * len + kk;
-            const double2 wv = cconj(__ldg(tw + kk * step));
-            const double2 u = x[idx], v = cmul(x[idx + hl], wv);
+            C wv = __ldg(tw + kk * step);
+            wv.y = -wv.y;
+            const C u = x[idx], v = cmul(x[idx + hl], wv);
             x[idx] = cadd(u, v);
             x[idx + hl] = csub(u, v);
         }
@@ -320,61 +324,69 @@ __device__ void fft_minus(double2 *x, int kp, int logkp, const double2 *__restri
 }
 
 // A[pl][yb][kx] = sum_{X in box} e^{-2 pi i kx X/kp} Gbar(X, Y=yb-Rb)[pl]; grid (NB, bb)
+// C: double2 (FP64 handle) or float2 (mixed handle: the k-space steps in FP32, the energy
+// sum of C(k) in FP64)
+template <class C>
 __global__ void __launch_bounds__(256) adj_cols_kernel(int kp, int logkp, int NB, int Rb, int bb, const double2 *__restrict__ gbox,
-                                                       const double2 *__restrict__ tw, double2 *__restrict__ A)
+                                                       const C *__restrict__ tw, C *__restrict__ A)
 {
-    extern __shared__ double2 xs[];
+    extern __shared__ __align__(16) unsigned char adj_xs_raw[];
+    C *xs = reinterpret_cast<C *>(adj_xs_raw);
     const int yb = blockIdx.x, pl = blockIdx.y;
     for (int pos = threadIdx.x; pos < kp; pos += blockDim.x) {
         double2 s = make_double2(0.0, 0.0);
         // box columns X = xb - Rb with X == pos (mod kp)
         int xb = ((pos + Rb) % kp);
         for (; xb < NB; xb += kp) s = cadd(s, gbox[((size_t)xb * NB + yb) * bb + pl]);
-        xs[pos] = s;
+        xs[pos] = cmake<C>(s.x, s.y);
     }
     __syncthreads();
-    fft_minus(xs, kp, logkp, tw);
-    double2 *dst = A + ((size_t)pl * NB + yb) * kp;
+    fft_minus<C>(xs, kp, logkp, tw);
+    C *dst = A + ((size_t)pl * NB + yb) * kp;
     for (int t = threadIdx.x; t < kp; t += blockDim.x) dst[t] = xs[t];
 }
 
 // Gbar(kx, ky)[pl] = kp^-2 sum_{Y in box} e^{-2 pi i ky Y/kp} A[pl][Y+Rb][kx]; grid (kp, bb)
+template <class C>
 __global__ void __launch_bounds__(256) adj_rows_kernel(int kp, int logkp, int NB, int Rb, int bb, double scale,
-                                                       const double2 *__restrict__ A, const double2 *__restrict__ tw,
-                                                       double2 *__restrict__ gk)
+                                                       const C *__restrict__ A, const C *__restrict__ tw,
+                                                       C *__restrict__ gk)
 {
-    extern __shared__ double2 xs[];
+    extern __shared__ __align__(16) unsigned char adj_xs_raw[];
+    C *xs = reinterpret_cast<C *>(adj_xs_raw);
     const int kx = blockIdx.x, pl = blockIdx.y;
-    const double2 *src = A + (size_t)pl * NB * kp + kx;
+    const C *src = A + (size_t)pl * NB * kp + kx;
     for (int pos = threadIdx.x; pos < kp; pos += blockDim.x) {
-        double2 s = make_double2(0.0, 0.0);
+        C s = cmake<C>(0.0, 0.0);
         int yb = ((pos + Rb) % kp);
         for (; yb < NB; yb += kp) s = cadd(s, src[(size_t)yb * kp]);
         xs[pos] = s;
     }
     __syncthreads();
-    fft_minus(xs, kp, logkp, tw);
+    fft_minus<C>(xs, kp, logkp, tw);
     const size_t nk = (size_t)kp * kp;
-    double2 *dst = gk + (size_t)pl * nk + (size_t)kx * kp;
-    for (int t = threadIdx.x; t < kp; t += blockDim.x) dst[t] = cscale(xs[t], scale);
+    C *dst = gk + (size_t)pl * nk + (size_t)kx * kp;
+    for (int t = threadIdx.x; t < kp; t += blockDim.x) dst[t] = cscale(xs[t], (typename real_of<C>::type)scale);
 }
 
 // ------------------------------------------------------------------ 5. per-k resolvent
 // C(k) += F* (U^H Gbar(k) U) F*, F = diag(1/(omega + i eta - eps_n)); one thread per k
-template <int B>
+// C: the working precision (double2, or float2 for the mixed handle: eigenvectors and Gbar(k)
+// in FP32, the pole factors from the FP64 eigenvalues, C(k) accumulated in FP64)
+template <int B, class C>
 __global__ void __launch_bounds__(128) adj_kacc_kernel(int b, long long nk, double omega, double eta,
-                                                       const double *__restrict__ eval, const double2 *__restrict__ evec,
-                                                       const double2 *__restrict__ gk, double2 *__restrict__ Cacc)
+                                                       const double *__restrict__ eval, const C *__restrict__ evec,
+                                                       const C *__restrict__ gk, double2 *__restrict__ Cacc)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nk) return;
-    double2 U[B][B], G[B][B], X[B][B], f[B];
+    C U[B][B], G[B][B], X[B][B], f[B];
 #pragma unroll
     for (int n = 0; n < B; n++) {
         if (n < b) {
             const double dr = omega - eval[(size_t)n * nk + k];
             const double den = dr * dr + eta * eta;
-            f[n] = make_double2(dr / den, eta / den);   // conj(1/(dr + i eta))
+            f[n] = cmake<C>(dr / den, eta / den);   // conj(1/(dr + i eta))
         }
     }
 #pragma unroll
@@ -391,7 +403,7 @@ __global__ void __launch_bounds__(128) adj_kacc_kernel(int b, long long nk, doub
 #pragma unroll
         for (int m = 0; m < B; m++) {
             if (o >= b || m >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
+            C s = cmake<C>(0.0, 0.0);
 #pragma unroll
             for (int a = 0; a < B; a++)
                 if (a < b) s = cadd(s, cmul(G[o][a], U[a][m]));
@@ -403,13 +415,17 @@ __global__ void __launch_bounds__(128) adj_kacc_kernel(int b, long long nk, doub
 #pragma unroll
         for (int m = 0; m < B; m++) {
             if (n >= b || m >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
+            C s = cmake<C>(0.0, 0.0);
 #pragma unroll
             for (int o = 0; o < B; o++)
-                if (o < b) s = cadd(s, cmul(cconj(U[o][n]), X[o][m]));
+                if (o < b) {
+                    C un = U[o][n];
+                    un.y = -un.y;
+                    s = cadd(s, cmul(un, X[o][m]));
+                }
             s = cmul(cmul(f[n], s), f[m]);
             double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
-            *c = cadd(*c, s);
+            *c = cadd(*c, to_d2(s));
         }
 }
 
@@ -548,18 +564,34 @@ template <int B>
 static void launch_kacc_t(cqpi_handle *h, double omega, AdjWorkspace &aw)
 {
     const long long nk = (long long)h->kp * h->kp;
-    adj_kacc_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec, aw.gk, aw.C);
+    if (h->precision == CQPI_PREC_FP64)
+        adj_kacc_kernel<B, double2><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec,
+                                                                         aw.gk, aw.C);
+    else
+        adj_kacc_kernel<B, float2><<<cdiv(nk, 128), 128, 0, h->stream>>>(
+            h->b, nk, omega, h->eta, h->d_eval, h->d_evec32, reinterpret_cast<const float2 *>(aw.gk), aw.C);
     h->launches++;
 }
 
 void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw)
 {
     const int kp = h->kp, logkp = ilog2_exact(kp), bb = h->b * h->b;
-    const size_t smem = sizeof(double2) * kp;
     const double2 *gbe = aw.gbox + (size_t)e * h->NB * h->NB * bb;
-    adj_cols_kernel<<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw, aw.A);
-    adj_rows_kernel<<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, 1.0 / ((double)kp * kp), aw.A,
-                                                           h->d_tw, aw.gk);
+    if (h->precision == CQPI_PREC_FP64) {
+        const size_t smem = sizeof(double2) * kp;
+        adj_cols_kernel<double2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw,
+                                                                            aw.A);
+        adj_rows_kernel<double2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
+                                                                         1.0 / ((double)kp * kp), aw.A, h->d_tw, aw.gk);
+    } else {
+        // the mixed handle: the transform and the per-k rotation in FP32, in the same buffers
+        const size_t smem = sizeof(float2) * kp;
+        float2 *A32 = reinterpret_cast<float2 *>(aw.A), *gk32 = reinterpret_cast<float2 *>(aw.gk);
+        adj_cols_kernel<float2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw32,
+                                                                           A32);
+        adj_rows_kernel<float2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
+                                                                        1.0 / ((double)kp * kp), A32, h->d_tw32, gk32);
+    }
     h->launches += 2;
     const int b = h->b;
     if (b <= 1) launch_kacc_t<1>(h, omega, aw);
