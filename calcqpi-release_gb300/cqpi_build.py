@@ -1,4 +1,5 @@
-"""Build libcqpi.so (CUDA, sm_103a) and the calcqpi CLI in-tree, under _build/.
+"""Build libcqpi.so (CUDA, sm_103a) and the host tools (calcqpi, mkwavefunctions) in-tree,
+under _build/.
 
 Every translation unit is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo``; objects are reused
@@ -20,6 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 OBJ = os.path.join(BUILD, "obj")
 LIB = os.path.join(BUILD, "libcqpi.so")
 CLI = os.path.join(BUILD, "calcqpi")
+MKWF = os.path.join(BUILD, "mkwavefunctions")
 INCLUDE = os.path.join(ROOT, "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -78,22 +80,32 @@ def build_lib(verbose=False, extra_flags=()) -> str:
 
 
 def build_cli(verbose=False) -> str:
+    """One executable per host/<tool>_main.cc (calcqpi, mkwavefunctions), linked against
+    libcqpi.so; the other host/*.cc files are shared by all tools."""
     srcs = sorted(glob.glob(os.path.join(HOST, "*.cc")))
-    if not srcs:
+    mains = [s for s in srcs if s.endswith("_main.cc")]
+    if not mains:
         return ""
+    shared = [s for s in srcs if s not in mains]
     headers = glob.glob(os.path.join(HOST, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h"))
-    if _newer(CLI, srcs + headers + [LIB]):
-        return CLI
-    tmp = CLI + ".tmp%d" % os.getpid()
-    _run_parallel([[CXX] + CXXFLAGS + srcs + ["-o", tmp, "-L" + BUILD, "-lcqpi", "-Wl,-rpath,$ORIGIN"]], verbose)
-    os.replace(tmp, CLI)
+    cmds, moves = [], []
+    for m in mains:
+        exe = os.path.join(BUILD, os.path.basename(m)[: -len("_main.cc")])
+        if _newer(exe, [m] + shared + headers + [LIB]):
+            continue
+        tmp = exe + ".tmp%d" % os.getpid()
+        cmds.append([CXX] + CXXFLAGS + [m] + shared + ["-o", tmp, "-L" + BUILD, "-lcqpi", "-Wl,-rpath,$ORIGIN"])
+        moves.append((tmp, exe))
+    _run_parallel(cmds, verbose)
+    for tmp, exe in moves:
+        os.replace(tmp, exe)
     return CLI
 
 
 def build(verbose=False) -> dict:
     lib = build_lib(verbose)
     cli = build_cli(verbose)
-    return {"lib": lib, "cli": cli}
+    return {"lib": lib, "cli": cli, "mkwavefunctions": MKWF if cli else ""}
 
 
 if __name__ == "__main__":

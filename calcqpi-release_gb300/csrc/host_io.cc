@@ -2,8 +2,11 @@
 //   cqpi_read_hr        Wannier90 _hr.dat reader   (tightbind::readfile, src/tightbinding.cc:70-149)
 //   cqpi_orbital_cache  analytic orbital cache    (wannierfunctions::precalculate + getwave,
 //                                                  src/wannierfunctions.cc:21-221,433-442)
+//   cqpi_orbital_cache_basis  the same with lattice basis vectors (mkwavefunctions)
 //   cqpi_xsf_orbital_cache  XSF orbital cache   (xcfloader + wannierfunctions(file, ...),
 //                                                  src/loadxcf.cc:37-345, src/wannierfunctions.cc:444-463)
+//   cqpi_xsf_orbital_cache_shifted / _mod  the XSF forms of mkwavefunctions (orbitalfiles with
+//                       shift, modorbitalfiles; src/wannierfunctions.cc:465-520)
 //   cqpi_idl_write / cqpi_idl_read_header / cqpi_idl_read
 //                       IDL map container          (idl::write / idl::read, src/idl.cc:50-97)
 // These run on the CPU only; none of them touches the GPU.
@@ -156,13 +159,20 @@ static int orbital_type(const char *name)
 int cqpi_orbital_known(const char *name) { return name && orbital_type(name) >= 0; }
 
 // Value of orbital 'type' at (x, y): z = 0 shifted by -height (tip plane below the
-// orbital centre, src/wannierfunctions.cc:127-130), optional rotation for non-s types.
+// orbital centre, src/wannierfunctions.cc:127-130), the in-plane point taken through the
+// basis vectors when given (wannierfunctions::transform, src/wannierfunctions.h:41-45:
+// (x, y) -> x b0 + y b1, basis = {b0x, b0y, b1x, b1y}), optional rotation for non-s types.
 static double orbital_value(int type, double x, double y, double width, double height, double xpos, double ypos,
-                            double theta, double phi, double prefact, double symmetry)
+                            double theta, double phi, double prefact, double symmetry, const double *basis)
 {
     double z = 0.0;
     x -= xpos; y -= ypos; z -= height;
     if (type == 17) return 0.0;
+    if (basis) {
+        const double a = x, b = y;
+        x = basis[0] * a + basis[2] * b;
+        y = basis[1] * a + basis[3] * b;
+    }
     if (type != 0 && (theta != 0.0 || phi != 0.0)) {
         const double xc = x, yc = y, zc = z;
         x = xc * cos(theta) + yc * sin(theta) * cos(phi) + zc * sin(theta) * sin(phi);
@@ -200,6 +210,14 @@ static double orbital_value(int type, double x, double y, double width, double h
 int cqpi_orbital_cache(const char *name, double width, double height, double xpos, double ypos, double theta,
                        double phi, double prefact, int32_t window, int32_t oversamp, double *out)
 {
+    return cqpi_orbital_cache_basis(name, width, height, xpos, ypos, theta, phi, prefact, nullptr, window, oversamp,
+                                    out);
+}
+
+int cqpi_orbital_cache_basis(const char *name, double width, double height, double xpos, double ypos, double theta,
+                             double phi, double prefact, const double *basis, int32_t window, int32_t oversamp,
+                             double *out)
+{
     const int type = name ? orbital_type(name) : -1;
     if (type < 0) return host_fail(CQPI_ERR_ARG, std::string("unknown orbital type ") + (name ? name : "(null)"));
     if (!out || window < 0 || oversamp < 1) return host_fail(CQPI_ERR_ARG, "invalid orbital cache arguments");
@@ -208,7 +226,7 @@ int cqpi_orbital_cache(const char *name, double width, double height, double xpo
         for (int j = 0; j < n; j++)
             out[(size_t)i * n + j] = orbital_value(type, (double)i / oversamp - (double)window - 0.5,
                                                    (double)j / oversamp - (double)window - 0.5, width, height, xpos,
-                                                   ypos, theta, phi, prefact, 4.0);
+                                                   ypos, theta, phi, prefact, 4.0, basis);
     return CQPI_OK;
 }
 
@@ -389,14 +407,13 @@ static bool xsf_read(const char *path, XsfGrid &g, std::string &err)
     return !g.error && g.has_grid && g.has_convvec;
 }
 
-// xcfloader::operator() after getvalue (src/loadxcf.cc:187-202,326-328): lattice units ->
-// Cartesian with CONVVEC, fractional grid coordinates by solving [a0 a1 a2] f = r - origin
-// (Gaussian elimination with partial pivoting), nearest grid point round(f * n), zero
-// outside the grid.  A NaN height (getzheight(0)) gives zero.
-static double xsf_value(const XsfGrid &g, double xu, double yu, double z)
+// xcfloader::operator() (src/loadxcf.cc:221-238) at the Cartesian point (x, y, z): fractional
+// grid coordinates by solving [a0 a1 a2] f = r - origin - shift (Gaussian elimination with
+// partial pivoting), nearest grid point round(f * n), zero outside the grid.  A NaN height
+// (getzheight(0)) gives zero.
+static double xsf_cart_value(const XsfGrid &g, double x, double y, double z, const double *shift)
 {
-    const double r[3] = {xu * g.convvec[0][0] + yu * g.convvec[1][0] - g.origin[0],
-                         xu * g.convvec[0][1] + yu * g.convvec[1][1] - g.origin[1], z - g.origin[2]};
+    const double r[3] = {x - g.origin[0] - shift[0], y - g.origin[1] - shift[1], z - g.origin[2] - shift[2]};
     double A[3][4];
     for (int row = 0; row < 3; row++) {
         for (int c = 0; c < 3; c++) A[row][c] = g.axis[c][row];
@@ -431,14 +448,16 @@ static double xsf_value(const XsfGrid &g, double xu, double yu, double z)
     return g.cube[((size_t)idx[0] * g.ys + (size_t)idx[1]) * g.zs + (size_t)idx[2]];
 }
 
-int cqpi_xsf_orbital_cache(const char *path, double height, int32_t window, int32_t oversamp, double prefact,
-                           double *out)
+// xcfloader::getvalue (src/loadxcf.cc:330-332): lattice units -> Cartesian with CONVVEC
+static double xsf_value(const XsfGrid &g, double xu, double yu, double z, const double *shift)
 {
-    if (!path || !out || window < 0 || oversamp < 1) return host_fail(CQPI_ERR_ARG, "invalid XSF orbital arguments");
-    XsfGrid g;
-    std::string err;
-    if (!xsf_read(path, g, err)) return host_fail(CQPI_ERR_ARG, err);
-    // xcfloader::getzheight (src/loadxcf.cc:330-345): above the highest / below the lowest atom
+    return xsf_cart_value(g, xu * g.convvec[0][0] + yu * g.convvec[1][0], xu * g.convvec[0][1] + yu * g.convvec[1][1],
+                          z, shift);
+}
+
+// xcfloader::getzheight (src/loadxcf.cc:334-348): above the highest / below the lowest atom
+static double xsf_zheight(const XsfGrid &g, double height)
+{
     double z = NAN;
     if (height > 0.0 && !g.atom_z.empty()) {
         z = g.atom_z[0];
@@ -449,11 +468,57 @@ int cqpi_xsf_orbital_cache(const char *path, double height, int32_t window, int3
         for (double v : g.atom_z) z = std::min(z, v);
         z += height;
     }
+    return z;
+}
+
+int cqpi_xsf_orbital_cache(const char *path, double height, int32_t window, int32_t oversamp, double prefact,
+                           double *out)
+{
+    const double zero[3] = {0.0, 0.0, 0.0};
+    return cqpi_xsf_orbital_cache_shifted(path, zero, 0, height, window, oversamp, prefact, out);
+}
+
+int cqpi_xsf_orbital_cache_shifted(const char *path, const double *shift, int32_t centre, double height,
+                                   int32_t window, int32_t oversamp, double prefact, double *out)
+{
+    if (!path || !out || !shift || window < 0 || oversamp < 1)
+        return host_fail(CQPI_ERR_ARG, "invalid XSF orbital arguments");
+    XsfGrid g;
+    std::string err;
+    if (!xsf_read(path, g, err)) return host_fail(CQPI_ERR_ARG, err);
+    const double z = xsf_zheight(g, height), ofs = centre ? 0.5 : 0.0;
     const int n = (2 * window + 1) * oversamp;
     for (int i = 0; i < n; i++)
         for (int j = 0; j < n; j++)
-            out[(size_t)i * n + j] =
-                prefact * xsf_value(g, (double)i / oversamp - (double)window, (double)j / oversamp - (double)window, z);
+            out[(size_t)i * n + j] = prefact * xsf_value(g, (double)i / oversamp - (double)window - ofs,
+                                                         (double)j / oversamp - (double)window - ofs, z, shift);
+    return CQPI_OK;
+}
+
+int cqpi_xsf_orbital_cache_mod(const char *path, const double *modshift, const double *basis, double height,
+                               double xpos, double ypos, double theta, double prefact, int32_t window,
+                               int32_t oversamp, double *out)
+{
+    if (!path || !out || !modshift || window < 0 || oversamp < 1)
+        return host_fail(CQPI_ERR_ARG, "invalid XSF orbital arguments");
+    XsfGrid g;
+    std::string err;
+    if (!xsf_read(path, g, err)) return host_fail(CQPI_ERR_ARG, err);
+    const double z = xsf_zheight(g, height), cs = cos(theta), sn = sin(theta);
+    const int n = (2 * window + 1) * oversamp;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            // wannierfunctions(ucv, xcfloader, ...) (src/wannierfunctions.cc:500-520): shift,
+            // basis, then xcfloader::getcartmodvalue (src/loadxcf.cc:268-290): rotation by theta
+            double x = (double)i / oversamp - (double)window - xpos, y = (double)j / oversamp - (double)window - ypos;
+            if (basis) {
+                const double a = x, b = y;
+                x = basis[0] * a + basis[2] * b;
+                y = basis[1] * a + basis[3] * b;
+            }
+            const double xr = x * cs - y * sn, yr = x * sn + y * cs;
+            out[(size_t)i * n + j] = prefact * xsf_cart_value(g, xr, yr, z, modshift);
+        }
     return CQPI_OK;
 }
 

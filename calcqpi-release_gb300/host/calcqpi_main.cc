@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "config.h"
+#include "log.h"
 #include "cqpi.h"
 #include "cqpi_host.h"
 
@@ -36,45 +37,7 @@ using cplx = std::complex<double>;
 
 namespace {
 
-// Line-buffered log sink that prefixes every line with "YYYY-MM-DD.HH:MM:SS ".
-class Log {
-    std::ostream *os_;
-    std::ofstream file_;
-    bool bol_ = true;
-
-public:
-    Log() : os_(&std::cout) {}
-    bool open_append(const std::string &path)
-    {
-        file_.open(path.c_str(), std::ios::out | std::ios::app);
-        if (file_.is_open()) os_ = &file_;
-        return file_.is_open();
-    }
-    Log &operator<<(const std::string &s)
-    {
-        for (char c : s) {
-            if (bol_) {
-                char buf[64];
-                time_t now = time(nullptr);
-                struct tm t;
-                localtime_r(&now, &t);
-                strftime(buf, sizeof buf, "%Y-%m-%d.%X ", &t);
-                *os_ << buf;
-            }
-            *os_ << c;
-            bol_ = (c == '\n');
-            if (bol_) os_->flush();
-        }
-        return *this;
-    }
-    template <class T>
-    Log &operator<<(const T &v)
-    {
-        std::ostringstream s;
-        s << v;
-        return *this << s.str();
-    }
-};
+using cqpi_cli::Log;
 
 struct Section {
     std::string name;

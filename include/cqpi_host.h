@@ -53,6 +53,46 @@ int cqpi_orbital_cache(const char *name, double width, double height, double xpo
 int cqpi_xsf_orbital_cache(const char *path, double height, int32_t window, int32_t oversamp, double prefact,
                            double *out);
 
+/* The orbital sources of the orbital-file tool mkwavefunctions (src/mkwavefunctions.cc):
+ *
+ * cqpi_orbital_cache_basis: wannierfunctions(basisvectors, name, ...) + precalculate, its
+ * 'orbitals' keyword (:241-300, src/wannierfunctions.cc:126-221): as cqpi_orbital_cache with
+ * the shifted in-plane point taken to x b0 + y b1 before the rotation (basis = {b0x, b0y, b1x,
+ * b1y}, the basisvector[0] and [1] keywords); basis NULL is the unit basis.
+ *
+ * cqpi_xsf_orbital_cache_shifted: wannierfunctions(filename, shift, height, window,
+ * oversamp, prefact, centre) (src/wannierfunctions.cc:465-487), its 'orbitalfiles' keyword
+ * (:301-324): as cqpi_xsf_orbital_cache with the XSF grid origin moved by shift[3]
+ * (Cartesian) and, for centre != 0, the lattice points at (i/os - w - 0.5, j/os - w - 0.5).
+ *
+ * cqpi_xsf_orbital_cache_mod: wannierfunctions(basisvectors, xcfloader, window, oversamp,
+ * height, xpos, ypos, theta) with xcfloader::getcartmodvalue (src/wannierfunctions.cc:
+ * 500-520, src/loadxcf.cc:268-290), its 'modorbitalfiles' keyword (:184-226):
+ * out[i][j] = prefact * grid value at the Cartesian point R(theta) B (i/os - w - xpos,
+ * j/os - w - ypos) (B the basis, or the unit matrix when NULL; R the rotation about z), with
+ * the grid origin moved by modshift[3] (the tool passes -modpos[k]), at z = height above the
+ * highest atom (below the lowest for height < 0).
+ *
+ * Unreadable files return CQPI_ERR_ARG with the reason in cqpi_host_last_error(). */
+int cqpi_orbital_cache_basis(const char *name, double width, double height, double xpos, double ypos, double theta,
+                             double phi, double prefact, const double *basis, int32_t window, int32_t oversamp,
+                             double *out);
+int cqpi_xsf_orbital_cache_shifted(const char *path, const double *shift, int32_t centre, double height,
+                                   int32_t window, int32_t oversamp, double prefact, double *out);
+int cqpi_xsf_orbital_cache_mod(const char *path, const double *modshift, const double *basis, double height,
+                               double xpos, double ypos, double theta, double prefact, int32_t window,
+                               int32_t oversamp, double *out);
+
+/* One-dimensional interpolation of mkwavefunctions' interpolate() (src/mkwavefunctions.cc:
+ * 39-70, GSL gsl_interp_init / gsl_interp_eval): y[q] = f(x[q]) for the curve f of 'method'
+ * ("linear", "polynomial", "cspline", "cspline_periodic", "akima", "akima_periodic",
+ * "steffen") through (xa[i], ya[i]), i < n.  CQPI_ERR_ARG for an unknown method, fewer points
+ * than the method needs, x values that do not strictly increase, or a point outside
+ * [xa[0], xa[n-1]] (where GSL's default error handler aborts the reference). */
+int cqpi_interp_known(const char *method);
+int cqpi_interp_eval(const char *method, int32_t n, const double *xa, const double *ya, int32_t count,
+                     const double *x, double *y);
+
 /* IDL map header (src/idl.h:41-60). */
 typedef struct {
     char name[1024];

@@ -9,6 +9,7 @@
 # two-line gitversion stub.  Outputs:
 #   oracle/_ref/calcqpi   the reference CLI (src/calcqpi.cc main)
 #   oracle/_ref/refdump   oracle/refdump.cc driving the reference's classes, float64 dumps
+#   oracle/_ref/mkwavefunctions   the reference's orbital-file tool (src/mkwavefunctions.cc main)
 # Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
@@ -24,7 +25,7 @@ CXX="${CXX:-g++}"
 FLAGS="-O2 -fopenmp -w -std=c++14 -I$HERE/compat -I$REF/include -I$REF/src"
 SRCS="qpi tightbinding wannierfunctions idl loadxcf"
 pids=()
-for s in $SRCS calcqpi gethostdata; do
+for s in $SRCS calcqpi gethostdata mkwavefunctions; do
   $CXX $FLAGS -c "$REF/src/$s.cc" -o "$OUT/$s.o" &
   pids+=($!)
 done
@@ -37,4 +38,5 @@ objs=""
 for s in $SRCS; do objs="$objs $OUT/$s.o"; done
 $CXX -fopenmp -o "$OUT/calcqpi" "$OUT/calcqpi.o" "$OUT/gethostdata.o" "$OUT/gitversion.o" $objs
 $CXX -fopenmp -o "$OUT/refdump" "$OUT/refdump.o" $objs
-echo "built $OUT/calcqpi $OUT/refdump"
+$CXX -fopenmp -o "$OUT/mkwavefunctions" "$OUT/mkwavefunctions.o" "$OUT/gitversion.o" $objs
+echo "built $OUT/calcqpi $OUT/refdump $OUT/mkwavefunctions"

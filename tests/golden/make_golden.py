@@ -12,7 +12,10 @@ oracle/_ref/refdump, and stores:
   ref_ldos64.npz                                      float64 maps + tmatrix::calcdos per layer
   meta.json                                           the parameters
 
-Run from the repository root:  python tests/golden/make_golden.py
+The mkwf_* cases do the same for the orbital-file tool (oracle/_ref/mkwavefunctions): the
+inputs, input_<k>.cfg, the reference's IDL output ref_<k>.idl and its log ref_<k>.txt.
+
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
 (requires the reference sources, i.e. only in the build container).
 """
 import json
@@ -219,11 +222,11 @@ XSF_GRID = dict(origin=(-2.5, -2.5, -1.0), axes=((5.0, 0.0, 0.0), (0.0, 5.0, 0.0
                 shape=(40, 40, 16), convvec=((1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 8.0)))
 
 
-def xsf_cubes(names, seed=5, sigma=0.6):
+def xsf_cubes(names, seed=5, sigma=0.6, grid=None):
     """Seeded Wannier-like orbitals on the XSF grid: d angular part (centred on the atom at
     the origin) times a Gaussian, plus 5% seeded noise so that no symmetry hides an index
     error.  Grid points r = origin + (i/xs, j/ys, k/zs) . axes, as the reference reads them."""
-    g = XSF_GRID
+    g = grid or XSF_GRID
     xs, ys, zs = g["shape"]
     i, j, k = np.meshgrid(np.arange(xs), np.arange(ys), np.arange(zs), indexing="ij")
     X = g["origin"][0] + g["axes"][0][0] * i / xs
@@ -439,8 +442,105 @@ def make_case(name, c):
     print(name, "ok", wn, "x", wn, "x", c["layers"])
 
 
+# ------------------------------------------------------------------ mkwavefunctions
+MKWF_XSF_GRID = dict(XSF_GRID, shape=(28, 28, 10))
+# Cases of the orbital-file tool: tests/golden/mkwf_<case>/ holds the inputs, one
+# input_<k>.cfg per configuration, the reference's outputs ref_<k>.idl and its log
+# ref_<k>.txt (oracle/_ref/mkwavefunctions, built from src/mkwavefunctions.cc).
+MKWF_INTERP_METHODS = ("linear", "polynomial", "cspline", "cspline_periodic", "akima", "akima_periodic", "steffen")
+
+MKWF_CASES = {
+    # analytic orbitals with every per-orbital keyword, lattice basis vectors, reorder, double
+    "mkwf_analytic": dict(kind="analytic", configs={
+        "basis": ["window=2;", "oversamp=4;", "orbitals=(dxy,dx2,pz,s,fxyz,n);", "radarr=(0.5,0.7,0.6);",
+                  "anglearr=(10,0,30,0,5,20);", "phiarr=(0,20,0,0,15,0);", "prearr=(1.0,0.5,2.0);",
+                  "pos[1]=(0.25,0.1,0.2);", "pos[4]=(-0.2,0.3);", "basisvector[0]=(1,0);",
+                  "basisvector[1]=(0.5,0.866);", "zheight=1.5;", "reorder=(2,0,1,5,4,3);", "double=1;"],
+        "plain": ["window=1;", "oversamp=5;", "orbitals=(dxz,dyz,dr2,fy3x2,z);", "radius=0.8;", "angle=12;",
+                  "zheight=0.9;", "pos[2]=(0.1,-0.1,0.3);"],
+    }),
+    # XSF orbitals with a global shift and centred pixels (orbitalfiles)
+    "mkwf_xsf": dict(kind="xsf", names=("dxz", "dyz", "dxy"), configs={
+        "shift": ["window=2;", "oversamp=3;", 'orbitalfiles=("orb0.xsf","orb1.xsf","orb2.xsf");',
+                  "shift=(0.3,-0.2,0.1);", "prearr=(1.0,-0.5,2.0);", "zheight=0.7;"],
+        "noshift": ["window=1;", "oversamp=4;", 'orbitalfiles=("orb2.xsf","orb0.xsf");', "zheight=-0.4;"],
+    }),
+    # XSF orbitals placed per orbital (modorbitalfiles): file indices, modpos, pos, rotation,
+    # basis vectors in Angstrom
+    "mkwf_mod": dict(kind="xsf", names=("dxz", "dxy"), configs={
+        "basis": ["window=2;", "oversamp=3;", 'modorbitalfiles=("orb0.xsf","orb1.xsf");',
+                  "modpos[0]=(0.2,0.1,0.0);", "modpos[1]=(-0.1,0.3,0.2);", "orbitals=(0,1,1);",
+                  "pos[1]=(0.25,0.25,0.1);", "pos[2]=(0.5,0);", "angle=15;", "anglearr=(0,10,45);",
+                  "zheight=0.6;", "basisvector[0]=(0.9,0.0);", "basisvector[1]=(0.45,0.78);"],
+        "plain": ["window=1;", "oversamp=4;", 'modorbitalfiles=("orb1.xsf");', "orbitals=(0,0);",
+                  "anglearr=(0,90);", "zheight=0.5;"],
+    }),
+    # an IDL orbital file scaled by prearr (idlorbitalfile)
+    "mkwf_idl": dict(kind="idl", configs={
+        "prearr": ["window=2;", "oversamp=3;", 'idlorbitalfile="orbitals.idl";', "prearr=(2.0,-1.0);",
+                   "double=1;"],
+    }),
+    # pixel-wise interpolation between five IDL orbital files (idlorbitalfiles)
+    "mkwf_interp": dict(kind="interp", configs={
+        m: ["window=1;", "oversamp=4;",
+            'idlorbitalfiles=("in0.idl","in1.idl","in2.idl","in3.idl","in4.idl");',
+            "values=(0.0,0.2,0.5,0.7,1.0);", "interpolate=0.35;", 'interpmethod="%s";' % m]
+        for m in MKWF_INTERP_METHODS
+    } | {"default": ["window=1;", "oversamp=4;",
+                     'idlorbitalfiles=("in0.idl","in1.idl","in2.idl","in3.idl","in4.idl");']}),
+}
+
+
+def _write_idl_cube(path, cube):
+    """cube[orbital][i][j] -> IDL data x fastest ([orb][y][x] in the file)."""
+    F.write_idl(path, np.ascontiguousarray(np.transpose(np.asarray(cube, np.float32), (0, 2, 1))), "orbital cube",
+                scan_range=(1.0, 1.0), offset=(0.0, 0.0), bias=(0.0, 0.0), date="Thu Jan  1 00:00:00 2026")
+
+
+def make_mkwf_case(name, c):
+    d = os.path.join(HERE, name)
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    rng = np.random.default_rng(17)
+    if c["kind"] == "xsf":
+        g = MKWF_XSF_GRID
+        for q, cube in enumerate(xsf_cubes(c["names"], seed=11, grid=g)):
+            F.write_xsf(os.path.join(d, "orb%d.xsf" % q), cube, g["origin"], g["axes"], g["convvec"], [("Fe", 0.0, 0.0, 0.0), ("O", 0.3, 0.2, -0.4)],
+                        comment="seeded %s-like orbital" % c["names"][q])
+    elif c["kind"] == "idl":
+        side = 5 * 3
+        _write_idl_cube(os.path.join(d, "orbitals.idl"), rng.normal(size=(2, side, side)))
+    elif c["kind"] == "interp":
+        side = 3 * 4
+        base = rng.normal(size=(2, side, side))
+        # a smooth, non-monotone family in the parameter plus seeded noise per file
+        for q, v in enumerate((0.0, 0.2, 0.5, 0.7, 1.0)):
+            cube = base * np.cos(2.0 * v) + 0.3 * np.sin(5.0 * v) + 0.05 * rng.normal(size=base.shape)
+            _write_idl_cube(os.path.join(d, "in%d.idl" % q), cube)
+    meta = {"configs": {}}
+    for k, lines in c["configs"].items():
+        cfg = ["# mkwavefunctions golden case %s/%s (generated by tests/golden/make_golden.py)" % (name, k),
+               'tbfile="model_hr.dat";', 'mkwffile="ref_%s.idl";' % k] + lines
+        with open(os.path.join(d, "input_%s.cfg" % k), "w") as fh:
+            fh.write("\n".join(cfg) + "\n")
+        r = subprocess.run([os.path.join(REF, "mkwavefunctions"), "input_%s.cfg" % k], cwd=d, capture_output=True,
+                           text=True, timeout=120)
+        if r.returncode != 0:
+            raise RuntimeError("reference mkwavefunctions failed for %s/%s:\n%s%s" % (name, k, r.stdout, r.stderr))
+        with open(os.path.join(d, "ref_%s.txt" % k), "w") as fh:
+            fh.write(r.stdout)
+        meta["configs"][k] = {"exact": c["kind"] != "interp"}
+    with open(os.path.join(d, "meta.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+    print("golden", name, "configs", list(c["configs"]))
+
+
 if __name__ == "__main__":
-    if not os.path.exists(os.path.join(REF, "calcqpi")):
+    if not os.path.exists(os.path.join(REF, "mkwavefunctions")):
         subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
-    for nm in (sys.argv[1:] or CASES):
-        make_case(nm, CASES[nm])
+    for nm in (sys.argv[1:] or list(CASES) + list(MKWF_CASES)):
+        if nm in MKWF_CASES:
+            make_mkwf_case(nm, MKWF_CASES[nm])
+        else:
+            make_case(nm, CASES[nm])
