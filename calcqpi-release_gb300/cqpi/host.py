@@ -33,6 +33,9 @@ def _lib():
                                      ctypes.c_int32, P, P, P, ctypes.c_double, P]
         L.cqpi_xsf_orbital_cache.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
                                              ctypes.c_double, P]
+        L.cqpi_idl_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_int32, P, P, P, ctypes.c_double]
+        L.cqpi_idl_write_layers.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, P]
         L.cqpi_idl_read_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(_IDLHeader)]
         L.cqpi_idl_read.argtypes = [ctypes.c_char_p, P, ctypes.c_int64]
         L.cqpi_host_last_error.restype = ctypes.c_char_p
@@ -99,6 +102,28 @@ def idl_write(path, data_kyx, name, scan_range=(2.0, 2.0), offset=(-1.0, -1.0), 
     rc = L.cqpi_idl_write(str(path).encode(), name.encode(), None if date is None else date.encode(), x, y, z,
                           sr.ctypes.data_as(ctypes.c_void_p), of.ctypes.data_as(ctypes.c_void_p),
                           bi.ctypes.data_as(ctypes.c_void_p), setpoint, d.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+
+
+def idl_create(path, shape_kyx, name, scan_range=(2.0, 2.0), offset=(-1.0, -1.0), bias=(0.0, 0.0), setpoint=0.0,
+               date=None):
+    """An IDL file of shape (layers, y, x) with zero data, for idl_write_layers."""
+    L = _lib()
+    z, y, x = shape_kyx
+    sr, of, bi = (np.array(v, np.float64) for v in (scan_range, offset, bias))
+    rc = L.cqpi_idl_create(str(path).encode(), name.encode(), None if date is None else date.encode(), x, y, z,
+                           sr.ctypes.data_as(ctypes.c_void_p), of.ctypes.data_as(ctypes.c_void_p),
+                           bi.ctypes.data_as(ctypes.c_void_p), setpoint)
+    if rc:
+        _err(L, rc)
+
+
+def idl_write_layers(path, k0, data_kyx):
+    """Overwrite layers k0 .. k0 + len(data_kyx) - 1 of an existing IDL file in place."""
+    L = _lib()
+    d = np.ascontiguousarray(data_kyx, np.float32)
+    rc = L.cqpi_idl_write_layers(str(path).encode(), int(k0), d.shape[0], d.ctypes.data_as(ctypes.c_void_p))
     if rc:
         _err(L, rc)
 

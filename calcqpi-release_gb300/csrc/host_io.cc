@@ -9,6 +9,8 @@
 //                       shift, modorbitalfiles; src/wannierfunctions.cc:465-520)
 //   cqpi_idl_write / cqpi_idl_read_header / cqpi_idl_read
 //                       IDL map container          (idl::write / idl::read, src/idl.cc:50-97)
+//   cqpi_idl_create / cqpi_idl_write_layers  the same file written layer by layer (the
+//                       CLI's flush / resume keywords)
 // These run on the CPU only; none of them touches the GPU.
 #include <algorithm>
 #include <cmath>
@@ -231,11 +233,10 @@ int cqpi_orbital_cache_basis(const char *name, double width, double height, doub
 }
 
 // ------------------------------------------------------------------ IDL files
-int cqpi_idl_write(const char *path, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
-                   const double *scan_range, const double *offset, const double *bias, double setpoint,
-                   const float *data)
+// idl::write's header (src/idl.cc:78-97): 12 lines formatted like std::ostream defaults
+static void idl_header(std::ostream &os, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
+                       const double *scan_range, const double *offset, const double *bias, double setpoint)
 {
-    if (!path || sx < 0 || sy < 0 || sz < 0 || (!data && (size_t)sx * sy * sz)) return host_fail(CQPI_ERR_ARG, "invalid IDL arguments");
     std::string d;
     if (date) d = date;
     else {
@@ -243,13 +244,56 @@ int cqpi_idl_write(const char *path, const char *name, const char *date, int32_t
         d = ctime(&tt);
         d.resize(d.length() - 1);
     }
-    std::ofstream os(path, std::ios::binary);
-    if (!os) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
     os << (name ? name : "") << std::endl << d << std::endl << (size_t)sx << std::endl << (size_t)sy << std::endl
        << (size_t)sz << std::endl << scan_range[0] << std::endl << scan_range[1] << std::endl << offset[0] << std::endl
        << offset[1] << std::endl << bias[0] << std::endl << bias[1] << std::endl << setpoint << std::endl;
+}
+
+int cqpi_idl_write(const char *path, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
+                   const double *scan_range, const double *offset, const double *bias, double setpoint,
+                   const float *data)
+{
+    if (!path || sx < 0 || sy < 0 || sz < 0 || (!data && (size_t)sx * sy * sz)) return host_fail(CQPI_ERR_ARG, "invalid IDL arguments");
+    std::ofstream os(path, std::ios::binary);
+    if (!os) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
+    idl_header(os, name, date, sx, sy, sz, scan_range, offset, bias, setpoint);
     os.write((const char *)data, (std::streamsize)(sizeof(float) * (size_t)sx * sy * sz));
     if (!os) return host_fail(CQPI_ERR_ARG, std::string("error writing to ") + path);
+    return CQPI_OK;
+}
+
+int cqpi_idl_create(const char *path, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
+                    const double *scan_range, const double *offset, const double *bias, double setpoint)
+{
+    if (!path || sx < 0 || sy < 0 || sz < 0) return host_fail(CQPI_ERR_ARG, "invalid IDL arguments");
+    std::ofstream os(path, std::ios::binary | std::ios::trunc);
+    if (!os) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
+    idl_header(os, name, date, sx, sy, sz, scan_range, offset, bias, setpoint);
+    const std::vector<char> zeros((size_t)1 << 20, 0);
+    size_t left = sizeof(float) * (size_t)sx * sy * sz;
+    while (left && os) {
+        const size_t c = std::min(left, zeros.size());
+        os.write(zeros.data(), (std::streamsize)c);
+        left -= c;
+    }
+    if (!os) return host_fail(CQPI_ERR_ARG, std::string("error writing to ") + path);
+    return CQPI_OK;
+}
+
+int cqpi_idl_write_layers(const char *path, int32_t k0, int32_t nk, const float *data)
+{
+    cqpi_idl_header h;
+    int rc = cqpi_idl_read_header(path, &h);
+    if (rc) return rc;
+    if (!data || k0 < 0 || nk < 0 || (int64_t)k0 + nk > h.size[2])
+        return host_fail(CQPI_ERR_ARG, "layers outside the IDL file");
+    const size_t plane = (size_t)h.size[0] * h.size[1];
+    std::fstream fs(path, std::ios::binary | std::ios::in | std::ios::out);
+    if (!fs) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
+    fs.seekp(h.data_offset + (std::streamoff)(sizeof(float) * plane * (size_t)k0));
+    fs.write((const char *)data, (std::streamsize)(sizeof(float) * plane * (size_t)nk));
+    fs.flush();
+    if (!fs) return host_fail(CQPI_ERR_ARG, std::string("error writing to ") + path);
     return CQPI_OK;
 }
 

@@ -11,7 +11,9 @@
 // keywords (:238, :619-635, :700-701), the map idl(n, n, layers, 2, 2, lenergy, henergy, 0,
 // -1, -1) with its comment line (:638-656), layer energies idl::getbias (src/idl.cc:969-973)
 // and the final save (:779-783).  The band-structure histogram (bsfile) stops with an
-// explicit "not supported" error instead of being ignored.
+// explicit "not supported" error instead of being ignored.  Extensions: precision=fp64|mixed,
+// and flush / resume, which write the map group by group as the layers finish and continue
+// an interrupted run from the layers already on disk.
 #include <unistd.h>
 #include <pwd.h>
 
@@ -103,7 +105,9 @@ void help()
               << " green (normal|surface|bulk), stbfile, epserr (1e-5), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
               << " pos[i], zheight (5.0), idlorbitalfile, orbitalfiles, deltat (0.001), etat (=eta), threshold,\n"
-              << " spinarr\n";
+              << " spinarr\n"
+              << "Extensions: precision (fp64|mixed), flush (true: write each group of layers as it is done),\n"
+              << " resume (true: continue a flushed run, computing only the layers not yet on disk)\n";
 }
 
 double getbias(double lb, double hb, size_t layers, size_t k)
@@ -621,17 +625,76 @@ int main(int argc, char **argv)
 
     std::vector<double> energies(layers);
     for (size_t k = 0; k < layers; k++) energies[k] = getbias(lenergy, henergy, layers, k);
-    std::vector<float> maps(wn * wn * layers);
-    // energies go through the engine in groups so that progress is reported per group
+    const double sr[2] = {2.0, 2.0}, of[2] = {-1.0, -1.0}, bi[2] = {lenergy, henergy};
+
+    // flush=true / resume=true (an extension; the reference writes the map once at the end):
+    // each group of layers goes into qpifile as soon as it is computed and its indices are
+    // appended to <qpifile>.progress; resume=true continues such a run, computing only the
+    // layers that file does not list.  The finished file equals the one-shot output.
+    const bool resume = lf.has("resume") && lf.field("resume") == "true";
+    const bool flush = resume || (lf.has("flush") && lf.field("flush") == "true");
+    const std::string progress = qpifile + ".progress";
+    std::vector<uint8_t> done(layers, 0);
+    if (flush) {
+        bool reuse = false;
+        if (resume) {
+            cqpi_idl_header hd;
+            std::ifstream pf(progress.c_str());
+            if (pf && cqpi_idl_read_header(qpifile.c_str(), &hd) == CQPI_OK) {
+                // the header holds the energies as the stream printed them
+                auto printed = [](double v) {
+                    std::ostringstream o;
+                    o << v;
+                    return o.str();
+                };
+                if ((size_t)hd.size[0] != wn || (size_t)hd.size[1] != wn || (size_t)hd.size[2] != layers ||
+                    printed(hd.bias[0]) != printed(lenergy) || printed(hd.bias[1]) != printed(henergy) ||
+                    comment.str() != hd.name) {
+                    log << "Error: " << qpifile << " does not belong to this calculation (size, energies or model"
+                        << " differ); not resuming over it.\n";
+                    cqpi_destroy(h);
+                    return 1;
+                }
+                long k;
+                while (pf >> k)
+                    if (k >= 0 && (size_t)k < layers) done[(size_t)k] = 1;
+                reuse = true;
+                size_t nd = 0;
+                for (uint8_t d : done) nd += d;
+                log << "Resuming " << qpifile << ": " << nd << " of " << layers << " layers already computed.\n";
+            } else {
+                log << "Nothing to resume (" << qpifile << " or " << progress << " missing), starting afresh.\n";
+            }
+        }
+        if (!reuse) {
+            if (cqpi_idl_create(qpifile.c_str(), comment.str().c_str(), nullptr, (int32_t)wn, (int32_t)wn,
+                                (int32_t)layers, sr, of, bi, 0.0) != CQPI_OK) {
+                log << "Error writing to stream.\n" << cqpi_host_last_error() << "\n";
+                cqpi_destroy(h);
+                return 1;
+            }
+            std::ofstream(progress.c_str(), std::ios::trunc);
+        }
+    }
+    // without flush all layers stay in host memory until the final save; with flush one
+    // group at a time
     const size_t group = 16;
-    for (size_t k0 = 0; k0 < layers; k0 += group) {
-        const size_t ne = std::min(group, layers - k0);
+    std::vector<float> maps(wn * wn * (flush ? std::min(group, layers) : layers));
+    // energies go through the engine in groups of consecutive layers still to compute, so
+    // that progress is reported (and flushed) per group
+    for (size_t k0 = 0; k0 < layers;) {
+        if (done[k0]) {
+            k0++;
+            continue;
+        }
+        size_t ne = 1;
+        while (k0 + ne < layers && ne < group && !done[k0 + ne]) ne++;
         for (size_t k = k0; k < k0 + ne; k++) {
             std::ostringstream l;
             l << "Calculating layer " << k << " at energy " << std::fixed << std::setprecision(4) << energies[k] << "\n";
             log << l.str();
         }
-        float *dst = maps.data() + k0 * wn * wn;
+        float *dst = maps.data() + (flush ? 0 : k0 * wn * wn);
         if (outmode == OUT_SPF)
             rc = cqpi_spf(h, energies.data() + k0, (int32_t)ne, (int32_t)maxbands, dst, nullptr);
         else if (outmode == OUT_USPF)
@@ -645,12 +708,27 @@ int main(int argc, char **argv)
             return 1;
         }
         timings.add("Calculation of CLDOS");
+        if (flush) {
+            if (cqpi_idl_write_layers(qpifile.c_str(), (int32_t)k0, (int32_t)ne, dst) != CQPI_OK) {
+                log << "Error writing to stream.\n" << cqpi_host_last_error() << "\n";
+                cqpi_destroy(h);
+                return 1;
+            }
+            std::ofstream pf(progress.c_str(), std::ios::app);
+            for (size_t k = k0; k < k0 + ne; k++) pf << k << "\n";
+            timings.add("Saving data");
+        }
+        k0 += ne;
     }
-    log << "Calculation finished.\nSaving to " << qpifile << "\n";
-    const double sr[2] = {2.0, 2.0}, of[2] = {-1.0, -1.0}, bi[2] = {lenergy, henergy};
-    rc = cqpi_idl_write(qpifile.c_str(), comment.str().c_str(), nullptr, (int32_t)wn, (int32_t)wn, (int32_t)layers, sr,
-                        of, bi, 0.0, maps.data());
-    if (rc != CQPI_OK) log << "Error writing to stream.\n" << cqpi_host_last_error() << "\n";
+    if (flush) {
+        log << "Calculation finished.\nAll layers saved to " << qpifile << "\n";
+        std::remove(progress.c_str());
+    } else {
+        log << "Calculation finished.\nSaving to " << qpifile << "\n";
+        rc = cqpi_idl_write(qpifile.c_str(), comment.str().c_str(), nullptr, (int32_t)wn, (int32_t)wn, (int32_t)layers,
+                            sr, of, bi, 0.0, maps.data());
+        if (rc != CQPI_OK) log << "Error writing to stream.\n" << cqpi_host_last_error() << "\n";
+    }
     log << "Done.\n";
     timings.add("Saving data");
     cqpi_destroy(h);

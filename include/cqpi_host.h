@@ -108,6 +108,14 @@ typedef struct {
 int cqpi_idl_write(const char *path, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
                    const double *scan_range, const double *offset, const double *bias, double setpoint,
                    const float *data);
+/* The same file written layer by layer (the calcqpi CLI's flush / resume keywords, an
+ * extension: the reference writes the map once at the end, src/calcqpi.cc:779-783).
+ * cqpi_idl_create writes the header of cqpi_idl_write and zero data for sz layers;
+ * cqpi_idl_write_layers overwrites layers k0 .. k0+nk-1 (sx*sy floats each, x fastest) of an
+ * existing file in place.  Layers outside the file return CQPI_ERR_ARG. */
+int cqpi_idl_create(const char *path, const char *name, const char *date, int32_t sx, int32_t sy, int32_t sz,
+                    const double *scan_range, const double *offset, const double *bias, double setpoint);
+int cqpi_idl_write_layers(const char *path, int32_t k0, int32_t nk, const float *data);
 /* Replaces idl::read (src/idl.cc:50-76). */
 int cqpi_idl_read_header(const char *path, cqpi_idl_header *hdr);
 int cqpi_idl_read(const char *path, float *data, int64_t count);

@@ -1,5 +1,6 @@
 """The calcqpi CLI (drop-in for the reference's `calcqpi inputfile`) on every golden case."""
 import os
+import re
 import shutil
 import subprocess
 
@@ -48,3 +49,44 @@ def test_cli_rejects_out_of_scope_modes(built_lib, tmp_path):
         fh.write('bsfile="bs.idl";\n')
     r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "not supported" in r.stdout
+
+
+def test_cli_flush_and_resume(built_lib, tmp_path):
+    """flush=true writes the map group by group; an interrupted run (here: the progress file
+    cut back to layer 0 and the other layers zeroed on disk) continues with resume=true,
+    computing only the missing layers, and ends with the map of a one-shot run."""
+    d, meta, ref = load("c2_analytic")
+    for f in ("model_hr.dat", "input.cfg"):
+        shutil.copy(os.path.join(d, f), tmp_path / f)
+    base = (tmp_path / "input.cfg").read_text()
+    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    oneshot = (tmp_path / "ref_qpi.idl").read_bytes()
+    _, full = F.read_idl(tmp_path / "ref_qpi.idl")
+    assert full.shape[0] >= 2
+    (tmp_path / "f.cfg").write_text(base.replace('qpifile="ref_qpi.idl";', 'qpifile="flush.idl";') + "flush=true;\n")
+    r = subprocess.run([built_lib["cli"], "f.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert not (tmp_path / "flush.idl.progress").exists()
+    got = (tmp_path / "flush.idl").read_bytes()
+    # identical header except the run date, identical data
+    assert got.split(b"\n", 12)[2:] == oneshot.split(b"\n", 12)[2:]
+    # interrupt: only layer 0 is on disk
+    from cqpi import host
+    host.idl_write_layers(tmp_path / "flush.idl", 1, np.zeros_like(full[1:]))
+    (tmp_path / "flush.idl.progress").write_text("0\n")
+    (tmp_path / "r.cfg").write_text(base.replace('qpifile="ref_qpi.idl";', 'qpifile="flush.idl";') + "resume=true;\n")
+    r = subprocess.run([built_lib["cli"], "r.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "1 of %d layers already computed" % full.shape[0] in r.stdout
+    assert "Calculating layer 0 " not in r.stdout and "Calculating layer 1 " in r.stdout
+    _, res = F.read_idl(tmp_path / "flush.idl")
+    assert np.array_equal(res[0], full[0])
+    assert np.abs(res.astype(np.float64) - full).max() <= 2e-7 * np.abs(full).max()
+    # a file of another calculation is not resumed over
+    (tmp_path / "flush.idl.progress").write_text("0\n")
+    cfg = base.replace('qpifile="ref_qpi.idl";', 'qpifile="flush.idl";') + "resume=true;\n"
+    cfg = re.sub(r"layers=(\d+);", lambda m: "layers=%d;" % (int(m.group(1)) + 1), cfg)
+    (tmp_path / "x.cfg").write_text(cfg)
+    r = subprocess.run([built_lib["cli"], "x.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1 and "does not belong" in r.stdout

@@ -86,6 +86,24 @@ def test_orbital_cache_matches_reference_wffile(built_lib):
         assert np.abs(got.astype(np.float32).T - data[o]).max() <= 1e-7 * np.abs(data[o]).max()
 
 
+def test_idl_layerwise_equals_oneshot(built_lib, tmp_path):
+    """cqpi_idl_create + cqpi_idl_write_layers (the CLI's flush / resume) give the file that
+    cqpi_idl_write gives in one go, whatever order the layer groups arrive in."""
+    from cqpi import host
+    rng = np.random.default_rng(3)
+    data = rng.normal(size=(7, 5, 6)).astype(np.float32)
+    kw = dict(scan_range=(2.0, 2.0), offset=(-1.0, -1.0), bias=(-0.1, 0.1), date="Thu Jan  1 00:00:00 2026")
+    host.idl_write(tmp_path / "one.idl", data, "CQPI calculation for m with window=2 and oversamp=4", **kw)
+    host.idl_create(tmp_path / "lay.idl", data.shape, "CQPI calculation for m with window=2 and oversamp=4", **kw)
+    _, z = host.idl_read(tmp_path / "lay.idl")
+    assert z.shape == data.shape and not z.any()
+    for k0, k1 in ((4, 7), (0, 2), (2, 4)):
+        host.idl_write_layers(tmp_path / "lay.idl", k0, data[k0:k1])
+    assert (tmp_path / "lay.idl").read_bytes() == (tmp_path / "one.idl").read_bytes()
+    with pytest.raises(host.HostError):
+        host.idl_write_layers(tmp_path / "lay.idl", 6, data[:2])   # past the last layer
+
+
 def test_idl_roundtrip_and_reference_bytes(built_lib, tmp_path):
     from cqpi import host
     for name in NAMES:
