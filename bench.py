@@ -178,6 +178,24 @@ def cpu_sample(cfg_name, target_s=8.0, threads=None):
     return value, O.num_threads(), desc
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over all ranks of the process group (every rank passes its own x and gets
+    the maximum back); x itself without a process group.  Replicas finish when the slowest
+    one does, so the job's time is the maximum."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, work_per_rank, seconds):
+    """Units all ranks processed per second: each of the world replicas did work_per_rank
+    units (weak scaling), and the job took the slowest rank's time."""
+    return world * work_per_rank / seconds
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -279,12 +297,9 @@ def run_ours(args):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
     launches = eng.kernel_launches() - launches0
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, "cuda")
     work_per_rank = c.pixels_per_energy * nE
-    value = world * work_per_rank / (ms / 1e3)
+    value = whole_job_rate(world, work_per_rank, ms / 1e3)
 
     # e2e through the public API with host buffers, as a serving host would call it: one
     # handle; every step uploads the model's hopping amplitudes, the orbitals and the
@@ -316,11 +331,8 @@ def run_ours(args):
     barrier()
     e2e_s = statistics.median(e2e_times)
     e2.close()
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * work_per_rank / e2e_s
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
+    e2e_value = whole_job_rate(world, work_per_rank, e2e_s)
 
     # roofline of the dominant kernel (the LDOS contraction)
     peaks, peak_src = measured_peaks()
