@@ -10,6 +10,8 @@
 #   oracle/_ref/calcqpi   the reference CLI (src/calcqpi.cc main)
 #   oracle/_ref/refdump   oracle/refdump.cc driving the reference's classes, float64 dumps
 #   oracle/_ref/mkwavefunctions   the reference's orbital-file tool (src/mkwavefunctions.cc main)
+#   oracle/_ref/seam_check   oracle/seam_check.cc: the GB300QPI backend built against the
+#                            reference's GPUQPI interface and linked with libcqpi.so
 # Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
@@ -39,4 +41,13 @@ for s in $SRCS; do objs="$objs $OUT/$s.o"; done
 $CXX -fopenmp -o "$OUT/calcqpi" "$OUT/calcqpi.o" "$OUT/gethostdata.o" "$OUT/gitversion.o" $objs
 $CXX -fopenmp -o "$OUT/refdump" "$OUT/refdump.o" $objs
 $CXX -fopenmp -o "$OUT/mkwavefunctions" "$OUT/mkwavefunctions.o" "$OUT/gitversion.o" $objs
+# the GB300QPI backend of the narrow seam, compiled against the reference's GPUQPI interface
+# and linked with libcqpi.so (when the library has been built)
+LIBDIR="$(cd "$HERE/.." && pwd)/calcqpi-release_gb300/_build"
+if [ -f "$LIBDIR/libcqpi.so" ]; then
+  $CXX $FLAGS -I"$HERE/../include" -I"$HERE/../calcqpi-release_gb300/seam" -c "$HERE/seam_check.cc" \
+    -o "$OUT/seam_check.o"
+  $CXX -fopenmp -o "$OUT/seam_check" "$OUT/seam_check.o" "$OUT/wannierfunctions.o" "$OUT/idl.o" \
+    "$OUT/loadxcf.o" -L"$LIBDIR" -lcqpi -Wl,-rpath,"$LIBDIR"
+fi
 echo "built $OUT/calcqpi $OUT/refdump $OUT/mkwavefunctions"
