@@ -38,6 +38,14 @@ def _lib():
         L.cqpi_idl_write_layers.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, P]
         L.cqpi_idl_read_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(_IDLHeader)]
         L.cqpi_idl_read.argtypes = [ctypes.c_char_p, P, ctypes.c_int64]
+        L.cqpi_orbital_cache_basis.argtypes = [ctypes.c_char_p] + [ctypes.c_double] * 7 + [P, ctypes.c_int32,
+                                                                                         ctypes.c_int32, P]
+        L.cqpi_xsf_orbital_cache_shifted.argtypes = [ctypes.c_char_p, P, ctypes.c_int32, ctypes.c_double,
+                                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P]
+        L.cqpi_xsf_orbital_cache_mod.argtypes = [ctypes.c_char_p, P, P] + [ctypes.c_double] * 5 + [ctypes.c_int32,
+                                                                                                 ctypes.c_int32, P]
+        L.cqpi_interp_known.argtypes = [ctypes.c_char_p]
+        L.cqpi_interp_eval.argtypes = [ctypes.c_char_p, ctypes.c_int32, P, P, ctypes.c_int32, P, P]
         L.cqpi_host_last_error.restype = ctypes.c_char_p
         L._host_ready = True
     return L
@@ -91,6 +99,81 @@ def xsf_orbital_cache(path, height, window, oversamp, prefact=1.0) -> np.ndarray
     if rc:
         _err(L, rc)
     return out
+
+
+def _vec(v, n):
+    """A float64 array of n values (or None for NULL)."""
+    if v is None:
+        return None
+    a = np.ascontiguousarray(np.asarray(v, np.float64).reshape(-1))
+    if a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def orbital_cache_basis(name, window, oversamp, width=0.5, height=5.0, xpos=0.0, ypos=0.0, theta=0.0, phi=0.0,
+                        prefact=1.0, basis=None) -> np.ndarray:
+    """Analytic orbital cache with lattice basis vectors basis = ((b0x, b0y), (b1x, b1y)) or
+    None (mkwavefunctions' 'orbitals' source)."""
+    L = _lib()
+    side = (2 * window + 1) * oversamp
+    out = np.empty((side, side), np.float64)
+    b = _vec(basis, 4)
+    rc = L.cqpi_orbital_cache_basis(name.encode(), width, height, xpos, ypos, theta, phi, prefact, _ptr(b), window,
+                                    oversamp, out.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+    return out
+
+
+def xsf_orbital_cache_shifted(path, height, window, oversamp, shift=(0.0, 0.0, 0.0), prefact=1.0,
+                              centre=True) -> np.ndarray:
+    """XSF orbital cache with the grid moved by shift and centred pixels (mkwavefunctions'
+    'orbitalfiles' source)."""
+    L = _lib()
+    side = (2 * window + 1) * oversamp
+    out = np.empty((side, side), np.float64)
+    sh = _vec(shift, 3)
+    rc = L.cqpi_xsf_orbital_cache_shifted(str(path).encode(), _ptr(sh), 1 if centre else 0, height, window, oversamp,
+                                          prefact, out.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+    return out
+
+
+def xsf_orbital_cache_mod(path, height, window, oversamp, modshift=(0.0, 0.0, 0.0), basis=None, xpos=0.0, ypos=0.0,
+                          theta=0.0, prefact=1.0) -> np.ndarray:
+    """XSF orbital placed at (xpos, ypos), rotated by theta, with the grid moved by modshift
+    (mkwavefunctions' 'modorbitalfiles' source)."""
+    L = _lib()
+    side = (2 * window + 1) * oversamp
+    out = np.empty((side, side), np.float64)
+    sh, b = _vec(modshift, 3), _vec(basis, 4)
+    rc = L.cqpi_xsf_orbital_cache_mod(str(path).encode(), _ptr(sh), _ptr(b), height, xpos, ypos, theta, prefact,
+                                      window, oversamp, out.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        _err(L, rc)
+    return out
+
+
+def interp_eval(method, xa, ya, x) -> np.ndarray:
+    """One-dimensional interpolation of mkwavefunctions (GSL's methods by name)."""
+    L = _lib()
+    xa = np.ascontiguousarray(xa, np.float64)
+    ya = np.ascontiguousarray(ya, np.float64)
+    xs = np.ascontiguousarray(np.atleast_1d(x), np.float64)
+    if xa.shape != ya.shape:
+        raise ValueError("xa and ya differ in length")
+    y = np.empty_like(xs)
+    rc = L.cqpi_interp_eval(method.encode(), xa.size, _ptr(xa), _ptr(ya), xs.size, _ptr(xs), _ptr(y))
+    if rc:
+        raise HostError(f"status {rc}: interpolation '{method}' rejected its input (method, point count, "
+                        "increasing x values, x inside the data range)")
+    return y
 
 
 def idl_write(path, data_kyx, name, scan_range=(2.0, 2.0), offset=(-1.0, -1.0), bias=(0.0, 0.0), setpoint=0.0,

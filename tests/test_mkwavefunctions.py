@@ -211,3 +211,25 @@ def test_tool_output_feeds_calcqpi_orbitals(built_lib, tmp_path):
                                       out.ctypes.data_as(dp))
     assert rc == 0
     np.testing.assert_array_equal(data[2].T, out.reshape(side, side).astype(np.float32))
+
+
+def test_python_bindings(built_lib, tmp_path):
+    """cqpi.host binds the tool's host functions: the same caches as the C ABI calls above."""
+    from cqpi import host
+    side = 3 * 5
+    a = host.orbital_cache_basis("dr2", 1, 5, width=0.8, height=0.6, xpos=0.1, ypos=-0.1,
+                                 theta=12 * np.pi / 180)
+    b = host.orbital_cache("dr2", 1, 5, width=0.8, height=0.6, xpos=0.1, ypos=-0.1, theta=12 * np.pi / 180)
+    assert a.shape == (side, side) and np.array_equal(a, b)
+    sheared = host.orbital_cache_basis("dxy", 1, 5, width=0.8, height=0.6, basis=((1.0, 0.0), (0.5, 0.866)))
+    assert not np.array_equal(sheared, host.orbital_cache("dxy", 1, 5, width=0.8, height=0.6))
+    xsf = os.path.join(GOLDEN, "mkwf_xsf", "orb0.xsf")
+    c0 = host.xsf_orbital_cache_shifted(xsf, 0.7, 2, 3, shift=(0.0, 0.0, 0.0), centre=False)
+    np.testing.assert_array_equal(c0, host.xsf_orbital_cache(xsf, 0.7, 2, 3))
+    m0 = host.xsf_orbital_cache_mod(xsf, 0.7, 2, 3)
+    assert m0.shape == (15, 15) and np.abs(m0).max() > 0
+    y = host.interp_eval("linear", [0.0, 1.0, 2.0], [0.0, 2.0, 0.0], [0.5, 1.5])
+    np.testing.assert_allclose(y, [1.0, 1.0])
+    with pytest.raises(host.HostError):
+        host.interp_eval("linear", [0.0, 1.0], [0.0, 1.0], 2.0)
+
