@@ -269,12 +269,12 @@ int cqpi_idl_create(const char *path, const char *name, const char *date, int32_
     std::ofstream os(path, std::ios::binary | std::ios::trunc);
     if (!os) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
     idl_header(os, name, date, sx, sy, sz, scan_range, offset, bias, setpoint);
-    const std::vector<char> zeros((size_t)1 << 20, 0);
-    size_t left = sizeof(float) * (size_t)sx * sy * sz;
-    while (left && os) {
-        const size_t c = std::min(left, zeros.size());
-        os.write(zeros.data(), (std::streamsize)c);
-        left -= c;
+    // the data region reads as zeros: extend the file to its full length by writing its last
+    // byte (the file system leaves the rest as a hole instead of writing gigabytes of zeros)
+    const size_t bytes = sizeof(float) * (size_t)sx * sy * sz;
+    if (bytes) {
+        os.seekp((std::streamoff)(bytes - 1), std::ios::cur);
+        os.put('\0');
     }
     if (!os) return host_fail(CQPI_ERR_ARG, std::string("error writing to ") + path);
     return CQPI_OK;
