@@ -10,8 +10,8 @@
 // (:577-600), wffile output (:602-618), the proximity list of the threshold / spinarr
 // keywords (:238, :619-635, :700-701), the map idl(n, n, layers, 2, 2, lenergy, henergy, 0,
 // -1, -1) with its comment line (:638-656), layer energies idl::getbias (src/idl.cc:969-973)
-// and the final save (:779-783).  The band-structure histogram (bsfile) stops with an
-// explicit "not supported" error instead of being ignored.  Extensions: precision=fp64|mixed,
+// and the final save (:779-783), and the band-structure histogram of bsfile (:308-326, computed
+// on the host cores as the reference does).  Extensions: precision=fp64|mixed,
 // and flush / resume, which write the map group by group as the layers finish and continue
 // an interrupted run from the layers already on disk.
 #include <unistd.h>
@@ -105,7 +105,7 @@ void help()
               << " green (normal|surface|bulk), stbfile, epserr (1e-5), fermi (0), scattering, phase ((1,0)), eta (0.005), spin, scmodel, magscat,\n"
               << " window (2; 0 = from the orbital range), radius (0.5), angle, anglearr, prearr, orbitals,\n"
               << " pos[i], zheight (5.0), idlorbitalfile, orbitalfiles, deltat (0.001), etat (=eta), threshold,\n"
-              << " spinarr\n"
+              << " spinarr, bsfile, bslattice (201), bsoversamp (8), bsenergies ((-0.1,0.1)), bslayers (21)\n"
               << "Extensions: precision (fp64|mixed), flush (true: write each group of layers as it is done),\n"
               << " resume (true: continue a flushed run, computing only the layers not yet on disk)\n";
 }
@@ -114,12 +114,6 @@ double getbias(double lb, double hb, size_t layers, size_t k)
 {
     if (layers == 1) return lb;
     return (hb - lb) * (double)k / ((double)layers - 1.0) + lb;
-}
-
-int not_supported(Log &log, const std::string &what)
-{
-    log << "Error: " << what << " is not supported by the GB300 continuum-LDOS engine - exiting.\n";
-    return 1;
 }
 
 }  // namespace
@@ -238,7 +232,6 @@ int main(int argc, char **argv)
         log << l.str() << "\n";
     }
     if (lf.has("magscat")) magscat = lf.value("magscat");
-    if (lf.has("bsfile")) return not_supported(log, "bsfile (band-structure histogram)");
     // density of states file (src/calcqpi.cc:336-391)
     std::string dosfile;
     size_t doslayers = 101;
@@ -292,6 +285,37 @@ int main(int argc, char **argv)
             log << "Warning: Tight-binding model in file " << tbfile << " is not in principal layer form.\n";
         if (shr && !principal(shr))
             log << "Warning: Surface tight-binding model in file " << stbfile << " is not in principal layer form.\n";
+    }
+    // band-structure histogram (src/calcqpi.cc:308-326), on the host cores as the reference
+    if (lf.has("bsfile")) {
+        size_t bslattice = 201, bslayers = 21, bsoversamp = 8;
+        double bslenergy = -0.1, bshenergy = 0.1;
+        const std::string bsfile = lf.str("bsfile");
+        if (lf.has("bslayers")) bslayers = lf.ivalue("bslayers");
+        if (lf.has("bsenergies")) {
+            std::vector<double> be = lf.vec("bsenergies");
+            be.resize(2, 0.0);
+            bslenergy = be[0];
+            bshenergy = be[1];
+        }
+        if (lf.has("bslattice")) bslattice = lf.ivalue("bslattice");
+        if (lf.has("bsoversamp")) bsoversamp = lf.ivalue("bsoversamp");
+        log << "Calculating band structure histogram in energy range (" << bslenergy << "," << bshenergy << ") with "
+            << bslayers << " layers and oversampling " << bsoversamp << ".\n";
+        const cqpi_model bm = {hr->bands, hr->scmaxbands, efermi, hr->nhops, hr->R, hr->orb, hr->t, hr->anti};
+        std::vector<double> hist(bslattice * bslattice * bslayers);
+        if (cqpi_band_histogram(&bm, (int32_t)bslattice, (int32_t)bsoversamp, bslenergy, bshenergy, (int32_t)bslayers,
+                                hist.data()) != CQPI_OK) {
+            log << "Error: invalid band-structure histogram parameters.\n";
+            return 1;
+        }
+        const std::vector<float> hf(hist.begin(), hist.end());
+        const double sr[2] = {1.0, 1.0}, of[2] = {-0.5, -0.5}, bi[2] = {bslenergy, bshenergy};
+        if (cqpi_idl_write(bsfile.c_str(), hr->name, nullptr, (int32_t)bslattice, (int32_t)bslattice,
+                           (int32_t)bslayers, sr, of, bi, 0.0, hf.data()) != CQPI_OK)
+            log << "Error writing to stream.\n" << cqpi_host_last_error() << "\n";
+        log << "... done and saved to " << bsfile << ".\n";
+        timings.add("Bandstructure calculation");
     }
     double maxhop = 0.0;
     for (int64_t i = 0; i < hr->nhops; i++) maxhop = std::max(maxhop, std::hypot(hr->t[2 * i], hr->t[2 * i + 1]));
@@ -539,6 +563,14 @@ int main(int argc, char **argv)
     }
 
     // ---------------------------------------------------------------- engine
+    if (outmode == OUT_NONE && dosfile.empty()) {
+        // nothing left for the GPU (output=nomode: at most the band-structure histogram and
+        // the wffile above)
+        cqpi_hr_free(hr);
+        if (shr) cqpi_hr_free(shr);
+        timings.print(log);
+        return 0;
+    }
     cqpi_model model = {hr->bands, hr->scmaxbands, efermi, hr->nhops, hr->R, hr->orb, hr->t, hr->anti};
     cqpi_params par = {(int32_t)n, (int32_t)kpoints, (int32_t)oversamp, (int32_t)window, (int32_t)maxbands,
                        spin ? 1 : 0, eta, CQPI_PREC_FP64};

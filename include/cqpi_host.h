@@ -8,6 +8,8 @@
 
 #include <stdint.h>
 
+#include "cqpi.h"   /* cqpi_model */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -92,6 +94,17 @@ int cqpi_xsf_orbital_cache_mod(const char *path, const double *modshift, const d
 int cqpi_interp_known(const char *method);
 int cqpi_interp_eval(const char *method, int32_t n, const double *xa, const double *ya, int32_t count,
                      const double *x, double *y);
+
+/* Band-structure histogram of the bsfile keyword: replaces tightbind::calcbst3dhisthr(fname,
+ * pix, le, ue, layers, oversamp) (src/tightbinding.cc:1158-1193; driver src/calcqpi.cc:308-326).
+ * Eigenvalues of H(k) (the model's terms with the Fermi-energy diagonal, all R_z at k_z = 0)
+ * on the (pix*oversamp)^2 grid k = (io, jo) / (pix*oversamp - 1) - 1/2, each adding a
+ * Lorentzian of width 2 (ue - le) / layers to the three nearest of the layers energies
+ * le .. ue in pixel (io / oversamp, jo / oversamp).  out[layers][pix][pix] (x fastest, the
+ * IDL order of idl(pix, pix, layers, 1, 1, le, ue, 0, -0.5, -0.5)).  CPU only, on all host
+ * cores, as the reference computes it. */
+int cqpi_band_histogram(const cqpi_model *m, int32_t pix, int32_t oversamp, double le, double ue, int32_t layers,
+                        double *out);
 
 /* IDL map header (src/idl.h:41-60). */
 typedef struct {

@@ -12,7 +12,8 @@ oracle/_ref/refdump, and stores:
   ref_ldos64.npz                                      float64 maps + tmatrix::calcdos per layer
   meta.json                                           the parameters
 
-The mkwf_* cases do the same for the orbital-file tool (oracle/_ref/mkwavefunctions): the
+The bs_* cases record band-structure histograms (bsfile, output=nomode) of the reference's
+CLI.  The mkwf_* cases do the same for the orbital-file tool (oracle/_ref/mkwavefunctions): the
 inputs, input_<k>.cfg, the reference's IDL output ref_<k>.idl and its log ref_<k>.txt.
 
 Run from the repository root:  python tests/golden/make_golden.py [case ...]
@@ -536,11 +537,49 @@ def make_mkwf_case(name, c):
     print("golden", name, "configs", list(c["configs"]))
 
 
+# ------------------------------------------------------------------ bsfile
+# Band-structure histograms (tightbind::calcbst3dhisthr through the driver's bsfile keyword,
+# output=nomode): tests/golden/bs_<case>/ holds model_hr.dat, input.cfg, the reference's
+# ref_bs.idl and its log.  The reference runs single-threaded: its OpenMP loop can let two
+# threads add into one pixel at once.
+BS_CASES = {
+    "bs_t2g": dict(model="t2g", keys=["bslattice=24;", "bsoversamp=3;", "bsenergies=(-0.6,0.4);",
+                                       "bslayers=15;", "fermi=0.05;"]),
+    "bs_bdg": dict(model="bdg_t2g", keys=["scmodel=true;", "bslattice=16;", "bsoversamp=4;",
+                                          "bsenergies=(-0.3,0.3);", "bslayers=9;"]),
+    "bs_layered": dict(model="c1_layered", keys=["bslattice=20;", "bsoversamp=2;", "bsenergies=(-2.0,2.0);",
+                                                 "bslayers=31;"]),
+}
+
+
+def make_bs_case(name, c):
+    d = os.path.join(HERE, name)
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    terms = {"t2g": lambda: W.t2g_c2().terms(), "bdg_t2g": bdg_t2g, "c1_layered": c1_layered}[c["model"]]()
+    bands = next(iter(terms.values())).shape[0]
+    F.write_hr(os.path.join(d, "model_hr.dat"), "band-structure case %s" % name, bands, terms, None)
+    cfg = ["# band-structure histogram case %s (generated by tests/golden/make_golden.py)" % name,
+           'tbfile="model_hr.dat";', "output=nomode;", 'bsfile="ref_bs.idl";'] + c["keys"]
+    with open(os.path.join(d, "input.cfg"), "w") as fh:
+        fh.write("\n".join(cfg) + "\n")
+    r = subprocess.run([os.path.join(REF, "calcqpi"), "input.cfg"], cwd=d, capture_output=True, text=True,
+                       timeout=600, env=dict(os.environ, OMP_NUM_THREADS="1"))
+    if r.returncode != 0 or not os.path.exists(os.path.join(d, "ref_bs.idl")):
+        raise RuntimeError("reference bsfile run failed for %s:\n%s%s" % (name, r.stdout, r.stderr))
+    with open(os.path.join(d, "ref_stdout.txt"), "w") as fh:
+        fh.write(r.stdout)
+    print("golden", name)
+
+
 if __name__ == "__main__":
     if not os.path.exists(os.path.join(REF, "mkwavefunctions")):
         subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
-    for nm in (sys.argv[1:] or list(CASES) + list(MKWF_CASES)):
+    for nm in (sys.argv[1:] or list(CASES) + list(MKWF_CASES) + list(BS_CASES)):
         if nm in MKWF_CASES:
             make_mkwf_case(nm, MKWF_CASES[nm])
+        elif nm in BS_CASES:
+            make_bs_case(nm, BS_CASES[nm])
         else:
             make_case(nm, CASES[nm])

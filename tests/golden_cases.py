@@ -5,9 +5,10 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# calcqpi cases; the mkwf_* directories hold the orbital-file tool's cases (own test file)
+# calcqpi cases; the mkwf_* directories hold the orbital-file tool's cases and the bs_* ones the
+# band-structure histograms (own test files)
 NAMES = sorted(d for d in os.listdir(GOLDEN)
-               if os.path.isdir(os.path.join(GOLDEN, d)) and not d.startswith(("_", "mkwf_")))
+               if os.path.isdir(os.path.join(GOLDEN, d)) and not d.startswith(("_", "mkwf_", "bs_")))
 
 
 def load(name):

@@ -1,0 +1,93 @@
+"""The band-structure histogram of the bsfile keyword (cqpi_band_histogram, run by the calcqpi
+CLI on the host cores as the reference's driver does) against the reference's own output:
+tests/golden/bs_*/ from tightbind::calcbst3dhisthr (src/tightbinding.cc:1158-1193) through
+the reference CLI with output=nomode (a 3-band model with a Fermi energy, a BdG model with
+conjugated hole terms, a layered model with R_z != 0 terms).  An output=nomode run needs no
+GPU, so these run on the CPU."""
+import ctypes
+import glob
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import formats as F
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+CASES = sorted(os.path.basename(d) for d in glob.glob(os.path.join(GOLDEN, "bs_*")))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cli_bsfile_matches_reference(built_lib, tmp_path, case):
+    src = os.path.join(GOLDEN, case)
+    for f in ("model_hr.dat", "input.cfg"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    cfg = (tmp_path / "input.cfg").read_text().replace('bsfile="ref_bs.idl";', 'bsfile="ours.idl";')
+    (tmp_path / "input.cfg").write_text(cfg)
+    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "... done and saved to ours.idl." in r.stdout
+    hr, ref = F.read_idl(os.path.join(src, "ref_bs.idl"))
+    ho, ours = F.read_idl(str(tmp_path / "ours.idl"))
+    for key in ("name", "size", "scan_range", "offset", "bias", "setpoint"):
+        assert ho[key] == hr[key], (key, ho[key], hr[key])
+    assert np.abs(ref).max() > 0
+    # eigenvalues from a different Jacobi order: agreement to float32 rounding
+    assert np.abs(ours.astype(np.float64) - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+def _restated_histogram(model, pix, os_, le, ue, layers, efermi, scmax):
+    """NumPy restatement (numpy.linalg.eigvalsh on the lower triangle)."""
+    b = model["bands"]
+    R, orb, t, anti = model["R"], model["orb"], model["t"], model["anti"]
+    osp = pix * os_
+    out = np.zeros((layers, pix, pix))
+    binsize = (ue - le) / (layers - 1)
+    w = (ue - le) / layers * 2.0
+    for io in range(osp):
+        for jo in range(osp):
+            kx, ky = io / (osp - 1) - 0.5, jo / (osp - 1) - 0.5
+            H = np.diag([-efermi if d < scmax else efermi for d in range(b)]).astype(complex)
+            ph = 2 * np.pi * (R[:, 0] * kx + R[:, 1] * ky)
+            ph = np.where(anti.astype(bool), -ph, ph)
+            np.add.at(H, (orb[:, 0], orb[:, 1]), (t[:, 0] + 1j * t[:, 1]) * np.exp(1j * ph))
+            for e in np.linalg.eigvalsh(H, UPLO="L"):
+                if not (le - 2 * binsize < e < ue + 2 * binsize):
+                    continue
+                lay = int(np.round((e - le) / (ue - le) * (layers - 1)))
+                for nl in (lay - 1, lay, lay + 1):
+                    if 0 <= nl < layers:
+                        x = (ue - le) * nl / (layers - 1) + le - e
+                        out[nl, jo // os_, io // os_] += w / 2 / (x * x + w * w / 4) / np.pi
+    return out
+
+
+def test_band_histogram_matches_numpy_restatement(built_lib):
+    from cqpi import host
+    hr = host.read_hr(os.path.join(GOLDEN, "bs_bdg", "model_hr.dat"), scmodel=True)
+    lib = ctypes.CDLL(built_lib["lib"])
+
+    class Model(ctypes.Structure):
+        _fields_ = [("bands", ctypes.c_int32), ("scmaxbands", ctypes.c_int32), ("efermi", ctypes.c_double),
+                    ("nhops", ctypes.c_int64), ("R", ctypes.c_void_p), ("orb", ctypes.c_void_p),
+                    ("t", ctypes.c_void_p), ("anti", ctypes.c_void_p)]
+
+    R = np.ascontiguousarray(hr["R"], np.int32)
+    orb = np.ascontiguousarray(hr["orb"], np.int32)
+    t = np.ascontiguousarray(np.stack([hr["t"].real, hr["t"].imag], -1), np.float64)
+    anti = np.ascontiguousarray(hr["anti"], np.uint8)
+    efermi = 0.02
+    m = Model(hr["bands"], hr["scmaxbands"], efermi, len(anti), R.ctypes.data, orb.ctypes.data, t.ctypes.data,
+              anti.ctypes.data)
+    pix, os_, le, ue, layers = 6, 3, -0.3, 0.3, 9
+    out = np.zeros((layers, pix, pix))
+    lib.cqpi_band_histogram.argtypes = [ctypes.POINTER(Model), ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int32, ctypes.c_void_p]
+    assert lib.cqpi_band_histogram(ctypes.byref(m), pix, os_, le, ue, layers, out.ctypes.data) == 0
+    want = _restated_histogram(dict(bands=hr["bands"], R=R, orb=orb, t=t, anti=anti), pix, os_, le, ue, layers,
+                               efermi, hr["scmaxbands"])
+    assert np.abs(want).max() > 0
+    np.testing.assert_allclose(out, want, rtol=1e-10, atol=1e-12 * np.abs(want).max())

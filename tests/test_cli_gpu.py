@@ -41,16 +41,6 @@ def test_cli_reproduces_reference_output(built_lib, name, tmp_path):
         assert np.abs(dw - dw0).max() <= 1e-7 * np.abs(dw0).max()
 
 
-def test_cli_rejects_out_of_scope_modes(built_lib, tmp_path):
-    d, meta, ref = load("c1_idl")
-    for f in ("model_hr.dat", "orbitals.idl", "input.cfg"):
-        shutil.copy(os.path.join(d, f), tmp_path / f)
-    with open(tmp_path / "input.cfg", "a") as fh:
-        fh.write('bsfile="bs.idl";\n')
-    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
-    assert r.returncode == 1 and "not supported" in r.stdout
-
-
 def test_cli_flush_and_resume(built_lib, tmp_path):
     """flush=true writes the map group by group; an interrupted run (here: the progress file
     cut back to layer 0 and the other layers zeroed on disk) continues with resume=true,
