@@ -74,7 +74,7 @@ def build_lib(verbose=False, extra_flags=()) -> str:
     _run_parallel(cmds, verbose)
     if cmds or not _newer(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        _run_parallel([[NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]], verbose)
+        _run_parallel([[NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]], verbose)
         os.replace(tmp, LIB)
     return LIB
 
