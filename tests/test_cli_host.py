@@ -1,9 +1,14 @@
-"""The band-structure histogram of the bsfile keyword (cqpi_band_histogram, run by the calcqpi
-CLI on the host cores as the reference's driver does) against the reference's own output:
-tests/golden/bs_*/ from tightbind::calcbst3dhisthr (src/tightbinding.cc:1158-1193) through
-the reference CLI with output=nomode (a 3-band model with a Fermi energy, a BdG model with
-conjugated hole terms, a layered model with R_z != 0 terms).  An output=nomode run needs no
-GPU, so these run on the CPU."""
+"""calcqpi CLI runs that need no GPU (output=nomode creates no engine), against the reference's
+own outputs:
+
+  * the band-structure histogram of the bsfile keyword (cqpi_band_histogram, on the host cores
+    as the reference's driver computes it): tests/golden/bs_*/ from tightbind::calcbst3dhisthr
+    (src/tightbinding.cc:1158-1193) through the reference CLI (a 3-band model with a Fermi
+    energy, a BdG model with conjugated hole terms, a layered model with R_z != 0 terms), and
+    a NumPy restatement;
+  * the orbital setup and wffile output of every golden case that has one (analytic, IDL and
+    XSF orbitals, padding, spin duplication).
+"""
 import ctypes
 import glob
 import os
@@ -91,3 +96,34 @@ def test_band_histogram_matches_numpy_restatement(built_lib):
                                efermi, hr["scmaxbands"])
     assert np.abs(want).max() > 0
     np.testing.assert_allclose(out, want, rtol=1e-10, atol=1e-12 * np.abs(want).max())
+
+
+def _wf_cases():
+    from golden_cases import NAMES
+    return [n for n in NAMES if os.path.exists(os.path.join(GOLDEN, n, "ref_wf.idl"))]
+
+
+@pytest.mark.parametrize("name", _wf_cases())
+def test_cli_wffile_matches_reference_without_gpu(built_lib, tmp_path, name):
+    """The orbital setup of the CLI (analytic, IDL and XSF orbitals, padding, spin duplication)
+    and its wffile output, in an output=nomode run that needs no GPU, against the reference's
+    wffile of the same golden case."""
+    src = os.path.join(GOLDEN, name)
+    for f in os.listdir(src):
+        if f in ("model_hr.dat", "surf_hr.dat", "orbitals.idl") or f.endswith(".xsf"):
+            shutil.copy(os.path.join(src, f), tmp_path / f)
+    lines = []
+    for line in open(os.path.join(src, "input.cfg")):
+        key = line.split("=")[0].strip()
+        if key in ("output", "dosfile", "qpifile"):
+            continue
+        lines.append(line.rstrip("\n").replace('wffile="ref_wf.idl";', 'wffile="ours_wf.idl";'))
+    lines.append("output=nomode;")
+    (tmp_path / "input.cfg").write_text("\n".join(lines) + "\n")
+    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    hw, dw = F.read_idl(str(tmp_path / "ours_wf.idl"))
+    hr, dr = F.read_idl(os.path.join(src, "ref_wf.idl"))
+    for key in ("name", "size", "scan_range", "offset", "bias", "setpoint"):
+        assert hw[key] == hr[key], (key, hw[key], hr[key])
+    assert np.abs(dw - dr).max() <= 1e-7 * max(np.abs(dr).max(), 1e-30)
