@@ -82,7 +82,7 @@ extern "C" {
 int cqpi_band_histogram(const cqpi_model *m, int32_t pix, int32_t oversamp, double le, double ue, int32_t layers,
                         double *out)
 {
-    if (!m || !out || pix < 1 || oversamp < 1 || layers < 1 || m->bands < 1 || m->nhops < 0 ||
+    if (!m || !out || pix < 1 || oversamp < 1 || layers < 1 || !(ue > le) || m->bands < 1 || m->nhops < 0 ||
         (m->nhops > 0 && (!m->R || !m->orb || !m->t)))
         return CQPI_ERR_ARG;
     for (int64_t h = 0; h < m->nhops; h++)
@@ -92,7 +92,8 @@ int cqpi_band_histogram(const cqpi_model *m, int32_t pix, int32_t oversamp, doub
     const long long ospix = (long long)pix * oversamp;
     const size_t plane = (size_t)pix * pix;
     std::fill(out, out + plane * (size_t)layers, 0.0);
-    const double bin = (ue - le) / (layers - 1.0);
+    // one layer: every eigenvalue counts, into that layer (the reference's bin is infinite then)
+    const double bin = layers > 1 ? (ue - le) / (layers - 1.0) : INFINITY;
     const double w = (ue - le) / layers * 2.0;
     auto lorentz = [w](double x) { return w / 2.0 / (x * x + w * w / 4.0) / M_PI; };
     auto layer_energy = [&](int l) { return layers == 1 ? le : (ue - le) * l / (layers - 1.0) + le; };
@@ -118,7 +119,7 @@ int cqpi_band_histogram(const cqpi_model *m, int32_t pix, int32_t oversamp, doub
                     for (int l = 0; l < b; l++) {
                         const double e = ev[l];
                         if (!(e > le - 2.0 * bin && e < ue + 2.0 * bin)) continue;
-                        const int lay = (int)std::round((e - le) / (ue - le) * (layers - 1.0));
+                        const int lay = layers > 1 ? (int)std::round((e - le) / (ue - le) * (layers - 1.0)) : 0;
                         for (int nl = lay - 1; nl <= lay + 1; nl++)
                             if (nl >= 0 && nl < layers)
                                 out[(size_t)nl * plane + (size_t)j * pix + (size_t)i] += lorentz(layer_energy(nl) - e);

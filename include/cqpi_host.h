@@ -102,7 +102,8 @@ int cqpi_interp_eval(const char *method, int32_t n, const double *xa, const doub
  * Lorentzian of width 2 (ue - le) / layers to the three nearest of the layers energies
  * le .. ue in pixel (io / oversamp, jo / oversamp).  out[layers][pix][pix] (x fastest, the
  * IDL order of idl(pix, pix, layers, 1, 1, le, ue, 0, -0.5, -0.5)).  CPU only, on all host
- * cores, as the reference computes it. */
+ * cores, as the reference computes it.  CQPI_ERR_ARG unless ue > le, pix, oversamp and layers
+ * are positive and the model's orbital indices lie inside its bands. */
 int cqpi_band_histogram(const cqpi_model *m, int32_t pix, int32_t oversamp, double le, double ue, int32_t layers,
                         double *out);
 

@@ -127,3 +127,13 @@ def test_cli_wffile_matches_reference_without_gpu(built_lib, tmp_path, name):
     for key in ("name", "size", "scan_range", "offset", "bias", "setpoint"):
         assert hw[key] == hr[key], (key, hw[key], hr[key])
     assert np.abs(dw - dr).max() <= 1e-7 * max(np.abs(dr).max(), 1e-30)
+
+
+def test_cli_bsfile_rejects_an_empty_energy_range(built_lib, tmp_path):
+    src = os.path.join(GOLDEN, "bs_t2g")
+    for f in ("model_hr.dat", "input.cfg"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    cfg = (tmp_path / "input.cfg").read_text().replace("bsenergies=(-0.6,0.4);", "bsenergies=(0.4,-0.6);")
+    (tmp_path / "input.cfg").write_text(cfg)
+    r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and "band-structure histogram" in r.stdout
