@@ -58,7 +58,8 @@ def _run_parallel(cmds, verbose=False):
 
 def build_lib(verbose=False, extra_flags=()) -> str:
     os.makedirs(OBJ, exist_ok=True)
-    headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    headers = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+               glob.glob(os.path.join(INCLUDE, "*.h")))
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     objs, cmds = [], []
     for s in srcs:

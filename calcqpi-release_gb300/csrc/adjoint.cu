@@ -370,102 +370,20 @@ __global__ void __launch_bounds__(256) adj_rows_kernel(int kp, int logkp, int NB
 }
 
 // ------------------------------------------------------------------ 5. per-k resolvent
-// C(k) += F* (U^H Gbar(k) U) F*, F = diag(1/(omega + i eta - eps_n)); one thread per k
-// C: the working precision (double2, or float2 for the mixed handle: eigenvectors and Gbar(k)
-// in FP32, the pole factors from the FP64 eigenvalues, C(k) accumulated in FP64)
-template <int B, class C>
-__global__ void __launch_bounds__(128) adj_kacc_kernel(int b, long long nk, double omega, double eta,
-                                                       const double *__restrict__ eval, const C *__restrict__ evec,
-                                                       const C *__restrict__ gk, double2 *__restrict__ Cacc)
-{
-    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk) return;
-    C U[B][B], G[B][B], X[B][B], f[B];
-#pragma unroll
-    for (int n = 0; n < B; n++) {
-        if (n < b) {
-            const double dr = omega - eval[(size_t)n * nk + k];
-            const double den = dr * dr + eta * eta;
-            f[n] = cmake<C>(dr / den, eta / den);   // conj(1/(dr + i eta))
-        }
-    }
-#pragma unroll
-    for (int o = 0; o < B; o++)
-#pragma unroll
-        for (int n = 0; n < B; n++)
-            if (o < b && n < b) {
-                U[o][n] = evec[(size_t)(o * b + n) * nk + k];
-                G[o][n] = gk[(size_t)(o * b + n) * nk + k];
-            }
-    // X = Gbar U
-#pragma unroll
-    for (int o = 0; o < B; o++)
-#pragma unroll
-        for (int m = 0; m < B; m++) {
-            if (o >= b || m >= b) continue;
-            C s = cmake<C>(0.0, 0.0);
-#pragma unroll
-            for (int a = 0; a < B; a++)
-                if (a < b) s = cadd(s, cmul(G[o][a], U[a][m]));
-            X[o][m] = s;
-        }
-    // C += f*_n (U^H X)_nm f*_m
-#pragma unroll
-    for (int n = 0; n < B; n++)
-#pragma unroll
-        for (int m = 0; m < B; m++) {
-            if (n >= b || m >= b) continue;
-            C s = cmake<C>(0.0, 0.0);
-#pragma unroll
-            for (int o = 0; o < B; o++)
-                if (o < b) {
-                    C un = U[o][n];
-                    un.y = -un.y;
-                    s = cadd(s, cmul(un, X[o][m]));
-                }
-            s = cmul(cmul(f[n], s), f[m]);
-            double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
-            *c = cadd(*c, to_d2(s));
-        }
-}
-
-// Hbar(k) = U C(k) U^H, written over gk
-template <int B>
-__global__ void __launch_bounds__(128) adj_hbar_kernel(int b, long long nk, const double2 *__restrict__ evec,
-                                                       const double2 *__restrict__ Cacc, double2 *__restrict__ hbar)
-{
-    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk) return;
-    double2 U[B][B], X[B][B];
-#pragma unroll
-    for (int o = 0; o < B; o++)
-#pragma unroll
-        for (int n = 0; n < B; n++)
-            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
-    // X = U C
-#pragma unroll
-    for (int o = 0; o < B; o++)
-#pragma unroll
-        for (int m = 0; m < B; m++) {
-            if (o >= b || m >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
-#pragma unroll
-            for (int n = 0; n < B; n++)
-                if (n < b) s = cadd(s, cmul(U[o][n], Cacc[(size_t)(n * b + m) * nk + k]));
-            X[o][m] = s;
-        }
-#pragma unroll
-    for (int o = 0; o < B; o++)
-#pragma unroll
-        for (int a = 0; a < B; a++) {
-            if (o >= b || a >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
-#pragma unroll
-            for (int m = 0; m < B; m++)
-                if (m < b) s = cadd(s, cmul(X[o][m], cconj(U[a][m])));
-            hbar[(size_t)(o * b + a) * nk + k] = s;
-        }
-}
+#define CQPI_ADJ_KACC adj_kacc_kernel
+#define CQPI_ADJ_HBAR adj_hbar_kernel
+#define CQPI_ADJ_UNROLL _Pragma("unroll")
+#include "adjoint_kspace.cuh"
+#undef CQPI_ADJ_KACC
+#undef CQPI_ADJ_HBAR
+#undef CQPI_ADJ_UNROLL
+#define CQPI_ADJ_KACC adj_kacc_kernel_wide
+#define CQPI_ADJ_HBAR adj_hbar_kernel_wide
+#define CQPI_ADJ_UNROLL _Pragma("unroll 1")
+#include "adjoint_kspace.cuh"
+#undef CQPI_ADJ_KACC
+#undef CQPI_ADJ_HBAR
+#undef CQPI_ADJ_UNROLL
 
 // ------------------------------------------------------------------ 6. hoppings
 // grid (nR, chunks); out[r][0][pq] = sum_k e^{-i th_r(k)} Hbar(k)[pq] (normal terms),
@@ -564,12 +482,23 @@ template <int B>
 static void launch_kacc_t(cqpi_handle *h, double omega, AdjWorkspace &aw)
 {
     const long long nk = (long long)h->kp * h->kp;
-    if (h->precision == CQPI_PREC_FP64)
-        adj_kacc_kernel<B, double2><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec,
-                                                                         aw.gk, aw.C);
-    else
-        adj_kacc_kernel<B, float2><<<cdiv(nk, 128), 128, 0, h->stream>>>(
-            h->b, nk, omega, h->eta, h->d_eval, h->d_evec32, reinterpret_cast<const float2 *>(aw.gk), aw.C);
+    const unsigned grid = (unsigned)cdiv(nk, 128);
+    const float2 *gk32 = reinterpret_cast<const float2 *>(aw.gk);
+    if constexpr (B <= 6) {
+        if (h->precision == CQPI_PREC_FP64)
+            adj_kacc_kernel<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec,
+                                                                     aw.gk, aw.C);
+        else
+            adj_kacc_kernel<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec32,
+                                                                    gk32, aw.C);
+    } else {
+        if (h->precision == CQPI_PREC_FP64)
+            adj_kacc_kernel_wide<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval,
+                                                                          h->d_evec, aw.gk, aw.C);
+        else
+            adj_kacc_kernel_wide<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval,
+                                                                         h->d_evec32, gk32, aw.C);
+    }
     h->launches++;
 }
 
@@ -608,7 +537,10 @@ template <int B>
 static void launch_hbar_t(cqpi_handle *h, AdjWorkspace &aw)
 {
     const long long nk = (long long)h->kp * h->kp;
-    adj_hbar_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
+    if constexpr (B <= 6)
+        adj_hbar_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
+    else
+        adj_hbar_kernel_wide<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
     h->launches++;
 }
 

@@ -1,0 +1,103 @@
+// adjoint_kspace.cuh -- the per-k kernels of the adjoint's step 5 (the resolvent bracket
+// C(k) and Hbar(k) = U C(k) U^H), included twice by adjoint.cu: with full unrolling of their
+// b x b loop nests for up to 6 bands (adj_kacc_kernel, adj_hbar_kernel) and with the loops kept
+// for 8 to 16 bands (adj_kacc_kernel_wide, adj_hbar_kernel_wide), whose matrices live in local
+// memory either way.  The includer defines CQPI_ADJ_KACC, CQPI_ADJ_HBAR (the kernels' names)
+// and CQPI_ADJ_UNROLL (the loop pragma).
+// C(k) += F* (U^H Gbar(k) U) F*, F = diag(1/(omega + i eta - eps_n)); one thread per k
+// C: the working precision (double2, or float2 for the mixed handle: eigenvectors and Gbar(k)
+// in FP32, the pole factors from the FP64 eigenvalues, C(k) accumulated in FP64)
+template <int B, class C>
+__global__ void __launch_bounds__(128) CQPI_ADJ_KACC(int b, long long nk, double omega, double eta,
+                                                       const double *__restrict__ eval, const C *__restrict__ evec,
+                                                       const C *__restrict__ gk, double2 *__restrict__ Cacc)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    C U[B][B], G[B][B], X[B][B], f[B];
+CQPI_ADJ_UNROLL
+    for (int n = 0; n < B; n++) {
+        if (n < b) {
+            const double dr = omega - eval[(size_t)n * nk + k];
+            const double den = dr * dr + eta * eta;
+            f[n] = cmake<C>(dr / den, eta / den);   // conj(1/(dr + i eta))
+        }
+    }
+CQPI_ADJ_UNROLL
+    for (int o = 0; o < B; o++)
+CQPI_ADJ_UNROLL
+        for (int n = 0; n < B; n++)
+            if (o < b && n < b) {
+                U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+                G[o][n] = gk[(size_t)(o * b + n) * nk + k];
+            }
+    // X = Gbar U
+CQPI_ADJ_UNROLL
+    for (int o = 0; o < B; o++)
+CQPI_ADJ_UNROLL
+        for (int m = 0; m < B; m++) {
+            if (o >= b || m >= b) continue;
+            C s = cmake<C>(0.0, 0.0);
+CQPI_ADJ_UNROLL
+            for (int a = 0; a < B; a++)
+                if (a < b) s = cadd(s, cmul(G[o][a], U[a][m]));
+            X[o][m] = s;
+        }
+    // C += f*_n (U^H X)_nm f*_m
+CQPI_ADJ_UNROLL
+    for (int n = 0; n < B; n++)
+CQPI_ADJ_UNROLL
+        for (int m = 0; m < B; m++) {
+            if (n >= b || m >= b) continue;
+            C s = cmake<C>(0.0, 0.0);
+CQPI_ADJ_UNROLL
+            for (int o = 0; o < B; o++)
+                if (o < b) {
+                    C un = U[o][n];
+                    un.y = -un.y;
+                    s = cadd(s, cmul(un, X[o][m]));
+                }
+            s = cmul(cmul(f[n], s), f[m]);
+            double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
+            *c = cadd(*c, to_d2(s));
+        }
+}
+
+// Hbar(k) = U C(k) U^H, written over gk
+template <int B>
+__global__ void __launch_bounds__(128) CQPI_ADJ_HBAR(int b, long long nk, const double2 *__restrict__ evec,
+                                                       const double2 *__restrict__ Cacc, double2 *__restrict__ hbar)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    double2 U[B][B], X[B][B];
+CQPI_ADJ_UNROLL
+    for (int o = 0; o < B; o++)
+CQPI_ADJ_UNROLL
+        for (int n = 0; n < B; n++)
+            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+    // X = U C
+CQPI_ADJ_UNROLL
+    for (int o = 0; o < B; o++)
+CQPI_ADJ_UNROLL
+        for (int m = 0; m < B; m++) {
+            if (o >= b || m >= b) continue;
+            double2 s = make_double2(0.0, 0.0);
+CQPI_ADJ_UNROLL
+            for (int n = 0; n < B; n++)
+                if (n < b) s = cadd(s, cmul(U[o][n], Cacc[(size_t)(n * b + m) * nk + k]));
+            X[o][m] = s;
+        }
+CQPI_ADJ_UNROLL
+    for (int o = 0; o < B; o++)
+CQPI_ADJ_UNROLL
+        for (int a = 0; a < B; a++) {
+            if (o >= b || a >= b) continue;
+            double2 s = make_double2(0.0, 0.0);
+CQPI_ADJ_UNROLL
+            for (int m = 0; m < B; m++)
+                if (m < b) s = cadd(s, cmul(X[o][m], cconj(U[a][m])));
+            hbar[(size_t)(o * b + a) * nk + k] = s;
+        }
+}
+
