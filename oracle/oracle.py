@@ -245,6 +245,44 @@ def spf(g0k: np.ndarray, maxband: int, shift: bool = True) -> np.ndarray:
     return tr[np.ix_(idx, idx)]
 
 
+def band_histogram(model: "Model", pix: int, oversamp: int, le: float, ue: float, layers: int) -> np.ndarray:
+    """tightbind::calcbst3dhisthr(fname, pix, le, ue, layers, oversamp),
+    src/tightbinding.cc:1158-1193 (the driver's bsfile, src/calcqpi.cc:308-326): eigenvalues
+    (numpy.linalg.eigvalsh on the lower triangle, as gsl_eigen_hermv reads it) of H(k) with the
+    Fermi-energy diagonal (tightbind::setmatrix, src/tightbinding.cc:210-219; all terms at
+    k_z = 0) on the (pix*oversamp)^2 grid k = (io, jo) / (pix*oversamp - 1) - 1/2; each
+    eigenvalue within two bins of [le, ue] adds the Lorentzian of width w = 2 (ue - le) / layers
+    (class lorentzian, src/tightbinding.h:42-49) at the layer energies (idl::getbias) to the
+    nearest layer and its two neighbours (idl::getbiasindex) of pixel (io/oversamp,
+    jo/oversamp).  Returns [layers][y][x]."""
+    b = model.bands
+    R = np.asarray(model.R).reshape(-1, 3)
+    orb = np.asarray(model.orb).reshape(-1, 2)
+    t = np.asarray(model.t, np.complex128).reshape(-1)
+    anti = np.asarray(model.anti if model.anti is not None else np.zeros(len(t)), bool).reshape(-1)
+    scmax = model.scmaxbands if model.scmaxbands is not None else b
+    osp = pix * oversamp
+    out = np.zeros((layers, pix, pix))
+    binsize = (ue - le) / (layers - 1) if layers > 1 else np.inf
+    w = (ue - le) / layers * 2.0
+    diag = np.array([-model.efermi if d < scmax else model.efermi for d in range(b)], np.complex128)
+    for io in range(osp):
+        for jo in range(osp):
+            kx, ky = io / (osp - 1) - 0.5, jo / (osp - 1) - 0.5
+            H = np.diag(diag)
+            ph = 2 * np.pi * (R[:, 0] * kx + R[:, 1] * ky)
+            np.add.at(H, (orb[:, 0], orb[:, 1]), t * np.exp(1j * np.where(anti, -ph, ph)))
+            for e in np.linalg.eigvalsh(H, UPLO="L"):
+                if not (le - 2 * binsize < e < ue + 2 * binsize):
+                    continue
+                lay = int(np.round((e - le) / (ue - le) * (layers - 1))) if layers > 1 else 0
+                for nl in (lay - 1, lay, lay + 1):
+                    if 0 <= nl < layers:
+                        x = ((ue - le) * nl / (layers - 1) + le if layers > 1 else le) - e
+                        out[nl, jo // oversamp, io // oversamp] += w / 2 / (x * x + w * w / 4) / np.pi
+    return out
+
+
 def uspf(g0k: np.ndarray, n: int, maxband: int, pos, prearr, spin: bool = False) -> np.ndarray:
     """tmatrix::calcuspf, src/qpi.cc:735-775: the spectral function unfolded with the orbital
     positions, ldos[i][j] = -sum_{k,l} pre_k pre_l Im(G0(ki,kj)[l][k] e^{2 pi i (kx dx + ky dy)}),

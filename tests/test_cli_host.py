@@ -5,7 +5,7 @@ own outputs:
     as the reference's driver computes it): tests/golden/bs_*/ from tightbind::calcbst3dhisthr
     (src/tightbinding.cc:1158-1193) through the reference CLI (a 3-band model with a Fermi
     energy, a BdG model with conjugated hole terms, a layered model with R_z != 0 terms), and
-    a NumPy restatement;
+    the oracle's restatement (oracle.band_histogram), itself pinned on those outputs;
   * the orbital setup and wffile output of every golden case that has one (analytic, IDL and
     XSF orbitals, padding, spin duplication).
 """
@@ -44,35 +44,39 @@ def test_cli_bsfile_matches_reference(built_lib, tmp_path, case):
     assert np.abs(ours.astype(np.float64) - ref).max() <= 1e-6 * np.abs(ref).max()
 
 
-def _restated_histogram(model, pix, os_, le, ue, layers, efermi, scmax):
-    """NumPy restatement (numpy.linalg.eigvalsh on the lower triangle)."""
-    b = model["bands"]
-    R, orb, t, anti = model["R"], model["orb"], model["t"], model["anti"]
-    osp = pix * os_
-    out = np.zeros((layers, pix, pix))
-    binsize = (ue - le) / (layers - 1)
-    w = (ue - le) / layers * 2.0
-    for io in range(osp):
-        for jo in range(osp):
-            kx, ky = io / (osp - 1) - 0.5, jo / (osp - 1) - 0.5
-            H = np.diag([-efermi if d < scmax else efermi for d in range(b)]).astype(complex)
-            ph = 2 * np.pi * (R[:, 0] * kx + R[:, 1] * ky)
-            ph = np.where(anti.astype(bool), -ph, ph)
-            np.add.at(H, (orb[:, 0], orb[:, 1]), (t[:, 0] + 1j * t[:, 1]) * np.exp(1j * ph))
-            for e in np.linalg.eigvalsh(H, UPLO="L"):
-                if not (le - 2 * binsize < e < ue + 2 * binsize):
-                    continue
-                lay = int(np.round((e - le) / (ue - le) * (layers - 1)))
-                for nl in (lay - 1, lay, lay + 1):
-                    if 0 <= nl < layers:
-                        x = (ue - le) * nl / (layers - 1) + le - e
-                        out[nl, jo // os_, io // os_] += w / 2 / (x * x + w * w / 4) / np.pi
-    return out
+def _oracle_model(case, scmodel, efermi):
+    from oracle import oracle as O
+    with open(os.path.join(GOLDEN, case, "model_hr.dat")) as fh:
+        hr = F.read_hr(fh.read(), scmodel=scmodel)
+    return O.Model.from_hr(hr, efermi=efermi)
 
 
-def test_band_histogram_matches_numpy_restatement(built_lib):
-    from cqpi import host
-    hr = host.read_hr(os.path.join(GOLDEN, "bs_bdg", "model_hr.dat"), scmodel=True)
+def _bs_keys(case):
+    """(pix, oversamp, le, ue, layers, scmodel, efermi) of a golden case's input.cfg."""
+    kv = {}
+    for line in open(os.path.join(GOLDEN, case, "input.cfg")):
+        if "=" in line and not line.startswith("#"):
+            k, v = line.split("=", 1)
+            kv[k.strip()] = v.strip().rstrip(";")
+    le, ue = (float(x) for x in kv["bsenergies"].strip("()").split(","))
+    return (int(kv["bslattice"]), int(kv["bsoversamp"]), le, ue, int(kv["bslayers"]),
+            kv.get("scmodel") == "true", float(kv.get("fermi", 0.0)))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_histogram_matches_reference(case):
+    """Pins the oracle's restatement (oracle.band_histogram) on the reference's outputs."""
+    from oracle import oracle as O
+    pix, os_, le, ue, layers, scmodel, efermi = _bs_keys(case)
+    got = O.band_histogram(_oracle_model(case, scmodel, efermi), pix, os_, le, ue, layers)
+    _, ref = F.read_idl(os.path.join(GOLDEN, case, "ref_bs.idl"))
+    assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+def test_band_histogram_matches_oracle(built_lib):
+    """cqpi_band_histogram against the oracle on a model and range no golden uses."""
+    from oracle import oracle as O
+    om = _oracle_model("bs_bdg", True, 0.02)
     lib = ctypes.CDLL(built_lib["lib"])
 
     class Model(ctypes.Structure):
@@ -80,20 +84,15 @@ def test_band_histogram_matches_numpy_restatement(built_lib):
                     ("nhops", ctypes.c_int64), ("R", ctypes.c_void_p), ("orb", ctypes.c_void_p),
                     ("t", ctypes.c_void_p), ("anti", ctypes.c_void_p)]
 
-    R = np.ascontiguousarray(hr["R"], np.int32)
-    orb = np.ascontiguousarray(hr["orb"], np.int32)
-    t = np.ascontiguousarray(np.stack([hr["t"].real, hr["t"].imag], -1), np.float64)
-    anti = np.ascontiguousarray(hr["anti"], np.uint8)
-    efermi = 0.02
-    m = Model(hr["bands"], hr["scmaxbands"], efermi, len(anti), R.ctypes.data, orb.ctypes.data, t.ctypes.data,
-              anti.ctypes.data)
+    t = np.ascontiguousarray(np.stack([om.t.real, om.t.imag], -1))
+    m = Model(om.bands, om.scmaxbands, om.efermi, len(om.t), om.R.ctypes.data, om.orb.ctypes.data, t.ctypes.data,
+              om.anti.ctypes.data)
     pix, os_, le, ue, layers = 6, 3, -0.3, 0.3, 9
     out = np.zeros((layers, pix, pix))
     lib.cqpi_band_histogram.argtypes = [ctypes.POINTER(Model), ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int32, ctypes.c_void_p]
     assert lib.cqpi_band_histogram(ctypes.byref(m), pix, os_, le, ue, layers, out.ctypes.data) == 0
-    want = _restated_histogram(dict(bands=hr["bands"], R=R, orb=orb, t=t, anti=anti), pix, os_, le, ue, layers,
-                               efermi, hr["scmaxbands"])
+    want = O.band_histogram(om, pix, os_, le, ue, layers)
     assert np.abs(want).max() > 0
     np.testing.assert_allclose(out, want, rtol=1e-10, atol=1e-12 * np.abs(want).max())
 
