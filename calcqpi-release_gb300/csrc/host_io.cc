@@ -28,7 +28,8 @@
 
 namespace {
 
-std::string g_host_err;
+// per calling thread, so that host calls from several threads each read their own message
+thread_local std::string g_host_err;
 
 int host_fail(int code, const std::string &m)
 {

@@ -134,6 +134,8 @@ int cqpi_idl_write_layers(const char *path, int32_t k0, int32_t nk, const float 
 int cqpi_idl_read_header(const char *path, cqpi_idl_header *hdr);
 int cqpi_idl_read(const char *path, float *data, int64_t count);
 
+/* The message of the last failing host call made by the calling thread (valid until that
+ * thread's next failing host call). */
 const char *cqpi_host_last_error(void);
 
 #ifdef __cplusplus
