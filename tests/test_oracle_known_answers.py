@@ -8,6 +8,7 @@
   * V = 0: T = 0 and the map is the term-1 tile of one unit cell repeated over the field of
     view (tmatrix::calcwannierldos, src/qpi.cc:876-950);
   * reciprocity with real hoppings: G0(R)[a][o] = G0(-R)[o][a];
+  * the surface / bulk decimation on a semi-infinite chain: the closed forms;
   * a C4v model with a centred impurity and an s-like orbital: the map is symmetric under
     x <-> y, inversion and 90-degree rotation about the impurity pixel (inside the field of
     view; the wrapped outermost pixel row has no partner).
@@ -82,3 +83,21 @@ def test_c4v_symmetry_about_the_impurity(c1_maps):
     sub = mp[np.ix_(idx, idx)]
     assert np.abs(sub - sub[::-1, ::-1]).max() <= tol
     assert np.abs(sub - np.rot90(sub)).max() <= tol
+
+
+@pytest.mark.parametrize("w,eta", [(0.7, 0.05), (2.5, 0.05), (-1.3, 0.2)])
+def test_semi_infinite_chain_surface_and_bulk_green_functions(w, eta):
+    """Only inter-layer hopping t: every k-point is a semi-infinite chain, whose surface and
+    bulk Green's functions are (z - sqrt(z^2 - 4t^2)) / (2t^2) and 1 / sqrt(z^2 - 4t^2), the
+    roots with Im G < 0 (the decimation of tmatrix::calcsurfacegreensfunction,
+    src/qpi.cc:488-554)."""
+    t = -1.0
+    m = O.Model(1, [[0, 0, 1], [0, 0, -1]], [[0, 0], [0, 0]], [t, t])
+    z = w + 1j * eta
+    r = np.sqrt(z * z - 4 * t * t)
+    surf = [g for g in ((z - r) / (2 * t * t), (z + r) / (2 * t * t)) if g.imag < 0][0]
+    bulk = [g for g in (1 / r, -1 / r) if g.imag < 0][0]
+    gs = O.surface_greens_k(m, 4, w, eta, 1e-12, True)
+    gb = O.surface_greens_k(m, 4, w, eta, 1e-12, False)
+    assert np.abs(gs - surf).max() <= 1e-12 * abs(surf)
+    assert np.abs(gb - bulk).max() <= 1e-12 * abs(bulk)
