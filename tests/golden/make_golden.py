@@ -360,7 +360,7 @@ def make_case(name, c):
         cubes = []
         for i, nm in enumerate(names):
             # pos[i] lines (orbital spec, or the uspf band positions) also place the orbitals
-            pos = tuple(dict(c.get("pos", {}), **spec.get("pos", {})).get(i, (0.0, 0.0, 0.0)))
+            pos = tuple({**c.get("pos", {}), **spec.get("pos", {})}.get(i, (0.0, 0.0, 0.0)))
             pos = pos + (0.0,) * (3 - len(pos))
             pre = spec.get("prearr", (1.0,) * len(names))[i] if i < len(spec.get("prearr", ())) else 1.0
             cubes.append(O.orbital_cache(nm, w, os_, width=spec["radius"], height=spec["zheight"] - pos[2],
@@ -573,10 +573,31 @@ def make_bs_case(name, c):
     print("golden", name)
 
 
+# ------------------------------------------------------------------ keywords
+def write_keywords():
+    """The input keywords the reference's programs read (loadconfig::probefield with a literal
+    name in src/calcqpi.cc and src/mkwavefunctions.cc), one per line, for the keyword
+    coverage test of the CLI and the orbital-file tool."""
+    import re
+    root = os.environ.get("CQPI_REFERENCE", "/root/reference")
+    for prog in ("calcqpi", "mkwavefunctions"):
+        with open(os.path.join(root, "src", prog + ".cc")) as fh:
+            names = sorted(set(re.findall(r'probefield\("([^"]+)"\)', fh.read())))
+        with open(os.path.join(HERE, "ref_%s_keywords.txt" % prog), "w") as fh:
+            fh.write("# keywords read by src/%s.cc (generated by tests/golden/make_golden.py)\n" % prog)
+            fh.write("\n".join(names) + "\n")
+        print("keywords", prog, len(names))
+
+
 if __name__ == "__main__":
     if not os.path.exists(os.path.join(REF, "mkwavefunctions")):
         subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
-    for nm in (sys.argv[1:] or list(CASES) + list(MKWF_CASES) + list(BS_CASES)):
+    names = [a for a in sys.argv[1:] if a != "keywords"]
+    if not sys.argv[1:] or "keywords" in sys.argv[1:]:
+        write_keywords()
+    if not sys.argv[1:]:
+        names = list(CASES) + list(MKWF_CASES) + list(BS_CASES)
+    for nm in names:
         if nm in MKWF_CASES:
             make_mkwf_case(nm, MKWF_CASES[nm])
         elif nm in BS_CASES:

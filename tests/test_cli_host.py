@@ -136,3 +136,26 @@ def test_cli_bsfile_rejects_an_empty_energy_range(built_lib, tmp_path):
     (tmp_path / "input.cfg").write_text(cfg)
     r = subprocess.run([built_lib["cli"], "input.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode == 1 and "band-structure histogram" in r.stdout
+
+
+def _ref_keywords(prog):
+    with open(os.path.join(GOLDEN, "ref_%s_keywords.txt" % prog)) as fh:
+        return {l.strip() for l in fh if l.strip() and not l.startswith("#")}
+
+
+def _read_keywords(source):
+    """Keys our program looks up (InputFile::has / field / str / value / ivalue / vec / list /
+    strlist with a literal name)."""
+    import re
+    with open(source) as fh:
+        return set(re.findall(r'lf\.(?:has|field|str|value|ivalue|vec|list|strlist)\("([^"]+)"\)', fh.read()))
+
+
+@pytest.mark.parametrize("prog,source", [("calcqpi", "calcqpi_main.cc"),
+                                         ("mkwavefunctions", "mkwavefunctions_main.cc")])
+def test_every_reference_keyword_is_read(prog, source):
+    """Every keyword the reference's program reads (tests/golden/ref_<prog>_keywords.txt, taken
+    from its sources) is read by ours: a reference input file loses nothing."""
+    ours = _read_keywords(os.path.join(os.path.dirname(HERE), "calcqpi-release_gb300", "host", source))
+    missing = sorted(_ref_keywords(prog) - ours)
+    assert not missing, missing
