@@ -44,6 +44,8 @@ def _lib():
                                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P]
         L.cqpi_xsf_orbital_cache_mod.argtypes = [ctypes.c_char_p, P, P] + [ctypes.c_double] * 5 + [ctypes.c_int32,
                                                                                                  ctypes.c_int32, P]
+        L.cqpi_band_histogram.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_int32, P]
         L.cqpi_interp_known.argtypes = [ctypes.c_char_p]
         L.cqpi_interp_eval.argtypes = [ctypes.c_char_p, ctypes.c_int32, P, P, ctypes.c_int32, P, P]
         L.cqpi_host_last_error.restype = ctypes.c_char_p
@@ -174,6 +176,30 @@ def interp_eval(method, xa, ya, x) -> np.ndarray:
         raise HostError(f"status {rc}: interpolation '{method}' rejected its input (method, point count, "
                         "increasing x values, x inside the data range)")
     return y
+
+
+def band_histogram(model, pix, oversamp, le, ue, layers) -> np.ndarray:
+    """The bsfile band-structure histogram [layers][pix][pix] of a model with fields bands, R,
+    orb, t (complex), anti and optionally efermi, scmaxbands (cqpi.workloads.TBModel, the
+    oracle's Model, or the dict of read_hr)."""
+    from . import _Model
+    L = _lib()
+    get = (lambda k, d=None: model.get(k, d)) if isinstance(model, dict) else (lambda k, d=None: getattr(model, k, d))
+    bands = int(get("bands"))
+    R = np.ascontiguousarray(np.asarray(get("R")).reshape(-1, 3), np.int32)
+    orb = np.ascontiguousarray(np.asarray(get("orb")).reshape(-1, 2), np.int32)
+    tc = np.asarray(get("t"), np.complex128).reshape(-1)
+    t = np.ascontiguousarray(np.stack([tc.real, tc.imag], -1), np.float64)
+    anti_v = get("anti")
+    anti = np.ascontiguousarray(np.zeros(len(tc)) if anti_v is None else np.asarray(anti_v).reshape(-1), np.uint8)
+    scmax = get("scmaxbands")
+    m = _Model(bands, bands if scmax is None else int(scmax), float(get("efermi", 0.0) or 0.0), len(tc),
+               R.ctypes.data, orb.ctypes.data, t.ctypes.data, anti.ctypes.data)
+    out = np.empty((layers, pix, pix), np.float64)
+    rc = L.cqpi_band_histogram(ctypes.addressof(m), pix, oversamp, le, ue, layers, _ptr(out))
+    if rc:
+        raise HostError(f"status {rc}: invalid band-structure histogram arguments")
+    return out
 
 
 def idl_write(path, data_kyx, name, scan_range=(2.0, 2.0), offset=(-1.0, -1.0), bias=(0.0, 0.0), setpoint=0.0,

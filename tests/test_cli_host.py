@@ -9,7 +9,6 @@ own outputs:
   * the orbital setup and wffile output of every golden case that has one (analytic, IDL and
     XSF orbitals, padding, spin duplication).
 """
-import ctypes
 import glob
 import os
 import shutil
@@ -77,21 +76,9 @@ def test_band_histogram_matches_oracle(built_lib):
     """cqpi_band_histogram against the oracle on a model and range no golden uses."""
     from oracle import oracle as O
     om = _oracle_model("bs_bdg", True, 0.02)
-    lib = ctypes.CDLL(built_lib["lib"])
-
-    class Model(ctypes.Structure):
-        _fields_ = [("bands", ctypes.c_int32), ("scmaxbands", ctypes.c_int32), ("efermi", ctypes.c_double),
-                    ("nhops", ctypes.c_int64), ("R", ctypes.c_void_p), ("orb", ctypes.c_void_p),
-                    ("t", ctypes.c_void_p), ("anti", ctypes.c_void_p)]
-
-    t = np.ascontiguousarray(np.stack([om.t.real, om.t.imag], -1))
-    m = Model(om.bands, om.scmaxbands, om.efermi, len(om.t), om.R.ctypes.data, om.orb.ctypes.data, t.ctypes.data,
-              om.anti.ctypes.data)
+    from cqpi import host
     pix, os_, le, ue, layers = 6, 3, -0.3, 0.3, 9
-    out = np.zeros((layers, pix, pix))
-    lib.cqpi_band_histogram.argtypes = [ctypes.POINTER(Model), ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
-                                        ctypes.c_double, ctypes.c_int32, ctypes.c_void_p]
-    assert lib.cqpi_band_histogram(ctypes.byref(m), pix, os_, le, ue, layers, out.ctypes.data) == 0
+    out = host.band_histogram(om, pix, os_, le, ue, layers)
     want = O.band_histogram(om, pix, os_, le, ue, layers)
     assert np.abs(want).max() > 0
     np.testing.assert_allclose(out, want, rtol=1e-10, atol=1e-12 * np.abs(want).max())
