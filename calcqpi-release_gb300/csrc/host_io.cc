@@ -254,7 +254,8 @@ int cqpi_idl_write(const char *path, const char *name, const char *date, int32_t
                    const double *scan_range, const double *offset, const double *bias, double setpoint,
                    const float *data)
 {
-    if (!path || sx < 0 || sy < 0 || sz < 0 || (!data && (size_t)sx * sy * sz)) return host_fail(CQPI_ERR_ARG, "invalid IDL arguments");
+    if (!path || sx < 0 || sy < 0 || sz < 0 || (!data && (size_t)sx * sy * sz != 0))
+        return host_fail(CQPI_ERR_ARG, "invalid IDL arguments");
     std::ofstream os(path, std::ios::binary);
     if (!os) return host_fail(CQPI_ERR_ARG, std::string("error while opening file ") + path + " for writing");
     idl_header(os, name, date, sx, sy, sz, scan_range, offset, bias, setpoint);
