@@ -206,7 +206,7 @@ CQPI_BANDS_UNROLL
             for (int q = p + 1; q < B; q++) {
                 const double c2 = ar[p][q] * ar[p][q] + ai[p][q] * ai[p][q];
                 if (c2 == 0.0) continue;
-                const double rc = rsqrt(c2), cab = c2 * rc;
+                const double rc = rsqrt(c2);
                 const double er = ar[p][q] * rc, ei = ai[p][q] * rc;
                 const double tau = (ar[q][q] - ar[p][p]) * (0.5 * rc);
                 const double tt = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
