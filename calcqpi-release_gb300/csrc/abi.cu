@@ -699,7 +699,7 @@ int upload_list(cqpi_handle *h, const std::vector<ListEnt> &ents)
 // of equal non-zero label).
 int build_list(cqpi_handle *h)
 {
-    const int wins = 2 * h->w + 1, os = h->os, xs = os * wins, norb = h->wf_norb, b = h->b;
+    const int wins = 2 * h->w + 1, os = h->os, xs = os * wins, norb = h->wf_norb;
     double maxval = 0.0;
     for (size_t k = 0; k < h->wf_host.size(); k++) maxval = std::max(maxval, h->wf_host[k] * h->wf_host[k]);
     const double thr = h->list_threshold * maxval;
