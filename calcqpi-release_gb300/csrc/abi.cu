@@ -58,6 +58,17 @@ void dfree(T *&p)
     p = nullptr;
 }
 
+// Host -> device copy ordered on the handle's stream (which does not wait for the legacy
+// default stream), complete when it returns, so that the host array may be reused at once and
+// every later kernel on the stream sees the data.
+template <class T>
+void h2d_sync(cqpi_handle *h, T *dst, const T *src, size_t count)
+{
+    if (count == 0) return;
+    CK(cudaMemcpyAsync(dst, src, sizeof(T) * count, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+}
+
 // Keep a device buffer of at least count elements, reallocating only when it must grow
 // (cudaFree synchronises the device; repeated uploads of same-sized data avoid it).
 template <class T>
@@ -684,11 +695,11 @@ int upload_list(cqpi_handle *h, const std::vector<ListEnt> &ents)
     dalloc(&h->d_list_f, f.size());
     dalloc(&h->d_list_f32, f32.size());
     dalloc(&h->d_list_pair, pairs.size());
-    CK(cudaMemcpy(h->d_list_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_u, u.data(), sizeof(int) * u.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_f, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_f32, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_list_pair, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice));
+    h2d_sync(h, h->d_list_off, off.data(), off.size());
+    h2d_sync(h, h->d_list_u, u.data(), u.size());
+    h2d_sync(h, h->d_list_f, f.data(), f.size());
+    h2d_sync(h, h->d_list_f32, f32.data(), f32.size());
+    h2d_sync(h, h->d_list_pair, pairs.data(), pairs.size());
     CK(configure_list(h));
     return CQPI_OK;
 }
@@ -886,9 +897,9 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
         dalloc(&h->d_tn, tn.size());
         dalloc(&h->d_ta, ta.size());
         if (h->nR) {
-            CK(cudaMemcpy(h->d_R, Rv.data(), sizeof(int32_t) * Rv.size(), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(h->d_tn, tn.data(), sizeof(double) * tn.size(), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(h->d_ta, ta.data(), sizeof(double) * ta.size(), cudaMemcpyHostToDevice));
+            h2d_sync(h, h->d_R, Rv.data(), Rv.size());
+            h2d_sync(h, h->d_tn, tn.data(), tn.size());
+            h2d_sync(h, h->d_ta, ta.data(), ta.size());
         }
         upload_pairs(h);
         // twiddles e^{+2 pi i t / kp}
@@ -899,7 +910,7 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
             tw[t] = make_double2(c, s);
         }
         dalloc(&h->d_tw, h->kp);
-        CK(cudaMemcpy(h->d_tw, tw.data(), sizeof(double2) * h->kp, cudaMemcpyHostToDevice));
+        h2d_sync(h, h->d_tw, tw.data(), (size_t)h->kp);
         const size_t nk = (size_t)h->kp * h->kp;
         dalloc(&h->d_eval, nk * b);
         dalloc(&h->d_evec, nk * bb);
@@ -909,16 +920,16 @@ int cqpi_create(const cqpi_model *model, const cqpi_params *p, cqpi_handle **out
             std::vector<float2> tw32(h->kp);
             for (int t = 0; t < h->kp; t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
             dalloc(&h->d_tw32, h->kp);
-            CK(cudaMemcpy(h->d_tw32, tw32.data(), sizeof(float2) * h->kp, cudaMemcpyHostToDevice));
+            h2d_sync(h, h->d_tw32, tw32.data(), (size_t)h->kp);
         }
         dalloc(&h->d_status, 1);
-        CK(cudaMemset(h->d_status, 0, sizeof(int)));
+        CK(cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
         // default scattering: phase (1,0) on every band (src/qpi.h:99)
         h->nimp = 1;
         std::vector<double2> V(bb, make_double2(0.0, 0.0));
         for (int i = 0; i < b; i++) V[(size_t)i * b + i] = make_double2(1.0, 0.0);
         dalloc(&h->d_V, bb);
-        CK(cudaMemcpy(h->d_V, V.data(), sizeof(double2) * bb, cudaMemcpyHostToDevice));
+        h2d_sync(h, h->d_V, V.data(), bb);
         // the transform kernels keep whole rows / column tiles in shared memory
         CK(configure_fft(h));
         // tensor-core contraction for the mixed path (CUDA-core FP32 kernel otherwise);
@@ -1107,7 +1118,7 @@ int cqpi_set_impurities(cqpi_handle *h, const double *V, int32_t nimp)
     try {
         dfree(h->d_V);
         dalloc(&h->d_V, bb * nimp);
-        CK(cudaMemcpy(h->d_V, V, sizeof(double2) * bb * nimp, cudaMemcpyHostToDevice));
+        h2d_sync(h, h->d_V, reinterpret_cast<const double2 *>(V), bb * nimp);
         if (nimp > h->nimp) {
             free_workspace(h);
             free_adj(h);
@@ -1559,13 +1570,15 @@ int cqpi_get_bands(cqpi_handle *h, double *eval, double *evec)
         CK(cudaStreamSynchronize(h->stream));
         if (eval) {
             std::vector<double> t(nk * b);
-            CK(cudaMemcpy(t.data(), h->d_eval, sizeof(double) * t.size(), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(t.data(), h->d_eval, sizeof(double) * t.size(), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
             for (size_t k = 0; k < nk; k++)
                 for (size_t n = 0; n < b; n++) eval[k * b + n] = t[n * nk + k];
         }
         if (evec) {
             std::vector<double2> t(nk * bb);
-            CK(cudaMemcpy(t.data(), h->d_evec, sizeof(double2) * t.size(), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(t.data(), h->d_evec, sizeof(double2) * t.size(), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
             for (size_t k = 0; k < nk; k++)
                 for (size_t e = 0; e < bb; e++) {
                     evec[2 * (k * bb + e)] = t[e * nk + k].x;

@@ -312,12 +312,28 @@ int cqpi_idl_read_header(const char *path, cqpi_idl_header *hdr)
         hdr->bias[0] >> hdr->bias[1] >> hdr->setpoint;
     if (!is) return host_fail(CQPI_ERR_ARG, std::string("error reading header of ") + path);
     is.ignore(1, '\n');
+    // a corrupt header must not produce wrapped sizes: each dimension fits int32, the data
+    // size in bytes fits int64, and the data lies inside the file
+    const uint64_t lim = (uint64_t)INT32_MAX;
+    if ((uint64_t)s0 > lim || (uint64_t)s1 > lim || (uint64_t)s2 > lim)
+        return host_fail(CQPI_ERR_ARG, std::string("IDL dimensions out of range in ") + path);
+    const uint64_t plane = (uint64_t)s0 * (uint64_t)s1;   // < 2^62
+    const uint64_t maxel = (uint64_t)INT64_MAX / sizeof(float);
+    if (s2 != 0 && plane > maxel / (uint64_t)s2)
+        return host_fail(CQPI_ERR_ARG, std::string("IDL data size overflows in ") + path);
+    const uint64_t bytes = plane * (uint64_t)s2 * sizeof(float);
+    const std::streamoff off = is.tellg();
+    if (off < 0) return host_fail(CQPI_ERR_ARG, std::string("error reading header of ") + path);
+    is.seekg(0, std::ios::end);
+    const std::streamoff end = is.tellg();
+    if (end < off || (uint64_t)(end - off) < bytes)
+        return host_fail(CQPI_ERR_ARG, std::string("IDL data region shorter than the header's dimensions in ") + path);
     snprintf(hdr->name, sizeof hdr->name, "%s", name.c_str());
     snprintf(hdr->date, sizeof hdr->date, "%s", date.c_str());
     hdr->size[0] = (int32_t)s0;
     hdr->size[1] = (int32_t)s1;
     hdr->size[2] = (int32_t)s2;
-    hdr->data_offset = (int64_t)is.tellg();
+    hdr->data_offset = (int64_t)off;
     return CQPI_OK;
 }
 

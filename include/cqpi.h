@@ -47,7 +47,10 @@ extern "C" {
 #define CQPI_ERR_NOT_CONVERGED 10 /* the surface / bulk decimation did not reach epserr */
 
 #define CQPI_PREC_FP64 0        /* every stage in FP64 */
-#define CQPI_PREC_MIXED 1       /* FP64 eigen/T/k-sum fold, FP32/tensor-core contraction */
+#define CQPI_PREC_MIXED 1       /* FP64: eigen-solve, T-matrix, term1; FP32: G0(k) and both
+                                   passes of the k-sum transform (pole distances from float
+                                   pairs); tensor-core contraction (split-FP16 x3, FP32
+                                   accumulation).  Maps within 1e-6 of the FP64 path. */
 
 /* Green's function of cqpi_set_greens (the green keyword, src/calcqpi.cc:129,206-209) */
 #define CQPI_GREEN_NORMAL 0     /* G0(k) from the eigen cache */
@@ -256,12 +259,14 @@ int cqpi_stage_times(cqpi_handle *h, float *ms5);
  * code running while a CUDA stream capture is active (cudaMalloc is not permitted there)
  * and hosts that pre-allocate a fixed device-memory budget and must not let a driver
  * allocation synchronise the device (e.g. a real-time instrument-control loop).
- * From a caller-owned device array g0k[kpoints][kpoints][bands][bands][2] (G0(k) of one
- * energy, k-grid order of src/qpi.cc:465-466) it writes the caller-owned device array
- * box[2rb+1][2rb+1][bands][bands][2] with G0(R) = kp^-2 sum_k G0(k) e^{+2 pi i k.R}
- * for R in [-rb, rb]^2 (the part of tmatrix::calcrealspacegreensfunction,
- * src/qpi.cc:557-578, that the LDOS needs), in FP64, asynchronously on 'stream'
- * (a cudaStream_t; NULL = default stream).
+ * Input: the caller-owned device array g0k[kpoints][kpoints][bands][bands][2], G0 of one
+ * energy at k = (i, j) / kpoints (index i, j in 0 .. kpoints-1; an index above
+ * kpoints/2 stands for i - kpoints), orbital pair (o1, o2), interleaved (re, im) doubles.
+ * Output: the caller-owned device array box[2rb+1][2rb+1][bands][bands][2] with, at
+ * [X + rb][Y + rb][o1][o2],
+ *     G0(R)[o1][o2] = kpoints^-2 sum_{i,j} g0k[i][j][o1][o2] e^{+2 pi i (i X + j Y) / kpoints}
+ * for R = (X, Y) in [-rb, rb]^2 (the only real-space values the LDOS contraction reads),
+ * in FP64, asynchronously on 'stream' (a cudaStream_t; NULL = default stream).
  * Limits: kpoints <= 4096, bands <= 16, and bands^2 * kpoints * (2rb+1) complex doubles
  * must fit the fixed scratch array of CQPI_NOALLOC_SCRATCH_BYTES -- larger requests
  * return CQPI_ERR_NOT_SUPPORTED.  The array is a file-scope __device__ variable held by

@@ -12,10 +12,14 @@
 #   oracle/_ref/mkwavefunctions   the reference's orbital-file tool (src/mkwavefunctions.cc main)
 #   oracle/_ref/seam_check   oracle/seam_check.cc: the GB300QPI backend built against the
 #                            reference's GPUQPI interface and linked with libcqpi.so
-# Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: oracle/build_ref.sh <reference-root>   (or the root in $CQPI_REFERENCE)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${CQPI_REFERENCE:-}}"
+if [ -z "$REF" ]; then
+  echo "no reference root given (argument or CQPI_REFERENCE); nothing to build" >&2
+  exit 3
+fi
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/qpi.cc" ]; then
   echo "reference sources not found under $REF; nothing to build" >&2

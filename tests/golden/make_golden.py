@@ -16,8 +16,9 @@ The bs_* cases record band-structure histograms (bsfile, output=nomode) of the r
 CLI.  The mkwf_* cases do the same for the orbital-file tool (oracle/_ref/mkwavefunctions): the
 inputs, input_<k>.cfg, the reference's IDL output ref_<k>.idl and its log ref_<k>.txt.
 
-Run from the repository root:  python tests/golden/make_golden.py [case ...]
-(requires the reference sources, i.e. only in the build container).
+Run from the repository root:
+    CQPI_REFERENCE=<reference checkout> python tests/golden/make_golden.py [case ...]
+(requires the reference sources; CQPI_REFERENCE names the folder that holds src/qpi.cc).
 """
 import json
 import os
@@ -579,7 +580,7 @@ def write_keywords():
     name in src/calcqpi.cc and src/mkwavefunctions.cc), one per line, for the keyword
     coverage test of the CLI and the orbital-file tool."""
     import re
-    root = os.environ.get("CQPI_REFERENCE", "/root/reference")
+    root = reference_root()
     for prog in ("calcqpi", "mkwavefunctions"):
         with open(os.path.join(root, "src", prog + ".cc")) as fh:
             names = sorted(set(re.findall(r'probefield\("([^"]+)"\)', fh.read())))
@@ -589,9 +590,18 @@ def write_keywords():
         print("keywords", prog, len(names))
 
 
+def reference_root():
+    """The reference checkout whose sources the fixtures are generated from: the
+    CQPI_REFERENCE environment variable (required; there is no default location)."""
+    root = os.environ.get("CQPI_REFERENCE")
+    if not root or not os.path.isfile(os.path.join(root, "src", "qpi.cc")):
+        raise SystemExit("set CQPI_REFERENCE to the reference checkout (the folder holding src/qpi.cc)")
+    return root
+
+
 if __name__ == "__main__":
     if not os.path.exists(os.path.join(REF, "mkwavefunctions")):
-        subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
+        subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), reference_root()])
     names = [a for a in sys.argv[1:] if a != "keywords"]
     if not sys.argv[1:] or "keywords" in sys.argv[1:]:
         write_keywords()
