@@ -367,33 +367,8 @@ def run_ours(args):
     # accuracy and speed of the all-FP64 path on the same workload (the metric's comparison)
     fp64_info = None
     if prec != cqpi.PREC_FP64 and not args.no_fp64_check:
-        sub = np.linspace(0, nE - 1, 5).astype(int)
-        with make_engine(cqpi, c, m, wf, vscat, cqpi.PREC_FP64) as e64:
-            ref = e64.run(E[sub], f32=False, f64=True)
-            t0 = time.perf_counter()
-            e64.solve_bands()
-            e64.run(E[sub], f32=False, f64=False)
-            t64 = time.perf_counter() - t0
-        got = out[sub].double().cpu().numpy()
-        # per-map relative errors; a map that vanishes to rounding in FP64 (the Josephson map
-        # at E = 0: ~1e-17 of the largest) has no relative error of its own and is reported
-        # against the largest checked map instead
-        gmax = max(float(np.abs(ref[i, 0]).max()) for i in range(len(sub)))
-        live = [i for i in range(len(sub)) if np.abs(ref[i, 0]).max() > 1e-9 * gmax]
-        zero = [i for i in range(len(sub)) if i not in live]
-        errs = [float(np.abs(got[i, 0] - ref[i, 0]).max() / np.abs(ref[i, 0]).max()) for i in live]
-        rms = [float(np.sqrt(np.mean((got[i, 0] - ref[i, 0]) ** 2) / np.mean(ref[i, 0] ** 2))) for i in live]
-        zero_info = {"energies": [float(E[sub][i]) for i in zero],
-                     "max_abs_err_over_largest_map": max([float(np.abs(got[i, 0] - ref[i, 0]).max()) / gmax
-                                                          for i in zero], default=0.0)} if zero else None
-        fp64_value = len(sub) * c.pixels_per_energy / t64
-        fp64_info = {"max_rel_err_vs_fp64": max(errs), "rms_rel_err_vs_fp64": max(rms),
-                     "rel_err_definitions": "max|rho-rho64|/max|rho64| and rms(rho-rho64)/rms(rho64) per map, worst map",
-                     "per_map_max_rel_err": errs,
-                     "energies_checked": [float(x) for x in E[sub]],
-                     "tolerance": 1e-6, "fp64_path_value": fp64_value, "mixed_over_fp64": value / world / fp64_value}
-        if zero_info:
-            fp64_info["vanishing_maps"] = zero_info
+        fp64_info = fp64_check(cqpi, c, m, wf, vscat, E, lambda sub: out[sub].double().cpu().numpy(), 5)
+        fp64_info["mixed_over_fp64"] = value / world / fp64_info["fp64_path_value"]
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -415,6 +390,17 @@ def run_ours(args):
         line["clocks"] = clk
     if rank == 0 and args.adjoint_steps > 0 and prec != cqpi.PREC_FP64:
         line["adjoint"] = adjoint_rate(args.adjoint_steps)
+    # the other workloads of the series, each measured the same way (device outputs, CUDA
+    # events on the engine's stream) with its error against the FP64 path
+    if rank == 0 and world == 1 and not args.no_extras and args.config == "C2" and not args.fov and not args.energies:
+        extras = {}
+        for nm, n_check in (("C3", 2), ("CJ", 3)):
+            extras[nm] = workload_measure(nm, 3, 2, n_check)
+        f4, _ = c4_measure(3, 2, not args.no_autotune)
+        extras["C4"] = {"workload": f4["config"]["workload"], "ms_per_job": f4["ms_per_step"], "value": f4["value"],
+                        "unit": UNIT, "latency_ms_per_map": f4["latency_ms_per_map"], "maps": f4["config"]["maps"],
+                        "pixel_energies": f4["config"]["pixel_energies"]}
+        line["extras"] = extras
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, desc = cpu_sample(args.config, target_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
@@ -443,16 +429,14 @@ def c4_workload(seed=4):
     return E, np.stack(Vs), fov
 
 
-def run_c4(args):
+def c4_measure(steps, warmup, autotune=True):
     """Batched workload: all energies, impurities and uneven fields of view of one job as
     one captured CUDA graph of cqpi_run_fov calls (chunks of 32 energies into a reused
-    device output ring); per-map latency from single-energy calls (12 maps each)."""
+    device output ring); per-map latency from single-energy calls (12 maps each).  Returns
+    (line fields, clocks)."""
     import torch
-    import cqpi_build
-    cqpi_build.build()
     import cqpi
     from cqpi import workloads as W
-    torch.cuda.set_device(0)
     c, m, wf = W.config("C2")
     E, Vs, fov = c4_workload()
     nimp, os_ = len(Vs), c.oversamp
@@ -471,7 +455,7 @@ def run_c4(args):
 
     eng.solve_bands()
     tune = None
-    if not args.no_autotune:
+    if autotune:
         ms_t, n_t = eng.autotune(E[:32])
         tune = {"shapes_timed": n_t, "batch_ms": ms_t}
     job()                                   # allocates every buffer
@@ -480,22 +464,22 @@ def run_c4(args):
     job()
     eng.graph_end()
     stream = torch.cuda.ExternalStream(eng.stream)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         eng.solve_bands()
         eng.graph_launch()
     eng.synchronize()
     launches0 = eng.kernel_launches()
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         eng.solve_bands()
         eng.graph_launch()
     ev1.record(stream)
     ev1.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = ev0.elapsed_time(ev1) / steps
     launches = eng.kernel_launches() - launches0
     # per-map latency: one energy (its 12 maps) per call, CUDA events around each call
     lat = []
@@ -510,24 +494,105 @@ def run_c4(args):
     eng.synchronize()
     per_call = np.array([a.elapsed_time(b) for a, b in lat])
     per_map = np.repeat(per_call, nimp)
-    line = {"metric": METRIC, "value": pix / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": f"mixed: f64 eigen/T/term1, f32 G0+FFT, {eng.contraction_kind()} contraction",
-            "data": "synthetic (seeded model, impurities and fields of view)",
-            "config": {"workload": "C4: C2 t2g model, k-grid 1024^2, 256 energies x 12 impurities (6 scalar, 6 Hermitian "
-                                   "3x3), field of view per map from {64,128,256,384}^2 sites, 10x10 px/cell, one CUDA "
-                                   "graph of cqpi_run_fov chunks (32 energies)",
-                       "maps": int(len(fov)), "pixel_energies": pix, "mean_pixels_per_map": pix / len(fov),
-                       "autotune": tune,
-                       "l2": "outputs far larger than L2"},
-            "gpu_launches": int(launches),
-            "latency_ms_per_map": {"p50": float(np.percentile(per_map, 50)), "p99": float(np.percentile(per_map, 99)),
-                                   "definition": "duration of the single-energy call (12 maps) that produced the map"}}
+    kind = eng.contraction_kind()
+    eng.close()
+    fields = {"value": pix / (ms / 1e3), "ms_per_step": ms, "gpu_launches": int(launches),
+              "dtype": f"mixed: f64 eigen/T/term1, f32 G0+FFT, {kind} contraction",
+              "config": {"workload": "C4: C2 t2g model, k-grid 1024^2, 256 energies x 12 impurities (6 scalar, 6 "
+                                     "Hermitian 3x3), field of view per map from {64,128,256,384}^2 sites, 10x10 "
+                                     "px/cell, one CUDA graph of cqpi_run_fov chunks (32 energies)",
+                         "maps": int(len(fov)), "pixel_energies": pix, "mean_pixels_per_map": pix / len(fov),
+                         "autotune": tune, "l2": "outputs far larger than L2"},
+              "latency_ms_per_map": {"p50": float(np.percentile(per_map, 50)), "p99": float(np.percentile(per_map, 99)),
+                                     "definition": "duration of the single-energy call (12 maps) that produced the map"}}
+    return fields, clk
+
+
+def run_c4(args):
+    import torch
+    import cqpi_build
+    cqpi_build.build()
+    torch.cuda.set_device(0)
+    f, clk = c4_measure(args.steps, args.warmup, not args.no_autotune)
+    line = {"metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": f["dtype"], "data": "synthetic (seeded model, impurities and fields of view)",
+            "config": f["config"], "gpu_launches": f["gpu_launches"], "latency_ms_per_map": f["latency_ms_per_map"]}
     if clk is not None:
         line["clocks"] = clk
     print(json.dumps(line), flush=True)
-    eng.close()
     return 0
+
+
+def fp64_check(cqpi, c, m, wf, vscat, E, maps, n_check):
+    """Per-map relative errors of the mixed maps (host [nE][wn][wn]) against the engine's
+    FP64 path on n_check energies spread over the list; maps that vanish to rounding in FP64
+    (the Josephson map at E = 0) are reported against the largest checked map."""
+    sub = np.linspace(0, len(E) - 1, n_check).astype(int)
+    with make_engine(cqpi, c, m, wf, vscat, cqpi.PREC_FP64) as e64:
+        ref = e64.run(E[sub], f32=False, f64=True)
+        t0 = time.perf_counter()
+        e64.solve_bands()
+        e64.run(E[sub], f32=False, f64=False)
+        t64 = time.perf_counter() - t0
+    got = maps(sub)
+    gmax = max(float(np.abs(ref[i, 0]).max()) for i in range(len(sub)))
+    live = [i for i in range(len(sub)) if np.abs(ref[i, 0]).max() > 1e-9 * gmax]
+    zero = [i for i in range(len(sub)) if i not in live]
+    errs = [float(np.abs(got[i, 0] - ref[i, 0]).max() / np.abs(ref[i, 0]).max()) for i in live]
+    rms = [float(np.sqrt(np.mean((got[i, 0] - ref[i, 0]) ** 2) / np.mean(ref[i, 0] ** 2))) for i in live]
+    info = {"max_rel_err_vs_fp64": max(errs), "rms_rel_err_vs_fp64": max(rms),
+            "rel_err_definitions": "max|rho-rho64|/max|rho64| and rms(rho-rho64)/rms(rho64) per map, worst map",
+            "per_map_max_rel_err": errs, "energies_checked": [float(x) for x in E[sub]], "tolerance": 1e-6,
+            "fp64_path_value": len(sub) * c.pixels_per_energy / t64}
+    if zero:
+        info["vanishing_maps"] = {"energies": [float(E[sub][i]) for i in zero],
+                                  "max_abs_err_over_largest_map": max(float(np.abs(got[i, 0] - ref[i, 0]).max()) / gmax
+                                                                      for i in zero)}
+    return info
+
+
+def workload_measure(name, steps, warmup, n_check):
+    """ms per job (eigen-solve + every energy, device outputs), pixel*E/s and the error
+    against the FP64 path of one workload of the C-series, for the extra objects of the
+    default line."""
+    import torch
+    import cqpi
+    from cqpi import workloads as W
+    c, m, wf = W.config(name)
+    E = c.energy_list()
+    vscat = np.array(c.scattering, complex)
+    if len(vscat) < m.bands:
+        vscat = np.concatenate([vscat, np.zeros(m.bands - len(vscat), complex)])
+    eng = make_engine(cqpi, c, m, wf, vscat, cqpi.PREC_MIXED)
+    wn = c.lattice * c.oversamp
+    out = torch.empty((len(E), 1, wn, wn), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(eng.stream)
+
+    def step():
+        eng.solve_bands()
+        eng.run_device(E, ptr32=out.data_ptr())
+
+    for _ in range(warmup):
+        step()
+    eng.synchronize()
+    eng.stage_times()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    stages = {k: v / steps for k, v in eng.stage_times().items()}
+    kind = eng.contraction_kind()
+    eng.close()
+    res = {"workload": workload_desc(name, c, m, len(E)), "ms_per_job": ms,
+           "value": c.pixels_per_energy * len(E) / (ms / 1e3), "unit": UNIT, "contraction": kind,
+           "stage_ms_per_job": stages, "steps": steps, "warmup": warmup}
+    res["accuracy"] = fp64_check(cqpi, c, m, wf, vscat, E, lambda sub: out[sub].double().cpu().numpy(), n_check)
+    del out
+    return res
 
 
 def adjoint_rate(steps):
@@ -567,6 +632,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the C3 / CJ / C4 objects of the default line")
     ap.add_argument("--no-autotune", action="store_true", help="keep the rule-based contraction tile shape")
     ap.add_argument("--fov", type=int, default=0, help="override the field of view (sites per side) for small captures")
     ap.add_argument("--energies", type=int, default=0, help="override the number of energies for small captures")

@@ -264,7 +264,7 @@ int host_batch()
 {
     const char *f = getenv("CQPI_HOST_BATCH");
     const int v = f ? atoi(f) : 0;
-    return v > 0 ? v : 16;
+    return v > 0 ? v : 8;
 }
 
 int choose_batch(const cqpi_handle *h, int nE)
