@@ -94,11 +94,14 @@ def _ldos_function():
     return LDOSMaps
 
 
-def qpi_loss(maps, target):
-    """sum over energies of || |FFT2(rho)| - target ||^2 (target: [nE][wn][wn] magnitudes)."""
+def qpi_loss(maps, target, dtype=None):
+    """sum over energies of || |FFT2(rho)| - target ||^2 (target: [nE][wn][wn] magnitudes).
+    dtype: the transform's real type (torch.float64 by default; torch.float32 runs the FFT in
+    single precision, the sum in double)."""
     torch = _torch()
-    q = torch.abs(torch.fft.fft2(maps[:, 0].to(torch.float64)))
-    return torch.sum((q - target) ** 2)
+    dt = torch.float64 if dtype is None else dtype
+    q = torch.abs(torch.fft.fft2(maps[:, 0].to(dt)))
+    return torch.sum(((q - target.to(dt)) ** 2).to(torch.float64))
 
 
 def target_maps(fit, rel=0.05, seed=7):
@@ -112,18 +115,22 @@ def target_maps(fit, rel=0.05, seed=7):
     return p_true, tgt
 
 
-def run_adam(fit, target, steps=200, lr=2e-3, fit_v=False, log=None):
-    """Adam on (p, V) from p0 / V0; returns (p, V, losses)."""
+def run_adam(fit, target, steps=200, lr=2e-3, fit_v=True, log=None, loss_dtype="float32", V_init=None):
+    """Adam on (p, V) from p0 / V0 (or V_init); returns (p, V, losses).  fit_v: optimise the
+    3x3 impurity matrix too; loss_dtype: the QPI loss's FFT precision ("float32": the
+    transform in single precision, the sum in double; "float64")."""
     torch = _torch()
     LDOSMaps = _ldos_function()
+    dt = torch.float32 if loss_dtype == "float32" else torch.float64
     p = torch.tensor(fit.p0.copy(), dtype=torch.float64, requires_grad=True)
-    Vr = torch.tensor(fit.V0.real.copy(), dtype=torch.float64, requires_grad=fit_v)
+    V0 = fit.V0.real if V_init is None else np.asarray(V_init, np.float64)
+    Vr = torch.tensor(V0.copy(), dtype=torch.float64, requires_grad=fit_v)
     opt = torch.optim.Adam([p, Vr] if fit_v else [p], lr=lr)
     losses = []
     for it in range(steps):
         opt.zero_grad()
         maps = LDOSMaps.apply(p, Vr, fit)
-        loss = qpi_loss(maps, target)
+        loss = qpi_loss(maps, target, dt)
         loss.backward()
         opt.step()
         losses.append(float(loss.detach()))
@@ -141,3 +148,48 @@ def gradient(fit, p, V, target):
     loss = qpi_loss(LDOSMaps.apply(pt, Vt, fit), target)
     loss.backward()
     return float(loss.detach()), pt.grad.numpy(), Vt.grad.numpy()
+
+
+def gauss_newton(fit, p, V, h_rel=1e-4, h_abs=1e-5):
+    """Gauss-Newton matrix J^T J of the QPI magnitudes F(x) = |FFT2 rho(x)| (every energy and
+    pixel) at x = (p, V) -- the p amplitudes, then the nine real entries of V -- with J by
+    central differences of the engine's maps (step h_rel |x_i|, at least h_abs), the
+    transforms and the products in FP64.  Returns (JtJ [n][n], x)."""
+    torch = _torch()
+    x = np.concatenate([np.asarray(p, np.float64), np.asarray(V, np.float64).reshape(-1)])
+    npar = len(x)
+    npp = len(p)
+
+    def F(xx):
+        m = fit.maps(xx[:npp], xx[npp:].reshape(fit.bands, fit.bands))
+        return torch.abs(torch.fft.fft2(m[:, 0].to(torch.float64))).reshape(-1).to(torch.float32)
+
+    cols = []
+    for i in range(npar):
+        h = max(h_rel * abs(x[i]), h_abs)
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        cols.append((F(xp) - F(xm)) / (2.0 * h))
+    J = torch.stack(cols, dim=1)                       # [outputs][npar] float32 on the device
+    JtJ = np.zeros((npar, npar))
+    step = 1 << 22
+    for r0 in range(0, J.shape[0], step):              # FP64 products, chunked over the outputs
+        Jc = J[r0:r0 + step].to(torch.float64)
+        JtJ += (Jc.T @ Jc).cpu().numpy()
+    del J, cols
+    return JtJ, x
+
+
+def identifiability(JtJ, x_true, x_start, x_fit):
+    """Eigen-directions of J^T J (descending eigenvalues) and, per direction, the parameter
+    error of the start and of the fit projected on it: how much of the start's error the fit
+    removed in the well-constrained directions and which directions the maps do not constrain."""
+    lam, vec = np.linalg.eigh(JtJ)
+    order = np.argsort(lam)[::-1]
+    lam, vec = lam[order], vec[:, order]
+    d0, d1 = vec.T @ (x_start - x_true), vec.T @ (x_fit - x_true)
+    return {"eigenvalues_rel": (lam / lam[0]).tolist(),
+            "start_error_per_direction": np.abs(d0).tolist(),
+            "fit_error_per_direction": np.abs(d1).tolist(),
+            "fit_over_start_per_direction": (np.abs(d1) / np.maximum(np.abs(d0), 1e-300)).tolist()}

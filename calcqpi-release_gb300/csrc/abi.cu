@@ -163,6 +163,10 @@ void free_adj(cqpi_handle *h)
     dfree(h->adj.gk);
     dfree(h->adj.C);
     dfree(h->adj.gR);
+    if (h->adj.win) cudaFree(h->adj.win);
+    h->adj.win = nullptr;
+    dfree(h->adj.Mp);
+    dfree(h->adj.kt);
     h->adj.ebatch = 0;
 }
 
@@ -176,9 +180,18 @@ void ensure_adj(cqpi_handle *h, int ebatch)
     dalloc(&h->adj.wsum, ebatch * (size_t)h->Q);
     dalloc(&h->adj.gV, (size_t)std::max(h->nimp, 1) * bb);
     dalloc(&h->adj.A, bb * (size_t)h->NB * h->kp);
-    dalloc(&h->adj.gk, bb * nk);
+    // Gbar(k) of every energy of a batch in the handle's precision (at least one FP64 plane
+    // set: Hbar(k) is written over it)
+    const size_t gk_per_e = h->precision == CQPI_PREC_FP64 ? bb * nk : (bb * nk + 1) / 2;
+    dalloc(&h->adj.gk, std::max(ebatch * gk_per_e, bb * nk));
     dalloc(&h->adj.C, bb * nk);
     dalloc(&h->adj.gR, (size_t)std::max(h->nR, 1) * 2 * bb);
+    const size_t nsite = (size_t)h->n * h->n, nmap = ebatch * (size_t)std::max(h->nimp, 1);
+    const size_t cs = h->precision == CQPI_PREC_FP64 ? sizeof(double2) : sizeof(float2);
+    CK(cudaMalloc(&h->adj.win, 2 * cs * nmap * h->W * h->mb * h->b * nsite));
+    dalloc(&h->adj.Mp, nmap * nsite * bb);
+    const size_t span = 4 * (size_t)h->w + 1;
+    dalloc(&h->adj.kt, span * span * h->mb * h->mb * h->Q);
     h->adj.ebatch = ebatch;
 }
 
@@ -1500,7 +1513,12 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
     const size_t mapn = (size_t)h->wn * h->wn, per_e = (size_t)h->nimp * mapn;
     const int nhops = (int)h->hop_r.size();
     try {
-        const int eb = choose_batch(h, std::max(nE, 1));
+        // energies per batch: also bounded by the stored window gradients of every site
+        // (2 x W x orbitals x bands complex values per site and map) within 8 GiB
+        const size_t win_map = 2 * (h->precision == CQPI_PREC_FP64 ? 16 : 8) * (size_t)h->W * h->mb * h->b *
+                               (size_t)h->n * h->n * (size_t)std::max(h->nimp, 1);
+        const size_t gk_e = (h->precision == CQPI_PREC_FP64 ? 16 : 8) * (size_t)h->b * h->b * h->kp * h->kp;
+        const int eb = std::max(1, std::min(choose_batch(h, std::max(nE, 1)), (int)(((size_t)12 << 30) / (win_map + gk_e))));
         ensure_workspace(h, eb);
         ensure_adj(h, eb);
         ensure_energies(h, std::max(nE, 1));
@@ -1532,9 +1550,11 @@ int cqpi_adjoint(cqpi_handle *h, const double *energies, int32_t nE, const float
             launch_adj_energy_batch(h, ne, wm, h->adj);
             check_launch();
             for (int e = 0; e < ne; e++) {
-                launch_adj_kspace(h, e, energies[e0 + e], h->adj);
+                launch_adj_kspace(h, e, h->adj);
                 check_launch();
             }
+            launch_adj_kacc(h, ne, den, h->adj);
+            check_launch();
         }
         launch_adj_hoppings(h, h->adj);
         check_launch();

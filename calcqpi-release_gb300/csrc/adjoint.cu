@@ -16,8 +16,11 @@
 // zbar = P^H ybar Q^H.  The adjoint recomputes G(R) and T per energy (nothing of the
 // forward run is stored) and goes back through:
 //   1. adj_contract_kernel: u, s per pixel; ubar = -i W conj(T s), sbar = -i W conj(u T);
-//      M = sum W u s^T (-> Tbar = -i conj M); window scatter of phi^T ubar / phi^T sbar into
-//      the G(R) box gradient; sum_p W per pixel for the term1 part.
+//      per site the window gradients phi^T ubar / phi^T sbar (one value per window entry,
+//      stored) and the site's part of M = sum W u s^T (-> Tbar = -i conj M);
+//      adj_gather_kernel sums the window gradients of the sites whose windows cover a box
+//      point into the G(R) box gradient (no atomics), adj_mreduce_kernel the M parts, and
+//      adj_wsum_kernel forms sum_p W per sub-pixel for the term1 part.
 //   2. adj_term1_kernel: term1 part of the box gradient.
 //   3. adj_tv_kernel: gbar(0) += T^H Tbar T^H, Vbar += A^-H Tbar (1 + g T)^H, A = 1 - V g.
 //   4. adj_cols_kernel / adj_rows_kernel: Gbar(k) = kp^-2 sum_R e^{-2 pi i k.R/kp} Gbar(R)
@@ -49,19 +52,25 @@ __device__ __forceinline__ void atomic_add2(double2 *p, double2 v)
 
 // ------------------------------------------------------------------ 1. contraction adjoint
 // grid (n*n sites, ne*nimp maps), block: one thread per sub-pixel q (Q <= 128).
+// Outputs of site p and map ei (nsite = n*n, t = d*mb + o a window entry, Wmb = W*mb):
+//   Ub[((ei*Wmb + t)*b + a)*nsite + p] = sum_q phi_o(q,d) ubar_a(p,q)   (-> Gbar(p+d)[o][a])
+//   Sb[((ei*Wmb + t)*b + c)*nsite + p] = sum_q phi_o(q,d) sbar_c(p,q)   (-> Gbar(-p-d)[c][o])
+//   Mp[(ei*nsite + p)*b*b + a*b + c]  = sum_q W u_a s_c
 template <int B, class C>
 __global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os, int w, int Rb, int NB, int Q, int W, int nimp,
                                                            int mb, int bs0, const typename real_of<C>::type *__restrict__ phi,
                                                            const C *__restrict__ box, const double2 *__restrict__ T,
-                                                           const float *__restrict__ wmap, double2 *__restrict__ gbox,
-                                                           double2 *__restrict__ Mbuf, double *__restrict__ wsum)
+                                                           const float *__restrict__ wmap, C *__restrict__ Ub,
+                                                           C *__restrict__ Sb, double2 *__restrict__ Mp)
 {
     using Rl = typename real_of<C>::type;
     extern __shared__ __align__(16) unsigned char adj_sm[];
     Rl *ubr = reinterpret_cast<Rl *>(adj_sm);               // [128][b] each: ubar, sbar (re, im)
     Rl *ubi = ubr + 128 * b, *sbr = ubi + 128 * b, *sbi = sbr + 128 * b;
+    double2 *mred = reinterpret_cast<double2 *>(sbi + 128 * b);   // [4 warps][b*b]
     const int site = blockIdx.x, ei = blockIdx.y;
     const int e = ei / nimp;
+    const int nsite = n * n;
     const int i = site / n, j = site % n;
     const int n2 = n >> 1, px = i - n2, py = j - n2;
     const int wn = n * os, bb = b * b, side = 2 * w + 1;
@@ -70,7 +79,6 @@ __global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os,
     const int qx = qv ? q / os : 0, qy = qv ? q % os : 0;
     const C *boxe = box + (size_t)e * NB * NB * bb;
     const double2 *Te = T + (size_t)ei * bb;
-    double2 *gb = gbox + (size_t)e * NB * NB * bb;
     const Rl *ph = phi + (size_t)q * W * mb;
 
     Rl W_ = 0;
@@ -120,8 +128,8 @@ __global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os,
             sbr[q * b + a] = -W_ * uti; sbi[q * b + a] = -W_ * utr;
         }
     }
-    if (qv && W_ != (Rl)0) atomicAdd(wsum + (size_t)e * Q + q, (double)W_);
-    // M_ac = sum_q W u_a s_c: warp sums, then one atomic per warp and element
+    // M_ac = sum_q W u_a s_c: warp sums, then the four warps' sums in shared memory
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int a = 0; a < B; a++)
 #pragma unroll
@@ -133,22 +141,24 @@ __global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os,
                 mr += __shfl_xor_sync(0xffffffffu, mr, o);
                 mi += __shfl_xor_sync(0xffffffffu, mi, o);
             }
-            if ((threadIdx.x & 31) == 0 && (mr != 0.0 || mi != 0.0)) atomic_add2(Mbuf + (size_t)ei * bb + a * b + c, make_double2(mr, mi));
+            if (lane == 0) mred[warp * bb + a * b + c] = make_double2(mr, mi);
         }
     __syncthreads();
-    // window gradients: entry (d, o) of phi^T ubar (into G(p+d)[o][a]) and of phi^T sbar
-    // (into G(-p-d)[c][o])
-    for (int t = threadIdx.x; t < W * mb; t += blockDim.x) {
-        const int d = t / mb, ol = t - d * mb, o = bs0 + ol;
-        const int dx = d / side - w, dy = d % side - w;
+    for (int k = threadIdx.x; k < bb; k += blockDim.x) {
+        double2 m = make_double2(0.0, 0.0);
+        for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) m = cadd(m, mred[wv * bb + k]);
+        Mp[((size_t)ei * nsite + site) * bb + k] = m;
+    }
+    // window gradients of this site: entry (d, o) of phi^T ubar and of phi^T sbar
+    const int Wmb = W * mb;
+    for (int t = threadIdx.x; t < Wmb; t += blockDim.x) {
+        const int d = t / mb, ol = t - d * mb;
         Rl gur[B], gui[B], gsr[B], gsi[B];
 #pragma unroll
         for (int a = 0; a < B; a++) { gur[a] = 0; gui[a] = 0; gsr[a] = 0; gsi[a] = 0; }
-        bool any = false;
         for (int qq = 0; qq < Q; qq++) {
             const Rl f = phi[((size_t)qq * W + d) * mb + ol];
             if (f == (Rl)0) continue;
-            any = true;
 #pragma unroll
             for (int a = 0; a < B; a++) {
                 if (a < b) {
@@ -157,53 +167,294 @@ __global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os,
                 }
             }
         }
-        if (!any) continue;
-        double2 *du = gb + ((size_t)(px + dx + Rb) * NB + (py + dy + Rb)) * bb;
-        double2 *ds = gb + ((size_t)(-px - dx + Rb) * NB + (-py - dy + Rb)) * bb;
 #pragma unroll
         for (int a = 0; a < B; a++) {
             if (a < b) {
-                atomic_add2(du + o * b + a, make_double2((double)gur[a], (double)gui[a]));
-                atomic_add2(ds + a * b + o, make_double2((double)gsr[a], (double)gsi[a]));
+                const size_t idx = (((size_t)ei * Wmb + t) * b + a) * nsite + site;
+                Ub[idx] = cmake<C>(gur[a], gui[a]);
+                Sb[idx] = cmake<C>(gsr[a], gsi[a]);
             }
         }
     }
 }
 
-// ------------------------------------------------------------------ 2. term1
-// grid ((4w+1)^2 offsets Delta, ne); threads over q.  rho has -term1, so
-// Gbar(Delta)[o2][o1] += -i sum_q wsum(q) sum_{d1} phi_o1(q,d1) phi_o2(q,d1+Delta).
-__global__ void __launch_bounds__(128) adj_term1_kernel(int b, int w, int Rb, int NB, int Q, int W, int mb, int bs0,
-                                                        const double *__restrict__ phi, const double *__restrict__ wsum,
-                                                        double2 *__restrict__ gbox)
+// The same outputs with one warp per site (up to 4 bands): the orbital table phi is staged in
+// shared memory as [entry t][q] (row stride QP = 129 words, zero past Q), lane l handles the
+// pixels q = l + 32k (k < 4) in the forward part, so every window value G(R)[o][a] loaded for a
+// site feeds 4 pixels, and the entries t = l + 32m in the window-gradient part, so every
+// ubar / sbar row read feeds 3 entries.  grid (ceil(n*n / 4), ne*nimp), 4 warps.
+constexpr int ADJ_QP = 129;
+template <int B, class C>
+__global__ void __launch_bounds__(128) adj_contract_warp_kernel(int b, int n, int os, int w, int Rb, int NB, int Q, int W,
+                                                                int nimp, int mb, int bs0,
+                                                                const typename real_of<C>::type *__restrict__ phi,
+                                                                const C *__restrict__ box, const double2 *__restrict__ T,
+                                                                const float *__restrict__ wmap, C *__restrict__ Ub,
+                                                                C *__restrict__ Sb, double2 *__restrict__ Mp)
 {
-    const int e = blockIdx.y;
-    const int span = 4 * w + 1, side = 2 * w + 1;
-    const int rx = blockIdx.x / span - 2 * w, ry = blockIdx.x % span - 2 * w;
-    const int bb = b * b;
-    __shared__ double acc[CQPI_MAX_BANDS * CQPI_MAX_BANDS];
-    for (int t = threadIdx.x; t < mb * mb; t += blockDim.x) acc[t] = 0.0;
+    using Rl = typename real_of<C>::type;
+    extern __shared__ __align__(16) unsigned char adj_sm[];
+    const int Wmb = W * mb;
+    Rl *phT = reinterpret_cast<Rl *>(adj_sm);                     // [Wmb][ADJ_QP]
+    Rl *ubs = phT + (size_t)Wmb * ADJ_QP;                          // [4 warps][128 q][b][4]: ubar re, im, sbar re, im
+    for (int i = threadIdx.x; i < Wmb * ADJ_QP; i += blockDim.x) {
+        const int t = i / ADJ_QP, q = i - t * ADJ_QP;
+        phT[i] = q < Q ? phi[(size_t)q * Wmb + t] : (Rl)0;
+    }
     __syncthreads();
-    for (int q = threadIdx.x; q < Q; q += blockDim.x) {
-        const double ws = wsum[(size_t)e * Q + q];
-        if (ws == 0.0) continue;
-        for (int d1 = 0; d1 < W; d1++) {
-            const int x2 = d1 / side + rx, y2 = d1 % side + ry;   // window position of d2 = d1 + Delta
-            if (x2 < 0 || x2 >= side || y2 < 0 || y2 >= side) continue;
-            const int d2 = x2 * side + y2;
-            const double *p1 = phi + ((size_t)q * W + d1) * mb;
-            const double *p2 = phi + ((size_t)q * W + d2) * mb;
-            for (int o1 = 0; o1 < mb; o1++) {
-                if (p1[o1] == 0.0) continue;
-                for (int o2 = 0; o2 < mb; o2++) atomicAdd(&acc[o2 * mb + o1], ws * p1[o1] * p2[o2]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nsite = n * n, site = blockIdx.x * 4 + warp;
+    if (site >= nsite) return;
+    const int ei = blockIdx.y, e = ei / nimp;
+    const int i = site / n, j = site % n;
+    const int n2 = n >> 1, px = i - n2, py = j - n2;
+    const int wn = n * os, bb = b * b, side = 2 * w + 1;
+    const C *boxe = box + (size_t)e * NB * NB * bb;
+    const double2 *Te = T + (size_t)ei * bb;
+    // forward part: u_a(q), s_a(q) for the 4 pixel slots of this lane
+    Rl ur[4][B], ui[4][B], sr[4][B], si[4][B];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int a = 0; a < B; a++) { ur[k][a] = 0; ui[k][a] = 0; sr[k][a] = 0; si[k][a] = 0; }
+    for (int d = 0; d < W; d++) {
+        const int dx = d / side - w, dy = d % side - w;
+        const C *gs = boxe + ((size_t)(-px - dx + Rb) * NB + (-py - dy + Rb)) * bb;
+        const C *gu = boxe + ((size_t)(px + dx + Rb) * NB + (py + dy + Rb)) * bb;
+        for (int ol = 0; ol < mb; ol++) {
+            const int o = bs0 + ol, t = d * mb + ol;
+            C vu[B], vs[B];
+#pragma unroll
+            for (int a = 0; a < B; a++)
+                if (a < b) { vu[a] = gu[o * b + a]; vs[a] = gs[a * b + o]; }
+            const Rl *pt = phT + (size_t)t * ADJ_QP + lane;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const Rl f = pt[32 * k];
+#pragma unroll
+                for (int a = 0; a < B; a++)
+                    if (a < b) {
+                        ur[k][a] += vu[a].x * f; ui[k][a] += vu[a].y * f;
+                        sr[k][a] += vs[a].x * f; si[k][a] += vs[a].y * f;
+                    }
             }
         }
     }
+    // ubar = -i W conj(T s), sbar = -i W conj(u^T T); M_ac = sum_q W u_a s_c
+    Rl *ub = ubs + (size_t)warp * 128 * b * 4;
+    // M partials of the lane's pixels in the working precision; the warp and site sums in FP64
+    Rl mr[B][B], mi[B][B];
+#pragma unroll
+    for (int a = 0; a < B; a++)
+#pragma unroll
+        for (int c = 0; c < B; c++) { mr[a][c] = 0; mi[a][c] = 0; }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int q = lane + 32 * k;
+        const bool qv = q < Q;
+        const int qx = qv ? q / os : 0, qy = qv ? q % os : 0;
+        const Rl W_ = qv ? (Rl)wmap[((size_t)ei * wn + (size_t)j * os + qy) * wn + (size_t)i * os + qx] : (Rl)0;
+#pragma unroll
+        for (int a = 0; a < B; a++) {
+            if (a >= b) continue;
+            Rl tsr = 0, tsi = 0, utr = 0, uti = 0;
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                if (c >= b) continue;
+                const double2 t = Te[a * b + c];      // T_ac
+                tsr += (Rl)t.x * sr[k][c] - (Rl)t.y * si[k][c];
+                tsi += (Rl)t.x * si[k][c] + (Rl)t.y * sr[k][c];
+                const double2 t2 = Te[c * b + a];     // T_ca
+                utr += ur[k][c] * (Rl)t2.x - ui[k][c] * (Rl)t2.y;
+                uti += ur[k][c] * (Rl)t2.y + ui[k][c] * (Rl)t2.x;
+                mr[a][c] += W_ * (ur[k][a] * sr[k][c] - ui[k][a] * si[k][c]);
+                mi[a][c] += W_ * (ur[k][a] * si[k][c] + ui[k][a] * sr[k][c]);
+            }
+            Rl *u4 = ub + ((size_t)q * b + a) * 4;
+            u4[0] = -W_ * tsi; u4[1] = -W_ * tsr; u4[2] = -W_ * uti; u4[3] = -W_ * utr;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < B; a++)
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            if (a >= b || c >= b) continue;
+            double x = (double)mr[a][c], y = (double)mi[a][c];
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                y += __shfl_xor_sync(0xffffffffu, y, o);
+            }
+            if (lane == 0) Mp[((size_t)ei * nsite + site) * bb + a * b + c] = make_double2(x, y);
+        }
+    __syncwarp();
+    // window gradients: entries t = t0 + lane + 32 m, 3 per lane per round
+    for (int t0 = 0; t0 < Wmb; t0 += 96) {
+        Rl gur[3][B], gui[3][B], gsr[3][B], gsi[3][B];
+#pragma unroll
+        for (int m = 0; m < 3; m++)
+#pragma unroll
+            for (int a = 0; a < B; a++) { gur[m][a] = 0; gui[m][a] = 0; gsr[m][a] = 0; gsi[m][a] = 0; }
+        for (int q = 0; q < Q; q++) {
+            Rl f[3];
+#pragma unroll
+            for (int m = 0; m < 3; m++) {
+                const int t = t0 + lane + 32 * m;
+                f[m] = t < Wmb ? phT[(size_t)t * ADJ_QP + q] : (Rl)0;
+            }
+#pragma unroll
+            for (int a = 0; a < B; a++) {
+                if (a >= b) continue;
+                const Rl *u4 = ub + ((size_t)q * b + a) * 4;
+                const Rl x0 = u4[0], x1 = u4[1], x2 = u4[2], x3 = u4[3];
+#pragma unroll
+                for (int m = 0; m < 3; m++) {
+                    gur[m][a] += f[m] * x0; gui[m][a] += f[m] * x1;
+                    gsr[m][a] += f[m] * x2; gsi[m][a] += f[m] * x3;
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            const int t = t0 + lane + 32 * m;
+            if (t >= Wmb) continue;
+#pragma unroll
+            for (int a = 0; a < B; a++) {
+                if (a >= b) continue;
+                const size_t idx = (((size_t)ei * Wmb + t) * b + a) * nsite + site;
+                Ub[idx] = cmake<C>(gur[m][a], gui[m][a]);
+                Sb[idx] = cmake<C>(gsr[m][a], gsi[m][a]);
+            }
+        }
+    }
+}
+
+// Box gradient from the stored window gradients: for box point R and element (r1, r2),
+//   Gbar(R)[r1][r2] += sum_{imp, d} Ub[(d, r1-bs0)][r2] of site R - d      (r1 in the block)
+//                    + sum_{imp, d} Sb[(d, r2-bs0)][r1] of site -R - d     (r2 in the block)
+// over the sites inside the field of view.  grid (ceil(NB/128), NB, ne*b*b); thread = Y.
+template <class C>
+__global__ void __launch_bounds__(128) adj_gather_kernel(int b, int n, int w, int Rb, int NB, int W, int mb, int bs0, int nimp,
+                                                         const C *__restrict__ Ub, const C *__restrict__ Sb,
+                                                         double2 *__restrict__ gbox)
+{
+    const int yb = blockIdx.x * blockDim.x + threadIdx.x, xb = blockIdx.y;
+    const int bb = b * b;
+    const int e = blockIdx.z / bb, el = blockIdx.z - e * bb, r1 = el / b, r2 = el - r1 * b;
+    if (yb >= NB) return;
+    const int n2 = n >> 1, side = 2 * w + 1, nsite = n * n, Wmb = W * mb;
+    const int X = xb - Rb, Y = yb - Rb;
+    const int ou = r1 - bs0, os_ = r2 - bs0;
+    double sx = 0.0, sy = 0.0;
+    for (int imp = 0; imp < nimp; imp++) {
+        const int ei = e * nimp + imp;
+        for (int d = 0; d < W; d++) {
+            const int dx = d / side - w, dy = d % side - w;
+            if (ou >= 0 && ou < mb) {
+                const int i = X - dx + n2, j = Y - dy + n2;    // site R - d
+                if (i >= 0 && i < n && j >= 0 && j < n) {
+                    const C v = Ub[(((size_t)ei * Wmb + d * mb + ou) * b + r2) * nsite + (size_t)i * n + j];
+                    sx += (double)v.x; sy += (double)v.y;
+                }
+            }
+            if (os_ >= 0 && os_ < mb) {
+                const int i = -X - dx + n2, j = -Y - dy + n2;  // site -R - d
+                if (i >= 0 && i < n && j >= 0 && j < n) {
+                    const C v = Sb[(((size_t)ei * Wmb + d * mb + os_) * b + r1) * nsite + (size_t)i * n + j];
+                    sx += (double)v.x; sy += (double)v.y;
+                }
+            }
+        }
+    }
+    double2 *g = gbox + (((size_t)e * NB + xb) * NB + yb) * bb + el;
+    *g = make_double2(g->x + sx, g->y + sy);
+}
+
+// M[ei] = sum over sites of the per-site parts; one block per map
+__global__ void __launch_bounds__(256) adj_mreduce_kernel(int nsite, int bb, const double2 *__restrict__ Mp,
+                                                          double2 *__restrict__ M)
+{
+    __shared__ double2 red[8];
+    const int ei = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = 0; k < bb; k++) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int p = threadIdx.x; p < nsite; p += blockDim.x) s = cadd(s, Mp[((size_t)ei * nsite + p) * bb + k]);
+        for (int o = 16; o > 0; o >>= 1) {
+            s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+            s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+        }
+        if (lane == 0) red[warp] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double2 t = make_double2(0.0, 0.0);
+            for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) t = cadd(t, red[wv]);
+            M[(size_t)ei * bb + k] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// wsum[e][q] = sum over the impurities' maps and the sites of W at sub-pixel q = qx*os + qy
+// (map pixel (x, y) = (i*os + qx, j*os + qy)); grid (ceil(wn/16), ne*nimp), rows of 16
+__global__ void __launch_bounds__(256) adj_wsum_kernel(int wn, int os, int Q, int nimp, const float *__restrict__ wmap,
+                                                       double *__restrict__ wsum)
+{
+    __shared__ double acc[128];
+    const int ei = blockIdx.y, e = ei / nimp;
+    for (int k = threadIdx.x; k < Q; k += blockDim.x) acc[k] = 0.0;
     __syncthreads();
+    const int y0 = blockIdx.x * 16;
+    for (int y = y0; y < min(y0 + 16, wn); y++) {
+        const float *row = wmap + ((size_t)ei * wn + y) * wn;
+        const int qy = y % os;
+        for (int x = threadIdx.x; x < wn; x += blockDim.x) {
+            const float v = row[x];
+            if (v != 0.f) atomicAdd(&acc[(x % os) * os + qy], (double)v);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < Q; k += blockDim.x)
+        if (acc[k] != 0.0) atomicAdd(wsum + (size_t)e * Q + k, acc[k]);
+}
+
+// ------------------------------------------------------------------ 2. term1
+// rho has -term1, so Gbar(Delta)[o2][o1] += -i sum_q wsum(q) K(q, Delta, o1, o2) with the
+// energy-independent K = sum_{d1} phi_o1(q,d1) phi_o2(q,d1+Delta), tabulated once per call:
+// Kt[(Delta * mb*mb + o2*mb + o1) * Q + q]; grid (4w+1)^2 offsets Delta, threads over q.
+__global__ void __launch_bounds__(128) adj_kt_kernel(int w, int Q, int W, int mb, const double *__restrict__ phi,
+                                                     double *__restrict__ Kt)
+{
+    const int span = 4 * w + 1, side = 2 * w + 1;
+    const int rx = blockIdx.x / span - 2 * w, ry = blockIdx.x % span - 2 * w;
+    for (int q = threadIdx.x; q < Q; q += blockDim.x)
+        for (int o2 = 0; o2 < mb; o2++)
+            for (int o1 = 0; o1 < mb; o1++) {
+                double k = 0.0;
+                for (int d1 = 0; d1 < W; d1++) {
+                    const int x2 = d1 / side + rx, y2 = d1 % side + ry;   // window position of d2 = d1 + Delta
+                    if (x2 < 0 || x2 >= side || y2 < 0 || y2 >= side) continue;
+                    k += phi[((size_t)q * W + d1) * mb + o1] * phi[((size_t)q * W + x2 * side + y2) * mb + o2];
+                }
+                Kt[(((size_t)blockIdx.x * mb + o2) * mb + o1) * Q + q] = k;
+            }
+}
+
+// grid ((4w+1)^2 offsets Delta, ne); one thread per orbital pair
+__global__ void __launch_bounds__(128) adj_term1_kernel(int b, int w, int Rb, int NB, int Q, int mb, int bs0,
+                                                        const double *__restrict__ Kt, const double *__restrict__ wsum,
+                                                        double2 *__restrict__ gbox)
+{
+    const int e = blockIdx.y;
+    const int span = 4 * w + 1;
+    const int rx = blockIdx.x / span - 2 * w, ry = blockIdx.x % span - 2 * w;
+    const int bb = b * b;
     double2 *g = gbox + ((size_t)e * NB * NB + (size_t)(rx + Rb) * NB + (ry + Rb)) * bb;
     for (int t = threadIdx.x; t < mb * mb; t += blockDim.x) {
         const int o2 = t / mb, o1 = t % mb;
-        if (acc[t] != 0.0) atomicAdd(&g[(bs0 + o2) * b + (bs0 + o1)].y, -acc[t]);
+        const double *k = Kt + ((size_t)blockIdx.x * mb * mb + t) * Q;
+        const double *ws = wsum + (size_t)e * Q;
+        double acc = 0.0;
+        for (int q = 0; q < Q; q++) acc += ws[q] * k[q];
+        if (acc != 0.0) atomicAdd(&g[(bs0 + o2) * b + (bs0 + o1)].y, -acc);
     }
 }
 
@@ -309,11 +560,11 @@ __device__ void fft_minus(C *x, int kp, int logkp, const C *__restrict__ tw)
         if (r > t) { const C a = x[t]; x[t] = x[r]; x[r] = a; }
     }
     __syncthreads();
-    for (int len = 2; len <= kp; len <<= 1) {
-        const int hl = len >> 1, step = kp / len;
+    for (int l = 1; l <= logkp; l++) {
+        const int len = 1 << l, hl = len >> 1, lstep = logkp - l;   // step = kp / len
         for (int t = threadIdx.x; t < (kp >> 1); t += blockDim.x) {
-            const int kk = t % hl, idx = (t / hl) * len + kk;
-            C wv = __ldg(tw + kk * step);
+            const int kk = t & (hl - 1), idx = ((t >> (l - 1)) << l) + kk;
+            C wv = __ldg(tw + (kk << lstep));
             wv.y = -wv.y;
             const C u = x[idx], v = cmul(x[idx + hl], wv);
             x[idx] = cadd(u, v);
@@ -388,7 +639,7 @@ __global__ void __launch_bounds__(256) adj_rows_kernel(int kp, int logkp, int NB
 // ------------------------------------------------------------------ 6. hoppings
 // grid (nR, chunks); out[r][0][pq] = sum_k e^{-i th_r(k)} Hbar(k)[pq] (normal terms),
 // out[r][1][pq] = sum_k e^{+i th_r(k)} Hbar(k)[pq] (conjugated terms), th = 2 pi (Rx i + Ry j)/kp
-__global__ void __launch_bounds__(256) adj_hop_kernel(int b, int kp, const int32_t *__restrict__ R,
+__global__ void __launch_bounds__(256) adj_hop_kernel(int b, int kp, int logkp, const int32_t *__restrict__ R,
                                                       const double2 *__restrict__ tw, const double2 *__restrict__ hbar,
                                                       double2 *__restrict__ out)
 {
@@ -401,9 +652,10 @@ __global__ void __launch_bounds__(256) adj_hop_kernel(int b, int kp, const int32
     for (int pq = 0; pq < bb; pq++) {
         double2 sn = make_double2(0.0, 0.0), sa = make_double2(0.0, 0.0);
         for (long long k = (long long)blockIdx.y * blockDim.x + threadIdx.x; k < nk; k += (long long)gridDim.y * blockDim.x) {
-            const long long i = k / kp, j = k - i * kp;
-            long long mm = (Rx * i + Ry * j) % kp;
-            if (mm < 0) mm += kp;
+            // kp is a power of two: k = i*kp + j, and the phase index (Rx i + Ry j) mod kp is
+            // the low bits of the product (two's complement)
+            const long long i = k >> logkp, j = k & (kp - 1);
+            const long long mm = (Rx * i + Ry * j) & (long long)(kp - 1);
             const double2 ph = __ldg(tw + mm);
             const double2 h = hbar[(size_t)pq * nk + k];
             sn = cadd(sn, cmul(cconj(ph), h));
@@ -431,11 +683,34 @@ template <int B, class C>
 static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>::type *phi, const C *box,
                               const float *wmap, AdjWorkspace &aw)
 {
-    dim3 grid((unsigned)(h->n * h->n), (unsigned)(ne * h->nimp));
-    const size_t smem = 4 * 128 * (size_t)h->b * sizeof(typename real_of<C>::type);
-    adj_contract_kernel<B, C><<<grid, 128, smem, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp, h->mb,
-                                                           h->blk_start[0], phi, box, h->ws.T, wmap, aw.gbox, aw.M, aw.wsum);
-    h->launches++;
+    const int nsite = h->n * h->n, bb = h->b * h->b;
+    dim3 grid((unsigned)nsite, (unsigned)(ne * h->nimp));
+    const size_t smem = 4 * 128 * (size_t)h->b * sizeof(typename real_of<C>::type) + 4 * sizeof(double2) * bb;
+    C *Ub = reinterpret_cast<C *>(aw.win);
+    C *Sb = Ub + (size_t)ne * h->nimp * h->W * h->mb * h->b * nsite;
+    using Rl = typename real_of<C>::type;
+    const size_t wsm = sizeof(Rl) * ((size_t)h->W * h->mb * ADJ_QP + 4 * 128 * (size_t)h->b * 4);
+    bool warp_form = false;
+    if constexpr (B <= 4) {
+        // one warp per site when the orbital table and the four warps' ubar / sbar rows fit
+        if (wsm <= 200 * 1024 &&
+            cudaFuncSetAttribute(adj_contract_warp_kernel<B, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm) ==
+                cudaSuccess) {
+            adj_contract_warp_kernel<B, C><<<dim3(cdiv(nsite, 4), (unsigned)(ne * h->nimp)), 128, wsm, h->stream>>>(
+                h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp, h->mb, h->blk_start[0], phi, box, h->ws.T, wmap,
+                Ub, Sb, aw.Mp);
+            warp_form = true;
+        }
+    }
+    if (!warp_form)
+        adj_contract_kernel<B, C><<<grid, 128, smem, h->stream>>>(h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp,
+                                                               h->mb, h->blk_start[0], phi, box, h->ws.T, wmap, Ub, Sb, aw.Mp);
+    adj_gather_kernel<C><<<dim3(cdiv(h->NB, 128), (unsigned)h->NB, (unsigned)(ne * bb)), 128, 0, h->stream>>>(
+        h->b, h->n, h->w, h->Rb, h->NB, h->W, h->mb, h->blk_start[0], h->nimp, Ub, Sb, aw.gbox);
+    adj_mreduce_kernel<<<(unsigned)(ne * h->nimp), 256, 0, h->stream>>>(nsite, bb, aw.Mp, aw.M);
+    adj_wsum_kernel<<<dim3(cdiv(h->wn, 16), (unsigned)(ne * h->nimp)), 256, 0, h->stream>>>(h->wn, h->os, h->Q, h->nimp,
+                                                                                             wmap, aw.wsum);
+    h->launches += 4;
 }
 
 template <class C>
@@ -458,9 +733,10 @@ void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorks
     if (h->precision == CQPI_PREC_FP64) dispatch_contract<double2>(h, ne, h->d_phi, h->ws.box, wmap, aw);
     else dispatch_contract<float2>(h, ne, h->d_phi32, h->ws.box32, wmap, aw);
     const int span = 4 * h->w + 1;
-    adj_term1_kernel<<<dim3(span * span, ne), 128, 0, h->stream>>>(h->b, h->w, h->Rb, h->NB, h->Q, h->W, h->mb,
-                                                                   h->blk_start[0], h->d_phi, aw.wsum, aw.gbox);
-    h->launches++;
+    adj_kt_kernel<<<span * span, 128, 0, h->stream>>>(h->w, h->Q, h->W, h->mb, h->d_phi, aw.kt);
+    adj_term1_kernel<<<dim3(span * span, ne), 128, 0, h->stream>>>(h->b, h->w, h->Rb, h->NB, h->Q, h->mb,
+                                                                   h->blk_start[0], aw.kt, aw.wsum, aw.gbox);
+    h->launches += 2;
     const int nt = ne * h->nimp;
     if (h->precision == CQPI_PREC_FP64)
         adj_tv_kernel<double2><<<cdiv(nt, 64), 64, 0, h->stream>>>(h->b, h->NB, h->Rb, h->nimp, ne, h->ws.box, h->d_V,
@@ -479,39 +755,42 @@ static int ilog2_exact(int v)
 }
 
 template <int B>
-static void launch_kacc_t(cqpi_handle *h, double omega, AdjWorkspace &aw)
+static void launch_kacc_t(cqpi_handle *h, int ne, const double *omegas, AdjWorkspace &aw)
 {
     const long long nk = (long long)h->kp * h->kp;
     const unsigned grid = (unsigned)cdiv(nk, 128);
     const float2 *gk32 = reinterpret_cast<const float2 *>(aw.gk);
     if constexpr (B <= 6) {
         if (h->precision == CQPI_PREC_FP64)
-            adj_kacc_kernel<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec,
+            adj_kacc_kernel<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval, h->d_evec,
                                                                      aw.gk, aw.C);
         else
-            adj_kacc_kernel<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval, h->d_evec32,
+            adj_kacc_kernel<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval, h->d_evec32,
                                                                     gk32, aw.C);
     } else {
         if (h->precision == CQPI_PREC_FP64)
-            adj_kacc_kernel_wide<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval,
+            adj_kacc_kernel_wide<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval,
                                                                           h->d_evec, aw.gk, aw.C);
         else
-            adj_kacc_kernel_wide<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, omega, h->eta, h->d_eval,
+            adj_kacc_kernel_wide<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval,
                                                                          h->d_evec32, gk32, aw.C);
     }
     h->launches++;
 }
 
-void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw)
+// Gbar(k) of energy e of the batch (box -> k-grid transform) into slot e of aw.gk
+void launch_adj_kspace(cqpi_handle *h, int e, AdjWorkspace &aw)
 {
     const int kp = h->kp, logkp = ilog2_exact(kp), bb = h->b * h->b;
+    const size_t nk = (size_t)kp * kp;
     const double2 *gbe = aw.gbox + (size_t)e * h->NB * h->NB * bb;
     if (h->precision == CQPI_PREC_FP64) {
         const size_t smem = sizeof(double2) * kp;
         adj_cols_kernel<double2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw,
                                                                             aw.A);
         adj_rows_kernel<double2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
-                                                                         1.0 / ((double)kp * kp), aw.A, h->d_tw, aw.gk);
+                                                                         1.0 / ((double)kp * kp), aw.A, h->d_tw,
+                                                                         aw.gk + (size_t)e * bb * nk);
     } else {
         // the mixed handle: the transform and the per-k rotation in FP32, in the same buffers
         const size_t smem = sizeof(float2) * kp;
@@ -519,18 +798,24 @@ void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw)
         adj_cols_kernel<float2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw32,
                                                                            A32);
         adj_rows_kernel<float2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
-                                                                        1.0 / ((double)kp * kp), A32, h->d_tw32, gk32);
+                                                                        1.0 / ((double)kp * kp), A32, h->d_tw32,
+                                                                        gk32 + (size_t)e * bb * nk);
     }
     h->launches += 2;
+}
+
+// C(k) += the resolvent brackets of the ne energies whose Gbar(k) fill the slots of aw.gk
+void launch_adj_kacc(cqpi_handle *h, int ne, const double *omegas, AdjWorkspace &aw)
+{
     const int b = h->b;
-    if (b <= 1) launch_kacc_t<1>(h, omega, aw);
-    else if (b <= 2) launch_kacc_t<2>(h, omega, aw);
-    else if (b <= 3) launch_kacc_t<3>(h, omega, aw);
-    else if (b <= 4) launch_kacc_t<4>(h, omega, aw);
-    else if (b <= 6) launch_kacc_t<6>(h, omega, aw);
-    else if (b <= 8) launch_kacc_t<8>(h, omega, aw);
-    else if (b <= 12) launch_kacc_t<12>(h, omega, aw);
-    else launch_kacc_t<16>(h, omega, aw);
+    if (b <= 1) launch_kacc_t<1>(h, ne, omegas, aw);
+    else if (b <= 2) launch_kacc_t<2>(h, ne, omegas, aw);
+    else if (b <= 3) launch_kacc_t<3>(h, ne, omegas, aw);
+    else if (b <= 4) launch_kacc_t<4>(h, ne, omegas, aw);
+    else if (b <= 6) launch_kacc_t<6>(h, ne, omegas, aw);
+    else if (b <= 8) launch_kacc_t<8>(h, ne, omegas, aw);
+    else if (b <= 12) launch_kacc_t<12>(h, ne, omegas, aw);
+    else launch_kacc_t<16>(h, ne, omegas, aw);
 }
 
 template <int B>
@@ -557,7 +842,8 @@ void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw)
     else launch_hbar_t<16>(h, aw);
     if (h->nR > 0) {
         const int chunks = std::max(1, std::min(64, (int)(((long long)h->kp * h->kp) / (256 * 64))));
-        adj_hop_kernel<<<dim3(h->nR, chunks), 256, 0, h->stream>>>(b, h->kp, h->d_R, h->d_tw, aw.gk, aw.gR);
+        adj_hop_kernel<<<dim3(h->nR, chunks), 256, 0, h->stream>>>(b, h->kp, ilog2_exact(h->kp), h->d_R, h->d_tw, aw.gk,
+                                                                   aw.gR);
         h->launches++;
     }
 }

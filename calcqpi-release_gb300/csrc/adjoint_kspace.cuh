@@ -4,63 +4,103 @@
 // for 8 to 16 bands (adj_kacc_kernel_wide, adj_hbar_kernel_wide), whose matrices live in local
 // memory either way.  The includer defines CQPI_ADJ_KACC, CQPI_ADJ_HBAR (the kernels' names)
 // and CQPI_ADJ_UNROLL (the loop pragma).
-// C(k) += F* (U^H Gbar(k) U) F*, F = diag(1/(omega + i eta - eps_n)); one thread per k
+// C(k) += sum_e F_e* (U^H Gbar_e(k) U) F_e*, F_e = diag(1/(omega_e + i eta - eps_n)), over the ne
+// energies of a batch (Gbar_e(k) at gk + e * b*b*nk); one thread per k.  Up to 3 bands the
+// energy sum is held in FP64 registers and C(k) is read and written once per batch; more bands
+// add each energy's bracket to C(k) in memory.
 // C: the working precision (double2, or float2 for the mixed handle: eigenvectors and Gbar(k)
 // in FP32, the pole factors from the FP64 eigenvalues, C(k) accumulated in FP64)
 template <int B, class C>
-__global__ void __launch_bounds__(128) CQPI_ADJ_KACC(int b, long long nk, double omega, double eta,
-                                                       const double *__restrict__ eval, const C *__restrict__ evec,
-                                                       const C *__restrict__ gk, double2 *__restrict__ Cacc)
+__global__ void __launch_bounds__(128) CQPI_ADJ_KACC(int b, long long nk, int ne, const double *__restrict__ omegas,
+                                                       double eta, const double *__restrict__ eval,
+                                                       const C *__restrict__ evec, const C *__restrict__ gk,
+                                                       double2 *__restrict__ Cacc)
 {
+    constexpr bool REG = B <= 3;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nk) return;
     C U[B][B], G[B][B], X[B][B], f[B];
+    double ev[B];
+    double2 acc[REG ? B : 1][REG ? B : 1];
 CQPI_ADJ_UNROLL
-    for (int n = 0; n < B; n++) {
-        if (n < b) {
-            const double dr = omega - eval[(size_t)n * nk + k];
-            const double den = dr * dr + eta * eta;
-            f[n] = cmake<C>(dr / den, eta / den);   // conj(1/(dr + i eta))
-        }
-    }
+    for (int n = 0; n < B; n++)
+        if (n < b) ev[n] = eval[(size_t)n * nk + k];
 CQPI_ADJ_UNROLL
     for (int o = 0; o < B; o++)
 CQPI_ADJ_UNROLL
         for (int n = 0; n < B; n++)
-            if (o < b && n < b) {
-                U[o][n] = evec[(size_t)(o * b + n) * nk + k];
-                G[o][n] = gk[(size_t)(o * b + n) * nk + k];
+            if (o < b && n < b) U[o][n] = evec[(size_t)(o * b + n) * nk + k];
+    if constexpr (REG) {
+CQPI_ADJ_UNROLL
+        for (int n = 0; n < B; n++)
+CQPI_ADJ_UNROLL
+            for (int m = 0; m < B; m++) acc[n][m] = make_double2(0.0, 0.0);
+    }
+    const size_t plane = (size_t)b * b * nk;
+    for (int e = 0; e < ne; e++) {
+        const double omega = omegas[e];
+CQPI_ADJ_UNROLL
+        for (int n = 0; n < B; n++) {
+            if (n < b) {
+                // conj(1/(dr + i eta)); the pole distance in FP64, the reciprocal in the
+                // bracket's precision (an FP32 reciprocal for the mixed handle)
+                const double dr = omega - ev[n];
+                const double den = dr * dr + eta * eta;
+                using R = typename real_of<C>::type;
+                const R inv = (R)1 / (R)den;
+                f[n] = cmake<C>((R)dr * inv, (R)eta * inv);
             }
-    // X = Gbar U
-CQPI_ADJ_UNROLL
-    for (int o = 0; o < B; o++)
-CQPI_ADJ_UNROLL
-        for (int m = 0; m < B; m++) {
-            if (o >= b || m >= b) continue;
-            C s = cmake<C>(0.0, 0.0);
-CQPI_ADJ_UNROLL
-            for (int a = 0; a < B; a++)
-                if (a < b) s = cadd(s, cmul(G[o][a], U[a][m]));
-            X[o][m] = s;
         }
-    // C += f*_n (U^H X)_nm f*_m
 CQPI_ADJ_UNROLL
-    for (int n = 0; n < B; n++)
+        for (int o = 0; o < B; o++)
 CQPI_ADJ_UNROLL
-        for (int m = 0; m < B; m++) {
-            if (n >= b || m >= b) continue;
-            C s = cmake<C>(0.0, 0.0);
+            for (int n = 0; n < B; n++)
+                if (o < b && n < b) G[o][n] = gk[e * plane + (size_t)(o * b + n) * nk + k];
+        // X = Gbar U
 CQPI_ADJ_UNROLL
-            for (int o = 0; o < B; o++)
-                if (o < b) {
-                    C un = U[o][n];
-                    un.y = -un.y;
-                    s = cadd(s, cmul(un, X[o][m]));
+        for (int o = 0; o < B; o++)
+CQPI_ADJ_UNROLL
+            for (int m = 0; m < B; m++) {
+                if (o >= b || m >= b) continue;
+                C s = cmake<C>(0.0, 0.0);
+CQPI_ADJ_UNROLL
+                for (int a = 0; a < B; a++)
+                    if (a < b) s = cadd(s, cmul(G[o][a], U[a][m]));
+                X[o][m] = s;
+            }
+        // C += f*_n (U^H X)_nm f*_m
+CQPI_ADJ_UNROLL
+        for (int n = 0; n < B; n++)
+CQPI_ADJ_UNROLL
+            for (int m = 0; m < B; m++) {
+                if (n >= b || m >= b) continue;
+                C s = cmake<C>(0.0, 0.0);
+CQPI_ADJ_UNROLL
+                for (int o = 0; o < B; o++)
+                    if (o < b) {
+                        C un = U[o][n];
+                        un.y = -un.y;
+                        s = cadd(s, cmul(un, X[o][m]));
+                    }
+                s = cmul(cmul(f[n], s), f[m]);
+                if constexpr (REG) {
+                    acc[n][m] = cadd(acc[n][m], to_d2(s));
+                } else {
+                    double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
+                    *c = cadd(*c, to_d2(s));
                 }
-            s = cmul(cmul(f[n], s), f[m]);
-            double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
-            *c = cadd(*c, to_d2(s));
-        }
+            }
+    }
+    if constexpr (REG) {
+CQPI_ADJ_UNROLL
+        for (int n = 0; n < B; n++)
+CQPI_ADJ_UNROLL
+            for (int m = 0; m < B; m++) {
+                if (n >= b || m >= b) continue;
+                double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
+                *c = cadd(*c, acc[n][m]);
+            }
+    }
 }
 
 // Hbar(k) = U C(k) U^H, written over gk

@@ -88,9 +88,14 @@ struct AdjWorkspace {
     double *wsum = nullptr;    // [E][Q]            sum_p W
     double2 *gV = nullptr;     // [nimp][b*b]       dL/dV
     double2 *A = nullptr;      // [b*b][NB][kp]     column pass of the box -> k transform
-    double2 *gk = nullptr;     // [b*b][nk]         dL/dG0(k), then dL/dH(k)
+    double2 *gk = nullptr;     // [E][b*b][nk]      dL/dG0(k) per energy of a batch (in the handle's
+                               // precision), then [b*b][nk] dL/dH(k) (FP64)
     double2 *C = nullptr;      // [b*b][nk]         eigenbasis accumulator over energies
     double2 *gR = nullptr;     // [nR][2][b*b]      dL/dtn, dL/dta per unique R
+    void *win = nullptr;       // [2][E][nimp][W*mb][b][n*n] window gradients of every site (u, s;
+                               // float2 for the mixed handle, double2 for the FP64 handle)
+    double2 *Mp = nullptr;     // [E][nimp][n*n][b*b] per-site parts of M
+    double *kt = nullptr;      // [(4w+1)^2][mb*mb][Q] the term1 kernel of the orbitals
 };
 
 // Hopping terms of the surface / bulk Green's function on the device: three sets (surface
@@ -291,7 +296,8 @@ void tc_build_a(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint
 void tc_build_a_window(cqpi_handle *h, const std::vector<double> &phi, std::vector<uint16_t> &img);
 // adjoint.cu
 void launch_adj_energy_batch(cqpi_handle *h, int ne, const float *wmap, AdjWorkspace &aw);
-void launch_adj_kspace(cqpi_handle *h, int e, double omega, AdjWorkspace &aw);
+void launch_adj_kspace(cqpi_handle *h, int e, AdjWorkspace &aw);
+void launch_adj_kacc(cqpi_handle *h, int ne, const double *omegas, AdjWorkspace &aw);
 void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw);
 // surface.cu
 void launch_surface_mats(cqpi_handle *h);
