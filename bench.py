@@ -627,6 +627,15 @@ def adjoint_rate(steps, analysis=False):
         x_start = np.concatenate([fm.p0, fm.V0.real.reshape(-1)])
         x_fit = np.concatenate([p, np.asarray(V).reshape(-1)])
         out["gauss_newton"] = F.identifiability(JtJ, x_true, x_start, x_fit)
+        # the same least-squares problem solved by Gauss-Newton steps (adjoint gradient, J^T J
+        # from differences of the maps) from the same start, for comparison with Adam
+        t0 = time.perf_counter()
+        x_gn, gn_losses = F.gauss_newton_fit(fm, target, x_start, iters=6)
+        out["gauss_newton_fit"] = {"iterations": len(gn_losses) - 1, "seconds": time.perf_counter() - t0,
+                                   "losses": gn_losses,
+                                   "param_rel_err_end": float(np.linalg.norm(x_gn[:len(fm.p0)] - p_true) /
+                                                              np.linalg.norm(p_true)),
+                                   "per_direction": F.identifiability(JtJ, x_true, x_start, x_gn)}
     fm.close()
     return out
 

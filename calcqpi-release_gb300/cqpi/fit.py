@@ -193,3 +193,40 @@ def identifiability(JtJ, x_true, x_start, x_fit):
             "start_error_per_direction": np.abs(d0).tolist(),
             "fit_error_per_direction": np.abs(d1).tolist(),
             "fit_over_start_per_direction": (np.abs(d1) / np.maximum(np.abs(d0), 1e-300)).tolist()}
+
+
+def loss_at(fit, x, target):
+    """The QPI loss (FP64 transform) at x = (p, V)."""
+    npp = len(fit.p0)
+    m = fit.maps(x[:npp], x[npp:].reshape(fit.bands, fit.bands))
+    return float(qpi_loss(m, target))
+
+
+def gauss_newton_fit(fit, target, x0, iters=6, log=None):
+    """Levenberg-Marquardt iterations on x = (p, V) for the QPI loss: J^T J from central
+    differences of the maps (gauss_newton), the gradient 2 J^T r from the adjoint (gradient),
+    the step -(J^T J + mu lambda_max I)^-1 J^T r with the damping mu chosen among 10^-8 ..
+    10^-1 as the one that lowers the loss most (the loss is far from quadratic: sharp poles
+    and |FFT| magnitudes); stops when no damping lowers the loss.  Returns (x, losses)."""
+    npp = len(fit.p0)
+    b = fit.bands
+    x = np.asarray(x0, np.float64).copy()
+    losses = [loss_at(fit, x, target)]
+    for it in range(iters):
+        JtJ, _ = gauss_newton(fit, x[:npp], x[npp:].reshape(b, b))
+        _, gp, gV = gradient(fit, x[:npp], x[npp:].reshape(b, b), target)
+        g = np.concatenate([gp, np.asarray(gV).reshape(-1)])
+        lam_max = float(np.linalg.eigvalsh(JtJ).max())
+        best = None
+        for mu in (1e-8, 1e-6, 1e-4, 1e-3, 1e-2, 1e-1):
+            step = -np.linalg.solve(JtJ + mu * lam_max * np.eye(len(x)), 0.5 * g)
+            l = loss_at(fit, x + step, target)
+            if l < losses[-1] and (best is None or l < best[0]):
+                best = (l, step)
+        if best is None:
+            break
+        x = x + best[1]
+        losses.append(best[0])
+        if log is not None:
+            log(it, best[0])
+    return x, losses

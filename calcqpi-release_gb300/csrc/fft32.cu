@@ -354,6 +354,105 @@ __global__ void __launch_bounds__(MAXT) g0_rowfft_reg_kernel(int b, int NB, int 
     }
 }
 
+// Persistent form of the fused G0 build + four-step row transform for up to 3 bands, where
+// every plane of a k_x row fits one shared-memory group (np = b^2, or the b(b+1)/2 upper
+// planes under reciprocity; one thread per (plane, n1) / (plane, k2) task).  The grid is the
+// number of blocks resident on the device; block c takes the (row i, energy e) items
+// [c * items / grid, (c + 1) * items / grid) in row-major order, so there is no partial last
+// wave and the blocks running at one time read the eigen data of a few neighbouring rows
+// (L1 / L2 hits).  Band count B as a template parameter keeps the G0 build's matrices in the
+// registers they need, so three blocks fit per SM.  The first pass's twiddles are stored as
+// [k2][n1] (a warp, consecutive n1, reads consecutive entries).
+template <int N1, int N2, int B>
+__global__ void __launch_bounds__(B * B * (N1 > N2 ? N1 : N2), (B == 3 ? 2 : 1))
+g0_rowfft_pk_kernel(int NB, int Rb, int tr, double eta, const double *__restrict__ energies, int ne,
+                    const float2 *__restrict__ eval_g, const float2 *__restrict__ evec_g,
+                    const float2 *__restrict__ tw, float2 *__restrict__ half)
+{
+    constexpr int KP = N1 * N2;
+    constexpr int PLEN = KP + KP / 32 + 1;
+    extern __shared__ __align__(16) float2 sm[];
+    const int np = tr ? (B * (B + 1)) / 2 : B * B;
+    float2 *tw2 = sm + (size_t)np * PLEN;        // [k2][n1] = e^{+2 pi i n1 k2 / kp}
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) {
+        const int k2 = t / N1, n1 = t - k2 * N1;
+        tw2[t] = tw[(n1 * k2) & (KP - 1)];
+    }
+    const long long nk = (long long)KP * KP;
+    const long long items = (long long)KP * ne;
+    const long long t0 = items * blockIdx.x / gridDim.x, t1 = items * (blockIdx.x + 1) / gridDim.x;
+    const float et = (float)eta;
+    for (long long t = t0; t < t1; t++) {
+        const int i = (int)(t / ne), e = (int)(t - (long long)i * ne);
+        const float2 *eval = eval_g + (size_t)i * KP;
+        const float2 *evec = evec_g + (size_t)i * KP;
+        const double om = energies[e];
+        // omega - eps in FP32 from float pairs (see g0_rowfft_reg_kernel)
+        const float om_hi = (float)om, om_lo = (float)(om - (double)om_hi);
+        __syncthreads();   // the previous item's second pass has read the planes (and tw2 is set)
+        for (int j = threadIdx.x; j < KP; j += blockDim.x) {
+            const int pos = pad32(j);
+            float2 f[B], U[B][B];
+#pragma unroll
+            for (int n = 0; n < B; n++) {
+                const float2 ev = eval[(size_t)n * nk + j];
+                const float dr = (om_hi - ev.x) + (om_lo - ev.y);
+                const float inv = __frcp_rn(dr * dr + et * et);
+                f[n] = make_float2(dr * inv, -et * inv);
+            }
+#pragma unroll
+            for (int o = 0; o < B; o++)
+#pragma unroll
+                for (int n = 0; n < B; n++) U[o][n] = evec[(size_t)(o * B + n) * nk + j];
+#pragma unroll
+            for (int o = 0; o < B; o++) {
+                float2 x[B];
+#pragma unroll
+                for (int n = 0; n < B; n++) x[n] = cmul(U[o][n], f[n]);
+#pragma unroll
+                for (int a = 0; a < B; a++) {
+                    if (tr && a < o) continue;
+                    float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int n = 0; n < B; n++) {
+                        s.x += x[n].x * U[a][n].x + x[n].y * U[a][n].y;
+                        s.y += x[n].y * U[a][n].x - x[n].x * U[a][n].y;
+                    }
+                    sm[(size_t)(tr ? tri_index(B, o, a) : o * B + a) * PLEN + pos] = s;
+                }
+            }
+        }
+        __syncthreads();
+        // first pass: (plane, n1) tasks, length-N2 transforms over n2, twiddle
+        for (int task = threadIdx.x; task < np * N1; task += blockDim.x) {
+            const int q = task / N1, n1 = task - q * N1;
+            float2 *a = sm + (size_t)q * PLEN;
+            float2 x[N2];
+#pragma unroll
+            for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
+            fft_reg<N2>(x);
+#pragma unroll
+            for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tw2[k2 * N1 + n1]);
+        }
+        __syncthreads();
+        // second pass: (plane, k2) tasks, length-N1 transforms over n1, pruned stores
+        for (int task = threadIdx.x; task < np * N2; task += blockDim.x) {
+            const int q = task / N2, k2 = task - q * N2;
+            const float2 *a = sm + (size_t)q * PLEN;
+            float2 x[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
+            fft_reg<N1>(x);
+            float2 *dst = half + (((size_t)e * np + q) * KP + i) * NB;
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) {
+                const int yb = (k2 + N2 * k1 + Rb) & (KP - 1);
+                if (yb < NB) dst[yb] = x[k1];
+            }
+        }
+    }
+}
+
 // Pass 1 of the unfused mixed path (more than 4 bands: G0(k) planes already in HBM, written
 // by greens_k_kernel): RPC rows r = (energy * b^2 + plane) * kp + i per CTA, loaded with
 // coalesced row reads, then the four-step register transform along j and the pruned stores
@@ -368,7 +467,10 @@ __global__ void __launch_bounds__(256) rowfft_reg_g0k_kernel(int NB, int Rb, lon
     constexpr int PLEN = KP + KP / 32 + 1;
     extern __shared__ __align__(16) float2 sm[];
     float2 *tws = sm + (size_t)RPC * PLEN;
-    for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) {   // [k2][n1], as in colfft_reg_kernel
+        const int k2 = t / N1, n1 = t - k2 * N1;
+        tws[t] = tw[(n1 * k2) & (KP - 1)];
+    }
     const long long r0 = (long long)blockIdx.x * RPC;
     for (int idx = threadIdx.x; idx < RPC * KP; idx += blockDim.x) {
         const int rr = idx / KP, j = idx - rr * KP;
@@ -383,7 +485,7 @@ __global__ void __launch_bounds__(256) rowfft_reg_g0k_kernel(int NB, int Rb, lon
         for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
         fft_reg<N2>(x);
 #pragma unroll
-        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[(n1 * k2) & (KP - 1)]);
+        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[k2 * N1 + n1]);
     }
     __syncthreads();
     for (int task = threadIdx.x; task < RPC * N2; task += blockDim.x) {
@@ -421,7 +523,12 @@ __global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int b, 
     const int bb = b * b;
     int po = pl / b, pa = pl - po * b;          // the plane's orbitals (o, a)
     if (tr) tri_plane(b, pl, po, pa);
-    for (int t = threadIdx.x; t < KP; t += blockDim.x) tws[t] = tw[t];
+    // first-pass twiddles as [k2][n1] = e^{+2 pi i n1 k2 / kp}: a warp (consecutive n1) reads
+    // consecutive entries
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) {
+        const int k2 = t / N1, n1 = t - k2 * N1;
+        tws[t] = tw[(n1 * k2) & (KP - 1)];
+    }
     const float2 *src = half + ((size_t)e * np + pl) * (size_t)KP * NB;
     for (int idx = threadIdx.x; idx < KP * NC; idx += blockDim.x) {
         const int i = idx / NC, c = idx - i * NC, yb = yb0 + c;
@@ -436,7 +543,7 @@ __global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int b, 
         for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
         fft_reg<N2>(x);
 #pragma unroll
-        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[(n1 * k2) & (KP - 1)]);
+        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[k2 * N1 + n1]);
     }
     __syncthreads();
     float mx = 0.0f;
@@ -643,6 +750,37 @@ static void launch_rowfft_reg_t(cqpi_handle *h, int ne, const double *d_energies
         h->ws.half32);
 }
 
+// shared memory of the persistent row transform at kp = 1024: np planes and the twiddles
+static size_t rowfft_pk_smem(int np) { return 8 * ((size_t)np * (1024 + 1024 / 32 + 1) + 1024); }
+
+// the persistent row transform (kp = 1024, up to 3 bands); CQPI_ROWFFT=classic keeps the
+// one-block-per-row kernel
+static bool rowfft_pk_ok(const cqpi_handle *h)
+{
+    const char *f = getenv("CQPI_ROWFFT");
+    return h->kp == 1024 && h->b <= 3 && h->NB <= h->kp && !(f && !strcmp(f, "classic"));
+}
+
+template <int B>
+static void launch_rowfft_pk(cqpi_handle *h, int ne, const double *d_energies)
+{
+    const int np = rowfft_planes(h);
+    const int tr = np != B * B ? 1 : 0;
+    const int threads = np * 32;
+    const size_t smem = rowfft_pk_smem(np);
+    // resident blocks per SM for this block size and shared memory (same on every GB300)
+    static int per_sm[2][4] = {};
+    int &r = per_sm[tr][B];
+    if (r == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, g0_rowfft_pk_kernel<32, 32, B>, threads, smem) !=
+                       cudaSuccess || r < 1))
+        r = 1;
+    const long long items = 1024LL * ne;
+    const int grid = (int)std::min<long long>(items, (long long)h->num_sms * r);
+    g0_rowfft_pk_kernel<32, 32, B><<<grid, threads, smem, h->stream>>>(h->NB, h->Rb, tr, h->eta, d_energies, ne,
+                                                                       h->d_eval32, h->d_evec32, h->d_tw32,
+                                                                       h->ws.half32);
+}
+
 static cudaError_t configure_rowfft_reg(cqpi_handle *h)
 {
     // the largest launch: every plane, or the reciprocity planes with the eigen cache
@@ -652,7 +790,17 @@ static cudaError_t configure_rowfft_reg(cqpi_handle *h)
     case 128: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<8, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 256: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 512: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    case 1024: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 32, 4, 288>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 1024: {
+        // the persistent kernel (up to 3 bands): every plane (at most 9) plus the twiddles
+        if (h->b <= 3) {
+            const int pk = (int)rowfft_pk_smem(9);
+            cudaError_t e = cudaFuncSetAttribute(g0_rowfft_pk_kernel<32, 32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pk);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(g0_rowfft_pk_kernel<32, 32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pk);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(g0_rowfft_pk_kernel<32, 32, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pk);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 32, 4, 288>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    }
     case 2048: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<32, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     case 4096: return cudaFuncSetAttribute(g0_rowfft_reg_kernel<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
@@ -754,7 +902,15 @@ static void launch_rowfft_reg(cqpi_handle *h, int ne, const double *d_energies)
     case 128: launch_rowfft_reg_t<8, 16>(h, ne, d_energies); break;
     case 256: launch_rowfft_reg_t<16, 16>(h, ne, d_energies); break;
     case 512: launch_rowfft_reg_t<16, 32>(h, ne, d_energies); break;
-    case 1024: launch_rowfft_reg_t<32, 32, 288>(h, ne, d_energies); break;
+    case 1024:
+        if (rowfft_pk_ok(h)) {
+            if (h->b == 1) launch_rowfft_pk<1>(h, ne, d_energies);
+            else if (h->b == 2) launch_rowfft_pk<2>(h, ne, d_energies);
+            else launch_rowfft_pk<3>(h, ne, d_energies);
+        } else {
+            launch_rowfft_reg_t<32, 32, 288>(h, ne, d_energies);
+        }
+        break;
     case 2048: launch_rowfft_reg_t<32, 64>(h, ne, d_energies); break;
     case 4096: launch_rowfft_reg_t<64, 64>(h, ne, d_energies); break;
     }

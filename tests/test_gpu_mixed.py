@@ -145,6 +145,36 @@ def test_register_row_fft_matches_radix2(built_lib, kp, lattice, monkeypatch):
     assert np.abs(a - b).max() <= 2e-6 * np.abs(b).max()
 
 
+@pytest.mark.parametrize("bands,real", [(1, True), (2, True), (3, True), (3, False)])
+def test_persistent_row_fft_matches_per_row_kernel(built_lib, bands, real, monkeypatch):
+    """kp = 1024, up to 3 bands: the persistent G0 + row transform (a resident grid walking
+    (row, energy) items) vs the one-block-per-row kernel (CQPI_ROWFFT=classic), with the
+    reciprocity planes (real hoppings) and with all b^2 planes (hoppings given a complex
+    phase e^{i theta.R}, which keeps H Hermitian)."""
+    import cqpi
+    from cqpi import workloads as W
+    terms = {}
+    for R, M in W.t2g_c2().terms().items():
+        ph = 1.0 if real else np.exp(1j * (0.3 * R[0] - 0.2 * R[1]))
+        terms[R] = M[:bands, :bands] * ph
+    m = W._from_terms(terms, bands, "t2g subset")
+    wf = W.t2g_orbitals_c2(2, 3)[:bands]
+
+    def box(classic):
+        if classic:
+            monkeypatch.setenv("CQPI_ROWFFT", "classic")
+        else:
+            monkeypatch.delenv("CQPI_ROWFFT", raising=False)
+        eng = cqpi.Engine(m, 16, 1024, 3, 2, 0.01, precision=cqpi.PREC_MIXED)
+        eng.set_orbitals(wf)
+        out = [eng.greens_box(e)[0] for e in (-0.05, 0.037)]
+        eng.close()
+        return out
+
+    for a, b in zip(box(False), box(True)):
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max()
+
+
 @pytest.mark.parametrize("name", ["c1", "c2", "c2_zero"])
 def test_pipelined_contraction_matches_serial(built_lib, name, monkeypatch):
     """Software-pipelined tcgen05 kernel (double-buffered B and accumulators) vs the serial one."""
