@@ -34,8 +34,12 @@
 // FP64 with the FP64 box) and accumulates in FP64; steps 4-5 follow the handle's precision
 // too (FP32 transform and per-k rotation for the mixed handle, the energy sum of C(k) in
 // FP64); steps 2, 3 and 6 are FP64.
+#include <cstdlib>
+#include <cstring>
+
 #include "cplx.h"
 #include "cqpi_internal.h"
+#include "fft_reg.cuh"
 
 namespace cqpi {
 
@@ -778,6 +782,93 @@ static void launch_kacc_t(cqpi_handle *h, int ne, const double *omegas, AdjWorks
     h->launches++;
 }
 
+// Rows of the box -> k-grid transform for the mixed handle on power-of-two k-grids of 64 ...
+// 4096 points with the box no wider than the grid: NC = 256 / max(N1, N2) k_x columns of one
+// plane per block.  The block reads the NB box rows of its columns (NC contiguous values per
+// row), puts row yb at k_y position (yb - Rb) mod kp (zero elsewhere), and runs the four-step
+// register transform of the forward rows with sign -1, as conj(F+(conj x)); each warp of the
+// second pass writes 32 consecutive k_y of one column.  (adj_rows_kernel: one block per
+// column, radix-2 with a barrier per stage, and a column read at stride kp.)
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) adj_rows_reg_kernel(int NB, int Rb, float scale, const float2 *__restrict__ A,
+                                                           const float2 *__restrict__ tw, float2 *__restrict__ gk)
+{
+    constexpr int KP = N1 * N2;
+    constexpr int NC = 256 / (N1 > N2 ? N1 : N2);
+    constexpr int PLEN = KP + KP / 32 + 1;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tws = sm + (size_t)NC * PLEN;       // [k2][n1] = e^{+2 pi i n1 k2 / kp}
+    const int kx0 = blockIdx.x * NC, pl = blockIdx.y;
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) {
+        const int k2 = t / N1, n1 = t - k2 * N1;
+        tws[t] = tw[(n1 * k2) & (KP - 1)];
+    }
+    for (int t = threadIdx.x; t < NC * PLEN; t += blockDim.x) sm[t] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const float2 *src = A + (size_t)pl * NB * KP + kx0;
+    for (int idx = threadIdx.x; idx < NB * NC; idx += blockDim.x) {
+        const int yb = idx / NC, c = idx - yb * NC;
+        const float2 v = src[(size_t)yb * KP + c];
+        const int pos = (yb - Rb + KP) & (KP - 1);
+        sm[(size_t)c * PLEN + pad32(pos)] = make_float2(v.x, -v.y);
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < NC * N1; task += blockDim.x) {
+        const int c = task / N1, n1 = task - c * N1;
+        float2 *a = sm + (size_t)c * PLEN;
+        float2 x[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
+        fft_reg<N2>(x);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[k2 * N1 + n1]);
+    }
+    __syncthreads();
+    const size_t nk = (size_t)KP * KP;
+    for (int task = threadIdx.x; task < NC * N2; task += blockDim.x) {
+        const int c = task / N2, k2 = task - c * N2;
+        const float2 *a = sm + (size_t)c * PLEN;
+        float2 x[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
+        fft_reg<N1>(x);
+        float2 *dst = gk + (size_t)pl * nk + (size_t)(kx0 + c) * KP;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; k1++) dst[k2 + N2 * k1] = make_float2(x[k1].x * scale, -x[k1].y * scale);
+    }
+}
+
+template <int N1, int N2>
+static void launch_adj_rows_reg(cqpi_handle *h, const float2 *A, float2 *gk)
+{
+    constexpr int KP = N1 * N2, NC = 256 / (N1 > N2 ? N1 : N2);
+    const size_t smem = 8 * ((size_t)NC * (KP + KP / 32 + 1) + KP);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(adj_rows_reg_kernel<N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
+    adj_rows_reg_kernel<N1, N2><<<dim3(KP / NC, h->b * h->b), 256, smem, h->stream>>>(
+        h->NB, h->Rb, (float)(1.0 / ((double)KP * KP)), A, h->d_tw32, gk);
+}
+
+// the register rows transform of the mixed handle (CQPI_ADJ_ROWS=radix2 keeps adj_rows_kernel)
+static bool adj_rows_reg(cqpi_handle *h, const float2 *A, float2 *gk)
+{
+    const char *f = getenv("CQPI_ADJ_ROWS");
+    if (h->NB > h->kp || (f && !strcmp(f, "radix2"))) return false;
+    switch (h->kp) {
+    case 64: launch_adj_rows_reg<8, 8>(h, A, gk); return true;
+    case 128: launch_adj_rows_reg<8, 16>(h, A, gk); return true;
+    case 256: launch_adj_rows_reg<16, 16>(h, A, gk); return true;
+    case 512: launch_adj_rows_reg<16, 32>(h, A, gk); return true;
+    case 1024: launch_adj_rows_reg<32, 32>(h, A, gk); return true;
+    case 2048: launch_adj_rows_reg<32, 64>(h, A, gk); return true;
+    case 4096: launch_adj_rows_reg<64, 64>(h, A, gk); return true;
+    }
+    return false;
+}
+
 // Gbar(k) of energy e of the batch (box -> k-grid transform) into slot e of aw.gk
 void launch_adj_kspace(cqpi_handle *h, int e, AdjWorkspace &aw)
 {
@@ -797,9 +888,10 @@ void launch_adj_kspace(cqpi_handle *h, int e, AdjWorkspace &aw)
         float2 *A32 = reinterpret_cast<float2 *>(aw.A), *gk32 = reinterpret_cast<float2 *>(aw.gk);
         adj_cols_kernel<float2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw32,
                                                                            A32);
-        adj_rows_kernel<float2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
-                                                                        1.0 / ((double)kp * kp), A32, h->d_tw32,
-                                                                        gk32 + (size_t)e * bb * nk);
+        if (!adj_rows_reg(h, A32, gk32 + (size_t)e * bb * nk))
+            adj_rows_kernel<float2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
+                                                                            1.0 / ((double)kp * kp), A32, h->d_tw32,
+                                                                            gk32 + (size_t)e * bb * nk);
     }
     h->launches += 2;
 }

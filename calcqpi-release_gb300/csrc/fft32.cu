@@ -27,10 +27,10 @@
 
 #include "cplx.h"
 #include "cqpi_internal.h"
+#include "fft_reg.cuh"
 
 namespace cqpi {
 
-__device__ __forceinline__ int pad32(int x) { return x + (x >> 5); }
 __device__ __forceinline__ int brev_bits(int x, int bits) { return bits == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - bits)); }
 __device__ __forceinline__ int pmod(int a, int m) { int r = a % m; return r < 0 ? r + m : r; }
 
@@ -155,65 +155,6 @@ __global__ void __launch_bounds__(256) g0_rowfft_kernel(int b, int kp, int logkp
 
 
 // ------------------------------------------------------------------ register four-step row transform
-// e^{+2 pi i k / 64}, k = 0..63 (cos, sin rounded to float): twiddles of the register FFTs.
-// Local constexpr tables: with k a compile-time constant (fully unrolled butterflies) the
-// values become immediates, so no twiddle is loaded and trivial ones are skipped.
-__device__ __forceinline__ float2 w64(int k)
-{
-    constexpr float re[64] = {
-        1.000000000e+00f, 9.951847267e-01f, 9.807852804e-01f, 9.569403357e-01f, 9.238795325e-01f, 8.819212643e-01f, 8.314696123e-01f, 7.730104534e-01f,
-        7.071067812e-01f, 6.343932842e-01f, 5.555702330e-01f, 4.713967368e-01f, 3.826834324e-01f, 2.902846773e-01f, 1.950903220e-01f, 9.801714033e-02f,
-        6.123233996e-17f, -9.801714033e-02f, -1.950903220e-01f, -2.902846773e-01f, -3.826834324e-01f, -4.713967368e-01f, -5.555702330e-01f, -6.343932842e-01f,
-        -7.071067812e-01f, -7.730104534e-01f, -8.314696123e-01f, -8.819212643e-01f, -9.238795325e-01f, -9.569403357e-01f, -9.807852804e-01f, -9.951847267e-01f,
-        -1.000000000e+00f, -9.951847267e-01f, -9.807852804e-01f, -9.569403357e-01f, -9.238795325e-01f, -8.819212643e-01f, -8.314696123e-01f, -7.730104534e-01f,
-        -7.071067812e-01f, -6.343932842e-01f, -5.555702330e-01f, -4.713967368e-01f, -3.826834324e-01f, -2.902846773e-01f, -1.950903220e-01f, -9.801714033e-02f,
-        -1.836970199e-16f, 9.801714033e-02f, 1.950903220e-01f, 2.902846773e-01f, 3.826834324e-01f, 4.713967368e-01f, 5.555702330e-01f, 6.343932842e-01f,
-        7.071067812e-01f, 7.730104534e-01f, 8.314696123e-01f, 8.819212643e-01f, 9.238795325e-01f, 9.569403357e-01f, 9.807852804e-01f, 9.951847267e-01f,
-    };
-    constexpr float im[64] = {
-        0.000000000e+00f, 9.801714033e-02f, 1.950903220e-01f, 2.902846773e-01f, 3.826834324e-01f, 4.713967368e-01f, 5.555702330e-01f, 6.343932842e-01f,
-        7.071067812e-01f, 7.730104534e-01f, 8.314696123e-01f, 8.819212643e-01f, 9.238795325e-01f, 9.569403357e-01f, 9.807852804e-01f, 9.951847267e-01f,
-        1.000000000e+00f, 9.951847267e-01f, 9.807852804e-01f, 9.569403357e-01f, 9.238795325e-01f, 8.819212643e-01f, 8.314696123e-01f, 7.730104534e-01f,
-        7.071067812e-01f, 6.343932842e-01f, 5.555702330e-01f, 4.713967368e-01f, 3.826834324e-01f, 2.902846773e-01f, 1.950903220e-01f, 9.801714033e-02f,
-        1.224646799e-16f, -9.801714033e-02f, -1.950903220e-01f, -2.902846773e-01f, -3.826834324e-01f, -4.713967368e-01f, -5.555702330e-01f, -6.343932842e-01f,
-        -7.071067812e-01f, -7.730104534e-01f, -8.314696123e-01f, -8.819212643e-01f, -9.238795325e-01f, -9.569403357e-01f, -9.807852804e-01f, -9.951847267e-01f,
-        -1.000000000e+00f, -9.951847267e-01f, -9.807852804e-01f, -9.569403357e-01f, -9.238795325e-01f, -8.819212643e-01f, -8.314696123e-01f, -7.730104534e-01f,
-        -7.071067812e-01f, -6.343932842e-01f, -5.555702330e-01f, -4.713967368e-01f, -3.826834324e-01f, -2.902846773e-01f, -1.950903220e-01f, -9.801714033e-02f,
-    };
-    return make_float2(re[k], im[k]);
-}
-
-// In-register radix-2 DFT of length L (sign +1), natural order in and out.
-template <int L>
-__device__ __forceinline__ void fft_reg(float2 (&x)[L])
-{
-    constexpr int LOG = (L == 2) ? 1 : (L == 4) ? 2 : (L == 8) ? 3 : (L == 16) ? 4 : (L == 32) ? 5 : 6;
-#pragma unroll
-    for (int i = 0; i < L; i++) {
-        int j = 0;
-#pragma unroll
-        for (int bt = 0; bt < LOG; bt++) j |= ((i >> bt) & 1) << (LOG - 1 - bt);
-        if (j > i) { const float2 t = x[i]; x[i] = x[j]; x[j] = t; }
-    }
-    // butterflies as one flat loop of constant trip count per stage, so that every index
-    // is a compile-time constant and x stays in registers
-#pragma unroll
-    for (int s = 0; s < LOG; s++) {
-#pragma unroll
-        for (int t = 0; t < L / 2; t++) {
-            const int hl = 1 << s;
-            const int k = t & (hl - 1);
-            const int i0 = ((t >> s) << (s + 1)) | k;
-            const int widx = k * (64 >> (s + 1));   // < 32; 0: w = 1, 16: w = i
-            const float2 y = x[i0 + hl];
-            const float2 v = widx == 0 ? y : (widx == 16 ? make_float2(-y.y, y.x) : cmul(y, w64(widx)));
-            const float2 u = x[i0];
-            x[i0] = cadd(u, v);
-            x[i0 + hl] = csub(u, v);
-        }
-    }
-}
-
 // Pass 1 with the transform along j done as kp = N1 x N2: for each n1 a length-N2 FFT over
 // n2 of x[n1 + N1 n2] (registers), twiddle e^{+2 pi i n1 k2 / kp}, then for each k2 a
 // length-N1 FFT over n1 (registers) giving X[k2 + N2 k1].  One shared-memory exchange
@@ -390,6 +331,7 @@ g0_rowfft_pk_kernel(int NB, int Rb, int tr, double eta, const double *__restrict
         // omega - eps in FP32 from float pairs (see g0_rowfft_reg_kernel)
         const float om_hi = (float)om, om_lo = (float)(om - (double)om_hi);
         __syncthreads();   // the previous item's second pass has read the planes (and tw2 is set)
+#pragma unroll 2
         for (int j = threadIdx.x; j < KP; j += blockDim.x) {
             const int pos = pad32(j);
             float2 f[B], U[B][B];
@@ -530,10 +472,15 @@ __global__ void __launch_bounds__(256) colfft_reg_kernel(int NB, int Rb, int b, 
         tws[t] = tw[(n1 * k2) & (KP - 1)];
     }
     const float2 *src = half + ((size_t)e * np + pl) * (size_t)KP * NB;
+    // every load of the block in flight at once (cp.async, zero-filled past the box)
     for (int idx = threadIdx.x; idx < KP * NC; idx += blockDim.x) {
         const int i = idx / NC, c = idx - i * NC, yb = yb0 + c;
-        sm[(size_t)c * PLEN + pad32(i)] = yb < NB ? src[(size_t)i * NB + yb] : make_float2(0.f, 0.f);
+        const bool in = yb < NB;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(sm + (size_t)c * PLEN + pad32(i));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(in ? src + (size_t)i * NB + yb : src),
+                     "r"(in ? 8u : 0u) : "memory");
     }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     for (int task = threadIdx.x; task < NC * N1; task += blockDim.x) {
         const int c = task / N1, n1 = task - c * N1;

@@ -815,7 +815,8 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         if (tid < 4) raw[zslot + tid] = 0.f;
     }
     if (tid == NW) {
-        for (int i = 0; i < 9; i++) mbar_init(smem_u32(&mbar[i]), 1);
+        // acc_empty[s] completes when every epilogue warp has arrived
+        for (int i = 0; i < 9; i++) mbar_init(smem_u32(&mbar[i]), (i == 6 || i == 7) ? TCW_EPI / 32 : 1);
         fence_mbar_init();
     }
     if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
@@ -1084,8 +1085,10 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         const int ncombo = EB * (TS >> 2);                        // (energy, 4-site group) pairs per tile
         constexpr bool jos = JOS;                                 // Josephson mode
         constexpr bool fold = FOLD;                               // T folded into the s operand
-        // T, the scale and term1 of an energy block, loaded once per block
+        // T, the scale and term1 of an energy block, loaded once per block (after every
+        // epilogue warp has finished the previous block's tiles)
         auto load_block = [&](int e0) {
+            bar_sync_group<1, TCW_EPI>();
             for (int i = tid; i < EB * p.nimp * bb; i += TCW_EPI) {
                 const int e = e0 + i / (p.nimp * bb);
                 cT[i] = e < p.ne ? p.T32[(size_t)e0 * p.nimp * bb + i] : make_float2(0.f, 0.f);
@@ -1191,30 +1194,33 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                     }
                 }
             }
-            // every TMEM read of this accumulator set is done: hand it back to the MMA warp
+            // this warp's TMEM reads of the accumulator set are done: its arrival on
+            // acc_empty (one per epilogue warp) hands the set back to the MMA warp
             tc_fence_before();
-            bar_sync_group<1, TCW_EPI>();
-            if (tid == 0) mbar_arrive(smem_u32(&acc_empty[accs]));
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acc_empty[accs]));
         };
+        // Epilogue warps run independently (no barrier per tile).  Every warp walks the same
+        // tiles, so the barriers of the energy-block changes stay matched after a time-out:
+        // from then on a warp skips the waits and the work but not the block changes.  The
+        // time-out decision is made uniform within a warp (its TMEM loads are warp-wide).
         bool ok = true;
         int cur_e0 = -1;
-        for (int it = 0; ok; it++) {
+        for (int it = 0;; it++) {
             int e0, j, i0;
             if (!tile_of(it, e0, j, i0)) break;
             if (e0 != cur_e0) {
                 load_block(e0);
                 cur_e0 = e0;
             }
+            if (!ok) continue;
             const int s = it & 1;
-            const bool done = mbar_wait(smem_u32(&acc_full[s]), (it >> 1) & 1, p.spin_limit);
-            if (bar_or_group<1, TCW_EPI>(!done)) {
-                ok = false;
-                break;
-            }
+            ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&acc_full[s]), (it >> 1) & 1, p.spin_limit));
+            if (!ok) continue;
             tc_fence_after();
             epilogue(s, e0, j, i0);
         }
-        if (!ok && tid == 0) atomicOr(p.status, 2);
+        if (!ok && lane == 0) atomicOr(p.status, 2);
     }
     tc_fence_before();
     __syncthreads();

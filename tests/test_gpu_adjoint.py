@@ -144,3 +144,31 @@ def test_set_hoppings_rebuilds_bands(built_lib):
     assert np.abs(a - c).max() <= 1e-13 * np.abs(a).max()
     assert np.abs(a - b_).max() > 1e-3 * np.abs(a).max()
     eng.close()
+
+
+@pytest.mark.parametrize("kp,lattice", [(64, 8), (256, 12)])
+def test_adjoint_register_rows_match_radix2(built_lib, kp, lattice, monkeypatch):
+    """Mixed handle: the box -> k-grid rows of the adjoint by the four-step register transform
+    (several k_x columns per block) give the gradients of the radix-2 one-column-per-block
+    kernel (CQPI_ADJ_ROWS=radix2) to FP32 rounding."""
+    import cqpi
+    from cqpi import workloads as W
+    m = W.t2g_c2()
+    wf = W.t2g_orbitals_c2(2, 3)
+    rng = np.random.default_rng(17)
+    E = np.array([-0.06, 0.021])
+    Wt = rng.normal(size=(len(E), 1, lattice * 3, lattice * 3)).astype(np.float32)
+    out = []
+    for env in (None, "radix2"):
+        if env:
+            monkeypatch.setenv("CQPI_ADJ_ROWS", env)
+        else:
+            monkeypatch.delenv("CQPI_ADJ_ROWS", raising=False)
+        eng = cqpi.Engine(m, lattice, kp, 3, 2, 0.01, precision=cqpi.PREC_MIXED)
+        eng.set_orbitals(wf)
+        eng.set_scattering(np.array([0.3, 0.3, 0.5], complex))
+        out.append(eng.adjoint(E, Wt))
+        eng.close()
+    (gt, gv), (rt, rv) = out
+    assert np.abs(gt - rt).max() <= 1e-5 * np.abs(rt).max()
+    assert np.abs(gv - rv).max() <= 1e-5 * np.abs(rv).max()
