@@ -356,12 +356,13 @@ def run_ours(args):
     roof["traffic"] = None
     if (args.config == "C2" and not args.fov and not args.energies and prec != cqpi.PREC_FP64
             and eng.contraction_kind() == "tcgen05"):
-        # dram__bytes_read.sum + dram__bytes_write.sum of one contraction launch (32 energies
-        # of this workload), one ncu capture: profiles/launches_c2_mixed.md
-        roof["traffic"] = 312.9e6 + 778.6e6
-        roof["traffic_note"] = ("bytes per contraction launch of 32 energies (ncu); algorithmic: the u windows from "
-                                "32 G0(R) boxes and the s windows from 32 T G0(R) boxes (2 x 157 MB) + 32 maps "
-                                "(839 MB)")
+        # dram__bytes_read.sum + dram__bytes_write.sum of one contraction launch of 32 energies
+        # on a 192^2-site field of view (one ncu capture: profiles/launches_c2_mixed.md), scaled
+        # to this 256^2-site launch by the pixels it writes and the window sites it reads
+        roof["traffic"] = (178.1e6 + 412.0e6) * (256.0 / 192.0) ** 2
+        roof["traffic_note"] = ("bytes per contraction launch of 32 energies (ncu, 192^2-site launch x 1.78); "
+                                "algorithmic: the u windows from 32 G0(R) boxes and the s windows from 32 T G0(R) "
+                                "boxes (2 x 157 MB) + 32 maps (839 MB)")
     roof["stage_ms_per_step"] = {k: v / args.steps for k, v in stage_acc.items()}
 
     # accuracy and speed of the all-FP64 path on the same workload (the metric's comparison)
