@@ -186,10 +186,16 @@ __global__ void __launch_bounds__(128) adj_contract_kernel(int b, int n, int os,
 // shared memory as [entry t][q] (row stride QP = 129 words, zero past Q), lane l handles the
 // pixels q = l + 32k (k < 4) in the forward part, so every window value G(R)[o][a] loaded for a
 // site feeds 4 pixels, and the entries t = l + 32m in the window-gradient part, so every
-// ubar / sbar row read feeds 3 entries.  grid (ceil(n*n / 4), ne*nimp), 4 warps.
+// ubar / sbar row read feeds 3 entries.  grid (ceil(n*n / wpb), ne*nimp), wpb warps: the orbital
+// table is shared by the block's sites, and 10 FP32 warps (two blocks of 100 KB per SM for the
+// C2 orbitals) keep 20 warps resident instead of the 12 of three 4-warp blocks.
 constexpr int ADJ_QP = 129;
+// warps (sites) per block: 10 for the FP32 working type; the FP64 one keeps 4 warps per block,
+// whose larger register budget it needs
+template <class C> struct AdjWpb { static constexpr int value = 10, blocks = 2; };
+template <> struct AdjWpb<double2> { static constexpr int value = 4, blocks = 1; };
 template <int B, class C>
-__global__ void __launch_bounds__(128) adj_contract_warp_kernel(int b, int n, int os, int w, int Rb, int NB, int Q, int W,
+__global__ void __launch_bounds__(32 * AdjWpb<C>::value, AdjWpb<C>::blocks) adj_contract_warp_kernel(int b, int n, int os, int w, int Rb, int NB, int Q, int W,
                                                                 int nimp, int mb, int bs0,
                                                                 const typename real_of<C>::type *__restrict__ phi,
                                                                 const C *__restrict__ box, const double2 *__restrict__ T,
@@ -200,14 +206,14 @@ __global__ void __launch_bounds__(128) adj_contract_warp_kernel(int b, int n, in
     extern __shared__ __align__(16) unsigned char adj_sm[];
     const int Wmb = W * mb;
     Rl *phT = reinterpret_cast<Rl *>(adj_sm);                     // [Wmb][ADJ_QP]
-    Rl *ubs = phT + (size_t)Wmb * ADJ_QP;                          // [4 warps][128 q][b][4]: ubar re, im, sbar re, im
+    Rl *ubs = phT + (size_t)Wmb * ADJ_QP;                          // [warp][128 q][b][4]: ubar re, im, sbar re, im
     for (int i = threadIdx.x; i < Wmb * ADJ_QP; i += blockDim.x) {
         const int t = i / ADJ_QP, q = i - t * ADJ_QP;
         phT[i] = q < Q ? phi[(size_t)q * Wmb + t] : (Rl)0;
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nsite = n * n, site = blockIdx.x * 4 + warp;
+    const int nsite = n * n, site = blockIdx.x * AdjWpb<C>::value + warp;
     if (site >= nsite) return;
     const int ei = blockIdx.y, e = ei / nimp;
     const int i = site / n, j = site % n;
@@ -625,6 +631,9 @@ __global__ void __launch_bounds__(256) adj_rows_kernel(int kp, int logkp, int NB
 }
 
 // ------------------------------------------------------------------ 5. per-k resolvent
+// eigenvalue storage read by the resolvent bracket: FP64, or the float pairs of the mixed handle
+template <class C> struct KaccEv { using T = double; };
+template <> struct KaccEv<float2> { using T = float2; };
 #define CQPI_ADJ_KACC adj_kacc_kernel
 #define CQPI_ADJ_HBAR adj_hbar_kernel
 #define CQPI_ADJ_UNROLL _Pragma("unroll")
@@ -693,14 +702,16 @@ static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>:
     C *Ub = reinterpret_cast<C *>(aw.win);
     C *Sb = Ub + (size_t)ne * h->nimp * h->W * h->mb * h->b * nsite;
     using Rl = typename real_of<C>::type;
-    const size_t wsm = sizeof(Rl) * ((size_t)h->W * h->mb * ADJ_QP + 4 * 128 * (size_t)h->b * 4);
+    constexpr int wpb = AdjWpb<C>::value;
+    const size_t wsm = sizeof(Rl) * ((size_t)h->W * h->mb * ADJ_QP + wpb * 128 * (size_t)h->b * 4);
     bool warp_form = false;
     if constexpr (B <= 4) {
-        // one warp per site when the orbital table and the four warps' ubar / sbar rows fit
+        // one warp per site when the orbital table and the warps' ubar / sbar rows fit
         if (wsm <= 200 * 1024 &&
             cudaFuncSetAttribute(adj_contract_warp_kernel<B, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm) ==
                 cudaSuccess) {
-            adj_contract_warp_kernel<B, C><<<dim3(cdiv(nsite, 4), (unsigned)(ne * h->nimp)), 128, wsm, h->stream>>>(
+            adj_contract_warp_kernel<B, C><<<dim3(cdiv(nsite, wpb), (unsigned)(ne * h->nimp)), 32 * wpb, wsm,
+                                             h->stream>>>(
                 h->b, h->n, h->os, h->w, h->Rb, h->NB, h->Q, h->W, h->nimp, h->mb, h->blk_start[0], phi, box, h->ws.T, wmap,
                 Ub, Sb, aw.Mp);
             warp_form = true;
@@ -769,14 +780,14 @@ static void launch_kacc_t(cqpi_handle *h, int ne, const double *omegas, AdjWorks
             adj_kacc_kernel<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval, h->d_evec,
                                                                      aw.gk, aw.C);
         else
-            adj_kacc_kernel<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval, h->d_evec32,
-                                                                    gk32, aw.C);
+            adj_kacc_kernel<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval32,
+                                                                    h->d_evec32, gk32, aw.C);
     } else {
         if (h->precision == CQPI_PREC_FP64)
             adj_kacc_kernel_wide<B, double2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval,
                                                                           h->d_evec, aw.gk, aw.C);
         else
-            adj_kacc_kernel_wide<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval,
+            adj_kacc_kernel_wide<B, float2><<<grid, 128, 0, h->stream>>>(h->b, nk, ne, omegas, h->eta, h->d_eval32,
                                                                          h->d_evec32, gk32, aw.C);
     }
     h->launches++;

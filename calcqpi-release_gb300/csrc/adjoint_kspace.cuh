@@ -8,20 +8,24 @@
 // energies of a batch (Gbar_e(k) at gk + e * b*b*nk); one thread per k.  Up to 3 bands the
 // energy sum is held in FP64 registers and C(k) is read and written once per batch; more bands
 // add each energy's bracket to C(k) in memory.
-// C: the working precision (double2, or float2 for the mixed handle: eigenvectors and Gbar(k)
-// in FP32, the pole factors from the FP64 eigenvalues, C(k) accumulated in FP64)
+// C: the working precision.  double2: FP64 throughout.  float2 (the mixed handle): eigenvectors
+// and Gbar(k) in FP32, the pole distances omega - eps from the eigenvalues' float pairs
+// (hi, lo) as the forward builds G0 (exact near a pole by Sterbenz), the energy sum of a batch
+// in FP32 with compensated (Kahan) addition, added to the FP64 C(k) once per batch.
 template <int B, class C>
 __global__ void __launch_bounds__(128) CQPI_ADJ_KACC(int b, long long nk, int ne, const double *__restrict__ omegas,
-                                                       double eta, const double *__restrict__ eval,
+                                                       double eta, const typename KaccEv<C>::T *__restrict__ eval,
                                                        const C *__restrict__ evec, const C *__restrict__ gk,
                                                        double2 *__restrict__ Cacc)
 {
     constexpr bool REG = B <= 3;
+    constexpr bool F32 = std::is_same<C, float2>::value;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nk) return;
     C U[B][B], G[B][B], X[B][B], f[B];
-    double ev[B];
-    double2 acc[REG ? B : 1][REG ? B : 1];
+    typename KaccEv<C>::T ev[B];
+    using A = typename std::conditional<F32, float2, double2>::type;   // the batch sum
+    A acc[REG ? B : 1][REG ? B : 1], cmp[REG && F32 ? B : 1][REG && F32 ? B : 1];
 CQPI_ADJ_UNROLL
     for (int n = 0; n < B; n++)
         if (n < b) ev[n] = eval[(size_t)n * nk + k];
@@ -34,7 +38,10 @@ CQPI_ADJ_UNROLL
 CQPI_ADJ_UNROLL
         for (int n = 0; n < B; n++)
 CQPI_ADJ_UNROLL
-            for (int m = 0; m < B; m++) acc[n][m] = make_double2(0.0, 0.0);
+            for (int m = 0; m < B; m++) {
+                acc[n][m] = cmake<A>(0.0, 0.0);
+                if constexpr (F32) cmp[n][m] = make_float2(0.f, 0.f);
+            }
     }
     const size_t plane = (size_t)b * b * nk;
     for (int e = 0; e < ne; e++) {
@@ -42,13 +49,18 @@ CQPI_ADJ_UNROLL
 CQPI_ADJ_UNROLL
         for (int n = 0; n < B; n++) {
             if (n < b) {
-                // conj(1/(dr + i eta)); the pole distance in FP64, the reciprocal in the
-                // bracket's precision (an FP32 reciprocal for the mixed handle)
-                const double dr = omega - ev[n];
-                const double den = dr * dr + eta * eta;
-                using R = typename real_of<C>::type;
-                const R inv = (R)1 / (R)den;
-                f[n] = cmake<C>((R)dr * inv, (R)eta * inv);
+                // conj(1/(dr + i eta))
+                if constexpr (F32) {
+                    const float om_hi = (float)omega, om_lo = (float)(omega - (double)om_hi);
+                    const float dr = (om_hi - ev[n].x) + (om_lo - ev[n].y);
+                    const float et = (float)eta;
+                    const float inv = 1.f / (dr * dr + et * et);
+                    f[n] = make_float2(dr * inv, et * inv);
+                } else {
+                    const double dr = omega - ev[n];
+                    const double inv = 1.0 / (dr * dr + eta * eta);
+                    f[n] = make_double2(dr * inv, eta * inv);
+                }
             }
         }
 CQPI_ADJ_UNROLL
@@ -83,7 +95,13 @@ CQPI_ADJ_UNROLL
                         s = cadd(s, cmul(un, X[o][m]));
                     }
                 s = cmul(cmul(f[n], s), f[m]);
-                if constexpr (REG) {
+                if constexpr (REG && F32) {
+                    // compensated: cmp holds the rounding error of the running sum
+                    const float2 y = make_float2(s.x - cmp[n][m].x, s.y - cmp[n][m].y);
+                    const float2 t = make_float2(acc[n][m].x + y.x, acc[n][m].y + y.y);
+                    cmp[n][m] = make_float2((t.x - acc[n][m].x) - y.x, (t.y - acc[n][m].y) - y.y);
+                    acc[n][m] = t;
+                } else if constexpr (REG) {
                     acc[n][m] = cadd(acc[n][m], to_d2(s));
                 } else {
                     double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
@@ -98,7 +116,11 @@ CQPI_ADJ_UNROLL
             for (int m = 0; m < B; m++) {
                 if (n >= b || m >= b) continue;
                 double2 *c = Cacc + (size_t)(n * b + m) * nk + k;
-                *c = cadd(*c, acc[n][m]);
+                if constexpr (F32)
+                    *c = make_double2(c->x + ((double)acc[n][m].x - (double)cmp[n][m].x),
+                                      c->y + ((double)acc[n][m].y - (double)cmp[n][m].y));
+                else
+                    *c = cadd(*c, acc[n][m]);
             }
     }
 }
