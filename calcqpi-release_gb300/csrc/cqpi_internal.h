@@ -289,6 +289,7 @@ bool fft32_supported(const cqpi_handle *h);
 cudaError_t configure_fft32(cqpi_handle *h);
 void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies);
 bool launch_fft32_planes(cqpi_handle *h, int ne);
+bool g0k_reciprocity(const cqpi_handle *h);   // G0(k) planes of the unfused path: upper triangle only
 // ldos_tc.cu
 bool tc_supported(const cqpi_handle *h);
 void tc_plan(cqpi_handle *h);

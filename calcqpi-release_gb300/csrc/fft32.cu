@@ -821,10 +821,10 @@ static cudaError_t configure_rowfft_g0k(cqpi_handle *h)
 }
 
 template <int N1, int N2>
-static void launch_rowfft_g0k_t(cqpi_handle *h, int ne)
+static void launch_rowfft_g0k_t(cqpi_handle *h, int ne, int np)
 {
     constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
-    const long long nrows = (long long)ne * h->b * h->b * h->kp;
+    const long long nrows = (long long)ne * np * h->kp;
     rowfft_reg_g0k_kernel<N1, N2><<<(unsigned)((nrows + RPC - 1) / RPC), 256, rowfft_g0k_smem<N1, N2>(), h->stream>>>(
         h->NB, h->Rb, nrows, h->ws.g0k32, h->d_tw32, h->ws.half32);
 }
@@ -894,24 +894,40 @@ void launch_greens_fft32(cqpi_handle *h, int ne, const double *d_energies)
     h->launches++;
 }
 
+static bool fft32_planes_ok(const cqpi_handle *h)
+{
+    const char *force = getenv("CQPI_ROWFFT");
+    return fft32_supported(h) && rowfft_reg_ok(h) && !(force && !strcmp(force, "radix2"));
+}
+
+// The unfused mixed path of the normal Green's function transforms only the b(b+1)/2
+// reciprocity planes when the hoppings are real (greens_k_kernel then writes those planes, in
+// the upper-triangle order, and the column kernel fills the rest of the box by reflection).
+bool g0k_reciprocity(const cqpi_handle *h)
+{
+    return h->precision == CQPI_PREC_MIXED && h->gmode == CQPI_GREEN_NORMAL && fft32_planes_ok(h) &&
+           rowfft_planes(h) != h->b * h->b;
+}
+
 // Transforms of the unfused mixed path (G0(k) planes in ws.g0k32) with the register
 // four-step kernels; false when the k-grid is outside their range (the radix-2 kernels of
 // greens.cu run instead).
 bool launch_fft32_planes(cqpi_handle *h, int ne)
 {
-    const char *force = getenv("CQPI_ROWFFT");
-    if (!fft32_supported(h) || !rowfft_reg_ok(h) || (force && !strcmp(force, "radix2"))) return false;
+    if (!fft32_planes_ok(h)) return false;
+    const bool tr = g0k_reciprocity(h);
+    const int np = tr ? rowfft_planes(h) : h->b * h->b;
     switch (h->kp) {
-    case 64: launch_rowfft_g0k_t<8, 8>(h, ne); break;
-    case 128: launch_rowfft_g0k_t<8, 16>(h, ne); break;
-    case 256: launch_rowfft_g0k_t<16, 16>(h, ne); break;
-    case 512: launch_rowfft_g0k_t<16, 32>(h, ne); break;
-    case 1024: launch_rowfft_g0k_t<32, 32>(h, ne); break;
-    case 2048: launch_rowfft_g0k_t<32, 64>(h, ne); break;
-    case 4096: launch_rowfft_g0k_t<64, 64>(h, ne); break;
+    case 64: launch_rowfft_g0k_t<8, 8>(h, ne, np); break;
+    case 128: launch_rowfft_g0k_t<8, 16>(h, ne, np); break;
+    case 256: launch_rowfft_g0k_t<16, 16>(h, ne, np); break;
+    case 512: launch_rowfft_g0k_t<16, 32>(h, ne, np); break;
+    case 1024: launch_rowfft_g0k_t<32, 32>(h, ne, np); break;
+    case 2048: launch_rowfft_g0k_t<32, 64>(h, ne, np); break;
+    case 4096: launch_rowfft_g0k_t<64, 64>(h, ne, np); break;
     }
     h->launches++;
-    launch_colfft_reg(h, ne, 0);
+    launch_colfft_reg(h, ne, tr ? 1 : 0);
     h->launches++;
     return true;
 }

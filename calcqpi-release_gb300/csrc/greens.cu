@@ -23,10 +23,12 @@
 namespace cqpi {
 
 // ------------------------------------------------------------------ G0(k,w)
+// tr: only the planes o <= a, stored in the upper-triangle order (index o*b - o(o-1)/2 + a - o),
+// np planes per energy; else all b^2 planes o*b + a
 template <int B, class C>
 __global__ void __launch_bounds__(256) greens_k_kernel(int b, long long nk, double eta, const double *__restrict__ energies,
                                                        const double *__restrict__ eval, const C *__restrict__ evec,
-                                                       C *__restrict__ g0k)
+                                                       C *__restrict__ g0k, int tr)
 {
     using R = typename real_of<C>::type;
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -45,7 +47,8 @@ __global__ void __launch_bounds__(256) greens_k_kernel(int b, long long nk, doub
             f[n].y = -et / den;
         }
     }
-    C *out = g0k + (size_t)e * bb * nk + k;
+    const int np = tr ? b * (b + 1) / 2 : bb;
+    C *out = g0k + (size_t)e * np * nk + k;
 #pragma unroll
     for (int o = 0; o < B; o++) {
         if (o >= b) continue;
@@ -55,7 +58,7 @@ __global__ void __launch_bounds__(256) greens_k_kernel(int b, long long nk, doub
             if (n < b) x[n] = cmul(evec[(size_t)(o * b + n) * nk + k], f[n]);
 #pragma unroll
         for (int a = 0; a < B; a++) {
-            if (a >= b) continue;
+            if (a >= b || (tr && a < o)) continue;
             C s = cmake<C>(0.0, 0.0);
 #pragma unroll
             for (int n = 0; n < B; n++) {
@@ -65,7 +68,8 @@ __global__ void __launch_bounds__(256) greens_k_kernel(int b, long long nk, doub
                     s.y += x[n].y * u.x - x[n].x * u.y;
                 }
             }
-            out[(size_t)(o * b + a) * nk] = s;
+            const int pl = tr ? o * b - (o * (o - 1)) / 2 + (a - o) : o * b + a;
+            out[(size_t)pl * nk] = s;
         }
     }
 }
@@ -77,10 +81,10 @@ static void launch_greens_k_t(cqpi_handle *h, int ne, const double *d_energies)
     dim3 grid(cdiv(nk, 256), ne);
     if (h->precision == CQPI_PREC_FP64)
         greens_k_kernel<B, double2><<<grid, 256, 0, h->stream>>>(h->b, nk, h->eta, d_energies, h->d_eval, h->d_evec,
-                                                                  h->ws.g0k);
+                                                                  h->ws.g0k, 0);
     else
         greens_k_kernel<B, float2><<<grid, 256, 0, h->stream>>>(h->b, nk, h->eta, d_energies, h->d_eval, h->d_evec32,
-                                                                 h->ws.g0k32);
+                                                                 h->ws.g0k32, g0k_reciprocity(h) ? 1 : 0);
     h->launches++;
 }
 
