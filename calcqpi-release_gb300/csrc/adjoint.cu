@@ -46,6 +46,7 @@ namespace cqpi {
 namespace {
 
 __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ void atomic_add2(double2 *p, double2 v)
 {
     atomicAdd(&p->x, v.x);
@@ -403,27 +404,33 @@ __global__ void __launch_bounds__(256) adj_mreduce_kernel(int nsite, int bb, con
     }
 }
 
-// wsum[e][q] = sum over the impurities' maps and the sites of W at sub-pixel q = qx*os + qy
-// (map pixel (x, y) = (i*os + qx, j*os + qy)); grid (ceil(wn/16), ne*nimp), rows of 16
+// wsum[e][q] = sum over the impurities' maps and the sites of W at sub-pixel q = qx*os + qy.
+// One block per (qy, energy of the batch): it reads the map rows y = j*os + qy of every
+// impurity, contiguous in x; the threads in use are a multiple of os, so thread t sums the one
+// sub-pixel column qx = t % os in a register, and the per-qx partial sums are added in shared
+// memory in a fixed order (no atomics; the result does not depend on scheduling).
 __global__ void __launch_bounds__(256) adj_wsum_kernel(int wn, int os, int Q, int nimp, const float *__restrict__ wmap,
                                                        double *__restrict__ wsum)
 {
-    __shared__ double acc[128];
-    const int ei = blockIdx.y, e = ei / nimp;
-    for (int k = threadIdx.x; k < Q; k += blockDim.x) acc[k] = 0.0;
+    __shared__ double part[256];
+    const int qy = blockIdx.x, e = blockIdx.y, t = threadIdx.x;
+    const int nt = ((int)blockDim.x / os) * os;
+    double acc = 0.0;
+    if (t < nt)
+        for (int imp = 0; imp < nimp; imp++)
+            for (int y = qy; y < wn; y += os) {
+                const float *row = wmap + (((size_t)e * nimp + imp) * wn + y) * wn;
+                float r = 0.f;
+                for (int x = t; x < wn; x += nt) r += row[x];
+                acc += (double)r;
+            }
+    part[t] = acc;
     __syncthreads();
-    const int y0 = blockIdx.x * 16;
-    for (int y = y0; y < min(y0 + 16, wn); y++) {
-        const float *row = wmap + ((size_t)ei * wn + y) * wn;
-        const int qy = y % os;
-        for (int x = threadIdx.x; x < wn; x += blockDim.x) {
-            const float v = row[x];
-            if (v != 0.f) atomicAdd(&acc[(x % os) * os + qy], (double)v);
-        }
+    if (t < os) {
+        double sum = 0.0;
+        for (int u = t; u < nt; u += os) sum += part[u];
+        wsum[(size_t)e * Q + t * os + qy] = sum;
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < Q; k += blockDim.x)
-        if (acc[k] != 0.0) atomicAdd(wsum + (size_t)e * Q + k, acc[k]);
 }
 
 // ------------------------------------------------------------------ 2. term1
@@ -691,6 +698,74 @@ __global__ void __launch_bounds__(256) adj_hop_kernel(int b, int kp, int logkp, 
     }
 }
 
+// The mixed handle's form of adj_hop_kernel: Hbar(k) and the phases in FP32, RG unique R per
+// block so that every Hbar(k) value loaded feeds RG of them, each thread's sums over its
+// k-points compensated (Kahan) in FP32, the warp and block sums in FP64.
+constexpr int HOP_RG = 4;
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    const float y = x - c, t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+__global__ void __launch_bounds__(256) adj_hop32_kernel(int b, int nR, int kp, int logkp, const int32_t *__restrict__ R,
+                                                        const float2 *__restrict__ tw, const float2 *__restrict__ hbar,
+                                                        double2 *__restrict__ out)
+{
+    const int r0 = blockIdx.x * HOP_RG;
+    const int bb = b * b;
+    const long long nk = (long long)kp * kp;
+    long long Rx[HOP_RG], Ry[HOP_RG];
+#pragma unroll
+    for (int g = 0; g < HOP_RG; g++) {
+        const int r = min(r0 + g, nR - 1);
+        Rx[g] = R[2 * r];
+        Ry[g] = R[2 * r + 1];
+    }
+    __shared__ double red[8][HOP_RG][4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int pq = 0; pq < bb; pq++) {
+        // [g][0..3] = normal re, im, conjugated re, im: sums and compensations
+        float sm[HOP_RG][4], cm[HOP_RG][4];
+#pragma unroll
+        for (int g = 0; g < HOP_RG; g++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) { sm[g][c] = 0.f; cm[g][c] = 0.f; }
+        for (long long k = (long long)blockIdx.y * blockDim.x + threadIdx.x; k < nk; k += (long long)gridDim.y * blockDim.x) {
+            const long long i = k >> logkp, j = k & (kp - 1);
+            const float2 h = hbar[(size_t)pq * nk + k];
+#pragma unroll
+            for (int g = 0; g < HOP_RG; g++) {
+                const float2 ph = __ldg(tw + ((Rx[g] * i + Ry[g] * j) & (long long)(kp - 1)));
+                // conj(ph) h and ph h
+                kahan_add(sm[g][0], cm[g][0], ph.x * h.x + ph.y * h.y);
+                kahan_add(sm[g][1], cm[g][1], ph.x * h.y - ph.y * h.x);
+                kahan_add(sm[g][2], cm[g][2], ph.x * h.x - ph.y * h.y);
+                kahan_add(sm[g][3], cm[g][3], ph.x * h.y + ph.y * h.x);
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < HOP_RG; g++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                double v = (double)sm[g][c] - (double)cm[g][c];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0) red[warp][g][c] = v;
+            }
+        __syncthreads();
+        if (threadIdx.x < 2 * HOP_RG) {
+            const int g = threadIdx.x >> 1, na = threadIdx.x & 1;
+            double2 t = make_double2(0.0, 0.0);
+            for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) {
+                t.x += red[wv][g][2 * na];
+                t.y += red[wv][g][2 * na + 1];
+            }
+            if (r0 + g < nR) atomic_add2(out + ((size_t)(r0 + g) * 2 + na) * bb + pq, t);
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ launchers
 template <int B, class C>
 static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>::type *phi, const C *box,
@@ -723,8 +798,8 @@ static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>:
     adj_gather_kernel<C><<<dim3(cdiv(h->NB, 128), (unsigned)h->NB, (unsigned)(ne * bb)), 128, 0, h->stream>>>(
         h->b, h->n, h->w, h->Rb, h->NB, h->W, h->mb, h->blk_start[0], h->nimp, Ub, Sb, aw.gbox);
     adj_mreduce_kernel<<<(unsigned)(ne * h->nimp), 256, 0, h->stream>>>(nsite, bb, aw.Mp, aw.M);
-    adj_wsum_kernel<<<dim3(cdiv(h->wn, 16), (unsigned)(ne * h->nimp)), 256, 0, h->stream>>>(h->wn, h->os, h->Q, h->nimp,
-                                                                                             wmap, aw.wsum);
+    adj_wsum_kernel<<<dim3((unsigned)h->os, (unsigned)ne), 256, 0, h->stream>>>(h->wn, h->os, h->Q, h->nimp, wmap,
+                                                                               aw.wsum);
     h->launches += 4;
 }
 
@@ -925,10 +1000,18 @@ template <int B>
 static void launch_hbar_t(cqpi_handle *h, AdjWorkspace &aw)
 {
     const long long nk = (long long)h->kp * h->kp;
-    if constexpr (B <= 6)
-        adj_hbar_kernel<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
-    else
-        adj_hbar_kernel_wide<B><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
+    float2 *hb32 = reinterpret_cast<float2 *>(aw.gk);
+    if (h->precision == CQPI_PREC_FP64) {
+        if constexpr (B <= 6)
+            adj_hbar_kernel<B, double2><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
+        else
+            adj_hbar_kernel_wide<B, double2><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec, aw.C, aw.gk);
+    } else {
+        if constexpr (B <= 6)
+            adj_hbar_kernel<B, float2><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec32, aw.C, hb32);
+        else
+            adj_hbar_kernel_wide<B, float2><<<cdiv(nk, 128), 128, 0, h->stream>>>(h->b, nk, h->d_evec32, aw.C, hb32);
+    }
     h->launches++;
 }
 
@@ -945,8 +1028,12 @@ void launch_adj_hoppings(cqpi_handle *h, AdjWorkspace &aw)
     else launch_hbar_t<16>(h, aw);
     if (h->nR > 0) {
         const int chunks = std::max(1, std::min(64, (int)(((long long)h->kp * h->kp) / (256 * 64))));
-        adj_hop_kernel<<<dim3(h->nR, chunks), 256, 0, h->stream>>>(b, h->kp, ilog2_exact(h->kp), h->d_R, h->d_tw, aw.gk,
-                                                                   aw.gR);
+        if (h->precision == CQPI_PREC_FP64)
+            adj_hop_kernel<<<dim3(h->nR, chunks), 256, 0, h->stream>>>(b, h->kp, ilog2_exact(h->kp), h->d_R, h->d_tw, aw.gk,
+                                                                       aw.gR);
+        else
+            adj_hop32_kernel<<<dim3(cdiv(h->nR, HOP_RG), chunks), 256, 0, h->stream>>>(
+                b, h->nR, h->kp, ilog2_exact(h->kp), h->d_R, h->d_tw32, reinterpret_cast<const float2 *>(aw.gk), aw.gR);
         h->launches++;
     }
 }

@@ -125,14 +125,15 @@ CQPI_ADJ_UNROLL
     }
 }
 
-// Hbar(k) = U C(k) U^H, written over gk
-template <int B>
-__global__ void __launch_bounds__(128) CQPI_ADJ_HBAR(int b, long long nk, const double2 *__restrict__ evec,
-                                                       const double2 *__restrict__ Cacc, double2 *__restrict__ hbar)
+// Hbar(k) = U C(k) U^H, written over gk in the working precision C (the mixed handle: the FP32
+// eigenvectors, C(k) rounded to FP32)
+template <int B, class C>
+__global__ void __launch_bounds__(128) CQPI_ADJ_HBAR(int b, long long nk, const C *__restrict__ evec,
+                                                       const double2 *__restrict__ Cacc, C *__restrict__ hbar)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nk) return;
-    double2 U[B][B], X[B][B];
+    C U[B][B], X[B][B];
 CQPI_ADJ_UNROLL
     for (int o = 0; o < B; o++)
 CQPI_ADJ_UNROLL
@@ -144,10 +145,13 @@ CQPI_ADJ_UNROLL
 CQPI_ADJ_UNROLL
         for (int m = 0; m < B; m++) {
             if (o >= b || m >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
+            C s = cmake<C>(0.0, 0.0);
 CQPI_ADJ_UNROLL
             for (int n = 0; n < B; n++)
-                if (n < b) s = cadd(s, cmul(U[o][n], Cacc[(size_t)(n * b + m) * nk + k]));
+                if (n < b) {
+                    const double2 c = Cacc[(size_t)(n * b + m) * nk + k];
+                    s = cadd(s, cmul(U[o][n], cmake<C>(c.x, c.y)));
+                }
             X[o][m] = s;
         }
 CQPI_ADJ_UNROLL
@@ -155,7 +159,7 @@ CQPI_ADJ_UNROLL
 CQPI_ADJ_UNROLL
         for (int a = 0; a < B; a++) {
             if (o >= b || a >= b) continue;
-            double2 s = make_double2(0.0, 0.0);
+            C s = cmake<C>(0.0, 0.0);
 CQPI_ADJ_UNROLL
             for (int m = 0; m < B; m++)
                 if (m < b) s = cadd(s, cmul(X[o][m], cconj(U[a][m])));
