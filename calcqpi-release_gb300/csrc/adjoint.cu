@@ -36,6 +36,7 @@
 // FP64); steps 2, 3 and 6 are FP64.
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "cplx.h"
 #include "cqpi_internal.h"
@@ -228,16 +229,41 @@ __global__ void __launch_bounds__(32 * AdjWpb<C>::value, AdjWpb<C>::blocks) adj_
     for (int k = 0; k < 4; k++)
 #pragma unroll
         for (int a = 0; a < B; a++) { ur[k][a] = 0; ui[k][a] = 0; sr[k][a] = 0; si[k][a] = 0; }
+    // the site's window values G(p+d)[o][a] and G(-p-d)[a][o], staged by the warp in its ubar /
+    // sbar region (free until the forward part is done) when they fit: [u/s][t][a] complex
+    Rl *ub = ubs + (size_t)warp * 128 * b * 4;
+    const bool staged = Wmb <= 128;
+    if (staged) {
+        for (int idx = lane; idx < 2 * Wmb * b; idx += 32) {
+            const int op = idx / (Wmb * b), rest = idx - op * Wmb * b;
+            const int t = rest / b, a = rest - t * b;
+            const int d = t / mb, o = bs0 + (t - d * mb);
+            const int dx = d / side - w, dy = d % side - w;
+            const C v = op == 0 ? boxe[((size_t)(px + dx + Rb) * NB + (py + dy + Rb)) * bb + o * b + a]
+                                : boxe[((size_t)(-px - dx + Rb) * NB + (-py - dy + Rb)) * bb + a * b + o];
+            ub[2 * idx] = v.x;
+            ub[2 * idx + 1] = v.y;
+        }
+        __syncwarp();
+    }
     for (int d = 0; d < W; d++) {
         const int dx = d / side - w, dy = d % side - w;
         const C *gs = boxe + ((size_t)(-px - dx + Rb) * NB + (-py - dy + Rb)) * bb;
         const C *gu = boxe + ((size_t)(px + dx + Rb) * NB + (py + dy + Rb)) * bb;
+#pragma unroll 3
         for (int ol = 0; ol < mb; ol++) {
             const int o = bs0 + ol, t = d * mb + ol;
             C vu[B], vs[B];
+            if (staged) {
+                const Rl *wu = ub + 2 * (t * b), *ws = ub + 2 * ((Wmb + t) * b);
 #pragma unroll
-            for (int a = 0; a < B; a++)
-                if (a < b) { vu[a] = gu[o * b + a]; vs[a] = gs[a * b + o]; }
+                for (int a = 0; a < B; a++)
+                    if (a < b) { vu[a] = cmake<C>(wu[2 * a], wu[2 * a + 1]); vs[a] = cmake<C>(ws[2 * a], ws[2 * a + 1]); }
+            } else {
+#pragma unroll
+                for (int a = 0; a < B; a++)
+                    if (a < b) { vu[a] = gu[o * b + a]; vs[a] = gs[a * b + o]; }
+            }
             const Rl *pt = phT + (size_t)t * ADJ_QP + lane;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -251,8 +277,9 @@ __global__ void __launch_bounds__(32 * AdjWpb<C>::value, AdjWpb<C>::blocks) adj_
             }
         }
     }
-    // ubar = -i W conj(T s), sbar = -i W conj(u^T T); M_ac = sum_q W u_a s_c
-    Rl *ub = ubs + (size_t)warp * 128 * b * 4;
+    // ubar = -i W conj(T s), sbar = -i W conj(u^T T); M_ac = sum_q W u_a s_c (the staged windows
+    // are read by every lane before the region is overwritten)
+    __syncwarp();
     // M partials of the lane's pixels in the working precision; the warp and site sums in FP64
     Rl mr[B][B], mi[B][B];
 #pragma unroll
@@ -355,7 +382,24 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(int b, int n, int w, in
     const int n2 = n >> 1, side = 2 * w + 1, nsite = n * n, Wmb = W * mb;
     const int X = xb - Rb, Y = yb - Rb;
     const int ou = r1 - bs0, os_ = r2 - bs0;
+    // FP64 sums for the FP64 working type; FP32 with compensation (Kahan) for the mixed
+    // handle's FP32 window gradients (FP64 adds run at 1/64 of the FP32 rate here)
+    constexpr bool F32 = std::is_same<C, float2>::value;
     double sx = 0.0, sy = 0.0;
+    float fx = 0.f, fy = 0.f, cx = 0.f, cy = 0.f;
+    auto add = [&](C v) {
+        if constexpr (F32) {
+            const float yx = (float)v.x - cx, tx = fx + yx;
+            cx = (tx - fx) - yx;
+            fx = tx;
+            const float yy = (float)v.y - cy, ty = fy + yy;
+            cy = (ty - fy) - yy;
+            fy = ty;
+        } else {
+            sx += (double)v.x;
+            sy += (double)v.y;
+        }
+    };
     for (int imp = 0; imp < nimp; imp++) {
         const int ei = e * nimp + imp;
         for (int d = 0; d < W; d++) {
@@ -363,18 +407,20 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(int b, int n, int w, in
             if (ou >= 0 && ou < mb) {
                 const int i = X - dx + n2, j = Y - dy + n2;    // site R - d
                 if (i >= 0 && i < n && j >= 0 && j < n) {
-                    const C v = Ub[(((size_t)ei * Wmb + d * mb + ou) * b + r2) * nsite + (size_t)i * n + j];
-                    sx += (double)v.x; sy += (double)v.y;
+                    add(Ub[(((size_t)ei * Wmb + d * mb + ou) * b + r2) * nsite + (size_t)i * n + j]);
                 }
             }
             if (os_ >= 0 && os_ < mb) {
                 const int i = -X - dx + n2, j = -Y - dy + n2;  // site -R - d
                 if (i >= 0 && i < n && j >= 0 && j < n) {
-                    const C v = Sb[(((size_t)ei * Wmb + d * mb + os_) * b + r1) * nsite + (size_t)i * n + j];
-                    sx += (double)v.x; sy += (double)v.y;
+                    add(Sb[(((size_t)ei * Wmb + d * mb + os_) * b + r1) * nsite + (size_t)i * n + j]);
                 }
             }
         }
+    }
+    if constexpr (F32) {
+        sx = (double)fx - (double)cx;
+        sy = (double)fy - (double)cy;
     }
     double2 *g = gbox + (((size_t)e * NB + xb) * NB + yb) * bb + el;
     *g = make_double2(g->x + sx, g->y + sy);
@@ -924,6 +970,90 @@ __global__ void __launch_bounds__(256) adj_rows_reg_kernel(int NB, int Rb, float
     }
 }
 
+// Columns of the same transform for the mixed handle: NC box columns yb of one plane per
+// block; the block gathers the plane's FP64 gradients of its columns from the box (NC values
+// of one X at a time), puts X at position (X - Rb) mod kp, and writes the transformed columns
+// A[plane][yb][kx] in FP32 (unscaled; the rows apply kp^-2).
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) adj_cols_reg_kernel(int NB, int Rb, int bb, const double2 *__restrict__ gbox,
+                                                           const float2 *__restrict__ tw, float2 *__restrict__ A)
+{
+    constexpr int KP = N1 * N2;
+    constexpr int NC = 256 / (N1 > N2 ? N1 : N2);
+    constexpr int PLEN = KP + KP / 32 + 1;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tws = sm + (size_t)NC * PLEN;
+    const int yb0 = blockIdx.x * NC, pl = blockIdx.y;
+    for (int t = threadIdx.x; t < KP; t += blockDim.x) {
+        const int k2 = t / N1, n1 = t - k2 * N1;
+        tws[t] = tw[(n1 * k2) & (KP - 1)];
+    }
+    for (int t = threadIdx.x; t < NC * PLEN; t += blockDim.x) sm[t] = make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < NB * NC; idx += blockDim.x) {
+        const int xb = idx / NC, c = idx - xb * NC, yb = yb0 + c;
+        if (yb >= NB) continue;
+        const double2 v = gbox[((size_t)xb * NB + yb) * bb + pl];
+        const int pos = (xb - Rb + KP) & (KP - 1);
+        sm[(size_t)c * PLEN + pad32(pos)] = make_float2((float)v.x, -(float)v.y);
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < NC * N1; task += blockDim.x) {
+        const int c = task / N1, n1 = task - c * N1;
+        float2 *a = sm + (size_t)c * PLEN;
+        float2 x[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; n2++) x[n2] = a[pad32(n1 + N1 * n2)];
+        fft_reg<N2>(x);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) a[pad32(n1 + N1 * k2)] = cmul(x[k2], tws[k2 * N1 + n1]);
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < NC * N2; task += blockDim.x) {
+        const int c = task / N2, k2 = task - c * N2, yb = yb0 + c;
+        if (yb >= NB) continue;
+        const float2 *a = sm + (size_t)c * PLEN;
+        float2 x[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++) x[n1] = a[pad32(n1 + N1 * k2)];
+        fft_reg<N1>(x);
+        float2 *dst = A + ((size_t)pl * NB + yb) * KP;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; k1++) dst[k2 + N2 * k1] = make_float2(x[k1].x, -x[k1].y);
+    }
+}
+
+template <int N1, int N2>
+static void launch_adj_cols_reg(cqpi_handle *h, const double2 *gbe, float2 *A)
+{
+    constexpr int KP = N1 * N2, NC = 256 / (N1 > N2 ? N1 : N2);
+    const size_t smem = 8 * ((size_t)NC * (KP + KP / 32 + 1) + KP);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(adj_cols_reg_kernel<N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
+    adj_cols_reg_kernel<N1, N2><<<dim3(cdiv(h->NB, NC), h->b * h->b), 256, smem, h->stream>>>(
+        h->NB, h->Rb, h->b * h->b, gbe, h->d_tw32, A);
+}
+
+// the register columns transform of the mixed handle (CQPI_ADJ_ROWS=radix2 keeps adj_cols_kernel)
+static bool adj_cols_reg(cqpi_handle *h, const double2 *gbe, float2 *A)
+{
+    const char *f = getenv("CQPI_ADJ_ROWS");
+    if (h->NB > h->kp || (f && !strcmp(f, "radix2"))) return false;
+    switch (h->kp) {
+    case 64: launch_adj_cols_reg<8, 8>(h, gbe, A); return true;
+    case 128: launch_adj_cols_reg<8, 16>(h, gbe, A); return true;
+    case 256: launch_adj_cols_reg<16, 16>(h, gbe, A); return true;
+    case 512: launch_adj_cols_reg<16, 32>(h, gbe, A); return true;
+    case 1024: launch_adj_cols_reg<32, 32>(h, gbe, A); return true;
+    case 2048: launch_adj_cols_reg<32, 64>(h, gbe, A); return true;
+    case 4096: launch_adj_cols_reg<64, 64>(h, gbe, A); return true;
+    }
+    return false;
+}
+
 template <int N1, int N2>
 static void launch_adj_rows_reg(cqpi_handle *h, const float2 *A, float2 *gk)
 {
@@ -972,8 +1102,9 @@ void launch_adj_kspace(cqpi_handle *h, int e, AdjWorkspace &aw)
         // the mixed handle: the transform and the per-k rotation in FP32, in the same buffers
         const size_t smem = sizeof(float2) * kp;
         float2 *A32 = reinterpret_cast<float2 *>(aw.A), *gk32 = reinterpret_cast<float2 *>(aw.gk);
-        adj_cols_kernel<float2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe, h->d_tw32,
-                                                                           A32);
+        if (!adj_cols_reg(h, gbe, A32))
+            adj_cols_kernel<float2><<<dim3(h->NB, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb, gbe,
+                                                                               h->d_tw32, A32);
         if (!adj_rows_reg(h, A32, gk32 + (size_t)e * bb * nk))
             adj_rows_kernel<float2><<<dim3(kp, bb), 256, smem, h->stream>>>(kp, logkp, h->NB, h->Rb, bb,
                                                                             1.0 / ((double)kp * kp), A32, h->d_tw32,

@@ -148,9 +148,9 @@ def test_set_hoppings_rebuilds_bands(built_lib):
 
 @pytest.mark.parametrize("kp,lattice", [(64, 8), (256, 12)])
 def test_adjoint_register_rows_match_radix2(built_lib, kp, lattice, monkeypatch):
-    """Mixed handle: the box -> k-grid rows of the adjoint by the four-step register transform
-    (several k_x columns per block) give the gradients of the radix-2 one-column-per-block
-    kernel (CQPI_ADJ_ROWS=radix2) to FP32 rounding."""
+    """Mixed handle: the box -> k-grid columns and rows of the adjoint by the four-step
+    register transforms (several columns per block) give the gradients of the radix-2
+    one-column-per-block kernels (CQPI_ADJ_ROWS=radix2) to FP32 rounding."""
     import cqpi
     from cqpi import workloads as W
     m = W.t2g_c2()
