@@ -3,8 +3,8 @@
 // Replaces tmatrix::calchamiltonian (src/qpi.cc:454-475), which calls
 // tightbind::setmatrix (src/tightbinding.cc:210-219) and gsl_eigen_hermv per
 // k-point.  One thread owns one k-point; the b x b matrix and its eigenvectors
-// live in registers (b is a template parameter padded up to B; up to 6 bands fully unrolled,
-// 8 to 16 bands in local memory with the loops kept: bands_kernel_wide, the same body
+// live in registers (b is a template parameter padded up to B; up to 5 bands fully unrolled,
+// 6 to 16 bands in local memory with the loops kept: bands_kernel_wide, the same body
 // from bands_kernel.cuh).  The solver is
 // cyclic complex Jacobi in FP64: G0(k) is invariant under eigenvector phase and
 // ordering, so it matches any exact Hermitian eigensolver to rounding.
@@ -42,7 +42,9 @@ static void launch_bands_t(cqpi_handle *h)
     const long long nk = (long long)h->kp * h->kp;
     const long long nthr = h->time_reversal ? (long long)(h->kp / 2 + 1) * h->kp : nk;
     const int tr = h->time_reversal ? 1 : 0, mixed = bands_mixed();
-    if constexpr (B <= 6)
+    // fully unrolled up to 5 bands; from 6 bands the loop-kept body (the unrolled 6-band copy
+    // spilled 7 KB per thread: CJ eigen-solve 13.6 ms against 12.9 ms loop-kept)
+    if constexpr (B <= 5)
         bands_kernel<B><<<cdiv(nthr, 128), 128, 0, h->stream>>>(h->b, h->kp, tr, h->scmax, h->efermi, h->npair_R,
                                                                 h->d_pR, h->d_pPQ, h->d_eval, h->d_evec,
                                                                 h->d_evec32, h->d_eval32, h->d_tw, mixed);
@@ -61,6 +63,7 @@ void launch_bands(cqpi_handle *h)
     else if (b <= 2) launch_bands_t<2>(h);
     else if (b <= 3) launch_bands_t<3>(h);
     else if (b <= 4) launch_bands_t<4>(h);
+    else if (b <= 5) launch_bands_t<5>(h);
     else if (b <= 6) launch_bands_t<6>(h);
     else if (b <= 8) launch_bands_t<8>(h);
     else if (b <= 10) launch_bands_t<10>(h);

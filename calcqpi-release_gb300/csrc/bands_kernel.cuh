@@ -1,8 +1,8 @@
 // bands_kernel.cuh -- the body of the per-k eigen-solve kernel, included twice by bands.cu:
-// as bands_kernel with full unrolling of its b x b loop nests (band counts up to 6, whose
-// matrices stay in registers) and as bands_kernel_wide with the loops kept (8 to 16 bands,
-// whose matrices live in local memory either way; unrolled, their b^3 .. b^4 nests only made
-// the compiler run for minutes).  The includer defines CQPI_BANDS_KERNEL (the kernel's name)
+// as bands_kernel with full unrolling of its b x b loop nests (band counts up to 5, whose
+// matrices stay in registers) and as bands_kernel_wide with the loops kept (6 to 16 bands,
+// whose matrices live in local memory either way; unrolled, the 6-band copy spilled 7 KB per
+// thread and the larger b^3 .. b^4 nests only made the compiler run for minutes).  The includer defines CQPI_BANDS_KERNEL (the kernel's name)
 // and CQPI_BANDS_UNROLL (the loop pragma).
 // tr: all hoppings are real, so H(-k) = conj(H(k)): threads cover the k_x rows
 // 0 .. kp/2 only and each writes its k-point and the point reflection -k (same

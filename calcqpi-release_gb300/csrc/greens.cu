@@ -95,6 +95,7 @@ void launch_greens_k(cqpi_handle *h, int ne, const double *d_energies)
     else if (b <= 2) launch_greens_k_t<2>(h, ne, d_energies);
     else if (b <= 3) launch_greens_k_t<3>(h, ne, d_energies);
     else if (b <= 4) launch_greens_k_t<4>(h, ne, d_energies);
+    else if (b <= 5) launch_greens_k_t<5>(h, ne, d_energies);
     else if (b <= 6) launch_greens_k_t<6>(h, ne, d_energies);
     else if (b <= 8) launch_greens_k_t<8>(h, ne, d_energies);
     else if (b <= 10) launch_greens_k_t<10>(h, ne, d_energies);
