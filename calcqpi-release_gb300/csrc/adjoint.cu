@@ -430,23 +430,23 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(int b, int n, int w, in
 __global__ void __launch_bounds__(256) adj_mreduce_kernel(int nsite, int bb, const double2 *__restrict__ Mp,
                                                           double2 *__restrict__ M)
 {
-    __shared__ double2 red[8];
-    const int ei = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = 0; k < bb; k++) {
-        double2 s = make_double2(0.0, 0.0);
-        for (int p = threadIdx.x; p < nsite; p += blockDim.x) s = cadd(s, Mp[((size_t)ei * nsite + p) * bb + k]);
-        for (int o = 16; o > 0; o >>= 1) {
-            s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
-            s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
-        }
-        if (lane == 0) red[warp] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 t = make_double2(0.0, 0.0);
-            for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) t = cadd(t, red[wv]);
-            M[(size_t)ei * bb + k] = t;
-        }
-        __syncthreads();
+    // the threads in use are a multiple of bb, so thread t reads the contiguous parts array
+    // at stride nt (coalesced) and always the element t % bb; then a fixed-order sum per element
+    __shared__ double2 red[256];
+    const int ei = blockIdx.x, t = threadIdx.x;
+    const int nt = ((int)blockDim.x / bb) * bb;
+    double2 sum = make_double2(0.0, 0.0);
+    if (t < nt) {
+        const double2 *src = Mp + (size_t)ei * nsite * bb;
+        const size_t n = (size_t)nsite * bb;
+        for (size_t i = t; i < n; i += nt) sum = cadd(sum, src[i]);
+    }
+    red[t] = sum;
+    __syncthreads();
+    if (t < bb) {
+        double2 u = make_double2(0.0, 0.0);
+        for (int v = t; v < nt; v += bb) u = cadd(u, red[v]);
+        M[(size_t)ei * bb + t] = u;
     }
 }
 
@@ -826,9 +826,13 @@ static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>:
     constexpr int wpb = AdjWpb<C>::value;
     const size_t wsm = sizeof(Rl) * ((size_t)h->W * h->mb * ADJ_QP + wpb * 128 * (size_t)h->b * 4);
     bool warp_form = false;
+    if constexpr (B <= 4 && std::is_same<C, float2>::value) {
+        // the mixed handle: the two products on the tensor cores (adjoint_mma.cu)
+        warp_form = launch_adj_contract_mma(h, ne, phi, box, wmap, Ub, Sb, aw.Mp);
+    }
     if constexpr (B <= 4) {
         // one warp per site when the orbital table and the warps' ubar / sbar rows fit
-        if (wsm <= 200 * 1024 &&
+        if (!warp_form && wsm <= 200 * 1024 &&
             cudaFuncSetAttribute(adj_contract_warp_kernel<B, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm) ==
                 cudaSuccess) {
             adj_contract_warp_kernel<B, C><<<dim3(cdiv(nsite, wpb), (unsigned)(ne * h->nimp)), 32 * wpb, wsm,

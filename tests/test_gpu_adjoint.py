@@ -172,3 +172,47 @@ def test_adjoint_register_rows_match_radix2(built_lib, kp, lattice, monkeypatch)
     (gt, gv), (rt, rv) = out
     assert np.abs(gt - rt).max() <= 1e-5 * np.abs(rt).max()
     assert np.abs(gv - rv).max() <= 1e-5 * np.abs(rv).max()
+
+
+@pytest.mark.parametrize("kind", ["c1", "c2", "c5_cell", "impurities"])
+def test_adjoint_tensor_core_contraction_matches_cuda_cores(built_lib, kind, monkeypatch):
+    """Mixed handle: the contraction adjoint on the tensor cores (split-fp16 x 3 products,
+    adjoint_mma.cu) against the CUDA-core warp-per-site kernel (CQPI_ADJ_MMA=0): the same
+    gradients to FP32 rounding, for 1 and 3 bands, a C5-sized cell (10x10 sub-pixels, 75 window
+    entries) and two impurities."""
+    import cqpi
+    from cqpi import workloads as W
+    rng = np.random.default_rng(23)
+    A = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+
+    def engine():
+        if kind in ("c1", "c2"):
+            m, p, wf, z, v, E = case(kind)
+            eng = cqpi.Engine(m, p["lattice"], p["kpoints"], p["oversamp"], p["window"], p["eta"],
+                              precision=cqpi.PREC_MIXED)
+            eng.set_orbitals(wf, z)
+            eng.set_scattering(v)
+            return eng, E, p["lattice"] * p["oversamp"], 1
+        eng = cqpi.Engine(W.t2g_c2(), 8, 64, 10, 2, 0.01, precision=cqpi.PREC_MIXED)
+        eng.set_orbitals(W.t2g_orbitals_c2(2, 10))
+        if kind == "impurities":
+            eng.set_impurities(np.stack([np.diag([0.3, 0.3, 0.5]), 0.2 * (A + A.conj().T)]).astype(complex))
+            return eng, np.array([-0.05, 0.03]), 80, 2
+        eng.set_scattering(np.array([0.3, 0.3, 0.5], complex))
+        return eng, np.array([-0.05, 0.03]), 80, 1
+
+    Wt = None
+    out = []
+    for env in (None, "0"):
+        if env:
+            monkeypatch.setenv("CQPI_ADJ_MMA", env)
+        else:
+            monkeypatch.delenv("CQPI_ADJ_MMA", raising=False)
+        eng, E, wn, nimp = engine()
+        if Wt is None:
+            Wt = rng.normal(size=(len(E), nimp, wn, wn)).astype(np.float32)
+        out.append(eng.adjoint(E, Wt))
+        eng.close()
+    (gt, gv), (rt, rv) = out
+    assert np.abs(gt - rt).max() <= 1e-5 * np.abs(rt).max()
+    assert np.abs(gv - rv).max() <= 1e-5 * np.abs(rv).max()
