@@ -450,6 +450,37 @@ __global__ void __launch_bounds__(256) adj_mreduce_kernel(int nsite, int bb, con
     }
 }
 
+// The same sum over FP32 per-site parts (the tensor-core contraction adjoint's): per-thread
+// sums in FP32 with compensation (Kahan), the fixed-order per-element sum in FP64
+__global__ void __launch_bounds__(256) adj_mreduce32_kernel(int nsite, int bb, const float2 *__restrict__ Mp,
+                                                            double2 *__restrict__ M)
+{
+    __shared__ double2 red[256];
+    const int ei = blockIdx.x, t = threadIdx.x;
+    const int nt = ((int)blockDim.x / bb) * bb;
+    float sx = 0.f, sy = 0.f, cx = 0.f, cy = 0.f;
+    if (t < nt) {
+        const float2 *src = Mp + (size_t)ei * nsite * bb;
+        const size_t n = (size_t)nsite * bb;
+        for (size_t i = t; i < n; i += nt) {
+            const float2 v = src[i];
+            const float yx = v.x - cx, tx = sx + yx;
+            cx = (tx - sx) - yx;
+            sx = tx;
+            const float yy = v.y - cy, ty = sy + yy;
+            cy = (ty - sy) - yy;
+            sy = ty;
+        }
+    }
+    red[t] = make_double2((double)sx - (double)cx, (double)sy - (double)cy);
+    __syncthreads();
+    if (t < bb) {
+        double2 u = make_double2(0.0, 0.0);
+        for (int v = t; v < nt; v += bb) u = cadd(u, red[v]);
+        M[(size_t)ei * bb + t] = u;
+    }
+}
+
 // wsum[e][q] = sum over the impurities' maps and the sites of W at sub-pixel q = qx*os + qy.
 // One block per (qy, energy of the batch): it reads the map rows y = j*os + qy of every
 // impurity, contiguous in x; the threads in use are a multiple of os, so thread t sums the one
@@ -825,10 +856,10 @@ static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>:
     using Rl = typename real_of<C>::type;
     constexpr int wpb = AdjWpb<C>::value;
     const size_t wsm = sizeof(Rl) * ((size_t)h->W * h->mb * ADJ_QP + wpb * 128 * (size_t)h->b * 4);
-    bool warp_form = false;
+    bool warp_form = false, mma = false;
     if constexpr (B <= 4 && std::is_same<C, float2>::value) {
         // the mixed handle: the two products on the tensor cores (adjoint_mma.cu)
-        warp_form = launch_adj_contract_mma(h, ne, phi, box, wmap, Ub, Sb, aw.Mp);
+        warp_form = mma = launch_adj_contract_mma(h, ne, phi, box, wmap, Ub, Sb, reinterpret_cast<float2 *>(aw.Mp));
     }
     if constexpr (B <= 4) {
         // one warp per site when the orbital table and the warps' ubar / sbar rows fit
@@ -847,7 +878,11 @@ static void launch_contract_t(cqpi_handle *h, int ne, const typename real_of<C>:
                                                                h->mb, h->blk_start[0], phi, box, h->ws.T, wmap, Ub, Sb, aw.Mp);
     adj_gather_kernel<C><<<dim3(cdiv(h->NB, 128), (unsigned)h->NB, (unsigned)(ne * bb)), 128, 0, h->stream>>>(
         h->b, h->n, h->w, h->Rb, h->NB, h->W, h->mb, h->blk_start[0], h->nimp, Ub, Sb, aw.gbox);
-    adj_mreduce_kernel<<<(unsigned)(ne * h->nimp), 256, 0, h->stream>>>(nsite, bb, aw.Mp, aw.M);
+    if (mma)
+        adj_mreduce32_kernel<<<(unsigned)(ne * h->nimp), 256, 0, h->stream>>>(
+            nsite, bb, reinterpret_cast<const float2 *>(aw.Mp), aw.M);
+    else
+        adj_mreduce_kernel<<<(unsigned)(ne * h->nimp), 256, 0, h->stream>>>(nsite, bb, aw.Mp, aw.M);
     adj_wsum_kernel<<<dim3((unsigned)h->os, (unsigned)ne), 256, 0, h->stream>>>(h->wn, h->os, h->Q, h->nimp, wmap,
                                                                                aw.wsum);
     h->launches += 4;

@@ -12,8 +12,9 @@
 // forward contraction (representation error 2^-22).  Phi's two fragment layouts (A of the
 // forward, M = q; A of the gradient, M = t) are built once per block in shared memory in the
 // per-lane register order of mma.m16n8k16, so each lane loads a fragment as one 16-byte read.
-// Outputs and the M partials are those of adj_contract_warp_kernel (same layouts), which stays
-// for more than 4 bands, more than 112 sub-pixels or 80 window entries, and the FP64 handle.
+// Outputs are those of adj_contract_warp_kernel (same layouts), which stays for more than 4
+// bands, more than 112 sub-pixels or 80 window entries, and the FP64 handle; the per-site M
+// parts are FP32 here (adj_mreduce32_kernel sums them).
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(32 * AM_WARPS, 1) adj_contract_mma_kernel(
     int b, int n, int os, int w, int Rb, int NB, int Q, int W, int nimp, int nmaps, int mb, int bs0,
     const float *__restrict__ phi,
     const float2 *__restrict__ box, const double2 *__restrict__ T, const float *__restrict__ wmap,
-    float2 *__restrict__ Ub, float2 *__restrict__ Sb, double2 *__restrict__ Mp)
+    float2 *__restrict__ Ub, float2 *__restrict__ Sb, float2 *__restrict__ Mp)
 {
     extern __shared__ __align__(16) unsigned char am_sm[];
     // [tile][step][hi/lo][lane] uint4 fragments: forward A (M = q) and gradient A (M = t)
@@ -288,13 +289,13 @@ __global__ void __launch_bounds__(32 * AM_WARPS, 1) adj_contract_mma_kernel(
 #pragma unroll
             for (int c = 0; c < B; c++) {
                 if (a >= b || c >= b) continue;
-                // the warp sum in FP32 (4 pixels per lane, 32 lanes); the site sum in FP64
+                // the warp sum in FP32 (4 pixels per lane, 32 lanes); FP32 parts per site
                 float xr = mr[a][c], xi = mi[a][c];
                 for (int o = 16; o > 0; o >>= 1) {
                     xr += __shfl_xor_sync(0xffffffffu, xr, o);
                     xi += __shfl_xor_sync(0xffffffffu, xi, o);
                 }
-                if (lane == 0) Mp[((size_t)ei * nsite + site) * bb + a * b + c] = make_double2(xr, xi);
+                if (lane == 0) Mp[((size_t)ei * nsite + site) * bb + a * b + c] = make_float2(xr, xi);
             }
         const float sX = pow2_scale_of(warp_max(xmx));
         __syncwarp();
@@ -347,7 +348,7 @@ static size_t mma_smem(const cqpi_handle *) { return 16 * (size_t)(2 * MQ * KT *
 
 template <int B>
 static bool launch_mma_t(cqpi_handle *h, int ne, const float *phi, const float2 *box, const float *wmap, float2 *Ub,
-                         float2 *Sb, double2 *Mp)
+                         float2 *Sb, float2 *Mp)
 {
     const size_t smem = mma_smem(h);
     if (cudaFuncSetAttribute(adj_contract_mma_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -364,7 +365,7 @@ static bool launch_mma_t(cqpi_handle *h, int ne, const float *phi, const float2 
 // The tensor-core contraction adjoint (false: not applicable, the caller runs the CUDA-core
 // kernel; CQPI_ADJ_MMA=0 forces that)
 bool launch_adj_contract_mma(cqpi_handle *h, int ne, const float *phi, const float2 *box, const float *wmap,
-                             float2 *Ub, float2 *Sb, double2 *Mp)
+                             float2 *Ub, float2 *Sb, float2 *Mp)
 {
     const char *f = getenv("CQPI_ADJ_MMA");
     if ((f && !strcmp(f, "0")) || h->b > 4 || h->Q > MQ * 16 || h->W * h->mb > KT * 16 || mma_smem(h) > 227 * 1024)

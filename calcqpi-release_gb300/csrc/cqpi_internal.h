@@ -292,7 +292,7 @@ bool launch_fft32_planes(cqpi_handle *h, int ne);
 bool g0k_reciprocity(const cqpi_handle *h);   // G0(k) planes of the unfused path: upper triangle only
 // adjoint_mma.cu: the mixed handle's contraction adjoint on the tensor cores (false: not applicable)
 bool launch_adj_contract_mma(cqpi_handle *h, int ne, const float *phi, const float2 *box, const float *wmap,
-                             float2 *Ub, float2 *Sb, double2 *Mp);
+                             float2 *Ub, float2 *Sb, float2 *Mp);
 // ldos_tc.cu
 bool tc_supported(const cqpi_handle *h);
 void tc_plan(cqpi_handle *h);
