@@ -84,9 +84,9 @@ __global__ void __launch_bounds__(32 * AM_WARPS, 1) adj_contract_mma_kernel(
     uint4 *gA = fA + MQ * KT * 2 * 32;
     float *wbuf = reinterpret_cast<float *>(gA + KT * MQ * 2 * 32);   // [warp][ROWS][RS]
     __shared__ float s_red[32];
-    // window staging: offset of entry (t, n) from the site's u or s base point in the box (bit 30
-    // set: the s operand), -1: zero (padding)
-    __shared__ int s_off[KT * 16 * 16];
+    // window staging: offset (floats) of the complex entry (t, n pair) from the site's u or s base
+    // point in the box (bit 30 set: the s operand), -1: zero (padding)
+    __shared__ int s_off[KT * 16 * 8];
     const int Wmb = W * mb;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = lane >> 2, tg = lane & 3;
@@ -129,11 +129,11 @@ __global__ void __launch_bounds__(32 * AM_WARPS, 1) adj_contract_mma_kernel(
     }
     {
         const int side_ = 2 * w + 1;
-        for (int idx = tid; idx < KT * 16 * 16; idx += blockDim.x) {
-            const int t = idx >> 4, nn = idx & 15;
+        for (int idx = tid; idx < KT * 16 * 8; idx += blockDim.x) {
+            const int t = idx >> 3, nn = 2 * (idx & 7), ri = 0;
             int off = -1;
             if (t < Wmb && nn < 4 * b) {
-                const int op = nn / (2 * b), a = (nn - op * 2 * b) >> 1, ri = nn & 1;
+                const int op = nn / (2 * b), a = (nn - op * 2 * b) >> 1;
                 const int d = t / mb, o = bs0 + (t - d * mb);
                 const int dx = d / side_ - w, dy = d % side_ - w;
                 // u: G(p+d)[o][a] at ((px+dx+Rb) NB + py+dy+Rb) bb; s: G(-p-d)[a][o] at ((-px-dx+Rb) NB + ...)
@@ -166,15 +166,15 @@ __global__ void __launch_bounds__(32 * AM_WARPS, 1) adj_contract_mma_kernel(
         const float *bf = reinterpret_cast<const float *>(boxe);
         const long long ub = 2LL * (((long long)(px + Rb) * NB + (py + Rb)) * bb);    // float units
         const long long sbs = 2LL * (((long long)(-px + Rb) * NB + (-py + Rb)) * bb);
-        for (int idx = lane; idx < KT * 16 * 16; idx += 32) {
+        for (int idx = lane; idx < KT * 16 * 8; idx += 32) {
             const int off = s_off[idx];
-            float v = 0.f;
+            float2 v = make_float2(0.f, 0.f);
             if (off >= 0) {
                 const int rel = ((off & 0x3fffffff) ^ 0x20000000) - 0x20000000;   // sign-extend 30 bits
-                v = bf[((off >> 30) ? sbs : ub) + rel];
+                v = *reinterpret_cast<const float2 *>(bf + ((off >> 30) ? sbs : ub) + rel);
             }
-            buf[(idx >> 4) * RS + (idx & 15)] = v;
-            wmx = fmaxf(wmx, fabsf(v));
+            *reinterpret_cast<float2 *>(buf + (idx >> 3) * RS + 2 * (idx & 7)) = v;
+            wmx = fmaxf(wmx, fmaxf(fabsf(v.x), fabsf(v.y)));
         }
         const float sG = pow2_scale_of(warp_max(wmx));
         __syncwarp();
