@@ -359,7 +359,7 @@ def run_ours(args):
         # dram__bytes_read.sum + dram__bytes_write.sum of one contraction launch of 32 energies
         # on a 192^2-site field of view (one ncu capture: profiles/launches_c2_mixed.md), scaled
         # to this 256^2-site launch by the pixels it writes and the window sites it reads
-        roof["traffic"] = (178.2e6 + 411.8e6) * (256.0 / 192.0) ** 2
+        roof["traffic"] = (178.1e6 + 414.6e6) * (256.0 / 192.0) ** 2
         roof["traffic_note"] = ("bytes per contraction launch of 32 energies (ncu, 192^2-site launch x 1.78); "
                                 "algorithmic: the u windows from 32 G0(R) boxes and the s windows from 32 T G0(R) "
                                 "boxes (2 x 157 MB) + 32 maps (839 MB)")
