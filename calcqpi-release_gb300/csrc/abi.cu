@@ -217,10 +217,12 @@ void ensure_workspace(cqpi_handle *h, int ebatch)
     } else {
         if (!h->use_fft32 || h->gmode != CQPI_GREEN_NORMAL) dalloc(&h->ws.g0k32, ebatch * bb * nk);
         dalloc(&h->ws.half32, ebatch * bb * (size_t)h->kp * h->NB);
-        dalloc(&h->ws.box32, ebatch * (size_t)h->NB * h->NB * bb);
+        const size_t nbox = box32_boxes(h, ebatch), ncnt = box32_count(h, ebatch);
+        dalloc(&h->ws.box32, ncnt);
+        CK(cudaMemsetAsync(h->ws.box32 + nbox, 0, sizeof(float2) * (ncnt - nbox), h->stream));
         dalloc(&h->ws.gmax, ebatch);
         if (h->use_tc) {
-            dalloc(&h->ws.boxT32, ebatch * (size_t)h->NB * h->NB * bb);
+            dalloc(&h->ws.boxT32, ncnt);
             dalloc(&h->ws.gmaxT, ebatch);
         }
     }

@@ -48,6 +48,7 @@ struct TcPlan {
     int wEB = 0;         // energies per tile
     int wNRAW = 0;       // raw-window ring depth (fetches run wNRAW-1 tiles ahead)
     int wNX = 0;         // window width in sites (8*wH + 2*window)
+    int w_nbulk = 0;     // raw columns per tile fetched by bulk copies, the rest by cp.async
     int wNKC = 0;        // 8-element K chunks per window row (even)
     int wKP = 0;         // A columns: (2*window+1) * wNKC * 8
     int w_a_bytes = 0, w_win_bytes = 0, w_sst = 0, w_tmem_cols = 0;
@@ -60,6 +61,7 @@ struct TcParams {
     int TS, N, KP, Q, nimp, ne, wn, ntx, sst;
     int tmem_cols, a_bytes, b_bytes;
     int H, NX, NKC, win_bytes, EB, nraw;   // direct-window variant
+    int nbulk;                   // direct-window variant: raw columns fetched by bulk copies (the rest by cp.async)
     int a_tmem;                  // direct-window variant: Phi operand held in tensor memory
     int stall;                   // fault injection: wait on a barrier nothing arrives on
     int coff;                    // Josephson mode: column offset of the s operand (bands/2), else 0
@@ -73,6 +75,7 @@ struct TcParams {
     const unsigned *gmax;
     const float2 *boxT;          // direct-window variant, one impurity: (T G0)(R) per energy for the s
     const unsigned *gmaxT;       // operand (T folded out of the epilogue) and its max |Re|,|Im|; else NULL
+    const float2 *zsrc;          // direct-window variant: 16-byte aligned zeros, at least one raw column
     const uint4 *Aimg;
     float *out;
     const int *fov;              // direct-window variant: per-map field of view (sites per side) or NULL
@@ -319,6 +322,13 @@ void launch_ldos_list(cqpi_handle *h, int ne, const void *box, const void *T, co
 cudaError_t launch_ldos_tc(cqpi_handle *h, int ne, float *out, const int *fov = nullptr,
                            const long long *fov_off = nullptr);
 bool tc_window_usable(const cqpi_handle *h);   // the direct-window kernel runs (per-map FOV support)
+// The FP32 box buffers (box32, boxT32) carry a tail after their ebatch boxes: slack for the
+// contraction's 16-byte-aligned bulk copies, which may read 16 bytes past a window column,
+// and (box32) zeros from the first 16-byte boundary after the boxes, NB*b*b + 8 complex
+// values long, the source of the raw columns outside the box (at least one column).
+inline size_t box32_boxes(const cqpi_handle *h, int ebatch) { return (size_t)ebatch * h->NB * h->NB * h->b * h->b; }
+inline size_t box32_count(const cqpi_handle *h, int ebatch) { return box32_boxes(h, ebatch) + 2 + (size_t)h->NB * h->b * h->b + 8; }
+inline const float2 *box32_zeros(const cqpi_handle *h) { return h->ws.box32 + ((box32_boxes(h, h->ws.ebatch) + 1) & ~(size_t)1); }
 bool window_config(const cqpi_handle *h, int EB, int H, int nraw, TcPlan &pl);
 cudaError_t tc_autotune(cqpi_handle *h, int ne, float *out, float *best_ms, int *tried);
 void launch_widen(cqpi_handle *h, const float *src, double *dst, size_t n);

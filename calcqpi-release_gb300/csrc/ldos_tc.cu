@@ -399,6 +399,12 @@ __device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, uint32_
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// arrive on mbar when every earlier cp.async of this thread has landed (counted in the
+// barrier's initial arrival count)
+__device__ __forceinline__ void cp_async_mbar_arrive(uint32_t mbar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mbar) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait_n() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
@@ -732,6 +738,20 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
+// arrive on mbar and add bytes of asynchronous copies to the current phase (the copies may
+// land before this arrival: the transaction count may go negative meanwhile)
+__device__ __forceinline__ void mbar_arrive_expect(uint32_t mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+// bulk copy global -> shared of bytes (a multiple of 16; both addresses 16-byte aligned),
+// completing its bytes on mbar
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
 // D (+)= A x B with A read from tensor memory (lane m = row m, 16-bit K pairs per column)
 __device__ __forceinline__ void mma_f16_ta(uint32_t dtmem, uint32_t atmem, uint64_t bd, uint32_t idesc, uint32_t acc)
 {
@@ -753,8 +773,10 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 }  // namespace tc
 
 // JOS: the Josephson form (p.coff, p.tip); a template flag so that the LDOS epilogue keeps
-// its register budget.
-template <int B, bool JOS, bool FOLD>
+// its register budget.  BULK: the first p.nbulk raw columns of a tile are fetched by bulk
+// copies (instantiated for 6 and 8 bands only; without it the producer carries no trace of
+// them: measured 1.3% on the 3-band contraction).
+template <int B, bool JOS, bool FOLD, bool BULK>
 __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_constant__ TcParams p)
 {
     using namespace tc;
@@ -764,7 +786,12 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     const int twob = 2 * p.b;
     const int NX = p.NX, NKC = p.NKC, TS = p.TS, EB = p.EB;
     const int rowlen = side * bb;                 // complex values per raw window column (one X)
-    const int rawfl = NX * rowlen * 2;            // floats per raw window
+    // raw column pitch (complex values): with bulk copies rowlen + 1 rounded up to even, so
+    // that a column's copy can start at the 16-byte boundary at or below its first value;
+    // else rowlen (an odd pitch spreads the converters' strided reads over more banks)
+    const int cpf = (BULK && p.nbulk > 0) ? (rowlen + 2) & ~1 : rowlen;
+    const int rawfl = NX * cpf * 2;               // floats per raw window
+    const int ncol = 2 * EB * NX;                 // raw columns per tile: [op][energy][x]
     const int nval = side * p.mb;                 // K entries per window row that carry data
     const int sbo_a = p.KP * 16;
     const int NMMA = 8 * 2 * EB * twob;           // MMA N: 8 sites x (u, s) x EB energies x (band, re/im)
@@ -785,15 +812,19 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     float *cInv2 = reinterpret_cast<float *>(cT + EB * p.nimp * bb);
     float *cT1 = cInv2 + EB;
     float *cTip = cT1 + EB * 128;   // Josephson tip factor (re, im) [energy]
-    // producer: source offset (float2 units, -1 outside the box) of every raw-window column
-    // of the tile being fetched, [op][energy][x]
+    // producer: float offset (0 or 2) of the first value of every raw column in its copy,
+    // [raw buffer][op][energy][x], then the column table
     const size_t ct_off = ((size_t)(reinterpret_cast<unsigned char *>(cTip + 2 * EB) - sm) + 15) & ~(size_t)15;
-    long long *colTab = reinterpret_cast<long long *>(sm + ct_off);
-    const size_t mb_off = ct_off + 8 * (size_t)(2 * EB * NX);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + mb_off);   // [8]
+    int *shTab = reinterpret_cast<int *>(sm + ct_off);
+    // producer: source offset (float2 units, -1 outside the box) of every raw column of the
+    // tile being fetched, [op][energy][x]
+    long long *colTab = reinterpret_cast<long long *>(sm + ct_off + 4 * (size_t)nraw * ncol);
+    const size_t mb_off = ct_off + 4 * (size_t)nraw * ncol + 8 * (size_t)ncol;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + mb_off);   // [9 + nraw]
     uint64_t *win_full = mbar, *win_empty = mbar + 2, *acc_full = mbar + 4, *acc_empty = mbar + 6;
     uint64_t *never = mbar + 8;    // fault injection: a barrier nothing arrives on
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 9);
+    uint64_t *raw_full = mbar + 9; // raw buffer r: its bulk copies landed
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 13);
     constexpr int NW = TCW_EPI + TCW_PROD;
 
     if (tid < NW) {
@@ -816,10 +847,14 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             offR[i] = v;
         }
         if (tid < 4) raw[zslot + tid] = 0.f;
+        for (int i = tid; i < nraw * ncol; i += NW) shTab[i] = 0;
     }
     if (tid == NW) {
         // acc_empty[s] completes when every epilogue warp has arrived
-        for (int i = 0; i < 9; i++) mbar_init(smem_u32(&mbar[i]), (i == 6 || i == 7) ? TCW_EPI / 32 : 1);
+        // raw_full[r] (i >= 9) completes on one expect-tx arrival and every producer thread's
+        // cp.async arrival
+        for (int i = 0; i < 9 + nraw; i++)
+            mbar_init(smem_u32(&mbar[i]), (i == 6 || i == 7) ? TCW_EPI / 32 : i >= 9 ? 1 + TCW_PROD : 1);
         fence_mbar_init();
     }
     if (warp == 0) tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
@@ -924,12 +959,12 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
     } else if (warp >= TCW_EPI / 32) {
         // ---------------------------------------------------------------- producer
         const int ptid = tid - TCW_EPI;
-        // staging items: one plane row (kchunk, operand, energy, band/re-im, x) of 8 halfs;
         // staging items: the re and im plane rows (kchunk, operand, energy, band, x) of one
         // complex window column, converted together from 8-byte (re, im) loads; the first
-        // three items of this thread are the same in every tile, so they are decomposed once
+        // three items of this thread are the same in every tile, so they are decomposed once.
+        // cidx: the item's raw column [op][energy][x]
         const int nitems = NKC * (nplanes >> 1) * NX;
-        auto item_of = [&](int it, int &rbase, int &toff, int &dst, int &eei) {
+        auto item_of = [&](int it, int &rbase, int &toff, int &dst, int &eei, int &cidx) {
             const int pp = it / NX, xl = it - pp * NX;
             const int a = pp % p.b;
             const int rest = pp / p.b;
@@ -937,16 +972,18 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             const int rest2 = rest / EB;
             const int op = rest2 & 1, kc = rest2 >> 1;
             const int plane = ((kc * 2 + op) * EB + ee) * twob + 2 * a;   // the re plane; im follows
-            const int wbase = (op * EB + ee) * rawfl;
-            rbase = op ? wbase + 2 * (NX - 1 - xl) * rowlen + 2 * a * p.b : wbase + 2 * xl * rowlen + 2 * a;
+            // the s operand reads its columns in reverse x order
+            cidx = (op * EB + ee) * NX + (op ? NX - 1 - xl : xl);
+            rbase = 2 * cidx * cpf + (op ? 2 * a * p.b : 2 * a);
             toff = op * NKC * 8 + kc * 8;
             dst = (plane * NX + xl) * 16;
             eei = op * EB + ee;   // operand and energy: the s operand may carry its own scale
         };
-        int r0 = 0, t0 = 0, d0 = 0, q0 = 0, r1 = 0, t1 = 0, d1 = 0, q1 = 0, r2 = 0, t2 = 0, d2 = 0, q2 = 0;
-        if (ptid < nitems) item_of(ptid, r0, t0, d0, q0);
-        if (ptid + TCW_PROD < nitems) item_of(ptid + TCW_PROD, r1, t1, d1, q1);
-        if (ptid + 2 * TCW_PROD < nitems) item_of(ptid + 2 * TCW_PROD, r2, t2, d2, q2);
+        int r0 = 0, t0 = 0, d0 = 0, q0 = 0, c0 = 0, r1 = 0, t1 = 0, d1 = 0, q1 = 0, c1 = 0;
+        int r2 = 0, t2 = 0, d2 = 0, q2 = 0, c2 = 0;
+        if (ptid < nitems) item_of(ptid, r0, t0, d0, q0, c0);
+        if (ptid + TCW_PROD < nitems) item_of(ptid + TCW_PROD, r1, t1, d1, q1, c1);
+        if (ptid + 2 * TCW_PROD < nitems) item_of(ptid + 2 * TCW_PROD, r2, t2, d2, q2, c2);
         // split scale of (operand, energy) qq = op * EB + ee: the s operand of the folded form is
         // T G0 with its own maximum
         auto scale_of = [&](int e0, int qq) {
@@ -955,11 +992,7 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             if (e >= p.ne) return 1.f;
             return pow2_scale((sop && p.gmaxT) ? p.gmaxT[e] : p.gmax[e]);
         };
-        // cp.async the raw FP32 windows of a tile (zero outside the box and past the last energy)
-        // raw-window columns: thread ptid < ncol owns column ptid = (op, energy, x) of the
-        // column table; copies: thread ptid issues copies ptid, ptid + 256, ... of the
-        // 8-byte pieces (column, piece) in column-major order, advanced without divisions
-        const int ncol = 2 * EB * NX, ncopy = ncol * rowlen;
+        // raw column ptid = (op, energy, x) of a tile, for threads ptid < ncol
         int my_op = 0, my_ee = 0, my_xl = 0;
         if (ptid < ncol) {
             const int w_ = ptid / NX;
@@ -967,36 +1000,59 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             my_op = w_ / EB;
             my_ee = w_ - my_op * EB;
         }
-        const int col0 = ptid / rowlen, pc0 = ptid - col0 * rowlen;
-        const int dcol = TCW_PROD / rowlen, dpc = TCW_PROD - dcol * rowlen;
+        const uint32_t colbytes = (uint32_t)cpf * 8u;
         const long long sofs = FOLD ? (long long)(((uintptr_t)p.boxT - (uintptr_t)p.box) / sizeof(float2)) : 0LL;
-        // column table of a tile (threads < ncol; read after a producer barrier)
+        // column table of a tile: source offset (float2 units from p.box, -1 outside the box
+        // and past the last energy) of every raw column (threads < ncol; read after a
+        // producer barrier)
         auto column_table = [&](int e0, int j, int i0) {
             if (ptid < ncol) {
                 const int py = j - n2, px0 = i0 - n2, e = e0 + my_ee;
                 const int X = my_op == 0 ? px0 - p.w + my_xl : -px0 - (TS - 1) - p.w + my_xl;
                 const int Y0 = my_op == 0 ? py - p.w : -py - p.w;
                 const bool in = e < p.ne && X >= -p.Rb && X <= p.Rb;
-                // the s columns of the folded form read T G0: offset of boxT from box, float2 units
+                // the s columns of the folded form read T G0: offset of boxT from box (both
+                // allocations 256-byte aligned, so the offset is even)
                 const long long base = (FOLD && my_op == 1) ? sofs : 0LL;
                 colTab[ptid] = in ? base + ((long long)e * p.NB * p.NB + (long long)(X + p.Rb) * p.NB + (Y0 + p.Rb)) * bb
                                   : -1LL;
             }
         };
-        // cp.async the raw FP32 windows described by the column table into raw buffer rb
-        // (zero-filled outside the box and past the last energy)
+        // copies: the first nbulk columns one bulk copy each (thread ptid < nbulk: cpf complex
+        // values from the 16-byte boundary at or below the column's first value; the source
+        // boxes have 16 bytes of slack at their end; zeros from p.zsrc), the rest as 8-byte
+        // cp.async pieces (zero-filled), issued by every producer thread in column-major order
+        // and advanced without divisions.  The bulk columns' shifts (0 or 2 floats) go to
+        // shTab (the other entries stay 0).  With bulk copies raw_full[rb] completes on ptid
+        // 0's arrival with the bulk bytes and every producer thread's cp.async arrival (noinc:
+        // counted in the barrier's initial count); without, each fetch is one cp.async group
+        // (measured: the 288 mbarrier arrivals per tile cost the 3-band contraction 7%).
+        const int nbulk = BULK ? (p.nbulk < ncol ? p.nbulk : ncol) : 0;
+        const int ncopy = (ncol - nbulk) * rowlen;
+        const int col0 = nbulk + ptid / rowlen, pc0 = ptid % rowlen;
+        const int dcol = TCW_PROD / rowlen, dpc = TCW_PROD - dcol * rowlen;
         auto fetch_raw = [&](int rb) {
+            const uint32_t bar = smem_u32(&raw_full[rb]);
             float *rawb = raw + rb * rawbuf;
+            if (nbulk > 0 && ptid == 0) mbar_arrive_expect(bar, (uint32_t)nbulk * colbytes);
+            if (ptid < nbulk) {
+                const long long so = colTab[ptid];
+                const int sh = so >= 0 ? (int)(so & 1) : 0;
+                const float2 *src = so >= 0 ? p.box + (so - sh) : p.zsrc;
+                shTab[rb * ncol + ptid] = 2 * sh;
+                bulk_load(smem_u32(rawb + 2 * ptid * cpf), src, colbytes, bar);
+            }
             int col = col0, pc = pc0;
             for (int idx = ptid; idx < ncopy; idx += TCW_PROD) {
                 const long long so = colTab[col];
                 const float2 *src = so >= 0 ? p.box + so + pc : p.box;
-                cp_async8(smem_u32(rawb + 2 * (col * rowlen + pc)), src, so >= 0 ? 8u : 0u);
+                cp_async8(smem_u32(rawb + 2 * (col * cpf + pc)), src, so >= 0 ? 8u : 0u);
                 col += dcol;
                 pc += dpc;
                 if (pc >= rowlen) { pc -= rowlen; col++; }
             }
-            cp_async_commit();
+            if (nbulk > 0) cp_async_mbar_arrive(bar);
+            else cp_async_commit();
         };
         // raw windows -> scaled, split fp16 rows in window buffer Wb (hi) and Wb + win_bytes (lo):
         // the re row at dst, the im row one plane (NX rows) later; every raw offset is even, so
@@ -1015,14 +1071,15 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
             *reinterpret_cast<uint4 *>(d) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
             *reinterpret_cast<uint4 *>(d + p.win_bytes) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         };
-        auto convert_item = [&](unsigned char *Wb, int rb, int rbase, int toff, int dst, float sB) {
+        auto convert_item = [&](unsigned char *Wb, int rb, int rbase, int toff, int dst, float sB, int cidx) {
             const int4 *t4 = reinterpret_cast<const int4 *>(offR + toff);
             const int4 ta = t4[0], tb = t4[1];
             const int offs[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+            const int cb = rb * rawbuf + rbase + (nbulk > 0 ? shTab[rb * ncol + cidx] : 0);
             float vr[8], vi[8];
 #pragma unroll
             for (int kk = 0; kk < 8; kk++) {
-                const float2 v = raw2[(offs[kk] < 0 ? zslot : rb * rawbuf + rbase + offs[kk]) >> 1];
+                const float2 v = raw2[(offs[kk] < 0 ? zslot : cb + offs[kk]) >> 1];
                 vr[kk] = v.x * sB;
                 vi[kk] = v.y * sB;
             }
@@ -1033,29 +1090,50 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
         int e0, j, i0;
         int se = -1;
         float sB0 = 1.f, sB1 = 1.f, sB2 = 1.f;
-        // raw windows run nraw-1 tiles ahead; every iteration commits exactly one cp.async
-        // group (possibly empty), so waiting for all but the newest nraw-1 groups means
-        // this tile's windows have landed
+        // raw windows run nraw-1 tiles ahead; tile k uses raw buffer k % nraw, the
+        // (k / nraw)-th phase of raw_full[k % nraw].  Every decision below is uniform over the
+        // producer threads, so nfetch (tiles fetched) is the same in each.
+        int nfetch = 0;
         for (int k = 0; k < nraw; k++) {
             int ke, kj, ki0;
             const bool has = tile_of(k, ke, kj, ki0);
             if (has) column_table(ke, kj, ki0);
             bar_sync_group<2, TCW_PROD>();
             if (k == nraw - 1) break;                 // its table is used by the first iteration
-            if (has) fetch_raw(k);
-            else cp_async_commit();
+            if (has) {
+                fetch_raw(k);
+                nfetch++;
+            } else if (nbulk == 0) {
+                cp_async_commit();                    // one group per tile slot
+            }
             bar_sync_group<2, TCW_PROD>();
         }
-        for (int it = 0; ok; it++) {
+        int it = 0;
+        for (;; it++) {
             if (!tile_of(it, e0, j, i0)) break;
             const int s = it & 1;
             // the tile nraw-1 ahead goes to the raw buffer last read by the previous
             // iteration's convert, which finished before that iteration's final barrier
             int ne_, nj, ni0;
             const int ahead = it + nraw - 1;
-            if (tile_of(ahead, ne_, nj, ni0)) fetch_raw(ahead % nraw);   // table computed last iteration
-            else cp_async_commit();
-            const bool good = it < 2 || mbar_wait(smem_u32(&win_empty[s]), ((it - 2) >> 1) & 1, p.spin_limit);
+            if (tile_of(ahead, ne_, nj, ni0)) {   // table computed last iteration
+                fetch_raw(ahead % nraw);
+                nfetch++;
+            } else if (nbulk == 0) {
+                cp_async_commit();
+            }
+            const int rb = it % nraw;
+            bool good = it < 2 || mbar_wait(smem_u32(&win_empty[s]), ((it - 2) >> 1) & 1, p.spin_limit);
+            if (nbulk > 0) {
+                good = good && mbar_wait(smem_u32(&raw_full[rb]), (it / nraw) & 1, p.spin_limit);
+            } else {
+                // all but the newest nraw-1 groups landed: this tile's windows
+                if (nraw == 4) cp_async_wait_n<3>();
+                else if (nraw == 3) cp_async_wait_n<2>();
+                else cp_async_wait_n<1>();
+            }
+            // (this barrier also makes every thread's landed copies and the shift-table
+            // writes of earlier fetches visible to the reads below)
             if (bar_or_group<2, TCW_PROD>(!good)) {
                 ok = false;
                 break;
@@ -1066,28 +1144,29 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                 sB2 = scale_of(e0, q2);
                 se = e0;
             }
-            if (nraw == 4) cp_async_wait_n<3>();
-            else if (nraw == 3) cp_async_wait_n<2>();
-            else cp_async_wait_n<1>();
-            bar_sync_group<2, TCW_PROD>();
             unsigned char *Wb = smW + (size_t)s * 2 * p.win_bytes;
-            const int rb = it % nraw;
-            if (ptid < nitems) convert_item(Wb, rb, r0, t0, d0, sB0);
-            if (ptid + TCW_PROD < nitems) convert_item(Wb, rb, r1, t1, d1, sB1);
-            if (ptid + 2 * TCW_PROD < nitems) convert_item(Wb, rb, r2, t2, d2, sB2);
+            if (ptid < nitems) convert_item(Wb, rb, r0, t0, d0, sB0, c0);
+            if (ptid + TCW_PROD < nitems) convert_item(Wb, rb, r1, t1, d1, sB1, c1);
+            if (ptid + 2 * TCW_PROD < nitems) convert_item(Wb, rb, r2, t2, d2, sB2, c2);
             for (int k = ptid + 3 * TCW_PROD; k < nitems; k += TCW_PROD) {
-                int rb_, to_, ds_, q_;
-                item_of(k, rb_, to_, ds_, q_);
-                convert_item(Wb, rb, rb_, to_, ds_, scale_of(e0, q_));
+                int rb_, to_, ds_, q_, c_;
+                item_of(k, rb_, to_, ds_, q_, c_);
+                convert_item(Wb, rb, rb_, to_, ds_, scale_of(e0, q_), c_);
             }
-            // every copy of this iteration was issued before the first barrier above, so the
-            // table can now describe the tile fetched next iteration
+            // every copy of this iteration was issued before the barrier above, so the table
+            // can now describe the tile fetched next iteration
             if (tile_of(ahead + 1, ne_, nj, ni0)) column_table(ne_, nj, ni0);
             fence_proxy_async();
             bar_sync_group<2, TCW_PROD>();           // buffer staged, raw buffer rb free
             if (ptid == 0) mbar_arrive(smem_u32(&win_full[s]));
         }
-        if (!ok && ptid == 0) atomicOr(p.status, 2);
+        if (!ok) {
+            if (ptid == 0) atomicOr(p.status, 2);
+            // bulk copies still in flight land before the block exits (bounded waits)
+            if (nbulk > 0)
+                for (int k = it; k < nfetch; k++) mbar_wait(smem_u32(&raw_full[k % nraw]), (k / nraw) & 1, p.spin_limit);
+        }
+        cp_async_commit();
         cp_async_wait_all();
     } else {
         // ---------------------------------------------------------------- epilogue
@@ -1304,6 +1383,9 @@ void tc_plan(cqpi_handle *h)
             for (int nraw = 4; nraw >= 2 && !pl.win; nraw--) window_config(h, EB, H, nraw, pl);
 }
 
+// band counts whose direct-window kernel has a bulk-copy variant (templates B = 6 and 8)
+static bool tcw_bulk_bands(int b) { return b >= 5 && b <= 8; }
+
 // Fill the direct-window fields of pl for EB energies x 8*H sites per tile and an nraw-deep
 // raw-window ring; false if the shape does not fit (N <= 256, two accumulator sets in the
 // 512 TMEM columns, shared memory with 16 KiB left for the per-impurity constants).
@@ -1326,21 +1408,30 @@ bool window_config(const cqpi_handle *h, int EB, int H, int nraw, TcPlan &pl)
     const int win_bytes = NKC * 2 * EB * twob * NX * 16;
     const int wwt = 8 * H * h->os;
     const int sst = wwt + ((h->os - wwt) % 32 + 32) % 32;
-    const size_t rawfl = (size_t)NX * side * h->b * h->b * 2;
+    // raw column pitch: side*b*b complex values + 1, rounded up to even (16-byte bulk copies)
+    const size_t cpf = (size_t)((side * h->b * h->b + 2) & ~1);
+    const size_t rawfl = (size_t)NX * cpf * 2;
     // shared memory with Phi in shared memory (the larger of the two layouts); the
-    // per-impurity epilogue constants are added at launch
+    // per-impurity epilogue constants are added at launch.  After the constants: the
+    // column shift table [nraw][2*EB*NX], the column table [2*EB*NX], 9 + nraw mbarriers and
+    // the TMEM slot
     const size_t smem = 2 * (size_t)a_bytes + 4 * (size_t)win_bytes + 4 * (nraw * 2 * EB * rawfl + 4) +
-                        4 * (size_t)(2 * NKC * 8) + 4 * (size_t)EB * (3 + 128) + 16 + 8 * (size_t)(2 * EB * NX) + 9 * 8 + 16;
+                        4 * (size_t)(2 * NKC * 8) + 4 * (size_t)EB * (3 + 128) + 16 + 4 * (size_t)nraw * (2 * EB * NX) +
+                        8 * (size_t)(2 * EB * NX) + 13 * 8 + 16;
     if (smem > 211 * 1024) return false;
     pl.wNKC = NKC; pl.wKP = KP; pl.w_a_bytes = a_bytes;
     pl.wNRAW = nraw; pl.wEB = EB; pl.wH = H; pl.wNX = NX; pl.w_win_bytes = win_bytes; pl.w_sst = sst;
+    // bulk copies pay off for long raw columns (measured: 6-band columns of 1.4 KB fetched in
+    // bulk cut the Josephson contraction by 16%; 3-band columns of 360 B ran 13% slower)
+    pl.w_nbulk = (tcw_bulk_bands(h->b) && side * h->b * h->b * 8 >= 1024) ? 2 * EB * NX : 0;
     pl.w_a_tmem = a_tmem; pl.w_tmem_cols = wc; pl.w_smem = smem;
     pl.win = true;
     return true;
 }
 
-// Time every valid direct-window shape on the current energy batch (workspace already holds
-// G0(R), T and term1 for ne energies) and keep the fastest.  out: ne*nimp maps of scratch.
+// Time every valid direct-window shape and raw-column fetch on the current energy batch
+// (workspace already holds G0(R), T and term1 for ne energies) and keep the fastest.
+// out: ne*nimp maps of scratch.
 cudaError_t tc_autotune(cqpi_handle *h, int ne, float *out, float *best_ms, int *tried)
 {
     TcPlan best = h->tc;
@@ -1354,23 +1445,26 @@ cudaError_t tc_autotune(cqpi_handle *h, int ne, float *out, float *best_ms, int 
     const TcPlan base = h->tc;
     for (int EB = 1; EB <= 4 && err == cudaSuccess; EB++)
         for (int H = 1; H <= 4 && err == cudaSuccess; H *= 2)
-            for (int nraw = 2; nraw <= 4 && err == cudaSuccess; nraw++) {
-                TcPlan pl = base;
-                if (!window_config(h, EB, H, nraw, pl)) continue;
-                h->tc = pl;
-                if (!tc_window_usable(h)) continue;
-                err = launch_ldos_tc(h, ne, out);                 // warm-up
-                if (err != cudaSuccess) break;
-                err = cudaEventRecord(e0, h->stream);
-                for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_ldos_tc(h, ne, out);
-                if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
-                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-                float ms = 0.f;
-                if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-                if (err != cudaSuccess) break;
-                n++;
-                if (best_t < 0.f || ms < best_t) { best_t = ms; best = pl; }
-            }
+            for (int nraw = 2; nraw <= 4 && err == cudaSuccess; nraw++)
+                for (int bulk = 0; bulk < (tcw_bulk_bands(h->b) ? 2 : 1) && err == cudaSuccess; bulk++) {
+                    TcPlan pl = base;
+                    if (!window_config(h, EB, H, nraw, pl)) continue;
+                    // raw columns by cp.async only, or all by bulk copies
+                    pl.w_nbulk = bulk ? 2 * EB * pl.wNX : 0;
+                    h->tc = pl;
+                    if (!tc_window_usable(h)) continue;
+                    err = launch_ldos_tc(h, ne, out);                 // warm-up
+                    if (err != cudaSuccess) break;
+                    err = cudaEventRecord(e0, h->stream);
+                    for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_ldos_tc(h, ne, out);
+                    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+                    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+                    if (err != cudaSuccess) break;
+                    n++;
+                    if (best_t < 0.f || ms < best_t) { best_t = ms; best = pl; }
+                }
     h->tc = (best_t >= 0.f) ? best : base;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1473,14 +1567,23 @@ __global__ void __launch_bounds__(256) tfold_kernel(int b, long long npt, const 
     if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(gmaxT + e, __float_as_uint(mx));
 }
 
+template <int B, bool JOS, bool FOLD, bool BULK>
+static cudaError_t launch_tcw_k(const TcParams &p, int grid, size_t smem, cudaStream_t st)
+{
+    cudaError_t err = cudaFuncSetAttribute(ldos_tcw_kernel<B, JOS, FOLD, BULK>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    ldos_tcw_kernel<B, JOS, FOLD, BULK><<<grid, TCW_THREADS, smem, st>>>(p);
+    return cudaSuccess;
+}
+// bulk-copy variants exist for 6 and 8 bands (p.nbulk is 0 for the other band counts)
 template <int B, bool JOS, bool FOLD>
 static cudaError_t launch_tcw(const TcParams &p, int grid, size_t smem, cudaStream_t st)
 {
-    cudaError_t err = cudaFuncSetAttribute(ldos_tcw_kernel<B, JOS, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
-    if (err != cudaSuccess) return err;
-    ldos_tcw_kernel<B, JOS, FOLD><<<grid, TCW_THREADS, smem, st>>>(p);
-    return cudaSuccess;
+    if constexpr (B == 6 || B == 8) {
+        if (p.nbulk > 0) return launch_tcw_k<B, JOS, FOLD, true>(p, grid, smem, st);
+    }
+    return launch_tcw_k<B, JOS, FOLD, false>(p, grid, smem, st);
 }
 
 template <int B>
@@ -1501,6 +1604,7 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
     p.stall = (stall && !strcmp(stall, "1")) ? 1 : 0;
     if (p.stall) p.spin_limit = 256;
     p.box = h->ws.box32; p.T32 = h->ws.T32; p.term1 = h->ws.term1; p.gmax = h->ws.gmax;
+    p.zsrc = box32_zeros(h);
     p.Aimg = reinterpret_cast<const uint4 *>(h->d_tc_a);
     p.out = out;
     p.scale = h->out_scale;
@@ -1536,6 +1640,10 @@ static cudaError_t launch_tc_t(cqpi_handle *h, int ne, float *out, const int *fo
             p.gmaxT = h->ws.gmaxT;
         }
         p.H = pl.wH; p.NX = pl.wNX; p.NKC = pl.wNKC; p.win_bytes = pl.w_win_bytes; p.EB = pl.wEB; p.nraw = pl.wNRAW;
+        // CQPI_TC_NBULK=<n>: fetch the first n raw columns of a tile by bulk copies
+        const char *fb = getenv("CQPI_TC_NBULK");
+        p.nbulk = fb ? std::max(0, atoi(fb)) : pl.w_nbulk;
+        if (!tcw_bulk_bands(h->b)) p.nbulk = 0;
         p.TS = 8 * pl.wH; p.KP = pl.wKP; p.a_bytes = pl.w_a_bytes; p.sst = pl.w_sst;
         p.ntx = (h->n + p.TS - 1) / p.TS;
         p.tmem_cols = pl.w_tmem_cols;
