@@ -774,8 +774,8 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 
 // JOS: the Josephson form (p.coff, p.tip); a template flag so that the LDOS epilogue keeps
 // its register budget.  BULK: the first p.nbulk raw columns of a tile are fetched by bulk
-// copies (instantiated for 6 and 8 bands only; without it the producer carries no trace of
-// them: measured 1.3% on the 3-band contraction).
+// copies (instantiated for 3, 6 and 8 bands only; without it the producer carries no trace
+// of them: measured 1.3% on the 3-band contraction).
 template <int B, bool JOS, bool FOLD, bool BULK>
 __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_constant__ TcParams p)
 {
@@ -1383,8 +1383,10 @@ void tc_plan(cqpi_handle *h)
             for (int nraw = 4; nraw >= 2 && !pl.win; nraw--) window_config(h, EB, H, nraw, pl);
 }
 
-// band counts whose direct-window kernel has a bulk-copy variant (templates B = 6 and 8)
-static bool tcw_bulk_bands(int b) { return b >= 5 && b <= 8; }
+// band counts whose direct-window kernel has a bulk-copy variant (templates B = 3, 6 and 8;
+// for 3 bands only autotuning takes it: with many impurities per map the epilogue is the
+// limit, and bulk copies leave it the issue slots of the producer's cp.async pieces)
+static bool tcw_bulk_bands(int b) { return b == 3 || (b >= 5 && b <= 8); }
 
 // Fill the direct-window fields of pl for EB energies x 8*H sites per tile and an nraw-deep
 // raw-window ring; false if the shape does not fit (N <= 256, two accumulator sets in the
@@ -1576,11 +1578,11 @@ static cudaError_t launch_tcw_k(const TcParams &p, int grid, size_t smem, cudaSt
     ldos_tcw_kernel<B, JOS, FOLD, BULK><<<grid, TCW_THREADS, smem, st>>>(p);
     return cudaSuccess;
 }
-// bulk-copy variants exist for 6 and 8 bands (p.nbulk is 0 for the other band counts)
+// bulk-copy variants exist for 3, 6 and 8 bands (p.nbulk is 0 for the other band counts)
 template <int B, bool JOS, bool FOLD>
 static cudaError_t launch_tcw(const TcParams &p, int grid, size_t smem, cudaStream_t st)
 {
-    if constexpr (B == 6 || B == 8) {
+    if constexpr (B == 3 || B == 6 || B == 8) {
         if (p.nbulk > 0) return launch_tcw_k<B, JOS, FOLD, true>(p, grid, smem, st);
     }
     return launch_tcw_k<B, JOS, FOLD, false>(p, grid, smem, st);

@@ -109,6 +109,21 @@ def test_device_wait_timeout_is_reported_and_handle_recovers(built_lib, monkeypa
     eng.close()
 
 
+def test_bulk_column_fetch_keeps_the_maps(built_lib, monkeypatch):
+    """The 3-band kernel's bulk-copy variant (one copy per raw window column, taken when
+    autotuning finds it faster) stages the same values as the cp.async pieces: identical
+    maps, also with only some columns in bulk."""
+    eng = _engine()
+    if eng.contraction_kind() != "tcgen05":
+        pytest.skip("tensor-core contraction not selected")
+    E = np.array([-0.04, 0.02, 0.07])
+    pieces = eng.run(E)
+    for nb in ("1000", "7"):
+        monkeypatch.setenv("CQPI_TC_NBULK", nb)
+        assert np.array_equal(eng.run(E), pieces), nb
+    eng.close()
+
+
 def test_autotune_keeps_the_maps(built_lib):
     """Tile shapes change the work split, not the arithmetic of a map value: after the
     autotuner picks a shape the maps are identical to the default shape's."""

@@ -189,3 +189,39 @@ def test_josephson_fields_of_view_crop_full_maps(built_lib):
         assert np.array_equal(got, full[k, 0, lo:lo + w, lo:lo + w])
         off += w * w
     eng.close()
+
+
+def test_josephson_bulk_and_piecewise_fetch_agree(built_lib, monkeypatch):
+    """6-band columns (1.4 KB) are fetched by one bulk copy each; fetched instead as 8-byte
+    cp.async pieces (CQPI_TC_NBULK=0), or half and half, the staged values and so the maps
+    are the same bit for bit."""
+    import cqpi
+    E = np.array([-0.07, 0.02, 0.05])
+    eng = _bdg_c2_engine(cqpi.PREC_MIXED)
+    assert eng.contraction_kind() == "tcgen05"
+    bulk = eng.run(E, f32=True, f64=False)
+    for nb in ("0", "5"):
+        monkeypatch.setenv("CQPI_TC_NBULK", nb)
+        assert np.array_equal(eng.run(E, f32=True, f64=False), bulk), nb
+    eng.close()
+
+
+def test_josephson_bulk_fetch_timeout_is_reported_and_handle_recovers(built_lib, monkeypatch):
+    """Fault injection without a GPU fault on the bulk-copy producer: with CQPI_TEST_STALL=1
+    the MMA warp waits (bounded) on a barrier nothing arrives on, the producer times out on
+    its next window-empty wait with bulk copies of later tiles in flight, waits (bounded) for
+    them to land and returns; the call reports CQPI_ERR_TIMEOUT and the handle then runs
+    normally.  (8 energies: 576 tiles, so every block has more tiles than the two window
+    buffers that need no window-empty wait.)"""
+    import cqpi
+    E = np.linspace(-0.06, 0.06, 8)
+    eng = _bdg_c2_engine(cqpi.PREC_MIXED)
+    assert eng.contraction_kind() == "tcgen05"
+    good = eng.run(E, f32=True, f64=False)
+    monkeypatch.setenv("CQPI_TEST_STALL", "1")
+    with pytest.raises(cqpi.CqpiError) as ei:
+        eng.run(E, f32=True, f64=False)
+    assert ei.value.code == cqpi.ERR_TIMEOUT
+    monkeypatch.delenv("CQPI_TEST_STALL")
+    assert np.array_equal(eng.run(E, f32=True, f64=False), good)
+    eng.close()
