@@ -127,6 +127,17 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float &a, float &b, flo
     a = __uint_as_float(r0); b = __uint_as_float(r1); c = __uint_as_float(r2); d = __uint_as_float(r3);
 }
 
+// Two consecutive accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, float &a, float &b)
+{
+    uint32_t r0, r1;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];"
+                 : "=r"(r0), "=r"(r1)
+                 : "r"(taddr)
+                 : "memory");
+    a = __uint_as_float(r0); b = __uint_as_float(r1);
+}
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Power-of-two scale that maps max|x| to [2^13, 2^14].
@@ -1213,24 +1224,36 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                     const float2 *Te = cT + (ee * p.nimp + imp) * bb;
                     const float t1 = cT1[ee * 128 + lq];
                     const uint32_t cb = (uint32_t)((s0 >> 3) * NMMA + ee * twob * 8 + (s0 & 7));
-                    float ur[2 * B][4], sr[2 * B][4];
+                    // sites per TMEM read: 4, or 2 for more than 4 bands (u and s of 4 sites
+                    // would not fit the 96-register cap of 576 threads)
+                    constexpr int SU = B > 4 ? 2 : 4;
+#pragma unroll
+                    for (int hs = 0; hs < 4; hs += SU) {
+                    float ur[2 * B][SU], sr[2 * B][SU];
 #pragma unroll
                     for (int ari = 0; ari < 2 * B; ari++) {
                         if (ari < 2 * nb) {
-                            const uint32_t cu = cb + (uint32_t)(ari * 8);
-                            tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
-                            tmem_ld4(acc + lane_base + cu + (uint32_t)opcols, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                            const uint32_t cu = cb + (uint32_t)(ari * 8 + hs);
+                            if constexpr (SU == 4) {
+                                tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
+                                tmem_ld4(acc + lane_base + cu + (uint32_t)opcols, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                            } else {
+                                tmem_ld2(acc + lane_base + cu, ur[ari][0], ur[ari][1]);
+                                tmem_ld2(acc + lane_base + cu + (uint32_t)opcols, sr[ari][0], sr[ari][1]);
+                            }
                         }
                     }
                     tmem_wait_ld();
-                    float term2[4] = {0.f, 0.f, 0.f, 0.f}, term2r[4] = {0.f, 0.f, 0.f, 0.f};
+                    float term2[SU], term2r[SU];
+#pragma unroll
+                    for (int u = 0; u < SU; u++) term2[u] = term2r[u] = 0.f;
                     if (fold) {
                         // the s accumulators already hold (T s)_a
 #pragma unroll
                         for (int a = 0; a < B; a++) {
                             if (a >= nb) continue;
 #pragma unroll
-                            for (int u = 0; u < 4; u++) {
+                            for (int u = 0; u < SU; u++) {
                                 term2[u] += ur[2 * a][u] * sr[2 * a + 1][u] + ur[2 * a + 1][u] * sr[2 * a][u];
                                 if (jos) term2r[u] += ur[2 * a][u] * sr[2 * a][u] - ur[2 * a + 1][u] * sr[2 * a + 1][u];
                             }
@@ -1239,31 +1262,33 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
 #pragma unroll
                     for (int a = 0; a < B; a++) {
                         if (a >= nb || fold) continue;
-                        float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
+                        float tsr[SU], tsi[SU];
+#pragma unroll
+                        for (int u = 0; u < SU; u++) tsr[u] = tsi[u] = 0.f;
 #pragma unroll
                         for (int c = 0; c < B; c++) {
                             if (c >= nb) continue;
                             const float2 tv = Te[a * nb + c];
 #pragma unroll
-                            for (int u = 0; u < 4; u++) {
+                            for (int u = 0; u < SU; u++) {
                                 tsr[u] += tv.x * sr[2 * c][u] - tv.y * sr[2 * c + 1][u];
                                 tsi[u] += tv.x * sr[2 * c + 1][u] + tv.y * sr[2 * c][u];
                             }
                         }
 #pragma unroll
-                        for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
+                        for (int u = 0; u < SU; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
                         if (jos) {
 #pragma unroll
-                            for (int u = 0; u < 4; u++) term2r[u] += ur[2 * a][u] * tsr[u] - ur[2 * a + 1][u] * tsi[u];
+                            for (int u = 0; u < SU; u++) term2r[u] += ur[2 * a][u] * tsr[u] - ur[2 * a + 1][u] * tsi[u];
                         }
                     }
                     if (jos) {
                         // Im(tip * sum u T s) (tmatrix::calcwannierjosephson, src/qpi.cc:986-990)
                         const float tx = cTip[2 * ee], ty = cTip[2 * ee + 1];
 #pragma unroll
-                        for (int u = 0; u < 4; u++) term2[u] = tx * term2[u] + ty * term2r[u];
+                        for (int u = 0; u < SU; u++) term2[u] = tx * term2[u] + ty * term2r[u];
                     }
-                    // pixel (qx, qy) of sites i0+s0 .. i0+s0+3 of row j, straight to the map
+                    // pixel (qx, qy) of sites i0+s0+hs .. of row j, straight to the map
                     if (qvalid && p.fov) {
                         // map (e, imp) covers the centred fov x fov sites of the full field
                         const int mi = e * p.nimp + imp;
@@ -1273,8 +1298,8 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                             const size_t wm = (size_t)fv * p.os;
                             float *dst = p.out + p.fov_off[mi] + ((size_t)jm * p.os + qy) * wm + qx;
 #pragma unroll
-                            for (int u = 0; u < 4; u++) {
-                                const int im = i0 + s0 + u - n2 + f2;
+                            for (int u = 0; u < SU; u++) {
+                                const int im = i0 + s0 + hs + u - n2 + f2;
                                 if (im >= 0 && im < fv) dst[(size_t)im * p.os] = (-t1 - term2[u] * inv2) * p.scale;
                             }
                         }
@@ -1283,8 +1308,9 @@ __global__ void __launch_bounds__(TCW_THREADS, 1) ldos_tcw_kernel(const __grid_c
                                               (size_t)(i0 + s0) * p.os + qx);
                         const int xrem = p.wn - (i0 + s0) * p.os - qx;   // columns left in this map row
 #pragma unroll
-                        for (int u = 0; u < 4; u++)
-                            if (u * p.os < xrem) dst[u * p.os] = (-t1 - term2[u] * inv2) * p.scale;
+                        for (int u = 0; u < SU; u++)
+                            if ((hs + u) * p.os < xrem) dst[(hs + u) * p.os] = (-t1 - term2[u] * inv2) * p.scale;
+                    }
                     }
                 }
             }
