@@ -558,38 +558,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __gri
         for (int imp = 0; imp < p.nimp; imp++) {
             const float2 *Te = p.T32 + ((size_t)e * p.nimp + imp) * bb;
             const float t1 = qvalid ? (float)p.term1[(size_t)e * p.Q + qx * p.os + qy] : 0.f;
+            // sites per TMEM read: 4, or 2 for more than 4 bands (u and s of 4 sites would not
+            // fit the 128-register cap of 512 threads: 322 bytes spilled at 6 bands)
+            constexpr int SU = B > 4 ? 2 : 4;
             for (int s0 = sgrp * 4; s0 < p.TS; s0 += 16) {
-                float ur[2 * B][4], sr[2 * B][4];
+#pragma unroll
+                for (int hs = 0; hs < 4; hs += SU) {
+                float ur[2 * B][SU], sr[2 * B][SU];
 #pragma unroll
                 for (int ari = 0; ari < 2 * B; ari++) {
                     if (ari < 2 * p.b) {
-                        const uint32_t cu = (uint32_t)(ari * p.TS + s0);
-                        tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
-                        tmem_ld4(acc + lane_base + cu + (uint32_t)p.N, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                        const uint32_t cu = (uint32_t)(ari * p.TS + s0 + hs);
+                        if constexpr (SU == 4) {
+                            tmem_ld4(acc + lane_base + cu, ur[ari][0], ur[ari][1], ur[ari][2], ur[ari][3]);
+                            tmem_ld4(acc + lane_base + cu + (uint32_t)p.N, sr[ari][0], sr[ari][1], sr[ari][2], sr[ari][3]);
+                        } else {
+                            tmem_ld2(acc + lane_base + cu, ur[ari][0], ur[ari][1]);
+                            tmem_ld2(acc + lane_base + cu + (uint32_t)p.N, sr[ari][0], sr[ari][1]);
+                        }
                     }
                 }
                 tmem_wait_ld();
-                float term2[4] = {0.f, 0.f, 0.f, 0.f};
+                float term2[SU];
+#pragma unroll
+                for (int u = 0; u < SU; u++) term2[u] = 0.f;
 #pragma unroll
                 for (int a = 0; a < B; a++) {
                     if (a >= p.b) continue;
-                    float tsr[4] = {0.f, 0.f, 0.f, 0.f}, tsi[4] = {0.f, 0.f, 0.f, 0.f};
+                    float tsr[SU], tsi[SU];
+#pragma unroll
+                    for (int u = 0; u < SU; u++) tsr[u] = tsi[u] = 0.f;
 #pragma unroll
                     for (int c = 0; c < B; c++) {
                         if (c >= p.b) continue;
                         const float2 tv = __ldg(Te + a * p.b + c);
 #pragma unroll
-                        for (int u = 0; u < 4; u++) {
+                        for (int u = 0; u < SU; u++) {
                             tsr[u] += tv.x * sr[2 * c][u] - tv.y * sr[2 * c + 1][u];
                             tsi[u] += tv.x * sr[2 * c + 1][u] + tv.y * sr[2 * c][u];
                         }
                     }
 #pragma unroll
-                    for (int u = 0; u < 4; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
+                    for (int u = 0; u < SU; u++) term2[u] += ur[2 * a][u] * tsi[u] + ur[2 * a + 1][u] * tsr[u];
                 }
                 if (qvalid)
 #pragma unroll
-                    for (int u = 0; u < 4; u++) stage[qy * sst + (s0 + u) * p.os + qx] = (-t1 - term2[u] * inv2) * p.scale;
+                    for (int u = 0; u < SU; u++)
+                        stage[qy * sst + (s0 + hs + u) * p.os + qx] = (-t1 - term2[u] * inv2) * p.scale;
+                }
             }
             __syncthreads();
             const int xbase = i0 * p.os;
