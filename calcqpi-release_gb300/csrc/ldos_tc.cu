@@ -726,7 +726,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) ldos_tc_pipe_kernel(const __gri
 //
 // Warp roles (18 warps), handing off through mbarriers only:
 //   warps 0-7    epilogue: TMEM -> rho (two warps per TMEM lane quarter, warp % 4)
-//   warps 8-16   producer: cp.async of the raw FP32 windows, fp16 split into a window buffer
+//   warps 8-16   producer: raw FP32 windows by cp.async pieces or one bulk copy per column
+//                (raw_full[r]), fp16 split into a window buffer
 //   warp 17      MMA issue (one elected lane)
 //   win_full[b]  : window buffer b staged            (producer -> MMA)
 //   win_empty[b] : MMAs reading buffer b completed    (tcgen05.commit -> producer)
