@@ -399,13 +399,18 @@ g0_rowfft_pk_kernel(int NB, int Rb, int tr, double eta, const double *__restrict
 // by greens_k_kernel): RPC rows r = (energy * b^2 + plane) * kp + i per CTA, loaded with
 // coalesced row reads, then the four-step register transform along j and the pruned stores
 // of g0_rowfft_reg_kernel.  HBM-bound: one read of the G0(k) planes, NB / kp of it written.
+// rows per CTA: 256 / min(N1, N2), so that the first register pass (RPC x N1 tasks) keeps
+// all 256 threads busy when N1 < N2 (kp = 2048: 8 rows, 151 KB of shared memory)
+template <int N1, int N2>
+__host__ __device__ constexpr int rowfft_g0k_rpc() { return 256 / (N1 < N2 ? N1 : N2); }
+
 template <int N1, int N2>
 __global__ void __launch_bounds__(256) rowfft_reg_g0k_kernel(int NB, int Rb, long long nrows,
                                                              const float2 *__restrict__ g0k,
                                                              const float2 *__restrict__ tw, float2 *__restrict__ half)
 {
     constexpr int KP = N1 * N2;
-    constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
+    constexpr int RPC = rowfft_g0k_rpc<N1, N2>();
     constexpr int PLEN = KP + KP / 32 + 1;
     extern __shared__ __align__(16) float2 sm[];
     float2 *tws = sm + (size_t)RPC * PLEN;
@@ -795,7 +800,7 @@ static cudaError_t configure_colfft_reg(cqpi_handle *h)
 template <int N1, int N2>
 static size_t rowfft_g0k_smem()
 {
-    constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
+    constexpr int RPC = rowfft_g0k_rpc<N1, N2>();
     return 8 * ((size_t)RPC * (N1 * N2 + (N1 * N2) / 32 + 1) + N1 * N2);
 }
 
@@ -823,7 +828,7 @@ static cudaError_t configure_rowfft_g0k(cqpi_handle *h)
 template <int N1, int N2>
 static void launch_rowfft_g0k_t(cqpi_handle *h, int ne, int np)
 {
-    constexpr int RPC = 256 / (N1 > N2 ? N1 : N2);
+    constexpr int RPC = rowfft_g0k_rpc<N1, N2>();
     const long long nrows = (long long)ne * np * h->kp;
     rowfft_reg_g0k_kernel<N1, N2><<<(unsigned)((nrows + RPC - 1) / RPC), 256, rowfft_g0k_smem<N1, N2>(), h->stream>>>(
         h->NB, h->Rb, nrows, h->ws.g0k32, h->d_tw32, h->ws.half32);
